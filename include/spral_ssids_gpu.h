@@ -1,0 +1,152 @@
+/*
+ * spral_ssids_gpu.h -- C-ABI of the GB300 numeric factorize-and-solve for
+ * SPRAL SSIDS.
+ *
+ * These entry points replace the GPU subtree of SSIDS (the type-bound
+ * procedures of gpu_symbolic_subtree / gpu_numeric_subtree in
+ * src/ssids/gpu/subtree.f90:20-72) and are shaped exactly like the CPU
+ * subtree's C interface (src/ssids/cpu/SymbolicSubtree.cxx:14-28,
+ * src/ssids/cpu/NumericSubtree.cxx:29-262), so that a Fortran binding can
+ * call them the way src/ssids/cpu/subtree.f90 calls the CPU ones.
+ *
+ * Conventions (as at the reference boundary, SURVEYed in
+ * src/ssids/cpu/SymbolicSubtree.hxx:20-48): all index arrays are 1-based and
+ * Fortran-ordered; x is column-major n x nrhs in pivot order (already
+ * permuted by invp and scaled by the caller, src/ssids/fkeep.F90:252-266).
+ * Options and statistics use the reference's struct layouts.  Errors are
+ * reported through ThreadStats.flag / return codes; nothing exits or throws.
+ */
+#ifndef SPRAL_SSIDS_GPU_H
+#define SPRAL_SSIDS_GPU_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same layout as struct cpu_factor_options (src/ssids/cpu/cpu_iface.hxx:27). */
+struct spral_ssids_cpu_factor_options {
+  int print_level;
+  bool action;
+  double small;
+  double u;
+  double multiplier;
+  int64_t small_subtree_threshold;
+  int cpu_block_size;
+  int pivot_method;        /* 1 app_aggressive, 2 app_block, 3 tpp */
+  int failed_pivot_method; /* 1 tpp, 2 pass */
+};
+
+/* Same layout as struct ThreadStats (src/ssids/cpu/ThreadStats.hxx:42). */
+struct spral_ssids_thread_stats {
+  int flag;
+  int num_delay;
+  int64_t num_factor;
+  int64_t num_flops;
+  int num_neg;
+  int num_two;
+  int num_zero;
+  int maxfront;
+  int maxsupernode;
+  int not_first_pass;
+  int not_second_pass;
+};
+
+/* Out-of-band options of the GPU path (the public spral_ssids_options
+ * struct is not changed).  precision: 0 = FP64 factors, 1 = FP32 factors with
+ * FP64 pivot decisions and FP64 iterative refinement in the solve. */
+struct spral_ssids_gpu_options {
+  int precision;
+  int max_refine;
+  double refine_tol;
+  int small_front_cols;
+  int use_graph;
+  int reserved[8];
+};
+
+/* Replaces construct_gpu_symbolic_subtree (src/ssids/gpu/subtree.f90:76);
+ * signature of spral_ssids_cpu_create_symbolic_subtree
+ * (src/ssids/cpu/SymbolicSubtree.cxx:14) with the CUDA device first and
+ * without the inter-subtree contribution list (the whole tree is one GPU
+ * subtree).  Nodes sa..en-1 (1-based) are the subtree. Returns NULL on error. */
+void* spral_ssids_gpu_create_symbolic_subtree(
+    int device, int n, int sa, int en, const int* sptr, const int* sparent,
+    const int64_t* rptr, const int* rlist, const int64_t* nptr, const int64_t* nlist,
+    const struct spral_ssids_cpu_factor_options* options);
+
+/* Replaces gpu_symbolic_subtree%cleanup (src/ssids/gpu/subtree.f90:283). */
+void spral_ssids_gpu_destroy_symbolic_subtree(void* symbolic);
+
+/* Out-of-band options; call before create_num_subtree.  Returns 0. */
+int spral_ssids_gpu_set_options(void* symbolic, const struct spral_ssids_gpu_options* opts);
+
+/* Replaces gpu_symbolic_subtree%factor (src/ssids/gpu/subtree.f90:304);
+ * signature of spral_ssids_cpu_create_num_subtree_dbl
+ * (src/ssids/cpu/NumericSubtree.cxx:30).  aval: host values in the user's
+ * lower-CSC order; scaling: NULL or n scaling factors in pivot order;
+ * child_contrib must be NULL.  Returns the numeric handle (also on failure,
+ * with stats->flag < 0) or NULL if nothing could be allocated. */
+void* spral_ssids_gpu_create_num_subtree_dbl(
+    bool posdef, const void* symbolic, const double* aval, const double* scaling,
+    void** child_contrib, const struct spral_ssids_cpu_factor_options* options,
+    struct spral_ssids_thread_stats* stats);
+
+/* Replaces gpu_numeric_subtree%cleanup (src/ssids/gpu/subtree.f90:484);
+ * cf. spral_ssids_cpu_destroy_num_subtree_dbl (NumericSubtree.cxx:63). */
+void spral_ssids_gpu_destroy_num_subtree_dbl(bool posdef, void* numeric);
+
+/* Replace gpu_numeric_subtree%solve_fwd/_diag/_diag_bwd/_bwd
+ * (src/ssids/gpu/subtree.f90:555-738); cf. spral_ssids_cpu_subtree_solve_*
+ * (NumericSubtree.cxx:76-180).  x: host, pivot order, ldx >= n.  Return an
+ * SSIDS flag (0 success, -50 allocation, -51 CUDA error). */
+int spral_ssids_gpu_subtree_solve_fwd_dbl(bool posdef, const void* numeric, int nrhs, double* x,
+                                          int ldx);
+int spral_ssids_gpu_subtree_solve_diag_dbl(bool posdef, const void* numeric, int nrhs, double* x,
+                                           int ldx);
+int spral_ssids_gpu_subtree_solve_diag_bwd_dbl(bool posdef, const void* numeric, int nrhs,
+                                               double* x, int ldx);
+int spral_ssids_gpu_subtree_solve_bwd_dbl(bool posdef, const void* numeric, int nrhs, double* x,
+                                          int ldx);
+
+/* Replaces gpu_numeric_subtree%enquire_indef (src/ssids/gpu/subtree.f90:855);
+ * cf. spral_ssids_cpu_subtree_enquire_dbl (NumericSubtree.cxx:183).
+ * piv_order[var] (0-based, negative for 2x2) and d (2 x n), either may be NULL. */
+void spral_ssids_gpu_subtree_enquire_dbl(bool posdef, const void* numeric, int* piv_order,
+                                         double* d);
+
+/* Replaces gpu_numeric_subtree%alter (src/ssids/gpu/subtree.f90:933);
+ * cf. spral_ssids_cpu_subtree_alter_dbl (NumericSubtree.cxx:204). */
+void spral_ssids_gpu_subtree_alter_dbl(bool posdef, void* numeric, const double* d);
+
+/* Same-pattern refactorisation with values already in device memory (no
+ * reference counterpart: the reference re-creates the numeric subtree and
+ * copies aval host-to-device each time, src/ssids/gpu/subtree.f90:375). */
+int spral_ssids_gpu_refactor_dev(void* numeric, const double* aval_dev,
+                                 struct spral_ssids_thread_stats* stats, void* stream);
+
+/* Solve with x in device memory (pivot order, FP64).  job: 0 full,
+ * 1 fwd, 2 diag, 3 bwd, 4 diag_bwd (ssids_solve job codes,
+ * src/ssids/ssids.f90:1232-1246). */
+int spral_ssids_gpu_solve_dev(void* numeric, int job, int nrhs, double* x_dev, int ldx,
+                              void* stream);
+
+/* Full solve with FP64 iterative refinement against the FP64 matrix held on
+ * the device (pivot order x, host).  Used by precision = 1; for FP64
+ * factors it performs max_refine steps of classical refinement.  iters
+ * receives the number of refinement steps taken. */
+int spral_ssids_gpu_solve_refined(void* numeric, int nrhs, double* x, int ldx, int* iters);
+
+/* Timings of the last factor (ms): [0] total, [1] assembly, [2] dense,
+ * [3] contribution GEMM, [4] host wait.  Returns number of entries. */
+int spral_ssids_gpu_last_timing(const void* numeric, double* out);
+
+/* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
+int spral_ssids_gpu_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPRAL_SSIDS_GPU_H */

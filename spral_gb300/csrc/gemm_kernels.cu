@@ -1,0 +1,123 @@
+// Lower-triangular rank-k updates C(r,c) -= sum_k A(r,k) B(c,k), r >= c, on
+// CUDA cores (SIMT).  Two uses per front, both batched over the fronts of a
+// level (blockIdx.y = front):
+//   panel   : trailing update of the APP candidate columns with the block's
+//             passed pivots (ldlt_app.cxx:1082-1165 Block::update)
+//   contrib : contribution block C -= L21 (L21 D)^T over all eliminated
+//             columns (factor.hxx:96-108; gpu path: syrk.cu:185 form_contrib)
+// The operand pointers depend on device-side pivoting state (p, npass,
+// nelim), so each CTA derives its job from the front's FrontState; tiles are
+// walked with a grid-stride loop over the lower trapezoid.
+#include "ssids_gpu.cuh"
+
+namespace ssids300 {
+
+namespace {
+
+constexpr int TM = kGemmTile;  // 64
+constexpr int TK = 16;
+
+template <typename T, int MODE>
+__device__ __forceinline__ bool make_job(const FrontDesc<T>& fd, const FrontState& st,
+                                         SyrkJob<T>& j) {
+  if (MODE == 0) {
+    if (st.bs == 0) return false;
+    const int p = st.p, bs = st.bs;
+    j.C = fd.L + (int64_t)(p + bs) * fd.ld + (p + bs);
+    j.A = fd.L + (int64_t)p * fd.ld + (p + bs);
+    j.B = fd.W;
+    j.ldc = fd.ld; j.lda = fd.ld; j.ldb = fd.ld;
+    j.M = fd.m - (p + bs);
+    j.N = fd.n - (p + bs);
+    j.K = st.npass;
+  } else {
+    const int cm = fd.m - fd.n;
+    j.C = fd.C;
+    j.A = fd.L + fd.n;
+    j.B = fd.LD;
+    j.ldc = cm; j.lda = fd.ld; j.ldb = cm;
+    j.M = cm; j.N = cm;
+    j.K = st.nelim;
+  }
+  return j.K > 0 && j.M > 0 && j.N > 0;
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) k_syrk(FrontDesc<T>* fds, const FrontState* sts,
+                                              const int* fronts) {
+  const int f = fronts[blockIdx.y];
+  const FrontDesc<T> fd = fds[f];
+  const FrontState st = sts[f];
+  SyrkJob<T> j;
+  if (!make_job<T, MODE>(fd, st, j)) return;
+  __shared__ T As[TK][TM + 4];
+  __shared__ T Bs[TK][TM + 4];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int tc = (j.N + TM - 1) / TM, tr = (j.M + TM - 1) / TM;
+  const int total = tc * tr - tc * (tc - 1) / 2;
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    int tj = 0, rem = t;
+    while (rem >= tr - tj) { rem -= tr - tj; ++tj; }
+    const int ti = tj + rem;
+    const int row0 = ti * TM, col0 = tj * TM;
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+    for (int k0 = 0; k0 < j.K; k0 += TK) {
+#pragma unroll
+      for (int q = 0; q < (TM * TK) / 256; ++q) {
+        int idx = tid + 256 * q;
+        int rr = idx % TM, kk = idx / TM;
+        int r = row0 + rr, c = col0 + rr, k = k0 + kk;
+        As[kk][rr] = (r < j.M && k < j.K) ? j.A[(int64_t)k * j.lda + r] : T(0);
+        Bs[kk][rr] = (c < j.N && k < j.K) ? j.B[(int64_t)k * j.ldb + c] : T(0);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < TK; ++kk) {
+        T a[4], b[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) { a[q] = As[kk][tx + 16 * q]; b[q] = Bs[kk][ty + 16 * q]; }
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int y = 0; y < 4; ++y) acc[x][y] += a[x] * b[y];
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int y = 0; y < 4; ++y) {
+      const int c = col0 + ty + 16 * y;
+#pragma unroll
+      for (int x = 0; x < 4; ++x) {
+        const int r = row0 + tx + 16 * x;
+        if (r < j.M && c < j.N && r >= c) j.C[(int64_t)c * j.ldc + r] -= acc[x][y];
+      }
+    }
+  }
+}
+
+}  // namespace
+
+template <typename T>
+void launch_syrk_panel(FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
+                       int max_tiles, cudaStream_t s) {
+  int gx = max_tiles < 1 ? 1 : (max_tiles > 4096 ? 4096 : max_tiles);
+  k_syrk<T, 0><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts);
+}
+template <typename T>
+void launch_syrk_contrib(FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
+                         int max_tiles, cudaStream_t s) {
+  int gx = max_tiles < 1 ? 1 : (max_tiles > 4096 ? 4096 : max_tiles);
+  k_syrk<T, 1><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts);
+}
+
+template void launch_syrk_panel<double>(FrontDesc<double>*, const FrontState*, const int*, int, int, cudaStream_t);
+template void launch_syrk_panel<float>(FrontDesc<float>*, const FrontState*, const int*, int, int, cudaStream_t);
+template void launch_syrk_contrib<double>(FrontDesc<double>*, const FrontState*, const int*, int, int, cudaStream_t);
+template void launch_syrk_contrib<float>(FrontDesc<float>*, const FrontState*, const int*, int, int, cudaStream_t);
+
+}  // namespace ssids300

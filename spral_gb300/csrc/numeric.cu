@@ -1,0 +1,928 @@
+// Host orchestration and C-ABI of the GB300 numeric factor/solve.
+//
+// Replaces the GPU subtree of SSIDS (src/ssids/gpu/subtree.f90:20-72 and the
+// level loop of src/ssids/gpu/factor.f90:240-656).  Design:
+//   * the whole assembly tree is one device-resident subtree; fronts are
+//     numbered level by level (leaves first) so that a level's descriptors,
+//     states and contribution blocks are contiguous;
+//   * per level: zero + assemble (A, delays, children) -> ceil(n/32) APP
+//     steps batched over the level's fronts -> TPP for failed columns ->
+//     contribution block -> inertia counts; one host synchronisation per
+//     level reads back the elimination counts, which fix the sizes (delays)
+//     of the next level's fronts (the reference syncs per 8 columns,
+//     dense_factor.f90:185-192);
+//   * factors stay resident for repeated solves and same-pattern
+//     refactorisation; solves take many right-hand sides at once.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <vector>
+
+#include "spral_ssids_gpu.h"
+#include "ssids_gpu.cuh"
+
+namespace ssids300 {
+
+struct CudaFail {
+  cudaError_t err;
+  int line;
+};
+
+#define CK(x)                                              \
+  do {                                                     \
+    cudaError_t e_ = (x);                                  \
+    if (e_ != cudaSuccess) throw CudaFail{e_, __LINE__};   \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// device arena: chunked bump allocator that can be rewound for refactorisation
+// ---------------------------------------------------------------------------
+struct DevArena {
+  struct Chunk {
+    char* p;
+    size_t cap;
+  };
+  std::vector<Chunk> chunks;
+  size_t ci = 0, used = 0;
+  size_t min_chunk = size_t(64) << 20;
+  void rewind() { ci = 0; used = 0; }
+  void* alloc(size_t bytes) {
+    bytes = (bytes + 255) & ~size_t(255);
+    if (bytes == 0) bytes = 256;
+    while (ci < chunks.size()) {
+      if (used + bytes <= chunks[ci].cap) {
+        void* r = chunks[ci].p + used;
+        used += bytes;
+        return r;
+      }
+      ++ci;
+      used = 0;
+    }
+    size_t cap = std::max(bytes, min_chunk);
+    void* p = nullptr;
+    CK(cudaMalloc(&p, cap));
+    chunks.push_back({(char*)p, cap});
+    ci = chunks.size() - 1;
+    used = bytes;
+    return p;
+  }
+  ~DevArena() {
+    for (auto& c : chunks) cudaFree(c.p);
+  }
+};
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t n) {
+    if (n <= cap) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    size_t nc = std::max(n, cap + cap / 2);
+    CK(cudaMalloc(&p, std::max<size_t>(nc, 1) * sizeof(T)));
+    cap = nc;
+  }
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+template <typename T>
+static T* upload(const std::vector<T>& v) {
+  T* p = nullptr;
+  CK(cudaMalloc(&p, std::max<size_t>(v.size(), 1) * sizeof(T)));
+  if (!v.empty()) CK(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// symbolic subtree
+// ---------------------------------------------------------------------------
+struct Symbolic {
+  int device = 0, n = 0, nnodes = 0, nlev = 0;
+  std::vector<int> sptr, ncol, nrow, parent;  // per node (0-based; parent -1 = root)
+  std::vector<int64_t> rptr, nptr;
+  std::vector<int> rlist;
+  std::vector<std::vector<int>> children;  // node ids, increasing
+  std::vector<int> front_of, node_of, lvl_start;
+  std::vector<int> cols_start;  // per level into cols
+  std::vector<int64_t> contrib_off;  // per front, elements
+  int64_t contrib_total = 0;
+  int64_t nnz = 0;
+  std::vector<int> rdir_h;
+  std::vector<int64_t> rdir_ptr_h;
+  // device
+  int64_t* d_nptr = nullptr;
+  int64_t* d_nlist = nullptr;
+  int* d_sptr = nullptr;
+  int* d_rlist = nullptr;
+  int64_t* d_rptr = nullptr;
+  int* d_rdir = nullptr;
+  int64_t* d_rdir_ptr = nullptr;
+  int* d_fronts = nullptr;
+  int4* d_cols = nullptr;
+  int2* d_pairs = nullptr;
+  // FP64 matrix in pivot order (full CSR, both triangles) for refinement
+  int64_t* d_aptr = nullptr;
+  int* d_acol = nullptr;
+  int64_t* d_asrc = nullptr;
+  spral_ssids_gpu_options gopts{};
+  spral_ssids_cpu_factor_options copts{};
+  ~Symbolic() {
+    cudaFree(d_nptr); cudaFree(d_nlist); cudaFree(d_sptr); cudaFree(d_rlist); cudaFree(d_rptr);
+    cudaFree(d_rdir); cudaFree(d_rdir_ptr); cudaFree(d_fronts); cudaFree(d_cols);
+    cudaFree(d_pairs); cudaFree(d_aptr); cudaFree(d_acol); cudaFree(d_asrc);
+  }
+};
+
+static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sptr1,
+                                const int* sparent1, const int64_t* rptr1, const int* rlist1,
+                                const int64_t* nptr1, const int64_t* nlist1,
+                                const spral_ssids_cpu_factor_options* opts) {
+  std::unique_ptr<Symbolic> S(new Symbolic());
+  S->device = device;
+  S->n = n;
+  const int s0 = sa - 1;  // first node (0-based)
+  const int nn = en - sa;
+  S->nnodes = nn;
+  if (opts) S->copts = *opts;
+  S->gopts.precision = 0;
+  S->gopts.max_refine = 10;
+  S->gopts.refine_tol = 1e-15;
+  S->sptr.resize(nn + 1);
+  S->ncol.resize(nn);
+  S->nrow.resize(nn);
+  S->parent.resize(nn);
+  S->rptr.resize(nn + 1);
+  S->nptr.resize(nn + 1);
+  for (int i = 0; i <= nn; ++i) {
+    S->sptr[i] = sptr1[s0 + i] - 1;
+    S->rptr[i] = rptr1[s0 + i] - rptr1[s0];
+    S->nptr[i] = nptr1[s0 + i] - nptr1[s0];
+  }
+  for (int i = 0; i < nn; ++i) {
+    S->ncol[i] = S->sptr[i + 1] - S->sptr[i];
+    S->nrow[i] = (int)(S->rptr[i + 1] - S->rptr[i]);
+    int p = sparent1[s0 + i] - 1 - s0;
+    S->parent[i] = (p >= 0 && p < nn) ? p : -1;
+  }
+  S->rlist.resize(S->rptr[nn]);
+  for (int64_t k = 0; k < S->rptr[nn]; ++k) S->rlist[k] = rlist1[rptr1[s0] - 1 + k] - 1;
+  // nlist: 0-based pairs
+  const int64_t npairs = S->nptr[nn];
+  std::vector<int64_t> nl(2 * npairs);
+  int64_t maxsrc = -1;
+  for (int64_t k = 0; k < npairs; ++k) {
+    nl[2 * k] = nlist1[2 * (nptr1[s0] - 1 + k)] - 1;
+    nl[2 * k + 1] = nlist1[2 * (nptr1[s0] - 1 + k) + 1] - 1;
+    maxsrc = std::max(maxsrc, nl[2 * k]);
+  }
+  S->nnz = maxsrc + 1;
+  S->children.assign(nn, {});
+  for (int i = 0; i < nn; ++i)
+    if (S->parent[i] >= 0) S->children[S->parent[i]].push_back(i);
+  // levels (leaves = 0)
+  std::vector<int> lev(nn, 0);
+  int nlev = 0;
+  for (int i = 0; i < nn; ++i) {
+    for (int c : S->children[i]) lev[i] = std::max(lev[i], lev[c] + 1);
+    nlev = std::max(nlev, lev[i] + 1);
+  }
+  S->nlev = nlev;
+  S->lvl_start.assign(nlev + 1, 0);
+  for (int i = 0; i < nn; ++i) S->lvl_start[lev[i] + 1]++;
+  for (int l = 0; l < nlev; ++l) S->lvl_start[l + 1] += S->lvl_start[l];
+  S->front_of.resize(nn);
+  S->node_of.resize(nn);
+  {
+    std::vector<int> pos(S->lvl_start.begin(), S->lvl_start.end() - 1);
+    for (int i = 0; i < nn; ++i) {
+      int f = pos[lev[i]]++;
+      S->front_of[i] = f;
+      S->node_of[f] = i;
+    }
+  }
+  // contribution block offsets (level-major)
+  S->contrib_off.resize(nn + 1);
+  int64_t off = 0;
+  for (int f = 0; f < nn; ++f) {
+    S->contrib_off[f] = off;
+    int64_t cm = S->nrow[S->node_of[f]] - S->ncol[S->node_of[f]];
+    off += ((cm * cm + 63) / 64) * 64;
+  }
+  S->contrib_off[nn] = off;
+  S->contrib_total = off;
+  // rdir: parent position of each contribution row of a child
+  S->rdir_ptr_h.assign(nn + 1, 0);
+  for (int i = 0; i < nn; ++i) S->rdir_ptr_h[i + 1] = S->rdir_ptr_h[i] + (S->nrow[i] - S->ncol[i]);
+  S->rdir_h.assign(S->rdir_ptr_h[nn], -1);
+  {
+    std::vector<int> pos(std::max(n, 1), -1);
+    for (int p = 0; p < nn; ++p) {
+      for (int k = 0; k < S->nrow[p]; ++k) pos[S->rlist[S->rptr[p] + k]] = k;
+      for (int c : S->children[p]) {
+        int cm = S->nrow[c] - S->ncol[c];
+        for (int ic = 0; ic < cm; ++ic) {
+          int var = S->rlist[S->rptr[c] + S->ncol[c] + ic];
+          S->rdir_h[S->rdir_ptr_h[c] + ic] = pos[var];
+        }
+      }
+      for (int k = 0; k < S->nrow[p]; ++k) pos[S->rlist[S->rptr[p] + k]] = -1;
+    }
+  }
+  // extend-add work: per level, per parent column, the (child, jc) pairs
+  std::vector<int4> cols;
+  std::vector<int2> pairs;
+  S->cols_start.assign(nlev + 1, 0);
+  for (int l = 0; l < nlev; ++l) {
+    S->cols_start[l] = (int)cols.size();
+    for (int f = S->lvl_start[l]; f < S->lvl_start[l + 1]; ++f) {
+      int p = S->node_of[f];
+      std::vector<std::vector<int2>> per(S->nrow[p]);
+      for (int c : S->children[p]) {
+        int cm = S->nrow[c] - S->ncol[c];
+        for (int jc = 0; jc < cm; ++jc) {
+          int P = S->rdir_h[S->rdir_ptr_h[c] + jc];
+          per[P].push_back(make_int2(S->front_of[c], jc));
+        }
+      }
+      for (int P = 0; P < S->nrow[p]; ++P) {
+        if (per[P].empty()) continue;
+        int beg = (int)pairs.size();
+        for (auto& q : per[P]) pairs.push_back(q);
+        cols.push_back(make_int4(f, P, beg, (int)pairs.size()));
+      }
+    }
+  }
+  S->cols_start[nlev] = (int)cols.size();
+  // full CSR of A in pivot order: for each nlist pair, (prow, pcol, src)
+  std::vector<int64_t> aptr(n + 1, 0);
+  {
+    std::vector<int> pr(npairs), pc(npairs);
+    for (int i = 0; i < nn; ++i) {
+      for (int64_t k = S->nptr[i]; k < S->nptr[i + 1]; ++k) {
+        int64_t dest = nl[2 * k + 1];
+        int c = (int)(dest / S->nrow[i]), r = (int)(dest % S->nrow[i]);
+        pr[k] = S->rlist[S->rptr[i] + r];
+        pc[k] = S->rlist[S->rptr[i] + c];
+      }
+    }
+    for (int64_t k = 0; k < npairs; ++k) {
+      aptr[pr[k] + 1]++;
+      if (pr[k] != pc[k]) aptr[pc[k] + 1]++;
+    }
+    for (int i = 0; i < n; ++i) aptr[i + 1] += aptr[i];
+    std::vector<int> acol(aptr[n]);
+    std::vector<int64_t> asrc(aptr[n]);
+    std::vector<int64_t> fill(aptr.begin(), aptr.end() - 1);
+    for (int64_t k = 0; k < npairs; ++k) {
+      acol[fill[pr[k]]] = pc[k];
+      asrc[fill[pr[k]]++] = nl[2 * k];
+      if (pr[k] != pc[k]) {
+        acol[fill[pc[k]]] = pr[k];
+        asrc[fill[pc[k]]++] = nl[2 * k];
+      }
+    }
+    CK(cudaSetDevice(device));
+    S->d_aptr = upload(aptr);
+    S->d_acol = upload(acol);
+    S->d_asrc = upload(asrc);
+  }
+  std::vector<int> fronts(nn);
+  for (int f = 0; f < nn; ++f) fronts[f] = f;
+  std::vector<int> sp(S->sptr.begin(), S->sptr.end());
+  S->d_nptr = upload(S->nptr);
+  S->d_nlist = upload(nl);
+  S->d_sptr = upload(sp);
+  S->d_rlist = upload(S->rlist);
+  S->d_rptr = upload(S->rptr);
+  S->d_rdir = upload(S->rdir_h);
+  S->d_rdir_ptr = upload(S->rdir_ptr_h);
+  S->d_fronts = upload(fronts);
+  S->d_cols = upload(cols);
+  S->d_pairs = upload(pairs);
+  return S.release();
+}
+
+// ---------------------------------------------------------------------------
+// numeric subtree
+// ---------------------------------------------------------------------------
+struct NumericBase {
+  virtual ~NumericBase() {}
+  bool posdef = false;
+  int precision = 0;
+  spral_ssids_thread_stats stats{};
+  double timing[5] = {0, 0, 0, 0, 0};
+  virtual int factor(const double* aval, bool aval_on_device, const double* scaling,
+                     cudaStream_t user_stream) = 0;
+  virtual int solve_dev(int job, int nrhs, double* x, int ldx, cudaStream_t s) = 0;
+  virtual int solve_refined(int nrhs, double* x_host, int ldx, int* iters) = 0;
+  virtual void enquire(int* piv, double* d) = 0;
+  virtual void alter(const double* d) = 0;
+  virtual Symbolic* symbolic() = 0;
+};
+
+template <typename T>
+void launch_zero_fronts(FrontDesc<T>* fd, const int* fronts, int nf, int max_elems,
+                        cudaStream_t s);
+void launch_spmv_resid(const int64_t* aptr, const int* acol, const int64_t* asrc,
+                       const double* aval, int n, const double* x, const double* b, double* r,
+                       int nrhs, int ld, cudaStream_t s);
+void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s);
+void launch_bwd_err(const int64_t* aptr, const int64_t* asrc, const double* aval, int n,
+                    const double* x, const double* r, const double* b, int nrhs, int ld,
+                    double* work, cudaStream_t s);
+
+template <typename T>
+struct Numeric : NumericBase {
+  Symbolic* S;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4];
+  std::vector<FrontDesc<T>> hfd;
+  std::vector<FrontState> hst;
+  std::vector<int> nelim_, ndin_, m_, n_, ld_, doff_, napp_;
+  std::vector<int> lvl_max_m, lvl_max_nelim;
+  FrontDesc<T>* d_fd = nullptr;
+  FrontState* d_st = nullptr;
+  Stats* d_stats = nullptr;
+  int4* d_dwork = nullptr;
+  DevBuf<double> aval_buf, scale_buf;
+  DevBuf<T> contrib;
+  DevArena farena, darena, iarena;
+  DevBuf<T> ws_W, ws_swap, ws_LD;
+  DevBuf<double> ws_step;
+  DevBuf<int> ws_lperm;
+  // solve
+  bool solve_ready = false;
+  SolveNode<T>* d_sn = nullptr;
+  int* d_children = nullptr;
+  DevBuf<double> xloc, xorig, xbuf, rbuf, dbuf, bbuf, nbuf;
+  const double* cur_aval = nullptr;  // device values of the last factor
+  double last_bwd_err = 0.0;
+
+  explicit Numeric(Symbolic* s) : S(s) {
+    CK(cudaSetDevice(S->device));
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    const int nn = S->nnodes;
+    hfd.resize(nn);
+    hst.resize(nn);
+    nelim_.assign(nn, 0); ndin_.assign(nn, 0); m_.assign(nn, 0); n_.assign(nn, 0);
+    ld_.assign(nn, 0); doff_.assign(nn, 0); napp_.assign(nn, 0);
+    CK(cudaMalloc(&d_fd, std::max(nn, 1) * sizeof(FrontDesc<T>)));
+    CK(cudaMalloc(&d_st, std::max(nn, 1) * sizeof(FrontState)));
+    CK(cudaMalloc(&d_stats, sizeof(Stats)));
+    CK(cudaMalloc(&d_dwork, std::max(nn, 1) * sizeof(int4)));
+    contrib.ensure(std::max<int64_t>(S->contrib_total, 1));
+    // factor storage estimate (no delays) + 10%
+    size_t est = 0;
+    for (int i = 0; i < nn; ++i) est += (size_t)((S->nrow[i] + 3) / 4 * 4) * S->ncol[i];
+    farena.min_chunk = std::max<size_t>(est * sizeof(T) * 11 / 10, size_t(16) << 20);
+  }
+  ~Numeric() override {
+    cudaFree(d_fd); cudaFree(d_st); cudaFree(d_stats); cudaFree(d_dwork);
+    cudaFree(d_sn); cudaFree(d_children);
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  Symbolic* symbolic() override { return S; }
+
+  int factor(const double* aval, bool on_device, const double* scaling,
+             cudaStream_t user_stream) override {
+    cudaStream_t s = stream;
+    if (user_stream) CK(cudaStreamSynchronize(user_stream));
+    const int nn = S->nnodes;
+    const auto& co = S->copts;
+    solve_ready = false;
+    stats = spral_ssids_thread_stats{};
+    CK(cudaEventRecord(ev[0], s));
+    if (on_device) {
+      cur_aval = aval;
+    } else {
+      aval_buf.ensure(std::max<int64_t>(S->nnz, 1));
+      CK(cudaMemcpyAsync(aval_buf.p, aval, S->nnz * sizeof(double), cudaMemcpyHostToDevice, s));
+      cur_aval = aval_buf.p;
+    }
+    const double* d_scale = nullptr;
+    if (scaling) {
+      scale_buf.ensure(S->n);
+      CK(cudaMemcpyAsync(scale_buf.p, scaling, S->n * sizeof(double), cudaMemcpyHostToDevice, s));
+      d_scale = scale_buf.p;
+    }
+    farena.rewind();
+    darena.rewind();
+    iarena.rewind();
+    CK(cudaMemsetAsync(d_st, 0, nn * sizeof(FrontState), s));
+    CK(cudaMemsetAsync(d_stats, 0, sizeof(Stats), s));
+    lvl_max_m.assign(S->nlev, 0);
+    lvl_max_nelim.assign(S->nlev, 0);
+    int maxfront = 0, maxsn = 0, nfp = 0, nsp = 0;
+    double host_wait = 0.0;
+    std::vector<int4> dwork;
+    for (int l = 0; l < S->nlev; ++l) {
+      const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1], nf = f1 - f0;
+      dwork.clear();
+      int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0;
+      size_t wsW = 0, wsSwap = 0, wsLD = 0;
+      for (int f = f0; f < f1; ++f) {
+        const int node = S->node_of[f];
+        int ndin = 0;
+        for (int c : S->children[node]) {
+          const int fc = S->front_of[c];
+          doff_[fc] = ndin;
+          const int nd = n_[fc] - nelim_[fc];
+          if (nd > 0) dwork.push_back(make_int4(f, fc, S->ncol[node] + ndin, 0));
+          ndin += nd;
+        }
+        const int m = S->nrow[node] + ndin, n = S->ncol[node] + ndin;
+        const int ld = (m + 3) / 4 * 4;
+        const int cm = S->nrow[node] - S->ncol[node];
+        ndin_[f] = ndin; m_[f] = m; n_[f] = n; ld_[f] = ld;
+        max_m = std::max(max_m, m);
+        max_n = std::max(max_n, n);
+        max_cm = std::max(max_cm, cm);
+        max_ent = std::max<int>(max_ent, (int)(S->nptr[node + 1] - S->nptr[node]));
+        wsW += (size_t)ld * kBlk;
+        wsSwap += (size_t)ld * 64 + 256;
+        wsLD += (size_t)cm * n;
+        maxfront = std::max(maxfront, m);
+        maxsn = std::max(maxsn, n);
+      }
+      ws_W.ensure(wsW + 64);
+      ws_swap.ensure(wsSwap + 64);
+      ws_LD.ensure(wsLD + 64);
+      ws_step.ensure((size_t)nf * (kBlk * kBlk + 2 * kBlk + 64));
+      ws_lperm.ensure((size_t)nf * kBlk);
+      size_t oW = 0, oS = 0, oL = 0;
+      for (int f = f0; f < f1; ++f) {
+        const int node = S->node_of[f];
+        FrontDesc<T>& d = hfd[f];
+        const int m = m_[f], n = n_[f], ld = ld_[f];
+        d.m = m; d.n = n; d.ld = ld;
+        d.nrow = S->nrow[node]; d.ncol = S->ncol[node];
+        d.ndelay_in = ndin_[f];
+        d.cm = S->nrow[node] - S->ncol[node];
+        d.node = node;
+        d.L = (T*)farena.alloc((size_t)ld * n * sizeof(T));
+        d.D = (double*)darena.alloc((size_t)2 * n * sizeof(double) + 16);
+        d.perm = (int*)iarena.alloc((size_t)n * sizeof(int));
+        d.opos = (int*)iarena.alloc((size_t)n * sizeof(int));
+        d.C = d.cm > 0 ? contrib.p + S->contrib_off[f] : nullptr;
+        d.W = ws_W.p + oW; oW += (size_t)ld * kBlk;
+        d.swapbuf = ws_swap.p + oS; oS += (size_t)ld * 64 + 256;
+        d.LD = ws_LD.p + oL; oL += (size_t)d.cm * n;
+        d.step = ws_step.p + (size_t)(f - f0) * (kBlk * kBlk + 2 * kBlk + 64);
+        d.lperm = ws_lperm.p + (size_t)(f - f0) * kBlk;
+      }
+      CK(cudaMemcpyAsync(d_fd + f0, hfd.data() + f0, nf * sizeof(FrontDesc<T>),
+                         cudaMemcpyHostToDevice, s));
+      if (!dwork.empty())
+        CK(cudaMemcpyAsync(d_dwork, dwork.data(), dwork.size() * sizeof(int4),
+                           cudaMemcpyHostToDevice, s));
+      const int* fr = S->d_fronts + f0;
+      // assembly
+      int64_t maxz = 0;
+      for (int f = f0; f < f1; ++f) {
+        int64_t z = std::max<int64_t>((int64_t)ld_[f] * n_[f], (int64_t)hfd[f].cm * hfd[f].cm);
+        maxz = std::max(maxz, z);
+      }
+      launch_zero_fronts<T>(d_fd, fr, nf, (int)std::min<int64_t>(maxz, 1 << 30), s);
+      launch_load_a<T>(d_fd, fr, nf, S->d_nptr, S->d_nlist, cur_aval, S->d_rlist, S->d_rptr,
+                       d_scale, max_ent, s);
+      launch_init_perm<T>(d_fd, fr, nf, S->d_sptr, max_n, s);
+      launch_assemble_delays<T>(d_fd, d_st, d_dwork, (int)dwork.size(), S->d_rdir,
+                                S->d_rdir_ptr, s);
+      launch_assemble_contrib<T>(d_fd, S->d_cols + S->cols_start[l],
+                                 S->cols_start[l + 1] - S->cols_start[l], S->d_pairs, S->d_rdir,
+                                 S->d_rdir_ptr, s);
+      // dense factorisation
+      const bool use_app = co.pivot_method != 3;
+      if (use_app) {
+        const int steps = (max_n + kBlk - 1) / kBlk;
+        for (int st = 0; st < steps; ++st) {
+          int mr = 0, tr = 0, tc = 0;
+          for (int f = f0; f < f1; ++f) {
+            mr = std::max(mr, m_[f] - kBlk * st);
+            tr = std::max(tr, m_[f] - kBlk * (st + 1));
+            tc = std::max(tc, n_[f] - kBlk * (st + 1));
+          }
+          launch_app_step<T>(d_fd, d_st, fr, nf, st, std::max(mr, 1), tr, tc, co.action, co.u,
+                             co.small, s);
+        }
+      }
+      launch_app_finish<T>(d_fd, d_st, fr, nf, s);
+      const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
+      launch_tpp<T>(d_fd, d_st, fr, nf, co.action, co.u, co.small, tpp_all, s);
+      launch_contrib<T>(d_fd, d_st, fr, nf, max_cm, max_n, s);
+      launch_stats<T>(d_fd, d_st, fr, nf, max_n, d_stats, s);
+      CK(cudaMemcpyAsync(hst.data() + f0, d_st + f0, nf * sizeof(FrontState),
+                         cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      bool singular = false, bad = false;
+      for (int f = f0; f < f1; ++f) {
+        if (hst[f].status == kDevSingular) singular = true;
+        else if (hst[f].status != kDevOk) bad = true;
+        nelim_[f] = hst[f].nelim;
+        napp_[f] = hst[f].step;
+        lvl_max_m[l] = std::max(lvl_max_m[l], m_[f]);
+        lvl_max_nelim[l] = std::max(lvl_max_nelim[l], nelim_[f]);
+        if (use_app && napp_[f] < n_[f]) nfp += n_[f] - napp_[f];
+        bool tpp_ran = tpp_all || (m_[f] == n_[f]);
+        if (!use_app) nfp += n_[f] - nelim_[f];
+        else if (tpp_ran && napp_[f] < n_[f]) nsp += n_[f] - nelim_[f];
+      }
+      if (singular) { stats.flag = -5; return stats.flag; }
+      if (bad) { stats.flag = -51; return stats.flag; }
+    }
+    Stats hs;
+    CK(cudaMemcpyAsync(&hs, d_stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(ev[1], s));
+    CK(cudaStreamSynchronize(s));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    timing[0] = ms;
+    (void)host_wait;
+    stats.num_delay = hs.num_delay;
+    stats.num_factor = hs.num_factor;
+    stats.num_flops = hs.num_flops;
+    stats.num_neg = hs.num_neg;
+    stats.num_two = hs.num_two;
+    stats.num_zero = hs.num_zero;
+    stats.maxfront = maxfront;
+    stats.maxsupernode = maxsn;
+    stats.not_first_pass = nfp;
+    stats.not_second_pass = nsp;
+    stats.flag = 0;
+    // delays left at a root are unrecoverable
+    for (int f = 0; f < nn; ++f)
+      if (S->parent[S->node_of[f]] < 0 && nelim_[f] < n_[f]) stats.flag = -5;
+    if (stats.num_zero > 0 && stats.flag == 0) stats.flag = 7;
+    if (posdef) {
+      if (stats.num_neg > 0 || stats.num_zero > 0 || stats.num_two > 0) stats.flag = -6;
+      stats.num_neg = 0; stats.num_two = 0; stats.num_zero = 0;
+    }
+    return stats.flag;
+  }
+
+  void prepare_solve() {
+    if (solve_ready) return;
+    const int nn = S->nnodes;
+    std::vector<SolveNode<T>> sn(nn);
+    std::vector<int> ch;
+    size_t xl = 0;
+    std::vector<size_t> xoff(nn);
+    for (int f = 0; f < nn; ++f) { xoff[f] = xl; xl += (size_t)m_[f] * kSolveRhs; }
+    xloc.ensure(xl + 1);
+    xorig.ensure(xl + 1);
+    for (int f = 0; f < nn; ++f) {
+      const int node = S->node_of[f];
+      SolveNode<T>& q = sn[f];
+      q.L = hfd[f].L; q.D = hfd[f].D; q.perm = hfd[f].perm; q.opos = hfd[f].opos;
+      q.rows = S->d_rlist + S->rptr[node];
+      q.rdir = S->d_rdir + S->rdir_ptr_h[node];
+      q.xloc = xloc.p + xoff[f];
+      q.xorig = xorig.p + xoff[f];
+      q.m = m_[f]; q.n = n_[f]; q.ld = ld_[f]; q.nelim = nelim_[f];
+      q.ncol = S->ncol[node]; q.nrow = S->nrow[node]; q.ndelay_in = ndin_[f];
+      q.cm = S->nrow[node] - S->ncol[node];
+      q.sptr0 = S->sptr[node];
+      q.child_beg = (int)ch.size();
+      for (int c : S->children[node]) ch.push_back(S->front_of[c]);
+      q.child_end = (int)ch.size();
+      q.doff = doff_[f];
+    }
+    cudaFree(d_sn);
+    cudaFree(d_children);
+    d_sn = nullptr;
+    d_children = nullptr;
+    d_sn = upload(sn);
+    d_children = upload(ch);
+    solve_ready = true;
+  }
+
+  int solve_dev(int job, int nrhs, double* x, int ldx, cudaStream_t us) override {
+    prepare_solve();
+    cudaStream_t s = stream;
+    if (us) CK(cudaStreamSynchronize(us));
+    const bool fwd = (job == 0 || job == 1);
+    const bool diag = (job == 0 || job == 2 || job == 4);
+    const bool bwd = (job == 0 || job == 3 || job == 4);
+    for (int r0 = 0; r0 < nrhs; r0 += kSolveRhs) {
+      const int q = std::min(kSolveRhs, nrhs - r0);
+      double* xp = x + (int64_t)r0 * ldx;
+      if (fwd) {
+        for (int l = 0; l < S->nlev; ++l) {
+          const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
+          const int* fr = S->d_fronts + f0;
+          launch_fwd_gather<T>(d_sn, fr, nf, d_children, xp, ldx, q, s);
+          launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, s);
+          launch_fwd_scatter<T>(d_sn, fr, nf, xp, ldx, q, lvl_max_nelim[l], s);
+        }
+      }
+      if (diag || bwd) {
+        for (int l = S->nlev - 1; l >= 0; --l) {
+          const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
+          launch_bwd<T>(d_sn, S->d_fronts + f0, nf, xp, ldx, q, lvl_max_m[l], lvl_max_nelim[l],
+                        diag, bwd, s);
+        }
+      }
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    return 0;
+  }
+
+  // full solve with FP64 iterative refinement; x (host) holds b on entry
+  int solve_refined(int nrhs, double* xh, int ldx, int* iters) override {
+    const int n = S->n;
+    cudaStream_t s = stream;
+    int itmax = 0;
+    for (int r0 = 0; r0 < nrhs; r0 += kSolveRhs) {
+      const int q = std::min(kSolveRhs, nrhs - r0);
+      bbuf.ensure((size_t)n * q + 1);
+      xbuf.ensure((size_t)n * q + 1);
+      rbuf.ensure((size_t)n * q + 1);
+      nbuf.ensure(q + 1 + 3 * kSolveRhs + 8);
+      for (int r = 0; r < q; ++r)
+        CK(cudaMemcpyAsync(bbuf.p + (size_t)r * n, xh + (size_t)(r0 + r) * ldx,
+                           n * sizeof(double), cudaMemcpyHostToDevice, s));
+      CK(cudaMemcpyAsync(xbuf.p, bbuf.p, (size_t)n * q * sizeof(double),
+                         cudaMemcpyDeviceToDevice, s));
+      solve_dev(0, q, xbuf.p, n, nullptr);
+      int it = refine_dev(q, xbuf.p, bbuf.p, n);
+      itmax = std::max(itmax, it);
+      for (int r = 0; r < q; ++r)
+        CK(cudaMemcpyAsync(xh + (size_t)(r0 + r) * ldx, xbuf.p + (size_t)r * n,
+                           n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    if (iters) *iters = itmax;
+    return 0;
+  }
+
+  // refinement of x (device, n x q, ld) against b; returns steps taken
+  int refine_dev(int q, double* x, const double* b, int ld) {
+    const int n = S->n;
+    cudaStream_t s = stream;
+    rbuf.ensure((size_t)ld * q + 1);
+    nbuf.ensure(q + 1 + 3 * kSolveRhs + 8);
+    std::vector<double> h(q);
+    int it = 0;
+    const int maxit = S->gopts.max_refine;
+    for (;; ++it) {
+      launch_spmv_resid(S->d_aptr, S->d_acol, S->d_asrc, cur_aval, n, x, b, rbuf.p, q, ld, s);
+      launch_bwd_err(S->d_aptr, S->d_asrc, cur_aval, n, x, rbuf.p, b, q, ld, nbuf.p, s);
+      CK(cudaMemcpyAsync(h.data(), nbuf.p, q * sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      double worst = 0;
+      for (int r = 0; r < q; ++r) worst = std::max(worst, h[r]);
+      last_bwd_err = worst;
+      if (!(worst > S->gopts.refine_tol) || it >= maxit) break;
+      solve_dev(0, q, rbuf.p, ld, nullptr);
+      launch_axpy(n, q, ld, x, rbuf.p, s);
+    }
+    return it;
+  }
+
+  void download_dp(std::vector<double>& D, std::vector<int>& P, int f) {
+    D.resize(2 * (size_t)n_[f]);
+    P.resize(n_[f]);
+    CK(cudaMemcpy(D.data(), hfd[f].D, D.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(P.data(), hfd[f].perm, P.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  }
+
+  // node order as the CPU enquire (NumericSubtree.hxx:402-445)
+  void enquire(int* piv_order, double* d) override {
+    std::vector<double> D;
+    std::vector<int> P;
+    int piv = 0;
+    for (int node = 0; node < S->nnodes; ++node) {
+      const int f = S->front_of[node];
+      download_dp(D, P, f);
+      const int ne = nelim_[f];
+      for (int i = 0; i < ne;) {
+        if (i + 1 == ne || std::isfinite(D[2 * i + 2])) {
+          if (piv_order) piv_order[P[i]] = piv++;
+          if (d) { *d++ = D[2 * i]; *d++ = 0.0; }
+          i += 1;
+        } else {
+          if (piv_order) { piv_order[P[i]] = -(piv++); piv_order[P[i + 1]] = -(piv++); }
+          if (d) { *d++ = D[2 * i]; *d++ = D[2 * i + 1]; *d++ = D[2 * i + 3]; *d++ = 0.0; }
+          i += 2;
+        }
+      }
+    }
+  }
+
+  void alter(const double* d) override {
+    std::vector<double> D;
+    std::vector<int> P;
+    for (int node = 0; node < S->nnodes; ++node) {
+      const int f = S->front_of[node];
+      download_dp(D, P, f);
+      const int ne = nelim_[f];
+      for (int i = 0; i < ne;) {
+        if (i + 1 == ne || std::isfinite(D[2 * i + 2])) {
+          D[2 * i] = *d++; d++;
+          i += 1;
+        } else {
+          D[2 * i] = *d++; D[2 * i + 1] = *d++; D[2 * i + 3] = *d++; d++;
+          i += 2;
+        }
+      }
+      CK(cudaMemcpy(hfd[f].D, D.data(), D.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+  }
+};
+
+}  // namespace ssids300
+
+using namespace ssids300;
+
+namespace {
+int map_cuda_error(const CudaFail& e, spral_ssids_thread_stats* st) {
+  if (st) st->flag = (e.err == cudaErrorMemoryAllocation) ? -50 : -51;
+  fprintf(stderr, "spral_gb300: CUDA error %d (%s) at numeric.cu:%d\n", (int)e.err,
+          cudaGetErrorString(e.err), e.line);
+  cudaGetLastError();
+  return (e.err == cudaErrorMemoryAllocation) ? -50 : -51;
+}
+}  // namespace
+
+extern "C" {
+
+int spral_ssids_gpu_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) { cudaGetLastError(); return 0; }
+  return n;
+}
+
+void* spral_ssids_gpu_create_symbolic_subtree(int device, int n, int sa, int en, const int* sptr,
+                                              const int* sparent, const int64_t* rptr,
+                                              const int* rlist, const int64_t* nptr,
+                                              const int64_t* nlist,
+                                              const struct spral_ssids_cpu_factor_options* options) {
+  try {
+    if (cudaSetDevice(device) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return build_symbolic(device, n, sa, en, sptr, sparent, rptr, rlist, nptr, nlist, options);
+  } catch (CudaFail const& e) {
+    map_cuda_error(e, nullptr);
+    return nullptr;
+  } catch (std::bad_alloc const&) {
+    return nullptr;
+  }
+}
+
+void spral_ssids_gpu_destroy_symbolic_subtree(void* symbolic) {
+  delete static_cast<Symbolic*>(symbolic);
+}
+
+int spral_ssids_gpu_set_options(void* symbolic, const struct spral_ssids_gpu_options* opts) {
+  if (!symbolic || !opts) return -1;
+  static_cast<Symbolic*>(symbolic)->gopts = *opts;
+  return 0;
+}
+
+void* spral_ssids_gpu_create_num_subtree_dbl(bool posdef, const void* symbolic, const double* aval,
+                                             const double* scaling, void** child_contrib,
+                                             const struct spral_ssids_cpu_factor_options* options,
+                                             struct spral_ssids_thread_stats* stats) {
+  Symbolic* S = const_cast<Symbolic*>(static_cast<const Symbolic*>(symbolic));
+  if (stats) *stats = spral_ssids_thread_stats{};
+  if (!S) { if (stats) stats->flag = -51; return nullptr; }
+  if (child_contrib) { /* inter-subtree contributions are not supported */ }
+  if (options) S->copts = *options;
+  NumericBase* N = nullptr;
+  try {
+    CK(cudaSetDevice(S->device));
+    if (S->gopts.precision == 1) N = new Numeric<float>(S);
+    else N = new Numeric<double>(S);
+    N->posdef = posdef;
+    N->precision = S->gopts.precision;
+    N->factor(aval, false, scaling, nullptr);
+    if (stats) *stats = N->stats;
+    return N;
+  } catch (CudaFail const& e) {
+    map_cuda_error(e, stats);
+    if (N) N->stats.flag = stats ? stats->flag : -51;
+    return N;
+  } catch (std::bad_alloc const&) {
+    if (stats) stats->flag = -50;
+    return N;
+  }
+}
+
+void spral_ssids_gpu_destroy_num_subtree_dbl(bool posdef, void* numeric) {
+  (void)posdef;
+  delete static_cast<NumericBase*>(numeric);
+}
+
+int spral_ssids_gpu_refactor_dev(void* numeric, const double* aval_dev,
+                                 struct spral_ssids_thread_stats* stats, void* stream) {
+  NumericBase* N = static_cast<NumericBase*>(numeric);
+  try {
+    int fl = N->factor(aval_dev, true, nullptr, (cudaStream_t)stream);
+    if (stats) *stats = N->stats;
+    return fl;
+  } catch (CudaFail const& e) {
+    return map_cuda_error(e, stats);
+  } catch (std::bad_alloc const&) {
+    return -50;
+  }
+}
+
+static int host_solve(const void* numeric, int job, int nrhs, double* x, int ldx) {
+  NumericBase* N = const_cast<NumericBase*>(static_cast<const NumericBase*>(numeric));
+  Symbolic* S = N->symbolic();
+  const int n = S->n;
+  double* dx = nullptr;
+  try {
+    CK(cudaSetDevice(S->device));
+    CK(cudaMalloc(&dx, std::max<size_t>((size_t)n * nrhs, 1) * sizeof(double)));
+    for (int r = 0; r < nrhs; ++r)
+      CK(cudaMemcpy(dx + (size_t)r * n, x + (size_t)r * ldx, n * sizeof(double),
+                    cudaMemcpyHostToDevice));
+    N->solve_dev(job, nrhs, dx, n, nullptr);
+    for (int r = 0; r < nrhs; ++r)
+      CK(cudaMemcpy(x + (size_t)r * ldx, dx + (size_t)r * n, n * sizeof(double),
+                    cudaMemcpyDeviceToHost));
+    cudaFree(dx);
+    return 0;
+  } catch (CudaFail const& e) {
+    if (dx) cudaFree(dx);
+    return map_cuda_error(e, nullptr);
+  }
+}
+
+int spral_ssids_gpu_subtree_solve_fwd_dbl(bool posdef, const void* numeric, int nrhs, double* x,
+                                          int ldx) {
+  (void)posdef;
+  return host_solve(numeric, 1, nrhs, x, ldx);
+}
+int spral_ssids_gpu_subtree_solve_diag_dbl(bool posdef, const void* numeric, int nrhs, double* x,
+                                           int ldx) {
+  (void)posdef;
+  return host_solve(numeric, 2, nrhs, x, ldx);
+}
+int spral_ssids_gpu_subtree_solve_diag_bwd_dbl(bool posdef, const void* numeric, int nrhs,
+                                               double* x, int ldx) {
+  (void)posdef;
+  return host_solve(numeric, 4, nrhs, x, ldx);
+}
+int spral_ssids_gpu_subtree_solve_bwd_dbl(bool posdef, const void* numeric, int nrhs, double* x,
+                                          int ldx) {
+  (void)posdef;
+  return host_solve(numeric, 3, nrhs, x, ldx);
+}
+
+int spral_ssids_gpu_solve_dev(void* numeric, int job, int nrhs, double* x_dev, int ldx,
+                              void* stream) {
+  NumericBase* N = static_cast<NumericBase*>(numeric);
+  try {
+    return N->solve_dev(job, nrhs, x_dev, ldx, (cudaStream_t)stream);
+  } catch (CudaFail const& e) {
+    return map_cuda_error(e, nullptr);
+  }
+}
+
+int spral_ssids_gpu_solve_refined(void* numeric, int nrhs, double* x, int ldx, int* iters) {
+  NumericBase* N = static_cast<NumericBase*>(numeric);
+  try {
+    return N->solve_refined(nrhs, x, ldx, iters);
+  } catch (CudaFail const& e) {
+    return map_cuda_error(e, nullptr);
+  }
+}
+
+void spral_ssids_gpu_subtree_enquire_dbl(bool posdef, const void* numeric, int* piv_order,
+                                         double* d) {
+  (void)posdef;
+  NumericBase* N = const_cast<NumericBase*>(static_cast<const NumericBase*>(numeric));
+  try {
+    N->enquire(piv_order, d);
+  } catch (CudaFail const& e) {
+    map_cuda_error(e, nullptr);
+  }
+}
+
+void spral_ssids_gpu_subtree_alter_dbl(bool posdef, void* numeric, const double* d) {
+  (void)posdef;
+  try {
+    static_cast<NumericBase*>(numeric)->alter(d);
+  } catch (CudaFail const& e) {
+    map_cuda_error(e, nullptr);
+  }
+}
+
+int spral_ssids_gpu_last_timing(const void* numeric, double* out) {
+  const NumericBase* N = static_cast<const NumericBase*>(numeric);
+  for (int i = 0; i < 5; ++i) out[i] = N->timing[i];
+  return 5;
+}
+
+}  // extern "C"

@@ -1,0 +1,144 @@
+// Shared declarations of the GB300 numeric factor/solve for SSIDS.
+//
+// Layout in HBM (one numeric subtree = the whole assembly tree):
+//   * front f: L is m x n column-major, leading dimension ld >= m (m, n
+//     include delayed columns from children; delays follow the node's own
+//     columns, as in src/ssids/cpu/kernels/assemble.hxx:227-263).  L holds the
+//     true factor (unit diagonal, scaled by D^{-1}) for eliminated columns.
+//   * D^{-1} per front: 2 x n doubles in the reference CPU format
+//     (src/ssids/cpu/kernels/ldlt_app.cxx:338-343): 1x1 -> (d11, 0); 2x2 ->
+//     (d11, d21), (+Inf, d22).  Always FP64, whatever the factor type.
+//   * perm per front: n ints, 0-based pivot positions (rlist order).
+//   * contribution block per front: cm x cm (cm = nrow - ncol), lower part.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ssids300 {
+
+constexpr int kBlk = 32;         // APP inner block (ldlt_app.cxx:41 INNER_BLOCK_SIZE)
+constexpr int kApplyRows = 128;  // rows per apply/fixup CTA
+constexpr int kGemmTile = 64;    // SIMT GEMM tile
+
+// Error codes written to the device status word (host maps to SSIDS flags).
+enum DevStatus : int {
+  kDevOk = 0,
+  kDevSingular = 1,   // zero pivot with action == false  -> SSIDS_ERROR_SINGULAR
+  kDevBadState = 2,   // internal consistency check failed -> SSIDS_ERROR_CUDA_UNKNOWN
+};
+
+template <typename T>
+struct FrontDesc {
+  T* L;          // m x n, ld
+  double* D;     // 2 x n
+  int* perm;     // n
+  int* opos;     // n: original (assembly-time) position of each final position
+  T* C;          // cm x cm contribution block (nullptr if cm == 0)
+  T* W;          // per-level workspace, >= ld x 32
+  double* step;  // per-front step buffer: L11 (32x32) + D (64) doubles
+  int* lperm;    // per-front step buffer: 32 ints (local block permutation)
+  T* swapbuf;    // per-level workspace for column moves: 64 x ld
+  T* LD;         // per-level workspace for L*D of the contribution rows (cm x n)
+  int m, n, ld;  // rows, fully-summed columns (incl. delays), leading dim
+  int nrow, ncol, ndelay_in, cm;
+  int node;
+  int pad;
+};
+
+struct FrontState {
+  int p;          // number eliminated so far (APP)
+  int end;        // end of the APP candidate range
+  int bs;         // current block width (0 = done)
+  int npass_raw;  // first failing column from the threshold test
+  int npass;      // adjusted (2x2 not split)
+  int nelim;      // final
+  int status;     // DevStatus
+  int step;       // step counter (sanity)
+};
+
+struct Stats {  // device-side reduction target (integers only -> deterministic)
+  int num_neg, num_two, num_zero, num_delay;
+  long long num_factor, num_flops;
+};
+
+// ---------------- launchers (defined in the kernel .cu files) --------------
+// assembly (assemble_kernels.cu)
+template <typename T>
+void launch_load_a(const FrontDesc<T>* fd, const int* fronts, int nf, const int64_t* nptr,
+                   const int64_t* nlist, const double* aval, const int* rlist,
+                   const int64_t* rptr, const double* scaling, int max_entries, cudaStream_t s);
+template <typename T>
+void launch_init_perm(const FrontDesc<T>* fd, const int* fronts, int nf, const int* sptr,
+                      int max_n, cudaStream_t s);
+template <typename T>
+void launch_assemble_delays(const FrontDesc<T>* fd, const FrontState* st, const int4* work,
+                            int nwork, const int* rdir, const int64_t* rdir_ptr, cudaStream_t s);
+template <typename T>
+void launch_assemble_contrib(const FrontDesc<T>* fd, const int4* cols, int ncols,
+                             const int2* pairs, const int* rdir, const int64_t* rdir_ptr,
+                             cudaStream_t s);
+template <typename T>
+void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int step,
+                     int max_rows, int max_trail_rows, int max_trail_cols, bool action,
+                     double u, double small, cudaStream_t s);
+template <typename T>
+void launch_app_finish(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf,
+                       cudaStream_t s);
+template <typename T>
+void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
+                double u, double small, bool root_only_or_all, cudaStream_t s);
+template <typename T>
+void launch_contrib(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
+                    int max_n, cudaStream_t s);
+template <typename T>
+void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
+                  int max_n, Stats* stats, cudaStream_t s);
+
+// syrk-like lower update C(r,c) -= sum_k A(r,k) B(c,k), r >= c
+template <typename T>
+struct SyrkJob {
+  T* C;
+  const T* A;
+  const T* B;
+  int ldc, lda, ldb;
+  int M, N, K;
+};
+
+// ---------------- solve (solve_kernels.cu) ----------------
+// Per node data for the level-set solves.  x is n x nrhs (ld = ldx) in pivot
+// order, FP64.  xloc holds the node's local vector (m x nrhs, ld = m) and is
+// kept for the whole forward pass: its rows [nelim, m) are the node's
+// contribution to its parent.
+template <typename T>
+struct SolveNode {
+  const T* L;
+  const double* D;
+  const int* perm;   // n: pivot position of each final front position
+  const int* opos;   // n: original position of each final front position
+  const int* rows;   // rlist of the node (0-based pivot positions), nrow entries
+  const int* rdir;   // cm entries: parent position of each contribution row
+  double* xloc;      // m x nrhs
+  double* xorig;     // m x nrhs scratch (forward gather)
+  int m, n, ld, nelim, ncol, nrow, ndelay_in, cm;
+  int sptr0;         // first own pivot
+  int child_beg, child_end;  // into the child arrays
+  int doff;          // offset of this node's delays inside its parent's delay block
+};
+
+constexpr int kSolveBlk = 64;   // diagonal block of the blocked triangular solves
+constexpr int kSolveRhs = 16;   // right-hand sides per pass
+
+template <typename T>
+void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const int* children,
+                       const double* x, int ldx, int nrhs, cudaStream_t s);
+template <typename T>
+void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_nelim,
+                      int max_m, int nrhs, cudaStream_t s);
+template <typename T>
+void launch_fwd_scatter(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx,
+                        int nrhs, int max_nelim, cudaStream_t s);
+template <typename T>
+void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx, int nrhs,
+                int max_m, int max_nelim, bool do_diag, bool do_bwd, cudaStream_t s);
+
+}  // namespace ssids300

@@ -1,0 +1,193 @@
+"""GPU parity tests: the CUDA factor/solve through the C-ABI against the
+analytic inertia, the committed reference fixtures and the oracle."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from spral_gb300 import matrices as M, ssids
+import oracle
+
+pytestmark = pytest.mark.gpu
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+# tolerances: inertia exact; scaled backward error of an FP64 direct solve;
+# solution against the FP64 reference within 1e-10 relative
+BWD_TOL = 1e-14
+SOL_TOL = 1e-10
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def test_gpu_lap2d_64_analytic():
+    p, r, v = M.laplacian_2d(64, 64, -0.5)
+    ak = ssids.analyse(p, r, M.nd_order_grid(64, 64))
+    fk, inf = ssids.factor(ak, v)
+    assert inf.flag == 0
+    assert inf.num_neg == 158
+    assert inf.matrix_rank == 4096
+    b = np.random.default_rng(0).uniform(-1, 1, 4096)
+    x = fk.solve(b)
+    assert M.scaled_bwd_error(p, r, v, x, b).max() <= BWD_TOL
+    xo = oracle.OracleFactor(ak, v).solve(b)
+    assert _rel(x, xo) < SOL_TOL
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_gpu_matches_reference_fixture(path):
+    g = np.load(path)
+    p, r, v, b = g["ptr"], g["row"], g["val"], g["b"]
+    ak = ssids.analyse(p, r, g["order"])
+    fk, inf = ssids.factor(ak, v)
+    assert inf.flag == int(g["stat_flag"])
+    assert inf.num_neg == int(g["stat_num_neg"])
+    assert inf.matrix_rank == len(p) - 1 - int(g["stat_num_zero"])
+    x = fk.solve(b)
+    assert M.scaled_bwd_error(p, r, v, x, b).max() <= 5e-14
+    assert _rel(x, g["x"]) < SOL_TOL
+
+
+@pytest.mark.parametrize("seed", [11, 12])
+def test_gpu_vs_oracle_with_delays(seed):
+    p, r, v = M.random_indef(400, density=0.02, seed=seed, diag_scale=0.01)
+    ak = ssids.analyse(p, r, ssids.order_mindeg(p, r))
+    fk, inf = ssids.factor(ak, v)
+    F = oracle.OracleFactor(ak, v)
+    assert inf.num_neg == F.stats["num_neg"]
+    assert inf.num_delay > 0  # the case must exercise delayed pivots
+    b = np.random.default_rng(seed).uniform(-1, 1, (400, 3))
+    x = fk.solve(b)
+    assert M.scaled_bwd_error(p, r, v, x, b).max() <= 1e-13
+    assert _rel(x, F.solve(b)) < 1e-8
+
+
+def test_gpu_kkt_2x2_and_delays():
+    p, r, v = M.kkt(600, 250, seed=2)
+    ak = ssids.analyse(p, r, ssids.order_mindeg(p, r))
+    fk, inf = ssids.factor(ak, v)
+    assert inf.num_neg == 250  # Sylvester: A has full row rank
+    assert inf.num_two > 0
+    b = np.random.default_rng(2).standard_normal((850, 2))
+    x = fk.solve(b)
+    assert M.scaled_bwd_error(p, r, v, x, b).max() <= 1e-14
+
+
+def test_gpu_partial_solves_compose():
+    p, r, v = M.random_indef(300, density=0.03, seed=5, diag_scale=0.01)
+    ak = ssids.analyse(p, r, ssids.order_mindeg(p, r))
+    fk, _ = ssids.factor(ak, v)
+    b = np.random.default_rng(5).uniform(-1, 1, (300, 2))
+    x_full = fk.solve(b)
+    y = fk.solve(b, job=1)
+    x2 = fk.solve(y, job=4)
+    assert _rel(x2, x_full) < 1e-12
+    z = fk.solve(fk.solve(y, job=2), job=3)
+    assert _rel(z, x_full) < 1e-12
+
+
+def test_gpu_partial_solves_match_oracle_when_pivots_match():
+    p, r, v = M.laplacian_2d(24, 24, -0.5)
+    ak = ssids.analyse(p, r, M.nd_order_grid(24, 24))
+    fk, _ = ssids.factor(ak, v)
+    F = oracle.OracleFactor(ak, v)
+    pg, dg = fk.enquire_indef()
+    po, do = F.enquire_indef()
+    if not np.array_equal(pg, po):
+        pytest.skip("pivot sequences differ by rounding; compare full solves only")
+    assert np.abs(dg - do).max() <= 1e-12 * np.abs(do).max()
+    b = np.random.default_rng(1).uniform(-1, 1, 576)
+    for job in (1, 2, 3, 4):
+        assert _rel(fk.solve(b, job=job), F.solve(b, job=job)) < 1e-11
+
+
+def test_gpu_many_rhs_chunks():
+    p, r, v = M.laplacian_3d(10, shift=-0.5)
+    ak = ssids.analyse(p, r, M.nd_order_grid(10, 10, 10))
+    fk, _ = ssids.factor(ak, v)
+    b = np.random.default_rng(3).standard_normal((1000, 37))
+    x = fk.solve(b)
+    assert M.scaled_bwd_error(p, r, v, x, b).max() <= BWD_TOL
+    x1 = fk.solve(b[:, 5])
+    assert _rel(x1, x[:, 5]) < 1e-14
+
+
+def test_gpu_3d_analytic_inertia():
+    k = 20
+    p, r, v = M.laplacian_3d(k, shift=-0.3)
+    ak = ssids.analyse(p, r, M.nd_order_grid(k, k, k))
+    fk, inf = ssids.factor(ak, v)
+    neg, zero, _ = M.laplacian_eig_count_3d(k, k, k, -0.3)
+    assert inf.num_neg == neg
+    b = np.random.default_rng(4).standard_normal((k ** 3, 8))
+    x = fk.solve(b)
+    assert M.scaled_bwd_error(p, r, v, x, b).max() <= BWD_TOL
+
+
+def test_gpu_singular_flags():
+    p, r, v = M.laplacian_2d(6, 6, -0.5)
+    v = v.copy()
+    cols = np.repeat(np.arange(36), np.diff(p))
+    v[(r == 7) | (cols == 7)] = 0.0
+    ak = ssids.analyse(p, r, M.nd_order_grid(6, 6))
+    fk, inf = ssids.factor(ak, v)
+    assert inf.flag == ssids.SSIDS_WARNING_FACT_SINGULAR
+    assert inf.matrix_rank == 35
+    fk2, inf2 = ssids.factor(ak, v, ssids.Options(action=False))
+    assert inf2.flag == ssids.SSIDS_ERROR_SINGULAR
+
+
+def test_gpu_tpp_only():
+    p, r, v = M.random_indef(150, density=0.04, seed=9, diag_scale=0.01)
+    ak = ssids.analyse(p, r, ssids.order_mindeg(p, r))
+    fk, inf = ssids.factor(ak, v, ssids.Options(pivot_method=3))
+    F = oracle.OracleFactor(ak, v, options=oracle.default_options(pivot_method=3))
+    assert inf.num_neg == F.stats["num_neg"]
+    b = np.random.default_rng(9).uniform(-1, 1, 150)
+    assert M.scaled_bwd_error(p, r, v, fk.solve(b), b).max() <= 1e-13
+
+
+def test_gpu_enquire_alter_roundtrip():
+    p, r, v = M.kkt(120, 40, seed=4)
+    ak = ssids.analyse(p, r, ssids.order_mindeg(p, r))
+    fk, _ = ssids.factor(ak, v)
+    piv, d = fk.enquire_indef()
+    b = np.random.default_rng(4).standard_normal(160)
+    x0 = fk.solve(b)
+    fk.alter(d)
+    assert _rel(fk.solve(b), x0) < 1e-15
+    # negative piv_order marks 2x2 pivots; every variable appears once
+    assert sorted(np.abs(piv).tolist())[-1] == 159
+
+
+def test_gpu_refactor_same_pattern_device_values():
+    torch = pytest.importorskip("torch")
+    p, r, v = M.laplacian_3d(12, shift=-0.4)
+    ak = ssids.analyse(p, r, M.nd_order_grid(12, 12, 12))
+    fk, inf0 = ssids.factor(ak, v)
+    v2 = v.copy()
+    cols = np.repeat(np.arange(len(p) - 1), np.diff(p))
+    v2[r == cols] *= 1.7
+    dv = torch.tensor(v2, dtype=torch.float64, device="cuda")
+    assert fk.refactor_dev(dv.data_ptr()) == 0
+    fresh, inf1 = ssids.factor(ak, v2)
+    assert fk.inform.num_neg == inf1.num_neg
+    b = np.random.default_rng(0).standard_normal(len(p) - 1)
+    assert _rel(fk.solve(b), fresh.solve(b)) < 1e-12
+
+
+@pytest.mark.parametrize("k", [16, 24])
+def test_gpu_mixed_precision_refined(k):
+    p, r, v = M.laplacian_3d(k, shift=-0.3)
+    ak = ssids.analyse(p, r, M.nd_order_grid(k, k, k))
+    fk, inf = ssids.factor(ak, v, ssids.Options(precision=ssids.PRECISION_MIXED, max_refine=20,
+                                                refine_tol=1e-15))
+    neg, _, _ = M.laplacian_eig_count_3d(k, k, k, -0.3)
+    assert inf.num_neg == neg  # exact inertia from the FP32 factor's FP64 pivots
+    b = np.random.default_rng(k).standard_normal((k ** 3, 4))
+    x = fk.solve_refined(b)
+    assert M.scaled_bwd_error(p, r, v, x, b).max() <= BWD_TOL
+    xd, _ = ssids.factor(ak, v)
+    assert _rel(x, xd.solve(b)) < SOL_TOL
