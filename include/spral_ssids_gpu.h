@@ -142,6 +142,13 @@ int spral_ssids_gpu_solve_refined(void* numeric, int nrhs, double* x, int ldx, i
  * [3] contribution GEMM, [4] host wait.  Returns number of entries. */
 int spral_ssids_gpu_last_timing(const void* numeric, double* out);
 
+/* Diagnostics (no reference counterpart): copy one front of the factors to
+ * the host.  info[0..4] = m, n, nelim, ndelay_in, ld; L is m x n
+ * (ld = m, FP64), D is 2 x n, perm n 0-based pivot positions (any may be
+ * NULL).  node is 0-based. */
+int spral_ssids_gpu_debug_front(const void* numeric, int node, int* info, double* L, double* D,
+                                int* perm);
+
 /* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
 int spral_ssids_gpu_device_count(void);
 

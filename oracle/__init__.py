@@ -68,6 +68,7 @@ def oracle_lib():
         L.oracle_free.argtypes = [ctypes.c_void_p]
         L.oracle_node_info.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         L.oracle_enquire.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_node_data.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 3
         L.oracle_set_blas.restype = ctypes.c_int
         L.oracle_set_blas.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
     return _olib
@@ -164,6 +165,14 @@ class OracleFactor(_Base):
             oracle_lib().oracle_node_info(self.h, i, _P(tmp))
             out[i] = tmp
         return out
+
+    def front(self, node):
+        m, n, nelim, ndin = self.node_info()[node]
+        L = np.zeros((n, m))
+        D = np.zeros(2 * n)
+        perm = np.zeros(n, dtype=np.int32)
+        oracle_lib().oracle_node_data(self.h, node, _P(L), _P(D), _P(perm))
+        return dict(m=m, n=n, nelim=nelim, ndin=ndin, L=L.T.copy(), D=D, perm=perm)
 
     def enquire_indef(self):
         piv = np.zeros(self.akeep.n, dtype=np.int32)

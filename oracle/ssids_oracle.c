@@ -673,6 +673,15 @@ void oracle_node_info(void* h, int node, int* info) {
   info[0] = nd->m; info[1] = nd->n; info[2] = nd->nelim; info[3] = nd->ndelay_in;
 }
 
+/* copy one front: L (m x n, ld m), D (2n), perm (n, 0-based) */
+void oracle_node_data(void* h, int node, double* L, double* D, int* perm) {
+  ofactors* F = (ofactors*)h;
+  onode* nd = &F->nodes[node];
+  if (L) memcpy(L, nd->l, sizeof(double) * (size_t)nd->m * nd->n);
+  if (D) memcpy(D, &nd->l[(int64_t)nd->n * nd->m], sizeof(double) * 2 * (size_t)nd->n);
+  if (perm) for (int i = 0; i < nd->n; ++i) perm[i] = nd->perm[i] - 1;
+}
+
 /* Solve in pivot order (x already permuted by invp), nrhs columns, ldx.
  * job: 0 full, 1 fwd, 2 diag, 3 bwd (no D), 4 diag_bwd
  * (NumericSubtree.hxx:284-400; ldlt_app.cxx:2538-2589). */

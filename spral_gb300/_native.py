@@ -85,3 +85,4 @@ def _declare(L):
     f("spral_ssids_gpu_solve_dev", I, P, I, I, P, I, P)
     f("spral_ssids_gpu_last_timing", I, P, P)
     f("spral_ssids_gpu_device_count", I)
+    f("spral_ssids_gpu_debug_front", I, P, I, P, P, P, P)

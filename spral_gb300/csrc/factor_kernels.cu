@@ -828,9 +828,12 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
   int gx = std::max(1, cdiv(max_rows, kApplyRows));
   k_app_apply<T><<<dim3(gx, nf), kApplyRows, 0, s>>>(fd, st, fronts, u, small);
   k_app_fixup<T><<<dim3(gx, nf), kApplyRows, 0, s>>>(fd, st, fronts);
-  int tr = cdiv(max_trail_rows, kGemmTile), tc = cdiv(max_trail_cols, kGemmTile);
+  // tile estimate assumes no failed columns so far; after failures the
+  // trailing region is wider and the kernel's grid-stride loop covers it, so
+  // the launch is never skipped
+  int tr = std::max(0, cdiv(max_trail_rows, kGemmTile)), tc = std::max(0, cdiv(max_trail_cols, kGemmTile));
   int tiles = tc * tr - tc * (tc - 1) / 2;
-  if (tiles > 0) launch_syrk_panel<T>(fd, st, fronts, nf, tiles, s);
+  launch_syrk_panel<T>(fd, st, fronts, nf, std::max(tiles, 1), s);
   k_app_swap_gather<T><<<dim3(64, nf), 256, 0, s>>>(fd, st, fronts);
   k_app_swap_scatter<T><<<dim3(64, nf), 256, 0, s>>>(fd, st, fronts);
 }

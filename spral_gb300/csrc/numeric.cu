@@ -325,6 +325,7 @@ struct NumericBase {
   virtual void enquire(int* piv, double* d) = 0;
   virtual void alter(const double* d) = 0;
   virtual Symbolic* symbolic() = 0;
+  virtual int debug_front(int node, int* info, double* L, double* D, int* perm) = 0;
 };
 
 template <typename T>
@@ -689,6 +690,20 @@ struct Numeric : NumericBase {
     return it;
   }
 
+  int debug_front(int node, int* info, double* Lout, double* Dout, int* Pout) override {
+    const int f = S->front_of[node];
+    info[0] = m_[f]; info[1] = n_[f]; info[2] = nelim_[f]; info[3] = ndin_[f]; info[4] = ld_[f];
+    if (Lout) {
+      std::vector<T> tmp((size_t)ld_[f] * n_[f]);
+      CK(cudaMemcpy(tmp.data(), hfd[f].L, tmp.size() * sizeof(T), cudaMemcpyDeviceToHost));
+      for (int c = 0; c < n_[f]; ++c)
+        for (int r = 0; r < m_[f]; ++r) Lout[(size_t)c * m_[f] + r] = (double)tmp[(size_t)c * ld_[f] + r];
+    }
+    if (Dout) CK(cudaMemcpy(Dout, hfd[f].D, 2 * n_[f] * sizeof(double), cudaMemcpyDeviceToHost));
+    if (Pout) CK(cudaMemcpy(Pout, hfd[f].perm, n_[f] * sizeof(int), cudaMemcpyDeviceToHost));
+    return 0;
+  }
+
   void download_dp(std::vector<double>& D, std::vector<int>& P, int f) {
     D.resize(2 * (size_t)n_[f]);
     P.resize(n_[f]);
@@ -916,6 +931,16 @@ void spral_ssids_gpu_subtree_alter_dbl(bool posdef, void* numeric, const double*
     static_cast<NumericBase*>(numeric)->alter(d);
   } catch (CudaFail const& e) {
     map_cuda_error(e, nullptr);
+  }
+}
+
+int spral_ssids_gpu_debug_front(const void* numeric, int node, int* info, double* L, double* D,
+                                int* perm) {
+  NumericBase* N = const_cast<NumericBase*>(static_cast<const NumericBase*>(numeric));
+  try {
+    return N->debug_front(node, info, L, D, perm);
+  } catch (CudaFail const& e) {
+    return map_cuda_error(e, nullptr);
   }
 }
 

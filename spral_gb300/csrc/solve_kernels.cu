@@ -265,7 +265,7 @@ void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_
   const int steps = cdiv(max_nelim, SB);
   for (int st = 0; st < steps; ++st) {
     k_fwd_diag<T><<<nn, 256, 0, s>>>(sn, nodes, st, nrhs);
-    int rows = max_m - st * SB - SB;
+    int rows = max_m - st * SB;  // upper bound; the kernel derives the exact range
     if (rows > 0) {
       int gx = std::max(1, std::min(cdiv(rows, 256), 128));
       k_fwd_update<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, st, nrhs);

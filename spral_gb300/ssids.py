@@ -255,6 +255,17 @@ class Fkeep:
         d = np.ascontiguousarray(d, dtype=np.float64).reshape(-1)
         _native.lib().spral_ssids_gpu_subtree_alter_dbl(self.posdef, self.num, _P(d))
 
+    def front(self, node):
+        """Diagnostics: one front of the factors (m, n, nelim, L, D, perm)."""
+        info = np.zeros(5, dtype=np.int32)
+        _native.lib().spral_ssids_gpu_debug_front(self.num, node, _P(info), None, None, None)
+        m, n = int(info[0]), int(info[1])
+        L = np.zeros((n, m))
+        D = np.zeros(2 * n)
+        perm = np.zeros(n, dtype=np.int32)
+        _native.lib().spral_ssids_gpu_debug_front(self.num, node, _P(info), _P(L), _P(D), _P(perm))
+        return dict(m=m, n=n, nelim=int(info[2]), ndin=int(info[3]), L=L.T.copy(), D=D, perm=perm)
+
     def timing(self):
         out = np.zeros(5, dtype=np.float64)
         _native.lib().spral_ssids_gpu_last_timing(self.num, _P(out))
