@@ -1,0 +1,360 @@
+#!/usr/bin/env python
+"""Benchmark of the SSIDS numeric factor + solve on one GB300 per rank.
+
+Workload (default): the 3D 7-point Laplacian on a 48^3 grid (n = 110,592),
+diagonal shifted by -0.3 (indefinite), geometric nested-dissection order
+(stand-in for METIS), 8 Gaussian right-hand sides from a fixed seed.  One
+step = numeric factorisation of the matrix plus the solution of its 8
+right-hand sides; the metric counts such solves per second and the line
+records the scaled backward error actually reached.
+
+Arms:
+  default            the GB300 path (FP64 factors, the plain FP64 GPU path)
+                     with inputs resident in HBM (value), the same through the
+                     C-ABI with host buffers (e2e), the mixed-precision path
+                     (FP32 factors + FP64 refinement) as a second line item,
+                     the contribution-GEMM roofline, and the CPU baseline
+  --impl reference   the reference's CPU numeric path on the host cores:
+                     the reference's own C++ core where it was compiled here,
+                     else the oracle's C restatement (with OpenBLAS)
+
+Multi-GPU: the factorizations are independent replicas (no data exchange in
+the path), one process per GPU; value = all ranks' solves / max time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "solves/s at bwd err<=1e-14 mixed vs FP64 GPU; factor TFLOP/s; p50/p99 latency"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--grid", type=int, default=48)
+    ap.add_argument("--shift", type=float, default=-0.3)
+    ap.add_argument("--nrhs", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    return ap.parse_args()
+
+
+def problem(args):
+    from spral_gb300 import matrices as M, ssids
+    k = args.grid
+    ptr, row, val = M.laplacian_3d(k, shift=args.shift)
+    order = M.nd_order_grid(k, k, k)
+    ak = ssids.analyse(ptr, row, order)
+    rng = np.random.default_rng(2024)
+    b = rng.standard_normal((len(ptr) - 1, args.nrhs))
+    return ptr, row, val, ak, b
+
+
+def config(args, ak, extra=None):
+    c = {"workload": f"3D 7-point Laplacian {args.grid}^3 (n={ak.n}), shift {args.shift}, "
+                     f"nested-dissection order, {args.nrhs} RHS N(0,1); one solve = numeric "
+                     f"factor + {args.nrhs}-RHS solve",
+         "n": ak.n, "nnz_lower": ak.nnz, "nrhs": args.nrhs, "nemin": 32,
+         "predicted_flops": ak.nflops, "nfactor": ak.nfact,
+         "l2": "inputs larger than L2 (factors ~%.0f MB)" % (ak.nfact * 8 / 1e6),
+         "parallelism": f"replicas x{args.gpus}"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for ln in fh:
+                parts = [x.strip() for x in ln.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_reference_step_fn(ak, val, b, use_ref):
+    import oracle
+    if use_ref:
+        def step():
+            F = oracle.RefFactor(ak, val)
+            return F.solve(b), F.stats
+        kind = "reference"
+    else:
+        def step():
+            F = oracle.OracleFactor(ak, val, blas=True)
+            return F.solve(b), F.stats
+        kind = "port"
+    return step, kind
+
+
+def run_reference(args):
+    world, rank, local = dist_setup(args)
+    if rank != 0:
+        return
+    import oracle
+    from spral_gb300 import matrices as M
+    oracle.build()
+    ptr, row, val, ak, b = problem(args)
+    use_ref = oracle.ref_available()
+    step, kind = cpu_reference_step_fn(ak, val, b, use_ref)
+    for _ in range(min(args.warmup, 1)):
+        step()
+    budget = 150.0
+    times = []
+    x = None
+    t_all = time.perf_counter()
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        x, st = step()
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > budget:
+            break
+    ms = 1000.0 * sum(times) / len(times)
+    bwd = float(M.scaled_bwd_error(ptr, row, val, x, b).max())
+    val_ = 1000.0 / ms
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": METRIC, "value": val_, "unit": "solves/s",
+            "n_gpus": args.gpus, "steps": len(times), "warmup": min(args.warmup, 1),
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": config(args, ak, {"bwd_err": bwd, "num_neg": st["num_neg"]}),
+            "cpu_baseline": {"value": val_, "unit": "solves/s", "cores": cores, "kind": kind,
+                             "sample": f"{len(times)} full factor+solve steps of the workload "
+                                       f"(OpenMP/OpenBLAS threads = {cores})"},
+            "e2e": {"value": val_, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "p50_ms": float(np.percentile(np.array(times) * 1e3, 50)),
+            "p99_ms": float(np.percentile(np.array(times) * 1e3, 99))}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl")
+    from spral_gb300 import _native, matrices as M, ssids
+    L = _native.lib()
+    ptr, row, val, ak, b = problem(args)
+    n, nrhs = ak.n, args.nrhs
+    dev = torch.device("cuda", local)
+    bp = np.ascontiguousarray(b[ak.invp, :].T)  # (nrhs, n): column-major n x nrhs
+    aval_d = torch.tensor(val, dtype=torch.float64, device=dev)
+    b_d = torch.tensor(bp, dtype=torch.float64, device=dev)
+    x_d = torch.empty_like(b_d)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def measure(fk, mixed):
+        it = ctypes.c_int(0)
+        bw = ctypes.c_double(0)
+
+        def step():
+            fk.refactor_dev(aval_d.data_ptr())
+            if mixed:
+                L.spral_ssids_gpu_solve_refined_dev(fk.num, nrhs, ctypes.c_void_p(b_d.data_ptr()),
+                                                    ctypes.c_void_p(x_d.data_ptr()), n,
+                                                    ctypes.byref(it), ctypes.byref(bw))
+            else:
+                x_d.copy_(b_d)
+                fk.solve_dev(x_d.data_ptr(), nrhs, n, job=0)
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        barrier()
+        lc0 = L.spral_ssids_gpu_launch_count()
+        clk = Clocks(local) if rank == 0 else None
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        per = []
+        torch.cuda.synchronize()
+        ev0.record()
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            step()
+            torch.cuda.synchronize()
+            per.append((time.perf_counter() - t0) * 1e3)
+        ev1.record()
+        torch.cuda.synchronize()
+        clocks = clk.stop() if clk else None
+        barrier()
+        ms = ev0.elapsed_time(ev1) / args.steps
+        launches = L.spral_ssids_gpu_launch_count() - lc0
+        if dist is not None:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        x = x_d.cpu().numpy().T
+        xu = np.empty_like(x)
+        xu[ak.invp, :] = x
+        bwd = float(M.scaled_bwd_error(ptr, row, val, xu, b).max())
+        return ms, per, launches, clocks, bwd, it.value
+
+    opts64 = ssids.Options(precision=ssids.PRECISION_FP64)
+    fk = ssids.Fkeep(ak, val, opts64)
+    inform = fk.inform
+    ms, per, launches, clocks, bwd, _ = measure(fk, mixed=False)
+    value = world * 1000.0 / ms
+    factor_tflops = inform.num_flops / (fk.timing()[0] * 1e-3) / 1e12
+
+    # roofline of the dominant kernel: contribution GEMM, timed per launch
+    L.spral_ssids_gpu_set_profiling(fk.num, 1)
+    fk.refactor_dev(aval_d.data_ptr())
+    ps = np.zeros(3)
+    L.spral_ssids_gpu_profile_stats(fk.num, ps.ctypes.data_as(ctypes.c_void_p))
+    L.spral_ssids_gpu_set_profiling(fk.num, 0)
+    fp64_peak = L.spral_ssids_gpu_fp64_peak_tflops(local)
+    achieved = ps[1] / (ps[0] * 1e-3) / 1e12 if ps[0] > 0 else 0.0
+    traffic = None
+    tfile = os.path.join(HERE, "profiles", "contrib_gemm_fp64_traffic.json")
+    if os.path.exists(tfile):
+        try:
+            traffic = json.load(open(tfile)).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+    roofline = {"bound": "fp64", "kernel": "k_syrk<double,contrib> (contribution block GEMM)",
+                "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": traffic,
+                "peak_source": "FP64 FMA probe measured by bench.py on this GPU (the driver's "
+                               "measured peaks cover HBM and bf16 tensor only)",
+                "launches": int(ps[2]), "flops_per_step": ps[1]}
+
+    # end to end through the C-ABI with host buffers
+    copts = opts64.cpu_options()
+    e2e_times = []
+    xh = np.asfortranarray(b[ak.invp, :])
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        st = _native.ThreadStats()
+        num = L.spral_ssids_gpu_create_num_subtree_dbl(False, fk.sym,
+                                                       val.ctypes.data_as(ctypes.c_void_p), None,
+                                                       None, ctypes.byref(copts), ctypes.byref(st))
+        xw = xh.copy(order="F")
+        L.spral_ssids_gpu_subtree_solve_fwd_dbl(False, num, nrhs, xw.ctypes.data_as(ctypes.c_void_p), n)
+        L.spral_ssids_gpu_subtree_solve_diag_bwd_dbl(False, num, nrhs,
+                                                     xw.ctypes.data_as(ctypes.c_void_p), n)
+        L.spral_ssids_gpu_destroy_num_subtree_dbl(False, num)
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_ms = 1000.0 * sum(e2e_times) / len(e2e_times)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e = {"value": world * 1000.0 / e2e_ms, "unit": "solves/s",
+           "h2d_bytes_per_step": int(val.nbytes + n * nrhs * 8),
+           "d2h_bytes_per_step": int(n * nrhs * 8),
+           "path": "spral_ssids_gpu_create_num_subtree_dbl + subtree_solve_fwd/diag_bwd (host "
+                   "aval and x)"}
+
+    mixed = None
+    if not args.no_mixed:
+        fm = ssids.Fkeep(ak, val, ssids.Options(precision=ssids.PRECISION_MIXED, max_refine=20,
+                                                 refine_tol=1e-15))
+        mms, mper, mlaunch, _, mbwd, mit = measure(fm, mixed=True)
+        mixed = {"value": world * 1000.0 / mms, "unit": "solves/s", "ms_per_step": mms,
+                 "bwd_err": mbwd, "refine_iters": mit, "num_neg": fm.inform.num_neg,
+                 "factor_ms": float(fm.timing()[0]),
+                 "speedup_vs_fp64_gpu": (1000.0 / mms) / (1000.0 / ms)}
+        fm.free()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        step, kind = cpu_reference_step_fn(ak, val, b, oracle.ref_available())
+        t0 = time.perf_counter()
+        xc, stc = step()
+        tc = time.perf_counter() - t0
+        cpu = {"value": 1.0 / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": kind,
+               "sample": "one full factor+solve of the workload (OpenBLAS threads = all cores)",
+               "bwd_err": float(M.scaled_bwd_error(ptr, row, val, xc, b).max()),
+               "num_neg": stc["num_neg"]}
+
+    if rank == 0:
+        neg_exact, _, _ = M.laplacian_eig_count_3d(args.grid, args.grid, args.grid, args.shift)
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded 3D Laplacian and RHS)",
+                "config": config(args, ak, {"bwd_err": bwd, "num_neg": inform.num_neg,
+                                            "num_neg_exact": neg_exact,
+                                            "num_delay": inform.num_delay,
+                                            "num_flops": inform.num_flops}),
+                "factor_tflops": factor_tflops,
+                "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99)),
+                "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
+                "cpu_baseline": cpu, "clocks": clocks, "mixed_precision": mixed}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

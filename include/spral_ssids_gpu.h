@@ -149,6 +149,21 @@ int spral_ssids_gpu_last_timing(const void* numeric, double* out);
 int spral_ssids_gpu_debug_front(const void* numeric, int node, int* info, double* L, double* D,
                                 int* perm);
 
+/* Full solve plus FP64 refinement with b and x in device memory (n x nrhs,
+ * leading dimension ld, pivot order).  iters / bwd_err receive the largest
+ * refinement count and the final scaled backward error. */
+int spral_ssids_gpu_solve_refined_dev(void* numeric, int nrhs, const double* b_dev, double* x_dev,
+                                      int ld, int* iters, double* bwd_err);
+
+/* Benchmark support (no reference counterpart): kernels launched by this
+ * library so far; per-factor timing of the contribution-block GEMM with CUDA
+ * events on the library's stream (out[0] ms, out[1] algorithmic flops,
+ * out[2] launches); measured FP64 FMA throughput of the device. */
+long long spral_ssids_gpu_launch_count(void);
+void spral_ssids_gpu_set_profiling(void* numeric, int on);
+void spral_ssids_gpu_profile_stats(const void* numeric, double* out);
+double spral_ssids_gpu_fp64_peak_tflops(int device);
+
 /* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
 int spral_ssids_gpu_device_count(void);
 

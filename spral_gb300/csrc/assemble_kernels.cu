@@ -120,27 +120,27 @@ void launch_load_a(const FrontDesc<T>* fd, const int* fronts, int nf, const int6
                    const int64_t* rptr, const double* scaling, int max_entries, cudaStream_t s) {
   if (nf <= 0 || max_entries <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_entries, 256), 512));
-  k_load_a<T><<<dim3(gx, nf), 256, 0, s>>>(fd, fronts, nptr, nlist, aval, rlist, rptr, scaling);
+  { k_load_a<T><<<dim3(gx, nf), 256, 0, s>>>(fd, fronts, nptr, nlist, aval, rlist, rptr, scaling); note_launches(1); }
 }
 template <typename T>
 void launch_init_perm(const FrontDesc<T>* fd, const int* fronts, int nf, const int* sptr,
                       int max_n, cudaStream_t s) {
   if (nf <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_n, 256), 64));
-  k_init_perm<T><<<dim3(gx, nf), 256, 0, s>>>(fd, fronts, sptr);
+  { k_init_perm<T><<<dim3(gx, nf), 256, 0, s>>>(fd, fronts, sptr); note_launches(1); }
 }
 template <typename T>
 void launch_assemble_delays(const FrontDesc<T>* fd, const FrontState* st, const int4* work,
                             int nwork, const int* rdir, const int64_t* rdir_ptr, cudaStream_t s) {
   if (nwork <= 0) return;
-  k_assemble_delays<T><<<nwork, 128, 0, s>>>(fd, st, work, rdir, rdir_ptr);
+  { k_assemble_delays<T><<<nwork, 128, 0, s>>>(fd, st, work, rdir, rdir_ptr); note_launches(1); }
 }
 template <typename T>
 void launch_assemble_contrib(const FrontDesc<T>* fd, const int4* cols, int ncols,
                              const int2* pairs, const int* rdir, const int64_t* rdir_ptr,
                              cudaStream_t s) {
   if (ncols <= 0) return;
-  k_assemble_contrib<T><<<ncols, 128, 0, s>>>(fd, cols, pairs, rdir, rdir_ptr);
+  { k_assemble_contrib<T><<<ncols, 128, 0, s>>>(fd, cols, pairs, rdir, rdir_ptr); note_launches(1); }
 }
 
 #define INST(T)                                                                                  \

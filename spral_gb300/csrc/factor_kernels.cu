@@ -819,48 +819,52 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
                      int max_rows, int max_trail_rows, int max_trail_cols, bool action,
                      double u, double small, cudaStream_t s) {
   if (nf <= 0) return;
-  k_app_diag<T><<<nf, 32, 0, s>>>(fd, st, fronts, step, action, small);
+  { k_app_diag<T><<<nf, 32, 0, s>>>(fd, st, fronts, step, action, small); note_launches(1); }
   {
     int pcols = step * kBlk;  // columns of L to the left (upper bound on p)
     int gx = std::max(1, std::min(cdiv(pcols, 8), 64));
-    if (pcols > 0) k_app_rowperm<T><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts);
+    if (pcols > 0) { k_app_rowperm<T><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts); note_launches(1); }
   }
   int gx = std::max(1, cdiv(max_rows, kApplyRows));
-  k_app_apply<T><<<dim3(gx, nf), kApplyRows, 0, s>>>(fd, st, fronts, u, small);
-  k_app_fixup<T><<<dim3(gx, nf), kApplyRows, 0, s>>>(fd, st, fronts);
+  { k_app_apply<T><<<dim3(gx, nf), kApplyRows, 0, s>>>(fd, st, fronts, u, small); note_launches(1); }
+  { k_app_fixup<T><<<dim3(gx, nf), kApplyRows, 0, s>>>(fd, st, fronts); note_launches(1); }
   // tile estimate assumes no failed columns so far; after failures the
   // trailing region is wider and the kernel's grid-stride loop covers it, so
   // the launch is never skipped
   int tr = std::max(0, cdiv(max_trail_rows, kGemmTile)), tc = std::max(0, cdiv(max_trail_cols, kGemmTile));
   int tiles = tc * tr - tc * (tc - 1) / 2;
   launch_syrk_panel<T>(fd, st, fronts, nf, std::max(tiles, 1), s);
-  k_app_swap_gather<T><<<dim3(64, nf), 256, 0, s>>>(fd, st, fronts);
-  k_app_swap_scatter<T><<<dim3(64, nf), 256, 0, s>>>(fd, st, fronts);
+  { k_app_swap_gather<T><<<dim3(64, nf), 256, 0, s>>>(fd, st, fronts); note_launches(1); }
+  { k_app_swap_scatter<T><<<dim3(64, nf), 256, 0, s>>>(fd, st, fronts); note_launches(1); }
 }
 
 template <typename T>
 void launch_app_finish(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf,
                        cudaStream_t s) {
   if (nf <= 0) return;
-  k_app_finish<T><<<cdiv(nf, 128), 128, 0, s>>>(fd, st, fronts, nf);
+  { k_app_finish<T><<<cdiv(nf, 128), 128, 0, s>>>(fd, st, fronts, nf); note_launches(1); }
 }
 
 template <typename T>
 void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
                 double u, double small, bool all_fronts, cudaStream_t s) {
   if (nf <= 0) return;
-  k_tpp<T><<<nf, kTppThreads, 0, s>>>(fd, st, fronts, action, u, small, all_fronts);
+  { k_tpp<T><<<nf, kTppThreads, 0, s>>>(fd, st, fronts, action, u, small, all_fronts); note_launches(1); }
 }
 
 template <typename T>
-void launch_contrib(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
-                    int max_n, cudaStream_t s) {
+void launch_calc_ld(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
+                    cudaStream_t s) {
   if (nf <= 0 || max_cm <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_cm, 128), 256));
-  k_calc_ld<T><<<dim3(gx, nf), 128, 0, s>>>(fd, st, fronts);
+  { k_calc_ld<T><<<dim3(gx, nf), 128, 0, s>>>(fd, st, fronts); note_launches(1); }
+}
+template <typename T>
+void launch_contrib_gemm(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
+                         cudaStream_t s) {
+  if (nf <= 0 || max_cm <= 0) return;
   int t = cdiv(max_cm, kGemmTile);
   launch_syrk_contrib<T>(fd, st, fronts, nf, t * (t + 1) / 2, s);
-  (void)max_n;
 }
 
 template <typename T>
@@ -868,7 +872,7 @@ void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* front
                   int max_n, Stats* stats, cudaStream_t s) {
   if (nf <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_n, 256), 64));
-  k_stats<T><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts, stats);
+  { k_stats<T><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts, stats); note_launches(1); }
 }
 
 #define INST(T)                                                                                 \
@@ -877,8 +881,9 @@ void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* front
   template void launch_app_finish<T>(FrontDesc<T>*, FrontState*, const int*, int, cudaStream_t); \
   template void launch_tpp<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double, double, \
                               bool, cudaStream_t);                                              \
-  template void launch_contrib<T>(FrontDesc<T>*, FrontState*, const int*, int, int, int,         \
-                                  cudaStream_t);                                                \
+  template void launch_calc_ld<T>(FrontDesc<T>*, FrontState*, const int*, int, int, cudaStream_t); \
+  template void launch_contrib_gemm<T>(FrontDesc<T>*, FrontState*, const int*, int, int,        \
+                                       cudaStream_t);                                           \
   template void launch_stats<T>(const FrontDesc<T>*, const FrontState*, const int*, int, int,    \
                                 Stats*, cudaStream_t);
 INST(double)

@@ -106,13 +106,13 @@ template <typename T>
 void launch_syrk_panel(FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
                        int max_tiles, cudaStream_t s) {
   int gx = max_tiles < 1 ? 1 : (max_tiles > 4096 ? 4096 : max_tiles);
-  k_syrk<T, 0><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts);
+  { k_syrk<T, 0><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts); note_launches(1); }
 }
 template <typename T>
 void launch_syrk_contrib(FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
                          int max_tiles, cudaStream_t s) {
   int gx = max_tiles < 1 ? 1 : (max_tiles > 4096 ? 4096 : max_tiles);
-  k_syrk<T, 1><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts);
+  { k_syrk<T, 1><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts); note_launches(1); }
 }
 
 template void launch_syrk_panel<double>(FrontDesc<double>*, const FrontState*, const int*, int, int, cudaStream_t);

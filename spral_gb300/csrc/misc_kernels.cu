@@ -96,7 +96,7 @@ void launch_zero_fronts(FrontDesc<T>* fd, const int* fronts, int nf, int max_ele
                         cudaStream_t s) {
   if (nf <= 0) return;
   int gx = std::max(1, std::min((max_elems + 1023) / 1024, 256));
-  k_zero_fronts<T><<<dim3(gx, nf), 256, 0, s>>>(fd, fronts);
+  { k_zero_fronts<T><<<dim3(gx, nf), 256, 0, s>>>(fd, fronts); note_launches(1); }
 }
 template void launch_zero_fronts<double>(FrontDesc<double>*, const int*, int, int, cudaStream_t);
 template void launch_zero_fronts<float>(FrontDesc<float>*, const int*, int, int, cudaStream_t);
@@ -105,13 +105,13 @@ void launch_spmv_resid(const int64_t* aptr, const int* acol, const int64_t* asrc
                        const double* aval, int n, const double* x, const double* b, double* r,
                        int nrhs, int ld, cudaStream_t s) {
   int blocks = std::max(1, std::min((n + 7) / 8, 4096));
-  k_spmv_resid<<<blocks, 256, 0, s>>>(aptr, acol, asrc, aval, n, x, b, r, nrhs, ld);
+  { k_spmv_resid<<<blocks, 256, 0, s>>>(aptr, acol, asrc, aval, n, x, b, r, nrhs, ld); note_launches(1); }
 }
 
 void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s) {
   int64_t total = (int64_t)n * nrhs;
   int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 4096));
-  k_axpy<<<blocks, 256, 0, s>>>(total, n, ld, x, d);
+  { k_axpy<<<blocks, 256, 0, s>>>(total, n, ld, x, d); note_launches(1); }
 }
 
 // work must hold 1 + 3*nrhs + nrhs doubles; the result (per rhs) is written
@@ -122,8 +122,51 @@ void launch_bwd_err(const int64_t* aptr, const int64_t* asrc, const double* aval
   double* acc = work + nrhs;
   cudaMemsetAsync(acc, 0, (1 + 3 * kSolveRhs) * sizeof(double), s);
   int blocks = std::max(1, std::min((n + 255) / 256, 1024));
-  k_norms<<<blocks, 256, 0, s>>>(aptr, asrc, aval, n, x, r, b, nrhs, ld, acc);
-  k_bwd_finish<<<1, 32, 0, s>>>(acc, nrhs, work);
+  { k_norms<<<blocks, 256, 0, s>>>(aptr, asrc, aval, n, x, r, b, nrhs, ld, acc); note_launches(1); }
+  { k_bwd_finish<<<1, 32, 0, s>>>(acc, nrhs, work); note_launches(1); }
 }
 
+}  // namespace ssids300
+
+// FP64 FMA throughput probe: independent DFMA chains per thread, no memory
+// traffic; used to state the FP64 roofline of the FP64 path (the driver's
+// measured peaks cover HBM and bf16 tensor only).
+namespace ssids300 {
+namespace {
+__global__ void k_dfma_probe(double* out, int iters, double seed) {
+  double a0 = seed + threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3;
+  double a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+  const double m = 0.999999, c = 1e-7;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+    a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+  }
+  double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 12345.678) out[0] = s;  // keep the chains live
+}
+}  // namespace
+
+double fp64_peak_tflops(int device) {
+  cudaSetDevice(device);
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  double* out = nullptr;
+  cudaMalloc(&out, sizeof(double));
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_dfma_probe<<<blocks, threads>>>(out, 64, 1.0);
+  cudaEventRecord(e0);
+  k_dfma_probe<<<blocks, threads>>>(out, iters, 1.0);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  double flops = 2.0 * 8.0 * (double)iters * blocks * threads;
+  return ms > 0 ? flops / (ms * 1e-3) / 1e12 : 0.0;
+}
 }  // namespace ssids300

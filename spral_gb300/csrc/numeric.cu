@@ -14,6 +14,7 @@
 //   * factors stay resident for repeated solves and same-pattern
 //     refactorisation; solves take many right-hand sides at once.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -31,6 +32,10 @@ struct CudaFail {
   cudaError_t err;
   int line;
 };
+
+static std::atomic<long long> g_launches{0};
+void note_launches(int k) { g_launches += k; }
+double fp64_peak_tflops(int device);
 
 #define CK(x)                                              \
   do {                                                     \
@@ -318,10 +323,15 @@ struct NumericBase {
   int precision = 0;
   spral_ssids_thread_stats stats{};
   double timing[5] = {0, 0, 0, 0, 0};
+  bool profile = false;
+  double prof_ms = 0, prof_flops = 0;
+  long long prof_launches = 0;
   virtual int factor(const double* aval, bool aval_on_device, const double* scaling,
                      cudaStream_t user_stream) = 0;
   virtual int solve_dev(int job, int nrhs, double* x, int ldx, cudaStream_t s) = 0;
   virtual int solve_refined(int nrhs, double* x_host, int ldx, int* iters) = 0;
+  virtual int solve_refined_dev(int nrhs, const double* b, double* x, int ld, int* iters,
+                                double* bwd) = 0;
   virtual void enquire(int* piv, double* d) = 0;
   virtual void alter(const double* d) = 0;
   virtual Symbolic* symbolic() = 0;
@@ -365,6 +375,7 @@ struct Numeric : NumericBase {
   DevBuf<double> xloc, xorig, xbuf, rbuf, dbuf, bbuf, nbuf;
   const double* cur_aval = nullptr;  // device values of the last factor
   double last_bwd_err = 0.0;
+  std::vector<cudaEvent_t> pev;
 
   explicit Numeric(Symbolic* s) : S(s) {
     CK(cudaSetDevice(S->device));
@@ -386,6 +397,7 @@ struct Numeric : NumericBase {
     farena.min_chunk = std::max<size_t>(est * sizeof(T) * 11 / 10, size_t(16) << 20);
   }
   ~Numeric() override {
+    for (auto e : pev) cudaEventDestroy(e);
     cudaFree(d_fd); cudaFree(d_st); cudaFree(d_stats); cudaFree(d_dwork);
     cudaFree(d_sn); cudaFree(d_children);
     for (auto& e : ev) cudaEventDestroy(e);
@@ -418,6 +430,13 @@ struct Numeric : NumericBase {
     farena.rewind();
     darena.rewind();
     iarena.rewind();
+    if (profile && (int)pev.size() < 2 * S->nlev) {
+      for (size_t i = pev.size(); i < (size_t)2 * S->nlev; ++i) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        pev.push_back(e);
+      }
+    }
     CK(cudaMemsetAsync(d_st, 0, nn * sizeof(FrontState), s));
     CK(cudaMemsetAsync(d_stats, 0, sizeof(Stats), s));
     lvl_max_m.assign(S->nlev, 0);
@@ -519,7 +538,10 @@ struct Numeric : NumericBase {
       launch_app_finish<T>(d_fd, d_st, fr, nf, s);
       const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
       launch_tpp<T>(d_fd, d_st, fr, nf, co.action, co.u, co.small, tpp_all, s);
-      launch_contrib<T>(d_fd, d_st, fr, nf, max_cm, max_n, s);
+      launch_calc_ld<T>(d_fd, d_st, fr, nf, max_cm, s);
+      if (profile) CK(cudaEventRecord(pev[2 * l], s));
+      launch_contrib_gemm<T>(d_fd, d_st, fr, nf, max_cm, s);
+      if (profile) CK(cudaEventRecord(pev[2 * l + 1], s));
       launch_stats<T>(d_fd, d_st, fr, nf, max_n, d_stats, s);
       CK(cudaMemcpyAsync(hst.data() + f0, d_st + f0, nf * sizeof(FrontState),
                          cudaMemcpyDeviceToHost, s));
@@ -536,6 +558,16 @@ struct Numeric : NumericBase {
         bool tpp_ran = tpp_all || (m_[f] == n_[f]);
         if (!use_app) nfp += n_[f] - nelim_[f];
         else if (tpp_ran && napp_[f] < n_[f]) nsp += n_[f] - nelim_[f];
+      }
+      if (profile) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, pev[2 * l], pev[2 * l + 1]));
+        double fl = 0;
+        for (int f = f0; f < f1; ++f) {
+          const double cm = hfd[f].cm;
+          fl += (double)nelim_[f] * cm * (cm + 1.0);
+        }
+        if (fl > 0) { prof_ms += ms; prof_flops += fl; prof_launches += 1; }
       }
       if (singular) { stats.flag = -5; return stats.flag; }
       if (bad) { stats.flag = -51; return stats.flag; }
@@ -663,6 +695,26 @@ struct Numeric : NumericBase {
     }
     CK(cudaStreamSynchronize(s));
     if (iters) *iters = itmax;
+    return 0;
+  }
+
+  // full solve + refinement with b and x in device memory (n x nrhs, ld)
+  int solve_refined_dev(int nrhs, const double* b, double* x, int ld, int* iters,
+                        double* bwd) override {
+    int itmax = 0;
+    double worst = 0;
+    for (int r0 = 0; r0 < nrhs; r0 += kSolveRhs) {
+      const int q = std::min(kSolveRhs, nrhs - r0);
+      double* xp = x + (size_t)r0 * ld;
+      const double* bp = b + (size_t)r0 * ld;
+      CK(cudaMemcpy2DAsync(xp, ld * sizeof(double), bp, ld * sizeof(double),
+                           S->n * sizeof(double), q, cudaMemcpyDeviceToDevice, stream));
+      solve_dev(0, q, xp, ld, nullptr);
+      itmax = std::max(itmax, refine_dev(q, xp, bp, ld));
+      worst = std::max(worst, last_bwd_err);
+    }
+    if (iters) *iters = itmax;
+    if (bwd) *bwd = worst;
     return 0;
   }
 
@@ -948,6 +1000,49 @@ int spral_ssids_gpu_last_timing(const void* numeric, double* out) {
   const NumericBase* N = static_cast<const NumericBase*>(numeric);
   for (int i = 0; i < 5; ++i) out[i] = N->timing[i];
   return 5;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+/* Profiling and bench support (no reference counterpart). */
+long long spral_ssids_gpu_launch_count(void) { return ssids300::g_launches.load(); }
+
+void spral_ssids_gpu_set_profiling(void* numeric, int on) {
+  auto* N = static_cast<ssids300::NumericBase*>(numeric);
+  N->profile = on != 0;
+  N->prof_ms = 0;
+  N->prof_flops = 0;
+  N->prof_launches = 0;
+}
+
+/* out[0] = contribution-GEMM time (ms) summed over profiled factors,
+ * out[1] = its algorithmic flops, out[2] = number of timed launches. */
+void spral_ssids_gpu_profile_stats(const void* numeric, double* out) {
+  auto* N = static_cast<const ssids300::NumericBase*>(numeric);
+  out[0] = N->prof_ms;
+  out[1] = N->prof_flops;
+  out[2] = (double)N->prof_launches;
+}
+
+int spral_ssids_gpu_solve_refined_dev(void* numeric, int nrhs, const double* b_dev, double* x_dev,
+                                      int ld, int* iters, double* bwd_err) {
+  auto* N = static_cast<ssids300::NumericBase*>(numeric);
+  try {
+    return N->solve_refined_dev(nrhs, b_dev, x_dev, ld, iters, bwd_err);
+  } catch (ssids300::CudaFail const& e) {
+    return map_cuda_error(e, nullptr);
+  }
+}
+
+double spral_ssids_gpu_fp64_peak_tflops(int device) {
+  try {
+    return ssids300::fp64_peak_tflops(device);
+  } catch (ssids300::CudaFail const& e) {
+    map_cuda_error(e, nullptr);
+    return 0.0;
+  }
 }
 
 }  // extern "C"

@@ -255,7 +255,7 @@ template <typename T>
 void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const int* children,
                        const double* x, int ldx, int nrhs, cudaStream_t s) {
   if (nn <= 0) return;
-  k_fwd_gather<T><<<nn, 256, 0, s>>>(sn, nodes, children, x, ldx, nrhs);
+  { k_fwd_gather<T><<<nn, 256, 0, s>>>(sn, nodes, children, x, ldx, nrhs); note_launches(1); }
 }
 
 template <typename T>
@@ -264,11 +264,11 @@ void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_
   if (nn <= 0) return;
   const int steps = cdiv(max_nelim, SB);
   for (int st = 0; st < steps; ++st) {
-    k_fwd_diag<T><<<nn, 256, 0, s>>>(sn, nodes, st, nrhs);
+    { k_fwd_diag<T><<<nn, 256, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
     int rows = max_m - st * SB;  // upper bound; the kernel derives the exact range
     if (rows > 0) {
       int gx = std::max(1, std::min(cdiv(rows, 256), 128));
-      k_fwd_update<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, st, nrhs);
+      { k_fwd_update<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
     }
   }
 }
@@ -278,7 +278,7 @@ void launch_fwd_scatter(const SolveNode<T>* sn, const int* nodes, int nn, double
                         int nrhs, int max_nelim, cudaStream_t s) {
   if (nn <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_nelim * nrhs, 256), 64));
-  k_fwd_scatter<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs);
+  { k_fwd_scatter<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs); note_launches(1); }
 }
 
 template <typename T>
@@ -286,21 +286,21 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
                 int max_m, int max_nelim, bool do_diag, bool do_bwd, cudaStream_t s) {
   if (nn <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_m * nrhs, 256), 64));
-  k_bwd_gather<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, do_diag, do_bwd);
+  { k_bwd_gather<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, do_diag, do_bwd); note_launches(1); }
   if (do_bwd) {
     int gw = std::max(1, std::min(cdiv(max_nelim, 8), 128));
-    k_bwd_l21<T><<<dim3(gw, nn), 256, 0, s>>>(sn, nodes, nrhs);
+    { k_bwd_l21<T><<<dim3(gw, nn), 256, 0, s>>>(sn, nodes, nrhs); note_launches(1); }
     const int steps = cdiv(max_nelim, SB);
     for (int st = steps - 1; st >= 0; --st) {
-      k_bwd_diag<T><<<nn, 256, 0, s>>>(sn, nodes, st, nrhs);
+      { k_bwd_diag<T><<<nn, 256, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
       if (st > 0) {
         int gu = std::max(1, std::min(cdiv(st * SB, 8), 128));
-        k_bwd_update<T><<<dim3(gu, nn), 256, 0, s>>>(sn, nodes, st, nrhs);
+        { k_bwd_update<T><<<dim3(gu, nn), 256, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
       }
     }
   }
   int gs = std::max(1, std::min(cdiv(max_nelim * nrhs, 256), 64));
-  k_fwd_scatter<T><<<dim3(gs, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs);
+  { k_fwd_scatter<T><<<dim3(gs, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs); note_launches(1); }
 }
 
 #define INST(T)                                                                                \

@@ -61,6 +61,9 @@ struct Stats {  // device-side reduction target (integers only -> deterministic)
   long long num_factor, num_flops;
 };
 
+// Count of kernels launched by this library (reported by the benchmark).
+void note_launches(int k);
+
 // ---------------- launchers (defined in the kernel .cu files) --------------
 // assembly (assemble_kernels.cu)
 template <typename T>
@@ -88,8 +91,11 @@ template <typename T>
 void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
                 double u, double small, bool root_only_or_all, cudaStream_t s);
 template <typename T>
-void launch_contrib(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
-                    int max_n, cudaStream_t s);
+void launch_calc_ld(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
+                    cudaStream_t s);
+template <typename T>
+void launch_contrib_gemm(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
+                         cudaStream_t s);
 template <typename T>
 void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
                   int max_n, Stats* stats, cudaStream_t s);
