@@ -208,13 +208,10 @@ def run_gpu(args):
 
         def step():
             fk.refactor_dev(aval_d.data_ptr())
-            if mixed:
-                L.spral_ssids_gpu_solve_refined_dev(fk.num, nrhs, ctypes.c_void_p(b_d.data_ptr()),
-                                                    ctypes.c_void_p(x_d.data_ptr()), n,
-                                                    ctypes.byref(it), ctypes.byref(bw))
-            else:
-                x_d.copy_(b_d)
-                fk.solve_dev(x_d.data_ptr(), nrhs, n, job=0)
+            # full solve plus FP64 refinement until bwd err <= 5e-15 (both paths)
+            L.spral_ssids_gpu_solve_refined_dev(fk.num, nrhs, ctypes.c_void_p(b_d.data_ptr()),
+                                                ctypes.c_void_p(x_d.data_ptr()), n,
+                                                ctypes.byref(it), ctypes.byref(bw))
 
         for _ in range(args.warmup):
             step()
@@ -248,10 +245,10 @@ def run_gpu(args):
         bwd = float(M.scaled_bwd_error(ptr, row, val, xu, b).max())
         return ms, per, launches, clocks, bwd, it.value
 
-    opts64 = ssids.Options(precision=ssids.PRECISION_FP64)
+    opts64 = ssids.Options(precision=ssids.PRECISION_FP64, max_refine=10, refine_tol=5e-15)
     fk = ssids.Fkeep(ak, val, opts64)
     inform = fk.inform
-    ms, per, launches, clocks, bwd, _ = measure(fk, mixed=False)
+    ms, per, launches, clocks, bwd, fp64_iters = measure(fk, mixed=False)
     value = world * 1000.0 / ms
     factor_tflops = inform.num_flops / (fk.timing()[0] * 1e-3) / 1e12
 
@@ -288,9 +285,9 @@ def run_gpu(args):
                                                        val.ctypes.data_as(ctypes.c_void_p), None,
                                                        None, ctypes.byref(copts), ctypes.byref(st))
         xw = xh.copy(order="F")
-        L.spral_ssids_gpu_subtree_solve_fwd_dbl(False, num, nrhs, xw.ctypes.data_as(ctypes.c_void_p), n)
-        L.spral_ssids_gpu_subtree_solve_diag_bwd_dbl(False, num, nrhs,
-                                                     xw.ctypes.data_as(ctypes.c_void_p), n)
+        its = ctypes.c_int(0)
+        L.spral_ssids_gpu_solve_refined(num, nrhs, xw.ctypes.data_as(ctypes.c_void_p), n,
+                                        ctypes.byref(its))
         L.spral_ssids_gpu_destroy_num_subtree_dbl(False, num)
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
@@ -302,13 +299,13 @@ def run_gpu(args):
     e2e = {"value": world * 1000.0 / e2e_ms, "unit": "solves/s",
            "h2d_bytes_per_step": int(val.nbytes + n * nrhs * 8),
            "d2h_bytes_per_step": int(n * nrhs * 8),
-           "path": "spral_ssids_gpu_create_num_subtree_dbl + subtree_solve_fwd/diag_bwd (host "
-                   "aval and x)"}
+           "path": "spral_ssids_gpu_create_num_subtree_dbl + spral_ssids_gpu_solve_refined "
+                   "(host aval and x, FP64 factors)"}
 
     mixed = None
     if not args.no_mixed:
         fm = ssids.Fkeep(ak, val, ssids.Options(precision=ssids.PRECISION_MIXED, max_refine=20,
-                                                 refine_tol=1e-15))
+                                                 refine_tol=5e-15))
         mms, mper, mlaunch, _, mbwd, mit = measure(fm, mixed=True)
         mixed = {"value": world * 1000.0 / mms, "unit": "solves/s", "ms_per_step": mms,
                  "bwd_err": mbwd, "refine_iters": mit, "num_neg": fm.inform.num_neg,
@@ -338,6 +335,7 @@ def run_gpu(args):
                 "config": config(args, ak, {"bwd_err": bwd, "num_neg": inform.num_neg,
                                             "num_neg_exact": neg_exact,
                                             "num_delay": inform.num_delay,
+                                            "refine_iters": fp64_iters,
                                             "num_flops": inform.num_flops}),
                 "factor_tflops": factor_tflops,
                 "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99)),

@@ -163,6 +163,10 @@ long long spral_ssids_gpu_launch_count(void);
 void spral_ssids_gpu_set_profiling(void* numeric, int on);
 void spral_ssids_gpu_profile_stats(const void* numeric, double* out);
 double spral_ssids_gpu_fp64_peak_tflops(int device);
+void spral_ssids_gpu_phase_times(const void* numeric, double* ms, long long* counts);
+/* Evaluates the device reciprocal used on the pivot-decision path for n
+ * values (device pointers), for accuracy tests against IEEE division. */
+int spral_ssids_gpu_recip_probe(const double* x_dev, double* y_dev, int n);
 
 /* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
 int spral_ssids_gpu_device_count(void);

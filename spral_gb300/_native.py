@@ -91,3 +91,5 @@ def _declare(L):
     f("spral_ssids_gpu_set_profiling", None, P, I)
     f("spral_ssids_gpu_profile_stats", None, P, P)
     f("spral_ssids_gpu_fp64_peak_tflops", D, I)
+    f("spral_ssids_gpu_phase_times", None, P, P, P)
+    f("spral_ssids_gpu_recip_probe", I, P, P, I)

@@ -6,16 +6,17 @@
 //                   (semantics of block_ldlt, src/ssids/cpu/kernels/
 //                   block_ldlt.hxx:290-413), FP64 arithmetic, writes L11, D^{-1}
 //                   and the local permutation
-//   k_app_rowperm   applies the block permutation to the eliminated L rows
 //   k_app_apply     rows below: X = A21 L11^{-T}, L21 = X D^{-1} and the
 //                   a-posteriori test |l| <= 1/u (apply_pivot/check_threshold,
-//                   ldlt_app.cxx:316-436); X (= L21 D) is kept for the update
+//                   ldlt_app.cxx:316-436); X (= L21 D) is kept for the update;
+//                   extra CTAs apply the block permutation to the eliminated
+//                   L rows
 //   k_app_fixup     Column::adjust (ldlt_app.cxx:112-130) and, for failed
 //                   columns, the restore-and-update of restore_if_required +
 //                   update, computed as X_f L_ff^T (rows below) and
 //                   L_ff D_f L_ff^T (diagonal block)
 //   k_syrk (panel)  trailing update of the candidate columns (gemm_kernels.cu)
-//   k_app_swap_*    failed columns are moved to the end of the APP range
+//   k_app_swap      failed columns are moved to the end of the APP range
 // After ceil(n/32) steps k_app_finish records nelim; k_tpp finishes failed
 // columns with threshold partial pivoting (ldlt_tpp.cxx:166-270) where the
 // reference does (root fronts or failed_pivot_method = tpp); k_calc_ld and
@@ -32,6 +33,35 @@ namespace {
 
 __device__ __forceinline__ double dinf() { return __longlong_as_double(0x7ff0000000000000LL); }
 
+}  // namespace
+
+// Reciprocal by Newton-Raphson iteration y <- y + y (1 - x y) from an FP32
+// seed (each step squares the relative error: 2^-23 -> 2^-46 -> 2^-92), so
+// the result is within one ulp of 1/x.  Two FP64 FMA pairs replace the long
+// dependent sequence of a correctly rounded FP64 division, which matters on
+// the serial path of the pivot decisions.  Arguments whose magnitude is
+// outside [2^-100, 2^100] (or zero/Inf/NaN) use ordinary division.
+__device__ __forceinline__ double recip_nr(double x) {
+  const int e = (int)((__double_as_longlong(x) >> 52) & 0x7ff);
+  if (e < 1023 - 100 || e > 1023 + 100) return 1.0 / x;
+  double y = (double)__frcp_rn((float)x);
+  double r = fma(-x, y, 1.0);
+  y = fma(y, r, y);
+  r = fma(-x, y, 1.0);
+  return fma(y, r, y);
+}
+
+__global__ void k_recip_probe(const double* x, double* y, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = recip_nr(x[i]);
+}
+
+void launch_recip_probe(const double* x, double* y, int n, cudaStream_t s) {
+  k_recip_probe<<<(n + 255) / 256, 256, 0, s>>>(x, y, n);
+}
+
+namespace {
+
 // read symmetric entry (r, c) of a lower-stored front (both < n or r >= n > c)
 template <typename T>
 __device__ __forceinline__ double sym_at(const T* L, int ld, int r, int c) {
@@ -39,212 +69,257 @@ __device__ __forceinline__ double sym_at(const T* L, int ld, int r, int c) {
 }
 
 // ------------------------------------------------------------------------
-// k_app_diag: advance state, factor the diagonal block with complete pivoting
+// k_app_diag: advance state, factor the diagonal block with complete pivoting.
+// 128 threads; thread t owns the 8 entries (rows 8*(t/32)+k, column t%32) of
+// the block, stored full-symmetric.  Pivoting never moves data: a logical <->
+// physical index map is updated instead, so each pivot costs one argmax
+// (warp shuffles + 4 partials), one parallel rank-1/2 update and three
+// barriers.  The block and its updates are in the factor precision T; pivot
+// selection values, D^{-1} and 2x2 inversions are FP64.
 // ------------------------------------------------------------------------
+constexpr int kDiagThreads = 128;
+
 template <typename T>
-__global__ void __launch_bounds__(32) k_app_diag(FrontDesc<T>* fds, FrontState* sts,
-                                                 const int* fronts, int step, bool action,
-                                                 double small) {
+__global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, FrontState* sts,
+                                                           const int* fronts, int step,
+                                                           bool action, double small) {
   const int f = fronts[blockIdx.x];
   FrontDesc<T> fd = fds[f];
   FrontState* st = &sts[f];
-  const int lane = threadIdx.x;
-  __shared__ double blk[kBlk][kBlk + 1];  // blk[c][r], full symmetric
-  __shared__ double wv[2][kBlk];          // unscaled pivot columns
-  __shared__ double lv[2][kBlk];          // scaled pivot columns
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int C = lane;          // owned physical column
+  const int R0 = warp * 8;     // owned physical rows R0..R0+7
+  __shared__ T blk[kBlk][kBlk + 1];  // blk[C][R] = A(R, C), physical indices
   __shared__ double dd[2 * kBlk + 2];
-  __shared__ int lp[kBlk];
-  __shared__ int s_piv[3];  // pivsiz, idx1, idx2
-  __shared__ double s_det[2];
+  __shared__ int map[kBlk], inv[kBlk];  // logical -> physical, physical -> logical
+  __shared__ double rdiag[kBlk];  // reciprocal of each physical diagonal entry
+  __shared__ long long pkey[4];
+  __shared__ int pi_[4], pj_[4];
+  __shared__ int s_piv[3];
+  __shared__ int s_sw[4];
+  __shared__ double s_d[4];
+  __shared__ int s_state[2];
 
-  int p, end;
-  if (step == 0) {
-    p = 0;
-    end = fd.n;
-  } else {
-    p = st->p;
-    end = st->end;
-    if (st->bs > 0) {
-      p += st->npass;
-      end -= st->bs - st->npass;
+  if (tid == 0) {
+    int p, end;
+    if (step == 0) {
+      p = 0;
+      end = fd.n;
+    } else {
+      p = st->p;
+      end = st->end;
+      if (st->bs > 0) {
+        p += st->npass;
+        end -= st->bs - st->npass;
+      }
     }
-  }
-  int bs = min(kBlk, end - p);
-  if (bs < 0) bs = 0;
-  __syncwarp();
-  if (lane == 0) {
+    int bs = min(kBlk, end - p);
+    if (bs < 0) bs = 0;
     st->p = p;
     st->end = end;
     st->bs = bs;
     st->npass_raw = bs;
     st->npass = bs;
     st->step = step;
+    s_state[0] = p;
+    s_state[1] = bs;
   }
+  __syncthreads();
+  const int p = s_state[0], bs = s_state[1];
   if (bs == 0) return;
-
-  // load block (lower storage) as full symmetric
-  for (int c = 0; c < bs; ++c) {
-    int r = lane;
-    if (r < bs) blk[c][r] = sym_at(fd.L, fd.ld, p + r, p + c);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int R = R0 + k;
+    blk[C][R] = (R < bs && C < bs) ? (T)sym_at(fd.L, fd.ld, p + R, p + C) : T(0);
   }
-  lp[lane] = lane;
-  for (int i = lane; i < 2 * kBlk + 2; i += 32) dd[i] = 0.0;
-  __syncwarp();
+  if (tid < kBlk) { map[tid] = tid; inv[tid] = tid; }
+  if (tid < 2 * kBlk + 2) dd[tid] = 0.0;
+  __syncthreads();
 
+  // logical indices of the owned column / rows, cached in registers
+  int lj = C;
+  int li[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) li[k] = R0 + k;
+  const bool colok = C < bs;
   bool singular = false;
   for (int q = 0; q < bs;) {
-    // argmax over lower triangle of the active block (first in column order)
-    double best = -1.0;
-    int br = -1;
-    const int c = lane;
-    if (c >= q && c < bs) {
-      for (int r = c; r < bs; ++r) {
-        double v = fabs(blk[c][r]);
-        if (v > best) { best = v; br = r; }
+    // ---- argmax of |A| over the logical lower triangle of columns >= q.
+    // Key = magnitude bits with the low 10 mantissa bits replaced by the
+    // (inverted) logical position j*32+i, so one unsigned max gives the
+    // largest entry and, among entries equal to 2^-42 relative, the first in
+    // logical column-major order (the reference's scan order).
+    if (colok && C >= R0 && C < R0 + 8 && lj >= q) rdiag[C] = recip_nr((double)blk[C][C]);
+    unsigned long long bk = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int R = R0 + k;
+      if (colok && R < bs && lj >= q && li[k] >= lj) {
+        const unsigned long long mag =
+            (unsigned long long)__double_as_longlong((double)blk[C][R]) & 0x7fffffffffffffffULL;
+        const unsigned long long key =
+            ((mag | 0x3ffULL) ^ 0x3ffULL) | (unsigned long long)(1023 - (lj * 32 + li[k])) |
+            (1ULL << 63);  // marks a valid candidate
+        bk = key > bk ? key : bk;
       }
     }
-    int bc = (br >= 0) ? c : 1 << 20;
     for (int off = 16; off > 0; off >>= 1) {
-      double ob = __shfl_xor_sync(0xffffffffu, best, off);
-      int obr = __shfl_xor_sync(0xffffffffu, br, off);
-      int obc = __shfl_xor_sync(0xffffffffu, bc, off);
-      if (ob > best || (ob == best && obc < bc)) { best = ob; br = obr; bc = obc; }
+      const unsigned long long ok = __shfl_xor_sync(0xffffffffu, bk, off);
+      bk = ok > bk ? ok : bk;
     }
-    if (best < small) {
-      if (!action) { singular = true; break; }
-      // remaining columns are zero pivots
-      for (int cc = q; cc < bs; ++cc) {
-        if (lane >= cc && lane < bs) blk[cc][lane] = 0.0;
-        if (lane == 0) { dd[2 * cc] = 0.0; dd[2 * cc + 1] = 0.0; }
+    if (lane == 0) pkey[warp] = (long long)bk;
+    __syncthreads();
+    if (tid == 0) {
+      for (int w = 1; w < 4; ++w) {
+        const unsigned long long ok = (unsigned long long)pkey[w];
+        bk = ok > bk ? ok : bk;
       }
-      __syncwarp();
-      break;
-    }
-    if (lane == 0) {
-      int t = br, mm = bc;
-      int pivsiz, i1, i2 = -1;
-      if (t == mm) {
-        pivsiz = 1; i1 = t;
+      const int pos = 1023 - (int)(bk & 0x3ffULL);
+      const int bj = pos >> 5, bi = pos & 31;  // logical column, row
+      const double bv = __longlong_as_double((long long)((bk & 0x7fffffffffffffffULL) | 0x3ffULL));
+      int pivsiz;
+      if (bv < small) {
+        pivsiz = 0;
       } else {
-        double a11 = blk[mm][mm], a22 = blk[t][t], a21 = blk[mm][t];
-        double detscale = 1.0 / fabs(a21);
-        double detpiv = (a11 * detscale) * a22 - fabs(a21);
-        if (fabs(detpiv) >= fabs(a21) / 2) {
-          pivsiz = 2; i1 = mm; i2 = t;
-          s_det[0] = detscale; s_det[1] = detpiv;
-        } else if (fabs(a11) > fabs(a22)) {
-          pivsiz = 1; i1 = mm;
-        } else {
+        const int t = bi, mm = bj;
+        int i1, i2 = -1;
+        if (t == mm) {
           pivsiz = 1; i1 = t;
+        } else {
+          const double a11 = (double)blk[map[mm]][map[mm]], a22 = (double)blk[map[t]][map[t]];
+          const double a21 = (double)blk[map[mm]][map[t]];
+          const double detscale = recip_nr(fabs(a21));
+          const double detpiv = (a11 * detscale) * a22 - fabs(a21);
+          if (fabs(detpiv) >= fabs(a21) / 2) {
+            pivsiz = 2; i1 = mm; i2 = t;
+            const double rdet = recip_nr(detpiv);
+            s_d[0] = (a22 * detscale) * rdet;   // d11 (logical q <- mm)
+            s_d[1] = (-a21 * detscale) * rdet;  // d21
+            s_d[2] = (a11 * detscale) * rdet;   // d22 (logical q+1 <- t)
+          } else if (fabs(a11) > fabs(a22)) {
+            pivsiz = 1; i1 = mm;
+          } else {
+            pivsiz = 1; i1 = t;
+          }
+        }
+        // logical swaps q <-> i1, then q+1 <-> i2 (i2 > i1 >= q); the four
+        // physical indices whose logical position changed are published
+        int sw[4] = {-1, -1, -1, -1};
+        {
+          const int a = map[q], b = map[i1];
+          map[q] = b; map[i1] = a; inv[b] = q; inv[a] = i1;
+          sw[0] = a; sw[1] = b;
+        }
+        if (pivsiz == 2) {
+          const int a = map[q + 1], b = map[i2];
+          map[q + 1] = b; map[i2] = a; inv[b] = q + 1; inv[a] = i2;
+          sw[2] = a; sw[3] = b;
+        }
+        for (int z = 0; z < 4; ++z) s_sw[z] = sw[z];
+        if (pivsiz == 1) {
+          const double d11 = rdiag[map[q]];
+          s_d[0] = d11;
+          dd[2 * q] = d11; dd[2 * q + 1] = 0.0;
+        } else {
+          dd[2 * q] = s_d[0]; dd[2 * q + 1] = s_d[1];
+          dd[2 * q + 2] = dinf(); dd[2 * q + 3] = s_d[2];
         }
       }
-      s_piv[0] = pivsiz; s_piv[1] = i1; s_piv[2] = i2;
+      s_piv[0] = pivsiz;
+      s_piv[1] = map[q];
+      s_piv[2] = (pivsiz == 2) ? map[q + 1] : -1;
     }
-    __syncwarp();
+    __syncthreads();
     const int pivsiz = s_piv[0];
-    // symmetric swaps q <-> i1 (and q+1 <-> i2)
-    for (int sw = 0; sw < pivsiz; ++sw) {
-      int a = q + sw, b = s_piv[1 + sw];
-      if (a != b) {
-        // rows
-        if (lane < bs) { double tmp = blk[lane][a]; blk[lane][a] = blk[lane][b]; blk[lane][b] = tmp; }
-        __syncwarp();
-        if (lane < bs) { double tmp = blk[a][lane]; blk[a][lane] = blk[b][lane]; blk[b][lane] = tmp; }
-        if (lane == 0) { int tmp = lp[a]; lp[a] = lp[b]; lp[b] = tmp; }
-        __syncwarp();
+    if (pivsiz == 0) {
+      if (!action) { singular = true; break; }
+      // remaining logical columns are zero pivots: zero their L entries
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int R = R0 + k;
+        if (R < bs && colok && lj >= q && li[k] >= lj) blk[C][R] = T(0);
+      }
+      if (tid >= q && tid < bs) { dd[2 * tid] = 0.0; dd[2 * tid + 1] = 0.0; }
+      __syncthreads();
+      break;
+    }
+    // refresh cached logical indices of the swapped physical positions
+#pragma unroll
+    for (int z = 0; z < 4; ++z) {
+      const int ph = s_sw[z];
+      if (ph >= 0) {
+        const int nlg = inv[ph];
+        if (ph == C) lj = nlg;
+        if (ph >= R0 && ph < R0 + 8) {
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            if (R0 + k == ph) li[k] = nlg;
+        }
       }
     }
     if (pivsiz == 1) {
-      double d11 = 1.0 / blk[q][q];
-      int r = lane;
-      if (r > q && r < bs) {
-        double w = blk[q][r];
-        wv[0][r] = w;
-        lv[0][r] = w * d11;
+      const int P = s_piv[1];
+      const T d11 = (T)s_d[0];
+      const T wc = blk[C][P] * d11;  // A(P, C) D^{-1}, from the pivot row
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int R = R0 + k;
+        if (R < bs && colok && li[k] > q) {
+          const T wr = blk[R][P];  // A(P, R)
+          if (lj > q) blk[C][R] -= wr * wc;
+          else if (C == P) blk[C][R] = wr * d11;  // L column of the pivot
+        }
       }
-      __syncwarp();
-      int cc = lane;
-      if (cc > q && cc < bs) {
-        double wc = wv[0][cc];
-        for (int rr = q + 1; rr < bs; ++rr) blk[cc][rr] -= wc * lv[0][rr];
-      }
-      __syncwarp();
-      if (r > q && r < bs) blk[q][r] = lv[0][r];
-      if (lane == 0) { blk[q][q] = 1.0; dd[2 * q] = d11; dd[2 * q + 1] = 0.0; }
-      __syncwarp();
+      __syncthreads();
       q += 1;
     } else {
-      double detscale = s_det[0], detpiv = s_det[1];
-      double a11 = blk[q][q], a22 = blk[q + 1][q + 1], a21 = blk[q][q + 1];
-      double d11 = (a22 * detscale) / detpiv;
-      double d22 = (a11 * detscale) / detpiv;
-      double d21 = (-a21 * detscale) / detpiv;
-      int r = lane;
-      if (r > q + 1 && r < bs) {
-        double w1 = blk[q][r], w2 = blk[q + 1][r];
-        wv[0][r] = w1; wv[1][r] = w2;
-        lv[0][r] = d11 * w1 + d21 * w2;
-        lv[1][r] = d21 * w1 + d22 * w2;
+      const int P1 = s_piv[1], P2 = s_piv[2];
+      const T e11 = (T)s_d[0], e21 = (T)s_d[1], e22 = (T)s_d[2];
+      const T w1c = blk[C][P1], w2c = blk[C][P2];
+      const T g1 = e11 * w1c + e21 * w2c, g2 = e21 * w1c + e22 * w2c;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int R = R0 + k;
+        if (R < bs && colok && li[k] > q + 1) {
+          const T w1r = blk[R][P1], w2r = blk[R][P2];
+          if (lj > q + 1) blk[C][R] -= w1r * g1 + w2r * g2;
+          else if (C == P1) blk[C][R] = e11 * w1r + e21 * w2r;
+          else if (C == P2) blk[C][R] = e21 * w1r + e22 * w2r;
+        }
       }
-      __syncwarp();
-      int cc = lane;
-      if (cc > q + 1 && cc < bs) {
-        double w1 = wv[0][cc], w2 = wv[1][cc];
-        for (int rr = q + 2; rr < bs; ++rr) blk[cc][rr] -= w1 * lv[0][rr] + w2 * lv[1][rr];
-      }
-      __syncwarp();
-      if (r > q + 1 && r < bs) { blk[q][r] = lv[0][r]; blk[q + 1][r] = lv[1][r]; }
-      if (lane == 0) {
-        blk[q][q] = 1.0; blk[q][q + 1] = 0.0; blk[q + 1][q + 1] = 1.0;
-        dd[2 * q] = d11; dd[2 * q + 1] = d21; dd[2 * q + 2] = dinf(); dd[2 * q + 3] = d22;
-      }
-      __syncwarp();
+      if (C == P1 && P2 >= R0 && P2 < R0 + 8) blk[P1][P2] = T(0);  // L(q+1, q) = 0
+      __syncthreads();
       q += 2;
     }
   }
   if (singular) {
-    if (lane == 0) { st->status = kDevSingular; st->bs = 0; }
+    if (tid == 0) { st->status = kDevSingular; st->bs = 0; }
     return;
   }
-  // write L11 (lower), D, step buffer, permutation
-  for (int cc = 0; cc < bs; ++cc) {
-    int r = lane;
-    if (r >= cc && r < bs) {
-      double v = blk[cc][r];
-      fd.L[(int64_t)(p + cc) * fd.ld + p + r] = (T)v;
-      fd.step[cc * kBlk + r] = v;
+  // write L11 (logical lower part, unit diagonal), D, step buffer, permutation
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int R = R0 + k;
+    if (R < bs && C < bs) {
+      const int i = li[k], j = lj;
+      if (i >= j) {
+        const T v = (i == j) ? T(1) : blk[C][R];
+        fd.L[(int64_t)(p + j) * fd.ld + p + i] = v;
+        fd.step[j * kBlk + i] = (double)v;
+      }
     }
   }
-  if (lane < bs) {
-    fd.D[2 * (p + lane)] = dd[2 * lane];
-    fd.D[2 * (p + lane) + 1] = dd[2 * lane + 1];
-    fd.step[kBlk * kBlk + 2 * lane] = dd[2 * lane];
-    fd.step[kBlk * kBlk + 2 * lane + 1] = dd[2 * lane + 1];
-    fd.lperm[lane] = lp[lane];
+  if (tid < bs) {
+    fd.D[2 * (p + tid)] = dd[2 * tid];
+    fd.D[2 * (p + tid) + 1] = dd[2 * tid + 1];
+    fd.step[kBlk * kBlk + 2 * tid] = dd[2 * tid];
+    fd.step[kBlk * kBlk + 2 * tid + 1] = dd[2 * tid + 1];
+    fd.lperm[tid] = map[tid];
   }
-  int oldp = (lane < bs) ? fd.perm[p + lp[lane]] : 0;
-  int oldo = (lane < bs) ? fd.opos[p + lp[lane]] : 0;
-  __syncwarp();
-  if (lane < bs) { fd.perm[p + lane] = oldp; fd.opos[p + lane] = oldo; }
-}
-
-// ------------------------------------------------------------------------
-// k_app_rowperm: permute rows [p, p+bs) of the eliminated columns [0, p)
-// ------------------------------------------------------------------------
-template <typename T>
-__global__ void k_app_rowperm(FrontDesc<T>* fds, const FrontState* sts, const int* fronts) {
-  const int f = fronts[blockIdx.y];
-  const FrontState st = sts[f];
-  if (st.bs == 0 || st.p == 0) return;
-  FrontDesc<T> fd = fds[f];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  int src = (lane < st.bs) ? fd.lperm[lane] : lane;
-  for (int c = blockIdx.x * nw + warp; c < st.p; c += gridDim.x * nw) {
-    T* col = fd.L + (int64_t)c * fd.ld + st.p;
-    T v = (lane < st.bs) ? col[src] : T(0);
-    __syncwarp();
-    if (lane < st.bs) col[lane] = v;
-  }
+  int oldp = 0, oldo = 0;
+  if (tid < bs) { oldp = fd.perm[p + map[tid]]; oldo = fd.opos[p + map[tid]]; }
+  __syncthreads();
+  if (tid < bs) { fd.perm[p + tid] = oldp; fd.opos[p + tid] = oldo; }
 }
 
 // ------------------------------------------------------------------------
@@ -253,43 +328,67 @@ __global__ void k_app_rowperm(FrontDesc<T>* fds, const FrontState* sts, const in
 template <typename T>
 __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, FrontState* sts,
                                                           const int* fronts, double u,
-                                                          double small) {
+                                                          double small, int napply) {
   const int f = fronts[blockIdx.y];
   FrontState* st = &sts[f];
   const int bs = st->bs;
   if (bs == 0) return;
   const int p = st->p;
   FrontDesc<T> fd = fds[f];
+  if ((int)blockIdx.x >= napply) {
+    // block permutation of rows [p, p+bs) in the eliminated columns [0, p)
+    if (p == 0) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int src = (lane < bs) ? fd.lperm[lane] : lane;
+    for (int c = (blockIdx.x - napply) * nw + warp; c < p; c += (gridDim.x - napply) * nw) {
+      T* col = fd.L + (int64_t)c * fd.ld + p;
+      const T v = (lane < bs) ? col[src] : T(0);
+      __syncwarp();
+      if (lane < bs) col[lane] = v;
+    }
+    return;
+  }
   const int r0 = p + bs;
   const int nrows = fd.m - r0;
   if (nrows <= 0) return;
-  __shared__ double l11[kBlk][kBlk + 1];  // l11[j][k] = L(j,k), row-major for broadcast
+  // X = A21 L11^{-T} in the factor precision T; D^{-1} application and the
+  // a-posteriori test in FP64
+  __shared__ T l11[kBlk][kBlk + 1];  // l11[j][k] = L(j,k), row-major for broadcast
   __shared__ double dd[2 * kBlk + 2];
   __shared__ int lp[kBlk];
   for (int i = threadIdx.x; i < kBlk * kBlk; i += blockDim.x) {
     int c = i / kBlk, r = i % kBlk;
-    l11[r][c] = (r > c && r < bs && c < bs) ? fd.step[c * kBlk + r] : 0.0;
+    l11[r][c] = (r > c && r < bs && c < bs) ? (T)fd.step[c * kBlk + r] : T(0);
   }
   for (int i = threadIdx.x; i < 2 * kBlk + 2; i += blockDim.x)
     dd[i] = (i < 2 * bs) ? fd.step[kBlk * kBlk + i] : 0.0;
   if (threadIdx.x < kBlk) lp[threadIdx.x] = (threadIdx.x < bs) ? fd.lperm[threadIdx.x] : 0;
   __syncthreads();
   const double thresh = 1.0 / u;
+  // |l| > 1/u tested on bit patterns (non-negative doubles order as integers)
+  const long long tkey = __double_as_longlong(thresh);
+  auto over = [tkey](double l) {  // Inf fails the test, NaN does not (as fabs(l) > 1/u)
+    const long long b = __double_as_longlong(l) & 0x7fffffffffffffffLL;
+    return b > tkey && b <= 0x7ff0000000000000LL;
+  };
   int myfail = bs;
-  for (int tile = blockIdx.x; tile * kApplyRows < nrows; tile += gridDim.x) {
+  for (int tile = blockIdx.x; tile * kApplyRows < nrows; tile += napply) {
     const int rr = tile * kApplyRows + threadIdx.x;
     const bool valid = rr < nrows;
     const int r = r0 + rr;
-    double x[kBlk];
+    T x[kBlk];
 #pragma unroll
     for (int j = 0; j < kBlk; ++j)
-      x[j] = (valid && j < bs) ? (double)fd.L[(int64_t)(p + lp[j]) * fd.ld + r] : 0.0;
+      x[j] = (valid && j < bs) ? fd.L[(int64_t)(p + lp[j]) * fd.ld + r] : T(0);
+    // right-looking: after x[k] is final, the updates of x[k+1..] are
+    // independent FMAs (instruction-level parallelism for the FP64 pipe)
 #pragma unroll
-    for (int j = 1; j < kBlk; ++j) {
-      double s = x[j];
+    for (int k = 0; k < kBlk - 1; ++k) {
+      if (k + 1 < bs) {
+        const T xk = x[k];
 #pragma unroll
-      for (int k = 0; k < j; ++k) s -= x[k] * l11[j][k];
-      x[j] = s;
+        for (int j = k + 1; j < kBlk; ++j) x[j] -= xk * l11[j][k];
+      }
     }
     if (valid) {
       T* W = fd.W + rr;
@@ -300,27 +399,27 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
           if (!isinf(dj)) {  // (second half of a 2x2 is handled with the first)
             if (j + 1 < bs && isinf(dd[2 * j + 2])) {
               const double d21 = dd[2 * j + 1], d22 = dd[2 * j + 3];
-              const double x1 = x[j], x2 = x[j + 1 < kBlk ? j + 1 : kBlk - 1];
+              const double x1 = (double)x[j], x2 = (double)x[j + 1 < kBlk ? j + 1 : kBlk - 1];
               const double l1 = dj * x1 + d21 * x2, l2 = d21 * x1 + d22 * x2;
               fd.L[(int64_t)(p + j) * fd.ld + r] = (T)l1;
               fd.L[(int64_t)(p + j + 1) * fd.ld + r] = (T)l2;
               W[(int64_t)j * fd.ld] = (T)x1;
               W[(int64_t)(j + 1) * fd.ld] = (T)x2;
-              int cand = (fabs(l1) > thresh) ? j : ((fabs(l2) > thresh) ? j + 1 : bs);
+              int cand = over(l1) ? j : (over(l2) ? j + 1 : bs);
               myfail = min(myfail, cand);
             } else {
               double l, w;
               if (dj == 0.0) {
-                const double v = x[j];
+                const double v = (double)x[j];
                 l = (fabs(v) < small) ? 0.0 : dinf() * v;
                 w = 0.0;
               } else {
-                l = x[j] * dj;
-                w = x[j];
+                l = (double)x[j] * dj;
+                w = (double)x[j];
               }
               fd.L[(int64_t)(p + j) * fd.ld + r] = (T)l;
               W[(int64_t)j * fd.ld] = (T)w;
-              if (fabs(l) > thresh) myfail = min(myfail, j);
+              if (over(l)) myfail = min(myfail, j);
             }
           }
         }
@@ -446,49 +545,35 @@ __device__ __forceinline__ int swap_partner(const SwapRanges& s, int x) {
   return x;
 }
 
+// One CTA per front (failures are rare): gather the affected symmetric lines
+// into the front's scratch, barrier, scatter them permuted.
 template <typename T>
-__global__ void k_app_swap_gather(FrontDesc<T>* fds, const FrontState* sts, const int* fronts) {
-  const int f = fronts[blockIdx.y];
+__global__ void k_app_swap(FrontDesc<T>* fds, const FrontState* sts, const int* fronts) {
+  const int f = fronts[blockIdx.x];
   const FrontState st = sts[f];
   if (st.bs == 0 || st.bs == st.npass) return;
   FrontDesc<T> fd = fds[f];
   SwapRanges sr = swap_ranges(st);
   const int nl = 2 * sr.npairs;
-  for (int li = blockIdx.x; li < nl; li += gridDim.x) {
-    int s = (li < sr.npairs) ? sr.a0 + li : sr.b0 + (li - sr.npairs);
+  int* ib = reinterpret_cast<int*>(fd.swapbuf + (int64_t)nl * fd.ld);
+  for (int li = 0; li < nl; ++li) {
+    const int s = (li < sr.npairs) ? sr.a0 + li : sr.b0 + (li - sr.npairs);
     T* line = fd.swapbuf + (int64_t)li * fd.ld;
     for (int x = threadIdx.x; x < fd.m; x += blockDim.x) line[x] = (T)sym_at(fd.L, fd.ld, x, s);
-    if (threadIdx.x == 0) {
-      int* ib = reinterpret_cast<int*>(fd.swapbuf + (int64_t)nl * fd.ld);
-      ib[2 * li] = fd.perm[s];
-      ib[2 * li + 1] = fd.opos[s];
-    }
+    if (threadIdx.x == 0) { ib[2 * li] = fd.perm[s]; ib[2 * li + 1] = fd.opos[s]; }
   }
-}
-
-template <typename T>
-__global__ void k_app_swap_scatter(FrontDesc<T>* fds, const FrontState* sts, const int* fronts) {
-  const int f = fronts[blockIdx.y];
-  const FrontState st = sts[f];
-  if (st.bs == 0 || st.bs == st.npass) return;
-  FrontDesc<T> fd = fds[f];
-  SwapRanges sr = swap_ranges(st);
-  const int nl = 2 * sr.npairs;
-  for (int li = blockIdx.x; li < nl; li += gridDim.x) {
-    int s = (li < sr.npairs) ? sr.a0 + li : sr.b0 + (li - sr.npairs);
-    int ps = swap_partner(sr, s);
-    int pli = (ps >= sr.a0 && ps < sr.a0 + sr.npairs) ? ps - sr.a0 : sr.npairs + (ps - sr.b0);
+  __syncthreads();
+  for (int li = 0; li < nl; ++li) {
+    const int s = (li < sr.npairs) ? sr.a0 + li : sr.b0 + (li - sr.npairs);
+    const int ps = swap_partner(sr, s);
+    const int pli = (ps >= sr.a0 && ps < sr.a0 + sr.npairs) ? ps - sr.a0 : sr.npairs + (ps - sr.b0);
     const T* line = fd.swapbuf + (int64_t)pli * fd.ld;
     for (int x = threadIdx.x; x < fd.m; x += blockDim.x) {
-      T v = line[swap_partner(sr, x)];
+      const T v = line[swap_partner(sr, x)];
       if (x <= s) fd.L[(int64_t)x * fd.ld + s] = v;
       else fd.L[(int64_t)s * fd.ld + x] = v;
     }
-    if (threadIdx.x == 0) {
-      const int* ib = reinterpret_cast<const int*>(fd.swapbuf + (int64_t)nl * fd.ld);
-      fd.perm[s] = ib[2 * pli];
-      fd.opos[s] = ib[2 * pli + 1];
-    }
+    if (threadIdx.x == 0) { fd.perm[s] = ib[2 * pli]; fd.opos[s] = ib[2 * pli + 1]; }
   }
 }
 
@@ -734,22 +819,38 @@ __global__ void k_calc_ld(FrontDesc<T>* fds, const FrontState* sts, const int* f
   const int nelim = sts[f].nelim;
   const int cm = fd.m - fd.n;
   if (cm <= 0 || nelim <= 0) return;
-  for (int rr = blockIdx.x * blockDim.x + threadIdx.x; rr < cm; rr += gridDim.x * blockDim.x) {
-    const int r = fd.n + rr;
-    for (int c = 0; c < nelim;) {
-      double d11 = fd.D[2 * c];
-      if (c + 1 == nelim || isfinite(fd.D[2 * c + 2])) {
-        if (d11 != 0.0) d11 = 1.0 / d11;
-        fd.LD[(int64_t)c * cm + rr] = (T)(d11 * (double)fd.L[(int64_t)c * fd.ld + r]);
-        c += 1;
+  // LD(:, c) = alpha_c L(:, c) + beta_c L(:, partner_c): the coefficients of
+  // D = (D^{-1})^{-1} are formed once per column chunk in shared memory
+  constexpr int CH = 64;
+  __shared__ double alpha[CH], beta[CH];
+  __shared__ int partner[CH];
+  for (int c0 = 0; c0 < nelim; c0 += CH) {
+    const int nc = min(CH, nelim - c0);
+    __syncthreads();
+    if ((int)threadIdx.x < nc) {
+      const int c = c0 + threadIdx.x;
+      const double d11 = fd.D[2 * c];
+      if (isinf(d11)) {  // second column of a 2x2
+        const double a = fd.D[2 * (c - 1)], b = fd.D[2 * (c - 1) + 1], d = fd.D[2 * c + 1];
+        const double det = a * d - b * b;
+        alpha[threadIdx.x] = a / det; beta[threadIdx.x] = -b / det; partner[threadIdx.x] = c - 1;
+      } else if (c + 1 < nelim && isinf(fd.D[2 * c + 2])) {  // first column of a 2x2
+        const double b = fd.D[2 * c + 1], d = fd.D[2 * c + 3];
+        const double det = d11 * d - b * b;
+        alpha[threadIdx.x] = d / det; beta[threadIdx.x] = -b / det; partner[threadIdx.x] = c + 1;
       } else {
-        double d21 = fd.D[2 * c + 1], d22 = fd.D[2 * c + 3];
-        double det = d11 * d22 - d21 * d21;
-        double e11 = d11 / det, e21 = d21 / det, e22 = d22 / det;
-        double a1 = (double)fd.L[(int64_t)c * fd.ld + r], a2 = (double)fd.L[(int64_t)(c + 1) * fd.ld + r];
-        fd.LD[(int64_t)c * cm + rr] = (T)(e22 * a1 - e21 * a2);
-        fd.LD[(int64_t)(c + 1) * cm + rr] = (T)(-e21 * a1 + e11 * a2);
-        c += 2;
+        alpha[threadIdx.x] = (d11 != 0.0) ? 1.0 / d11 : 0.0; beta[threadIdx.x] = 0.0;
+        partner[threadIdx.x] = c;
+      }
+    }
+    __syncthreads();
+    for (int rr = blockIdx.x * blockDim.x + threadIdx.x; rr < cm; rr += gridDim.x * blockDim.x) {
+      const int r = fd.n + rr;
+      for (int k = 0; k < nc; ++k) {
+        const int c = c0 + k;
+        double v = alpha[k] * (double)fd.L[(int64_t)c * fd.ld + r];
+        if (beta[k] != 0.0) v += beta[k] * (double)fd.L[(int64_t)partner[k] * fd.ld + r];
+        fd.LD[(int64_t)c * cm + rr] = (T)v;
       }
     }
   }
@@ -817,25 +918,27 @@ static inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 template <typename T>
 void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int step,
                      int max_rows, int max_trail_rows, int max_trail_cols, bool action,
-                     double u, double small, cudaStream_t s) {
+                     double u, double small, cudaStream_t s, PhaseTimer* tm) {
   if (nf <= 0) return;
-  { k_app_diag<T><<<nf, 32, 0, s>>>(fd, st, fronts, step, action, small); note_launches(1); }
-  {
-    int pcols = step * kBlk;  // columns of L to the left (upper bound on p)
-    int gx = std::max(1, std::min(cdiv(pcols, 8), 64));
-    if (pcols > 0) { k_app_rowperm<T><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts); note_launches(1); }
-  }
-  int gx = std::max(1, cdiv(max_rows, kApplyRows));
-  { k_app_apply<T><<<dim3(gx, nf), kApplyRows, 0, s>>>(fd, st, fronts, u, small); note_launches(1); }
-  { k_app_fixup<T><<<dim3(gx, nf), kApplyRows, 0, s>>>(fd, st, fronts); note_launches(1); }
+  pmark(tm, kPhDiag, s);
+  { k_app_diag<T><<<nf, kDiagThreads, 0, s>>>(fd, st, fronts, step, action, small); note_launches(1); }
+  // apply (+ row permutation of the eliminated part in extra CTAs)
+  const int napply = std::max(1, cdiv(max_rows, kApplyRows));
+  const int pcols = step * kBlk;  // upper bound on p
+  const int nperm = pcols > 0 ? std::max(1, std::min(cdiv(pcols, kApplyRows / 32), 64)) : 0;
+  pmark(tm, kPhApply, s);
+  { k_app_apply<T><<<dim3(napply + nperm, nf), kApplyRows, 0, s>>>(fd, st, fronts, u, small, napply); note_launches(1); }
+  pmark(tm, kPhFixup, s);
+  { k_app_fixup<T><<<dim3(napply, nf), kApplyRows, 0, s>>>(fd, st, fronts); note_launches(1); }
   // tile estimate assumes no failed columns so far; after failures the
   // trailing region is wider and the kernel's grid-stride loop covers it, so
   // the launch is never skipped
   int tr = std::max(0, cdiv(max_trail_rows, kGemmTile)), tc = std::max(0, cdiv(max_trail_cols, kGemmTile));
   int tiles = tc * tr - tc * (tc - 1) / 2;
+  pmark(tm, kPhPanel, s);
   launch_syrk_panel<T>(fd, st, fronts, nf, std::max(tiles, 1), s);
-  { k_app_swap_gather<T><<<dim3(64, nf), 256, 0, s>>>(fd, st, fronts); note_launches(1); }
-  { k_app_swap_scatter<T><<<dim3(64, nf), 256, 0, s>>>(fd, st, fronts); note_launches(1); }
+  pmark(tm, kPhSwap, s);
+  { k_app_swap<T><<<nf, 256, 0, s>>>(fd, st, fronts); note_launches(1); }
 }
 
 template <typename T>
@@ -877,7 +980,7 @@ void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* front
 
 #define INST(T)                                                                                 \
   template void launch_app_step<T>(FrontDesc<T>*, FrontState*, const int*, int, int, int, int,  \
-                                   int, bool, double, double, cudaStream_t);                    \
+                                   int, bool, double, double, cudaStream_t, PhaseTimer*);       \
   template void launch_app_finish<T>(FrontDesc<T>*, FrontState*, const int*, int, cudaStream_t); \
   template void launch_tpp<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double, double, \
                               bool, cudaStream_t);                                              \

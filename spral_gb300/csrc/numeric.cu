@@ -34,8 +34,52 @@ struct CudaFail {
 };
 
 static std::atomic<long long> g_launches{0};
+
+void PhaseTimer::mark(int phase, cudaStream_t s) {
+  if (used == cap) {
+    int nc = cap ? 2 * cap : 1024;
+    cudaEvent_t* ne = new cudaEvent_t[nc];
+    int* np = new int[nc];
+    for (int i = 0; i < cap; ++i) { ne[i] = ev[i]; np[i] = ph[i]; }
+    for (int i = cap; i < nc; ++i) cudaEventCreate(&ne[i]);
+    delete[] ev;
+    delete[] ph;
+    ev = ne;
+    ph = np;
+    cap = nc;
+  }
+  cudaEventRecord(ev[used], s);
+  ph[used++] = phase;
+}
+void PhaseTimer::flush() {
+  for (int i = 0; i + 1 < used; ++i) {
+    float t = 0;
+    if (cudaEventElapsedTime(&t, ev[i], ev[i + 1]) == cudaSuccess) {
+      ms[ph[i]] += t;
+      cnt[ph[i]] += 1;
+    }
+  }
+  if (used > 0) { ev[0] = ev[0]; }
+  // keep the last event as the start of the next interval
+  if (used > 0) {
+    std::swap(ev[0], ev[used - 1]);
+    ph[0] = ph[used - 1];
+    used = 1;
+  }
+  cudaGetLastError();
+}
+void PhaseTimer::reset() {
+  used = 0;
+  for (int i = 0; i < kPhCount; ++i) { ms[i] = 0; cnt[i] = 0; }
+}
+PhaseTimer::~PhaseTimer() {
+  for (int i = 0; i < cap; ++i) cudaEventDestroy(ev[i]);
+  delete[] ev;
+  delete[] ph;
+}
 void note_launches(int k) { g_launches += k; }
 double fp64_peak_tflops(int device);
+void launch_recip_probe(const double* x, double* y, int n, cudaStream_t s);
 
 #define CK(x)                                              \
   do {                                                     \
@@ -326,6 +370,8 @@ struct NumericBase {
   bool profile = false;
   double prof_ms = 0, prof_flops = 0;
   long long prof_launches = 0;
+  PhaseTimer ptimer;
+  PhaseTimer* tm() { return profile ? &ptimer : nullptr; }
   virtual int factor(const double* aval, bool aval_on_device, const double* scaling,
                      cudaStream_t user_stream) = 0;
   virtual int solve_dev(int job, int nrhs, double* x, int ldx, cudaStream_t s) = 0;
@@ -372,7 +418,8 @@ struct Numeric : NumericBase {
   bool solve_ready = false;
   SolveNode<T>* d_sn = nullptr;
   int* d_children = nullptr;
-  DevBuf<double> xloc, xorig, xbuf, rbuf, dbuf, bbuf, nbuf;
+  DevBuf<T> xloc, xorig;
+  DevBuf<double> xbuf, rbuf, dbuf, bbuf, nbuf;
   const double* cur_aval = nullptr;  // device values of the last factor
   double last_bwd_err = 0.0;
   std::vector<cudaEvent_t> pev;
@@ -511,12 +558,17 @@ struct Numeric : NumericBase {
         int64_t z = std::max<int64_t>((int64_t)ld_[f] * n_[f], (int64_t)hfd[f].cm * hfd[f].cm);
         maxz = std::max(maxz, z);
       }
+      pmark(tm(), kPhZero, s);
       launch_zero_fronts<T>(d_fd, fr, nf, (int)std::min<int64_t>(maxz, 1 << 30), s);
+      pmark(tm(), kPhLoadA, s);
       launch_load_a<T>(d_fd, fr, nf, S->d_nptr, S->d_nlist, cur_aval, S->d_rlist, S->d_rptr,
                        d_scale, max_ent, s);
+      pmark(tm(), kPhInitPerm, s);
       launch_init_perm<T>(d_fd, fr, nf, S->d_sptr, max_n, s);
+      pmark(tm(), kPhDelays, s);
       launch_assemble_delays<T>(d_fd, d_st, d_dwork, (int)dwork.size(), S->d_rdir,
                                 S->d_rdir_ptr, s);
+      pmark(tm(), kPhAssemble, s);
       launch_assemble_contrib<T>(d_fd, S->d_cols + S->cols_start[l],
                                  S->cols_start[l + 1] - S->cols_start[l], S->d_pairs, S->d_rdir,
                                  S->d_rdir_ptr, s);
@@ -532,20 +584,27 @@ struct Numeric : NumericBase {
             tc = std::max(tc, n_[f] - kBlk * (st + 1));
           }
           launch_app_step<T>(d_fd, d_st, fr, nf, st, std::max(mr, 1), tr, tc, co.action, co.u,
-                             co.small, s);
+                             co.small, s, tm());
         }
       }
+      pmark(tm(), kPhFinish, s);
       launch_app_finish<T>(d_fd, d_st, fr, nf, s);
+      pmark(tm(), kPhTpp, s);
       const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
       launch_tpp<T>(d_fd, d_st, fr, nf, co.action, co.u, co.small, tpp_all, s);
+      pmark(tm(), kPhCalcLd, s);
       launch_calc_ld<T>(d_fd, d_st, fr, nf, max_cm, s);
+      pmark(tm(), kPhContrib, s);
       if (profile) CK(cudaEventRecord(pev[2 * l], s));
       launch_contrib_gemm<T>(d_fd, d_st, fr, nf, max_cm, s);
       if (profile) CK(cudaEventRecord(pev[2 * l + 1], s));
+      pmark(tm(), kPhStats, s);
       launch_stats<T>(d_fd, d_st, fr, nf, max_n, d_stats, s);
+      pmark(tm(), kPhHost, s);
       CK(cudaMemcpyAsync(hst.data() + f0, d_st + f0, nf * sizeof(FrontState),
                          cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
+      if (profile) ptimer.flush();
       bool singular = false, bad = false;
       for (int f = f0; f < f1; ++f) {
         if (hst[f].status == kDevSingular) singular = true;
@@ -652,8 +711,10 @@ struct Numeric : NumericBase {
         for (int l = 0; l < S->nlev; ++l) {
           const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
           const int* fr = S->d_fronts + f0;
+          pmark(tm(), kPhFwdGather, s);
           launch_fwd_gather<T>(d_sn, fr, nf, d_children, xp, ldx, q, s);
-          launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, s);
+          launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, s, tm());
+          pmark(tm(), kPhFwdScatter, s);
           launch_fwd_scatter<T>(d_sn, fr, nf, xp, ldx, q, lvl_max_nelim[l], s);
         }
       }
@@ -661,12 +722,14 @@ struct Numeric : NumericBase {
         for (int l = S->nlev - 1; l >= 0; --l) {
           const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
           launch_bwd<T>(d_sn, S->d_fronts + f0, nf, xp, ldx, q, lvl_max_m[l], lvl_max_nelim[l],
-                        diag, bwd, s);
+                        diag, bwd, s, tm());
         }
       }
     }
+    pmark(tm(), kPhHost, s);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
+    if (profile) ptimer.flush();
     return 0;
   }
 
@@ -728,16 +791,21 @@ struct Numeric : NumericBase {
     int it = 0;
     const int maxit = S->gopts.max_refine;
     for (;; ++it) {
+      pmark(tm(), kPhResid, s);
       launch_spmv_resid(S->d_aptr, S->d_acol, S->d_asrc, cur_aval, n, x, b, rbuf.p, q, ld, s);
       launch_bwd_err(S->d_aptr, S->d_asrc, cur_aval, n, x, rbuf.p, b, q, ld, nbuf.p, s);
+      pmark(tm(), kPhHost, s);
       CK(cudaMemcpyAsync(h.data(), nbuf.p, q * sizeof(double), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
+      if (profile) ptimer.flush();
       double worst = 0;
       for (int r = 0; r < q; ++r) worst = std::max(worst, h[r]);
       last_bwd_err = worst;
       if (!(worst > S->gopts.refine_tol) || it >= maxit) break;
       solve_dev(0, q, rbuf.p, ld, nullptr);
+      pmark(tm(), kPhAxpy, s);
       launch_axpy(n, q, ld, x, rbuf.p, s);
+      pmark(tm(), kPhHost, s);
     }
     return it;
   }
@@ -1015,6 +1083,17 @@ void spral_ssids_gpu_set_profiling(void* numeric, int on) {
   N->prof_ms = 0;
   N->prof_flops = 0;
   N->prof_launches = 0;
+  N->ptimer.reset();
+}
+
+/* Per-phase device time (ms) and interval counts accumulated while profiling
+ * (32 phases; see the Phase enum of the implementation). */
+void spral_ssids_gpu_phase_times(const void* numeric, double* ms, long long* counts) {
+  auto* N = static_cast<const ssids300::NumericBase*>(numeric);
+  for (int i = 0; i < ssids300::kPhCount; ++i) {
+    ms[i] = N->ptimer.ms[i];
+    counts[i] = N->ptimer.cnt[i];
+  }
 }
 
 /* out[0] = contribution-GEMM time (ms) summed over profiled factors,
@@ -1034,6 +1113,11 @@ int spral_ssids_gpu_solve_refined_dev(void* numeric, int nrhs, const double* b_d
   } catch (ssids300::CudaFail const& e) {
     return map_cuda_error(e, nullptr);
   }
+}
+
+int spral_ssids_gpu_recip_probe(const double* x_dev, double* y_dev, int n) {
+  ssids300::launch_recip_probe(x_dev, y_dev, n, 0);
+  return (int)cudaDeviceSynchronize();
 }
 
 double spral_ssids_gpu_fp64_peak_tflops(int device) {

@@ -11,8 +11,13 @@
 // never update the same entry: each node gathers b for its own pivots plus
 // its children's local vectors (fixed order, no atomics), solves, and leaves
 // rows [nelim, m) of its local vector for its parent.  The triangular solves
-// are blocked by 64 rows: a one-CTA diagonal-block solve followed by a
-// row-parallel (forward) or column-parallel (backward) update.
+// are blocked by 64 rows: a one-warp diagonal-block solve (values in
+// registers, the pivot row broadcast by shuffles) followed by a row-parallel
+// (forward) or column-parallel (backward) update.  Arithmetic is in the
+// factor precision T; the number of right-hand sides per pass NR is a
+// template parameter so that no work is spent on absent columns.
+#include <type_traits>
+
 #include "ssids_gpu.cuh"
 
 namespace ssids300 {
@@ -20,17 +25,16 @@ namespace ssids300 {
 namespace {
 
 constexpr int SB = kSolveBlk;
-constexpr int SR = kSolveRhs;
 
 template <typename T>
 __global__ void k_fwd_gather(const SolveNode<T>* sns, const int* nodes, const int* children,
                              const double* x, int ldx, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.x]];
   const int m = sn.m;
-  double* xo = sn.xorig;
+  T* xo = sn.xorig;
   for (int e = threadIdx.x; e < m * nrhs; e += blockDim.x) {
     const int i = e % m, r = e / m;
-    xo[e] = (i < sn.ncol) ? x[(int64_t)r * ldx + sn.sptr0 + i] : 0.0;
+    xo[e] = (i < sn.ncol) ? (T)x[(int64_t)r * ldx + sn.sptr0 + i] : T(0);
   }
   __syncthreads();
   for (int ci = sn.child_beg; ci < sn.child_end; ++ci) {
@@ -40,7 +44,7 @@ __global__ void k_fwd_gather(const SolveNode<T>* sns, const int* nodes, const in
     for (int e = threadIdx.x; e < tot * nrhs; e += blockDim.x) {
       const int k = e % tot, r = e / tot;
       int pos;
-      double v;
+      T v;
       if (k < nd) {
         pos = sn.ncol + cn.doff + k;
         v = cn.xloc[(int64_t)r * cn.m + cn.nelim + k];
@@ -60,38 +64,53 @@ __global__ void k_fwd_gather(const SolveNode<T>* sns, const int* nodes, const in
   }
 }
 
+// stage the jb x jb diagonal block (strictly lower part) into shared memory
 template <typename T>
-__global__ void k_fwd_diag(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
+__device__ __forceinline__ void load_diag_block(const SolveNode<T>& sn, int j0, int jb,
+                                                T (*Lb)[SB + 1]) {
+  for (int e = threadIdx.x; e < SB * SB; e += blockDim.x) {
+    const int c = e / SB, r = e % SB;
+    Lb[c][r] = (r > c && r < jb && c < jb) ? sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : T(0);
+  }
+}
+
+// forward: unit lower triangular solve of rows [j0, j0+jb) in place
+template <typename T, int NR>
+__global__ void __launch_bounds__(64) k_fwd_diag(const SolveNode<T>* sns, const int* nodes,
+                                                 int step, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.x]];
   const int j0 = step * SB;
   if (j0 >= sn.nelim) return;
   const int jb = min(SB, sn.nelim - j0);
-  __shared__ double Lb[SB][SB + 1];
-  __shared__ double xb[SB][SR];
-  for (int e = threadIdx.x; e < SB * SB; e += blockDim.x) {
-    const int c = e / SB, r = e % SB;
-    Lb[c][r] = (r > c && r < jb && c < jb) ? (double)sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : 0.0;
-  }
-  for (int e = threadIdx.x; e < jb * nrhs; e += blockDim.x) {
-    const int r = e % jb, q = e / jb;
-    xb[r][q] = sn.xloc[(int64_t)q * sn.m + j0 + r];
-  }
+  __shared__ T Lb[SB][SB + 1];  // Lb[c][r] = L(j0+r, j0+c)
+  load_diag_block(sn, j0, jb, Lb);
   __syncthreads();
-  for (int c = 0; c < jb - 1; ++c) {
-    const int nr = jb - c - 1;
-    for (int e = threadIdx.x; e < nr * nrhs; e += blockDim.x) {
-      const int r = c + 1 + e % nr, q = e / nr;
-      xb[r][q] -= Lb[c][r] * xb[c][q];
-    }
-    __syncthreads();
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  T x0[NR], x1[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    x0[q] = (q < nrhs && lane < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane] : T(0);
+    x1[q] = (q < nrhs && lane + 32 < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] : T(0);
   }
-  for (int e = threadIdx.x; e < jb * nrhs; e += blockDim.x) {
-    const int r = e % jb, q = e / jb;
-    sn.xloc[(int64_t)q * sn.m + j0 + r] = xb[r][q];
+  for (int k = 0; k < jb - 1; ++k) {
+    const T l0 = Lb[k][lane], l1 = Lb[k][lane + 32];  // zero on and above the diagonal
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      const T xk = (k < 32) ? __shfl_sync(0xffffffffu, x0[q], k & 31)
+                            : __shfl_sync(0xffffffffu, x1[q], k & 31);
+      x0[q] -= l0 * xk;
+      x1[q] -= l1 * xk;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    if (q < nrhs && lane < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane] = x0[q];
+    if (q < nrhs && lane + 32 < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] = x1[q];
   }
 }
 
-template <typename T>
+template <typename T, int NR>
 __global__ void k_fwd_update(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];
   const int j0 = step * SB;
@@ -99,22 +118,25 @@ __global__ void k_fwd_update(const SolveNode<T>* sns, const int* nodes, int step
   const int jb = min(SB, sn.nelim - j0);
   const int i0 = j0 + jb;
   if (i0 >= sn.m) return;
-  __shared__ double yb[SB][SR];
-  for (int e = threadIdx.x; e < jb * nrhs; e += blockDim.x) {
-    const int r = e % jb, q = e / jb;
-    yb[r][q] = sn.xloc[(int64_t)q * sn.m + j0 + r];
+  __shared__ T yb[SB][NR];
+  for (int e = threadIdx.x; e < SB * NR; e += blockDim.x) {
+    const int r = e % SB, q = e / SB;
+    yb[r][q] = (r < jb && q < nrhs) ? sn.xloc[(int64_t)q * sn.m + j0 + r] : T(0);
   }
   __syncthreads();
   for (int i = i0 + blockIdx.x * blockDim.x + threadIdx.x; i < sn.m; i += gridDim.x * blockDim.x) {
-    double acc[SR];
+    T acc[NR];
 #pragma unroll
-    for (int q = 0; q < SR; ++q) acc[q] = 0.0;
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
+    const T* lrow = sn.L + (int64_t)j0 * sn.ld + i;
     for (int c = 0; c < jb; ++c) {
-      const double l = (double)sn.L[(int64_t)(j0 + c) * sn.ld + i];
+      const T l = lrow[(int64_t)c * sn.ld];
 #pragma unroll
-      for (int q = 0; q < SR; ++q) acc[q] += l * yb[c][q];
+      for (int q = 0; q < NR; ++q) acc[q] += l * yb[c][q];
     }
-    for (int q = 0; q < nrhs; ++q) sn.xloc[(int64_t)q * sn.m + i] -= acc[q];
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+      if (q < nrhs) sn.xloc[(int64_t)q * sn.m + i] -= acc[q];
   }
 }
 
@@ -125,7 +147,7 @@ __global__ void k_fwd_scatter(const SolveNode<T>* sns, const int* nodes, double*
   const int tot = sn.nelim * nrhs;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
     const int i = e % sn.nelim, q = e / sn.nelim;
-    x[(int64_t)q * ldx + sn.perm[i]] = sn.xloc[(int64_t)q * sn.m + i];
+    x[(int64_t)q * ldx + sn.perm[i]] = (double)sn.xloc[(int64_t)q * sn.m + i];
   }
 }
 
@@ -155,92 +177,99 @@ __global__ void k_bwd_gather(const SolveNode<T>* sns, const int* nodes, const do
         v = di * v;
       }
     }
-    sn.xloc[(int64_t)q * sn.m + i] = v;
+    sn.xloc[(int64_t)q * sn.m + i] = (T)v;
   }
 }
 
 // xloc[j] -= sum_{i in [nelim, m)} L(i, j) xloc[i]   (warp per column j)
-template <typename T>
+template <typename T, int NR>
 __global__ void k_bwd_l21(const SolveNode<T>* sns, const int* nodes, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   if (sn.m <= sn.nelim) return;
   for (int j = blockIdx.x * nw + warp; j < sn.nelim; j += gridDim.x * nw) {
-    double acc[SR];
+    T acc[NR];
 #pragma unroll
-    for (int q = 0; q < SR; ++q) acc[q] = 0.0;
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
     const T* col = sn.L + (int64_t)j * sn.ld;
     for (int i = sn.nelim + lane; i < sn.m; i += 32) {
-      const double l = (double)col[i];
+      const T l = col[i];
 #pragma unroll
-      for (int q = 0; q < SR; ++q)
+      for (int q = 0; q < NR; ++q)
         if (q < nrhs) acc[q] += l * sn.xloc[(int64_t)q * sn.m + i];
     }
 #pragma unroll
-    for (int q = 0; q < SR; ++q)
+    for (int q = 0; q < NR; ++q)
       for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
     if (lane == 0)
       for (int q = 0; q < nrhs; ++q) sn.xloc[(int64_t)q * sn.m + j] -= acc[q];
   }
 }
 
-template <typename T>
-__global__ void k_bwd_diag(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
+// backward: unit upper (L^T) triangular solve of rows [j0, j0+jb) in place
+template <typename T, int NR>
+__global__ void __launch_bounds__(64) k_bwd_diag(const SolveNode<T>* sns, const int* nodes,
+                                                 int step, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.x]];
   const int j0 = step * SB;
   if (j0 >= sn.nelim) return;
   const int jb = min(SB, sn.nelim - j0);
-  __shared__ double Lb[SB][SB + 1];  // Lb[c][r] = L(j0+r, j0+c)
-  __shared__ double xb[SB][SR];
-  for (int e = threadIdx.x; e < SB * SB; e += blockDim.x) {
-    const int c = e / SB, r = e % SB;
-    Lb[c][r] = (r > c && r < jb && c < jb) ? (double)sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : 0.0;
-  }
-  for (int e = threadIdx.x; e < jb * nrhs; e += blockDim.x) {
-    const int r = e % jb, q = e / jb;
-    xb[r][q] = sn.xloc[(int64_t)q * sn.m + j0 + r];
-  }
+  __shared__ T Lb[SB][SB + 1];  // Lb[c][r] = L(j0+r, j0+c)
+  load_diag_block(sn, j0, jb, Lb);
   __syncthreads();
-  // (L^T y)_r = y_r + sum_{c>r} L(c, r) y_c
-  for (int c = jb - 1; c > 0; --c) {
-    for (int e = threadIdx.x; e < c * nrhs; e += blockDim.x) {
-      const int r = e % c, q = e / c;
-      xb[r][q] -= Lb[r][c] * xb[c][q];
-    }
-    __syncthreads();
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
+  T x0[NR], x1[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    x0[q] = (q < nrhs && lane < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane] : T(0);
+    x1[q] = (q < nrhs && lane + 32 < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] : T(0);
   }
-  for (int e = threadIdx.x; e < jb * nrhs; e += blockDim.x) {
-    const int r = e % jb, q = e / jb;
-    sn.xloc[(int64_t)q * sn.m + j0 + r] = xb[r][q];
+  // (L^T y)_r = y_r + sum_{c > r} L(c, r) y_c ; process c from the bottom.
+  // L(c, r) = Lb[r][c] is zero unless c > r, so no lane masks are needed.
+  for (int c = jb - 1; c > 0; --c) {
+    const T l0 = Lb[lane][c], l1 = Lb[lane + 32][c];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      const T yc = (c < 32) ? __shfl_sync(0xffffffffu, x0[q], c & 31)
+                            : __shfl_sync(0xffffffffu, x1[q], c & 31);
+      x0[q] -= l0 * yc;
+      x1[q] -= l1 * yc;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NR; ++q) {
+    if (q < nrhs && lane < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane] = x0[q];
+    if (q < nrhs && lane + 32 < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] = x1[q];
   }
 }
 
 // columns j < j0: xloc[j] -= sum_{c < jb} L(j0+c, j) y_c   (warp per column)
-template <typename T>
+template <typename T, int NR>
 __global__ void k_bwd_update(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];
   const int j0 = step * SB;
   if (j0 >= sn.nelim || j0 == 0) return;
   const int jb = min(SB, sn.nelim - j0);
-  __shared__ double yb[SB][SR];
-  for (int e = threadIdx.x; e < jb * nrhs; e += blockDim.x) {
-    const int r = e % jb, q = e / jb;
-    yb[r][q] = sn.xloc[(int64_t)q * sn.m + j0 + r];
+  __shared__ T yb[SB][NR];
+  for (int e = threadIdx.x; e < SB * NR; e += blockDim.x) {
+    const int r = e % SB, q = e / SB;
+    yb[r][q] = (r < jb && q < nrhs) ? sn.xloc[(int64_t)q * sn.m + j0 + r] : T(0);
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int j = blockIdx.x * nw + warp; j < j0; j += gridDim.x * nw) {
     const T* col = sn.L + (int64_t)j * sn.ld + j0;
-    double acc[SR];
+    T acc[NR];
 #pragma unroll
-    for (int q = 0; q < SR; ++q) acc[q] = 0.0;
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
     for (int c = lane; c < jb; c += 32) {
-      const double l = (double)col[c];
+      const T l = col[c];
 #pragma unroll
-      for (int q = 0; q < SR; ++q) acc[q] += l * yb[c][q];
+      for (int q = 0; q < NR; ++q) acc[q] += l * yb[c][q];
     }
 #pragma unroll
-    for (int q = 0; q < SR; ++q)
+    for (int q = 0; q < NR; ++q)
       for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
     if (lane == 0)
       for (int q = 0; q < nrhs; ++q) sn.xloc[(int64_t)q * sn.m + j] -= acc[q];
@@ -248,6 +277,17 @@ __global__ void k_bwd_update(const SolveNode<T>* sns, const int* nodes, int step
 }
 
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+// call f(std::integral_constant<int, NR>) with the smallest NR in
+// {1, 2, 4, 8, 16} that holds q right-hand sides
+template <typename F>
+void with_nr(int q, F&& f) {
+  if (q <= 1) f(std::integral_constant<int, 1>());
+  else if (q <= 2) f(std::integral_constant<int, 2>());
+  else if (q <= 4) f(std::integral_constant<int, 4>());
+  else if (q <= 8) f(std::integral_constant<int, 8>());
+  else f(std::integral_constant<int, 16>());
+}
 
 }  // namespace
 
@@ -260,17 +300,22 @@ void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const i
 
 template <typename T>
 void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_nelim,
-                      int max_m, int nrhs, cudaStream_t s) {
+                      int max_m, int nrhs, cudaStream_t s, PhaseTimer* tm) {
   if (nn <= 0) return;
   const int steps = cdiv(max_nelim, SB);
-  for (int st = 0; st < steps; ++st) {
-    { k_fwd_diag<T><<<nn, 256, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
-    int rows = max_m - st * SB;  // upper bound; the kernel derives the exact range
-    if (rows > 0) {
-      int gx = std::max(1, std::min(cdiv(rows, 256), 128));
-      { k_fwd_update<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
+  with_nr(nrhs, [&](auto nrc) {
+    constexpr int NR = decltype(nrc)::value;
+    for (int st = 0; st < steps; ++st) {
+      pmark(tm, kPhFwdDiag, s);
+      { k_fwd_diag<T, NR><<<nn, 64, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
+      int rows = max_m - st * SB;  // upper bound; the kernel derives the exact range
+      if (rows > 0) {
+        int gx = std::max(1, std::min(cdiv(rows, 128), 128));
+        pmark(tm, kPhFwdUpdate, s);
+        { k_fwd_update<T, NR><<<dim3(gx, nn), 128, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
+      }
     }
-  }
+  });
 }
 
 template <typename T>
@@ -283,23 +328,32 @@ void launch_fwd_scatter(const SolveNode<T>* sn, const int* nodes, int nn, double
 
 template <typename T>
 void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx, int nrhs,
-                int max_m, int max_nelim, bool do_diag, bool do_bwd, cudaStream_t s) {
+                int max_m, int max_nelim, bool do_diag, bool do_bwd, cudaStream_t s,
+                PhaseTimer* tm) {
   if (nn <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_m * nrhs, 256), 64));
+  pmark(tm, kPhBwdGather, s);
   { k_bwd_gather<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, do_diag, do_bwd); note_launches(1); }
   if (do_bwd) {
-    int gw = std::max(1, std::min(cdiv(max_nelim, 8), 128));
-    { k_bwd_l21<T><<<dim3(gw, nn), 256, 0, s>>>(sn, nodes, nrhs); note_launches(1); }
-    const int steps = cdiv(max_nelim, SB);
-    for (int st = steps - 1; st >= 0; --st) {
-      { k_bwd_diag<T><<<nn, 256, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
-      if (st > 0) {
-        int gu = std::max(1, std::min(cdiv(st * SB, 8), 128));
-        { k_bwd_update<T><<<dim3(gu, nn), 256, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
+    with_nr(nrhs, [&](auto nrc) {
+      constexpr int NR = decltype(nrc)::value;
+      int gw = std::max(1, std::min(cdiv(max_nelim, 8), 128));
+      pmark(tm, kPhBwdL21, s);
+      { k_bwd_l21<T, NR><<<dim3(gw, nn), 256, 0, s>>>(sn, nodes, nrhs); note_launches(1); }
+      const int steps = cdiv(max_nelim, SB);
+      for (int st = steps - 1; st >= 0; --st) {
+        pmark(tm, kPhBwdDiag, s);
+        { k_bwd_diag<T, NR><<<nn, 64, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
+        if (st > 0) {
+          int gu = std::max(1, std::min(cdiv(st * SB, 8), 128));
+          pmark(tm, kPhBwdUpdate, s);
+          { k_bwd_update<T, NR><<<dim3(gu, nn), 256, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
+        }
       }
-    }
+    });
   }
   int gs = std::max(1, std::min(cdiv(max_nelim * nrhs, 256), 64));
+  pmark(tm, kPhBwdScatter, s);
   { k_fwd_scatter<T><<<dim3(gs, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs); note_launches(1); }
 }
 
@@ -307,11 +361,11 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
   template void launch_fwd_gather<T>(const SolveNode<T>*, const int*, int, const int*,         \
                                      const double*, int, int, cudaStream_t);                   \
   template void launch_fwd_steps<T>(const SolveNode<T>*, const int*, int, int, int, int,       \
-                                    cudaStream_t);                                             \
+                                    cudaStream_t, PhaseTimer*);                                \
   template void launch_fwd_scatter<T>(const SolveNode<T>*, const int*, int, double*, int, int, \
                                       int, cudaStream_t);                                      \
   template void launch_bwd<T>(const SolveNode<T>*, const int*, int, double*, int, int, int, int, \
-                              bool, bool, cudaStream_t);
+                              bool, bool, cudaStream_t, PhaseTimer*);
 INST(double)
 INST(float)
 #undef INST

@@ -17,7 +17,7 @@
 namespace ssids300 {
 
 constexpr int kBlk = 32;         // APP inner block (ldlt_app.cxx:41 INNER_BLOCK_SIZE)
-constexpr int kApplyRows = 128;  // rows per apply/fixup CTA
+constexpr int kApplyRows = 64;   // rows per apply/fixup CTA
 constexpr int kGemmTile = 64;    // SIMT GEMM tile
 
 // Error codes written to the device status word (host maps to SSIDS flags).
@@ -64,6 +64,30 @@ struct Stats {  // device-side reduction target (integers only -> deterministic)
 // Count of kernels launched by this library (reported by the benchmark).
 void note_launches(int k);
 
+// Optional per-phase device timing: a CUDA event is recorded before each
+// kernel of interest (and at the end); the time between consecutive events
+// is attributed to the phase of the earlier one.  Only used when profiling.
+enum Phase : int {
+  kPhZero = 0, kPhLoadA, kPhInitPerm, kPhDelays, kPhAssemble, kPhDiag, kPhRowPerm, kPhApply,
+  kPhFixup, kPhPanel, kPhSwap, kPhFinish, kPhTpp, kPhCalcLd, kPhContrib, kPhStats, kPhHost,
+  kPhFwdGather = 20, kPhFwdDiag, kPhFwdUpdate, kPhFwdScatter, kPhBwdGather, kPhBwdL21,
+  kPhBwdDiag, kPhBwdUpdate, kPhBwdScatter, kPhResid, kPhAxpy, kPhCount = 32
+};
+struct PhaseTimer {
+  cudaEvent_t* ev = nullptr;
+  int* ph = nullptr;
+  int cap = 0, used = 0;
+  double ms[kPhCount] = {0};
+  long long cnt[kPhCount] = {0};
+  void mark(int phase, cudaStream_t s);
+  void flush();  // after a stream synchronisation
+  void reset();
+  ~PhaseTimer();
+};
+inline void pmark(PhaseTimer* t, int phase, cudaStream_t s) {
+  if (t) t->mark(phase, s);
+}
+
 // ---------------- launchers (defined in the kernel .cu files) --------------
 // assembly (assemble_kernels.cu)
 template <typename T>
@@ -83,7 +107,7 @@ void launch_assemble_contrib(const FrontDesc<T>* fd, const int4* cols, int ncols
 template <typename T>
 void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int step,
                      int max_rows, int max_trail_rows, int max_trail_cols, bool action,
-                     double u, double small, cudaStream_t s);
+                     double u, double small, cudaStream_t s, PhaseTimer* tm);
 template <typename T>
 void launch_app_finish(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf,
                        cudaStream_t s);
@@ -123,8 +147,8 @@ struct SolveNode {
   const int* opos;   // n: original position of each final front position
   const int* rows;   // rlist of the node (0-based pivot positions), nrow entries
   const int* rdir;   // cm entries: parent position of each contribution row
-  double* xloc;      // m x nrhs
-  double* xorig;     // m x nrhs scratch (forward gather)
+  T* xloc;           // m x nrhs, in the factor precision
+  T* xorig;          // m x nrhs scratch (forward gather)
   int m, n, ld, nelim, ncol, nrow, ndelay_in, cm;
   int sptr0;         // first own pivot
   int child_beg, child_end;  // into the child arrays
@@ -139,12 +163,13 @@ void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const i
                        const double* x, int ldx, int nrhs, cudaStream_t s);
 template <typename T>
 void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_nelim,
-                      int max_m, int nrhs, cudaStream_t s);
+                      int max_m, int nrhs, cudaStream_t s, PhaseTimer* tm);
 template <typename T>
 void launch_fwd_scatter(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx,
                         int nrhs, int max_nelim, cudaStream_t s);
 template <typename T>
 void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx, int nrhs,
-                int max_m, int max_nelim, bool do_diag, bool do_bwd, cudaStream_t s);
+                int max_m, int max_nelim, bool do_diag, bool do_bwd, cudaStream_t s,
+                PhaseTimer* tm);
 
 }  // namespace ssids300

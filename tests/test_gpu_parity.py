@@ -191,3 +191,24 @@ def test_gpu_mixed_precision_refined(k):
     assert M.scaled_bwd_error(p, r, v, x, b).max() <= BWD_TOL
     xd, _ = ssids.factor(ak, v)
     assert _rel(x, xd.solve(b)) < SOL_TOL
+
+
+def test_gpu_recip_within_one_ulp():
+    """The Newton reciprocal on the pivot-decision path agrees with IEEE
+    division to one unit in the last place (and exactly at special values)."""
+    torch = pytest.importorskip("torch")
+    from spral_gb300 import _native
+    rng = np.random.default_rng(7)
+    x = np.concatenate([rng.uniform(-1, 1, 4000) * 10.0 ** rng.integers(-40, 40, 4000),
+                        np.array([1.0, -1.0, 3.0, 1e-20, 1e20, 2.0 ** -100, 2.0 ** 100,
+                                  1e-300, 1e300, 0.0, np.inf, -np.inf])])
+    xd = torch.tensor(x, dtype=torch.float64, device="cuda")
+    yd = torch.empty_like(xd)
+    assert _native.lib().spral_ssids_gpu_recip_probe(xd.data_ptr(), yd.data_ptr(), len(x)) == 0
+    y = yd.cpu().numpy()
+    with np.errstate(divide="ignore"):
+        ref = 1.0 / x
+    fin = np.isfinite(ref) & (ref != 0)
+    ulp = np.spacing(np.abs(ref[fin]))
+    assert np.all(np.abs(y[fin] - ref[fin]) <= ulp)
+    assert np.array_equal(y[~fin], ref[~fin])
