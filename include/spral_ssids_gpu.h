@@ -168,6 +168,26 @@ void spral_ssids_gpu_phase_times(const void* numeric, double* ms, long long* cou
  * values (device pointers), for accuracy tests against IEEE division. */
 int spral_ssids_gpu_recip_probe(const double* x_dev, double* y_dev, int n);
 
+/* Dense LDL^T with a-posteriori threshold pivoting of one front, all
+ * pointers in device memory: the per-front kernel of the factorization as a
+ * stand-alone call.  Counterpart of ldlt_app_factor
+ * (src/ssids/cpu/kernels/ldlt_app.cxx:2506) followed by the TPP finish of
+ * factor_node_indef (src/ssids/cpu/factor.hxx:38-110); on the GPU path,
+ * node_ldlt (src/ssids/gpu/dense_factor.f90:28).
+ *   a (m x n, lda >= m): lower part of the n fully-summed columns and the
+ *     rows below; on exit L (unit diagonal) of the nelim eliminated columns
+ *     followed by the failed (delayed) columns, updated;
+ *   d (2n): D^{-1} in the reference format; perm (n): labels, permuted;
+ *   upd ((m-n) x (m-n), ldupd >= m-n) or NULL: upd = beta*upd - L21 D L21^T
+ *     (beta 0 or 1), e.g. the trailing block of a with ldupd = lda.
+ * Returns nelim, or a negative SSIDS flag (-5 singular with action false,
+ * -50 allocation, -51 CUDA).  Allocates its workspace with cudaMalloc and
+ * synchronises the stream before returning. */
+int spral_ssids_gpu_ldlt_app_factor(int m, int n, int* perm_dev, double* a_dev, int lda,
+                                    double* d_dev, double beta, double* upd_dev, int ldupd,
+                                    const struct spral_ssids_cpu_factor_options* options,
+                                    void* stream);
+
 /* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
 int spral_ssids_gpu_device_count(void);
 

@@ -93,3 +93,5 @@ def _declare(L):
     f("spral_ssids_gpu_fp64_peak_tflops", D, I)
     f("spral_ssids_gpu_phase_times", None, P, P, P)
     f("spral_ssids_gpu_recip_probe", I, P, P, I)
+    f("spral_ssids_gpu_ldlt_app_factor", I, I, I, P, P, I, P, D, P, I,
+      ctypes.POINTER(CpuFactorOptions), P)

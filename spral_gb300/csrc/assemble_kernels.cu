@@ -91,13 +91,13 @@ __global__ void k_assemble_contrib(const FrontDesc<T>* fds, const int4* cols, co
   const FrontDesc<T> fp = fds[cw.x];
   const int P = cw.y;
   const bool into_l = P < fp.ncol;
-  T* dst = into_l ? fp.L + (int64_t)P * fp.ld : fp.C + (int64_t)(P - fp.ncol) * fp.cm;
+  T* dst = into_l ? fp.L + (int64_t)P * fp.ld : fp.C + (int64_t)(P - fp.ncol) * fp.ldc;
   for (int q = cw.z; q < cw.w; ++q) {
     const int2 pr = pairs[q];
     const FrontDesc<T> fc = fds[pr.x];
     const int jc = pr.y;
     const int cmc = fc.cm;
-    const T* src = fc.C + (int64_t)jc * cmc;
+    const T* src = fc.C + (int64_t)jc * fc.ldc;
     const int* rd = rdir + rdir_ptr[fc.node];
     for (int ic = jc + threadIdx.x; ic < cmc; ic += blockDim.x) {
       const int Q = rd[ic];

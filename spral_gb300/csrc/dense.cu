@@ -1,0 +1,158 @@
+// Dense LDL^T of one front with a-posteriori threshold pivoting, as a
+// stand-alone entry point (the GPU counterpart of ldlt_app_factor,
+// src/ssids/cpu/kernels/ldlt_app.cxx:2506, and of the GPU path's
+// node_ldlt, src/ssids/gpu/dense_factor.f90:28).  It runs the same APP step
+// kernels, TPP fallback and contribution update as the tree factorization,
+// on one front held by the caller in device memory.
+#include <algorithm>
+#include <cstdio>
+
+#include "spral_ssids_gpu.h"
+#include "ssids_gpu.cuh"
+
+namespace ssids300 {
+
+namespace {
+
+__global__ void k_iota(int* v, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = i;
+}
+
+__global__ void k_zero_upd(double* upd, int ldupd, int cm) {
+  const int64_t tot = (int64_t)cm * cm;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot;
+       e += (int64_t)gridDim.x * blockDim.x)
+    upd[(e / cm) * ldupd + e % cm] = 0.0;
+}
+
+inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+}  // namespace
+
+// Workspace carve-up for one front (sizes in bytes, 256-aligned pieces).
+struct DenseWorkspace {
+  FrontDesc<double>* desc;
+  FrontState* state;
+  int* front0;
+  int* opos;
+  int* lperm;
+  double* step;
+  double* W;
+  double* swapbuf;
+  double* LD;
+};
+
+static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+size_t dense_workspace_bytes(int m, int n, int lda) {
+  const int cm = m - n;
+  return align256(sizeof(FrontDesc<double>)) + align256(sizeof(FrontState)) + align256(sizeof(int)) +
+         align256(sizeof(int) * (size_t)std::max(n, 1)) + align256(sizeof(int) * kBlk) +
+         align256(sizeof(double) * (kBlk * kBlk + 2 * kBlk + 64)) +
+         align256(sizeof(double) * (size_t)lda * kBlk) +
+         align256(sizeof(double) * ((size_t)lda * 64 + 256)) +
+         align256(sizeof(double) * (size_t)std::max(cm, 0) * std::max(n, 1));
+}
+
+DenseWorkspace dense_workspace_carve(void* base, int m, int n, int lda) {
+  char* p = static_cast<char*>(base);
+  DenseWorkspace w;
+  const int cm = m - n;
+  auto take = [&](size_t b) { char* r = p; p += align256(b); return r; };
+  w.desc = (FrontDesc<double>*)take(sizeof(FrontDesc<double>));
+  w.state = (FrontState*)take(sizeof(FrontState));
+  w.front0 = (int*)take(sizeof(int));
+  w.opos = (int*)take(sizeof(int) * (size_t)std::max(n, 1));
+  w.lperm = (int*)take(sizeof(int) * kBlk);
+  w.step = (double*)take(sizeof(double) * (kBlk * kBlk + 2 * kBlk + 64));
+  w.W = (double*)take(sizeof(double) * (size_t)lda * kBlk);
+  w.swapbuf = (double*)take(sizeof(double) * ((size_t)lda * 64 + 256));
+  w.LD = (double*)take(sizeof(double) * (size_t)std::max(cm, 0) * std::max(n, 1));
+  return w;
+}
+
+// Enqueue the factorization of one front on stream s using workspace w and
+// return nelim (after a synchronisation) or a negative SSIDS flag.
+int dense_factor_run(const DenseWorkspace& w, int m, int n, int* perm, double* a, int lda,
+                     double* d, double beta, double* upd, int ldupd,
+                     const spral_ssids_cpu_factor_options& co, cudaStream_t s) {
+  FrontDesc<double> h{};
+  h.L = a;
+  h.D = d;
+  h.perm = perm;
+  h.opos = w.opos;
+  h.C = (m > n) ? upd : nullptr;
+  h.W = w.W;
+  h.step = w.step;
+  h.lperm = w.lperm;
+  h.swapbuf = w.swapbuf;
+  h.LD = w.LD;
+  h.m = m; h.n = n; h.ld = lda;
+  h.nrow = m; h.ncol = n; h.ndelay_in = 0; h.cm = m - n;
+  h.node = 0;
+  h.ldc = ldupd;
+  const int zero = 0;
+  if (cudaMemcpyAsync(w.desc, &h, sizeof(h), cudaMemcpyHostToDevice, s) != cudaSuccess) return -51;
+  if (cudaMemcpyAsync(w.front0, &zero, sizeof(int), cudaMemcpyHostToDevice, s) != cudaSuccess) return -51;
+  if (cudaMemsetAsync(w.state, 0, sizeof(FrontState), s) != cudaSuccess) return -51;
+  k_iota<<<std::max(1, std::min(cdiv(n, 256), 64)), 256, 0, s>>>(w.opos, n);
+  note_launches(1);
+  if (m > n && upd && beta == 0.0) {
+    k_zero_upd<<<std::max(1, std::min(cdiv((m - n) * (m - n), 256), 1024)), 256, 0, s>>>(upd, ldupd, m - n);
+    note_launches(1);
+  }
+  const bool use_app = co.pivot_method != 3;
+  if (use_app) {
+    const int steps = cdiv(n, kBlk);
+    for (int st = 0; st < steps; ++st)
+      launch_app_step<double>(w.desc, w.state, w.front0, 1, st, std::max(m - kBlk * st, 1),
+                              m - kBlk * (st + 1), n - kBlk * (st + 1), co.action, co.u,
+                              co.small, s, nullptr);
+  }
+  launch_app_finish<double>(w.desc, w.state, w.front0, 1, s);
+  const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
+  launch_tpp<double>(w.desc, w.state, w.front0, 1, co.action, co.u, co.small, tpp_all, s);
+  if (m > n && upd) {
+    launch_calc_ld<double>(w.desc, w.state, w.front0, 1, m - n, s);
+    launch_contrib_gemm<double>(w.desc, w.state, w.front0, 1, m - n, s);
+  }
+  FrontState hs{};
+  if (cudaMemcpyAsync(&hs, w.state, sizeof(FrontState), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return -51;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -51;
+  if (hs.status == kDevSingular) return -5;
+  if (hs.status != kDevOk) return -51;
+  return hs.nelim;
+}
+
+}  // namespace ssids300
+
+using namespace ssids300;
+
+extern "C" {
+
+int spral_ssids_gpu_ldlt_app_factor(int m, int n, int* perm_dev, double* a_dev, int lda,
+                                    double* d_dev, double beta, double* upd_dev, int ldupd,
+                                    const struct spral_ssids_cpu_factor_options* options,
+                                    void* stream) {
+  if (m < n || n < 0) return -1;
+  if (lda < m) return -4;
+  if (m > n && upd_dev && ldupd < m - n) return -9;
+  if (n == 0) return 0;
+  spral_ssids_cpu_factor_options co{};
+  co.action = true; co.small = 1e-20; co.u = 0.01; co.pivot_method = 2; co.failed_pivot_method = 1;
+  if (options) co = *options;
+  cudaStream_t s = (cudaStream_t)stream;
+  void* base = nullptr;
+  const size_t bytes = dense_workspace_bytes(m, n, lda);
+  if (cudaMalloc(&base, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return -50;
+  }
+  DenseWorkspace w = dense_workspace_carve(base, m, n, lda);
+  int r = dense_factor_run(w, m, n, perm_dev, a_dev, lda, d_dev, beta, upd_dev, ldupd, co, s);
+  cudaFree(base);
+  return r;
+}
+
+}  // extern "C"

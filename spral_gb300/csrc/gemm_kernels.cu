@@ -35,7 +35,7 @@ __device__ __forceinline__ bool make_job(const FrontDesc<T>& fd, const FrontStat
     j.C = fd.C;
     j.A = fd.L + fd.n;
     j.B = fd.LD;
-    j.ldc = cm; j.lda = fd.ld; j.ldb = cm;
+    j.ldc = fd.ldc; j.lda = fd.ld; j.ldb = cm;
     j.M = cm; j.N = cm;
     j.K = st.nelim;
   }

@@ -18,7 +18,8 @@ __global__ void k_zero_fronts(FrontDesc<T>* fds, const int* fronts) {
   const int64_t nc = (int64_t)fd.cm * fd.cm;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += stride) fd.L[i] = T(0);
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nc; i += stride) fd.C[i] = T(0);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nc; i += stride)
+    fd.C[(i / fd.cm) * fd.ldc + i % fd.cm] = T(0);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 2 * fd.n; i += stride) fd.D[i] = 0.0;
 }
 

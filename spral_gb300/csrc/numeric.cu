@@ -534,6 +534,7 @@ struct Numeric : NumericBase {
         d.nrow = S->nrow[node]; d.ncol = S->ncol[node];
         d.ndelay_in = ndin_[f];
         d.cm = S->nrow[node] - S->ncol[node];
+        d.ldc = d.cm;
         d.node = node;
         d.L = (T*)farena.alloc((size_t)ld * n * sizeof(T));
         d.D = (double*)darena.alloc((size_t)2 * n * sizeof(double) + 16);

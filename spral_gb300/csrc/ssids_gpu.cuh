@@ -42,7 +42,7 @@ struct FrontDesc {
   int m, n, ld;  // rows, fully-summed columns (incl. delays), leading dim
   int nrow, ncol, ndelay_in, cm;
   int node;
-  int pad;
+  int ldc;       // leading dimension of C (cm for the tree's own blocks)
 };
 
 struct FrontState {
