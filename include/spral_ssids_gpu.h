@@ -188,6 +188,25 @@ int spral_ssids_gpu_ldlt_app_factor(int m, int n, int* perm_dev, double* a_dev, 
                                     const struct spral_ssids_cpu_factor_options* options,
                                     void* stream);
 
+/* No counterpart in the reference.  The same factorization as
+ * spral_ssids_gpu_ldlt_app_factor for callers that must not allocate device
+ * memory at factorization time (memory owned by another allocator, a budget
+ * fixed at load time, or a latency-critical path where cudaMalloc/cudaFree
+ * can stall the device): the workspace is a fixed 3 MiB device array inside
+ * the library, present on every GPU that loads it until the process exits.
+ * lda <= 1024 (so m <= 1024); larger fronts return
+ * SPRAL_SSIDS_GPU_NOALLOC_TOO_LARGE.  The first call on a device looks up
+ * the array's device address and should come before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  Calls no cudaMalloc, cudaFree or allocating
+ * library routine. */
+#define SPRAL_SSIDS_GPU_NOALLOC_TOO_LARGE (-60)
+int spral_ssids_gpu_ldlt_app_factor_noalloc(int m, int n, int* perm_dev, double* a_dev, int lda,
+                                            double* d_dev, double beta, double* upd_dev,
+                                            int ldupd,
+                                            const struct spral_ssids_cpu_factor_options* options,
+                                            void* stream);
+
 /* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
 int spral_ssids_gpu_device_count(void);
 

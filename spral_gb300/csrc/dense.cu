@@ -156,3 +156,99 @@ int spral_ssids_gpu_ldlt_app_factor(int m, int n, int* perm_dev, double* a_dev, 
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Variant of spral_ssids_gpu_ldlt_app_factor that allocates nothing.
+//
+// Some callers cannot call cudaMalloc at the point where they factor a
+// front: their device memory may belong to another allocator (a framework's
+// caching pool that has reserved most of the GPU), their memory budget may be
+// fixed when the library is loaded, or they sit on a latency-critical path
+// where cudaMalloc/cudaFree can stall the whole device.  For them the
+// workspace lives in one fixed device array that is part of this library's
+// image: every GPU that loads the library holds it until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+// Largest leading dimension (hence front height m) the fixed scratch serves.
+constexpr int kNoAllocMaxLda = 1024;
+// Workspace of the largest front: desc/state/index pieces, opos, step
+// buffers, W (lda x 32), column-move buffer (64 x lda) and L*D for the
+// contribution rows ((m-n) x n, largest at n = m/2).  3 MiB holds it.
+constexpr size_t kNoAllocScratchBytes = size_t(3) << 20;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device.  The host-side
+// symbol g_noalloc_scratch is only a stand-in and must never reach a kernel;
+// the address is looked up once per device, with that device current.
+int noalloc_scratch_address(void** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return -51; }
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return -51;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      cudaGetLastError();
+      fprintf(stderr, "spral_gb300: cannot locate the fixed factorization scratch on device %d: %s\n",
+              dev, cudaGetErrorString(e));
+      return -51;
+    }
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Same arguments and results as spral_ssids_gpu_ldlt_app_factor, but the
+// workspace is the library's fixed device scratch array instead of
+// cudaMalloc'd memory.  Limits and behaviour:
+//  * lda must be at most 1024 (so m <= 1024); larger fronts are refused with
+//    SPRAL_SSIDS_GPU_NOALLOC_TOO_LARGE (-60) and a message on stderr.
+//  * The first call on each device looks up the scratch array's device
+//    address (with that device current); make that first call before any
+//    stream capture begins.
+//  * All calls share the one array and it keeps the previous call's contents;
+//    the per-call state that must start from zero is cleared by each call.
+//    Calls whose GPU work overlaps (different host threads or streams at the
+//    same time on the same device) race on the array: serialise them.
+//  * No cudaMalloc, cudaFree or allocating library routine is called.
+int spral_ssids_gpu_ldlt_app_factor_noalloc(int m, int n, int* perm_dev, double* a_dev, int lda,
+                                            double* d_dev, double beta, double* upd_dev,
+                                            int ldupd,
+                                            const struct spral_ssids_cpu_factor_options* options,
+                                            void* stream) {
+  if (m < n || n < 0) return -1;
+  if (lda < m) return -4;
+  if (m > n && upd_dev && ldupd < m - n) return -9;
+  if (lda > kNoAllocMaxLda || dense_workspace_bytes(m, n, lda) > kNoAllocScratchBytes) {
+    fprintf(stderr,
+            "spral_gb300: front too large for the fixed scratch (lda=%d, limit %d)\n", lda,
+            kNoAllocMaxLda);
+    return -60;
+  }
+  if (n == 0) return 0;
+  void* base = nullptr;
+  const int st = noalloc_scratch_address(&base);
+  if (st != 0) return st;
+  spral_ssids_cpu_factor_options co{};
+  co.action = true; co.small = 1e-20; co.u = 0.01; co.pivot_method = 2; co.failed_pivot_method = 1;
+  if (options) co = *options;
+  DenseWorkspace w = dense_workspace_carve(base, m, n, lda);
+  return dense_factor_run(w, m, n, perm_dev, a_dev, lda, d_dev, beta, upd_dev, ldupd, co,
+                          (cudaStream_t)stream);
+}
+
+}  // extern "C"
