@@ -207,6 +207,21 @@ int spral_ssids_gpu_ldlt_app_factor_noalloc(int m, int n, int* perm_dev, double*
                                             const struct spral_ssids_cpu_factor_options* options,
                                             void* stream);
 
+/* Tensor-core Schur update used by the mixed-precision path, exposed for
+ * tests and measurements: C (M x N, column-major, ldc) -= A B^T with A
+ * (M x K) and B (N x K) column-major FP32 device arrays; 3xTF32 split
+ * products on tcgen05, accumulated in TMEM for at most `chunk` 32-deep
+ * k-tiles (chunk = 0: the whole depth; chunk < 0: the library default) and
+ * then in FP32 registers; lower != 0 updates only r >= c.  With reps > 0 and
+ * ms != NULL the update runs reps times and ms[0], ms[1] receive the mean
+ * split-kernel and GEMM-kernel times in ms.  Returns 0, -1 bad argument,
+ * -50 allocation, -51 CUDA error, -52 pipeline timeout.  No reference
+ * counterpart (the reference's contribution update is FP64 SIMT,
+ * src/ssids/gpu/kernels/syrk.cu:185). */
+int spral_ssids_gpu_tc_gemm_f32(int M, int N, int K, const float* A, int lda, const float* B,
+                                int ldb, float* C, int ldc, int lower, int chunk, int reps,
+                                float* ms);
+
 /* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
 int spral_ssids_gpu_device_count(void);
 

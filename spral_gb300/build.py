@@ -52,7 +52,7 @@ def build(verbose=False):
         objs = list(ex.map(_compile, srcs))
     if os.path.exists(OUT) and all(os.path.getmtime(OUT) >= os.path.getmtime(o) for o in objs):
         return OUT
-    cmd = [NVCC, *ARCH, "-shared", "-o", OUT, *objs, "-lcudart", "-lcuda"]
+    cmd = [NVCC, *ARCH, "-shared", "-o", OUT, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

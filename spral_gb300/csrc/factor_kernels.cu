@@ -356,9 +356,21 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
   __shared__ T l11[kBlk][kBlk + 1];  // l11[j][k] = L(j,k), row-major for broadcast
   __shared__ double dd[2 * kBlk + 2];
   __shared__ int lp[kBlk];
-  for (int i = threadIdx.x; i < kBlk * kBlk; i += blockDim.x) {
-    int c = i / kBlk, r = i % kBlk;
-    l11[r][c] = (r > c && r < bs && c < bs) ? (T)fd.step[c * kBlk + r] : T(0);
+  {
+    // all loads first (one latency), then the shared-memory stores
+    constexpr int PER = kBlk * kBlk / kApplyRows;  // 16
+    double v[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int i = threadIdx.x + k * kApplyRows;
+      const int c = i / kBlk, r = i % kBlk;
+      v[k] = (r > c && r < bs && c < bs) ? fd.step[c * kBlk + r] : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int i = threadIdx.x + k * kApplyRows;
+      l11[i % kBlk][i / kBlk] = (T)v[k];
+    }
   }
   for (int i = threadIdx.x; i < 2 * kBlk + 2; i += blockDim.x)
     dd[i] = (i < 2 * bs) ? fd.step[kBlk * kBlk + i] : 0.0;

@@ -31,6 +31,7 @@ __device__ __forceinline__ bool make_job(const FrontDesc<T>& fd, const FrontStat
     j.N = fd.n - (p + bs);
     j.K = st.npass;
   } else {
+    if (fd.tc) return false;  // formed on the tensor cores instead
     const int cm = fd.m - fd.n;
     j.C = fd.C;
     j.A = fd.L + fd.n;

@@ -21,7 +21,10 @@
 #include <memory>
 #include <new>
 #include <stdexcept>
+#include <type_traits>
 #include <vector>
+
+#include <cstdlib>
 
 #include "spral_ssids_gpu.h"
 #include "ssids_gpu.cuh"
@@ -420,6 +423,40 @@ struct Numeric : NumericBase {
   int* d_children = nullptr;
   DevBuf<T> xloc, xorig;
   DevBuf<double> xbuf, rbuf, dbuf, bbuf, nbuf;
+  // tensor-core contribution GEMM (FP32 factors only)
+  bool use_tc = false;
+  int tc_chunk = kTcChunk;
+  int tc_min_cm = 192;  // smallest contribution block formed on the tensor cores
+  TcBuffers tcbuf;
+  DevBuf<char> tc_scratch;
+  int* d_tc_status = nullptr;
+
+  void run_tc_contrib(int f0, int f1, cudaStream_t s) {
+    if (!use_tc) return;
+    std::vector<TcProblem> ps;
+    for (int f = f0; f < f1; ++f) {
+      const FrontDesc<T>& d = hfd[f];
+      if (!d.tc) continue;
+      TcProblem p;
+      p.A = reinterpret_cast<const float*>(d.L + d.n);
+      p.lda = d.ld;
+      p.B = reinterpret_cast<const float*>(d.LD);
+      p.ldb = d.cm;
+      p.C = reinterpret_cast<float*>(d.C);
+      p.ldc = d.ldc;
+      p.M = d.cm;
+      p.N = d.cm;
+      p.kmax = d.n;
+      p.kval_dev = &d_st[f].nelim;
+      p.lower = 1;
+      ps.push_back(p);
+    }
+    if (ps.empty()) return;
+    tc_scratch.ensure(tc_gemm_scratch_bytes(ps));
+    if (tc_gemm_run(ps, tc_scratch.p, tcbuf, d_tc_status, s, tc_chunk) != 0)
+      throw CudaFail{cudaErrorUnknown, __LINE__};
+  }
+
   const double* cur_aval = nullptr;  // device values of the last factor
   double last_bwd_err = 0.0;
   std::vector<cudaEvent_t> pev;
@@ -437,6 +474,15 @@ struct Numeric : NumericBase {
     CK(cudaMalloc(&d_st, std::max(nn, 1) * sizeof(FrontState)));
     CK(cudaMalloc(&d_stats, sizeof(Stats)));
     CK(cudaMalloc(&d_dwork, std::max(nn, 1) * sizeof(int4)));
+    CK(cudaMalloc(&d_tc_status, sizeof(int)));
+    if (std::is_same<T, float>::value) {
+      const char* env = getenv("SPRAL_GB300_TENSOR_CORES");
+      use_tc = !(env && env[0] == '0');
+      const char* ch = getenv("SPRAL_GB300_TC_CHUNK");
+      if (ch) tc_chunk = std::max(0, atoi(ch));
+      const char* mc = getenv("SPRAL_GB300_TC_MIN_CM");
+      if (mc) tc_min_cm = std::max(1, atoi(mc));
+    }
     contrib.ensure(std::max<int64_t>(S->contrib_total, 1));
     // factor storage estimate (no delays) + 10%
     size_t est = 0;
@@ -445,7 +491,7 @@ struct Numeric : NumericBase {
   }
   ~Numeric() override {
     for (auto e : pev) cudaEventDestroy(e);
-    cudaFree(d_fd); cudaFree(d_st); cudaFree(d_stats); cudaFree(d_dwork);
+    cudaFree(d_fd); cudaFree(d_st); cudaFree(d_stats); cudaFree(d_dwork); cudaFree(d_tc_status);
     cudaFree(d_sn); cudaFree(d_children);
     for (auto& e : ev) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
@@ -485,6 +531,7 @@ struct Numeric : NumericBase {
       }
     }
     CK(cudaMemsetAsync(d_st, 0, nn * sizeof(FrontState), s));
+    CK(cudaMemsetAsync(d_tc_status, 0, sizeof(int), s));
     CK(cudaMemsetAsync(d_stats, 0, sizeof(Stats), s));
     lvl_max_m.assign(S->nlev, 0);
     lvl_max_nelim.assign(S->nlev, 0);
@@ -546,6 +593,7 @@ struct Numeric : NumericBase {
         d.LD = ws_LD.p + oL; oL += (size_t)d.cm * n;
         d.step = ws_step.p + (size_t)(f - f0) * (kBlk * kBlk + 2 * kBlk + 64);
         d.lperm = ws_lperm.p + (size_t)(f - f0) * kBlk;
+        d.tc = (use_tc && d.cm >= tc_min_cm) ? 1 : 0;
       }
       CK(cudaMemcpyAsync(d_fd + f0, hfd.data() + f0, nf * sizeof(FrontDesc<T>),
                          cudaMemcpyHostToDevice, s));
@@ -598,6 +646,7 @@ struct Numeric : NumericBase {
       pmark(tm(), kPhContrib, s);
       if (profile) CK(cudaEventRecord(pev[2 * l], s));
       launch_contrib_gemm<T>(d_fd, d_st, fr, nf, max_cm, s);
+      run_tc_contrib(f0, f1, s);
       if (profile) CK(cudaEventRecord(pev[2 * l + 1], s));
       pmark(tm(), kPhStats, s);
       launch_stats<T>(d_fd, d_st, fr, nf, max_n, d_stats, s);
@@ -628,6 +677,11 @@ struct Numeric : NumericBase {
           fl += (double)nelim_[f] * cm * (cm + 1.0);
         }
         if (fl > 0) { prof_ms += ms; prof_flops += fl; prof_launches += 1; }
+      }
+      if (use_tc) {
+        int tcs = 0;
+        CK(cudaMemcpy(&tcs, d_tc_status, sizeof(int), cudaMemcpyDeviceToHost));
+        if (tcs != 0) bad = true;
       }
       if (singular) { stats.flag = -5; return stats.flag; }
       if (bad) { stats.flag = -51; return stats.flag; }

@@ -64,19 +64,31 @@ __global__ void k_fwd_gather(const SolveNode<T>* sns, const int* nodes, const in
   }
 }
 
-// stage the jb x jb diagonal block (strictly lower part) into shared memory
+// stage the jb x jb diagonal block (strictly lower part) into shared memory;
+// every thread issues all of its loads before the first store so that the
+// global-memory latency is paid once, not once per element
+constexpr int kSolveDiagThreads = 256;
 template <typename T>
 __device__ __forceinline__ void load_diag_block(const SolveNode<T>& sn, int j0, int jb,
                                                 T (*Lb)[SB + 1]) {
-  for (int e = threadIdx.x; e < SB * SB; e += blockDim.x) {
+  constexpr int PER = SB * SB / kSolveDiagThreads;  // 16
+  T v[PER];
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int e = threadIdx.x + k * kSolveDiagThreads;
     const int c = e / SB, r = e % SB;
-    Lb[c][r] = (r > c && r < jb && c < jb) ? sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : T(0);
+    v[k] = (r > c && r < jb && c < jb) ? sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : T(0);
+  }
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int e = threadIdx.x + k * kSolveDiagThreads;
+    Lb[e / SB][e % SB] = v[k];
   }
 }
 
 // forward: unit lower triangular solve of rows [j0, j0+jb) in place
 template <typename T, int NR>
-__global__ void __launch_bounds__(64) k_fwd_diag(const SolveNode<T>* sns, const int* nodes,
+__global__ void __launch_bounds__(kSolveDiagThreads) k_fwd_diag(const SolveNode<T>* sns, const int* nodes,
                                                  int step, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.x]];
   const int j0 = step * SB;
@@ -129,6 +141,7 @@ __global__ void k_fwd_update(const SolveNode<T>* sns, const int* nodes, int step
 #pragma unroll
     for (int q = 0; q < NR; ++q) acc[q] = T(0);
     const T* lrow = sn.L + (int64_t)j0 * sn.ld + i;
+#pragma unroll 8
     for (int c = 0; c < jb; ++c) {
       const T l = lrow[(int64_t)c * sn.ld];
 #pragma unroll
@@ -208,7 +221,7 @@ __global__ void k_bwd_l21(const SolveNode<T>* sns, const int* nodes, int nrhs) {
 
 // backward: unit upper (L^T) triangular solve of rows [j0, j0+jb) in place
 template <typename T, int NR>
-__global__ void __launch_bounds__(64) k_bwd_diag(const SolveNode<T>* sns, const int* nodes,
+__global__ void __launch_bounds__(kSolveDiagThreads) k_bwd_diag(const SolveNode<T>* sns, const int* nodes,
                                                  int step, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.x]];
   const int j0 = step * SB;
@@ -307,7 +320,7 @@ void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_
     constexpr int NR = decltype(nrc)::value;
     for (int st = 0; st < steps; ++st) {
       pmark(tm, kPhFwdDiag, s);
-      { k_fwd_diag<T, NR><<<nn, 64, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
+      { k_fwd_diag<T, NR><<<nn, kSolveDiagThreads, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
       int rows = max_m - st * SB;  // upper bound; the kernel derives the exact range
       if (rows > 0) {
         int gx = std::max(1, std::min(cdiv(rows, 128), 128));
@@ -343,7 +356,7 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
       const int steps = cdiv(max_nelim, SB);
       for (int st = steps - 1; st >= 0; --st) {
         pmark(tm, kPhBwdDiag, s);
-        { k_bwd_diag<T, NR><<<nn, 64, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
+        { k_bwd_diag<T, NR><<<nn, kSolveDiagThreads, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
         if (st > 0) {
           int gu = std::max(1, std::min(cdiv(st * SB, 8), 128));
           pmark(tm, kPhBwdUpdate, s);

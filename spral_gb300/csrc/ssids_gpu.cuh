@@ -43,6 +43,8 @@ struct FrontDesc {
   int nrow, ncol, ndelay_in, cm;
   int node;
   int ldc;       // leading dimension of C (cm for the tree's own blocks)
+  int tc;        // contribution block formed by the tensor-core GEMM
+  int pad2;
 };
 
 struct FrontState {
@@ -123,6 +125,40 @@ void launch_contrib_gemm(FrontDesc<T>* fd, FrontState* st, const int* fronts, in
 template <typename T>
 void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
                   int max_n, Stats* stats, cudaStream_t s);
+
+// ---------------- tensor-core Schur update (tc_gemm.cu) ----------------
+// C_i -= A_i B_i^T (lower if requested) with 3xTF32 split products on
+// tcgen05.  A_i: M_i x kmax column-major (lda), B_i: N_i x kmax (ldb); the
+// effective depth may be read from device memory (kval_dev).
+struct TcProblem {
+  const float* A;
+  int lda;
+  const float* B;
+  int ldb;
+  float* C;
+  int ldc, M, N, kmax;
+  const int* kval_dev;
+  int lower;
+};
+struct TcBuffers {  // reusable descriptor staging of tc_gemm_run
+  void* h_stage = nullptr;  // pinned host copy of the descriptors
+  void* d_stage = nullptr;  // device copy
+  size_t cap = 0;
+  cudaEvent_t uploaded = nullptr;  // the last upload from h_stage has completed
+  ~TcBuffers();
+};
+}  // namespace ssids300
+#include <vector>
+namespace ssids300 {
+// Default number of 32-deep k-tiles accumulated in TMEM before the partial
+// sum is added (round-to-nearest) into the register accumulator.
+constexpr int kTcChunk = 8;
+size_t tc_gemm_scratch_bytes(const std::vector<TcProblem>& ps);
+// Returns 0, or a negative code: -1 allocation, -2 tensor-map encoding,
+// -3 launch error.  Device-side pipeline timeouts are reported in *status.
+int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf, int* status,
+                cudaStream_t s, int chunk = kTcChunk, float* ms_split = nullptr,
+                float* ms_gemm = nullptr);
 
 // syrk-like lower update C(r,c) -= sum_k A(r,k) B(c,k), r >= c
 template <typename T>

@@ -1,0 +1,614 @@
+// Contribution-block Schur update on the 5th-generation tensor cores.
+//
+//   C(r, c) -= sum_k A(r, k) B(c, k)      (lower part, r >= c, or full)
+//
+// with A = L21 and B = L21 D of a front (FP32 factors of the mixed-precision
+// path).  FP32-class accuracy comes from split products: each FP32 value x is
+// written as x = hi + lo with hi = tf32(x) and lo = tf32(x - hi), and
+//   A B^T ~ Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T,
+// which is ONE TF32 GEMM over a 3K-deep operand pair
+//   A' = [Ahi | Ahi | Alo],  B' = [Bhi | Blo | Bhi]   (interleaved per k).
+// k_split builds A' and B' K-major (row-major, ld = kpad); k_tc_gemm is a
+// persistent kernel that computes 128 x 256 tiles of the result: it streams
+// 32-deep k-tiles of A' (128 rows) and B' (256 rows) with TMA (128-byte
+// swizzle) through a 4-stage mbarrier pipeline into tcgen05.mma.kind::tf32
+// (M = 128, N = 256, FP32 accumulators in TMEM) and subtracts the result
+// from C.
+//
+// Accumulation: the tensor cores accumulate at most `chunk` k-tiles
+// (32 * chunk split products) in TMEM; the epilogue warps then add that
+// partial sum into registers with round-to-nearest FP32 adds.  This keeps
+// the tensor cores' internal accumulation short and recovers FP32-class
+// accuracy for deep updates (the contribution of a front with nelim
+// eliminated columns is 3 * nelim split products deep).
+//
+// Every mbarrier wait is bounded; on timeout the CTA records an error in
+// the status word, waits (bounded) for its in-flight copies and MMAs, frees
+// its TMEM and returns.
+#include <cuda.h>
+#include <cstdint>
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "ssids_gpu.cuh"
+
+namespace ssids300 {
+
+namespace {
+
+constexpr int TC_M = 128, TC_N = 256, TC_K = 32;  // K = 32 fp32 = 128 bytes
+constexpr int TC_STAGES = 4;
+constexpr int TC_A_BYTES = TC_M * TC_K * 4;  // 16 KiB of A' per stage
+constexpr int TC_B_BYTES = TC_N * TC_K * 4;  // 32 KiB of B' per stage
+constexpr uint32_t TC_TMEM_COLS = 2 * TC_N;  // two FP32 accumulators = all of TMEM
+constexpr int TC_EPI_WARPS = 8;              // two per TMEM lane quarter
+constexpr int TC_EPI_THREADS = 32 * TC_EPI_WARPS;
+constexpr int TC_THREADS = 64 + TC_EPI_THREADS;
+// try_wait rounds before a wait gives up (each round may suspend briefly);
+// no legitimate wait in the pipeline comes close
+constexpr long long TC_WAIT_LIMIT = 1LL << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Bounded wait for the phase with the given parity.  Gives up (returns
+// false) after TC_WAIT_LIMIT rounds, setting the CTA's abort flag, or as
+// soon as another role has set it.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  const uint32_t a = smem_u32(bar);
+  for (long long it = 0; it < TC_WAIT_LIMIT; ++it) {
+    if (mbar_try(a, parity)) return true;
+    if ((it & 31) == 31 && *abort) return false;
+  }
+  *abort = 1;
+  return false;
+}
+
+// Bounded wait that ignores the abort flag (used to drain after an abort).
+__device__ __forceinline__ bool mbar_wait_plain(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (long long it = 0; it < TC_WAIT_LIMIT; ++it)
+    if (mbar_try(a, parity)) return true;
+  return false;
+}
+
+// arrive on `bar` once every tcgen05 operation issued so far by this thread
+// has completed
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes (one lane per thread)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of
+// 1024 bytes (stride byte offset), descriptor version 1
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;                  // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;        // stride byte offset
+  d |= (uint64_t)1 << 46;                  // version
+  d |= (uint64_t)2 << 61;                  // 128-byte swizzle
+  return d;
+}
+
+// instruction descriptor: D = F32, A = B = TF32, both K-major, N = TC_N, M = 128
+__host__ __device__ constexpr uint32_t idesc_tf32() {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+         ((uint32_t)(TC_M >> 4) << 24);
+}
+
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Split operands.  For row r < rows and k < kval: dst[r*ld + 3k + {0,1,2}] =
+// (hi, hi, lo) of src(r, k) for the A side, (hi, lo, hi) for the B side;
+// columns [3*kval, kpad) are zero.  src is column-major (ld_src).
+// ---------------------------------------------------------------------------
+struct SplitJob {
+  const float* src;
+  float* dst;
+  int rows, kval, kpad, ld_src, ld_dst, is_b;
+  const int* kval_dev;  // nullptr or device-side effective depth (<= kval)
+};
+
+__global__ void k_split(const SplitJob* jobs) {
+  const SplitJob j = jobs[blockIdx.z];
+  __shared__ float tile[32][33];
+  const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  if (r0 >= j.rows || 3 * k0 >= j.kpad) return;  // uniform per CTA
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  const int kval = j.kval_dev ? min(j.kval, *j.kval_dev) : j.kval;
+  for (int i = ty; i < 32; i += 8) {
+    const int r = r0 + tx, k = k0 + i;
+    tile[i][tx] = (r < j.rows && k < kval) ? j.src[(int64_t)k * j.ld_src + r] : 0.f;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int r = r0 + i;
+    if (r >= j.rows) continue;
+    const int k = k0 + tx;
+    if (3 * k >= j.kpad) continue;
+    const float x = tile[tx][i];
+    const float hi = to_tf32(x);
+    const float lo = to_tf32(x - hi);
+    float* d = j.dst + (int64_t)r * j.ld_dst + 3 * k;
+    // columns past kpad belong to the next row: write only inside the row
+    d[0] = hi;
+    if (3 * k + 1 < j.kpad) d[1] = j.is_b ? lo : hi;
+    if (3 * k + 2 < j.kpad) d[2] = j.is_b ? hi : lo;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GEMM jobs: one per front; the tiles of all results are enumerated by the
+// host into one flat list (job index, tile row, tile col), longest first.
+// ---------------------------------------------------------------------------
+struct TcJob {
+  float* C;
+  int ldc, M, N;
+  int kpad;        // depth of A', B' (multiple of 32)
+  int lower;       // 1: only r >= c is updated
+  const int* kval; // nullptr or device pointer: effective depth = 3 * (*kval)
+};
+
+__device__ __forceinline__ int tile_ktiles(const TcJob& j) {
+  int kd = j.kpad;
+  if (j.kval) kd = min(kd, 3 * max(*j.kval, 0));
+  return (kd + TC_K - 1) / TC_K;
+}
+
+// Persistent kernel, one CTA per SM, 320 threads:
+//   warp 0 lane 0   TMA producer (A' and B' k-tiles into a TC_STAGES ring)
+//   warp 1 lane 0   MMA issuer (tcgen05.mma into one of two TMEM accumulators)
+//   warps 2..9      accumulate / epilogue (warp w reads TMEM lanes 32*(w%4)..)
+// The k range of a tile is cut into chunks of `chunk` k-tiles (0 = one chunk).
+// Each chunk is accumulated by the tensor cores in a fresh TMEM accumulator;
+// the epilogue warps add it, rounding to nearest, into a per-thread register
+// row of the tile, so the tensor cores' own accumulation spans at most
+// 32 * chunk products.  Two accumulators let the MMAs of the next chunk (or
+// tile) run while the previous one is drained.
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_tc_gemm(const TcJob* jobs, const int4* tiles, int ntiles, const CUtensorMap* maps,
+              int chunk, int* status) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  unsigned char* sA = smem;
+  unsigned char* sB = smem + TC_STAGES * TC_A_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + TC_STAGES * (TC_A_BYTES + TC_B_BYTES));
+  uint64_t* empty = full + TC_STAGES;
+  uint64_t* accf = empty + TC_STAGES;  // accumulator b holds a finished chunk
+  uint64_t* acce = accf + 2;           // accumulator b has been drained
+  uint64_t* drain = acce + 2;          // all MMAs of this CTA have completed
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  int* s_abort = reinterpret_cast<int*>(tmem_slot + 1);
+  int* s_issued = s_abort + 1;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+    for (int b = 0; b < 2; ++b) { mbar_init(&accf[b], 1); mbar_init(&acce[b], TC_EPI_THREADS); }
+    mbar_init(drain, 1);
+    *s_abort = 0;
+    *s_issued = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(TC_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+  volatile int* abort_flag = s_abort;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- producer ----
+      uint32_t it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int4 tl = tiles[t];
+        const int nk = tile_ktiles(jobs[tl.x]);
+        const CUtensorMap* mapA = maps + 2 * tl.x;
+        const CUtensorMap* mapB = mapA + 1;
+        for (int kt = 0; kt < nk; ++kt, ++it) {
+          const uint32_t s = it % TC_STAGES;
+          if (it >= (uint32_t)TC_STAGES &&
+              !mbar_wait(&empty[s], ((it / TC_STAGES) - 1) & 1, abort_flag)) {
+            ok = false;
+            break;
+          }
+          mbar_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
+          tma_load_2d(sA + s * TC_A_BYTES, mapA, kt * TC_K, tl.y * TC_M, &full[s]);
+          tma_load_2d(sB + s * TC_B_BYTES, mapB, kt * TC_K, tl.z * TC_N, &full[s]);
+        }
+      }
+      *s_issued = (int)it;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      const uint32_t idesc = idesc_tf32();
+      uint32_t it = 0, ch = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int nk = tile_ktiles(jobs[tiles[t].x]);
+        const int per = chunk > 0 ? chunk : max(nk, 1);
+        for (int k0 = 0; k0 < nk && ok; k0 += per, ++ch) {
+          const uint32_t b = ch & 1;
+          if (ch >= 2 && !mbar_wait(&acce[b], ((ch >> 1) - 1) & 1, abort_flag)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t dacc = tmem + b * TC_N;
+          const int k1 = min(nk, k0 + per);
+          for (int kt = k0; kt < k1; ++kt, ++it) {
+            const uint32_t s = it % TC_STAGES;
+            if (!mbar_wait(&full[s], (it / TC_STAGES) & 1, abort_flag)) { ok = false; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t a0 = smem_u32(sA + s * TC_A_BYTES);
+            const uint32_t b0 = smem_u32(sB + s * TC_B_BYTES);
+#pragma unroll
+            for (int kk = 0; kk < TC_K / 8; ++kk) {  // 8 tf32 = 32 bytes per MMA
+              const uint64_t ad = smem_desc_sw128(a0 + kk * 32);
+              const uint64_t bd = smem_desc_sw128(b0 + kk * 32);
+              const uint32_t acc = (kt > k0 || kk > 0) ? 1u : 0u;
+              asm volatile(
+                  "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                  " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dacc),
+                  "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            }
+            // stage s is free once these MMAs have read it
+            mma_commit(&empty[s]);
+          }
+          if (ok) mma_commit(&accf[b]);
+        }
+      }
+      // every MMA issued above has completed once `drain` flips
+      mma_commit(drain);
+      (void)mbar_wait_plain(drain, 0);
+    }
+  } else {
+    // ---- accumulate + epilogue ----
+    // warp w (2..9) reads TMEM lane quarter w % 4 and owns the 128-column
+    // half (w - 2) / 4 of the tile: one register row of 128 sums per thread
+    const int q = warp & 3;
+    const int half = (warp - 2) >> 2;
+    uint32_t ch = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      const int4 tl = tiles[t];
+      const TcJob job = jobs[tl.x];
+      const int nk = tile_ktiles(job);
+      if (nk == 0) continue;
+      const int per = chunk > 0 ? chunk : nk;
+      float acc[128];
+#pragma unroll
+      for (int j = 0; j < 128; ++j) acc[j] = 0.f;
+      for (int k0 = 0; k0 < nk; k0 += per, ++ch) {
+        const uint32_t b = ch & 1;
+        // the TMEM loads below are warp-collective: decide as a warp
+        const bool got = mbar_wait(&accf[b], (ch >> 1) & 1, abort_flag);
+        if (!__all_sync(0xffffffffu, got)) { *abort_flag = 1; ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + b * TC_N + half * 128;
+#pragma unroll
+        for (int cb = 0; cb < 128; cb += 16) {
+          uint32_t v[16];
+          tmem_ld16(base + (uint32_t)cb, v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) acc[cb + j] += __uint_as_float(v[j]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        mbar_arrive(&acce[b]);
+      }
+      if (!ok) break;
+      const int r = tl.y * TC_M + q * 32 + lane;
+      if (r < job.M) {
+        const int col0 = tl.z * TC_N + half * 128;
+        float* crow = job.C + r;
+        // 8 columns at a time: all loads in flight before the stores
+        const int64_t ldc = job.ldc;
+        const float* cbase = crow + col0 * ldc;
+#pragma unroll
+        for (int cb = 0; cb < 128; cb += 8) {
+          float cv[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int c = col0 + cb + j;
+            cv[j] = (c < job.N && (!job.lower || r >= c)) ? cbase[(cb + j) * ldc] : 0.f;
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int c = col0 + cb + j;
+            if (c < job.N && (!job.lower || r >= c))
+              const_cast<float*>(cbase)[(cb + j) * ldc] = cv[j] - acc[cb + j];
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (*abort_flag) {
+    if (threadIdx.x == 0) {
+      atomicExch(status, kDevBadState);
+      // let the copies still in flight land before shared memory is released
+      const int issued = *s_issued;
+      for (int it = max(0, issued - TC_STAGES); it < issued; ++it)
+        (void)mbar_wait_plain(&full[it % TC_STAGES], (it / TC_STAGES) & 1);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TC_TMEM_COLS));
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+// The tensor-map encoder is a driver entry point; it is looked up through the
+// runtime so that the library does not link the driver library directly
+// (hosts without a GPU driver can still load it for the CPU-side tests).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+static CUresult encode_kmajor(CUtensorMap* map, const float* base, int rows, int kpad, int ld,
+                              int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return CUDA_ERROR_NOT_FOUND;
+  cuuint64_t gdim[2] = {(cuuint64_t)kpad, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)ld * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)TC_K, (cuuint32_t)box_rows};
+  cuuint32_t estride[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, gdim, gstride, box, estride,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+}
+
+size_t tc_gemm_smem_bytes() {
+  return 1024 + TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + (2 * TC_STAGES + 5) * 8 + 16;
+}
+
+
+size_t tc_gemm_scratch_bytes(const std::vector<TcProblem>& ps) {
+  size_t b = 0;
+  for (auto& p : ps) {
+    const size_t kpad = (size_t)((3 * p.kmax + TC_K - 1) / TC_K) * TC_K;
+    b += ((size_t)p.M * kpad * 4 + 255) / 256 * 256;
+    b += ((size_t)p.N * kpad * 4 + 255) / 256 * 256;
+  }
+  return b + 256;
+}
+
+TcBuffers::~TcBuffers() {
+  if (uploaded) cudaEventSynchronize(uploaded);
+  cudaFreeHost(h_stage);
+  cudaFree(d_stage);
+  if (uploaded) cudaEventDestroy(uploaded);
+}
+
+static size_t up64(size_t b) { return (b + 63) & ~size_t(63); }
+
+int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf, int* status,
+                cudaStream_t s, int chunk, float* ms_split, float* ms_gemm) {
+  if (ps.empty()) return 0;
+  std::vector<SplitJob> sj;
+  std::vector<TcJob> jobs;
+  std::vector<int4> tiles;
+  std::vector<CUtensorMap> maps;
+  char* sp = static_cast<char*>(scratch);
+  sp = (char*)(((uintptr_t)sp + 255) & ~(uintptr_t)255);
+  int maxr = 0, maxk = 0;
+  for (size_t i = 0; i < ps.size(); ++i) {
+    const TcProblem& p = ps[i];
+    const int kpad = (3 * p.kmax + TC_K - 1) / TC_K * TC_K;
+    float* a2 = (float*)sp; sp += ((size_t)p.M * kpad * 4 + 255) / 256 * 256;
+    float* b2 = (float*)sp; sp += ((size_t)p.N * kpad * 4 + 255) / 256 * 256;
+    sj.push_back({p.A, a2, p.M, p.kmax, kpad, p.lda, kpad, 0, p.kval_dev});
+    sj.push_back({p.B, b2, p.N, p.kmax, kpad, p.ldb, kpad, 1, p.kval_dev});
+    maxr = std::max(maxr, std::max(p.M, p.N));
+    maxk = std::max(maxk, (kpad + 2) / 3);  // split columns 3k..3k+2 cover [0, kpad)
+    CUtensorMap ma, mb;
+    if (encode_kmajor(&ma, a2, p.M, kpad, kpad, TC_M) != CUDA_SUCCESS) return -2;
+    if (encode_kmajor(&mb, b2, p.N, kpad, kpad, TC_N) != CUDA_SUCCESS) return -2;
+    maps.push_back(ma);
+    maps.push_back(mb);
+    jobs.push_back({p.C, p.ldc, p.M, p.N, kpad, p.lower, p.kval_dev});
+    const int tm = (p.M + TC_M - 1) / TC_M, tn = (p.N + TC_N - 1) / TC_N;
+    for (int ti = 0; ti < tm; ++ti)
+      for (int tj = 0; tj < tn; ++tj) {
+        if (p.lower && (tj * TC_N > ti * TC_M + TC_M - 1)) continue;  // tile above diagonal
+        tiles.push_back(make_int4((int)i, ti, tj, kpad));
+      }
+  }
+  // deepest tiles first: the persistent CTAs take tiles round-robin
+  std::stable_sort(tiles.begin(), tiles.end(),
+                   [](const int4& a, const int4& b) { return a.w > b.w; });
+
+  // one upload of all descriptors through a pinned staging buffer
+  const size_t o_jobs = up64(sj.size() * sizeof(SplitJob));
+  const size_t o_tiles = o_jobs + up64(jobs.size() * sizeof(TcJob));
+  const size_t o_maps = o_tiles + up64(tiles.size() * sizeof(int4));
+  const size_t total = o_maps + maps.size() * sizeof(CUtensorMap);
+  if (!buf.uploaded && cudaEventCreateWithFlags(&buf.uploaded, cudaEventDisableTiming) != cudaSuccess)
+    return -1;
+  if (cudaEventSynchronize(buf.uploaded) != cudaSuccess) return -3;  // staging free again
+  if (total > buf.cap) {
+    cudaFreeHost(buf.h_stage);
+    cudaFree(buf.d_stage);
+    buf.h_stage = buf.d_stage = nullptr;
+    buf.cap = 0;
+    const size_t nc = std::max(total, (size_t)64 << 10);
+    if (cudaMallocHost(&buf.h_stage, nc) != cudaSuccess) return -1;
+    if (cudaMalloc(&buf.d_stage, nc) != cudaSuccess) return -1;
+    buf.cap = nc;
+  }
+  char* h = static_cast<char*>(buf.h_stage);
+  memcpy(h, sj.data(), sj.size() * sizeof(SplitJob));
+  memcpy(h + o_jobs, jobs.data(), jobs.size() * sizeof(TcJob));
+  memcpy(h + o_tiles, tiles.data(), tiles.size() * sizeof(int4));
+  memcpy(h + o_maps, maps.data(), maps.size() * sizeof(CUtensorMap));
+  char* d = static_cast<char*>(buf.d_stage);
+  if (cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, s) != cudaSuccess) return -3;
+  if (cudaEventRecord(buf.uploaded, s) != cudaSuccess) return -3;
+
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  const bool timed = ms_split || ms_gemm;
+  if (timed) {
+    for (auto& e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], s);
+  }
+  dim3 sg((maxr + 31) / 32, (maxk + 31) / 32, (unsigned)sj.size());
+  k_split<<<sg, 256, 0, s>>>(reinterpret_cast<const SplitJob*>(d));
+  note_launches(1);
+  if (timed) cudaEventRecord(ev[1], s);
+  if (!tiles.empty()) {
+    static int nsm = 0;
+    if (nsm == 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (nsm <= 0) nsm = 1;
+    }
+    const size_t smem = tc_gemm_smem_bytes();
+    cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int grid = std::min((int)tiles.size(), nsm);
+    k_tc_gemm<<<grid, TC_THREADS, smem, s>>>(
+        reinterpret_cast<const TcJob*>(d + o_jobs), reinterpret_cast<const int4*>(d + o_tiles),
+        (int)tiles.size(), reinterpret_cast<const CUtensorMap*>(d + o_maps), chunk, status);
+    note_launches(1);
+  }
+  if (timed) {
+    cudaEventRecord(ev[2], s);
+    cudaEventSynchronize(ev[2]);
+    if (ms_split) cudaEventElapsedTime(ms_split, ev[0], ev[1]);
+    if (ms_gemm) cudaEventElapsedTime(ms_gemm, ev[1], ev[2]);
+    for (auto& e : ev) cudaEventDestroy(e);
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+}  // namespace ssids300
+
+// ---------------------------------------------------------------------------
+// Stand-alone entry point for tests and measurements: C (M x N, col-major,
+// ldc) -= A B^T with A (M x K, lda) and B (N x K, ldb) column-major FP32, all
+// device pointers.  chunk < 0 selects the default accumulation chunk.  With
+// reps > 0 and ms != nullptr the update is repeated reps times and
+// ms[0], ms[1] receive the mean split and GEMM times of the repetitions.
+// ---------------------------------------------------------------------------
+extern "C" int spral_ssids_gpu_tc_gemm_f32(int M, int N, int K, const float* A, int lda,
+                                           const float* B, int ldb, float* C, int ldc, int lower,
+                                           int chunk, int reps, float* ms) {
+  using namespace ssids300;
+  if (M < 0 || N < 0 || K < 0 || lda < M || ldb < N || ldc < M) return -1;
+  if (chunk < 0) chunk = kTcChunk;
+  std::vector<TcProblem> ps(1);
+  ps[0] = {A, lda, B, ldb, C, ldc, M, N, K, nullptr, lower};
+  void* scratch = nullptr;
+  int* status = nullptr;
+  const size_t bytes = tc_gemm_scratch_bytes(ps);
+  if (cudaMalloc(&scratch, bytes) != cudaSuccess) return -50;
+  if (cudaMalloc(&status, sizeof(int)) != cudaSuccess) { cudaFree(scratch); return -50; }
+  cudaMemset(status, 0, sizeof(int));
+  int rc = 0;
+  {
+    TcBuffers buf;
+    const int n = std::max(reps, 1);
+    double tsplit = 0, tgemm = 0;
+    for (int i = 0; i < n && rc == 0; ++i) {
+      float a = 0, b = 0;
+      rc = tc_gemm_run(ps, scratch, buf, status, 0, chunk, ms ? &a : nullptr, ms ? &b : nullptr);
+      tsplit += a;
+      tgemm += b;
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) rc = -51;
+    if (ms) { ms[0] = (float)(tsplit / n); ms[1] = (float)(tgemm / n); }
+  }
+  int hs = 0;
+  cudaMemcpy(&hs, status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (rc == 0 && hs != 0) rc = -52;
+  cudaFree(scratch);
+  cudaFree(status);
+  return rc;
+}
