@@ -156,9 +156,11 @@ int spral_ssids_gpu_solve_refined_dev(void* numeric, int nrhs, const double* b_d
                                       int ld, int* iters, double* bwd_err);
 
 /* Benchmark support (no reference counterpart): kernels launched by this
- * library so far; per-factor timing of the contribution-block GEMM with CUDA
- * events on the library's stream (out[0] ms, out[1] algorithmic flops,
- * out[2] launches); measured FP64 FMA throughput of the device. */
+ * library so far; per-factor timing of the contribution-block update with
+ * CUDA events on the library's stream (out[0] ms, out[1] algorithmic flops,
+ * out[2] timed levels; out[3..5] the same for the tensor-core GEMM kernel
+ * alone, flops counted as the FP32 update); measured FP64 FMA throughput of
+ * the device. */
 long long spral_ssids_gpu_launch_count(void);
 void spral_ssids_gpu_set_profiling(void* numeric, int on);
 void spral_ssids_gpu_profile_stats(const void* numeric, double* out);

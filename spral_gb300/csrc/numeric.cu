@@ -373,6 +373,8 @@ struct NumericBase {
   bool profile = false;
   double prof_ms = 0, prof_flops = 0;
   long long prof_launches = 0;
+  double prof_tc_ms = 0, prof_tc_flops = 0;  // tensor-core GEMM kernel alone
+  long long prof_tc_launches = 0;
   PhaseTimer ptimer;
   PhaseTimer* tm() { return profile ? &ptimer : nullptr; }
   virtual int factor(const double* aval, bool aval_on_device, const double* scaling,
@@ -421,6 +423,23 @@ struct Numeric : NumericBase {
   bool solve_ready = false;
   SolveNode<T>* d_sn = nullptr;
   int* d_children = nullptr;
+  size_t sn_cap = 0, ch_cap = 0;
+  // Captured solve sequences (CUDA graphs), replayed while the launch
+  // sequence and every pointer it uses are unchanged (solve_sig).
+  struct SolveGraph {
+    int job, q, ldx;
+    const double* x;
+    uint64_t sig;
+    cudaGraphExec_t exec;
+    int nlaunch;
+  };
+  std::vector<SolveGraph> sgraphs;
+  uint64_t solve_sig = 0;
+  bool use_graphs = true;
+  void drop_graphs() {
+    for (auto& g : sgraphs) cudaGraphExecDestroy(g.exec);
+    sgraphs.clear();
+  }
   DevBuf<T> xloc, xorig;
   DevBuf<double> xbuf, rbuf, dbuf, bbuf, nbuf;
   // tensor-core contribution GEMM (FP32 factors only)
@@ -453,8 +472,11 @@ struct Numeric : NumericBase {
     }
     if (ps.empty()) return;
     tc_scratch.ensure(tc_gemm_scratch_bytes(ps));
-    if (tc_gemm_run(ps, tc_scratch.p, tcbuf, d_tc_status, s, tc_chunk) != 0)
+    float ms_split = 0, ms_gemm = 0;
+    if (tc_gemm_run(ps, tc_scratch.p, tcbuf, d_tc_status, s, tc_chunk,
+                    profile ? &ms_split : nullptr, profile ? &ms_gemm : nullptr) != 0)
       throw CudaFail{cudaErrorUnknown, __LINE__};
+    if (profile) { prof_tc_ms += ms_gemm; prof_tc_launches += 1; }
   }
 
   const double* cur_aval = nullptr;  // device values of the last factor
@@ -475,6 +497,10 @@ struct Numeric : NumericBase {
     CK(cudaMalloc(&d_stats, sizeof(Stats)));
     CK(cudaMalloc(&d_dwork, std::max(nn, 1) * sizeof(int4)));
     CK(cudaMalloc(&d_tc_status, sizeof(int)));
+    {
+      const char* gr = getenv("SPRAL_GB300_GRAPHS");
+      use_graphs = !(gr && gr[0] == '0');
+    }
     if (std::is_same<T, float>::value) {
       const char* env = getenv("SPRAL_GB300_TENSOR_CORES");
       use_tc = !(env && env[0] == '0');
@@ -492,6 +518,7 @@ struct Numeric : NumericBase {
   ~Numeric() override {
     for (auto e : pev) cudaEventDestroy(e);
     cudaFree(d_fd); cudaFree(d_st); cudaFree(d_stats); cudaFree(d_dwork); cudaFree(d_tc_status);
+    drop_graphs();
     cudaFree(d_sn); cudaFree(d_children);
     for (auto& e : ev) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
@@ -677,6 +704,10 @@ struct Numeric : NumericBase {
           fl += (double)nelim_[f] * cm * (cm + 1.0);
         }
         if (fl > 0) { prof_ms += ms; prof_flops += fl; prof_launches += 1; }
+        for (int f = f0; f < f1; ++f) {
+          const double cm = hfd[f].cm;
+          if (hfd[f].tc) prof_tc_flops += (double)nelim_[f] * cm * (cm + 1.0);
+        }
       }
       if (use_tc) {
         int tcs = 0;
@@ -743,43 +774,103 @@ struct Numeric : NumericBase {
       q.child_end = (int)ch.size();
       q.doff = doff_[f];
     }
-    cudaFree(d_sn);
-    cudaFree(d_children);
-    d_sn = nullptr;
-    d_children = nullptr;
-    d_sn = upload(sn);
-    d_children = upload(ch);
+    // the tables keep their device addresses across refactorisations
+    if (sn.size() > sn_cap) {
+      cudaFree(d_sn);
+      d_sn = nullptr;
+      CK(cudaMalloc(&d_sn, sn.size() * sizeof(SolveNode<T>)));
+      sn_cap = sn.size();
+    }
+    if (std::max<size_t>(ch.size(), 1) > ch_cap) {
+      cudaFree(d_children);
+      d_children = nullptr;
+      CK(cudaMalloc(&d_children, std::max<size_t>(ch.size(), 1) * sizeof(int)));
+      ch_cap = std::max<size_t>(ch.size(), 1);
+    }
+    CK(cudaMemcpyAsync(d_sn, sn.data(), sn.size() * sizeof(SolveNode<T>), cudaMemcpyHostToDevice,
+                       stream));
+    if (!ch.empty())
+      CK(cudaMemcpyAsync(d_children, ch.data(), ch.size() * sizeof(int), cudaMemcpyHostToDevice,
+                         stream));
+    CK(cudaStreamSynchronize(stream));
+    // signature of everything a captured solve sequence depends on
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ull; };
+    for (int l = 0; l < S->nlev; ++l) { mix((uint64_t)lvl_max_m[l]); mix((uint64_t)lvl_max_nelim[l]); }
+    mix((uint64_t)(uintptr_t)d_sn); mix((uint64_t)(uintptr_t)d_children);
+    mix((uint64_t)(uintptr_t)xloc.p); mix((uint64_t)(uintptr_t)xorig.p);
+    if (h != solve_sig) drop_graphs();
+    solve_sig = h;
     solve_ready = true;
+  }
+
+  // enqueue one solve pass of q <= kSolveRhs right-hand sides on s
+  void enqueue_solve(int job, int q, double* xp, int ldx, cudaStream_t s) {
+    const bool fwd = (job == 0 || job == 1);
+    const bool diag = (job == 0 || job == 2 || job == 4);
+    const bool bwd = (job == 0 || job == 3 || job == 4);
+    if (fwd) {
+      for (int l = 0; l < S->nlev; ++l) {
+        const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
+        const int* fr = S->d_fronts + f0;
+        pmark(tm(), kPhFwdGather, s);
+        launch_fwd_gather<T>(d_sn, fr, nf, d_children, xp, ldx, q, s);
+        launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, s, tm());
+        pmark(tm(), kPhFwdScatter, s);
+        launch_fwd_scatter<T>(d_sn, fr, nf, xp, ldx, q, lvl_max_nelim[l], s);
+      }
+    }
+    if (diag || bwd) {
+      for (int l = S->nlev - 1; l >= 0; --l) {
+        const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
+        launch_bwd<T>(d_sn, S->d_fronts + f0, nf, xp, ldx, q, lvl_max_m[l], lvl_max_nelim[l],
+                      diag, bwd, s, tm());
+      }
+    }
+  }
+
+  // the same pass through a captured graph (captured on first use)
+  void run_solve(int job, int q, double* xp, int ldx, cudaStream_t s) {
+    if (profile || !use_graphs) { enqueue_solve(job, q, xp, ldx, s); return; }
+    for (auto& g : sgraphs)
+      if (g.job == job && g.q == q && g.x == xp && g.ldx == ldx && g.sig == solve_sig) {
+        CK(cudaGraphLaunch(g.exec, s));
+        note_launches(g.nlaunch);
+        return;
+      }
+    if (sgraphs.size() >= 8) {
+      cudaGraphExecDestroy(sgraphs.front().exec);
+      sgraphs.erase(sgraphs.begin());
+    }
+    const long long l0 = g_launches.load();
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue_solve(job, q, xp, ldx, s);
+    } catch (...) {
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    CK(cudaStreamEndCapture(s, &g));
+    const int nl = (int)(g_launches.load() - l0);
+    g_launches -= nl;  // counted at each replay instead
+    cudaGraphExec_t ge = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    CK(e);
+    sgraphs.push_back({job, q, ldx, xp, solve_sig, ge, nl});
+    CK(cudaGraphLaunch(ge, s));
+    note_launches(nl);
   }
 
   int solve_dev(int job, int nrhs, double* x, int ldx, cudaStream_t us) override {
     prepare_solve();
     cudaStream_t s = stream;
     if (us) CK(cudaStreamSynchronize(us));
-    const bool fwd = (job == 0 || job == 1);
-    const bool diag = (job == 0 || job == 2 || job == 4);
-    const bool bwd = (job == 0 || job == 3 || job == 4);
     for (int r0 = 0; r0 < nrhs; r0 += kSolveRhs) {
       const int q = std::min(kSolveRhs, nrhs - r0);
-      double* xp = x + (int64_t)r0 * ldx;
-      if (fwd) {
-        for (int l = 0; l < S->nlev; ++l) {
-          const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
-          const int* fr = S->d_fronts + f0;
-          pmark(tm(), kPhFwdGather, s);
-          launch_fwd_gather<T>(d_sn, fr, nf, d_children, xp, ldx, q, s);
-          launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, s, tm());
-          pmark(tm(), kPhFwdScatter, s);
-          launch_fwd_scatter<T>(d_sn, fr, nf, xp, ldx, q, lvl_max_nelim[l], s);
-        }
-      }
-      if (diag || bwd) {
-        for (int l = S->nlev - 1; l >= 0; --l) {
-          const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
-          launch_bwd<T>(d_sn, S->d_fronts + f0, nf, xp, ldx, q, lvl_max_m[l], lvl_max_nelim[l],
-                        diag, bwd, s, tm());
-        }
-      }
+      run_solve(job, q, x + (int64_t)r0 * ldx, ldx, s);
     }
     pmark(tm(), kPhHost, s);
     CK(cudaGetLastError());
@@ -1138,6 +1229,9 @@ void spral_ssids_gpu_set_profiling(void* numeric, int on) {
   N->prof_ms = 0;
   N->prof_flops = 0;
   N->prof_launches = 0;
+  N->prof_tc_ms = 0;
+  N->prof_tc_flops = 0;
+  N->prof_tc_launches = 0;
   N->ptimer.reset();
 }
 
@@ -1151,13 +1245,18 @@ void spral_ssids_gpu_phase_times(const void* numeric, double* ms, long long* cou
   }
 }
 
-/* out[0] = contribution-GEMM time (ms) summed over profiled factors,
- * out[1] = its algorithmic flops, out[2] = number of timed launches. */
+/* out[0] = contribution-update time (ms) summed over profiled factors,
+ * out[1] = its algorithmic flops, out[2] = number of timed levels;
+ * out[3..5] = the same for the tensor-core GEMM kernel alone (flops counted
+ * as the FP32 update it performs, not the 3x split products). */
 void spral_ssids_gpu_profile_stats(const void* numeric, double* out) {
   auto* N = static_cast<const ssids300::NumericBase*>(numeric);
   out[0] = N->prof_ms;
   out[1] = N->prof_flops;
   out[2] = (double)N->prof_launches;
+  out[3] = N->prof_tc_ms;
+  out[4] = N->prof_tc_flops;
+  out[5] = (double)N->prof_tc_launches;
 }
 
 int spral_ssids_gpu_solve_refined_dev(void* numeric, int nrhs, const double* b_dev, double* x_dev,

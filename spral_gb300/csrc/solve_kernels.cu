@@ -11,10 +11,15 @@
 // never update the same entry: each node gathers b for its own pivots plus
 // its children's local vectors (fixed order, no atomics), solves, and leaves
 // rows [nelim, m) of its local vector for its parent.  The triangular solves
-// are blocked by 64 rows: a one-warp diagonal-block solve (values in
-// registers, the pivot row broadcast by shuffles) followed by a row-parallel
-// (forward) or column-parallel (backward) update.  Arithmetic is in the
-// factor precision T; the number of right-hand sides per pass NR is a
+// are blocked by 64 rows.  A diagonal-block solve stages the block in shared
+// memory and gives each right-hand side its own warp (values in registers,
+// the pivot row broadcast by shuffles), so the serial chains of different
+// right-hand sides run on different SM sub-partitions.  One kernel per block
+// step applies the block's update (rows below it in the forward pass,
+// columns left of it in the backward pass) and, in the CTA that owns the
+// next block's rows or columns, solves that next diagonal block right after
+// updating it: one launch per block step instead of two.  Arithmetic is in
+// the factor precision T; the number of right-hand sides per pass NR is a
 // template parameter so that no work is spent on absent columns.
 #include <type_traits>
 
@@ -26,10 +31,12 @@ namespace {
 
 constexpr int SB = kSolveBlk;
 
+// gather b and the children's local vectors into the node's local vector
+// (the whole CTA works on one node)
 template <typename T>
-__global__ void k_fwd_gather(const SolveNode<T>* sns, const int* nodes, const int* children,
-                             const double* x, int ldx, int nrhs) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.x]];
+__device__ __forceinline__ void fwd_gather_node(const SolveNode<T>& sn, const SolveNode<T>* sns,
+                                                const int* children, const double* x, int ldx,
+                                                int nrhs) {
   const int m = sn.m;
   T* xo = sn.xorig;
   for (int e = threadIdx.x; e < m * nrhs; e += blockDim.x) {
@@ -67,63 +74,113 @@ __global__ void k_fwd_gather(const SolveNode<T>* sns, const int* nodes, const in
 // stage the jb x jb diagonal block (strictly lower part) into shared memory;
 // every thread issues all of its loads before the first store so that the
 // global-memory latency is paid once, not once per element
-constexpr int kSolveDiagThreads = 256;
+constexpr int kSolveThreads = 256;
+constexpr int kSolveWarps = kSolveThreads / 32;
 template <typename T>
 __device__ __forceinline__ void load_diag_block(const SolveNode<T>& sn, int j0, int jb,
                                                 T (*Lb)[SB + 1]) {
-  constexpr int PER = SB * SB / kSolveDiagThreads;  // 16
+  constexpr int PER = SB * SB / kSolveThreads;  // 16
   T v[PER];
 #pragma unroll
   for (int k = 0; k < PER; ++k) {
-    const int e = threadIdx.x + k * kSolveDiagThreads;
+    const int e = threadIdx.x + k * kSolveThreads;
     const int c = e / SB, r = e % SB;
     v[k] = (r > c && r < jb && c < jb) ? sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : T(0);
   }
 #pragma unroll
   for (int k = 0; k < PER; ++k) {
-    const int e = threadIdx.x + k * kSolveDiagThreads;
+    const int e = threadIdx.x + k * kSolveThreads;
     Lb[e / SB][e % SB] = v[k];
   }
 }
 
-// forward: unit lower triangular solve of rows [j0, j0+jb) in place
-template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveDiagThreads) k_fwd_diag(const SolveNode<T>* sns, const int* nodes,
-                                                 int step, int nrhs) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.x]];
-  const int j0 = step * SB;
-  if (j0 >= sn.nelim) return;
-  const int jb = min(SB, sn.nelim - j0);
-  __shared__ T Lb[SB][SB + 1];  // Lb[c][r] = L(j0+r, j0+c)
-  load_diag_block(sn, j0, jb, Lb);
-  __syncthreads();
-  if (threadIdx.x >= 32) return;
-  const int lane = threadIdx.x;
-  T x0[NR], x1[NR];
+// Unit lower (FWD) or unit upper L^T (!FWD) triangular solve of rows
+// [j0, j0+jb) of xloc in place, with the block staged in Lb (Lb[c][r] =
+// L(j0+r, j0+c), zero on and above the diagonal).  Warp w solves the
+// right-hand sides w, w + 8, ...; lane l holds rows l and l + 32.  The
+// caller has synchronised the CTA after staging Lb; nothing follows.
+template <typename T, int NR, bool FWD>
+__device__ __forceinline__ void diag_block_solve(const SolveNode<T>& sn, int j0, int jb,
+                                                 int nrhs, T (*Lb)[SB + 1]) {
+  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp >= nrhs) return;
+  T x0[R], x1[R];
 #pragma unroll
-  for (int q = 0; q < NR; ++q) {
-    x0[q] = (q < nrhs && lane < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane] : T(0);
-    x1[q] = (q < nrhs && lane + 32 < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] : T(0);
+  for (int r = 0; r < R; ++r) {
+    const int q = warp + r * kSolveWarps;
+    x0[r] = (q < nrhs && lane < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane] : T(0);
+    x1[r] = (q < nrhs && lane + 32 < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] : T(0);
   }
-  for (int k = 0; k < jb - 1; ++k) {
-    const T l0 = Lb[k][lane], l1 = Lb[k][lane + 32];  // zero on and above the diagonal
+  if (FWD) {
+    for (int k = 0; k < jb - 1; ++k) {
+      const T l0 = Lb[k][lane], l1 = Lb[k][lane + 32];
 #pragma unroll
-    for (int q = 0; q < NR; ++q) {
-      const T xk = (k < 32) ? __shfl_sync(0xffffffffu, x0[q], k & 31)
-                            : __shfl_sync(0xffffffffu, x1[q], k & 31);
-      x0[q] -= l0 * xk;
-      x1[q] -= l1 * xk;
+      for (int r = 0; r < R; ++r) {
+        const T xk = (k < 32) ? __shfl_sync(0xffffffffu, x0[r], k & 31)
+                              : __shfl_sync(0xffffffffu, x1[r], k & 31);
+        x0[r] -= l0 * xk;
+        x1[r] -= l1 * xk;
+      }
+    }
+  } else {
+    // (L^T y)_r = y_r + sum_{c > r} L(c, r) y_c ; process c from the bottom.
+    // L(c, r) = Lb[r][c] is zero unless c > r, so no lane masks are needed.
+    for (int c = jb - 1; c > 0; --c) {
+      const T l0 = Lb[lane][c], l1 = Lb[lane + 32][c];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const T yc = (c < 32) ? __shfl_sync(0xffffffffu, x0[r], c & 31)
+                              : __shfl_sync(0xffffffffu, x1[r], c & 31);
+        x0[r] -= l0 * yc;
+        x1[r] -= l1 * yc;
+      }
     }
   }
 #pragma unroll
-  for (int q = 0; q < NR; ++q) {
-    if (q < nrhs && lane < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane] = x0[q];
-    if (q < nrhs && lane + 32 < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] = x1[q];
+  for (int r = 0; r < R; ++r) {
+    const int q = warp + r * kSolveWarps;
+    if (q < nrhs && lane < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane] = x0[r];
+    if (q < nrhs && lane + 32 < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] = x1[r];
   }
 }
 
+// ---- forward ----
+// gather (one CTA per node), then the first diagonal block
 template <typename T, int NR>
-__global__ void k_fwd_update(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
+__global__ void __launch_bounds__(kSolveThreads)
+    k_fwd_gather_diag(const SolveNode<T>* sns, const int* nodes, const int* children,
+                      const double* x, int ldx, int nrhs) {
+  const SolveNode<T> sn = sns[nodes[blockIdx.x]];
+  fwd_gather_node(sn, sns, children, x, ldx, nrhs);
+  if (sn.nelim == 0) return;
+  __shared__ T Lb[SB][SB + 1];
+  __syncthreads();  // xloc rows written by the gather
+  const int jb = min(SB, sn.nelim);
+  load_diag_block(sn, 0, jb, Lb);
+  __syncthreads();
+  diag_block_solve<T, NR, true>(sn, 0, jb, nrhs, Lb);
+}
+
+// Thread layout of the update kernels: G = min(4, NR) groups of 256 / G
+// threads; a thread owns one row (forward) or column (backward) for the
+// right-hand sides g, g + G, ... of its group g.  No cross-thread reductions
+// (each FP64 add of a shuffle reduction costs a full FP64 issue slot).
+template <int NR>
+struct UpdLayout {
+  static constexpr int G = NR < 4 ? NR : 4;
+  static constexpr int W = kSolveThreads / G;  // rows / columns per CTA pass
+  static constexpr int R = (NR + G - 1) / G;   // right-hand sides per thread
+};
+
+// Block step st: rows i >= i0 = j0 + jb get x_i -= sum_c L(i, j0+c) y_c with
+// y = the solved rows [j0, j0+jb).  CTA 0 updates rows [i0, i0 + W) first,
+// which hold the whole next diagonal block (W >= 64), and then solves that
+// block.
+template <typename T, int NR>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_fwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
+  using LY = UpdLayout<NR>;
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];
   const int j0 = step * SB;
   if (j0 >= sn.nelim) return;
@@ -131,26 +188,36 @@ __global__ void k_fwd_update(const SolveNode<T>* sns, const int* nodes, int step
   const int i0 = j0 + jb;
   if (i0 >= sn.m) return;
   __shared__ T yb[SB][NR];
+  __shared__ T Lb[SB][SB + 1];
   for (int e = threadIdx.x; e < SB * NR; e += blockDim.x) {
     const int r = e % SB, q = e / SB;
     yb[r][q] = (r < jb && q < nrhs) ? sn.xloc[(int64_t)q * sn.m + j0 + r] : T(0);
   }
   __syncthreads();
-  for (int i = i0 + blockIdx.x * blockDim.x + threadIdx.x; i < sn.m; i += gridDim.x * blockDim.x) {
-    T acc[NR];
+  const int g = threadIdx.x / LY::W, t = threadIdx.x % LY::W;
+  for (int i = i0 + blockIdx.x * LY::W + t; i < sn.m; i += gridDim.x * LY::W) {
+    T acc[LY::R];
 #pragma unroll
-    for (int q = 0; q < NR; ++q) acc[q] = T(0);
+    for (int r = 0; r < LY::R; ++r) acc[r] = T(0);
     const T* lrow = sn.L + (int64_t)j0 * sn.ld + i;
 #pragma unroll 8
     for (int c = 0; c < jb; ++c) {
       const T l = lrow[(int64_t)c * sn.ld];
 #pragma unroll
-      for (int q = 0; q < NR; ++q) acc[q] += l * yb[c][q];
+      for (int r = 0; r < LY::R; ++r) acc[r] += l * yb[c][g + r * LY::G];
     }
 #pragma unroll
-    for (int q = 0; q < NR; ++q)
-      if (q < nrhs) sn.xloc[(int64_t)q * sn.m + i] -= acc[q];
+    for (int r = 0; r < LY::R; ++r) {
+      const int q = g + r * LY::G;
+      if (q < nrhs) sn.xloc[(int64_t)q * sn.m + i] -= acc[r];
+    }
   }
+  if (blockIdx.x != 0 || i0 >= sn.nelim) return;
+  __syncthreads();  // rows [i0, i0 + jb1) updated by this CTA
+  const int jb1 = min(SB, sn.nelim - i0);
+  load_diag_block(sn, i0, jb1, Lb);
+  __syncthreads();
+  diag_block_solve<T, NR, true>(sn, i0, jb1, nrhs, Lb);
 }
 
 template <typename T>
@@ -194,99 +261,101 @@ __global__ void k_bwd_gather(const SolveNode<T>* sns, const int* nodes, const do
   }
 }
 
-// xloc[j] -= sum_{i in [nelim, m)} L(i, j) xloc[i]   (warp per column j)
+// xloc[j] -= sum_{i in [nelim, m)} L(i, j) xloc[i] for one column j (one warp)
 template <typename T, int NR>
-__global__ void k_bwd_l21(const SolveNode<T>* sns, const int* nodes, int nrhs) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.y]];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if (sn.m <= sn.nelim) return;
-  for (int j = blockIdx.x * nw + warp; j < sn.nelim; j += gridDim.x * nw) {
-    T acc[NR];
+__device__ __forceinline__ void bwd_l21_column(const SolveNode<T>& sn, int j, int nrhs,
+                                               int lane) {
+  T acc[NR];
 #pragma unroll
-    for (int q = 0; q < NR; ++q) acc[q] = T(0);
-    const T* col = sn.L + (int64_t)j * sn.ld;
-    for (int i = sn.nelim + lane; i < sn.m; i += 32) {
-      const T l = col[i];
-#pragma unroll
-      for (int q = 0; q < NR; ++q)
-        if (q < nrhs) acc[q] += l * sn.xloc[(int64_t)q * sn.m + i];
-    }
+  for (int q = 0; q < NR; ++q) acc[q] = T(0);
+  const T* col = sn.L + (int64_t)j * sn.ld;
+  for (int i = sn.nelim + lane; i < sn.m; i += 32) {
+    const T l = col[i];
 #pragma unroll
     for (int q = 0; q < NR; ++q)
-      for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
-    if (lane == 0)
-      for (int q = 0; q < nrhs; ++q) sn.xloc[(int64_t)q * sn.m + j] -= acc[q];
+      if (q < nrhs) acc[q] += l * sn.xloc[(int64_t)q * sn.m + i];
   }
+#pragma unroll
+  for (int q = 0; q < NR; ++q)
+    for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
+  if (lane == 0)
+    for (int q = 0; q < nrhs; ++q) sn.xloc[(int64_t)q * sn.m + j] -= acc[q];
 }
 
-// backward: unit upper (L^T) triangular solve of rows [j0, j0+jb) in place
+// L21^T part of the backward solve for every eliminated column (one warp per
+// column: the dot products run over the m - nelim rows below the pivots)
 template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveDiagThreads) k_bwd_diag(const SolveNode<T>* sns, const int* nodes,
-                                                 int step, int nrhs) {
+__global__ void __launch_bounds__(kSolveThreads)
+    k_bwd_l21(const SolveNode<T>* sns, const int* nodes, int nrhs) {
+  const SolveNode<T> sn = sns[nodes[blockIdx.y]];
+  if (sn.m <= sn.nelim) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j = blockIdx.x * kSolveWarps + warp; j < sn.nelim; j += gridDim.x * kSolveWarps)
+    bwd_l21_column<T, NR>(sn, j, nrhs, lane);
+}
+
+// the last diagonal block of each node (one CTA per node)
+template <typename T, int NR>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_bwd_diag_last(const SolveNode<T>* sns, const int* nodes, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.x]];
-  const int j0 = step * SB;
-  if (j0 >= sn.nelim) return;
-  const int jb = min(SB, sn.nelim - j0);
-  __shared__ T Lb[SB][SB + 1];  // Lb[c][r] = L(j0+r, j0+c)
-  load_diag_block(sn, j0, jb, Lb);
+  if (sn.nelim == 0) return;
+  const int jl = ((sn.nelim - 1) / SB) * SB;
+  __shared__ T Lb[SB][SB + 1];
+  load_diag_block(sn, jl, sn.nelim - jl, Lb);
   __syncthreads();
-  if (threadIdx.x >= 32) return;
-  const int lane = threadIdx.x;
-  T x0[NR], x1[NR];
-#pragma unroll
-  for (int q = 0; q < NR; ++q) {
-    x0[q] = (q < nrhs && lane < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane] : T(0);
-    x1[q] = (q < nrhs && lane + 32 < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] : T(0);
-  }
-  // (L^T y)_r = y_r + sum_{c > r} L(c, r) y_c ; process c from the bottom.
-  // L(c, r) = Lb[r][c] is zero unless c > r, so no lane masks are needed.
-  for (int c = jb - 1; c > 0; --c) {
-    const T l0 = Lb[lane][c], l1 = Lb[lane + 32][c];
-#pragma unroll
-    for (int q = 0; q < NR; ++q) {
-      const T yc = (c < 32) ? __shfl_sync(0xffffffffu, x0[q], c & 31)
-                            : __shfl_sync(0xffffffffu, x1[q], c & 31);
-      x0[q] -= l0 * yc;
-      x1[q] -= l1 * yc;
-    }
-  }
-#pragma unroll
-  for (int q = 0; q < NR; ++q) {
-    if (q < nrhs && lane < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane] = x0[q];
-    if (q < nrhs && lane + 32 < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] = x1[q];
-  }
+  diag_block_solve<T, NR, false>(sn, jl, sn.nelim - jl, nrhs, Lb);
 }
 
-// columns j < j0: xloc[j] -= sum_{c < jb} L(j0+c, j) y_c   (warp per column)
+// Block step st (> 0) of the backward solve: the columns j left of block st
+// take x_j -= sum_c L(j0+c, j) y_c with y = its solved rows.  CTA 0 updates
+// the columns of block st-1 and then solves that block; CTAs 1.. update the
+// columns before it, W columns per pass.
 template <typename T, int NR>
-__global__ void k_bwd_update(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
+__global__ void __launch_bounds__(kSolveThreads)
+    k_bwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
+  using LY = UpdLayout<NR>;
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];
   const int j0 = step * SB;
   if (j0 >= sn.nelim || j0 == 0) return;
   const int jb = min(SB, sn.nelim - j0);
   __shared__ T yb[SB][NR];
+  __shared__ T Lb[SB][SB + 1];
   for (int e = threadIdx.x; e < SB * NR; e += blockDim.x) {
     const int r = e % SB, q = e / SB;
     yb[r][q] = (r < jb && q < nrhs) ? sn.xloc[(int64_t)q * sn.m + j0 + r] : T(0);
   }
   __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int j = blockIdx.x * nw + warp; j < j0; j += gridDim.x * nw) {
+  const int g = threadIdx.x / LY::W, t = threadIdx.x % LY::W;
+  const int jp = j0 - SB;  // first column of block st-1 (a full block)
+  int jbeg, jend, jstep;
+  if (blockIdx.x == 0) {
+    jbeg = jp + t; jend = j0; jstep = LY::W;
+  } else {
+    jbeg = (blockIdx.x - 1) * LY::W + t; jend = jp; jstep = (gridDim.x - 1) * LY::W;
+  }
+  for (int j = jbeg; j < jend; j += jstep) {
     const T* col = sn.L + (int64_t)j * sn.ld + j0;
-    T acc[NR];
+    T acc[LY::R];
 #pragma unroll
-    for (int q = 0; q < NR; ++q) acc[q] = T(0);
-    for (int c = lane; c < jb; c += 32) {
+    for (int r = 0; r < LY::R; ++r) acc[r] = T(0);
+#pragma unroll 8
+    for (int c = 0; c < jb; ++c) {
       const T l = col[c];
 #pragma unroll
-      for (int q = 0; q < NR; ++q) acc[q] += l * yb[c][q];
+      for (int r = 0; r < LY::R; ++r) acc[r] += l * yb[c][g + r * LY::G];
     }
 #pragma unroll
-    for (int q = 0; q < NR; ++q)
-      for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
-    if (lane == 0)
-      for (int q = 0; q < nrhs; ++q) sn.xloc[(int64_t)q * sn.m + j] -= acc[q];
+    for (int r = 0; r < LY::R; ++r) {
+      const int q = g + r * LY::G;
+      if (q < nrhs) sn.xloc[(int64_t)q * sn.m + j] -= acc[r];
+    }
   }
+  if (blockIdx.x != 0) return;
+  __syncthreads();
+  load_diag_block(sn, jp, SB, Lb);
+  __syncthreads();
+  diag_block_solve<T, NR, false>(sn, jp, SB, nrhs, Lb);
 }
 
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
@@ -304,13 +373,20 @@ void with_nr(int q, F&& f) {
 
 }  // namespace
 
+// gather plus the first diagonal block of every node of the level
 template <typename T>
 void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const int* children,
                        const double* x, int ldx, int nrhs, cudaStream_t s) {
   if (nn <= 0) return;
-  { k_fwd_gather<T><<<nn, 256, 0, s>>>(sn, nodes, children, x, ldx, nrhs); note_launches(1); }
+  with_nr(nrhs, [&](auto nrc) {
+    constexpr int NR = decltype(nrc)::value;
+    k_fwd_gather_diag<T, NR><<<nn, kSolveThreads, 0, s>>>(sn, nodes, children, x, ldx, nrhs);
+    note_launches(1);
+  });
 }
 
+// block steps: update below block st, then solve block st + 1
+// block steps: update below block st, then solve block st + 1
 template <typename T>
 void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_nelim,
                       int max_m, int nrhs, cudaStream_t s, PhaseTimer* tm) {
@@ -318,15 +394,14 @@ void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_
   const int steps = cdiv(max_nelim, SB);
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
+    constexpr int W = UpdLayout<NR>::W;
     for (int st = 0; st < steps; ++st) {
-      pmark(tm, kPhFwdDiag, s);
-      { k_fwd_diag<T, NR><<<nn, kSolveDiagThreads, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
-      int rows = max_m - st * SB;  // upper bound; the kernel derives the exact range
-      if (rows > 0) {
-        int gx = std::max(1, std::min(cdiv(rows, 128), 128));
-        pmark(tm, kPhFwdUpdate, s);
-        { k_fwd_update<T, NR><<<dim3(gx, nn), 128, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
-      }
+      const int rows = max_m - st * SB;  // upper bound; the kernel derives the exact range
+      if (rows <= 0) break;
+      const int gx = std::max(1, std::min(cdiv(rows, W), 152));
+      pmark(tm, kPhFwdUpdate, s);
+      k_fwd_step<T, NR><<<dim3(gx, nn), kSolveThreads, 0, s>>>(sn, nodes, st, nrhs);
+      note_launches(1);
     }
   });
 }
@@ -350,18 +425,21 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
   if (do_bwd) {
     with_nr(nrhs, [&](auto nrc) {
       constexpr int NR = decltype(nrc)::value;
-      int gw = std::max(1, std::min(cdiv(max_nelim, 8), 128));
+      constexpr int W = UpdLayout<NR>::W;
+      const int gw = std::max(1, std::min(cdiv(max_nelim, kSolveWarps), 152));
       pmark(tm, kPhBwdL21, s);
-      { k_bwd_l21<T, NR><<<dim3(gw, nn), 256, 0, s>>>(sn, nodes, nrhs); note_launches(1); }
+      k_bwd_l21<T, NR><<<dim3(gw, nn), kSolveThreads, 0, s>>>(sn, nodes, nrhs);
+      note_launches(1);
+      pmark(tm, kPhBwdDiag, s);
+      k_bwd_diag_last<T, NR><<<nn, kSolveThreads, 0, s>>>(sn, nodes, nrhs);
+      note_launches(1);
       const int steps = cdiv(max_nelim, SB);
-      for (int st = steps - 1; st >= 0; --st) {
-        pmark(tm, kPhBwdDiag, s);
-        { k_bwd_diag<T, NR><<<nn, kSolveDiagThreads, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
-        if (st > 0) {
-          int gu = std::max(1, std::min(cdiv(st * SB, 8), 128));
-          pmark(tm, kPhBwdUpdate, s);
-          { k_bwd_update<T, NR><<<dim3(gu, nn), 256, 0, s>>>(sn, nodes, st, nrhs); note_launches(1); }
-        }
+      for (int st = steps - 1; st >= 1; --st) {
+        // CTA 0 takes block st-1; at least one more CTA for the columns before it
+        const int gu = std::max(1, std::min(cdiv((st - 1) * SB, W), 151));
+        pmark(tm, kPhBwdUpdate, s);
+        k_bwd_step<T, NR><<<dim3(1 + gu, nn), kSolveThreads, 0, s>>>(sn, nodes, st, nrhs);
+        note_launches(1);
       }
     });
   }
