@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--nrhs", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--mixed-only", action="store_true",
+                    help="profiling aid: time only the mixed-precision path and print its object")
     return ap.parse_args()
 
 
@@ -276,6 +278,18 @@ def run_gpu(args):
         xu[ak.invp, :] = x
         bwd = float(M.scaled_bwd_error(ptr, row, val, xu, b).max())
         return ms, per, launches, clocks, bwd, it.value
+
+    if args.mixed_only:
+        fm = ssids.Fkeep(ak, val, ssids.Options(precision=ssids.PRECISION_MIXED, max_refine=20,
+                                                 refine_tol=REFINE_TOL))
+        mms, mper, mlaunch, _, mbwd, mit = measure(fm, mixed=True)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "mixed_only": True, "ms_per_step": mms,
+                              "value": world * 1000.0 / mms, "unit": "solves/s", "bwd_err": mbwd,
+                              "refine_iters": mit, "gpu_launches": int(mlaunch),
+                              "roofline": tensor_roofline(L, fm, aval_d)}), flush=True)
+        fm.free()
+        return
 
     opts64 = ssids.Options(precision=ssids.PRECISION_FP64, max_refine=10, refine_tol=REFINE_TOL)
     fk = ssids.Fkeep(ak, val, opts64)

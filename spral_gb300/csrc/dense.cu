@@ -113,7 +113,7 @@ int dense_factor_run(const DenseWorkspace& w, int m, int n, int* perm, double* a
   const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
   launch_tpp<double>(w.desc, w.state, w.front0, 1, co.action, co.u, co.small, tpp_all, s);
   if (m > n && upd) {
-    launch_calc_ld<double>(w.desc, w.state, w.front0, 1, m - n, s);
+    launch_calc_ld<double>(w.desc, w.state, w.front0, 1, m - n, n, s);
     launch_contrib_gemm<double>(w.desc, w.state, w.front0, 1, m - n, s);
   }
   FrontState hs{};

@@ -824,47 +824,53 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontSta
 // ------------------------------------------------------------------------
 // contribution block: LD = L(n:m, 0:nelim) * D, then C -= L LD^T
 // ------------------------------------------------------------------------
+// LD(:, c) = alpha_c L(:, c) + beta_c L(:, partner_c) for the contribution
+// rows, where (alpha, beta) are the entries of D = (D^{-1})^{-1} in column c.
+// Grid: (row blocks of 128, column chunks of kLdCols, fronts).  Each thread
+// issues the loads of all of its chunk's columns before the first store, so
+// one memory round trip covers kLdCols columns.
+constexpr int kLdCols = 16;
 template <typename T>
-__global__ void k_calc_ld(FrontDesc<T>* fds, const FrontState* sts, const int* fronts) {
-  const int f = fronts[blockIdx.y];
-  FrontDesc<T> fd = fds[f];
+__global__ void __launch_bounds__(128) k_calc_ld(FrontDesc<T>* fds, const FrontState* sts,
+                                                 const int* fronts) {
+  const int f = fronts[blockIdx.z];
+  const FrontDesc<T> fd = fds[f];
   const int nelim = sts[f].nelim;
   const int cm = fd.m - fd.n;
-  if (cm <= 0 || nelim <= 0) return;
-  // LD(:, c) = alpha_c L(:, c) + beta_c L(:, partner_c): the coefficients of
-  // D = (D^{-1})^{-1} are formed once per column chunk in shared memory
-  constexpr int CH = 64;
-  __shared__ double alpha[CH], beta[CH];
-  __shared__ int partner[CH];
-  for (int c0 = 0; c0 < nelim; c0 += CH) {
-    const int nc = min(CH, nelim - c0);
-    __syncthreads();
-    if ((int)threadIdx.x < nc) {
-      const int c = c0 + threadIdx.x;
-      const double d11 = fd.D[2 * c];
-      if (isinf(d11)) {  // second column of a 2x2
-        const double a = fd.D[2 * (c - 1)], b = fd.D[2 * (c - 1) + 1], d = fd.D[2 * c + 1];
-        const double det = a * d - b * b;
-        alpha[threadIdx.x] = a / det; beta[threadIdx.x] = -b / det; partner[threadIdx.x] = c - 1;
-      } else if (c + 1 < nelim && isinf(fd.D[2 * c + 2])) {  // first column of a 2x2
-        const double b = fd.D[2 * c + 1], d = fd.D[2 * c + 3];
-        const double det = d11 * d - b * b;
-        alpha[threadIdx.x] = d / det; beta[threadIdx.x] = -b / det; partner[threadIdx.x] = c + 1;
-      } else {
-        alpha[threadIdx.x] = (d11 != 0.0) ? 1.0 / d11 : 0.0; beta[threadIdx.x] = 0.0;
-        partner[threadIdx.x] = c;
-      }
+  const int c0 = blockIdx.y * kLdCols;
+  if (cm <= 0 || c0 >= nelim) return;
+  const int nc = min(kLdCols, nelim - c0);
+  __shared__ double alpha[kLdCols], beta[kLdCols];
+  __shared__ int partner[kLdCols];
+  if ((int)threadIdx.x < nc) {
+    const int c = c0 + threadIdx.x;
+    const double d11 = fd.D[2 * c];
+    if (isinf(d11)) {  // second column of a 2x2
+      const double a = fd.D[2 * (c - 1)], b = fd.D[2 * (c - 1) + 1], d = fd.D[2 * c + 1];
+      const double det = a * d - b * b;
+      alpha[threadIdx.x] = a / det; beta[threadIdx.x] = -b / det; partner[threadIdx.x] = c - 1;
+    } else if (c + 1 < nelim && isinf(fd.D[2 * c + 2])) {  // first column of a 2x2
+      const double b = fd.D[2 * c + 1], d = fd.D[2 * c + 3];
+      const double det = d11 * d - b * b;
+      alpha[threadIdx.x] = d / det; beta[threadIdx.x] = -b / det; partner[threadIdx.x] = c + 1;
+    } else {
+      alpha[threadIdx.x] = (d11 != 0.0) ? 1.0 / d11 : 0.0; beta[threadIdx.x] = 0.0;
+      partner[threadIdx.x] = c;
     }
-    __syncthreads();
-    for (int rr = blockIdx.x * blockDim.x + threadIdx.x; rr < cm; rr += gridDim.x * blockDim.x) {
-      const int r = fd.n + rr;
-      for (int k = 0; k < nc; ++k) {
-        const int c = c0 + k;
-        double v = alpha[k] * (double)fd.L[(int64_t)c * fd.ld + r];
-        if (beta[k] != 0.0) v += beta[k] * (double)fd.L[(int64_t)partner[k] * fd.ld + r];
-        fd.LD[(int64_t)c * cm + rr] = (T)v;
-      }
+  }
+  __syncthreads();
+  for (int rr = blockIdx.x * blockDim.x + threadIdx.x; rr < cm; rr += gridDim.x * blockDim.x) {
+    const T* Lr = fd.L + fd.n + rr;
+    T lv[kLdCols], lp[kLdCols];
+#pragma unroll
+    for (int k = 0; k < kLdCols; ++k) {
+      lv[k] = (k < nc) ? Lr[(int64_t)(c0 + k) * fd.ld] : T(0);
+      lp[k] = (k < nc && beta[k] != 0.0) ? Lr[(int64_t)partner[k] * fd.ld] : T(0);
     }
+#pragma unroll
+    for (int k = 0; k < kLdCols; ++k)
+      if (k < nc)
+        fd.LD[(int64_t)(c0 + k) * cm + rr] = (T)(alpha[k] * (double)lv[k] + beta[k] * (double)lp[k]);
   }
 }
 
@@ -969,10 +975,12 @@ void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, boo
 
 template <typename T>
 void launch_calc_ld(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
-                    cudaStream_t s) {
+                    int max_n, cudaStream_t s) {
   if (nf <= 0 || max_cm <= 0) return;
-  int gx = std::max(1, std::min(cdiv(max_cm, 128), 256));
-  { k_calc_ld<T><<<dim3(gx, nf), 128, 0, s>>>(fd, st, fronts); note_launches(1); }
+  // column chunks cover the largest possible nelim (the front width)
+  int gx = std::max(1, std::min(cdiv(max_cm, 128), 64));
+  int gy = std::max(1, cdiv(max_n, kLdCols));
+  { k_calc_ld<T><<<dim3(gx, gy, nf), 128, 0, s>>>(fd, st, fronts); note_launches(1); }
 }
 template <typename T>
 void launch_contrib_gemm(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
@@ -996,7 +1004,8 @@ void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* front
   template void launch_app_finish<T>(FrontDesc<T>*, FrontState*, const int*, int, cudaStream_t); \
   template void launch_tpp<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double, double, \
                               bool, cudaStream_t);                                              \
-  template void launch_calc_ld<T>(FrontDesc<T>*, FrontState*, const int*, int, int, cudaStream_t); \
+  template void launch_calc_ld<T>(FrontDesc<T>*, FrontState*, const int*, int, int, int,        \
+                                  cudaStream_t);                                                 \
   template void launch_contrib_gemm<T>(FrontDesc<T>*, FrontState*, const int*, int, int,        \
                                        cudaStream_t);                                           \
   template void launch_stats<T>(const FrontDesc<T>*, const FrontState*, const int*, int, int,    \

@@ -669,7 +669,7 @@ struct Numeric : NumericBase {
       const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
       launch_tpp<T>(d_fd, d_st, fr, nf, co.action, co.u, co.small, tpp_all, s);
       pmark(tm(), kPhCalcLd, s);
-      launch_calc_ld<T>(d_fd, d_st, fr, nf, max_cm, s);
+      launch_calc_ld<T>(d_fd, d_st, fr, nf, max_cm, max_n, s);
       pmark(tm(), kPhContrib, s);
       if (profile) CK(cudaEventRecord(pev[2 * l], s));
       launch_contrib_gemm<T>(d_fd, d_st, fr, nf, max_cm, s);

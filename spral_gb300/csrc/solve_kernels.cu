@@ -32,42 +32,77 @@ namespace {
 constexpr int SB = kSolveBlk;
 
 // gather b and the children's local vectors into the node's local vector
-// (the whole CTA works on one node)
+// (the whole CTA works on one node).  Every loop handles kGatherBatch
+// elements per thread with all loads issued before the stores, so each
+// batch costs one memory round trip (positions within one child are
+// distinct, so a batch never updates one entry twice).
+constexpr int kGatherBatch = 8;
 template <typename T>
 __device__ __forceinline__ void fwd_gather_node(const SolveNode<T>& sn, const SolveNode<T>* sns,
                                                 const int* children, const double* x, int ldx,
                                                 int nrhs) {
+  constexpr int GB = kGatherBatch;
   const int m = sn.m;
+  const int nt = blockDim.x;
   T* xo = sn.xorig;
-  for (int e = threadIdx.x; e < m * nrhs; e += blockDim.x) {
-    const int i = e % m, r = e / m;
-    xo[e] = (i < sn.ncol) ? (T)x[(int64_t)r * ldx + sn.sptr0 + i] : T(0);
+  for (int e0 = threadIdx.x; e0 < m * nrhs; e0 += GB * nt) {
+    T v[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int e = e0 + u * nt;
+      const int i = e % m, r = e / m;
+      v[u] = (e < m * nrhs && i < sn.ncol) ? (T)x[(int64_t)r * ldx + sn.sptr0 + i] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < GB; ++u)
+      if (e0 + u * nt < m * nrhs) xo[e0 + u * nt] = v[u];
   }
   __syncthreads();
   for (int ci = sn.child_beg; ci < sn.child_end; ++ci) {
     const SolveNode<T> cn = sns[children[ci]];
     const int nd = cn.n - cn.nelim;
     const int tot = nd + cn.cm;
-    for (int e = threadIdx.x; e < tot * nrhs; e += blockDim.x) {
-      const int k = e % tot, r = e / tot;
-      int pos;
-      T v;
-      if (k < nd) {
-        pos = sn.ncol + cn.doff + k;
-        v = cn.xloc[(int64_t)r * cn.m + cn.nelim + k];
-      } else {
-        const int ic = k - nd;
-        const int Q = cn.rdir[ic];
-        pos = (Q < sn.ncol) ? Q : Q + sn.ndelay_in;
-        v = cn.xloc[(int64_t)r * cn.m + cn.n + ic];
+    for (int e0 = threadIdx.x; e0 < tot * nrhs; e0 += GB * nt) {
+      int pos[GB];
+      T v[GB];
+#pragma unroll
+      for (int u = 0; u < GB; ++u) {
+        const int e = e0 + u * nt;
+        const int k = e % tot, r = e / tot;
+        pos[u] = -1;
+        v[u] = T(0);
+        if (e < tot * nrhs) {
+          if (k < nd) {
+            pos[u] = r * m + sn.ncol + cn.doff + k;
+            v[u] = cn.xloc[(int64_t)r * cn.m + cn.nelim + k];
+          } else {
+            const int ic = k - nd;
+            const int Q = cn.rdir[ic];
+            pos[u] = r * m + ((Q < sn.ncol) ? Q : Q + sn.ndelay_in);
+            v[u] = cn.xloc[(int64_t)r * cn.m + cn.n + ic];
+          }
+        }
       }
-      xo[(int64_t)r * m + pos] += v;
+      T old[GB];
+#pragma unroll
+      for (int u = 0; u < GB; ++u) old[u] = (pos[u] >= 0) ? xo[pos[u]] : T(0);
+#pragma unroll
+      for (int u = 0; u < GB; ++u)
+        if (pos[u] >= 0) xo[pos[u]] = old[u] + v[u];
     }
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < m * nrhs; e += blockDim.x) {
-    const int i = e % m, r = e / m;
-    sn.xloc[e] = (i < sn.n) ? xo[(int64_t)r * m + sn.opos[i]] : xo[e];
+  for (int e0 = threadIdx.x; e0 < m * nrhs; e0 += GB * nt) {
+    T v[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int e = e0 + u * nt;
+      const int i = e % m, r = e / m;
+      v[u] = (e < m * nrhs) ? ((i < sn.n) ? xo[(int64_t)r * m + sn.opos[i]] : xo[e]) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < GB; ++u)
+      if (e0 + u * nt < m * nrhs) sn.xloc[e0 + u * nt] = v[u];
   }
 }
 
@@ -162,25 +197,51 @@ __global__ void __launch_bounds__(kSolveThreads)
   diag_block_solve<T, NR, true>(sn, 0, jb, nrhs, Lb);
 }
 
-// Thread layout of the update kernels: G = min(4, NR) groups of 256 / G
-// threads; a thread owns one row (forward) or column (backward) for the
-// right-hand sides g, g + G, ... of its group g.  No cross-thread reductions
-// (each FP64 add of a shuffle reduction costs a full FP64 issue slot).
-template <int NR>
-struct UpdLayout {
-  static constexpr int G = NR < 4 ? NR : 4;
-  static constexpr int W = kSolveThreads / G;  // rows / columns per CTA pass
-  static constexpr int R = (NR + G - 1) / G;   // right-hand sides per thread
-};
+// Update kernels of the block steps: a CTA pass covers 64 rows (forward) or
+// columns (backward); thread (t, qq) = (threadIdx.x % 64, threadIdx.x / 64)
+// forms the partial dot products of entry t over the 16 block columns
+// [16 qq, 16 qq + 16) for every right-hand side, with its 16 loads issued
+// together, and the four partial sums are added through shared memory.
+constexpr int kPassRows = 64;
+constexpr int kQuarter = SB / 4;
+
+template <typename T, int NR>
+__device__ __forceinline__ void partial_dots(const T* p, int64_t stride, int cq, int jb,
+                                             const T (*yb)[NR], T (&acc)[NR]) {
+  T lv[kQuarter];
+#pragma unroll
+  for (int k = 0; k < kQuarter; ++k) lv[k] = (cq + k < jb) ? p[(int64_t)k * stride] : T(0);
+#pragma unroll
+  for (int q = 0; q < NR; ++q) acc[q] = T(0);
+#pragma unroll
+  for (int k = 0; k < kQuarter; ++k)
+#pragma unroll
+    for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[cq + k][q];
+}
+
+// red[(qq * NR + q) * 64 + t] holds the partial sums; entry t of the pass
+// (global index base + t < lim) gets x -= the sum of its four partials
+template <typename T, int NR>
+__device__ __forceinline__ void apply_partials(const SolveNode<T>& sn, const T* red, int base,
+                                               int lim, int nrhs) {
+  for (int e = threadIdx.x; e < kPassRows * NR; e += blockDim.x) {
+    const int t = e % kPassRows, q = e / kPassRows;
+    const int idx = base + t;
+    if (q < nrhs && idx < lim) {
+      const T v = red[(0 * NR + q) * kPassRows + t] + red[(1 * NR + q) * kPassRows + t] +
+                  red[(2 * NR + q) * kPassRows + t] + red[(3 * NR + q) * kPassRows + t];
+      sn.xloc[(int64_t)q * sn.m + idx] -= v;
+    }
+  }
+}
 
 // Block step st: rows i >= i0 = j0 + jb get x_i -= sum_c L(i, j0+c) y_c with
-// y = the solved rows [j0, j0+jb).  CTA 0 updates rows [i0, i0 + W) first,
-// which hold the whole next diagonal block (W >= 64), and then solves that
-// block.
+// y = the solved rows [j0, j0+jb).  CTA 0's first pass covers rows
+// [i0, i0 + 64), which hold the whole next diagonal block; it then solves
+// that block.
 template <typename T, int NR>
 __global__ void __launch_bounds__(kSolveThreads)
     k_fwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
-  using LY = UpdLayout<NR>;
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];
   const int j0 = step * SB;
   if (j0 >= sn.nelim) return;
@@ -188,32 +249,31 @@ __global__ void __launch_bounds__(kSolveThreads)
   const int i0 = j0 + jb;
   if (i0 >= sn.m) return;
   __shared__ T yb[SB][NR];
-  __shared__ T Lb[SB][SB + 1];
+  __shared__ T Lb[SB][SB + 1];  // also the partial-sum buffer (4 * NR * 64 entries fit)
+  T* red = &Lb[0][0];
   for (int e = threadIdx.x; e < SB * NR; e += blockDim.x) {
     const int r = e % SB, q = e / SB;
     yb[r][q] = (r < jb && q < nrhs) ? sn.xloc[(int64_t)q * sn.m + j0 + r] : T(0);
   }
   __syncthreads();
-  const int g = threadIdx.x / LY::W, t = threadIdx.x % LY::W;
-  for (int i = i0 + blockIdx.x * LY::W + t; i < sn.m; i += gridDim.x * LY::W) {
-    T acc[LY::R];
+  const int t = threadIdx.x % kPassRows, qq = threadIdx.x / kPassRows;
+  for (int base = i0 + blockIdx.x * kPassRows; base < sn.m; base += gridDim.x * kPassRows) {
+    const int i = base + t;
+    T acc[NR];
+    if (i < sn.m) {
+      partial_dots<T, NR>(sn.L + (int64_t)(j0 + qq * kQuarter) * sn.ld + i, sn.ld, qq * kQuarter,
+                          jb, yb, acc);
+    } else {
 #pragma unroll
-    for (int r = 0; r < LY::R; ++r) acc[r] = T(0);
-    const T* lrow = sn.L + (int64_t)j0 * sn.ld + i;
-#pragma unroll 8
-    for (int c = 0; c < jb; ++c) {
-      const T l = lrow[(int64_t)c * sn.ld];
-#pragma unroll
-      for (int r = 0; r < LY::R; ++r) acc[r] += l * yb[c][g + r * LY::G];
+      for (int q = 0; q < NR; ++q) acc[q] = T(0);
     }
 #pragma unroll
-    for (int r = 0; r < LY::R; ++r) {
-      const int q = g + r * LY::G;
-      if (q < nrhs) sn.xloc[(int64_t)q * sn.m + i] -= acc[r];
-    }
+    for (int q = 0; q < NR; ++q) red[(qq * NR + q) * kPassRows + t] = acc[q];
+    __syncthreads();
+    apply_partials<T, NR>(sn, red, base, sn.m, nrhs);
+    __syncthreads();
   }
   if (blockIdx.x != 0 || i0 >= sn.nelim) return;
-  __syncthreads();  // rows [i0, i0 + jb1) updated by this CTA
   const int jb1 = min(SB, sn.nelim - i0);
   load_diag_block(sn, i0, jb1, Lb);
   __syncthreads();
@@ -309,50 +369,48 @@ __global__ void __launch_bounds__(kSolveThreads)
 
 // Block step st (> 0) of the backward solve: the columns j left of block st
 // take x_j -= sum_c L(j0+c, j) y_c with y = its solved rows.  CTA 0 updates
-// the columns of block st-1 and then solves that block; CTAs 1.. update the
-// columns before it, W columns per pass.
+// the 64 columns of block st-1 and then solves that block; CTAs 1.. update
+// the columns before it, 64 per pass.
 template <typename T, int NR>
 __global__ void __launch_bounds__(kSolveThreads)
     k_bwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
-  using LY = UpdLayout<NR>;
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];
   const int j0 = step * SB;
   if (j0 >= sn.nelim || j0 == 0) return;
   const int jb = min(SB, sn.nelim - j0);
   __shared__ T yb[SB][NR];
-  __shared__ T Lb[SB][SB + 1];
+  __shared__ T Lb[SB][SB + 1];  // also the partial-sum buffer
+  T* red = &Lb[0][0];
   for (int e = threadIdx.x; e < SB * NR; e += blockDim.x) {
     const int r = e % SB, q = e / SB;
     yb[r][q] = (r < jb && q < nrhs) ? sn.xloc[(int64_t)q * sn.m + j0 + r] : T(0);
   }
   __syncthreads();
-  const int g = threadIdx.x / LY::W, t = threadIdx.x % LY::W;
+  const int t = threadIdx.x % kPassRows, qq = threadIdx.x / kPassRows;
   const int jp = j0 - SB;  // first column of block st-1 (a full block)
-  int jbeg, jend, jstep;
+  int first, lim, stride;
   if (blockIdx.x == 0) {
-    jbeg = jp + t; jend = j0; jstep = LY::W;
+    first = jp; lim = j0; stride = kPassRows;
   } else {
-    jbeg = (blockIdx.x - 1) * LY::W + t; jend = jp; jstep = (gridDim.x - 1) * LY::W;
+    first = (blockIdx.x - 1) * kPassRows; lim = jp; stride = (gridDim.x - 1) * kPassRows;
   }
-  for (int j = jbeg; j < jend; j += jstep) {
-    const T* col = sn.L + (int64_t)j * sn.ld + j0;
-    T acc[LY::R];
+  for (int base = first; base < lim; base += stride) {
+    const int j = base + t;
+    T acc[NR];
+    if (j < lim) {
+      partial_dots<T, NR>(sn.L + (int64_t)j * sn.ld + j0 + qq * kQuarter, 1, qq * kQuarter, jb,
+                          yb, acc);
+    } else {
 #pragma unroll
-    for (int r = 0; r < LY::R; ++r) acc[r] = T(0);
-#pragma unroll 8
-    for (int c = 0; c < jb; ++c) {
-      const T l = col[c];
-#pragma unroll
-      for (int r = 0; r < LY::R; ++r) acc[r] += l * yb[c][g + r * LY::G];
+      for (int q = 0; q < NR; ++q) acc[q] = T(0);
     }
 #pragma unroll
-    for (int r = 0; r < LY::R; ++r) {
-      const int q = g + r * LY::G;
-      if (q < nrhs) sn.xloc[(int64_t)q * sn.m + j] -= acc[r];
-    }
+    for (int q = 0; q < NR; ++q) red[(qq * NR + q) * kPassRows + t] = acc[q];
+    __syncthreads();
+    apply_partials<T, NR>(sn, red, base, lim, nrhs);
+    __syncthreads();
   }
   if (blockIdx.x != 0) return;
-  __syncthreads();
   load_diag_block(sn, jp, SB, Lb);
   __syncthreads();
   diag_block_solve<T, NR, false>(sn, jp, SB, nrhs, Lb);
@@ -394,11 +452,10 @@ void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_
   const int steps = cdiv(max_nelim, SB);
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
-    constexpr int W = UpdLayout<NR>::W;
     for (int st = 0; st < steps; ++st) {
       const int rows = max_m - st * SB;  // upper bound; the kernel derives the exact range
       if (rows <= 0) break;
-      const int gx = std::max(1, std::min(cdiv(rows, W), 152));
+      const int gx = std::max(1, std::min(cdiv(rows, kPassRows), 152));
       pmark(tm, kPhFwdUpdate, s);
       k_fwd_step<T, NR><<<dim3(gx, nn), kSolveThreads, 0, s>>>(sn, nodes, st, nrhs);
       note_launches(1);
@@ -425,7 +482,6 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
   if (do_bwd) {
     with_nr(nrhs, [&](auto nrc) {
       constexpr int NR = decltype(nrc)::value;
-      constexpr int W = UpdLayout<NR>::W;
       const int gw = std::max(1, std::min(cdiv(max_nelim, kSolveWarps), 152));
       pmark(tm, kPhBwdL21, s);
       k_bwd_l21<T, NR><<<dim3(gw, nn), kSolveThreads, 0, s>>>(sn, nodes, nrhs);
@@ -436,7 +492,7 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
       const int steps = cdiv(max_nelim, SB);
       for (int st = steps - 1; st >= 1; --st) {
         // CTA 0 takes block st-1; at least one more CTA for the columns before it
-        const int gu = std::max(1, std::min(cdiv((st - 1) * SB, W), 151));
+        const int gu = std::max(1, std::min(cdiv((st - 1) * SB, kPassRows), 151));
         pmark(tm, kPhBwdUpdate, s);
         k_bwd_step<T, NR><<<dim3(1 + gu, nn), kSolveThreads, 0, s>>>(sn, nodes, st, nrhs);
         note_launches(1);

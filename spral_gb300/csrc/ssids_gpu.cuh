@@ -118,7 +118,7 @@ void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, boo
                 double u, double small, bool root_only_or_all, cudaStream_t s);
 template <typename T>
 void launch_calc_ld(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
-                    cudaStream_t s);
+                    int max_n, cudaStream_t s);
 template <typename T>
 void launch_contrib_gemm(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
                          cudaStream_t s);
