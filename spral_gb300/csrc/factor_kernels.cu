@@ -70,37 +70,88 @@ __device__ __forceinline__ double sym_at(const T* L, int ld, int r, int c) {
 
 // ------------------------------------------------------------------------
 // k_app_diag: advance state, factor the diagonal block with complete pivoting.
-// 128 threads; thread t owns the 8 entries (rows 8*(t/32)+k, column t%32) of
-// the block, stored full-symmetric.  Pivoting never moves data: a logical <->
-// physical index map is updated instead, so each pivot costs one argmax
-// (warp shuffles + 4 partials), one parallel rank-1/2 update and three
-// barriers.  The block and its updates are in the factor precision T; pivot
-// selection values, D^{-1} and 2x2 inversions are FP64.
+// 1024 threads, thread (R, C) = (warp, lane) owns entry (R, C) of the block,
+// which is stored full-symmetric and kept exactly symmetric: for R > C the
+// thread computes the update of the pair once and writes both copies.
+// Pivoting never moves data: a logical <-> physical index map is updated
+// instead.  Each pivot: every thread keys its entry (64-bit: magnitude, then
+// the reference's column-major scan order over the logical lower triangle),
+// warps reduce, warp 0 reduces the 32 partial maxima and takes the 1x1 / 2x2
+// decision, and every thread applies the rank-1/2 update to its entry.  The
+// block and its updates are in the factor precision T; pivot values, D^{-1}
+// and 2x2 inversions are FP64.  Semantics follow block_ldlt
+// (src/ssids/cpu/kernels/block_ldlt.hxx:290-413): find_maxloc, the 2x2 test
+// |det| >= |a21|/2 on the scaled determinant, otherwise the larger diagonal
+// as a 1x1 pivot, zero pivots below `small`.
 // ------------------------------------------------------------------------
-constexpr int kDiagThreads = 128;
+template <typename T>
+struct DiagKey;
+template <>
+struct DiagKey<double> {
+  // magnitude with its low 10 mantissa bits replaced by the inverted
+  // logical position: one unsigned max gives the largest entry and, among
+  // entries equal to 2^-42 relative, the first in column-major order
+  static __device__ __forceinline__ unsigned long long make(double v, int pos) {
+    const unsigned long long mag =
+        (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+    return ((mag | 0x3ffULL) ^ 0x3ffULL) | (unsigned long long)(1023 - pos) | (1ULL << 63);
+  }
+  static __device__ __forceinline__ double mag(unsigned long long k) {
+    return __longlong_as_double((long long)((k & 0x7fffffffffffffffULL) | 0x3ffULL));
+  }
+};
+template <>
+struct DiagKey<float> {
+  // the exact FP32 magnitude above the 10-bit inverted position
+  static __device__ __forceinline__ unsigned long long make(float v, int pos) {
+    const unsigned long long mag = (unsigned long long)(__float_as_uint(v) & 0x7fffffffu);
+    return (mag << 10) | (unsigned long long)(1023 - pos) | (1ULL << 63);
+  }
+  static __device__ __forceinline__ double mag(unsigned long long k) {
+    return (double)__uint_as_float((unsigned int)((k >> 10) & 0x7fffffffULL));
+  }
+};
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long k) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, k, off);
+    k = o > k ? o : k;
+  }
+  return k;
+}
+
+// 17 warps: thread t < 528 owns the pair {R, C}, R >= C, t = R(R+1)/2 + C
+constexpr int kDiagPairs = kBlk * (kBlk + 1) / 2;
+constexpr int kDiagThreads = (kDiagPairs + 31) / 32 * 32;
+constexpr int kDiagWarps = kDiagThreads / 32;
 
 template <typename T>
 __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, FrontState* sts,
                                                            const int* fronts, int step,
                                                            bool action, double small) {
+  constexpr bool kF64 = sizeof(T) == 8;
   const int f = fronts[blockIdx.x];
-  FrontDesc<T> fd = fds[f];
   FrontState* st = &sts[f];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int C = lane;          // owned physical column
-  const int R0 = warp * 8;     // owned physical rows R0..R0+7
-  __shared__ T blk[kBlk][kBlk + 1];  // blk[C][R] = A(R, C), physical indices
-  __shared__ double dd[2 * kBlk + 2];
+  // owned pair (physical R >= C)
+  int R = (int)((sqrtf(8.0f * tid + 1.0f) - 1.0f) * 0.5f);
+  while ((R + 1) * (R + 2) / 2 <= tid) ++R;
+  while (R * (R + 1) / 2 > tid) --R;
+  const int C = tid - R * (R + 1) / 2;
+  const bool pair = tid < kDiagPairs;
+  __shared__ T blk[kBlk][kBlk + 1];   // blk[c][r] = A(r, c), physical indices, symmetric
+  __shared__ T outb[kBlk][kBlk + 1];  // outb[j][X] = L(inv[X], j): logical column, physical row
   __shared__ int map[kBlk], inv[kBlk];  // logical -> physical, physical -> logical
-  __shared__ double rdiag[kBlk];  // reciprocal of each physical diagonal entry
-  __shared__ long long pkey[4];
-  __shared__ int pi_[4], pj_[4];
-  __shared__ int s_piv[3];
-  __shared__ int s_sw[4];
-  __shared__ double s_d[4];
+  __shared__ unsigned long long wkey[kBlk];
+  __shared__ double rdiag[kBlk];
+  __shared__ double dd[2 * kBlk + 2];
+  __shared__ int s_dec[3];  // pivot size (0: zero pivot), physical pivot(s)
   __shared__ int s_state[2];
+  __shared__ FrontDesc<T> fd;
 
   if (tid == 0) {
+    fd = fds[f];
     int p, end;
     if (step == 0) {
       p = 0;
@@ -127,167 +178,134 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
   __syncthreads();
   const int p = s_state[0], bs = s_state[1];
   if (bs == 0) return;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int R = R0 + k;
-    blk[C][R] = (R < bs && C < bs) ? (T)sym_at(fd.L, fd.ld, p + R, p + C) : T(0);
+  const bool mine = pair && R < bs;  // (C <= R < bs)
+  if (pair) {
+    const T v = mine ? (T)fd.L[(int64_t)(p + C) * fd.ld + p + R] : T(0);
+    blk[C][R] = v;
+    blk[R][C] = v;
   }
+  for (int e = tid; e < kBlk * (kBlk + 1); e += kDiagThreads) (&outb[0][0])[e] = T(0);
   if (tid < kBlk) { map[tid] = tid; inv[tid] = tid; }
   if (tid < 2 * kBlk + 2) dd[tid] = 0.0;
+  if (tid < kBlk) wkey[tid] = 0;
   __syncthreads();
 
-  // logical indices of the owned column / rows, cached in registers
-  int lj = C;
-  int li[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) li[k] = R0 + k;
-  const bool colok = C < bs;
   bool singular = false;
   for (int q = 0; q < bs;) {
-    // ---- argmax of |A| over the logical lower triangle of columns >= q.
-    // Key = magnitude bits with the low 10 mantissa bits replaced by the
-    // (inverted) logical position j*32+i, so one unsigned max gives the
-    // largest entry and, among entries equal to 2^-42 relative, the first in
-    // logical column-major order (the reference's scan order).
-    if (colok && C >= R0 && C < R0 + 8 && lj >= q) rdiag[C] = recip_nr((double)blk[C][C]);
-    unsigned long long bk = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int R = R0 + k;
-      if (colok && R < bs && lj >= q && li[k] >= lj) {
-        const unsigned long long mag =
-            (unsigned long long)__double_as_longlong((double)blk[C][R]) & 0x7fffffffffffffffULL;
-        const unsigned long long key =
-            ((mag | 0x3ffULL) ^ 0x3ffULL) | (unsigned long long)(1023 - (lj * 32 + li[k])) |
-            (1ULL << 63);  // marks a valid candidate
-        bk = key > bk ? key : bk;
-      }
+    // ---- candidates: the logical lower triangle of the trailing block
+    {
+      const int li = inv[R], lj = inv[C];
+      const int hi = max(li, lj), lo = min(li, lj);
+      unsigned long long key = 0;
+      if (mine && lo >= q) key = DiagKey<T>::make(blk[C][R], lo * 32 + hi);
+      key = warp_max_u64(key);
+      if (lane == 0) wkey[warp] = key;
+      // FP64 factors: reciprocals of the trailing diagonal, ready for a 1x1
+      if (kF64 && mine && R == C && lo >= q) rdiag[C] = recip_nr((double)blk[C][C]);
     }
-    for (int off = 16; off > 0; off >>= 1) {
-      const unsigned long long ok = __shfl_xor_sync(0xffffffffu, bk, off);
-      bk = ok > bk ? ok : bk;
-    }
-    if (lane == 0) pkey[warp] = (long long)bk;
     __syncthreads();
-    if (tid == 0) {
-      for (int w = 1; w < 4; ++w) {
-        const unsigned long long ok = (unsigned long long)pkey[w];
-        bk = ok > bk ? ok : bk;
-      }
-      const int pos = 1023 - (int)(bk & 0x3ffULL);
-      const int bj = pos >> 5, bi = pos & 31;  // logical column, row
-      const double bv = __longlong_as_double((long long)((bk & 0x7fffffffffffffffULL) | 0x3ffULL));
-      int pivsiz;
+    // ---- decision and the pivot's L column(s) (warp 0; every lane takes the
+    // same decision, lane X then forms row X of the new L column(s))
+    if (warp == 0) {
+      const unsigned long long gk = warp_max_u64(wkey[lane]);
+      const int pos = 1023 - (int)(gk & 0x3ffULL);
+      const int bj = pos >> 5, bi = pos & 31;  // logical column, row of the maximum
+      const double bv = DiagKey<T>::mag(gk);
+      int pivsiz = 1, i1 = bi, i2 = -1;
+      double e11 = 0.0, e21 = 0.0, e22 = 0.0;
       if (bv < small) {
         pivsiz = 0;
-      } else {
-        const int t = bi, mm = bj;
-        int i1, i2 = -1;
-        if (t == mm) {
-          pivsiz = 1; i1 = t;
+      } else if (bi != bj) {
+        const int mm = map[bj], tt = map[bi];
+        const double a11 = (double)blk[mm][mm], a22 = (double)blk[tt][tt];
+        const double a21 = (double)blk[mm][tt];
+        const double detscale = recip_nr(fabs(a21));
+        const double detpiv = (a11 * detscale) * a22 - fabs(a21);
+        if (fabs(detpiv) >= fabs(a21) / 2) {
+          pivsiz = 2; i1 = bj; i2 = bi;
+          const double rdet = recip_nr(detpiv);
+          e11 = (a22 * detscale) * rdet;
+          e21 = (-a21 * detscale) * rdet;
+          e22 = (a11 * detscale) * rdet;
+        } else if (fabs(a11) > fabs(a22)) {
+          i1 = bj;
         } else {
-          const double a11 = (double)blk[map[mm]][map[mm]], a22 = (double)blk[map[t]][map[t]];
-          const double a21 = (double)blk[map[mm]][map[t]];
-          const double detscale = recip_nr(fabs(a21));
-          const double detpiv = (a11 * detscale) * a22 - fabs(a21);
-          if (fabs(detpiv) >= fabs(a21) / 2) {
-            pivsiz = 2; i1 = mm; i2 = t;
-            const double rdet = recip_nr(detpiv);
-            s_d[0] = (a22 * detscale) * rdet;   // d11 (logical q <- mm)
-            s_d[1] = (-a21 * detscale) * rdet;  // d21
-            s_d[2] = (a11 * detscale) * rdet;   // d22 (logical q+1 <- t)
-          } else if (fabs(a11) > fabs(a22)) {
-            pivsiz = 1; i1 = mm;
+          i1 = bi;
+        }
+      }
+      if (pivsiz > 0) {
+        // logical swaps q <-> i1, then q+1 <-> i2 (i2 > i1 >= q) on the
+        // updated map; P1, P2 are the physical pivots at q and q+1
+        const int pa = map[q], pb = map[i1];
+        const int cq1 = (pivsiz == 2) ? ((i1 == q + 1) ? pa : map[q + 1]) : -1;
+        const int ci2 = (pivsiz == 2) ? map[i2] : -1;
+        __syncwarp();
+        if (lane == 0) {
+          map[q] = pb; map[i1] = pa; inv[pb] = q; inv[pa] = i1;
+          if (pivsiz == 2) { map[q + 1] = ci2; map[i2] = cq1; inv[ci2] = q + 1; inv[cq1] = i2; }
+          s_dec[0] = pivsiz; s_dec[1] = pb; s_dec[2] = ci2;
+        }
+        __syncwarp();
+        const int X = lane, lx = inv[X];
+        if (pivsiz == 1) {
+          const int P = pb;
+          T dT;
+          if (kF64) {
+            const double d11 = rdiag[P];
+            dT = (T)d11;
+            if (lane == 0) { dd[2 * q] = d11; dd[2 * q + 1] = 0.0; }
           } else {
-            pivsiz = 1; i1 = t;
+            // FP32 factors: the L column uses the FP32 reciprocal; D^{-1} is
+            // formed in FP64 during the trailing update, off the critical path
+            dT = T(1) / blk[P][P];
+          }
+          if (X < bs && lx > q) outb[q][X] = blk[P][X] * dT;  // L(lx, q) = A(X, P) / A(P, P)
+        } else {
+          if (lane == 0) {
+            dd[2 * q] = e11; dd[2 * q + 1] = e21;
+            dd[2 * q + 2] = dinf(); dd[2 * q + 3] = e22;
+          }
+          if (X < bs && lx > q + 1) {
+            const T v1 = blk[pb][X], v2 = blk[ci2][X];
+            outb[q][X] = (T)e11 * v1 + (T)e21 * v2;
+            outb[q + 1][X] = (T)e21 * v1 + (T)e22 * v2;
           }
         }
-        // logical swaps q <-> i1, then q+1 <-> i2 (i2 > i1 >= q); the four
-        // physical indices whose logical position changed are published
-        int sw[4] = {-1, -1, -1, -1};
-        {
-          const int a = map[q], b = map[i1];
-          map[q] = b; map[i1] = a; inv[b] = q; inv[a] = i1;
-          sw[0] = a; sw[1] = b;
-        }
-        if (pivsiz == 2) {
-          const int a = map[q + 1], b = map[i2];
-          map[q + 1] = b; map[i2] = a; inv[b] = q + 1; inv[a] = i2;
-          sw[2] = a; sw[3] = b;
-        }
-        for (int z = 0; z < 4; ++z) s_sw[z] = sw[z];
-        if (pivsiz == 1) {
-          const double d11 = rdiag[map[q]];
-          s_d[0] = d11;
-          dd[2 * q] = d11; dd[2 * q + 1] = 0.0;
-        } else {
-          dd[2 * q] = s_d[0]; dd[2 * q + 1] = s_d[1];
-          dd[2 * q + 2] = dinf(); dd[2 * q + 3] = s_d[2];
-        }
+      } else if (lane == 0) {
+        s_dec[0] = 0;
       }
-      s_piv[0] = pivsiz;
-      s_piv[1] = map[q];
-      s_piv[2] = (pivsiz == 2) ? map[q + 1] : -1;
     }
     __syncthreads();
-    const int pivsiz = s_piv[0];
+    const int pivsiz = s_dec[0];
     if (pivsiz == 0) {
       if (!action) { singular = true; break; }
-      // remaining logical columns are zero pivots: zero their L entries
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int R = R0 + k;
-        if (R < bs && colok && lj >= q && li[k] >= lj) blk[C][R] = T(0);
-      }
+      // the remaining logical columns are zero pivots: their L columns stay zero
       if (tid >= q && tid < bs) { dd[2 * tid] = 0.0; dd[2 * tid + 1] = 0.0; }
       __syncthreads();
       break;
     }
-    // refresh cached logical indices of the swapped physical positions
-#pragma unroll
-    for (int z = 0; z < 4; ++z) {
-      const int ph = s_sw[z];
-      if (ph >= 0) {
-        const int nlg = inv[ph];
-        if (ph == C) lj = nlg;
-        if (ph >= R0 && ph < R0 + 8) {
-#pragma unroll
-          for (int k = 0; k < 8; ++k)
-            if (R0 + k == ph) li[k] = nlg;
-        }
-      }
-    }
+    // ---- trailing update, one pair per thread, both copies written
+    const int li = inv[R], lj = inv[C];
     if (pivsiz == 1) {
-      const int P = s_piv[1];
-      const T d11 = (T)s_d[0];
-      const T wc = blk[C][P] * d11;  // A(P, C) D^{-1}, from the pivot row
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int R = R0 + k;
-        if (R < bs && colok && li[k] > q) {
-          const T wr = blk[R][P];  // A(P, R)
-          if (lj > q) blk[C][R] -= wr * wc;
-          else if (C == P) blk[C][R] = wr * d11;  // L column of the pivot
-        }
+      const int P = s_dec[1];
+      if (!kF64 && tid == kDiagThreads - 1) {  // an idle (non-pair) thread
+        dd[2 * q] = recip_nr((double)blk[P][P]);
+        dd[2 * q + 1] = 0.0;
+      }
+      if (mine && li > q && lj > q) {
+        const T nv = blk[C][R] - blk[P][R] * outb[q][C];  // A(R,P) (A(C,P) / A(P,P))
+        blk[C][R] = nv;
+        blk[R][C] = nv;
       }
       __syncthreads();
       q += 1;
     } else {
-      const int P1 = s_piv[1], P2 = s_piv[2];
-      const T e11 = (T)s_d[0], e21 = (T)s_d[1], e22 = (T)s_d[2];
-      const T w1c = blk[C][P1], w2c = blk[C][P2];
-      const T g1 = e11 * w1c + e21 * w2c, g2 = e21 * w1c + e22 * w2c;
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int R = R0 + k;
-        if (R < bs && colok && li[k] > q + 1) {
-          const T w1r = blk[R][P1], w2r = blk[R][P2];
-          if (lj > q + 1) blk[C][R] -= w1r * g1 + w2r * g2;
-          else if (C == P1) blk[C][R] = e11 * w1r + e21 * w2r;
-          else if (C == P2) blk[C][R] = e21 * w1r + e22 * w2r;
-        }
+      const int P1 = s_dec[1], P2 = s_dec[2];
+      if (mine && li > q + 1 && lj > q + 1) {
+        const T nv = blk[C][R] - (blk[P1][R] * outb[q][C] + blk[P2][R] * outb[q + 1][C]);
+        blk[C][R] = nv;
+        blk[R][C] = nv;
       }
-      if (C == P1 && P2 >= R0 && P2 < R0 + 8) blk[P1][P2] = T(0);  // L(q+1, q) = 0
       __syncthreads();
       q += 2;
     }
@@ -296,14 +314,13 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
     if (tid == 0) { st->status = kDevSingular; st->bs = 0; }
     return;
   }
-  // write L11 (logical lower part, unit diagonal), D, step buffer, permutation
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int R = R0 + k;
-    if (R < bs && C < bs) {
-      const int i = li[k], j = lj;
+  // ---- write L11 (logical lower part, unit diagonal), D, step buffer, perm
+  for (int e = tid; e < kBlk * kBlk; e += kDiagThreads) {
+    const int j = e >> 5, X = e & 31;  // logical column, physical row
+    if (j < bs && X < bs) {
+      const int i = inv[X];
       if (i >= j) {
-        const T v = (i == j) ? T(1) : blk[C][R];
+        const T v = (i == j) ? T(1) : outb[j][X];
         fd.L[(int64_t)(p + j) * fd.ld + p + i] = v;
         fd.step[j * kBlk + i] = (double)v;
       }
