@@ -450,8 +450,7 @@ struct Numeric : NumericBase {
   DevBuf<char> tc_scratch;
   int* d_tc_status = nullptr;
 
-  void run_tc_contrib(int f0, int f1, cudaStream_t s) {
-    if (!use_tc) return;
+  std::vector<TcProblem> tc_problems(int f0, int f1) const {
     std::vector<TcProblem> ps;
     for (int f = f0; f < f1; ++f) {
       const FrontDesc<T>& d = hfd[f];
@@ -470,6 +469,12 @@ struct Numeric : NumericBase {
       p.lower = 1;
       ps.push_back(p);
     }
+    return ps;
+  }
+
+  void run_tc_contrib(int f0, int f1, cudaStream_t s) {
+    if (!use_tc) return;
+    const std::vector<TcProblem> ps = tc_problems(f0, f1);
     if (ps.empty()) return;
     tc_scratch.ensure(tc_gemm_scratch_bytes(ps));
     float ms_split = 0, ms_gemm = 0;
@@ -477,6 +482,268 @@ struct Numeric : NumericBase {
                     profile ? &ms_split : nullptr, profile ? &ms_gemm : nullptr) != 0)
       throw CudaFail{cudaErrorUnknown, __LINE__};
     if (profile) { prof_tc_ms += ms_gemm; prof_tc_launches += 1; }
+  }
+
+  // ---------------- captured factorisation (CUDA graph) ----------------
+  // After an eager factorisation in which no front delayed a column, the
+  // next same-pattern factorisation plans every level up front (sizes are
+  // then fixed: no front receives delayed columns), uploads all front
+  // descriptors and tensor-core job tables once, and captures the whole
+  // level sweep as one graph.  Each replay is checked on the device's
+  // results (every front OK with nelim == n); otherwise the factorisation is
+  // redone eagerly.  The graph reads the values from aval_buf and the
+  // scaling from scale_buf, so callers' pointers may change between calls.
+  static constexpr int kGraphFallback = 1000;
+  bool last_zero_delay = false;
+  cudaGraphExec_t fgraph = nullptr;
+  int fgraph_nlaunch = 0;
+  bool fgraph_scaled = false;
+  std::vector<void*> fgraph_blobs;
+  std::vector<FrontDesc<T>> fg_hfd;
+  std::vector<const void*> fgraph_key;
+  int fg_maxfront = 0, fg_maxsn = 0;
+
+  void drop_fgraph() {
+    if (fgraph) cudaGraphExecDestroy(fgraph);
+    fgraph = nullptr;
+    for (void* b : fgraph_blobs) cudaFree(b);
+    fgraph_blobs.clear();
+    fgraph_key.clear();
+  }
+
+  std::vector<const void*> graph_key() const {
+    return {aval_buf.p, scale_buf.p, ws_W.p,    ws_swap.p, ws_LD.p,   ws_step.p,
+            ws_lperm.p, contrib.p,   tc_scratch.p, d_fd,   d_st,      d_stats};
+  }
+
+  void build_fgraph(bool scaled) {
+    drop_fgraph();
+    cudaStream_t s = stream;
+    const int nn = S->nnodes;
+    const auto& co = S->copts;
+    // plan: no delayed columns anywhere, so front sizes are the symbolic ones
+    size_t wsW = 0, wsSwap = 0, wsLD = 0, wsStep = 0, wsLp = 0;
+    fg_maxfront = 0; fg_maxsn = 0;
+    for (int l = 0; l < S->nlev; ++l) {
+      size_t w1 = 0, w2 = 0, w3 = 0;
+      const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1];
+      for (int f = f0; f < f1; ++f) {
+        const int node = S->node_of[f];
+        const int m = S->nrow[node], n = S->ncol[node], ld = (m + 3) / 4 * 4, cm = m - n;
+        ndin_[f] = 0; m_[f] = m; n_[f] = n; ld_[f] = ld;
+        w1 += (size_t)ld * kBlk;
+        w2 += (size_t)ld * 64 + 256;
+        w3 += (size_t)cm * n;
+        fg_maxfront = std::max(fg_maxfront, m);
+        fg_maxsn = std::max(fg_maxsn, n);
+        for (int c : S->children[node]) doff_[S->front_of[c]] = 0;
+      }
+      wsW = std::max(wsW, w1); wsSwap = std::max(wsSwap, w2); wsLD = std::max(wsLD, w3);
+      wsStep = std::max(wsStep, (size_t)(f1 - f0) * (kBlk * kBlk + 2 * kBlk + 64));
+      wsLp = std::max(wsLp, (size_t)(f1 - f0) * kBlk);
+    }
+    ws_W.ensure(wsW + 64);
+    ws_swap.ensure(wsSwap + 64);
+    ws_LD.ensure(wsLD + 64);
+    ws_step.ensure(wsStep);
+    ws_lperm.ensure(wsLp);
+    farena.rewind();
+    darena.rewind();
+    iarena.rewind();
+    for (int l = 0; l < S->nlev; ++l) {
+      const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1];
+      size_t oW = 0, oS = 0, oL = 0;
+      for (int f = f0; f < f1; ++f) {
+        const int node = S->node_of[f];
+        FrontDesc<T>& d = hfd[f];
+        d = FrontDesc<T>{};
+        d.m = m_[f]; d.n = n_[f]; d.ld = ld_[f];
+        d.nrow = S->nrow[node]; d.ncol = S->ncol[node];
+        d.ndelay_in = 0;
+        d.cm = d.nrow - d.ncol;
+        d.ldc = d.cm;
+        d.node = node;
+        d.L = (T*)farena.alloc((size_t)d.ld * d.n * sizeof(T));
+        d.D = (double*)darena.alloc((size_t)2 * d.n * sizeof(double) + 16);
+        d.perm = (int*)iarena.alloc((size_t)d.n * sizeof(int));
+        d.opos = (int*)iarena.alloc((size_t)d.n * sizeof(int));
+        d.C = d.cm > 0 ? contrib.p + S->contrib_off[f] : nullptr;
+        d.W = ws_W.p + oW; oW += (size_t)d.ld * kBlk;
+        d.swapbuf = ws_swap.p + oS; oS += (size_t)d.ld * 64 + 256;
+        d.LD = ws_LD.p + oL; oL += (size_t)d.cm * d.n;
+        d.step = ws_step.p + (size_t)(f - f0) * (kBlk * kBlk + 2 * kBlk + 64);
+        d.lperm = ws_lperm.p + (size_t)(f - f0) * kBlk;
+        d.tc = (use_tc && d.cm >= tc_min_cm) ? 1 : 0;
+      }
+    }
+    fg_hfd = hfd;
+    CK(cudaMemcpy(d_fd, hfd.data(), nn * sizeof(FrontDesc<T>), cudaMemcpyHostToDevice));
+    // tensor-core job tables, one device blob per level
+    std::vector<TcPlan> tplans(S->nlev);
+    std::vector<const void*> tblob(S->nlev, nullptr);
+    if (use_tc) {
+      size_t scr = 0;
+      std::vector<std::vector<TcProblem>> lps(S->nlev);
+      for (int l = 0; l < S->nlev; ++l) {
+        lps[l] = tc_problems(S->lvl_start[l], S->lvl_start[l + 1]);
+        if (!lps[l].empty()) scr = std::max(scr, tc_gemm_scratch_bytes(lps[l]));
+      }
+      if (scr > 0) tc_scratch.ensure(scr);
+      for (int l = 0; l < S->nlev; ++l) {
+        if (lps[l].empty()) continue;
+        if (tc_gemm_prepare(lps[l], tc_scratch.p, tplans[l]) != 0)
+          throw CudaFail{cudaErrorUnknown, __LINE__};
+        void* b = nullptr;
+        CK(cudaMalloc(&b, tplans[l].blob.size()));
+        fgraph_blobs.push_back(b);
+        CK(cudaMemcpy(b, tplans[l].blob.data(), tplans[l].blob.size(), cudaMemcpyHostToDevice));
+        tblob[l] = b;
+      }
+    }
+    const double* d_scale = scaled ? scale_buf.p : nullptr;
+    const long long l0 = g_launches.load();
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    try {
+      CK(cudaMemsetAsync(d_st, 0, nn * sizeof(FrontState), s));
+      CK(cudaMemsetAsync(d_tc_status, 0, sizeof(int), s));
+      CK(cudaMemsetAsync(d_stats, 0, sizeof(Stats), s));
+      for (int l = 0; l < S->nlev; ++l) {
+        const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1], nf = f1 - f0;
+        int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0;
+        int64_t maxz = 0;
+        for (int f = f0; f < f1; ++f) {
+          const int node = S->node_of[f];
+          max_m = std::max(max_m, m_[f]);
+          max_n = std::max(max_n, n_[f]);
+          max_cm = std::max(max_cm, hfd[f].cm);
+          max_ent = std::max<int>(max_ent, (int)(S->nptr[node + 1] - S->nptr[node]));
+          maxz = std::max(maxz, std::max<int64_t>((int64_t)ld_[f] * n_[f],
+                                                  (int64_t)hfd[f].cm * hfd[f].cm));
+        }
+        const int* fr = S->d_fronts + f0;
+        launch_zero_fronts<T>(d_fd, fr, nf, (int)std::min<int64_t>(maxz, 1 << 30), s);
+        launch_load_a<T>(d_fd, fr, nf, S->d_nptr, S->d_nlist, aval_buf.p, S->d_rlist, S->d_rptr,
+                         d_scale, max_ent, s);
+        launch_init_perm<T>(d_fd, fr, nf, S->d_sptr, max_n, s);
+        launch_assemble_contrib<T>(d_fd, S->d_cols + S->cols_start[l],
+                                   S->cols_start[l + 1] - S->cols_start[l], S->d_pairs,
+                                   S->d_rdir, S->d_rdir_ptr, s);
+        const int steps = (max_n + kBlk - 1) / kBlk;
+        for (int st = 0; st < steps; ++st) {
+          int mr = 0, tr = 0, tc = 0;
+          for (int f = f0; f < f1; ++f) {
+            mr = std::max(mr, m_[f] - kBlk * st);
+            tr = std::max(tr, m_[f] - kBlk * (st + 1));
+            tc = std::max(tc, n_[f] - kBlk * (st + 1));
+          }
+          launch_app_step<T>(d_fd, d_st, fr, nf, st, std::max(mr, 1), tr, tc, co.action, co.u,
+                             co.small, s, nullptr);
+        }
+        launch_app_finish<T>(d_fd, d_st, fr, nf, s);
+        const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
+        launch_tpp<T>(d_fd, d_st, fr, nf, co.action, co.u, co.small, tpp_all, s);
+        launch_calc_ld<T>(d_fd, d_st, fr, nf, max_cm, max_n, s);
+        launch_contrib_gemm<T>(d_fd, d_st, fr, nf, max_cm, s);
+        if (tblob[l] && tc_gemm_launch(tplans[l], tblob[l], d_tc_status, s, tc_chunk) != 0)
+          throw CudaFail{cudaErrorUnknown, __LINE__};
+        launch_stats<T>(d_fd, d_st, fr, nf, max_n, d_stats, s);
+      }
+    } catch (...) {
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      g_launches -= g_launches.load() - l0;
+      drop_fgraph();
+      throw;
+    }
+    CK(cudaStreamEndCapture(s, &g));
+    fgraph_nlaunch = (int)(g_launches.load() - l0);
+    g_launches -= fgraph_nlaunch;  // counted at each replay instead
+    const cudaError_t e = cudaGraphInstantiate(&fgraph, g, 0);
+    cudaGraphDestroy(g);
+    CK(e);
+    fgraph_scaled = scaled;
+    fgraph_key = graph_key();
+  }
+
+  // One factorisation by graph replay; kGraphFallback if it must be redone
+  // eagerly (a front delayed columns or failed), else the SSIDS flag.
+  int factor_graph(const double* aval, bool on_device, const double* scaling) {
+    cudaStream_t s = stream;
+    const int nn = S->nnodes;
+    aval_buf.ensure(std::max<int64_t>(S->nnz, 1));
+    if (scaling) scale_buf.ensure(S->n);
+    if (!fgraph || fgraph_scaled != (scaling != nullptr) || graph_key() != fgraph_key)
+      build_fgraph(scaling != nullptr);
+    CK(cudaEventRecord(ev[0], s));
+    CK(cudaMemcpyAsync(aval_buf.p, aval, S->nnz * sizeof(double),
+                       on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+    if (scaling)
+      CK(cudaMemcpyAsync(scale_buf.p, scaling, S->n * sizeof(double), cudaMemcpyHostToDevice, s));
+    // an eager factorisation since the capture may have changed the descriptors
+    hfd = fg_hfd;
+    CK(cudaMemcpyAsync(d_fd, hfd.data(), nn * sizeof(FrontDesc<T>), cudaMemcpyHostToDevice, s));
+    CK(cudaGraphLaunch(fgraph, s));
+    note_launches(fgraph_nlaunch);
+    Stats hs;
+    int tcs = 0;
+    CK(cudaMemcpyAsync(hst.data(), d_st, nn * sizeof(FrontState), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&hs, d_stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&tcs, d_tc_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(ev[1], s));
+    CK(cudaStreamSynchronize(s));
+    cur_aval = aval_buf.p;
+    bool ok = tcs == 0;
+    for (int f = 0; f < nn && ok; ++f)
+      ok = hst[f].status == kDevOk && hst[f].nelim == n_[f];
+    if (!ok) {
+      last_zero_delay = false;
+      return kGraphFallback;
+    }
+    const auto& co = S->copts;
+    const bool use_app = co.pivot_method != 3;
+    const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
+    int nfp = 0, nsp = 0;
+    lvl_max_m.assign(S->nlev, 0);
+    lvl_max_nelim.assign(S->nlev, 0);
+    for (int l = 0; l < S->nlev; ++l)
+      for (int f = S->lvl_start[l]; f < S->lvl_start[l + 1]; ++f) {
+        nelim_[f] = hst[f].nelim;
+        napp_[f] = hst[f].step;
+        lvl_max_m[l] = std::max(lvl_max_m[l], m_[f]);
+        lvl_max_nelim[l] = std::max(lvl_max_nelim[l], nelim_[f]);
+        if (use_app && napp_[f] < n_[f]) nfp += n_[f] - napp_[f];
+        const bool tpp_ran = tpp_all || (m_[f] == n_[f]);
+        if (!use_app) nfp += n_[f] - nelim_[f];
+        else if (tpp_ran && napp_[f] < n_[f]) nsp += n_[f] - nelim_[f];
+      }
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    timing[0] = ms;
+    return finish_stats(hs, fg_maxfront, fg_maxsn, nfp, nsp);
+  }
+
+  int finish_stats(const Stats& hs, int maxfront, int maxsn, int nfp, int nsp) {
+    stats.num_delay = hs.num_delay;
+    stats.num_factor = hs.num_factor;
+    stats.num_flops = hs.num_flops;
+    stats.num_neg = hs.num_neg;
+    stats.num_two = hs.num_two;
+    stats.num_zero = hs.num_zero;
+    stats.maxfront = maxfront;
+    stats.maxsupernode = maxsn;
+    stats.not_first_pass = nfp;
+    stats.not_second_pass = nsp;
+    stats.flag = 0;
+    // delays left at a root are unrecoverable
+    for (int f = 0; f < S->nnodes; ++f)
+      if (S->parent[S->node_of[f]] < 0 && nelim_[f] < n_[f]) stats.flag = -5;
+    if (stats.num_zero > 0 && stats.flag == 0) stats.flag = 7;
+    if (posdef) {
+      if (stats.num_neg > 0 || stats.num_zero > 0 || stats.num_two > 0) stats.flag = -6;
+      stats.num_neg = 0; stats.num_two = 0; stats.num_zero = 0;
+    }
+    return stats.flag;
   }
 
   const double* cur_aval = nullptr;  // device values of the last factor
@@ -519,6 +786,7 @@ struct Numeric : NumericBase {
     for (auto e : pev) cudaEventDestroy(e);
     cudaFree(d_fd); cudaFree(d_st); cudaFree(d_stats); cudaFree(d_dwork); cudaFree(d_tc_status);
     drop_graphs();
+    drop_fgraph();
     cudaFree(d_sn); cudaFree(d_children);
     for (auto& e : ev) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
@@ -527,11 +795,24 @@ struct Numeric : NumericBase {
 
   int factor(const double* aval, bool on_device, const double* scaling,
              cudaStream_t user_stream) override {
-    cudaStream_t s = stream;
     if (user_stream) CK(cudaStreamSynchronize(user_stream));
+    solve_ready = false;
+    if (use_graphs && !profile && last_zero_delay) {
+      stats = spral_ssids_thread_stats{};
+      const int r = factor_graph(aval, on_device, scaling);
+      if (r != kGraphFallback) return r;
+    }
+    const int r = factor_eager(aval, on_device, scaling);
+    bool zero_delay = r >= 0 && S->copts.pivot_method != 3;
+    for (int f = 0; f < S->nnodes && zero_delay; ++f) zero_delay = nelim_[f] == n_[f];
+    last_zero_delay = zero_delay;
+    return r;
+  }
+
+  int factor_eager(const double* aval, bool on_device, const double* scaling) {
+    cudaStream_t s = stream;
     const int nn = S->nnodes;
     const auto& co = S->copts;
-    solve_ready = false;
     stats = spral_ssids_thread_stats{};
     CK(cudaEventRecord(ev[0], s));
     if (on_device) {
@@ -725,26 +1006,7 @@ struct Numeric : NumericBase {
     CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
     timing[0] = ms;
     (void)host_wait;
-    stats.num_delay = hs.num_delay;
-    stats.num_factor = hs.num_factor;
-    stats.num_flops = hs.num_flops;
-    stats.num_neg = hs.num_neg;
-    stats.num_two = hs.num_two;
-    stats.num_zero = hs.num_zero;
-    stats.maxfront = maxfront;
-    stats.maxsupernode = maxsn;
-    stats.not_first_pass = nfp;
-    stats.not_second_pass = nsp;
-    stats.flag = 0;
-    // delays left at a root are unrecoverable
-    for (int f = 0; f < nn; ++f)
-      if (S->parent[S->node_of[f]] < 0 && nelim_[f] < n_[f]) stats.flag = -5;
-    if (stats.num_zero > 0 && stats.flag == 0) stats.flag = 7;
-    if (posdef) {
-      if (stats.num_neg > 0 || stats.num_zero > 0 || stats.num_two > 0) stats.flag = -6;
-      stats.num_neg = 0; stats.num_two = 0; stats.num_zero = 0;
-    }
-    return stats.flag;
+    return finish_stats(hs, maxfront, maxsn, nfp, nsp);
   }
 
   void prepare_solve() {

@@ -154,6 +154,17 @@ namespace ssids300 {
 // sum is added (round-to-nearest) into the register accumulator.
 constexpr int kTcChunk = 8;
 size_t tc_gemm_scratch_bytes(const std::vector<TcProblem>& ps);
+// Descriptor tables of one tc_gemm launch pair (split + GEMM), built on the
+// host; tc_gemm_launch only enqueues kernels, so it can be graph-captured
+// once the blob is in device memory.
+struct TcPlan {
+  std::vector<char> blob;
+  size_t o_jobs = 0, o_tiles = 0, o_maps = 0;
+  int nsplit = 0, ntiles = 0, maxr = 0, maxk = 0, grid = 0;
+};
+int tc_gemm_prepare(const std::vector<TcProblem>& ps, void* scratch, TcPlan& plan);
+int tc_gemm_launch(const TcPlan& plan, const void* d_blob, int* status, cudaStream_t s,
+                   int chunk);
 // Returns 0, or a negative code: -1 allocation, -2 tensor-map encoding,
 // -3 launch error.  Device-side pipeline timeouts are reported in *status.
 int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf, int* status,

@@ -469,8 +469,8 @@ TcBuffers::~TcBuffers() {
 
 static size_t up64(size_t b) { return (b + 63) & ~size_t(63); }
 
-int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf, int* status,
-                cudaStream_t s, int chunk, float* ms_split, float* ms_gemm) {
+int tc_gemm_prepare(const std::vector<TcProblem>& ps, void* scratch, TcPlan& plan) {
+  plan = TcPlan{};
   if (ps.empty()) return 0;
   std::vector<SplitJob> sj;
   std::vector<TcJob> jobs;
@@ -504,12 +504,54 @@ int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf,
   // deepest tiles first: the persistent CTAs take tiles round-robin
   std::stable_sort(tiles.begin(), tiles.end(),
                    [](const int4& a, const int4& b) { return a.w > b.w; });
+  plan.o_jobs = up64(sj.size() * sizeof(SplitJob));
+  plan.o_tiles = plan.o_jobs + up64(jobs.size() * sizeof(TcJob));
+  plan.o_maps = plan.o_tiles + up64(tiles.size() * sizeof(int4));
+  const size_t total = plan.o_maps + maps.size() * sizeof(CUtensorMap);
+  plan.blob.assign(total, 0);
+  memcpy(plan.blob.data(), sj.data(), sj.size() * sizeof(SplitJob));
+  memcpy(plan.blob.data() + plan.o_jobs, jobs.data(), jobs.size() * sizeof(TcJob));
+  memcpy(plan.blob.data() + plan.o_tiles, tiles.data(), tiles.size() * sizeof(int4));
+  memcpy(plan.blob.data() + plan.o_maps, maps.data(), maps.size() * sizeof(CUtensorMap));
+  plan.nsplit = (int)sj.size();
+  plan.ntiles = (int)tiles.size();
+  plan.maxr = maxr;
+  plan.maxk = maxk;
+  // launch configuration, fixed here so that tc_gemm_launch only enqueues
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  plan.grid = std::min(plan.ntiles, std::max(nsm, 1));
+  if (cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)tc_gemm_smem_bytes()) != cudaSuccess)
+    return -3;
+  return 0;
+}
 
+int tc_gemm_launch(const TcPlan& plan, const void* d_blob, int* status, cudaStream_t s, int chunk) {
+  if (plan.nsplit == 0) return 0;
+  const char* d = static_cast<const char*>(d_blob);
+  dim3 sg((plan.maxr + 31) / 32, (plan.maxk + 31) / 32, (unsigned)plan.nsplit);
+  k_split<<<sg, 256, 0, s>>>(reinterpret_cast<const SplitJob*>(d));
+  note_launches(1);
+  if (plan.ntiles > 0) {
+    k_tc_gemm<<<plan.grid, TC_THREADS, tc_gemm_smem_bytes(), s>>>(
+        reinterpret_cast<const TcJob*>(d + plan.o_jobs),
+        reinterpret_cast<const int4*>(d + plan.o_tiles), plan.ntiles,
+        reinterpret_cast<const CUtensorMap*>(d + plan.o_maps), chunk, status);
+    note_launches(1);
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+}
+
+int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf, int* status,
+                cudaStream_t s, int chunk, float* ms_split, float* ms_gemm) {
+  if (ps.empty()) return 0;
+  TcPlan plan;
+  const int rp = tc_gemm_prepare(ps, scratch, plan);
+  if (rp != 0) return rp;
   // one upload of all descriptors through a pinned staging buffer
-  const size_t o_jobs = up64(sj.size() * sizeof(SplitJob));
-  const size_t o_tiles = o_jobs + up64(jobs.size() * sizeof(TcJob));
-  const size_t o_maps = o_tiles + up64(tiles.size() * sizeof(int4));
-  const size_t total = o_maps + maps.size() * sizeof(CUtensorMap);
+  const size_t total = plan.blob.size();
   if (!buf.uploaded && cudaEventCreateWithFlags(&buf.uploaded, cudaEventDisableTiming) != cudaSuccess)
     return -1;
   if (cudaEventSynchronize(buf.uploaded) != cudaSuccess) return -3;  // staging free again
@@ -523,49 +565,35 @@ int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf,
     if (cudaMalloc(&buf.d_stage, nc) != cudaSuccess) return -1;
     buf.cap = nc;
   }
-  char* h = static_cast<char*>(buf.h_stage);
-  memcpy(h, sj.data(), sj.size() * sizeof(SplitJob));
-  memcpy(h + o_jobs, jobs.data(), jobs.size() * sizeof(TcJob));
-  memcpy(h + o_tiles, tiles.data(), tiles.size() * sizeof(int4));
-  memcpy(h + o_maps, maps.data(), maps.size() * sizeof(CUtensorMap));
-  char* d = static_cast<char*>(buf.d_stage);
-  if (cudaMemcpyAsync(d, h, total, cudaMemcpyHostToDevice, s) != cudaSuccess) return -3;
+  memcpy(buf.h_stage, plan.blob.data(), total);
+  if (cudaMemcpyAsync(buf.d_stage, buf.h_stage, total, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return -3;
   if (cudaEventRecord(buf.uploaded, s) != cudaSuccess) return -3;
-
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   const bool timed = ms_split || ms_gemm;
-  if (timed) {
-    for (auto& e : ev) cudaEventCreate(&e);
-    cudaEventRecord(ev[0], s);
-  }
-  dim3 sg((maxr + 31) / 32, (maxk + 31) / 32, (unsigned)sj.size());
-  k_split<<<sg, 256, 0, s>>>(reinterpret_cast<const SplitJob*>(d));
-  note_launches(1);
-  if (timed) cudaEventRecord(ev[1], s);
-  if (!tiles.empty()) {
-    static int nsm = 0;
-    if (nsm == 0) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      if (nsm <= 0) nsm = 1;
-    }
-    const size_t smem = tc_gemm_smem_bytes();
-    cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    const int grid = std::min((int)tiles.size(), nsm);
-    k_tc_gemm<<<grid, TC_THREADS, smem, s>>>(
-        reinterpret_cast<const TcJob*>(d + o_jobs), reinterpret_cast<const int4*>(d + o_tiles),
-        (int)tiles.size(), reinterpret_cast<const CUtensorMap*>(d + o_maps), chunk, status);
+  if (!timed) return tc_gemm_launch(plan, buf.d_stage, status, s, chunk);
+  for (auto& e : ev) cudaEventCreate(&e);
+  // split and GEMM timed separately
+  TcPlan only_split = plan;
+  only_split.ntiles = 0;
+  cudaEventRecord(ev[0], s);
+  int rc = tc_gemm_launch(only_split, buf.d_stage, status, s, chunk);
+  cudaEventRecord(ev[1], s);
+  if (rc == 0 && plan.ntiles > 0) {
+    const char* d = static_cast<const char*>(buf.d_stage);
+    k_tc_gemm<<<plan.grid, TC_THREADS, tc_gemm_smem_bytes(), s>>>(
+        reinterpret_cast<const TcJob*>(d + plan.o_jobs),
+        reinterpret_cast<const int4*>(d + plan.o_tiles), plan.ntiles,
+        reinterpret_cast<const CUtensorMap*>(d + plan.o_maps), chunk, status);
     note_launches(1);
+    rc = cudaGetLastError() == cudaSuccess ? 0 : -3;
   }
-  if (timed) {
-    cudaEventRecord(ev[2], s);
-    cudaEventSynchronize(ev[2]);
-    if (ms_split) cudaEventElapsedTime(ms_split, ev[0], ev[1]);
-    if (ms_gemm) cudaEventElapsedTime(ms_gemm, ev[1], ev[2]);
-    for (auto& e : ev) cudaEventDestroy(e);
-  }
-  return cudaGetLastError() == cudaSuccess ? 0 : -3;
+  cudaEventRecord(ev[2], s);
+  cudaEventSynchronize(ev[2]);
+  if (ms_split) cudaEventElapsedTime(ms_split, ev[0], ev[1]);
+  if (ms_gemm) cudaEventElapsedTime(ms_gemm, ev[1], ev[2]);
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
 }
 
 }  // namespace ssids300

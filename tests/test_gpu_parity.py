@@ -242,3 +242,45 @@ def test_gpu_graph_replay_matches_direct_launches(precision, monkeypatch):
     assert np.array_equal(res["1"][0], res["1"][1])
     tol = BWD_TOL if precision == ssids.PRECISION_FP64 else 1e-5
     assert M.scaled_bwd_error(p, r, v2, res["1"][2], b).max() <= tol
+
+
+def _diag_positions(p, r):
+    """Index of each column's diagonal entry in lower-CSC value order."""
+    return np.array([p[j] + np.nonzero(r[p[j]:p[j + 1]] == j)[0][0] for j in range(len(p) - 1)])
+
+
+@pytest.mark.parametrize("precision", [ssids.PRECISION_FP64, ssids.PRECISION_MIXED])
+def test_gpu_captured_refactorisation_matches_eager(precision, monkeypatch):
+    """Same-pattern refactorisations replayed from the captured graph give
+    bitwise the results of the eager launch sequence; a refactorisation whose
+    values cause delayed pivots falls back to the eager path and is still
+    correct; the graph is used again afterwards."""
+    torch = pytest.importorskip("torch")
+    p, r, v = M.random_indef(400, density=0.02, seed=11, diag_scale=0.01)
+    ak = ssids.analyse(p, r, ssids.order_mindeg(p, r))
+    dpos = _diag_positions(p, r)
+    v_dd = v.copy()
+    v_dd[dpos] = 50.0  # strongly diagonal: no delays
+    v_dd2 = v_dd.copy()
+    v_dd2[dpos] = 40.0
+    b = np.random.default_rng(3).standard_normal((400, 2))
+    seq = [v_dd, v_dd2, v, v_dd2]  # the third set delays pivots
+    res = {}
+    for graphs in ("1", "0"):
+        monkeypatch.setenv("SPRAL_GB300_GRAPHS", graphs)
+        fk = ssids.Fkeep(ak, seq[0], ssids.Options(precision=precision))
+        assert fk.inform.num_delay == 0
+        out = []
+        for vals in seq[1:]:
+            vd = torch.tensor(vals, dtype=torch.float64, device="cuda")
+            assert fk.refactor_dev(vd.data_ptr()) >= 0
+            out.append((fk.solve(b), fk.inform.num_neg, fk.inform.num_delay))
+        res[graphs] = out
+        fk.free()
+    for (xa, na, da), (xb, nb, db) in zip(res["1"], res["0"]):
+        assert na == nb and da == db
+        assert np.array_equal(xa, xb)
+    assert res["1"][1][2] > 0  # the third value set exercised delays
+    tol = 1e-13 if precision == ssids.PRECISION_FP64 else 1e-4
+    for (x, _, _), vals in zip(res["1"], seq[1:]):
+        assert M.scaled_bwd_error(p, r, vals, x, b).max() <= tol
