@@ -126,6 +126,13 @@ void spral_ssids_gpu_subtree_alter_dbl(bool posdef, void* numeric, const double*
 int spral_ssids_gpu_refactor_dev(void* numeric, const double* aval_dev,
                                  struct spral_ssids_thread_stats* stats, void* stream);
 
+/* Same-pattern refactorisation with host values (and optional host
+ * scaling): the numeric subtree constructor's inputs, reusing the handle,
+ * its device memory and, when no pivot was delayed last time, its captured
+ * factorisation graph.  Returns the SSIDS flag. */
+int spral_ssids_gpu_refactor(void* numeric, const double* aval, const double* scaling,
+                             struct spral_ssids_thread_stats* stats);
+
 /* Solve with x in device memory (pivot order, FP64).  job: 0 full,
  * 1 fwd, 2 diag, 3 bwd, 4 diag_bwd (ssids_solve job codes,
  * src/ssids/ssids.f90:1232-1246). */
@@ -223,6 +230,14 @@ int spral_ssids_gpu_ldlt_app_factor_noalloc(int m, int n, int* perm_dev, double*
 int spral_ssids_gpu_tc_gemm_f32(int M, int N, int K, const float* A, int lda, const float* B,
                                 int ldb, float* C, int ldc, int lower, int chunk, int reps,
                                 float* ms);
+
+/* Per-node inertia of the last factorisation: out[3*node + {0, 1, 2}] =
+ * (negative eigenvalues, 2x2 pivots, zero pivots) of each node's D, nodes
+ * numbered 0-based as in the symbolic subtree.  Batched factorisations of
+ * many independent matrices (one forest) sum these per matrix.  No
+ * reference counterpart (the reference reports whole-subtree totals,
+ * src/ssids/cpu/NumericSubtree.hxx:249-280).  Returns 0 or -51. */
+int spral_ssids_gpu_node_inertia(const void* numeric, int* out);
 
 /* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
 int spral_ssids_gpu_device_count(void);

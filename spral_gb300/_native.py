@@ -82,12 +82,14 @@ def _declare(L):
     f("spral_ssids_gpu_subtree_alter_dbl", None, B, P, P)
     f("spral_ssids_gpu_set_options", I, P, ctypes.POINTER(GpuOptions))
     f("spral_ssids_gpu_refactor_dev", I, P, P, ctypes.POINTER(ThreadStats), P)
+    f("spral_ssids_gpu_refactor", I, P, P, P, ctypes.POINTER(ThreadStats))
     f("spral_ssids_gpu_solve_dev", I, P, I, I, P, I, P)
     f("spral_ssids_gpu_last_timing", I, P, P)
     f("spral_ssids_gpu_device_count", I)
     f("spral_ssids_gpu_debug_front", I, P, I, P, P, P, P)
     f("spral_ssids_gpu_solve_refined_dev", I, P, I, P, P, I, P, P)
     f("spral_ssids_gpu_launch_count", ctypes.c_longlong)
+    f("spral_ssids_gpu_node_inertia", I, P, P)
     f("spral_ssids_gpu_set_profiling", None, P, I)
     f("spral_ssids_gpu_profile_stats", None, P, P)
     f("spral_ssids_gpu_fp64_peak_tflops", D, I)

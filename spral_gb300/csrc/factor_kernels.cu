@@ -896,7 +896,7 @@ __global__ void __launch_bounds__(128) k_calc_ld(FrontDesc<T>* fds, const FrontS
 // ------------------------------------------------------------------------
 template <typename T>
 __global__ void k_stats(const FrontDesc<T>* fds, const FrontState* sts, const int* fronts,
-                        Stats* stats) {
+                        Stats* stats, int* node_counts) {
   const int f = fronts[blockIdx.y];
   const FrontDesc<T> fd = fds[f];
   const int nelim = sts[f].nelim;
@@ -924,6 +924,12 @@ __global__ void k_stats(const FrontDesc<T>* fds, const FrontState* sts, const in
     if (neg) atomicAdd(&stats->num_neg, neg);
     if (two) atomicAdd(&stats->num_two, two);
     if (zero) atomicAdd(&stats->num_zero, zero);
+    if (node_counts) {  // per-node inertia (neg, two, zero), indexed by node
+      int* nc = node_counts + 3 * fd.node;
+      if (neg) atomicAdd(nc, neg);
+      if (two) atomicAdd(nc + 1, two);
+      if (zero) atomicAdd(nc + 2, zero);
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     long long m = fd.m, a = fd.m - nelim + 1;
@@ -1009,10 +1015,10 @@ void launch_contrib_gemm(FrontDesc<T>* fd, FrontState* st, const int* fronts, in
 
 template <typename T>
 void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
-                  int max_n, Stats* stats, cudaStream_t s) {
+                  int max_n, Stats* stats, int* node_counts, cudaStream_t s) {
   if (nf <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_n, 256), 64));
-  { k_stats<T><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts, stats); note_launches(1); }
+  { k_stats<T><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts, stats, node_counts); note_launches(1); }
 }
 
 #define INST(T)                                                                                 \
@@ -1026,7 +1032,7 @@ void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* front
   template void launch_contrib_gemm<T>(FrontDesc<T>*, FrontState*, const int*, int, int,        \
                                        cudaStream_t);                                           \
   template void launch_stats<T>(const FrontDesc<T>*, const FrontState*, const int*, int, int,    \
-                                Stats*, cudaStream_t);
+                                Stats*, int*, cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

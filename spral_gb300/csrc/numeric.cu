@@ -245,6 +245,22 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
     for (int c : S->children[i]) lev[i] = std::max(lev[i], lev[c] + 1);
     nlev = std::max(nlev, lev[i] + 1);
   }
+  {
+    // split crowded levels: kernels index a level's fronts in blockIdx.y
+    // (at most 65535) and the tensor-core split kernel two jobs per front in
+    // blockIdx.z; fronts of one level are independent, so consecutive
+    // sub-levels keep the schedule valid
+    constexpr int kMaxLevelFronts = 16384;
+    std::vector<int> cnt(nlev, 0), base(nlev + 1, 0), seen(nlev, 0);
+    for (int i = 0; i < nn; ++i) cnt[lev[i]]++;
+    for (int l = 0; l < nlev; ++l)
+      base[l + 1] = base[l] + std::max(1, (cnt[l] + kMaxLevelFronts - 1) / kMaxLevelFronts);
+    for (int i = 0; i < nn; ++i) {
+      const int l = lev[i];
+      lev[i] = base[l] + seen[l]++ / kMaxLevelFronts;
+    }
+    nlev = base[nlev];
+  }
   S->nlev = nlev;
   S->lvl_start.assign(nlev + 1, 0);
   for (int i = 0; i < nn; ++i) S->lvl_start[lev[i] + 1]++;
@@ -387,6 +403,7 @@ struct NumericBase {
   virtual void alter(const double* d) = 0;
   virtual Symbolic* symbolic() = 0;
   virtual int debug_front(int node, int* info, double* L, double* D, int* perm) = 0;
+  virtual int node_inertia(int* out) = 0;
 };
 
 template <typename T>
@@ -449,6 +466,7 @@ struct Numeric : NumericBase {
   TcBuffers tcbuf;
   DevBuf<char> tc_scratch;
   int* d_tc_status = nullptr;
+  int* d_ncount = nullptr;  // per-node inertia counts (neg, two, zero)
 
   std::vector<TcProblem> tc_problems(int f0, int f1) const {
     std::vector<TcProblem> ps;
@@ -512,8 +530,8 @@ struct Numeric : NumericBase {
   }
 
   std::vector<const void*> graph_key() const {
-    return {aval_buf.p, scale_buf.p, ws_W.p,    ws_swap.p, ws_LD.p,   ws_step.p,
-            ws_lperm.p, contrib.p,   tc_scratch.p, d_fd,   d_st,      d_stats};
+    return {aval_buf.p, scale_buf.p, ws_W.p, ws_swap.p, ws_LD.p, ws_step.p, ws_lperm.p,
+            contrib.p,  tc_scratch.p, d_fd,  d_st,      d_stats, d_ncount};
   }
 
   void build_fgraph(bool scaled) {
@@ -608,6 +626,7 @@ struct Numeric : NumericBase {
       CK(cudaMemsetAsync(d_st, 0, nn * sizeof(FrontState), s));
       CK(cudaMemsetAsync(d_tc_status, 0, sizeof(int), s));
       CK(cudaMemsetAsync(d_stats, 0, sizeof(Stats), s));
+      CK(cudaMemsetAsync(d_ncount, 0, 3 * (size_t)nn * sizeof(int), s));
       for (int l = 0; l < S->nlev; ++l) {
         const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1], nf = f1 - f0;
         int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0;
@@ -647,7 +666,7 @@ struct Numeric : NumericBase {
         launch_contrib_gemm<T>(d_fd, d_st, fr, nf, max_cm, s);
         if (tblob[l] && tc_gemm_launch(tplans[l], tblob[l], d_tc_status, s, tc_chunk) != 0)
           throw CudaFail{cudaErrorUnknown, __LINE__};
-        launch_stats<T>(d_fd, d_st, fr, nf, max_n, d_stats, s);
+        launch_stats<T>(d_fd, d_st, fr, nf, max_n, d_stats, d_ncount, s);
       }
     } catch (...) {
       cudaStreamEndCapture(s, &g);
@@ -764,6 +783,7 @@ struct Numeric : NumericBase {
     CK(cudaMalloc(&d_stats, sizeof(Stats)));
     CK(cudaMalloc(&d_dwork, std::max(nn, 1) * sizeof(int4)));
     CK(cudaMalloc(&d_tc_status, sizeof(int)));
+    CK(cudaMalloc(&d_ncount, 3 * (size_t)std::max(nn, 1) * sizeof(int)));
     {
       const char* gr = getenv("SPRAL_GB300_GRAPHS");
       use_graphs = !(gr && gr[0] == '0');
@@ -785,6 +805,7 @@ struct Numeric : NumericBase {
   ~Numeric() override {
     for (auto e : pev) cudaEventDestroy(e);
     cudaFree(d_fd); cudaFree(d_st); cudaFree(d_stats); cudaFree(d_dwork); cudaFree(d_tc_status);
+    cudaFree(d_ncount);
     drop_graphs();
     drop_fgraph();
     cudaFree(d_sn); cudaFree(d_children);
@@ -841,6 +862,7 @@ struct Numeric : NumericBase {
     CK(cudaMemsetAsync(d_st, 0, nn * sizeof(FrontState), s));
     CK(cudaMemsetAsync(d_tc_status, 0, sizeof(int), s));
     CK(cudaMemsetAsync(d_stats, 0, sizeof(Stats), s));
+    CK(cudaMemsetAsync(d_ncount, 0, 3 * (size_t)nn * sizeof(int), s));
     lvl_max_m.assign(S->nlev, 0);
     lvl_max_nelim.assign(S->nlev, 0);
     int maxfront = 0, maxsn = 0, nfp = 0, nsp = 0;
@@ -957,7 +979,7 @@ struct Numeric : NumericBase {
       run_tc_contrib(f0, f1, s);
       if (profile) CK(cudaEventRecord(pev[2 * l + 1], s));
       pmark(tm(), kPhStats, s);
-      launch_stats<T>(d_fd, d_st, fr, nf, max_n, d_stats, s);
+      launch_stats<T>(d_fd, d_st, fr, nf, max_n, d_stats, d_ncount, s);
       pmark(tm(), kPhHost, s);
       CK(cudaMemcpyAsync(hst.data() + f0, d_st + f0, nf * sizeof(FrontState),
                          cudaMemcpyDeviceToHost, s));
@@ -1218,6 +1240,11 @@ struct Numeric : NumericBase {
     return it;
   }
 
+  int node_inertia(int* out) override {
+    CK(cudaMemcpy(out, d_ncount, 3 * (size_t)S->nnodes * sizeof(int), cudaMemcpyDeviceToHost));
+    return 0;
+  }
+
   int debug_front(int node, int* info, double* Lout, double* Dout, int* Pout) override {
     const int f = S->front_of[node];
     info[0] = m_[f]; info[1] = n_[f]; info[2] = nelim_[f]; info[3] = ndin_[f]; info[4] = ld_[f];
@@ -1379,6 +1406,20 @@ int spral_ssids_gpu_refactor_dev(void* numeric, const double* aval_dev,
   }
 }
 
+int spral_ssids_gpu_refactor(void* numeric, const double* aval, const double* scaling,
+                             struct spral_ssids_thread_stats* stats) {
+  NumericBase* N = static_cast<NumericBase*>(numeric);
+  try {
+    int fl = N->factor(aval, false, scaling, nullptr);
+    if (stats) *stats = N->stats;
+    return fl;
+  } catch (CudaFail const& e) {
+    return map_cuda_error(e, stats);
+  } catch (std::bad_alloc const&) {
+    return -50;
+  }
+}
+
 static int host_solve(const void* numeric, int job, int nrhs, double* x, int ldx) {
   NumericBase* N = const_cast<NumericBase*>(static_cast<const NumericBase*>(numeric));
   Symbolic* S = N->symbolic();
@@ -1504,6 +1545,18 @@ void spral_ssids_gpu_phase_times(const void* numeric, double* ms, long long* cou
   for (int i = 0; i < ssids300::kPhCount; ++i) {
     ms[i] = N->ptimer.ms[i];
     counts[i] = N->ptimer.cnt[i];
+  }
+}
+
+/* Per-node inertia of the last factorisation: out[3*node + {0, 1, 2}] =
+ * (negative eigenvalues, 2x2 pivots, zero pivots) of the node's D (0-based
+ * node numbering of the symbolic subtree). */
+int spral_ssids_gpu_node_inertia(const void* numeric, int* out) {
+  auto* N = const_cast<ssids300::NumericBase*>(static_cast<const ssids300::NumericBase*>(numeric));
+  try {
+    return N->node_inertia(out);
+  } catch (...) {
+    return -51;
   }
 }
 

@@ -124,7 +124,7 @@ void launch_contrib_gemm(FrontDesc<T>* fd, FrontState* st, const int* fronts, in
                          cudaStream_t s);
 template <typename T>
 void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
-                  int max_n, Stats* stats, cudaStream_t s);
+                  int max_n, Stats* stats, int* node_counts, cudaStream_t s);
 
 // ---------------- tensor-core Schur update (tc_gemm.cu) ----------------
 // C_i -= A_i B_i^T (lower if requested) with 3xTF32 split products on

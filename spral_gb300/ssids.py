@@ -188,6 +188,27 @@ class Fkeep:
         inf.matrix_rank = self.akeep.n - st.num_zero
         return inf
 
+    def refactor(self, val, scaling=None):
+        """Same-pattern refactorisation from host values."""
+        st = ThreadStats()
+        self.val = np.ascontiguousarray(val, dtype=np.float64)
+        sc = None if scaling is None else np.ascontiguousarray(scaling, dtype=np.float64)
+        fl = _native.lib().spral_ssids_gpu_refactor(self.num, _P(self.val),
+                                                    None if sc is None else _P(sc),
+                                                    ctypes.byref(st))
+        self.stats = {k: getattr(st, k) for k, _ in ThreadStats._fields_}
+        self.inform = self._inform(st)
+        return fl
+
+    def node_inertia(self):
+        """(nnodes, 3) array: negative eigenvalues, 2x2 pivots and zero
+        pivots of each node's D from the last factorisation."""
+        out = np.zeros(3 * self.akeep.nnodes, dtype=np.int32)
+        fl = _native.lib().spral_ssids_gpu_node_inertia(self.num, _P(out))
+        if fl != 0:
+            raise RuntimeError(f"spral_gb300 node_inertia failed, flag {fl}")
+        return out.reshape(-1, 3)
+
     def refactor_dev(self, val_dev_ptr, stream=0):
         """Same-pattern refactorisation from a device pointer of values."""
         st = ThreadStats()
