@@ -102,5 +102,11 @@ class BatchFkeep:
         B, two = self.bak.stack_rhs(bs)
         return self.bak.split(self.fk.solve(B), two)
 
+    def solve_refined(self, bs):
+        """Solve with FP64 iterative refinement of the whole batch against its
+        FP64 values (options max_refine / refine_tol)."""
+        B, two = self.bak.stack_rhs(bs)
+        return self.bak.split(self.fk.solve_refined(B), two)
+
     def free(self):
         self.fk.free()
