@@ -239,6 +239,11 @@ int spral_ssids_gpu_tc_gemm_f32(int M, int N, int K, const float* A, int lda, co
  * src/ssids/cpu/NumericSubtree.hxx:249-280).  Returns 0 or -51. */
 int spral_ssids_gpu_node_inertia(const void* numeric, int* out);
 
+/* Free and total memory of the current device (cudaMemGetInfo), for
+ * callers that admit work by device memory.  No reference counterpart.
+ * Returns 0 or -51. */
+int spral_ssids_gpu_mem_info(size_t* free_bytes, size_t* total_bytes);
+
 /* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
 int spral_ssids_gpu_device_count(void);
 

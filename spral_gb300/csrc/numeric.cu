@@ -22,6 +22,7 @@
 #include <new>
 #include <stdexcept>
 #include <type_traits>
+#include <mutex>
 #include <vector>
 
 #include <cstdlib>
@@ -37,6 +38,8 @@ struct CudaFail {
 };
 
 static std::atomic<long long> g_launches{0};
+// stream capture and graph instantiation are serialised across handles
+static std::mutex g_capture_mutex;
 
 void PhaseTimer::mark(int phase, cudaStream_t s) {
   if (used == cap) {
@@ -80,7 +83,12 @@ PhaseTimer::~PhaseTimer() {
   delete[] ev;
   delete[] ph;
 }
-void note_launches(int k) { g_launches += k; }
+// launches issued by this thread (a capture counts the launches it records)
+static thread_local long long t_launches = 0;
+void note_launches(int k) {
+  g_launches += k;
+  t_launches += k;
+}
 double fp64_peak_tflops(int device);
 void launch_recip_probe(const double* x, double* y, int n, cudaStream_t s);
 
@@ -404,6 +412,8 @@ struct NumericBase {
   virtual Symbolic* symbolic() = 0;
   virtual int debug_front(int node, int* info, double* L, double* D, int* perm) = 0;
   virtual int node_inertia(int* out) = 0;
+  virtual cudaStream_t get_stream() const = 0;
+  DevBuf<double> hsolve;  // device copy of host right-hand sides (host-buffer solves)
 };
 
 template <typename T>
@@ -619,7 +629,8 @@ struct Numeric : NumericBase {
       }
     }
     const double* d_scale = scaled ? scale_buf.p : nullptr;
-    const long long l0 = g_launches.load();
+    std::lock_guard<std::mutex> lock(g_capture_mutex);
+    const long long l0 = t_launches;
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     try {
@@ -671,13 +682,15 @@ struct Numeric : NumericBase {
     } catch (...) {
       cudaStreamEndCapture(s, &g);
       if (g) cudaGraphDestroy(g);
-      g_launches -= g_launches.load() - l0;
+      g_launches -= t_launches - l0;
+      t_launches = l0;
       drop_fgraph();
       throw;
     }
     CK(cudaStreamEndCapture(s, &g));
-    fgraph_nlaunch = (int)(g_launches.load() - l0);
+    fgraph_nlaunch = (int)(t_launches - l0);
     g_launches -= fgraph_nlaunch;  // counted at each replay instead
+    t_launches = l0;
     const cudaError_t e = cudaGraphInstantiate(&fgraph, g, 0);
     cudaGraphDestroy(g);
     CK(e);
@@ -1122,11 +1135,12 @@ struct Numeric : NumericBase {
         note_launches(g.nlaunch);
         return;
       }
-    if (sgraphs.size() >= 8) {
+    if (sgraphs.size() >= 32) {
       cudaGraphExecDestroy(sgraphs.front().exec);
       sgraphs.erase(sgraphs.begin());
     }
-    const long long l0 = g_launches.load();
+    std::lock_guard<std::mutex> lock(g_capture_mutex);
+    const long long l0 = t_launches;
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     try {
@@ -1134,11 +1148,14 @@ struct Numeric : NumericBase {
     } catch (...) {
       cudaStreamEndCapture(s, &g);
       if (g) cudaGraphDestroy(g);
+      g_launches -= t_launches - l0;
+      t_launches = l0;
       throw;
     }
     CK(cudaStreamEndCapture(s, &g));
-    const int nl = (int)(g_launches.load() - l0);
+    const int nl = (int)(t_launches - l0);
     g_launches -= nl;  // counted at each replay instead
+    t_launches = l0;
     cudaGraphExec_t ge = nullptr;
     const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
@@ -1239,6 +1256,8 @@ struct Numeric : NumericBase {
     }
     return it;
   }
+
+  cudaStream_t get_stream() const override { return stream; }
 
   int node_inertia(int* out) override {
     CK(cudaMemcpy(out, d_ncount, 3 * (size_t)S->nnodes * sizeof(int), cudaMemcpyDeviceToHost));
@@ -1424,21 +1443,23 @@ static int host_solve(const void* numeric, int job, int nrhs, double* x, int ldx
   NumericBase* N = const_cast<NumericBase*>(static_cast<const NumericBase*>(numeric));
   Symbolic* S = N->symbolic();
   const int n = S->n;
-  double* dx = nullptr;
   try {
     CK(cudaSetDevice(S->device));
-    CK(cudaMalloc(&dx, std::max<size_t>((size_t)n * nrhs, 1) * sizeof(double)));
+    // a per-handle device buffer and the handle's stream: no allocation and
+    // no device-wide synchronisation per call
+    N->hsolve.ensure(std::max<size_t>((size_t)n * nrhs, 1));
+    double* dx = N->hsolve.p;
+    cudaStream_t s = N->get_stream();
     for (int r = 0; r < nrhs; ++r)
-      CK(cudaMemcpy(dx + (size_t)r * n, x + (size_t)r * ldx, n * sizeof(double),
-                    cudaMemcpyHostToDevice));
+      CK(cudaMemcpyAsync(dx + (size_t)r * n, x + (size_t)r * ldx, n * sizeof(double),
+                         cudaMemcpyHostToDevice, s));
     N->solve_dev(job, nrhs, dx, n, nullptr);
     for (int r = 0; r < nrhs; ++r)
-      CK(cudaMemcpy(x + (size_t)r * ldx, dx + (size_t)r * n, n * sizeof(double),
-                    cudaMemcpyDeviceToHost));
-    cudaFree(dx);
+      CK(cudaMemcpyAsync(x + (size_t)r * ldx, dx + (size_t)r * n, n * sizeof(double),
+                         cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
     return 0;
   } catch (CudaFail const& e) {
-    if (dx) cudaFree(dx);
     return map_cuda_error(e, nullptr);
   }
 }
@@ -1546,6 +1567,16 @@ void spral_ssids_gpu_phase_times(const void* numeric, double* ms, long long* cou
     ms[i] = N->ptimer.ms[i];
     counts[i] = N->ptimer.cnt[i];
   }
+}
+
+/* Free and total device memory of the current device (cudaMemGetInfo);
+ * used by callers that admit work by memory.  Returns 0 or -51. */
+int spral_ssids_gpu_mem_info(size_t* free_bytes, size_t* total_bytes) {
+  if (cudaMemGetInfo(free_bytes, total_bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return -51;
+  }
+  return 0;
 }
 
 /* Per-node inertia of the last factorisation: out[3*node + {0, 1, 2}] =

@@ -86,3 +86,21 @@ def test_oracle_singular_action():
     assert F.stats["num_zero"] == 1
     G = oracle.OracleFactor(ak, v, options=oracle.default_options(action=False))
     assert G.stats["flag"] == ssids.SSIDS_ERROR_SINGULAR
+
+
+def test_every_called_c_entry_point_has_a_prototype():
+    """ctypes passes arguments of an unprototyped function as C ints, which
+    truncates 64-bit handles (a crash once the handle lies above 4 GiB, as
+    it does for handles made in worker threads)."""
+    import glob
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    files = (glob.glob(os.path.join(root, "spral_gb300", "*.py")) +
+             glob.glob(os.path.join(root, "tests", "*.py")) +
+             [os.path.join(root, "bench.py"), os.path.join(root, "__graft_entry__.py")])
+    called = set()
+    for f in files:
+        called |= set(re.findall(r"\.(spral_ssids_gpu_\w+|spral_gb300_\w+)\(", open(f).read()))
+    declared = set(re.findall(r'f\("(\w+)"',
+                              open(os.path.join(root, "spral_gb300", "_native.py")).read()))
+    assert called <= declared, sorted(called - declared)
