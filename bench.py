@@ -53,10 +53,14 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--mixed-only", action="store_true",
                     help="profiling aid: time only the mixed-precision path and print its object")
-    ap.add_argument("--workload", default="lap3d", choices=["lap3d", "batch"],
+    ap.add_argument("--workload", default="lap3d", choices=["lap3d", "batch", "serve"],
                     help="lap3d: the headline 48^3 Laplacian; batch: many small 2D Laplacians "
-                         "factored and solved as one forest")
+                         "factored and solved as one forest; serve: a Poisson stream of factor "
+                         "and refactor requests through the request loop")
     ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--serve-count", type=int, default=96)
+    ap.add_argument("--serve-rate", type=float, default=8.0)
+    ap.add_argument("--serve-slots", type=int, default=4)
     return ap.parse_args()
 
 
@@ -526,12 +530,107 @@ def run_batch(args):
     bf.free()
 
 
+def run_serve(args):
+    """The request loop on a seeded Poisson stream: 3D 7-point Laplacians with
+    n log-uniform in [1e3, 2e5] (shift uniform[-0.5, 0]) and same-pattern
+    refactorisations (diagonal x uniform[0.5, 2]), nrhs uniform in [1, 64],
+    FP64, solves refined to bwd err <= 1e-14.  The timed region is the whole
+    stream; `value` is requests served per second with overlapping slots and
+    `alone` the same stream served one request at a time."""
+    world, rank, local = dist_setup(args)
+    import torch
+    torch.cuda.set_device(local)
+    from spral_gb300 import _native, matrices as M, serve, ssids
+    L = _native.lib()
+    reqs = serve.poisson_stream(args.serve_count, rate=args.serve_rate, seed=2025 + rank)
+    opts = ssids.Options(max_refine=10, refine_tol=REFINE_TOL)
+    # untimed warm-up: a few requests through a throw-away server
+    warm = serve.Server(slots=args.serve_slots, options=opts)
+    warm.run(serve.poisson_stream(4, rate=1000.0, seed=1, nmax=20000), realtime=False)
+    warm.close()
+    srv = serve.Server(slots=args.serve_slots, options=opts)
+    for q in reqs:  # the host-side analyse is outside the timed region
+        if q.kind == "factor":
+            srv.akeeps[q.key] = ssids.analyse(q.ptr, q.row, q.order)
+    lc0 = L.spral_ssids_gpu_launch_count()
+    clk = Clocks(local) if rank == 0 else None
+    t0 = time.perf_counter()
+    res = srv.run(reqs, realtime=True)
+    span = time.perf_counter() - t0
+    clocks = clk.stop() if clk else None
+    launches = L.spral_ssids_gpu_launch_count() - lc0
+    srv.close()
+    errors = [r.error for r in res if r.error]
+    lat = np.array([r.latency for r in res if r.error is None]) * 1e3
+    pats, bwd = {}, 0.0
+    for q, r in zip(reqs, res):
+        if q.kind == "factor":
+            pats[q.key] = (q.ptr, q.row)
+        if r.error is None:
+            p, rw = pats[q.key]
+            bwd = max(bwd, float(M.scaled_bwd_error(p, rw, q.val, r.x, q.b).max()))
+    alone = serve.Server(slots=1, options=opts)
+    alone.akeeps.update(srv.akeeps)
+    ta = time.perf_counter()
+    ref = alone.run(reqs, realtime=False)
+    t_alone = time.perf_counter() - ta
+    alone.close()
+    same = all(a.error is None and np.array_equal(a.x, b.x) for a, b in zip(res, ref))
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        t_all, done = 0.0, 0
+        for q in reqs:
+            if q.kind != "factor":
+                continue
+            ak = srv.akeeps[q.key]
+            t1 = time.perf_counter()
+            F = oracle.OracleFactor(ak, q.val, blas=True)
+            F.solve(q.b)
+            t_all += time.perf_counter() - t1
+            done += 1
+            if t_all > 20.0:
+                break
+        cpu = {"value": done / t_all, "unit": "requests/s", "cores": os.cpu_count(),
+               "kind": "port",
+               "sample": f"the first {done} factor requests of the stream, one at a time, "
+                         "factor + solve (OpenBLAS threads = all cores)"}
+    nfac = sum(1 for q in reqs if q.kind == "factor")
+    if rank == 0:
+        line = {"metric": "requests served per second (Poisson stream); p50/p99 latency",
+                "workload": "serve", "value": len(reqs) / span, "unit": "requests/s",
+                "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": span * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic (seeded Poisson stream of 3D Laplacians)",
+                "config": {"workload": f"{len(reqs)} requests ({nfac} new matrices, "
+                                       f"{len(reqs) - nfac} same-pattern refactorisations), "
+                                       "3D 7-point Laplacians n log-uniform in [1e3, 2e5], "
+                                       "shift uniform[-0.5,0], nrhs uniform[1,64], "
+                                       f"Poisson arrivals at {args.serve_rate}/s, "
+                                       f"{args.serve_slots} slots, memory-based admission",
+                           "errors": errors[:3], "bwd_err": bwd,
+                           "same_alone_and_in_mix": bool(same)},
+                "p50_ms": float(np.percentile(lat, 50)) if lat.size else None,
+                "p99_ms": float(np.percentile(lat, 99)) if lat.size else None,
+                "alone": {"value": len(reqs) / t_alone, "unit": "requests/s",
+                          "note": "same stream, one request at a time, no arrival waits"},
+                "e2e": {"value": len(reqs) / span, "unit": "requests/s",
+                        "h2d_bytes_per_step": int(sum(q.val.nbytes + q.b.nbytes for q in reqs)),
+                        "d2h_bytes_per_step": int(sum(q.b.nbytes for q in reqs)),
+                        "path": "serve.Server.run (host values and right-hand sides)"},
+                "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clocks}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_gpu(args)
 
