@@ -53,10 +53,11 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--mixed-only", action="store_true",
                     help="profiling aid: time only the mixed-precision path and print its object")
-    ap.add_argument("--workload", default="lap3d", choices=["lap3d", "batch", "serve"],
+    ap.add_argument("--workload", default="lap3d", choices=["lap3d", "batch", "serve", "tc-gemm"],
                     help="lap3d: the headline 48^3 Laplacian; batch: many small 2D Laplacians "
                          "factored and solved as one forest; serve: a Poisson stream of factor "
-                         "and refactor requests through the request loop")
+                         "and refactor requests through the request loop; tc-gemm: the "
+                         "tensor-core Schur update kernel alone")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-count", type=int, default=96)
     ap.add_argument("--serve-rate", type=float, default=8.0)
@@ -315,12 +316,11 @@ def run_gpu(args):
     fp64_peak = L.spral_ssids_gpu_fp64_peak_tflops(local)
     achieved = ps[1] / (ps[0] * 1e-3) / 1e12 if ps[0] > 0 else 0.0
     traffic = None
-    tfile = os.path.join(HERE, "profiles", "contrib_gemm_fp64_traffic.json")
+    tfile = os.path.join(HERE, "profiles", "contrib_gemm_fp64_lap3d48.md")
     if os.path.exists(tfile):
-        try:
-            traffic = json.load(open(tfile)).get("dram_bytes_per_launch")
-        except Exception:
-            traffic = None
+        import re
+        m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", open(tfile).read())
+        traffic = float(m.group(1)) if m else None
     roofline = {"bound": "fp64", "kernel": "k_syrk<double,contrib> (contribution block GEMM)",
                 "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak if fp64_peak > 0 else None, "traffic": traffic,
@@ -623,8 +623,49 @@ def run_serve(args):
         print(json.dumps(line), flush=True)
 
 
+def run_tc_gemm(args):
+    """The tensor-core Schur update alone (C -= A B^T, 3xTF32 split products,
+    chunked FP32 accumulation): the largest contribution block of the 48^3
+    workload (lower, 2304 x 2304, depth 1152) and a large square update;
+    timed with CUDA events by the library, error against an FP64 product."""
+    import torch
+    from spral_gb300 import _native
+    L = _native.lib()
+    peak, src = tf32_peak_tflops()
+    out = []
+    for M_, N_, K_, lower in ((2304, 2304, 1152, 1), (8192, 8192, 2048, 0)):
+        rng = np.random.default_rng(M_ + K_)
+        A = rng.standard_normal((M_, K_)).astype(np.float32)
+        B = rng.standard_normal((N_, K_)).astype(np.float32)
+        dA = torch.tensor(A.ravel(order="F"), device="cuda")
+        dB = torch.tensor(B.ravel(order="F"), device="cuda")
+        dC = torch.zeros(M_ * N_, device="cuda", dtype=torch.float32)
+        assert L.spral_ssids_gpu_tc_gemm_f32(M_, N_, K_, dA.data_ptr(), M_, dB.data_ptr(), N_,
+                                             dC.data_ptr(), M_, lower, -1, 0, None) == 0
+        got = dC.cpu().numpy().reshape(M_, N_, order="F").astype(np.float64)
+        ref = -(A.astype(np.float64) @ B.astype(np.float64).T)
+        mask = np.tril(np.ones((M_, N_), bool)) if lower else np.ones((M_, N_), bool)
+        rms = float(np.sqrt(np.mean((got - ref)[mask] ** 2)) / np.sqrt(K_))
+        ms = (ctypes.c_float * 2)()
+        assert L.spral_ssids_gpu_tc_gemm_f32(M_, N_, K_, dA.data_ptr(), M_, dB.data_ptr(), N_,
+                                             dC.data_ptr(), M_, lower, -1,
+                                             max(args.steps, 3), ms) == 0
+        flops = 2.0 * K_ * mask.sum()
+        alg = flops / (ms[1] * 1e-3) / 1e12
+        out.append({"shape": f"{M_}x{N_}x{K_}" + (" lower" if lower else ""),
+                    "gemm_ms": ms[1], "split_ms": ms[0], "fp32_update_tflops": alg,
+                    "tensor_tflops": 3 * alg, "frac": 3 * alg / peak,
+                    "rms_err_over_sqrtK": rms})
+    print(json.dumps({"metric": "tensor-core Schur update TFLOP/s (3xTF32)", "workload": "tc-gemm",
+                      "value": out[-1]["tensor_tflops"], "unit": "TFLOP/s",
+                      "peak": peak, "peak_source": src, "cases": out}), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "tc-gemm":
+        run_tc_gemm(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
