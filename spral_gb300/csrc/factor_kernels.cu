@@ -2,7 +2,7 @@
 //
 // One APP step processes a block of up to 32 candidate columns [p, p+bs) of
 // every active front of a level at once:
-//   k_app_diag      one warp per front: complete pivoting inside the block
+//   k_app_diag      diagonal block: complete pivoting (indefinite) or none (posdef)
 //                   (semantics of block_ldlt, src/ssids/cpu/kernels/
 //                   block_ldlt.hxx:290-413), FP64 arithmetic, writes L11, D^{-1}
 //                   and the local permutation
@@ -126,7 +126,11 @@ constexpr int kDiagPairs = kBlk * (kBlk + 1) / 2;
 constexpr int kDiagThreads = (kDiagPairs + 31) / 32 * 32;
 constexpr int kDiagWarps = kDiagThreads / 32;
 
-template <typename T>
+// POSDEF: the Cholesky case (cpu/kernels/cholesky.cxx, LAPACK potrf): no
+// pivoting, pivot q is the block's q-th diagonal, and a pivot that is not
+// > 0 ends the factorisation with kDevNotPosdef.  The factors are kept as
+// L D L^T (unit L, D > 0); L_chol = L D^(1/2).
+template <typename T, bool POSDEF>
 __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, FrontState* sts,
                                                            const int* fronts, int step,
                                                            bool action, double small) {
@@ -190,10 +194,12 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
   if (tid < kBlk) wkey[tid] = 0;
   __syncthreads();
 
-  bool singular = false;
+  bool singular = false, notpd = false;
   for (int q = 0; q < bs;) {
     // ---- candidates: the logical lower triangle of the trailing block
-    {
+    if (POSDEF) {
+      if (kF64 && R == q && C == q) rdiag[q] = recip_nr((double)blk[q][q]);
+    } else {
       const int li = inv[R], lj = inv[C];
       const int hi = max(li, lj), lo = min(li, lj);
       unsigned long long key = 0;
@@ -207,13 +213,16 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
     // ---- decision and the pivot's L column(s) (warp 0; every lane takes the
     // same decision, lane X then forms row X of the new L column(s))
     if (warp == 0) {
-      const unsigned long long gk = warp_max_u64(wkey[lane]);
+      const unsigned long long gk = POSDEF ? 0ULL : warp_max_u64(wkey[lane]);
       const int pos = 1023 - (int)(gk & 0x3ffULL);
       const int bj = pos >> 5, bi = pos & 31;  // logical column, row of the maximum
       const double bv = DiagKey<T>::mag(gk);
       int pivsiz = 1, i1 = bi, i2 = -1;
       double e11 = 0.0, e21 = 0.0, e22 = 0.0;
-      if (bv < small) {
+      if (POSDEF) {
+        i1 = q;  // no pivoting
+        if (!((double)blk[q][q] > 0.0)) pivsiz = -1;
+      } else if (bv < small) {
         pivsiz = 0;
       } else if (bi != bj) {
         const int mm = map[bj], tt = map[bi];
@@ -272,11 +281,12 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
           }
         }
       } else if (lane == 0) {
-        s_dec[0] = 0;
+        s_dec[0] = pivsiz;  // 0: zero pivot, -1: not positive definite
       }
     }
     __syncthreads();
     const int pivsiz = s_dec[0];
+    if (pivsiz < 0) { notpd = true; break; }
     if (pivsiz == 0) {
       if (!action) { singular = true; break; }
       // the remaining logical columns are zero pivots: their L columns stay zero
@@ -310,8 +320,8 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
       q += 2;
     }
   }
-  if (singular) {
-    if (tid == 0) { st->status = kDevSingular; st->bs = 0; }
+  if (singular || notpd) {
+    if (tid == 0) { st->status = notpd ? kDevNotPosdef : kDevSingular; st->bs = 0; }
     return;
   }
   // ---- write L11 (logical lower part, unit diagonal), D, step buffer, perm
@@ -959,10 +969,15 @@ static inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 template <typename T>
 void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int step,
                      int max_rows, int max_trail_rows, int max_trail_cols, bool action,
-                     double u, double small, cudaStream_t s, PhaseTimer* tm) {
+                     double u, double small, cudaStream_t s, PhaseTimer* tm, bool posdef) {
   if (nf <= 0) return;
   pmark(tm, kPhDiag, s);
-  { k_app_diag<T><<<nf, kDiagThreads, 0, s>>>(fd, st, fronts, step, action, small); note_launches(1); }
+  if (posdef) {
+    k_app_diag<T, true><<<nf, kDiagThreads, 0, s>>>(fd, st, fronts, step, action, small);
+  } else {
+    k_app_diag<T, false><<<nf, kDiagThreads, 0, s>>>(fd, st, fronts, step, action, small);
+  }
+  note_launches(1);
   // apply (+ row permutation of the eliminated part in extra CTAs)
   const int napply = std::max(1, cdiv(max_rows, kApplyRows));
   const int pcols = step * kBlk;  // upper bound on p
@@ -1023,7 +1038,7 @@ void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* front
 
 #define INST(T)                                                                                 \
   template void launch_app_step<T>(FrontDesc<T>*, FrontState*, const int*, int, int, int, int,  \
-                                   int, bool, double, double, cudaStream_t, PhaseTimer*);       \
+                                   int, bool, double, double, cudaStream_t, PhaseTimer*, bool); \
   template void launch_app_finish<T>(FrontDesc<T>*, FrontState*, const int*, int, cudaStream_t); \
   template void launch_tpp<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double, double, \
                               bool, cudaStream_t);                                              \

@@ -667,8 +667,8 @@ struct Numeric : NumericBase {
             tr = std::max(tr, m_[f] - kBlk * (st + 1));
             tc = std::max(tc, n_[f] - kBlk * (st + 1));
           }
-          launch_app_step<T>(d_fd, d_st, fr, nf, st, std::max(mr, 1), tr, tc, co.action, co.u,
-                             co.small, s, nullptr);
+          launch_app_step<T>(d_fd, d_st, fr, nf, st, std::max(mr, 1), tr, tc, co.action,
+                             posdef ? 0.0 : co.u, co.small, s, nullptr, posdef);
         }
         launch_app_finish<T>(d_fd, d_st, fr, nf, s);
         const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
@@ -975,8 +975,8 @@ struct Numeric : NumericBase {
             tr = std::max(tr, m_[f] - kBlk * (st + 1));
             tc = std::max(tc, n_[f] - kBlk * (st + 1));
           }
-          launch_app_step<T>(d_fd, d_st, fr, nf, st, std::max(mr, 1), tr, tc, co.action, co.u,
-                             co.small, s, tm());
+          launch_app_step<T>(d_fd, d_st, fr, nf, st, std::max(mr, 1), tr, tc, co.action,
+                             posdef ? 0.0 : co.u, co.small, s, tm(), posdef);
         }
       }
       pmark(tm(), kPhFinish, s);
@@ -998,9 +998,10 @@ struct Numeric : NumericBase {
                          cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
       if (profile) ptimer.flush();
-      bool singular = false, bad = false;
+      bool singular = false, bad = false, notpd = false;
       for (int f = f0; f < f1; ++f) {
         if (hst[f].status == kDevSingular) singular = true;
+        else if (hst[f].status == kDevNotPosdef) notpd = true;
         else if (hst[f].status != kDevOk) bad = true;
         nelim_[f] = hst[f].nelim;
         napp_[f] = hst[f].step;
@@ -1030,6 +1031,7 @@ struct Numeric : NumericBase {
         CK(cudaMemcpy(&tcs, d_tc_status, sizeof(int), cudaMemcpyDeviceToHost));
         if (tcs != 0) bad = true;
       }
+      if (notpd) { stats.flag = -6; return stats.flag; }
       if (singular) { stats.flag = -5; return stats.flag; }
       if (bad) { stats.flag = -51; return stats.flag; }
     }
@@ -1101,11 +1103,14 @@ struct Numeric : NumericBase {
     solve_ready = true;
   }
 
-  // enqueue one solve pass of q <= kSolveRhs right-hand sides on s
+  // enqueue one solve pass of q <= kSolveRhs right-hand sides on s.
+  // Jobs: 0 full, 1 fwd, 2 diag, 3 bwd, 4 diag+bwd (L D L^T); 5 fwd and
+  // 6 bwd with the Cholesky factor L_chol = L D^(1/2) (posdef).
   void enqueue_solve(int job, int q, double* xp, int ldx, cudaStream_t s) {
-    const bool fwd = (job == 0 || job == 1);
+    const bool fwd = (job == 0 || job == 1 || job == 5);
     const bool diag = (job == 0 || job == 2 || job == 4);
-    const bool bwd = (job == 0 || job == 3 || job == 4);
+    const bool bwd = (job == 0 || job == 3 || job == 4 || job == 6);
+    const int diag_mode = diag ? 1 : (job == 6 ? 2 : 0);
     if (fwd) {
       for (int l = 0; l < S->nlev; ++l) {
         const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
@@ -1114,14 +1119,14 @@ struct Numeric : NumericBase {
         launch_fwd_gather<T>(d_sn, fr, nf, d_children, xp, ldx, q, s);
         launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, s, tm());
         pmark(tm(), kPhFwdScatter, s);
-        launch_fwd_scatter<T>(d_sn, fr, nf, xp, ldx, q, lvl_max_nelim[l], s);
+        launch_fwd_scatter<T>(d_sn, fr, nf, xp, ldx, q, lvl_max_nelim[l], s, job == 5);
       }
     }
     if (diag || bwd) {
       for (int l = S->nlev - 1; l >= 0; --l) {
         const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
         launch_bwd<T>(d_sn, S->d_fronts + f0, nf, xp, ldx, q, lvl_max_m[l], lvl_max_nelim[l],
-                      diag, bwd, s, tm());
+                      diag_mode, bwd, s, tm());
       }
     }
   }
@@ -1289,6 +1294,15 @@ struct Numeric : NumericBase {
   void enquire(int* piv_order, double* d) override {
     std::vector<double> D;
     std::vector<int> P;
+    if (posdef) {
+      // diagonal of L_chol = L D^(1/2), node by node (NumericSubtree.hxx:424-431)
+      for (int node = 0; node < S->nnodes; ++node) {
+        const int f = S->front_of[node];
+        download_dp(D, P, f);
+        for (int i = 0; i < nelim_[f]; ++i) *d++ = 1.0 / std::sqrt(D[2 * i]);
+      }
+      return;
+    }
     int piv = 0;
     for (int node = 0; node < S->nnodes; ++node) {
       const int f = S->front_of[node];
@@ -1466,23 +1480,23 @@ static int host_solve(const void* numeric, int job, int nrhs, double* x, int ldx
 
 int spral_ssids_gpu_subtree_solve_fwd_dbl(bool posdef, const void* numeric, int nrhs, double* x,
                                           int ldx) {
-  (void)posdef;
-  return host_solve(numeric, 1, nrhs, x, ldx);
+  // posdef: L_chol y = b with L_chol = L D^(1/2) (cholesky_solve_fwd)
+  return host_solve(numeric, posdef ? 5 : 1, nrhs, x, ldx);
 }
 int spral_ssids_gpu_subtree_solve_diag_dbl(bool posdef, const void* numeric, int nrhs, double* x,
                                            int ldx) {
-  (void)posdef;
+  // the diagonal solve is a no-op for posdef (NumericSubtree.hxx:343)
+  if (posdef) return 0;
   return host_solve(numeric, 2, nrhs, x, ldx);
 }
 int spral_ssids_gpu_subtree_solve_diag_bwd_dbl(bool posdef, const void* numeric, int nrhs,
                                                double* x, int ldx) {
-  (void)posdef;
-  return host_solve(numeric, 4, nrhs, x, ldx);
+  return host_solve(numeric, posdef ? 6 : 4, nrhs, x, ldx);
 }
 int spral_ssids_gpu_subtree_solve_bwd_dbl(bool posdef, const void* numeric, int nrhs, double* x,
                                           int ldx) {
-  (void)posdef;
-  return host_solve(numeric, 3, nrhs, x, ldx);
+  // posdef: L_chol^T x = y (cholesky_solve_bwd)
+  return host_solve(numeric, posdef ? 6 : 3, nrhs, x, ldx);
 }
 
 int spral_ssids_gpu_solve_dev(void* numeric, int job, int nrhs, double* x_dev, int ldx,

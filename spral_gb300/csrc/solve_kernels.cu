@@ -280,21 +280,28 @@ __global__ void __launch_bounds__(kSolveThreads)
   diag_block_solve<T, NR, true>(sn, i0, jb1, nrhs, Lb);
 }
 
+// scale_sqrt: the posdef forward solve with L_chol = L D^(1/2) returns
+// D^(-1/2) L^{-1} b, i.e. each pivot's value times sqrt(D^{-1}) (1x1 pivots
+// only in the posdef case)
 template <typename T>
 __global__ void k_fwd_scatter(const SolveNode<T>* sns, const int* nodes, double* x, int ldx,
-                              int nrhs) {
+                              int nrhs, bool scale_sqrt) {
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];
   const int tot = sn.nelim * nrhs;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
     const int i = e % sn.nelim, q = e / sn.nelim;
-    x[(int64_t)q * ldx + sn.perm[i]] = (double)sn.xloc[(int64_t)q * sn.m + i];
+    double v = (double)sn.xloc[(int64_t)q * sn.m + i];
+    if (scale_sqrt) v *= sqrt(sn.D[2 * i]);
+    x[(int64_t)q * ldx + sn.perm[i]] = v;
   }
 }
 
 // ---- backward ----
+// diag_mode: 0 none, 1 apply D^{-1} (1x1 and 2x2), 2 apply sqrt(D^{-1}) (the
+// posdef backward solve with L_chol^T = D^(1/2) L^T)
 template <typename T>
 __global__ void k_bwd_gather(const SolveNode<T>* sns, const int* nodes, const double* x, int ldx,
-                             int nrhs, bool do_diag, bool do_bwd) {
+                             int nrhs, int diag_mode, bool do_bwd) {
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];
   const int mm = do_bwd ? sn.m : sn.nelim;
   const int tot = mm * nrhs;
@@ -302,7 +309,9 @@ __global__ void k_bwd_gather(const SolveNode<T>* sns, const int* nodes, const do
     const int i = e % mm, q = e / mm;
     const int src = (i < sn.n) ? sn.perm[i] : sn.rows[sn.ncol + i - sn.n];
     double v = x[(int64_t)q * ldx + src];
-    if (do_diag && i < sn.nelim) {
+    if (diag_mode == 2 && i < sn.nelim) {
+      v *= sqrt(sn.D[2 * i]);
+    } else if (diag_mode == 1 && i < sn.nelim) {
       const double di = sn.D[2 * i];
       if (isinf(di)) {
         // second half of a 2x2: d21*x1 + d22*x2
@@ -465,20 +474,20 @@ void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_
 
 template <typename T>
 void launch_fwd_scatter(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx,
-                        int nrhs, int max_nelim, cudaStream_t s) {
+                        int nrhs, int max_nelim, cudaStream_t s, bool scale_sqrt) {
   if (nn <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_nelim * nrhs, 256), 64));
-  { k_fwd_scatter<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs); note_launches(1); }
+  { k_fwd_scatter<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, scale_sqrt); note_launches(1); }
 }
 
 template <typename T>
 void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx, int nrhs,
-                int max_m, int max_nelim, bool do_diag, bool do_bwd, cudaStream_t s,
+                int max_m, int max_nelim, int diag_mode, bool do_bwd, cudaStream_t s,
                 PhaseTimer* tm) {
   if (nn <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_m * nrhs, 256), 64));
   pmark(tm, kPhBwdGather, s);
-  { k_bwd_gather<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, do_diag, do_bwd); note_launches(1); }
+  { k_bwd_gather<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, diag_mode, do_bwd); note_launches(1); }
   if (do_bwd) {
     with_nr(nrhs, [&](auto nrc) {
       constexpr int NR = decltype(nrc)::value;
@@ -501,7 +510,7 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
   }
   int gs = std::max(1, std::min(cdiv(max_nelim * nrhs, 256), 64));
   pmark(tm, kPhBwdScatter, s);
-  { k_fwd_scatter<T><<<dim3(gs, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs); note_launches(1); }
+  { k_fwd_scatter<T><<<dim3(gs, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, false); note_launches(1); }
 }
 
 #define INST(T)                                                                                \
@@ -510,9 +519,9 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
   template void launch_fwd_steps<T>(const SolveNode<T>*, const int*, int, int, int, int,       \
                                     cudaStream_t, PhaseTimer*);                                \
   template void launch_fwd_scatter<T>(const SolveNode<T>*, const int*, int, double*, int, int, \
-                                      int, cudaStream_t);                                      \
+                                      int, cudaStream_t, bool);                                \
   template void launch_bwd<T>(const SolveNode<T>*, const int*, int, double*, int, int, int, int, \
-                              bool, bool, cudaStream_t, PhaseTimer*);
+                              int, bool, cudaStream_t, PhaseTimer*);
 INST(double)
 INST(float)
 #undef INST

@@ -25,6 +25,7 @@ enum DevStatus : int {
   kDevOk = 0,
   kDevSingular = 1,   // zero pivot with action == false  -> SSIDS_ERROR_SINGULAR
   kDevBadState = 2,   // internal consistency check failed -> SSIDS_ERROR_CUDA_UNKNOWN
+  kDevNotPosdef = 3,  // posdef factorisation met a pivot that is not > 0 -> SSIDS_ERROR_NOT_POS_DEF
 };
 
 template <typename T>
@@ -109,7 +110,7 @@ void launch_assemble_contrib(const FrontDesc<T>* fd, const int4* cols, int ncols
 template <typename T>
 void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int step,
                      int max_rows, int max_trail_rows, int max_trail_cols, bool action,
-                     double u, double small, cudaStream_t s, PhaseTimer* tm);
+                     double u, double small, cudaStream_t s, PhaseTimer* tm, bool posdef = false);
 template <typename T>
 void launch_app_finish(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf,
                        cudaStream_t s);
@@ -213,10 +214,11 @@ void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_
                       int max_m, int nrhs, cudaStream_t s, PhaseTimer* tm);
 template <typename T>
 void launch_fwd_scatter(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx,
-                        int nrhs, int max_nelim, cudaStream_t s);
+                        int nrhs, int max_nelim, cudaStream_t s, bool scale_sqrt);
 template <typename T>
+// diag_mode: 0 none, 1 D^{-1}, 2 sqrt(D^{-1}) (posdef backward solve)
 void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx, int nrhs,
-                int max_m, int max_nelim, bool do_diag, bool do_bwd, cudaStream_t s,
+                int max_m, int max_nelim, int diag_mode, bool do_bwd, cudaStream_t s,
                 PhaseTimer* tm);
 
 }  // namespace ssids300

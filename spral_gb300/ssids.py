@@ -227,7 +227,8 @@ class Fkeep:
     def solve(self, b, job=0):
         """ssids_solve (src/ssids/ssids.f90:1140) job codes: 0 full, 1 fwd,
         2 diag, 3 bwd, 4 diag_bwd."""
-        if job not in (0, 1, 2, 3, 4):
+        if job not in (0, 1, 2, 3, 4) or (self.posdef and job in (2, 4)):
+            # posdef has no diagonal solve (src/ssids/ssids.f90:1234-1238)
             raise ValueError(f"job out of range (SSIDS_ERROR_JOB_OOR={SSIDS_ERROR_JOB_OOR})")
         L = _native.lib()
         b = np.asarray(b, dtype=np.float64)
@@ -263,6 +264,15 @@ class Fkeep:
         x = np.empty_like(B)
         x[invp, :] = xp
         return x[:, 0] if one else x
+
+    def enquire_posdef(self):
+        """Diagonal entries of the Cholesky factor of a posdef factorisation,
+        node by node in pivot order (ssids_enquire_posdef)."""
+        if not self.posdef:
+            raise ValueError("enquire_posdef needs a posdef factorisation")
+        d = np.zeros(self.akeep.n, dtype=np.float64)
+        _native.lib().spral_ssids_gpu_subtree_enquire_dbl(True, self.num, None, _P(d))
+        return d
 
     def enquire_indef(self):
         """piv_order (indexed by pivot position, negative for 2x2) and d (n x 2),
