@@ -218,3 +218,19 @@ def scaled_bwd_error(ptr, row, val, x, b):
     b2 = b if b.ndim == 2 else b[:, None]
     r = b2 - sym_matvec(ptr, row, val, x2)
     return np.abs(r).max(axis=0) / (anorm * np.abs(x2).max(axis=0) + np.abs(b2).max(axis=0))
+
+
+def equilibrate(ptr, row, val, iters=3):
+    """Symmetric equilibration scaling s (S A S with unit inf-norm rows, a few
+    Ruiz-style sweeps), for tests of scaled factorisations."""
+    n = len(ptr) - 1
+    cols = np.repeat(np.arange(n), np.diff(ptr))
+    s = np.ones(n)
+    for _ in range(iters):
+        a = np.abs(val) * s[row] * s[cols]
+        m = np.zeros(n)
+        np.maximum.at(m, row, a)
+        np.maximum.at(m, cols, a)
+        m[m == 0] = 1.0
+        s /= np.sqrt(m)
+    return s

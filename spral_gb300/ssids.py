@@ -154,7 +154,11 @@ class Fkeep:
     options%use_gpu; src/ssids/ssids.f90:767).  Solves take right-hand sides
     in the user's variable order."""
 
-    def __init__(self, akeep, val, options=None, posdef=False):
+    def __init__(self, akeep, val, options=None, posdef=False, scaling=None):
+        """scaling: optional symmetric scaling s (user variable order); the
+        factors are those of S A S with S = diag(s), and solves scale the
+        right-hand side and the solution as inner_solve_cpu does
+        (src/ssids/fkeep.F90:249-315)."""
         L = _native.lib()
         if L.spral_ssids_gpu_device_count() < 1:
             raise RuntimeError("spral_gb300: no CUDA device; the numeric path has no CPU fallback")
@@ -171,10 +175,14 @@ class Fkeep:
         g = self.options.gpu_options()
         L.spral_ssids_gpu_set_options(self.sym, ctypes.byref(g))
         self.val = np.ascontiguousarray(val, dtype=np.float64)
+        # the subtree takes the scaling in pivot order, as fkeep%scaling
+        self.scaling = (None if scaling is None else
+                        np.ascontiguousarray(np.asarray(scaling, dtype=np.float64)[a.invp]))
         st = ThreadStats()
         self.num = L.spral_ssids_gpu_create_num_subtree_dbl(
-            self.posdef, self.sym, _P(self.val), None, None, ctypes.byref(self._copts),
-            ctypes.byref(st))
+            self.posdef, self.sym, _P(self.val),
+            None if self.scaling is None else _P(self.scaling), None,
+            ctypes.byref(self._copts), ctypes.byref(st))
         self.stats = {k: getattr(st, k) for k, _ in ThreadStats._fields_}
         self.inform = self._inform(st)
         if not self.num:
@@ -189,10 +197,14 @@ class Fkeep:
         return inf
 
     def refactor(self, val, scaling=None):
-        """Same-pattern refactorisation from host values."""
+        """Same-pattern refactorisation from host values (scaling in user
+        variable order; default: the scaling given at construction)."""
         st = ThreadStats()
         self.val = np.ascontiguousarray(val, dtype=np.float64)
-        sc = None if scaling is None else np.ascontiguousarray(scaling, dtype=np.float64)
+        if scaling is not None:
+            self.scaling = np.ascontiguousarray(
+                np.asarray(scaling, dtype=np.float64)[self.akeep.invp])
+        sc = self.scaling
         fl = _native.lib().spral_ssids_gpu_refactor(self.num, _P(self.val),
                                                     None if sc is None else _P(sc),
                                                     ctypes.byref(st))
@@ -236,6 +248,9 @@ class Fkeep:
         B = b[:, None] if one else b
         invp = self.akeep.invp
         xp = np.asfortranarray(B[invp, :])
+        sc = self.scaling
+        if sc is not None and job in (0, 1):  # x2 = S b (fkeep.F90:253-260)
+            xp *= sc[:, None]
         nrhs, ldx = xp.shape[1], xp.shape[0]
         fns = {1: ["fwd"], 2: ["diag"], 3: ["bwd"], 4: ["diag_bwd"], 0: ["fwd", "diag_bwd"]}
         for nm in fns[job]:
@@ -243,12 +258,18 @@ class Fkeep:
                                                                        _P(xp), ldx)
             if fl != 0:
                 raise RuntimeError(f"spral_gb300 solve failed, flag {fl}")
+        if sc is not None and job in (0, 3, 4):  # x = S x2 (fkeep.F90:300-308)
+            xp *= sc[:, None]
         x = np.empty_like(B)
         x[invp, :] = xp
         return x[:, 0] if one else x
 
     def solve_refined(self, b):
-        """Full solve followed by FP64 iterative refinement on the device."""
+        """Full solve followed by FP64 iterative refinement on the device
+        (against the unscaled matrix: not available with a scaling)."""
+        if self.scaling is not None:
+            raise ValueError("solve_refined refines against the unscaled matrix; "
+                             "use solve() with a scaled factorisation")
         L = _native.lib()
         b = np.asarray(b, dtype=np.float64)
         one = b.ndim == 1
