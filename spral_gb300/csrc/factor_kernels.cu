@@ -124,7 +124,6 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long k)
 // 17 warps: thread t < 528 owns the pair {R, C}, R >= C, t = R(R+1)/2 + C
 constexpr int kDiagPairs = kBlk * (kBlk + 1) / 2;
 constexpr int kDiagThreads = (kDiagPairs + 31) / 32 * 32;
-constexpr int kDiagWarps = kDiagThreads / 32;
 
 // POSDEF: the Cholesky case (cpu/kernels/cholesky.cxx, LAPACK potrf): no
 // pivoting, pivot q is the block's q-th diagonal, and a pivot that is not
@@ -401,9 +400,14 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
   }
   for (int i = threadIdx.x; i < 2 * kBlk + 2; i += blockDim.x)
     dd[i] = (i < 2 * bs) ? fd.step[kBlk * kBlk + i] : 0.0;
+  __shared__ float ddf[kBlk];  // FP32 copies of the 1x1 D^{-1} entries
+  for (int i = threadIdx.x; i < kBlk; i += blockDim.x)
+    ddf[i] = (i < bs) ? (float)fd.step[kBlk * kBlk + 2 * i] : 0.f;
   if (threadIdx.x < kBlk) lp[threadIdx.x] = (threadIdx.x < bs) ? fd.lperm[threadIdx.x] : 0;
   __syncthreads();
   const double thresh = 1.0 / u;
+  // FP32 guard band of the threshold test (FP32 factors)
+  const float thr_lo = (float)(thresh * (1.0 - 1e-6)), thr_hi = (float)(thresh * (1.0 + 1e-6));
   // |l| > 1/u tested on bit patterns (non-negative doubles order as integers)
   const long long tkey = __double_as_longlong(thresh);
   auto over = [tkey](double l) {  // Inf fails the test, NaN does not (as fabs(l) > 1/u)
@@ -446,6 +450,18 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
               W[(int64_t)(j + 1) * fd.ld] = (T)x2;
               int cand = over(l1) ? j : (over(l2) ? j + 1 : bs);
               myfail = min(myfail, cand);
+            } else if (sizeof(T) == 4 && dj != 0.0) {
+              // FP32 factors: L in FP32; the a-posteriori test |l| <= 1/u is
+              // decided in FP32 outside a relative guard band of 1e-6 around
+              // the threshold and in FP64 inside it, so every decision is
+              // the FP64 one
+              const float lf = (float)x[j] * ddf[j];
+              fd.L[(int64_t)(p + j) * fd.ld + r] = (T)lf;
+              W[(int64_t)j * fd.ld] = x[j];
+              const float al = fabsf(lf);
+              if (!(al <= thr_lo)) {  // above the band, in it, or NaN
+                if (al > thr_hi || over((double)x[j] * dj)) myfail = min(myfail, j);
+              }
             } else {
               double l, w;
               if (dj == 0.0) {
