@@ -239,6 +239,13 @@ int spral_ssids_gpu_tc_gemm_f32(int M, int N, int K, const float* A, int lda, co
  * src/ssids/cpu/NumericSubtree.hxx:249-280).  Returns 0 or -51. */
 int spral_ssids_gpu_node_inertia(const void* numeric, int* out);
 
+/* Contribution-block size (rows) from which the FP32-factor path forms the
+ * update on the tensor cores instead of the SIMT kernel: measured once per
+ * device by timing both on synthetic fronts (the environment variable
+ * SPRAL_GB300_TC_MIN_CM overrides it).  No reference counterpart.  Returns
+ * the size, or -51 on a CUDA error. */
+int spral_ssids_gpu_tc_crossover(void);
+
 /* Free and total memory of the current device (cudaMemGetInfo), for
  * callers that admit work by device memory.  No reference counterpart.
  * Returns 0 or -51. */

@@ -427,6 +427,106 @@ void launch_bwd_err(const int64_t* aptr, const int64_t* asrc, const double* aval
                     const double* x, const double* r, const double* b, int nrhs, int ld,
                     double* work, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// Crossover of the FP32 contribution update between the SIMT kernel and the
+// tensor cores, measured once per device: the kernels of both are timed
+// (CUDA events, best of three; the tensor path's host-side job tables are
+// built beforehand, as they are when the factorisation is replayed from its
+// graph) on synthetic fronts with contribution blocks of cm rows and cm/2
+// eliminated columns; the threshold is the smallest cm from which the tensor
+// cores are faster for every larger size of the grid.
+// ---------------------------------------------------------------------------
+static std::mutex g_tune_mutex;
+static int g_tuned_min_cm[64];  // 0: not measured yet
+
+static int autotune_tc_min_cm() {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  if (dev >= 0 && dev < 64 && g_tuned_min_cm[dev] > 0) return g_tuned_min_cm[dev];
+  const int grid[] = {64, 96, 128, 192, 256, 384, 512};
+  constexpr int ng = sizeof(grid) / sizeof(grid[0]);
+  const int maxcm = grid[ng - 1], k = maxcm / 2;  // storage for the deepest case
+  cudaStream_t s;
+  CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  DevBuf<float> L, LD, C;
+  DevBuf<char> scratch;
+  DevBuf<int> fr;
+  FrontDesc<float>* d_fd = nullptr;
+  FrontState* d_st = nullptr;
+  int* d_status = nullptr;
+  const int ld = ((maxcm + k) + 3) / 4 * 4;
+  L.ensure((size_t)ld * k);
+  LD.ensure((size_t)maxcm * k);
+  C.ensure((size_t)maxcm * maxcm);
+  fr.ensure(1);
+  CK(cudaMalloc(&d_fd, sizeof(FrontDesc<float>)));
+  CK(cudaMalloc(&d_st, sizeof(FrontState)));
+  CK(cudaMalloc(&d_status, sizeof(int)));
+  CK(cudaMemsetAsync(L.p, 0, L.cap * sizeof(float), s));
+  CK(cudaMemsetAsync(LD.p, 0, LD.cap * sizeof(float), s));
+  CK(cudaMemsetAsync(C.p, 0, C.cap * sizeof(float), s));
+  CK(cudaMemsetAsync(fr.p, 0, sizeof(int), s));
+  CK(cudaMemsetAsync(d_status, 0, sizeof(int), s));
+
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  auto best = [&](auto&& run) {
+    float b = 1e30f;
+    for (int r = 0; r < 4; ++r) {  // first run warms up
+      CK(cudaEventRecord(e0, s));
+      run();
+      CK(cudaEventRecord(e1, s));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (r > 0) b = std::min(b, ms);
+    }
+    return b;
+  };
+  bool tc_wins[ng];
+  void* blob = nullptr;
+  for (int g = 0; g < ng; ++g) {
+    const int cm = grid[g], kk = std::max(32, cm / 2);
+    FrontDesc<float> h{};
+    h.L = L.p; h.LD = LD.p; h.C = C.p;
+    h.m = cm + kk; h.n = kk; h.ld = ld; h.cm = cm; h.ldc = cm;
+    h.nrow = cm + kk; h.ncol = kk;
+    FrontState hs{};
+    hs.nelim = kk;
+    CK(cudaMemcpyAsync(d_fd, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_st, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+    const float t_simt = best([&] { launch_contrib_gemm<float>(d_fd, d_st, fr.p, 1, cm, s); });
+    std::vector<TcProblem> ps(1);
+    ps[0] = {L.p + kk, ld, LD.p, cm, C.p, cm, cm, cm, kk, &d_st->nelim, 1};
+    scratch.ensure(tc_gemm_scratch_bytes(ps));
+    TcPlan plan;
+    if (tc_gemm_prepare(ps, scratch.p, plan) != 0) throw CudaFail{cudaErrorUnknown, __LINE__};
+    cudaFree(blob);
+    blob = nullptr;
+    CK(cudaMalloc(&blob, plan.blob.size()));
+    CK(cudaMemcpy(blob, plan.blob.data(), plan.blob.size(), cudaMemcpyHostToDevice));
+    const float t_tc = best([&] {
+      if (tc_gemm_launch(plan, blob, d_status, s, kTcChunk) != 0)
+        throw CudaFail{cudaErrorUnknown, __LINE__};
+    });
+    tc_wins[g] = t_tc < t_simt;
+  }
+  cudaFree(blob);
+  int pick = grid[ng - 1] + 1;
+  for (int g = ng - 1; g >= 0 && tc_wins[g]; --g) pick = grid[g];
+  CK(cudaStreamSynchronize(s));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d_fd);
+  cudaFree(d_st);
+  cudaFree(d_status);
+  cudaStreamDestroy(s);
+  if (dev >= 0 && dev < 64) g_tuned_min_cm[dev] = pick;
+  return pick;
+}
+
 template <typename T>
 struct Numeric : NumericBase {
   Symbolic* S;
@@ -808,6 +908,7 @@ struct Numeric : NumericBase {
       if (ch) tc_chunk = std::max(0, atoi(ch));
       const char* mc = getenv("SPRAL_GB300_TC_MIN_CM");
       if (mc) tc_min_cm = std::max(1, atoi(mc));
+      else if (use_tc) tc_min_cm = autotune_tc_min_cm();
     }
     contrib.ensure(std::max<int64_t>(S->contrib_total, 1));
     // factor storage estimate (no delays) + 10%
@@ -1580,6 +1681,16 @@ void spral_ssids_gpu_phase_times(const void* numeric, double* ms, long long* cou
   for (int i = 0; i < ssids300::kPhCount; ++i) {
     ms[i] = N->ptimer.ms[i];
     counts[i] = N->ptimer.cnt[i];
+  }
+}
+
+/* Smallest contribution block (rows) formed on the tensor cores by the
+ * FP32-factor path on the current device, as measured by the autotuner. */
+int spral_ssids_gpu_tc_crossover(void) {
+  try {
+    return ssids300::autotune_tc_min_cm();
+  } catch (...) {
+    return -51;
   }
 }
 

@@ -46,3 +46,12 @@ def test_tc_gemm_chunked_accuracy_matches_fp32():
     _, got, ref = _run(384, 384, 1152, 0, -1, 7)
     rms = np.sqrt(np.mean((got - ref) ** 2)) / np.sqrt(1152)
     assert rms <= 1.5e-6
+
+
+def test_tc_crossover_is_measured_once_per_device():
+    from spral_gb300 import _native
+    L = _native.lib()
+    a = L.spral_ssids_gpu_tc_crossover()
+    b = L.spral_ssids_gpu_tc_crossover()
+    assert a == b  # cached per device
+    assert 64 <= a <= 513  # a size of the grid, or "never" (one past the largest)
