@@ -192,6 +192,52 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def hbm_peak_gbs():
+    try:
+        pk = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+        return pk["hbm_gbs"], "measured copy bandwidth (MEASURED_PEAKS.json)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def hbm_rooflines(ak, L, fk, ph_ms, b_d, x_d, n, nrhs):
+    """HBM rooflines of the solve and of the assembly (FP64 path), with the
+    algorithmic byte counts: solve = 2 sum_nodes m*nelim*8 (L read in the
+    forward and the backward pass) + sum_nodes 2*nelim*8 (D) + 2 sum_nodes
+    m*nrhs*8*2 (local vectors gathered and scattered); assembly = sum over
+    children cm(cm+1)/2 * (8 read + 16 parent read-modify-write) + 4 cm
+    (row map) plus loading A: nnz * (8 value + 16 index pair + 8 front)."""
+    import torch
+    peak, src = hbm_peak_gbs()
+    nrow, ncol = ak.front_sizes()
+    solve_bytes = float(2 * (nrow * ncol).sum() * 8 + (2 * ncol * 8).sum()
+                        + 2 * (nrow * nrhs * 8 * 2).sum())
+    times = []
+    for _ in range(5):
+        x_d.copy_(b_d)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fk.solve_dev(x_d.data_ptr(), nrhs, n)  # returns after its stream is idle
+        times.append(time.perf_counter() - t0)
+    t_solve = float(np.median(times))
+    cm = nrow - ncol
+    parent = ak.sparent[:ak.nnodes] - 1
+    has_parent = parent < ak.nnodes
+    asm_bytes = float((cm[has_parent] * (cm[has_parent] + 1) / 2 * 24 + 4 * cm[has_parent]).sum()
+                      + ak.nnz * 32)
+    t_asm = (ph_ms[1] + ph_ms[4]) * 1e-3  # load A + extend-add phases
+    return {"peak": peak, "unit": "GB/s", "peak_source": src,
+            "solve": {"bytes": solve_bytes, "ms": t_solve * 1e3,
+                      "achieved": solve_bytes / t_solve / 1e9,
+                      "frac": solve_bytes / t_solve / 1e9 / peak,
+                      "note": f"one {nrhs}-RHS forward+backward solve, FP64 factors"},
+            "assembly": {"bytes": asm_bytes, "ms": t_asm * 1e3,
+                         "achieved": asm_bytes / t_asm / 1e9 if t_asm > 0 else None,
+                         "frac": asm_bytes / t_asm / 1e9 / peak if t_asm > 0 else None,
+                         "note": "load A + extend-add phases of one factorisation "
+                                 "(phase timer, CUDA events)"}}
+
+
 def tf32_peak_tflops():
     """TF32 tensor peak: the measured dense bf16 burst rate halved (tcgen05
     issues kind::tf32 at half the kind::f16 rate); fallback 1.9 PF/s bf16."""
@@ -312,7 +358,12 @@ def run_gpu(args):
     fk.refactor_dev(aval_d.data_ptr())
     ps = np.zeros(6)
     L.spral_ssids_gpu_profile_stats(fk.num, ps.ctypes.data_as(ctypes.c_void_p))
+    ph_ms = np.zeros(32)
+    ph_cnt = np.zeros(32, dtype=np.int64)
+    L.spral_ssids_gpu_phase_times(fk.num, ph_ms.ctypes.data_as(ctypes.c_void_p),
+                                  ph_cnt.ctypes.data_as(ctypes.c_void_p))
     L.spral_ssids_gpu_set_profiling(fk.num, 0)
+    bandwidth = hbm_rooflines(ak, L, fk, ph_ms, b_d, x_d, n, nrhs)
     fp64_peak = L.spral_ssids_gpu_fp64_peak_tflops(local)
     achieved = ps[1] / (ps[0] * 1e-3) / 1e12 if ps[0] > 0 else 0.0
     traffic = None
@@ -398,6 +449,7 @@ def run_gpu(args):
                 "factor_tflops": factor_tflops,
                 "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99)),
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
+                "bandwidth": bandwidth,
                 "cpu_baseline": cpu, "clocks": clocks, "mixed_precision": mixed}
         print(json.dumps(line), flush=True)
     if dist is not None:
