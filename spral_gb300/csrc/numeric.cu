@@ -1149,6 +1149,7 @@ struct Numeric : NumericBase {
 
   void prepare_solve() {
     if (solve_ready) return;
+    solve_init<T>();
     const int nn = S->nnodes;
     std::vector<SolveNode<T>> sn(nn);
     std::vector<int> ch;

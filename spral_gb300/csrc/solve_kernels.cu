@@ -21,6 +21,7 @@
 // updating it: one launch per block step instead of two.  Arithmetic is in
 // the factor precision T; the number of right-hand sides per pass NR is a
 // template parameter so that no work is spent on absent columns.
+#include <mutex>
 #include <type_traits>
 
 #include "ssids_gpu.cuh"
@@ -107,77 +108,102 @@ __device__ __forceinline__ void fwd_gather_node(const SolveNode<T>& sn, const So
 }
 
 // stage the jb x jb diagonal block (strictly lower part) into shared memory;
-// every thread issues all of its loads before the first store so that the
-// global-memory latency is paid once, not once per element
+// every thread issues a batch of loads before the stores, so the
+// global-memory latency is paid once per batch, not once per element
 constexpr int kSolveThreads = 256;
 constexpr int kSolveWarps = kSolveThreads / 32;
+constexpr int LDB = SB + 1;  // leading dimension of a staged block Lb[c * LDB + r]
 template <typename T>
-__device__ __forceinline__ void load_diag_block(const SolveNode<T>& sn, int j0, int jb,
-                                                T (*Lb)[SB + 1]) {
-  constexpr int PER = SB * SB / kSolveThreads;  // 16
-  T v[PER];
+__device__ __forceinline__ void load_diag_block(const SolveNode<T>& sn, int j0, int jb, T* Lb) {
+  constexpr int PER = SB * SB / kSolveThreads;
+  constexpr int BATCH = PER < 32 ? PER : 32;
 #pragma unroll
-  for (int k = 0; k < PER; ++k) {
-    const int e = threadIdx.x + k * kSolveThreads;
-    const int c = e / SB, r = e % SB;
-    v[k] = (r > c && r < jb && c < jb) ? sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : T(0);
-  }
+  for (int b0 = 0; b0 < PER; b0 += BATCH) {
+    T v[BATCH];
 #pragma unroll
-  for (int k = 0; k < PER; ++k) {
-    const int e = threadIdx.x + k * kSolveThreads;
-    Lb[e / SB][e % SB] = v[k];
+    for (int k = 0; k < BATCH; ++k) {
+      const int e = threadIdx.x + (b0 + k) * kSolveThreads;
+      const int c = e / SB, r = e % SB;
+      v[k] = (r > c && r < jb && c < jb) ? sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : T(0);
+    }
+#pragma unroll
+    for (int k = 0; k < BATCH; ++k) {
+      const int e = threadIdx.x + (b0 + k) * kSolveThreads;
+      Lb[(e / SB) * LDB + e % SB] = v[k];
+    }
   }
 }
 
 // Unit lower (FWD) or unit upper L^T (!FWD) triangular solve of rows
-// [j0, j0+jb) of xloc in place, with the block staged in Lb (Lb[c][r] =
+// [j0, j0+jb) of xloc in place, with the block staged in Lb (Lb[c*LDB + r] =
 // L(j0+r, j0+c), zero on and above the diagonal).  Warp w solves the
-// right-hand sides w, w + 8, ...; lane l holds rows l and l + 32.  The
+// right-hand sides w, w + 8, ...; lane l holds rows l, l + 32, ...  The
 // caller has synchronised the CTA after staging Lb; nothing follows.
 template <typename T, int NR, bool FWD>
 __device__ __forceinline__ void diag_block_solve(const SolveNode<T>& sn, int j0, int jb,
-                                                 int nrhs, T (*Lb)[SB + 1]) {
+                                                 int nrhs, const T* Lb) {
   constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
+  constexpr int G = SB / 32;  // rows per lane
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp >= nrhs) return;
-  T x0[R], x1[R];
+  T x[R][G];
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int q = warp + r * kSolveWarps;
-    x0[r] = (q < nrhs && lane < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane] : T(0);
-    x1[r] = (q < nrhs && lane + 32 < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] : T(0);
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+      x[r][g] = (q < nrhs && lane + 32 * g < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane + 32 * g]
+                                                 : T(0);
   }
   if (FWD) {
     for (int k = 0; k < jb - 1; ++k) {
-      const T l0 = Lb[k][lane], l1 = Lb[k][lane + 32];
+      T l[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) l[g] = Lb[k * LDB + lane + 32 * g];
+      const int kg = k >> 5;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const T xk = (k < 32) ? __shfl_sync(0xffffffffu, x0[r], k & 31)
-                              : __shfl_sync(0xffffffffu, x1[r], k & 31);
-        x0[r] -= l0 * xk;
-        x1[r] -= l1 * xk;
+        T src = x[r][0];
+#pragma unroll
+        for (int g = 1; g < G; ++g) src = (kg == g) ? x[r][g] : src;
+        const T xk = __shfl_sync(0xffffffffu, src, k & 31);
+#pragma unroll
+        for (int g = 0; g < G; ++g) x[r][g] -= l[g] * xk;
       }
     }
   } else {
     // (L^T y)_r = y_r + sum_{c > r} L(c, r) y_c ; process c from the bottom.
-    // L(c, r) = Lb[r][c] is zero unless c > r, so no lane masks are needed.
+    // L(c, r) = Lb[r*LDB + c] is zero unless c > r, so no lane masks are needed.
     for (int c = jb - 1; c > 0; --c) {
-      const T l0 = Lb[lane][c], l1 = Lb[lane + 32][c];
+      T l[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) l[g] = Lb[(lane + 32 * g) * LDB + c];
+      const int cg = c >> 5;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const T yc = (c < 32) ? __shfl_sync(0xffffffffu, x0[r], c & 31)
-                              : __shfl_sync(0xffffffffu, x1[r], c & 31);
-        x0[r] -= l0 * yc;
-        x1[r] -= l1 * yc;
+        T src = x[r][0];
+#pragma unroll
+        for (int g = 1; g < G; ++g) src = (cg == g) ? x[r][g] : src;
+        const T yc = __shfl_sync(0xffffffffu, src, c & 31);
+#pragma unroll
+        for (int g = 0; g < G; ++g) x[r][g] -= l[g] * yc;
       }
     }
   }
 #pragma unroll
   for (int r = 0; r < R; ++r) {
     const int q = warp + r * kSolveWarps;
-    if (q < nrhs && lane < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane] = x0[r];
-    if (q < nrhs && lane + 32 < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane + 32] = x1[r];
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+      if (q < nrhs && lane + 32 * g < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane + 32 * g] = x[r][g];
   }
+}
+
+// dynamic shared memory of the solve kernels: the staged block, then the
+// block's solved values yb[r * NR + q]
+template <typename T, int NR>
+constexpr size_t solve_smem_bytes() {
+  return sizeof(T) * ((size_t)SB * LDB + (size_t)SB * NR);
 }
 
 // ---- forward ----
@@ -189,7 +215,8 @@ __global__ void __launch_bounds__(kSolveThreads)
   const SolveNode<T> sn = sns[nodes[blockIdx.x]];
   fwd_gather_node(sn, sns, children, x, ldx, nrhs);
   if (sn.nelim == 0) return;
-  __shared__ T Lb[SB][SB + 1];
+  extern __shared__ __align__(16) unsigned char solve_smem[];
+  T* Lb = reinterpret_cast<T*>(solve_smem);
   __syncthreads();  // xloc rows written by the gather
   const int jb = min(SB, sn.nelim);
   load_diag_block(sn, 0, jb, Lb);
@@ -199,15 +226,15 @@ __global__ void __launch_bounds__(kSolveThreads)
 
 // Update kernels of the block steps: a CTA pass covers 64 rows (forward) or
 // columns (backward); thread (t, qq) = (threadIdx.x % 64, threadIdx.x / 64)
-// forms the partial dot products of entry t over the 16 block columns
-// [16 qq, 16 qq + 16) for every right-hand side, with its 16 loads issued
+// forms the partial dot products of entry t over the block columns
+// [qq SB/4, (qq+1) SB/4) for every right-hand side, with those loads issued
 // together, and the four partial sums are added through shared memory.
 constexpr int kPassRows = 64;
 constexpr int kQuarter = SB / 4;
 
 template <typename T, int NR>
 __device__ __forceinline__ void partial_dots(const T* p, int64_t stride, int cq, int jb,
-                                             const T (*yb)[NR], T (&acc)[NR]) {
+                                             const T* yb, T (&acc)[NR]) {
   T lv[kQuarter];
 #pragma unroll
   for (int k = 0; k < kQuarter; ++k) lv[k] = (cq + k < jb) ? p[(int64_t)k * stride] : T(0);
@@ -216,7 +243,7 @@ __device__ __forceinline__ void partial_dots(const T* p, int64_t stride, int cq,
 #pragma unroll
   for (int k = 0; k < kQuarter; ++k)
 #pragma unroll
-    for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[cq + k][q];
+    for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(cq + k) * NR + q];
 }
 
 // red[(qq * NR + q) * 64 + t] holds the partial sums; entry t of the pass
@@ -235,10 +262,19 @@ __device__ __forceinline__ void apply_partials(const SolveNode<T>& sn, const T* 
   }
 }
 
+// the solved rows [j0, j0+jb) of every right-hand side into yb[r*NR + q]
+template <typename T, int NR>
+__device__ __forceinline__ void load_y(const SolveNode<T>& sn, int j0, int jb, int nrhs, T* yb) {
+  for (int e = threadIdx.x; e < SB * NR; e += blockDim.x) {
+    const int r = e % SB, q = e / SB;
+    yb[r * NR + q] = (r < jb && q < nrhs) ? sn.xloc[(int64_t)q * sn.m + j0 + r] : T(0);
+  }
+}
+
 // Block step st: rows i >= i0 = j0 + jb get x_i -= sum_c L(i, j0+c) y_c with
-// y = the solved rows [j0, j0+jb).  CTA 0's first pass covers rows
-// [i0, i0 + 64), which hold the whole next diagonal block; it then solves
-// that block.
+// y = the solved rows [j0, j0+jb).  CTA 0 updates the next block's rows
+// [i0, i0 + SB) and then solves that block; CTAs 1.. update the rows after
+// it (CTA 0 as well when it is alone).
 template <typename T, int NR>
 __global__ void __launch_bounds__(kSolveThreads)
     k_fwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
@@ -248,16 +284,15 @@ __global__ void __launch_bounds__(kSolveThreads)
   const int jb = min(SB, sn.nelim - j0);
   const int i0 = j0 + jb;
   if (i0 >= sn.m) return;
-  __shared__ T yb[SB][NR];
-  __shared__ T Lb[SB][SB + 1];  // also the partial-sum buffer (4 * NR * 64 entries fit)
-  T* red = &Lb[0][0];
-  for (int e = threadIdx.x; e < SB * NR; e += blockDim.x) {
-    const int r = e % SB, q = e / SB;
-    yb[r][q] = (r < jb && q < nrhs) ? sn.xloc[(int64_t)q * sn.m + j0 + r] : T(0);
-  }
+  extern __shared__ __align__(16) unsigned char solve_smem[];
+  T* Lb = reinterpret_cast<T*>(solve_smem);  // also the partial-sum buffer
+  T* yb = Lb + SB * LDB;
+  T* red = Lb;
+  load_y<T, NR>(sn, j0, jb, nrhs, yb);
   __syncthreads();
   const int t = threadIdx.x % kPassRows, qq = threadIdx.x / kPassRows;
-  for (int base = i0 + blockIdx.x * kPassRows; base < sn.m; base += gridDim.x * kPassRows) {
+  const int ih = min(sn.m, i0 + SB);  // end of the next block's rows
+  auto pass = [&](int base) {
     const int i = base + t;
     T acc[NR];
     if (i < sn.m) {
@@ -272,6 +307,16 @@ __global__ void __launch_bounds__(kSolveThreads)
     __syncthreads();
     apply_partials<T, NR>(sn, red, base, sn.m, nrhs);
     __syncthreads();
+  };
+  if (blockIdx.x == 0) {
+    for (int base = i0; base < ih; base += kPassRows) pass(base);
+  }
+  if (gridDim.x == 1) {
+    for (int base = ih; base < sn.m; base += kPassRows) pass(base);
+  } else if (blockIdx.x > 0) {
+    for (int base = ih + (blockIdx.x - 1) * kPassRows; base < sn.m;
+         base += (gridDim.x - 1) * kPassRows)
+      pass(base);
   }
   if (blockIdx.x != 0 || i0 >= sn.nelim) return;
   const int jb1 = min(SB, sn.nelim - i0);
@@ -280,9 +325,6 @@ __global__ void __launch_bounds__(kSolveThreads)
   diag_block_solve<T, NR, true>(sn, i0, jb1, nrhs, Lb);
 }
 
-// scale_sqrt: the posdef forward solve with L_chol = L D^(1/2) returns
-// D^(-1/2) L^{-1} b, i.e. each pivot's value times sqrt(D^{-1}) (1x1 pivots
-// only in the posdef case)
 template <typename T>
 __global__ void k_fwd_scatter(const SolveNode<T>* sns, const int* nodes, double* x, int ldx,
                               int nrhs, bool scale_sqrt) {
@@ -370,7 +412,8 @@ __global__ void __launch_bounds__(kSolveThreads)
   const SolveNode<T> sn = sns[nodes[blockIdx.x]];
   if (sn.nelim == 0) return;
   const int jl = ((sn.nelim - 1) / SB) * SB;
-  __shared__ T Lb[SB][SB + 1];
+  extern __shared__ __align__(16) unsigned char solve_smem[];
+  T* Lb = reinterpret_cast<T*>(solve_smem);
   load_diag_block(sn, jl, sn.nelim - jl, Lb);
   __syncthreads();
   diag_block_solve<T, NR, false>(sn, jl, sn.nelim - jl, nrhs, Lb);
@@ -378,8 +421,8 @@ __global__ void __launch_bounds__(kSolveThreads)
 
 // Block step st (> 0) of the backward solve: the columns j left of block st
 // take x_j -= sum_c L(j0+c, j) y_c with y = its solved rows.  CTA 0 updates
-// the 64 columns of block st-1 and then solves that block; CTAs 1.. update
-// the columns before it, 64 per pass.
+// the columns of block st-1 and then solves that block; CTAs 1.. update the
+// columns before it (CTA 0 as well when it is alone), 64 per pass.
 template <typename T, int NR>
 __global__ void __launch_bounds__(kSolveThreads)
     k_bwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
@@ -387,23 +430,15 @@ __global__ void __launch_bounds__(kSolveThreads)
   const int j0 = step * SB;
   if (j0 >= sn.nelim || j0 == 0) return;
   const int jb = min(SB, sn.nelim - j0);
-  __shared__ T yb[SB][NR];
-  __shared__ T Lb[SB][SB + 1];  // also the partial-sum buffer
-  T* red = &Lb[0][0];
-  for (int e = threadIdx.x; e < SB * NR; e += blockDim.x) {
-    const int r = e % SB, q = e / SB;
-    yb[r][q] = (r < jb && q < nrhs) ? sn.xloc[(int64_t)q * sn.m + j0 + r] : T(0);
-  }
+  extern __shared__ __align__(16) unsigned char solve_smem[];
+  T* Lb = reinterpret_cast<T*>(solve_smem);  // also the partial-sum buffer
+  T* yb = Lb + SB * LDB;
+  T* red = Lb;
+  load_y<T, NR>(sn, j0, jb, nrhs, yb);
   __syncthreads();
   const int t = threadIdx.x % kPassRows, qq = threadIdx.x / kPassRows;
   const int jp = j0 - SB;  // first column of block st-1 (a full block)
-  int first, lim, stride;
-  if (blockIdx.x == 0) {
-    first = jp; lim = j0; stride = kPassRows;
-  } else {
-    first = (blockIdx.x - 1) * kPassRows; lim = jp; stride = (gridDim.x - 1) * kPassRows;
-  }
-  for (int base = first; base < lim; base += stride) {
+  auto pass = [&](int base, int lim) {
     const int j = base + t;
     T acc[NR];
     if (j < lim) {
@@ -418,6 +453,15 @@ __global__ void __launch_bounds__(kSolveThreads)
     __syncthreads();
     apply_partials<T, NR>(sn, red, base, lim, nrhs);
     __syncthreads();
+  };
+  if (blockIdx.x == 0) {
+    for (int base = jp; base < j0; base += kPassRows) pass(base, j0);
+  }
+  if (gridDim.x == 1) {
+    for (int base = 0; base < jp; base += kPassRows) pass(base, jp);
+  } else if (blockIdx.x > 0) {
+    for (int base = (blockIdx.x - 1) * kPassRows; base < jp; base += (gridDim.x - 1) * kPassRows)
+      pass(base, jp);
   }
   if (blockIdx.x != 0) return;
   load_diag_block(sn, jp, SB, Lb);
@@ -447,7 +491,8 @@ void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const i
   if (nn <= 0) return;
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
-    k_fwd_gather_diag<T, NR><<<nn, kSolveThreads, 0, s>>>(sn, nodes, children, x, ldx, nrhs);
+    k_fwd_gather_diag<T, NR><<<nn, kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
+        sn, nodes, children, x, ldx, nrhs);
     note_launches(1);
   });
 }
@@ -464,9 +509,12 @@ void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_
     for (int st = 0; st < steps; ++st) {
       const int rows = max_m - st * SB;  // upper bound; the kernel derives the exact range
       if (rows <= 0) break;
-      const int gx = std::max(1, std::min(cdiv(rows, kPassRows), 152));
+      // CTA 0 takes the next block's rows, the others the rows after it
+      const int tail = rows - SB - 1;
+      const int gx = tail > 0 ? 1 + std::min(cdiv(tail, kPassRows), 151) : 1;
       pmark(tm, kPhFwdUpdate, s);
-      k_fwd_step<T, NR><<<dim3(gx, nn), kSolveThreads, 0, s>>>(sn, nodes, st, nrhs);
+      k_fwd_step<T, NR><<<dim3(gx, nn), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
+          sn, nodes, st, nrhs);
       note_launches(1);
     }
   });
@@ -496,14 +544,17 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
       k_bwd_l21<T, NR><<<dim3(gw, nn), kSolveThreads, 0, s>>>(sn, nodes, nrhs);
       note_launches(1);
       pmark(tm, kPhBwdDiag, s);
-      k_bwd_diag_last<T, NR><<<nn, kSolveThreads, 0, s>>>(sn, nodes, nrhs);
+      k_bwd_diag_last<T, NR><<<nn, kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(sn, nodes,
+                                                                                   nrhs);
       note_launches(1);
       const int steps = cdiv(max_nelim, SB);
       for (int st = steps - 1; st >= 1; --st) {
-        // CTA 0 takes block st-1; at least one more CTA for the columns before it
-        const int gu = std::max(1, std::min(cdiv((st - 1) * SB, kPassRows), 151));
+        // CTA 0 takes block st-1, the others the columns before it
+        const int jp = (st - 1) * SB;
+        const int gu = jp > 0 ? std::min(cdiv(jp, kPassRows), 151) : 0;
         pmark(tm, kPhBwdUpdate, s);
-        k_bwd_step<T, NR><<<dim3(1 + gu, nn), kSolveThreads, 0, s>>>(sn, nodes, st, nrhs);
+        k_bwd_step<T, NR><<<dim3(1 + gu, nn), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
+            sn, nodes, st, nrhs);
         note_launches(1);
       }
     });
@@ -513,7 +564,29 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
   { k_fwd_scatter<T><<<dim3(gs, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, false); note_launches(1); }
 }
 
+// the dynamic shared memory limit of every solve kernel instantiation; called
+// before solves are enqueued (never during a stream capture)
+template <typename T>
+void solve_init() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    auto set = [](auto kernel, size_t bytes) {
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    };
+    for (int q : {1, 2, 4, 8, 16}) {
+      with_nr(q, [&](auto nrc) {
+        constexpr int NR = decltype(nrc)::value;
+        set(k_fwd_gather_diag<T, NR>, solve_smem_bytes<T, NR>());
+        set(k_fwd_step<T, NR>, solve_smem_bytes<T, NR>());
+        set(k_bwd_diag_last<T, NR>, solve_smem_bytes<T, NR>());
+        set(k_bwd_step<T, NR>, solve_smem_bytes<T, NR>());
+      });
+    }
+  });
+}
+
 #define INST(T)                                                                                \
+  template void solve_init<T>();                                                               \
   template void launch_fwd_gather<T>(const SolveNode<T>*, const int*, int, const int*,         \
                                      const double*, int, int, cudaStream_t);                   \
   template void launch_fwd_steps<T>(const SolveNode<T>*, const int*, int, int, int, int,       \
