@@ -24,6 +24,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <type_traits>
 
 #include "ssids_gpu.cuh"
 
@@ -344,6 +345,278 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
   }
   int oldp = 0, oldo = 0;
   if (tid < bs) { oldp = fd.perm[p + map[tid]]; oldo = fd.opos[p + map[tid]]; }
+  __syncthreads();
+  if (tid < bs) { fd.perm[p + tid] = oldp; fd.opos[p + tid] = oldo; }
+}
+
+// ------------------------------------------------------------------------
+// k_app_diag_f32: the indefinite diagonal block for FP32 factors with one
+// barrier per pivot.  Pair ownership, keys and pivot semantics as
+// k_app_diag; the pivot loop is restructured so that no warp waits on a
+// serial decision phase:
+//   * every warp reduces the 17 warp maxima itself (two 32-bit redux.sync
+//     per reduction) and takes the same pivot decision;
+//   * the key of an entry also carries the physical row and column of its
+//     logical column and row, so the decision reads the pivot entries
+//     directly;
+//   * each thread keeps the logical indices of its pair in registers and
+//     applies the pivot's swaps to them;
+//   * the block, the logical -> physical map and the warp maxima are double
+//     buffered: pivot q reads buffer q&1 and writes the other, and the key
+//     of each updated entry is formed right after its update;
+//   * the 2x2 test and the L columns are FP32; D^{-1} is formed in FP64
+//     after the loop, for all pivots at once, from the recorded pivot
+//     entries (the same formulas as k_app_diag).
+// ------------------------------------------------------------------------
+constexpr int kDiagWarps = kDiagThreads / 32;
+
+// lexicographic maximum of 64-bit keys over the warp
+__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k) {
+  const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+  const unsigned mh = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? lo : 0u);
+  return ((unsigned long long)mh << 32) | ml;
+}
+
+// key of entry value v at logical (lo, hi), lo <= hi, physical (plo, phi):
+// magnitude, then the inverted column-major position, then the physical
+// indices (never decisive: positions are distinct)
+__device__ __forceinline__ unsigned long long diag_key_f32(float v, int lo, int hi, int plo,
+                                                            int phi) {
+  const unsigned mag = __float_as_uint(v) & 0x7fffffffu;
+  const unsigned low = ((unsigned)(1023 - (lo * 32 + hi)) << 10) | ((unsigned)plo << 5) |
+                       (unsigned)phi;
+  return (1ULL << 63) | ((unsigned long long)mag << 32) | low;
+}
+
+__global__ void __launch_bounds__(kDiagThreads)
+    k_app_diag_f32(FrontDesc<float>* fds, FrontState* sts, const int* fronts, int step,
+                   bool action, double small) {
+  const int f = fronts[blockIdx.x];
+  FrontState* st = &sts[f];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int R = (int)((sqrtf(8.0f * tid + 1.0f) - 1.0f) * 0.5f);
+  while ((R + 1) * (R + 2) / 2 <= tid) ++R;
+  while (R * (R + 1) / 2 > tid) --R;
+  const int C = tid - R * (R + 1) / 2;
+  const bool pair = tid < kDiagPairs;
+  __shared__ float blk[2][kBlk][kBlk + 1];   // blk[b][c][r] = A(r, c), physical, symmetric
+  __shared__ float outb[kBlk][kBlk + 1];     // outb[j][X] = L(inv[X], j)
+  __shared__ int map[2][kBlk];               // logical -> physical
+  __shared__ int inv[kBlk];                  // physical -> logical (after the loop)
+  __shared__ unsigned long long wkey[2][kDiagWarps];
+  __shared__ float pv[kBlk][3];              // pivot entries: a11 (1x1: d), a21, a22
+  __shared__ int psz[kBlk];                  // 1: 1x1, 2: first of a 2x2, 3: second, 0: zero
+  __shared__ double dd[2 * kBlk + 2];
+  __shared__ int s_state[2];
+  __shared__ FrontDesc<float> fd;
+
+  if (tid == 0) {
+    fd = fds[f];
+    int p, end;
+    if (step == 0) {
+      p = 0;
+      end = fd.n;
+    } else {
+      p = st->p;
+      end = st->end;
+      if (st->bs > 0) {
+        p += st->npass;
+        end -= st->bs - st->npass;
+      }
+    }
+    int bs = min(kBlk, end - p);
+    if (bs < 0) bs = 0;
+    st->p = p;
+    st->end = end;
+    st->bs = bs;
+    st->npass_raw = bs;
+    st->npass = bs;
+    st->step = step;
+    s_state[0] = p;
+    s_state[1] = bs;
+  }
+  __syncthreads();
+  const int p = s_state[0], bs = s_state[1];
+  if (bs == 0) return;
+  // FP32 threshold with (bv < fsmall) == ((double)bv < small) for every float bv
+  float fsmall = (float)small;
+  if ((double)fsmall < small) fsmall = nextafterf(fsmall, INFINITY);
+  const bool mine = pair && R < bs;  // (C <= R < bs)
+  float a = mine ? fd.L[(int64_t)(p + C) * fd.ld + p + R] : 0.f;  // the owned entry
+  if (pair) {
+    blk[0][C][R] = a;
+    blk[0][R][C] = a;
+  }
+  for (int e = tid; e < kBlk * (kBlk + 1); e += kDiagThreads) (&outb[0][0])[e] = 0.f;
+  if (tid < kBlk) {
+    map[0][tid] = tid;
+    psz[tid] = 0;
+  }
+  {
+    const unsigned long long k0 = warp_max_key(mine ? diag_key_f32(a, C, R, C, R) : 0ULL);
+    if (lane == 0) wkey[0][warp] = k0;
+  }
+  int li = R, lj = C;  // logical indices of physical R and C
+  int lx = lane;       // warp 0: logical index of physical row `lane`
+  int cur = 0;
+  bool singular = false;
+  for (int q = 0; q < bs;) {
+    __syncthreads();
+    const int nxt = cur ^ 1;
+    const unsigned long long gk = warp_max_key(lane < kDiagWarps ? wkey[cur][lane] : 0ULL);
+    const unsigned lo32 = (unsigned)gk;
+    const int pos = 1023 - (int)(lo32 >> 10);
+    const int bj = pos >> 5, bi = pos & 31;                   // logical column, row
+    const int pj = (int)((lo32 >> 5) & 31), pi = (int)(lo32 & 31);  // their physical
+    const float bv = __uint_as_float((unsigned)(gk >> 32) & 0x7fffffffu);
+    int pivsiz = 1, i1 = bi, i2 = -1;
+    float e11 = 0.f, e21 = 0.f, e22 = 0.f, a11 = 0.f, a21 = 0.f, a22 = 0.f;
+    if (bv < fsmall) {
+      pivsiz = 0;
+    } else if (bi != bj) {
+      a11 = blk[cur][pj][pj];
+      a22 = blk[cur][pi][pi];
+      a21 = blk[cur][pj][pi];
+      const float aa21 = fabsf(a21);
+      const float detscale = __frcp_rn(aa21);
+      const float detpiv = (a11 * detscale) * a22 - aa21;
+      if (fabsf(detpiv) >= aa21 * 0.5f) {
+        pivsiz = 2; i1 = bj; i2 = bi;
+        const float rdet = __frcp_rn(detpiv);
+        e11 = (a22 * detscale) * rdet;
+        e21 = (-a21 * detscale) * rdet;
+        e22 = (a11 * detscale) * rdet;
+      } else if (fabsf(a11) > fabsf(a22)) {
+        i1 = bj;
+      } else {
+        i1 = bi;
+      }
+    }
+    if (pivsiz == 0) {
+      // the remaining logical columns are zero pivots (psz 0): L columns and
+      // D^{-1} stay zero
+      if (!action) singular = true;
+      break;
+    }
+    const int* mp = map[cur];
+    const int pa = mp[q], pb = mp[i1];
+    const int cq1 = (pivsiz == 2) ? ((i1 == q + 1) ? pa : mp[q + 1]) : -1;
+    const int ci2 = (pivsiz == 2) ? mp[i2] : -1;
+    // swaps q <-> i1, then q+1 <-> i2, applied to logical indices
+    auto relabel = [&](int x) {
+      x = (x == q) ? i1 : (x == i1) ? q : x;
+      if (pivsiz == 2) x = (x == q + 1) ? i2 : (x == i2) ? q + 1 : x;
+      return x;
+    };
+    li = relabel(li);
+    lj = relabel(lj);
+    const int qn = q + pivsiz;
+    const int lo = min(li, lj), hi = max(li, lj);
+    if (pivsiz == 1) {
+      const int P = pb;
+      const float dT = __frcp_rn(blk[cur][P][P]);
+      if (mine && lo >= qn) a = a - blk[cur][P][R] * (blk[cur][P][C] * dT);
+      if (warp == 0) {
+        lx = relabel(lx);
+        if (lane < bs && lx > q) outb[q][lane] = blk[cur][P][lane] * dT;
+      }
+      if (tid == 0) {
+        psz[q] = 1;
+        pv[q][0] = blk[cur][P][P];
+      }
+    } else {
+      const int P1 = pb, P2 = ci2;
+      if (mine && lo >= qn) {
+        const float v1 = blk[cur][P1][C], v2 = blk[cur][P2][C];
+        a = a - (blk[cur][P1][R] * (e11 * v1 + e21 * v2) + blk[cur][P2][R] * (e21 * v1 + e22 * v2));
+      }
+      if (warp == 0) {
+        lx = relabel(lx);
+        if (lane < bs && lx > q + 1) {
+          const float v1 = blk[cur][P1][lane], v2 = blk[cur][P2][lane];
+          outb[q][lane] = e11 * v1 + e21 * v2;
+          outb[q + 1][lane] = e21 * v1 + e22 * v2;
+        }
+      }
+      if (tid == 0) {
+        psz[q] = 2;
+        psz[q + 1] = 3;
+        pv[q][0] = a11;
+        pv[q][1] = a21;
+        pv[q][2] = a22;
+      }
+    }
+    if (pair) {
+      blk[nxt][C][R] = a;
+      blk[nxt][R][C] = a;
+    }
+    const unsigned long long k =
+        (mine && lo >= qn)
+            ? diag_key_f32(a, lo, hi, li <= lj ? R : C, li <= lj ? C : R)
+            : 0ULL;
+    const unsigned long long wk = warp_max_key(k);
+    if (lane == 0) wkey[nxt][warp] = wk;
+    if (warp == 0) {
+      int v = mp[lane];
+      if (lane == q) v = pb; else if (lane == i1) v = pa;
+      if (pivsiz == 2) {
+        if (lane == q + 1) v = ci2; else if (lane == i2) v = cq1;
+      }
+      map[nxt][lane] = v;
+    }
+    cur = nxt;
+    q = qn;
+  }
+  if (warp == 0) inv[lane] = lx;
+  __syncthreads();
+  if (singular) {
+    if (tid == 0) { st->status = kDevSingular; st->bs = 0; }
+    return;
+  }
+  // D^{-1} in FP64 from the recorded pivots
+  if (tid < bs) {
+    const int ps = psz[tid];
+    if (ps == 1) {
+      dd[2 * tid] = recip_nr((double)pv[tid][0]);
+      dd[2 * tid + 1] = 0.0;
+    } else if (ps == 2) {
+      const double d11 = pv[tid][0], d21 = pv[tid][1], d22 = pv[tid][2];
+      const double detscale = recip_nr(fabs(d21));
+      const double detpiv = (d11 * detscale) * d22 - fabs(d21);
+      const double rdet = recip_nr(detpiv);
+      dd[2 * tid] = (d22 * detscale) * rdet;
+      dd[2 * tid + 1] = (-d21 * detscale) * rdet;
+      dd[2 * tid + 2] = dinf();
+      dd[2 * tid + 3] = (d11 * detscale) * rdet;
+    } else if (ps == 0) {
+      dd[2 * tid] = 0.0;
+      dd[2 * tid + 1] = 0.0;
+    }
+  }
+  __syncthreads();
+  // ---- write L11 (logical lower part, unit diagonal), D, step buffer, perm
+  const int* fmap = map[cur];
+  for (int e = tid; e < kBlk * kBlk; e += kDiagThreads) {
+    const int j = e >> 5, X = e & 31;  // logical column, physical row
+    if (j < bs && X < bs) {
+      const int i = inv[X];
+      if (i >= j) {
+        const float v = (i == j) ? 1.f : outb[j][X];
+        fd.L[(int64_t)(p + j) * fd.ld + p + i] = v;
+        fd.step[j * kBlk + i] = (double)v;
+      }
+    }
+  }
+  if (tid < bs) {
+    fd.D[2 * (p + tid)] = dd[2 * tid];
+    fd.D[2 * (p + tid) + 1] = dd[2 * tid + 1];
+    fd.step[kBlk * kBlk + 2 * tid] = dd[2 * tid];
+    fd.step[kBlk * kBlk + 2 * tid + 1] = dd[2 * tid + 1];
+    fd.lperm[tid] = fmap[tid];
+  }
+  int oldp = 0, oldo = 0;
+  if (tid < bs) { oldp = fd.perm[p + fmap[tid]]; oldo = fd.opos[p + fmap[tid]]; }
   __syncthreads();
   if (tid < bs) { fd.perm[p + tid] = oldp; fd.opos[p + tid] = oldo; }
 }
@@ -990,6 +1263,8 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
   pmark(tm, kPhDiag, s);
   if (posdef) {
     k_app_diag<T, true><<<nf, kDiagThreads, 0, s>>>(fd, st, fronts, step, action, small);
+  } else if constexpr (std::is_same<T, float>::value) {
+    k_app_diag_f32<<<nf, kDiagThreads, 0, s>>>(fd, st, fronts, step, action, small);
   } else {
     k_app_diag<T, false><<<nf, kDiagThreads, 0, s>>>(fd, st, fronts, step, action, small);
   }

@@ -284,3 +284,25 @@ def test_gpu_captured_refactorisation_matches_eager(precision, monkeypatch):
     tol = 1e-13 if precision == ssids.PRECISION_FP64 else 1e-4
     for (x, _, _), vals in zip(res["1"], seq[1:]):
         assert M.scaled_bwd_error(p, r, vals, x, b).max() <= tol
+
+
+@pytest.mark.parametrize("seed,diag_scale", [(1, 0.01), (2, 0.001), (3, 0.1), (5, 1e-5)])
+def test_gpu_mixed_indefinite_pivots(seed, diag_scale):
+    """FP32 factors of nonsingular matrices with many 2x2 pivots and delays
+    (FP32 pivot decisions, FP64 D^{-1}): the inertia equals the FP64
+    factorisation's and FP64 refinement reaches the backward-error target.
+    (For a singular matrix the rank found depends on the factor precision:
+    FP32 rounding noise stays far above the zero-pivot threshold.)"""
+    p, r, v = M.random_indef(600, density=0.02, seed=seed, diag_scale=diag_scale)
+    ak = ssids.analyse(p, r, ssids.order_mindeg(p, r))
+    fd, infd = ssids.factor(ak, v)
+    fm, infm = ssids.factor(ak, v, ssids.Options(precision=ssids.PRECISION_MIXED,
+                                                 max_refine=30, refine_tol=1e-15))
+    assert infm.flag >= 0
+    assert infm.num_two > 0
+    assert (infm.num_neg, infm.matrix_rank) == (infd.num_neg, infd.matrix_rank)
+    b = np.random.default_rng(seed).standard_normal((600, 3))
+    x = fm.solve_refined(b)
+    assert M.scaled_bwd_error(p, r, v, x, b).max() <= BWD_TOL
+    fd.free()
+    fm.free()
