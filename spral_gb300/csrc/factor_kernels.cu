@@ -136,6 +136,8 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
                                                            bool action, double small) {
   constexpr bool kF64 = sizeof(T) == 8;
   const int f = fronts[blockIdx.x];
+  pdl_wait();
+  pdl_trigger();
   FrontState* st = &sts[f];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // owned pair (physical R >= C)
@@ -393,6 +395,8 @@ __global__ void __launch_bounds__(kDiagThreads)
     k_app_diag_f32(FrontDesc<float>* fds, FrontState* sts, const int* fronts, int step,
                    bool action, double small) {
   const int f = fronts[blockIdx.x];
+  pdl_wait();
+  pdl_trigger();
   FrontState* st = &sts[f];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int R = (int)((sqrtf(8.0f * tid + 1.0f) - 1.0f) * 0.5f);
@@ -621,6 +625,10 @@ __global__ void __launch_bounds__(kDiagThreads)
   if (tid < bs) { fd.perm[p + tid] = oldp; fd.opos[p + tid] = oldo; }
 }
 
+// columns of the eliminated part that one warp of k_app_apply's permutation
+// CTAs moves per round
+constexpr int kPermCols = 8;
+
 // ------------------------------------------------------------------------
 // k_app_apply: rows below the block; solve, scale, threshold test
 // ------------------------------------------------------------------------
@@ -629,6 +637,8 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
                                                           const int* fronts, double u,
                                                           double small, int napply) {
   const int f = fronts[blockIdx.y];
+  pdl_wait();
+  pdl_trigger();
   FrontState* st = &sts[f];
   const int bs = st->bs;
   if (bs == 0) return;
@@ -637,13 +647,20 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
   if ((int)blockIdx.x >= napply) {
     // block permutation of rows [p, p+bs) in the eliminated columns [0, p)
     if (p == 0) return;
+    // a warp permutes kPermCols columns per round: all loads, then all stores
+    constexpr int U = kPermCols;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int src = (lane < bs) ? fd.lperm[lane] : lane;
-    for (int c = (blockIdx.x - napply) * nw + warp; c < p; c += (gridDim.x - napply) * nw) {
-      T* col = fd.L + (int64_t)c * fd.ld + p;
-      const T v = (lane < bs) ? col[src] : T(0);
+    const int wstride = (gridDim.x - napply) * nw;
+    for (int c0 = ((blockIdx.x - napply) * nw + warp) * U; c0 < p; c0 += wstride * U) {
+      T v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        v[u] = (lane < bs && c0 + u < p) ? fd.L[(int64_t)(c0 + u) * fd.ld + p + src] : T(0);
       __syncwarp();
-      if (lane < bs) col[lane] = v;
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (lane < bs && c0 + u < p) fd.L[(int64_t)(c0 + u) * fd.ld + p + lane] = v[u];
     }
     return;
   }
@@ -774,6 +791,8 @@ template <typename T>
 __global__ void __launch_bounds__(kApplyRows) k_app_fixup(FrontDesc<T>* fds, FrontState* sts,
                                                           const int* fronts) {
   const int f = fronts[blockIdx.y];
+  pdl_wait();
+  pdl_trigger();
   FrontState* st = &sts[f];
   const int bs = st->bs;
   if (bs == 0) return;
@@ -878,6 +897,8 @@ __device__ __forceinline__ int swap_partner(const SwapRanges& s, int x) {
 template <typename T>
 __global__ void k_app_swap(FrontDesc<T>* fds, const FrontState* sts, const int* fronts) {
   const int f = fronts[blockIdx.x];
+  pdl_wait();
+  pdl_trigger();
   const FrontState st = sts[f];
   if (st.bs == 0 || st.bs == st.npass) return;
   FrontDesc<T> fd = fds[f];
@@ -1262,21 +1283,25 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
   if (nf <= 0) return;
   pmark(tm, kPhDiag, s);
   if (posdef) {
-    k_app_diag<T, true><<<nf, kDiagThreads, 0, s>>>(fd, st, fronts, step, action, small);
+    launch_pdl(k_app_diag<T, true>, nf, kDiagThreads, 0, s, fd, st, fronts, step, action, small);
   } else if constexpr (std::is_same<T, float>::value) {
-    k_app_diag_f32<<<nf, kDiagThreads, 0, s>>>(fd, st, fronts, step, action, small);
+    launch_pdl(k_app_diag_f32, nf, kDiagThreads, 0, s, fd, st, fronts, step, action, small);
   } else {
-    k_app_diag<T, false><<<nf, kDiagThreads, 0, s>>>(fd, st, fronts, step, action, small);
+    launch_pdl(k_app_diag<T, false>, nf, kDiagThreads, 0, s, fd, st, fronts, step, action, small);
   }
   note_launches(1);
   // apply (+ row permutation of the eliminated part in extra CTAs)
   const int napply = std::max(1, cdiv(max_rows, kApplyRows));
   const int pcols = step * kBlk;  // upper bound on p
-  const int nperm = pcols > 0 ? std::max(1, std::min(cdiv(pcols, kApplyRows / 32), 64)) : 0;
+  const int nperm =
+      pcols > 0 ? std::max(1, std::min(cdiv(pcols, (kApplyRows / 32) * kPermCols), 128)) : 0;
   pmark(tm, kPhApply, s);
-  { k_app_apply<T><<<dim3(napply + nperm, nf), kApplyRows, 0, s>>>(fd, st, fronts, u, small, napply); note_launches(1); }
+  launch_pdl(k_app_apply<T>, dim3(napply + nperm, nf), kApplyRows, 0, s, fd, st, fronts, u, small,
+             napply);
+  note_launches(1);
   pmark(tm, kPhFixup, s);
-  { k_app_fixup<T><<<dim3(napply, nf), kApplyRows, 0, s>>>(fd, st, fronts); note_launches(1); }
+  launch_pdl(k_app_fixup<T>, dim3(napply, nf), kApplyRows, 0, s, fd, st, fronts);
+  note_launches(1);
   // tile estimate assumes no failed columns so far; after failures the
   // trailing region is wider and the kernel's grid-stride loop covers it, so
   // the launch is never skipped
@@ -1285,7 +1310,8 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
   pmark(tm, kPhPanel, s);
   launch_syrk_panel<T>(fd, st, fronts, nf, std::max(tiles, 1), s);
   pmark(tm, kPhSwap, s);
-  { k_app_swap<T><<<nf, 256, 0, s>>>(fd, st, fronts); note_launches(1); }
+  launch_pdl(k_app_swap<T>, nf, 256, 0, s, fd, st, fronts);
+  note_launches(1);
 }
 
 template <typename T>

@@ -47,7 +47,9 @@ template <typename T, int MODE>
 __global__ void __launch_bounds__(256) k_syrk(FrontDesc<T>* fds, const FrontState* sts,
                                               const int* fronts) {
   const int f = fronts[blockIdx.y];
-  const FrontDesc<T> fd = fds[f];
+  const FrontDesc<T> fd = fds[f];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
   const FrontState st = sts[f];
   SyrkJob<T> j;
   if (!make_job<T, MODE>(fd, st, j)) return;
@@ -107,7 +109,8 @@ template <typename T>
 void launch_syrk_panel(FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
                        int max_tiles, cudaStream_t s) {
   int gx = max_tiles < 1 ? 1 : (max_tiles > 4096 ? 4096 : max_tiles);
-  { k_syrk<T, 0><<<dim3(gx, nf), 256, 0, s>>>(fd, st, fronts); note_launches(1); }
+  launch_pdl(k_syrk<T, 0>, dim3(gx, nf), 256, 0, s, fd, st, fronts);
+  note_launches(1);
 }
 template <typename T>
 void launch_syrk_contrib(FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,

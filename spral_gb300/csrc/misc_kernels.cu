@@ -23,55 +23,103 @@ __global__ void k_zero_fronts(FrontDesc<T>* fds, const int* fronts) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 2 * fd.n; i += stride) fd.D[i] = 0.0;
 }
 
-// r = b - A x, warp per row
-__global__ void k_spmv_resid(const int64_t* aptr, const int* acol, const int64_t* asrc,
-                             const double* aval, int n, const double* x, const double* b,
-                             double* r, int nrhs, int ld) {
-  const int lane = threadIdx.x & 31;
-  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = w; i < n; i += nw) {
-    for (int q = 0; q < nrhs; ++q) {
-      double s = 0.0;
-      for (int64_t k = aptr[i] + lane; k < aptr[i + 1]; k += 32)
-        s += aval[asrc[k]] * x[(int64_t)q * ld + acol[k]];
-      for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-      if (lane == 0) r[(int64_t)q * ld + i] = b[(int64_t)q * ld + i] - s;
-    }
-  }
-}
-
 __device__ __forceinline__ void atomic_max_pos(double* a, double v) {
   // non-negative doubles order like their bit patterns
   atomicMax(reinterpret_cast<unsigned long long*>(a), (unsigned long long)__double_as_longlong(v));
 }
 
-// work: [0] ||A||, then per rhs (xn, bn, rn) at 1 + 3q
-__global__ void k_norms(const int64_t* aptr, const int64_t* asrc, const double* aval, int n,
-                        const double* x, const double* r, const double* b, int nrhs, int ld,
-                        double* work) {
-  double an = 0.0;
-  double loc[3 * kSolveRhs];
-  for (int i = 0; i < 3 * kSolveRhs; ++i) loc[i] = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    double rs = 0.0;
-    for (int64_t k = aptr[i]; k < aptr[i + 1]; ++k) rs += fabs(aval[asrc[k]]);
-    an = fmax(an, rs);
-    for (int q = 0; q < nrhs && q < kSolveRhs; ++q) {
-      loc[3 * q] = fmax(loc[3 * q], fabs(x[(int64_t)q * ld + i]));
-      loc[3 * q + 1] = fmax(loc[3 * q + 1], fabs(b[(int64_t)q * ld + i]));
-      loc[3 * q + 2] = fmax(loc[3 * q + 2], fabs(r[(int64_t)q * ld + i]));
+// r = b - A x and the maxima of the scaled backward error in one pass.
+// kResG lanes share a row (its non-zeros strided over the lanes); each
+// non-zero is applied to kResQC right-hand sides at once (chunk
+// blockIdx.y), so the row's index and value loads are shared by the chunk.
+// Every lane of a warp runs the same number of row iterations, so the lane
+// reductions use full-warp shuffles.  work: [0] ||A||_inf, then per rhs
+// (||x||, ||b||, ||r||) at 1 + 3q (maxima, order-independent).
+constexpr int kResG = 4;
+constexpr int kResQC = 4;
+__global__ void __launch_bounds__(256) k_resid_norms(const int64_t* aptr, const int* acol,
+                                                     const int64_t* asrc, const double* aval,
+                                                     int n, const double* x, const double* b,
+                                                     double* r, int nrhs, int ld, double* work) {
+  constexpr int G = kResG, QC = kResQC, RPW = 32 / G;
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1);
+  const int q0 = blockIdx.y * QC;
+  const int nq = min(QC, nrhs - q0);
+  const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double an = 0.0, mx[QC], mb[QC], mr[QC];
+#pragma unroll
+  for (int q = 0; q < QC; ++q) mx[q] = mb[q] = mr[q] = 0.0;
+  for (int64_t base = warp * RPW; base < n; base += nwarp * RPW) {
+    const int64_t i = base + lane / G;
+    const bool ok = i < n;
+    double s[QC], ra = 0.0;
+#pragma unroll
+    for (int q = 0; q < QC; ++q) s[q] = 0.0;
+    if (ok) {
+      const int64_t k1 = aptr[i + 1];
+      for (int64_t k = aptr[i] + sub; k < k1; k += G) {
+        const double a = aval[asrc[k]];
+        const int64_t c = acol[k];
+        ra += fabs(a);
+#pragma unroll
+        for (int q = 0; q < QC; ++q)
+          if (q < nq) s[q] = fma(a, x[(int64_t)(q0 + q) * ld + c], s[q]);
+      }
+    }
+#pragma unroll
+    for (int off = G / 2; off > 0; off >>= 1) {
+      ra += __shfl_xor_sync(0xffffffffu, ra, off);
+#pragma unroll
+      for (int q = 0; q < QC; ++q) s[q] += __shfl_xor_sync(0xffffffffu, s[q], off);
+    }
+    if (ok && sub == 0) {
+      an = fmax(an, ra);
+#pragma unroll
+      for (int q = 0; q < QC; ++q) {
+        if (q < nq) {
+          const int64_t e = (int64_t)(q0 + q) * ld + i;
+          const double bi = b[e], ri = bi - s[q];
+          r[e] = ri;
+          mx[q] = fmax(mx[q], fabs(x[e]));
+          mb[q] = fmax(mb[q], fabs(bi));
+          mr[q] = fmax(mr[q], fabs(ri));
+        }
+      }
     }
   }
+  // warp maxima -> block maxima in shared memory -> one atomic per value
+  // and block (same-address atomics from every warp would serialise)
+  constexpr int NV = 1 + 3 * QC;
+  __shared__ double red[256 / 32][NV];
+  const int warp_in_block = threadIdx.x >> 5;
   for (int off = 16; off > 0; off >>= 1) an = fmax(an, __shfl_xor_sync(0xffffffffu, an, off));
-  if ((threadIdx.x & 31) == 0) atomic_max_pos(&work[0], an);
-  for (int q = 0; q < nrhs && q < kSolveRhs; ++q)
-    for (int j = 0; j < 3; ++j) {
-      double v = loc[3 * q + j];
-      for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
-      if ((threadIdx.x & 31) == 0) atomic_max_pos(&work[1 + 3 * q + j], v);
+  if (lane == 0) red[warp_in_block][0] = an;
+#pragma unroll
+  for (int q = 0; q < QC; ++q) {
+    double v0 = mx[q], v1 = mb[q], v2 = mr[q];
+    for (int off = 16; off > 0; off >>= 1) {
+      v0 = fmax(v0, __shfl_xor_sync(0xffffffffu, v0, off));
+      v1 = fmax(v1, __shfl_xor_sync(0xffffffffu, v1, off));
+      v2 = fmax(v2, __shfl_xor_sync(0xffffffffu, v2, off));
     }
+    if (lane == 0) {
+      red[warp_in_block][1 + 3 * q] = v0;
+      red[warp_in_block][2 + 3 * q] = v1;
+      red[warp_in_block][3 + 3 * q] = v2;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    const int v = threadIdx.x;
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w][v]);
+    if (v == 0) {
+      if (blockIdx.y == 0) atomic_max_pos(&work[0], m);
+    } else if ((v - 1) / 3 < nq) {
+      atomic_max_pos(&work[1 + 3 * q0 + (v - 1)], m);
+    }
+  }
 }
 
 __global__ void k_bwd_finish(const double* work, int nrhs, double* out) {
@@ -102,29 +150,25 @@ void launch_zero_fronts(FrontDesc<T>* fd, const int* fronts, int nf, int max_ele
 template void launch_zero_fronts<double>(FrontDesc<double>*, const int*, int, int, cudaStream_t);
 template void launch_zero_fronts<float>(FrontDesc<float>*, const int*, int, int, cudaStream_t);
 
-void launch_spmv_resid(const int64_t* aptr, const int* acol, const int64_t* asrc,
-                       const double* aval, int n, const double* x, const double* b, double* r,
-                       int nrhs, int ld, cudaStream_t s) {
-  int blocks = std::max(1, std::min((n + 7) / 8, 4096));
-  { k_spmv_resid<<<blocks, 256, 0, s>>>(aptr, acol, asrc, aval, n, x, b, r, nrhs, ld); note_launches(1); }
+// r = b - A x and the scaled backward error of each right-hand side (work
+// must hold nrhs + 1 + 3*kSolveRhs doubles; the result per rhs is written
+// to work[0 .. nrhs)).
+void launch_resid_bwd_err(const int64_t* aptr, const int* acol, const int64_t* asrc,
+                          const double* aval, int n, const double* x, const double* b, double* r,
+                          int nrhs, int ld, double* work, cudaStream_t s) {
+  double* acc = work + nrhs;
+  cudaMemsetAsync(acc, 0, (1 + 3 * kSolveRhs) * sizeof(double), s);
+  const int rows_per_block = 256 / 32 * (32 / kResG);
+  const int bx = std::max(1, std::min((n + rows_per_block - 1) / rows_per_block, 4 * 152));
+  const int by = (nrhs + kResQC - 1) / kResQC;
+  { k_resid_norms<<<dim3(bx, by), 256, 0, s>>>(aptr, acol, asrc, aval, n, x, b, r, nrhs, ld, acc); note_launches(1); }
+  { k_bwd_finish<<<1, 32, 0, s>>>(acc, nrhs, work); note_launches(1); }
 }
 
 void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s) {
   int64_t total = (int64_t)n * nrhs;
   int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 4096));
   { k_axpy<<<blocks, 256, 0, s>>>(total, n, ld, x, d); note_launches(1); }
-}
-
-// work must hold 1 + 3*nrhs + nrhs doubles; the result (per rhs) is written
-// to work[0 .. nrhs) after the reduction.
-void launch_bwd_err(const int64_t* aptr, const int64_t* asrc, const double* aval, int n,
-                    const double* x, const double* r, const double* b, int nrhs, int ld,
-                    double* work, cudaStream_t s) {
-  double* acc = work + nrhs;
-  cudaMemsetAsync(acc, 0, (1 + 3 * kSolveRhs) * sizeof(double), s);
-  int blocks = std::max(1, std::min((n + 255) / 256, 1024));
-  { k_norms<<<blocks, 256, 0, s>>>(aptr, asrc, aval, n, x, r, b, nrhs, ld, acc); note_launches(1); }
-  { k_bwd_finish<<<1, 32, 0, s>>>(acc, nrhs, work); note_launches(1); }
 }
 
 }  // namespace ssids300

@@ -187,6 +187,8 @@ struct Symbolic {
   int* d_fronts = nullptr;
   int4* d_cols = nullptr;
   int2* d_pairs = nullptr;
+  int* d_gp = nullptr;        // per front, nrow + 1 offsets into d_pairs by parent position
+  std::vector<int64_t> gp_off;
   // FP64 matrix in pivot order (full CSR, both triangles) for refinement
   int64_t* d_aptr = nullptr;
   int* d_acol = nullptr;
@@ -196,7 +198,7 @@ struct Symbolic {
   ~Symbolic() {
     cudaFree(d_nptr); cudaFree(d_nlist); cudaFree(d_sptr); cudaFree(d_rlist); cudaFree(d_rptr);
     cudaFree(d_rdir); cudaFree(d_rdir_ptr); cudaFree(d_fronts); cudaFree(d_cols);
-    cudaFree(d_pairs); cudaFree(d_aptr); cudaFree(d_acol); cudaFree(d_asrc);
+    cudaFree(d_pairs); cudaFree(d_gp); cudaFree(d_aptr); cudaFree(d_acol); cudaFree(d_asrc);
   }
 };
 
@@ -312,9 +314,14 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
     }
   }
   // extend-add work: per level, per parent column, the (child, jc) pairs
+  // (the same pairs, indexed by parent position through gp, drive the
+  // forward solve's gather: gp[gp_off[f] + P] .. gp[gp_off[f] + P + 1])
   std::vector<int4> cols;
   std::vector<int2> pairs;
   S->cols_start.assign(nlev + 1, 0);
+  S->gp_off.assign(nn + 1, 0);
+  for (int f = 0; f < nn; ++f) S->gp_off[f + 1] = S->gp_off[f] + S->nrow[S->node_of[f]] + 1;
+  std::vector<int> gp(S->gp_off[nn] + 1, 0);
   for (int l = 0; l < nlev; ++l) {
     S->cols_start[l] = (int)cols.size();
     for (int f = S->lvl_start[l]; f < S->lvl_start[l + 1]; ++f) {
@@ -328,11 +335,13 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
         }
       }
       for (int P = 0; P < S->nrow[p]; ++P) {
+        gp[S->gp_off[f] + P] = (int)pairs.size();
         if (per[P].empty()) continue;
         int beg = (int)pairs.size();
         for (auto& q : per[P]) pairs.push_back(q);
         cols.push_back(make_int4(f, P, beg, (int)pairs.size()));
       }
+      gp[S->gp_off[f] + S->nrow[p]] = (int)pairs.size();
     }
   }
   S->cols_start[nlev] = (int)cols.size();
@@ -382,6 +391,7 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
   S->d_fronts = upload(fronts);
   S->d_cols = upload(cols);
   S->d_pairs = upload(pairs);
+  S->d_gp = upload(gp);
   return S.release();
 }
 
@@ -419,13 +429,10 @@ struct NumericBase {
 template <typename T>
 void launch_zero_fronts(FrontDesc<T>* fd, const int* fronts, int nf, int max_elems,
                         cudaStream_t s);
-void launch_spmv_resid(const int64_t* aptr, const int* acol, const int64_t* asrc,
-                       const double* aval, int n, const double* x, const double* b, double* r,
-                       int nrhs, int ld, cudaStream_t s);
+void launch_resid_bwd_err(const int64_t* aptr, const int* acol, const int64_t* asrc,
+                          const double* aval, int n, const double* x, const double* b, double* r,
+                          int nrhs, int ld, double* work, cudaStream_t s);
 void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s);
-void launch_bwd_err(const int64_t* aptr, const int64_t* asrc, const double* aval, int n,
-                    const double* x, const double* r, const double* b, int nrhs, int ld,
-                    double* work, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // Crossover of the FP32 contribution update between the SIMT kernel and the
@@ -567,7 +574,7 @@ struct Numeric : NumericBase {
     for (auto& g : sgraphs) cudaGraphExecDestroy(g.exec);
     sgraphs.clear();
   }
-  DevBuf<T> xloc, xorig;
+  DevBuf<T> xloc;
   DevBuf<double> xbuf, rbuf, dbuf, bbuf, nbuf;
   // tensor-core contribution GEMM (FP32 factors only)
   bool use_tc = false;
@@ -1157,7 +1164,6 @@ struct Numeric : NumericBase {
     std::vector<size_t> xoff(nn);
     for (int f = 0; f < nn; ++f) { xoff[f] = xl; xl += (size_t)m_[f] * kSolveRhs; }
     xloc.ensure(xl + 1);
-    xorig.ensure(xl + 1);
     for (int f = 0; f < nn; ++f) {
       const int node = S->node_of[f];
       SolveNode<T>& q = sn[f];
@@ -1165,7 +1171,7 @@ struct Numeric : NumericBase {
       q.rows = S->d_rlist + S->rptr[node];
       q.rdir = S->d_rdir + S->rdir_ptr_h[node];
       q.xloc = xloc.p + xoff[f];
-      q.xorig = xorig.p + xoff[f];
+      q.gp = S->d_gp + S->gp_off[f];
       q.m = m_[f]; q.n = n_[f]; q.ld = ld_[f]; q.nelim = nelim_[f];
       q.ncol = S->ncol[node]; q.nrow = S->nrow[node]; q.ndelay_in = ndin_[f];
       q.cm = S->nrow[node] - S->ncol[node];
@@ -1199,7 +1205,7 @@ struct Numeric : NumericBase {
     auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ull; };
     for (int l = 0; l < S->nlev; ++l) { mix((uint64_t)lvl_max_m[l]); mix((uint64_t)lvl_max_nelim[l]); }
     mix((uint64_t)(uintptr_t)d_sn); mix((uint64_t)(uintptr_t)d_children);
-    mix((uint64_t)(uintptr_t)xloc.p); mix((uint64_t)(uintptr_t)xorig.p);
+    mix((uint64_t)(uintptr_t)xloc.p);
     if (h != solve_sig) drop_graphs();
     solve_sig = h;
     solve_ready = true;
@@ -1218,7 +1224,7 @@ struct Numeric : NumericBase {
         const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
         const int* fr = S->d_fronts + f0;
         pmark(tm(), kPhFwdGather, s);
-        launch_fwd_gather<T>(d_sn, fr, nf, d_children, xp, ldx, q, s);
+        launch_fwd_gather<T>(d_sn, fr, nf, d_children, S->d_pairs, xp, ldx, q, lvl_max_m[l], s);
         launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, s, tm());
         pmark(tm(), kPhFwdScatter, s);
         launch_fwd_scatter<T>(d_sn, fr, nf, xp, ldx, q, lvl_max_nelim[l], s, job == 5);
@@ -1346,8 +1352,8 @@ struct Numeric : NumericBase {
     const int maxit = S->gopts.max_refine;
     for (;; ++it) {
       pmark(tm(), kPhResid, s);
-      launch_spmv_resid(S->d_aptr, S->d_acol, S->d_asrc, cur_aval, n, x, b, rbuf.p, q, ld, s);
-      launch_bwd_err(S->d_aptr, S->d_asrc, cur_aval, n, x, rbuf.p, b, q, ld, nbuf.p, s);
+      launch_resid_bwd_err(S->d_aptr, S->d_acol, S->d_asrc, cur_aval, n, x, b, rbuf.p, q, ld,
+                           nbuf.p, s);
       pmark(tm(), kPhHost, s);
       CK(cudaMemcpyAsync(h.data(), nbuf.p, q * sizeof(double), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));

@@ -32,79 +32,41 @@ namespace {
 
 constexpr int SB = kSolveBlk;
 
-// gather b and the children's local vectors into the node's local vector
-// (the whole CTA works on one node).  Every loop handles kGatherBatch
-// elements per thread with all loads issued before the stores, so each
-// batch costs one memory round trip (positions within one child are
-// distinct, so a batch never updates one entry twice).
-constexpr int kGatherBatch = 8;
+// Value of assembly-order position pos of a node's local vector for
+// right-hand side q: b for the node's own pivots, the delayed entry of the
+// child that delayed it, and the contribution rows that the children map to
+// pos (pair list gp, children in their fixed order).  Each entry is a pure
+// function of b and the children's local vectors, so any number of CTAs can
+// gather one node; the additions run in child order, so the sums do not
+// depend on the launch shape.
 template <typename T>
-__device__ __forceinline__ void fwd_gather_node(const SolveNode<T>& sn, const SolveNode<T>* sns,
-                                                const int* children, const double* x, int ldx,
-                                                int nrhs) {
-  constexpr int GB = kGatherBatch;
-  const int m = sn.m;
-  const int nt = blockDim.x;
-  T* xo = sn.xorig;
-  for (int e0 = threadIdx.x; e0 < m * nrhs; e0 += GB * nt) {
-    T v[GB];
-#pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int e = e0 + u * nt;
-      const int i = e % m, r = e / m;
-      v[u] = (e < m * nrhs && i < sn.ncol) ? (T)x[(int64_t)r * ldx + sn.sptr0 + i] : T(0);
+__device__ __forceinline__ T gather_value(const SolveNode<T>& sn, const SolveNode<T>* sns,
+                                          const int* children, const int2* pairs,
+                                          const double* x, int ldx, int q, int pos) {
+  T v = T(0);
+  int P;
+  if (pos < sn.ncol) {
+    v = (T)x[(int64_t)q * ldx + sn.sptr0 + pos];
+    P = pos;
+  } else if (pos < sn.ncol + sn.ndelay_in) {
+    const int k = pos - sn.ncol;
+    for (int ci = sn.child_beg; ci < sn.child_end; ++ci) {
+      const SolveNode<T>& cn = sns[children[ci]];
+      const int nd = cn.n - cn.nelim;
+      if (k >= cn.doff && k < cn.doff + nd)
+        return cn.xloc[(int64_t)q * cn.m + cn.nelim + (k - cn.doff)];
     }
-#pragma unroll
-    for (int u = 0; u < GB; ++u)
-      if (e0 + u * nt < m * nrhs) xo[e0 + u * nt] = v[u];
+    return v;
+  } else {
+    P = pos - sn.ndelay_in;
   }
-  __syncthreads();
-  for (int ci = sn.child_beg; ci < sn.child_end; ++ci) {
-    const SolveNode<T> cn = sns[children[ci]];
-    const int nd = cn.n - cn.nelim;
-    const int tot = nd + cn.cm;
-    for (int e0 = threadIdx.x; e0 < tot * nrhs; e0 += GB * nt) {
-      int pos[GB];
-      T v[GB];
-#pragma unroll
-      for (int u = 0; u < GB; ++u) {
-        const int e = e0 + u * nt;
-        const int k = e % tot, r = e / tot;
-        pos[u] = -1;
-        v[u] = T(0);
-        if (e < tot * nrhs) {
-          if (k < nd) {
-            pos[u] = r * m + sn.ncol + cn.doff + k;
-            v[u] = cn.xloc[(int64_t)r * cn.m + cn.nelim + k];
-          } else {
-            const int ic = k - nd;
-            const int Q = cn.rdir[ic];
-            pos[u] = r * m + ((Q < sn.ncol) ? Q : Q + sn.ndelay_in);
-            v[u] = cn.xloc[(int64_t)r * cn.m + cn.n + ic];
-          }
-        }
-      }
-      T old[GB];
-#pragma unroll
-      for (int u = 0; u < GB; ++u) old[u] = (pos[u] >= 0) ? xo[pos[u]] : T(0);
-#pragma unroll
-      for (int u = 0; u < GB; ++u)
-        if (pos[u] >= 0) xo[pos[u]] = old[u] + v[u];
-    }
-    __syncthreads();
+  const int k1 = sn.gp[P + 1];
+  for (int k = sn.gp[P]; k < k1; ++k) {
+    const int2 pr = pairs[k];
+    const SolveNode<T>& cn = sns[pr.x];
+    v += cn.xloc[(int64_t)q * cn.m + cn.n + pr.y];
   }
-  for (int e0 = threadIdx.x; e0 < m * nrhs; e0 += GB * nt) {
-    T v[GB];
-#pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int e = e0 + u * nt;
-      const int i = e % m, r = e / m;
-      v[u] = (e < m * nrhs) ? ((i < sn.n) ? xo[(int64_t)r * m + sn.opos[i]] : xo[e]) : T(0);
-    }
-#pragma unroll
-    for (int u = 0; u < GB; ++u)
-      if (e0 + u * nt < m * nrhs) sn.xloc[e0 + u * nt] = v[u];
-  }
+  return v;
 }
 
 // stage the jb x jb diagonal block (strictly lower part) into shared memory;
@@ -113,25 +75,56 @@ __device__ __forceinline__ void fwd_gather_node(const SolveNode<T>& sn, const So
 constexpr int kSolveThreads = 256;
 constexpr int kSolveWarps = kSolveThreads / 32;
 constexpr int LDB = SB + 1;  // leading dimension of a staged block Lb[c * LDB + r]
+constexpr int kDiagPer = SB * SB / kSolveThreads;  // entries of a staged block per thread
 template <typename T>
-__device__ __forceinline__ void load_diag_block(const SolveNode<T>& sn, int j0, int jb, T* Lb) {
-  constexpr int PER = SB * SB / kSolveThreads;
-  constexpr int BATCH = PER < 32 ? PER : 32;
+__device__ __forceinline__ void fetch_diag_block(const SolveNode<T>& sn, int j0, int jb,
+                                                 T (&v)[kDiagPer]) {
 #pragma unroll
-  for (int b0 = 0; b0 < PER; b0 += BATCH) {
-    T v[BATCH];
+  for (int k = 0; k < kDiagPer; ++k) {
+    const int e = threadIdx.x + k * kSolveThreads;
+    const int c = e / SB, r = e % SB;
+    v[k] = (r > c && r < jb && c < jb) ? sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : T(0);
+  }
+}
+template <typename T>
+__device__ __forceinline__ void store_diag_block(const T (&v)[kDiagPer], T* Lb) {
 #pragma unroll
-    for (int k = 0; k < BATCH; ++k) {
-      const int e = threadIdx.x + (b0 + k) * kSolveThreads;
-      const int c = e / SB, r = e % SB;
-      v[k] = (r > c && r < jb && c < jb) ? sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : T(0);
-    }
+  for (int k = 0; k < kDiagPer; ++k) {
+    const int e = threadIdx.x + k * kSolveThreads;
+    Lb[(e / SB) * LDB + e % SB] = v[k];
+  }
+}
+// the same staging with asynchronous copies (cp.async), so that a CTA can
+// start it, do other work, and wait for it with cp_async_wait_all() and a
+// barrier before the block is read
+template <typename T>
+__device__ __forceinline__ void prefetch_diag_block(const SolveNode<T>& sn, int j0, int jb, T* Lb) {
 #pragma unroll
-    for (int k = 0; k < BATCH; ++k) {
-      const int e = threadIdx.x + (b0 + k) * kSolveThreads;
-      Lb[(e / SB) * LDB + e % SB] = v[k];
+  for (int k = 0; k < kDiagPer; ++k) {
+    const int e = threadIdx.x + k * kSolveThreads;
+    const int c = e / SB, r = e % SB;
+    T* dst = Lb + c * LDB + r;
+    if (r > c && r < jb && c < jb) {
+      const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+      const T* src = sn.L + (int64_t)(j0 + c) * sn.ld + j0 + r;
+      if constexpr (sizeof(T) == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(src) : "memory");
+      else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(src) : "memory");
+    } else {
+      *dst = T(0);
     }
   }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+template <typename T>
+__device__ __forceinline__ void load_diag_block(const SolveNode<T>& sn, int j0, int jb, T* Lb) {
+  T v[kDiagPer];
+  fetch_diag_block(sn, j0, jb, v);
+  store_diag_block(v, Lb);
 }
 
 // Unit lower (FWD) or unit upper L^T (!FWD) triangular solve of rows
@@ -199,25 +192,45 @@ __device__ __forceinline__ void diag_block_solve(const SolveNode<T>& sn, int j0,
   }
 }
 
-// dynamic shared memory of the solve kernels: the staged block, then the
-// block's solved values yb[r * NR + q]
+// dynamic shared memory of the solve kernels: the staged block, the
+// block's solved values yb[r * NR + q], then the partial sums of the
+// update passes red[(qq * NR + q) * 64 + t] (qq = 0..3)
 template <typename T, int NR>
 constexpr size_t solve_smem_bytes() {
-  return sizeof(T) * ((size_t)SB * LDB + (size_t)SB * NR);
+  return sizeof(T) * ((size_t)SB * LDB + (size_t)SB * NR + (size_t)4 * NR * 64);
 }
 
 // ---- forward ----
-// gather (one CTA per node), then the first diagonal block
+// Gather every node of the level into its local vector (final positions:
+// xloc[i] = value of assembly position opos[i] for i < n), then solve the
+// first diagonal block.  CTA 0 of a node gathers rows [0, SB) and solves
+// block 0 from them; CTAs 1.. gather the rows after it (CTA 0 gathers all
+// rows when it is alone).
 template <typename T, int NR>
 __global__ void __launch_bounds__(kSolveThreads)
     k_fwd_gather_diag(const SolveNode<T>* sns, const int* nodes, const int* children,
-                      const double* x, int ldx, int nrhs) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.x]];
-  fwd_gather_node(sn, sns, children, x, ldx, nrhs);
-  if (sn.nelim == 0) return;
+                      const int2* pairs, const double* x, int ldx, int nrhs) {
+  const SolveNode<T> sn = sns[nodes[blockIdx.y]];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
+  const int m = sn.m;
+  const int h = (gridDim.x == 1) ? m : min(m, SB);
+  int lo, len, e0, stride;
+  if (blockIdx.x == 0) {
+    lo = 0; len = h; e0 = threadIdx.x; stride = blockDim.x;
+  } else {
+    lo = h; len = m - h; e0 = (blockIdx.x - 1) * blockDim.x + threadIdx.x;
+    stride = (gridDim.x - 1) * blockDim.x;
+  }
+  for (int e = e0; e < len * nrhs; e += stride) {
+    const int i = lo + e % len, q = e / len;
+    const int pos = (i < sn.n) ? sn.opos[i] : i;
+    sn.xloc[(int64_t)q * m + i] = gather_value(sn, sns, children, pairs, x, ldx, q, pos);
+  }
+  if (blockIdx.x != 0 || sn.nelim == 0) return;
   extern __shared__ __align__(16) unsigned char solve_smem[];
   T* Lb = reinterpret_cast<T*>(solve_smem);
-  __syncthreads();  // xloc rows written by the gather
+  __syncthreads();  // rows [0, h) written by this CTA
   const int jb = min(SB, sn.nelim);
   load_diag_block(sn, 0, jb, Lb);
   __syncthreads();
@@ -278,16 +291,23 @@ __device__ __forceinline__ void load_y(const SolveNode<T>& sn, int j0, int jb, i
 template <typename T, int NR>
 __global__ void __launch_bounds__(kSolveThreads)
     k_fwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.y]];
+  const SolveNode<T> sn = sns[nodes[blockIdx.y]];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
   const int j0 = step * SB;
   if (j0 >= sn.nelim) return;
   const int jb = min(SB, sn.nelim - j0);
   const int i0 = j0 + jb;
   if (i0 >= sn.m) return;
   extern __shared__ __align__(16) unsigned char solve_smem[];
-  T* Lb = reinterpret_cast<T*>(solve_smem);  // also the partial-sum buffer
+  T* Lb = reinterpret_cast<T*>(solve_smem);
   T* yb = Lb + SB * LDB;
-  T* red = Lb;
+  T* red = yb + SB * NR;
+  // CTA 0 starts staging the next diagonal block first: the copies overlap
+  // the update passes (L is read-only here)
+  const bool solve_next = blockIdx.x == 0 && i0 < sn.nelim;
+  const int jb1 = solve_next ? min(SB, sn.nelim - i0) : 0;
+  if (solve_next) prefetch_diag_block(sn, i0, jb1, Lb);
   load_y<T, NR>(sn, j0, jb, nrhs, yb);
   __syncthreads();
   const int t = threadIdx.x % kPassRows, qq = threadIdx.x / kPassRows;
@@ -318,9 +338,8 @@ __global__ void __launch_bounds__(kSolveThreads)
          base += (gridDim.x - 1) * kPassRows)
       pass(base);
   }
-  if (blockIdx.x != 0 || i0 >= sn.nelim) return;
-  const int jb1 = min(SB, sn.nelim - i0);
-  load_diag_block(sn, i0, jb1, Lb);
+  if (!solve_next) return;
+  cp_async_wait_all();
   __syncthreads();
   diag_block_solve<T, NR, true>(sn, i0, jb1, nrhs, Lb);
 }
@@ -328,7 +347,9 @@ __global__ void __launch_bounds__(kSolveThreads)
 template <typename T>
 __global__ void k_fwd_scatter(const SolveNode<T>* sns, const int* nodes, double* x, int ldx,
                               int nrhs, bool scale_sqrt) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.y]];
+  const SolveNode<T> sn = sns[nodes[blockIdx.y]];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
   const int tot = sn.nelim * nrhs;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
     const int i = e % sn.nelim, q = e / sn.nelim;
@@ -344,7 +365,9 @@ __global__ void k_fwd_scatter(const SolveNode<T>* sns, const int* nodes, double*
 template <typename T>
 __global__ void k_bwd_gather(const SolveNode<T>* sns, const int* nodes, const double* x, int ldx,
                              int nrhs, int diag_mode, bool do_bwd) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.y]];
+  const SolveNode<T> sn = sns[nodes[blockIdx.y]];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
   const int mm = do_bwd ? sn.m : sn.nelim;
   const int tot = mm * nrhs;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
@@ -372,44 +395,84 @@ __global__ void k_bwd_gather(const SolveNode<T>* sns, const int* nodes, const do
   }
 }
 
-// xloc[j] -= sum_{i in [nelim, m)} L(i, j) xloc[i] for one column j (one warp)
+// Partial sums of sum_{i in [nelim, m)} L(i, j) xloc[i] for column j over
+// the rows i = nelim + i0, i0 + stride, ... of one lane.  Each lane takes U
+// rows per round with all their loads issued before the FMAs, so a column
+// costs about (m - nelim) / (stride U) memory round trips.
 template <typename T, int NR>
-__device__ __forceinline__ void bwd_l21_column(const SolveNode<T>& sn, int j, int nrhs,
-                                               int lane) {
-  T acc[NR];
-#pragma unroll
-  for (int q = 0; q < NR; ++q) acc[q] = T(0);
+__device__ __forceinline__ void bwd_l21_partial(const SolveNode<T>& sn, int j, int i0, int stride,
+                                                int nrhs, T (&acc)[NR]) {
+  constexpr int U = (NR * sizeof(T) >= 64) ? 2 : 4;
   const T* col = sn.L + (int64_t)j * sn.ld;
-  for (int i = sn.nelim + lane; i < sn.m; i += 32) {
+  int i = sn.nelim + i0;
+  for (; i + stride * (U - 1) < sn.m; i += stride * U) {
+    T l[U], xv[U][NR];
+#pragma unroll
+    for (int u = 0; u < U; ++u) l[u] = col[i + stride * u];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int q = 0; q < NR; ++q)
+        xv[u][q] = (q < nrhs) ? sn.xloc[(int64_t)q * sn.m + i + stride * u] : T(0);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int q = 0; q < NR; ++q) acc[q] += l[u] * xv[u][q];
+  }
+  for (; i < sn.m; i += stride) {
     const T l = col[i];
 #pragma unroll
     for (int q = 0; q < NR; ++q)
       if (q < nrhs) acc[q] += l * sn.xloc[(int64_t)q * sn.m + i];
   }
-#pragma unroll
-  for (int q = 0; q < NR; ++q)
-    for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
-  if (lane == 0)
-    for (int q = 0; q < nrhs; ++q) sn.xloc[(int64_t)q * sn.m + j] -= acc[q];
 }
 
-// L21^T part of the backward solve for every eliminated column (one warp per
-// column: the dot products run over the m - nelim rows below the pivots)
-template <typename T, int NR>
+// L21^T part of the backward solve for every eliminated column:
+// xloc[j] -= sum_{i in [nelim, m)} L(i, j) xloc[i].  W warps share a column
+// (rows strided over their 32 W lanes); their partial sums are added in
+// shared memory in warp order, so the result does not depend on the grid.
+template <typename T, int NR, int W>
 __global__ void __launch_bounds__(kSolveThreads)
     k_bwd_l21(const SolveNode<T>* sns, const int* nodes, int nrhs) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.y]];
+  const SolveNode<T> sn = sns[nodes[blockIdx.y]];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
   if (sn.m <= sn.nelim) return;
+  constexpr int CPB = kSolveWarps / W;  // columns per CTA round
+  __shared__ T part[kSolveWarps][NR];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int j = blockIdx.x * kSolveWarps + warp; j < sn.nelim; j += gridDim.x * kSolveWarps)
-    bwd_l21_column<T, NR>(sn, j, nrhs, lane);
+  const int cw = warp / W, wi = warp % W;
+  for (int jb = blockIdx.x * CPB; jb < sn.nelim; jb += gridDim.x * CPB) {
+    const int j = jb + cw;
+    T acc[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
+    if (j < sn.nelim) bwd_l21_partial<T, NR>(sn, j, wi * 32 + lane, 32 * W, nrhs, acc);
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+      for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], off);
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < NR; ++q) part[warp][q] = acc[q];
+    }
+    __syncthreads();
+    if (wi == 0 && lane < nrhs && j < sn.nelim) {
+      T v = part[warp][lane];
+#pragma unroll
+      for (int w = 1; w < W; ++w) v += part[warp + w][lane];
+      sn.xloc[(int64_t)lane * sn.m + j] -= v;
+    }
+    __syncthreads();
+  }
 }
 
 // the last diagonal block of each node (one CTA per node)
 template <typename T, int NR>
 __global__ void __launch_bounds__(kSolveThreads)
     k_bwd_diag_last(const SolveNode<T>* sns, const int* nodes, int nrhs) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.x]];
+  const SolveNode<T> sn = sns[nodes[blockIdx.x]];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
   if (sn.nelim == 0) return;
   const int jl = ((sn.nelim - 1) / SB) * SB;
   extern __shared__ __align__(16) unsigned char solve_smem[];
@@ -426,18 +489,21 @@ __global__ void __launch_bounds__(kSolveThreads)
 template <typename T, int NR>
 __global__ void __launch_bounds__(kSolveThreads)
     k_bwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.y]];
+  const SolveNode<T> sn = sns[nodes[blockIdx.y]];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
   const int j0 = step * SB;
   if (j0 >= sn.nelim || j0 == 0) return;
   const int jb = min(SB, sn.nelim - j0);
   extern __shared__ __align__(16) unsigned char solve_smem[];
-  T* Lb = reinterpret_cast<T*>(solve_smem);  // also the partial-sum buffer
+  T* Lb = reinterpret_cast<T*>(solve_smem);
   T* yb = Lb + SB * LDB;
-  T* red = Lb;
+  T* red = yb + SB * NR;
+  const int jp = j0 - SB;  // first column of block st-1 (a full block)
+  if (blockIdx.x == 0) prefetch_diag_block(sn, jp, SB, Lb);  // overlaps the passes
   load_y<T, NR>(sn, j0, jb, nrhs, yb);
   __syncthreads();
   const int t = threadIdx.x % kPassRows, qq = threadIdx.x / kPassRows;
-  const int jp = j0 - SB;  // first column of block st-1 (a full block)
   auto pass = [&](int base, int lim) {
     const int j = base + t;
     T acc[NR];
@@ -464,7 +530,7 @@ __global__ void __launch_bounds__(kSolveThreads)
       pass(base, jp);
   }
   if (blockIdx.x != 0) return;
-  load_diag_block(sn, jp, SB, Lb);
+  cp_async_wait_all();
   __syncthreads();
   diag_block_solve<T, NR, false>(sn, jp, SB, nrhs, Lb);
 }
@@ -487,17 +553,19 @@ void with_nr(int q, F&& f) {
 // gather plus the first diagonal block of every node of the level
 template <typename T>
 void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const int* children,
-                       const double* x, int ldx, int nrhs, cudaStream_t s) {
+                       const int2* pairs, const double* x, int ldx, int nrhs, int max_m,
+                       cudaStream_t s) {
   if (nn <= 0) return;
+  const int rest = std::max(0, max_m - SB) * nrhs;
+  const int gx = rest > 0 ? 1 + std::min(cdiv(rest, kSolveThreads), 151) : 1;
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
-    k_fwd_gather_diag<T, NR><<<nn, kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
-        sn, nodes, children, x, ldx, nrhs);
+    launch_pdl(k_fwd_gather_diag<T, NR>, dim3(gx, nn), kSolveThreads, solve_smem_bytes<T, NR>(),
+               s, sn, nodes, children, pairs, x, ldx, nrhs);
     note_launches(1);
   });
 }
 
-// block steps: update below block st, then solve block st + 1
 // block steps: update below block st, then solve block st + 1
 template <typename T>
 void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_nelim,
@@ -513,8 +581,8 @@ void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_
       const int tail = rows - SB - 1;
       const int gx = tail > 0 ? 1 + std::min(cdiv(tail, kPassRows), 151) : 1;
       pmark(tm, kPhFwdUpdate, s);
-      k_fwd_step<T, NR><<<dim3(gx, nn), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
-          sn, nodes, st, nrhs);
+      launch_pdl(k_fwd_step<T, NR>, dim3(gx, nn), kSolveThreads, solve_smem_bytes<T, NR>(), s,
+                 sn, nodes, st, nrhs);
       note_launches(1);
     }
   });
@@ -525,7 +593,8 @@ void launch_fwd_scatter(const SolveNode<T>* sn, const int* nodes, int nn, double
                         int nrhs, int max_nelim, cudaStream_t s, bool scale_sqrt) {
   if (nn <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_nelim * nrhs, 256), 64));
-  { k_fwd_scatter<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, scale_sqrt); note_launches(1); }
+  launch_pdl(k_fwd_scatter<T>, dim3(gx, nn), 256, 0, s, sn, nodes, x, ldx, nrhs, scale_sqrt);
+  note_launches(1);
 }
 
 template <typename T>
@@ -535,17 +604,28 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
   if (nn <= 0) return;
   int gx = std::max(1, std::min(cdiv(max_m * nrhs, 256), 64));
   pmark(tm, kPhBwdGather, s);
-  { k_bwd_gather<T><<<dim3(gx, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, diag_mode, do_bwd); note_launches(1); }
+  launch_pdl(k_bwd_gather<T>, dim3(gx, nn), 256, 0, s, sn, nodes, x, ldx, nrhs, diag_mode,
+             do_bwd);
+  note_launches(1);
   if (do_bwd) {
     with_nr(nrhs, [&](auto nrc) {
       constexpr int NR = decltype(nrc)::value;
-      const int gw = std::max(1, std::min(cdiv(max_nelim, kSolveWarps), 152));
+      // warps per column from the level's largest front (rows below the
+      // pivots <= max_m), columns spread over up to 4 CTAs per SM
+      auto l21 = [&](auto wc) {
+        constexpr int W = decltype(wc)::value;
+        const int gw = std::max(1, std::min(cdiv(max_nelim, kSolveWarps / W), 4 * 152));
+        launch_pdl(k_bwd_l21<T, NR, W>, dim3(gw, nn), kSolveThreads, 0, s, sn, nodes, nrhs);
+      };
       pmark(tm, kPhBwdL21, s);
-      k_bwd_l21<T, NR><<<dim3(gw, nn), kSolveThreads, 0, s>>>(sn, nodes, nrhs);
+      if (max_m <= 128) l21(std::integral_constant<int, 1>());
+      else if (max_m <= 512) l21(std::integral_constant<int, 2>());
+      else if (max_m <= 1024) l21(std::integral_constant<int, 4>());
+      else l21(std::integral_constant<int, 8>());
       note_launches(1);
       pmark(tm, kPhBwdDiag, s);
-      k_bwd_diag_last<T, NR><<<nn, kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(sn, nodes,
-                                                                                   nrhs);
+      launch_pdl(k_bwd_diag_last<T, NR>, nn, kSolveThreads, solve_smem_bytes<T, NR>(), s, sn,
+                 nodes, nrhs);
       note_launches(1);
       const int steps = cdiv(max_nelim, SB);
       for (int st = steps - 1; st >= 1; --st) {
@@ -553,15 +633,16 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
         const int jp = (st - 1) * SB;
         const int gu = jp > 0 ? std::min(cdiv(jp, kPassRows), 151) : 0;
         pmark(tm, kPhBwdUpdate, s);
-        k_bwd_step<T, NR><<<dim3(1 + gu, nn), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
-            sn, nodes, st, nrhs);
+        launch_pdl(k_bwd_step<T, NR>, dim3(1 + gu, nn), kSolveThreads,
+                   solve_smem_bytes<T, NR>(), s, sn, nodes, st, nrhs);
         note_launches(1);
       }
     });
   }
   int gs = std::max(1, std::min(cdiv(max_nelim * nrhs, 256), 64));
   pmark(tm, kPhBwdScatter, s);
-  { k_fwd_scatter<T><<<dim3(gs, nn), 256, 0, s>>>(sn, nodes, x, ldx, nrhs, false); note_launches(1); }
+  launch_pdl(k_fwd_scatter<T>, dim3(gs, nn), 256, 0, s, sn, nodes, x, ldx, nrhs, false);
+  note_launches(1);
 }
 
 // the dynamic shared memory limit of every solve kernel instantiation; called
@@ -588,7 +669,7 @@ void solve_init() {
 #define INST(T)                                                                                \
   template void solve_init<T>();                                                               \
   template void launch_fwd_gather<T>(const SolveNode<T>*, const int*, int, const int*,         \
-                                     const double*, int, int, cudaStream_t);                   \
+                                     const int2*, const double*, int, int, int, cudaStream_t); \
   template void launch_fwd_steps<T>(const SolveNode<T>*, const int*, int, int, int, int,       \
                                     cudaStream_t, PhaseTimer*);                                \
   template void launch_fwd_scatter<T>(const SolveNode<T>*, const int*, int, double*, int, int, \

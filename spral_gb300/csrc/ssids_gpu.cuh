@@ -20,6 +20,37 @@ constexpr int kBlk = 32;         // APP inner block (ldlt_app.cxx:41 INNER_BLOCK
 constexpr int kApplyRows = 64;   // rows per apply/fixup CTA
 constexpr int kGemmTile = 64;    // SIMT GEMM tile
 
+// Programmatic dependent launch (PDL).  The serial chains of the path (the
+// APP block steps of a level, the block steps of the solves) are strings of
+// small dependent kernels; launched with launch_pdl, a kernel is scheduled
+// while its predecessor in the stream is still running and blocks in
+// pdl_wait() until that predecessor has completed and its memory is
+// visible, which hides the launch latency of every link (also inside a
+// captured graph, where the launches become programmatic edges).  Rules for
+// a kernel launched this way: before pdl_wait() it may read only what the
+// host wrote before the launch (front/solve descriptors, level lists) and
+// writes nothing; pdl_trigger() after the wait lets the next kernel of the
+// chain be scheduled.  Both are no-ops for an ordinary launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // Error codes written to the device status word (host maps to SSIDS flags).
 enum DevStatus : int {
   kDevOk = 0,
@@ -196,7 +227,7 @@ struct SolveNode {
   const int* rows;   // rlist of the node (0-based pivot positions), nrow entries
   const int* rdir;   // cm entries: parent position of each contribution row
   T* xloc;           // m x nrhs, in the factor precision
-  T* xorig;          // m x nrhs scratch (forward gather)
+  const int* gp;     // nrow + 1: children's contribution pairs of each parent position
   int m, n, ld, nelim, ncol, nrow, ndelay_in, cm;
   int sptr0;         // first own pivot
   int child_beg, child_end;  // into the child arrays
@@ -208,7 +239,8 @@ constexpr int kSolveRhs = 16;   // right-hand sides per pass
 
 template <typename T>
 void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const int* children,
-                       const double* x, int ldx, int nrhs, cudaStream_t s);
+                       const int2* pairs, const double* x, int ldx, int nrhs, int max_m,
+                       cudaStream_t s);
 template <typename T>
 void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_nelim,
                       int max_m, int nrhs, cudaStream_t s, PhaseTimer* tm);
