@@ -1225,9 +1225,8 @@ struct Numeric : NumericBase {
         const int* fr = S->d_fronts + f0;
         pmark(tm(), kPhFwdGather, s);
         launch_fwd_gather<T>(d_sn, fr, nf, d_children, S->d_pairs, xp, ldx, q, lvl_max_m[l], s);
-        launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, s, tm());
-        pmark(tm(), kPhFwdScatter, s);
-        launch_fwd_scatter<T>(d_sn, fr, nf, xp, ldx, q, lvl_max_nelim[l], s, job == 5);
+        launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, xp, ldx, job == 5, s,
+                            tm());
       }
     }
     if (diag || bwd) {

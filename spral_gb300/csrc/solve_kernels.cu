@@ -11,16 +11,16 @@
 // never update the same entry: each node gathers b for its own pivots plus
 // its children's local vectors (fixed order, no atomics), solves, and leaves
 // rows [nelim, m) of its local vector for its parent.  The triangular solves
-// are blocked by 64 rows.  A diagonal-block solve stages the block in shared
-// memory and gives each right-hand side its own warp (values in registers,
-// the pivot row broadcast by shuffles), so the serial chains of different
-// right-hand sides run on different SM sub-partitions.  One kernel per block
-// step applies the block's update (rows below it in the forward pass,
-// columns left of it in the backward pass) and, in the CTA that owns the
-// next block's rows or columns, solves that next diagonal block right after
-// updating it: one launch per block step instead of two.  Arithmetic is in
-// the factor precision T; the number of right-hand sides per pass NR is a
-// template parameter so that no work is spent on absent columns.
+// are blocked by 64 rows, one kernel per block step: every CTA of the step
+// stages the step's diagonal block in shared memory (cp.async) and solves it
+// itself, each right-hand side in its own warp (values in registers, the
+// pivot row broadcast by shuffles), then takes its share of the block's
+// update (rows below the block in the forward pass, columns left of it in
+// the backward pass).  No CTA waits for another and the solution is written
+// to the output vector by CTA 0 of the step, so a level needs no scatter
+// launch.  Arithmetic is in the factor precision T; the number of
+// right-hand sides per pass NR is a template parameter so that no work is
+// spent on absent columns.
 #include <mutex>
 #include <type_traits>
 
@@ -69,34 +69,15 @@ __device__ __forceinline__ T gather_value(const SolveNode<T>& sn, const SolveNod
   return v;
 }
 
-// stage the jb x jb diagonal block (strictly lower part) into shared memory;
-// every thread issues a batch of loads before the stores, so the
-// global-memory latency is paid once per batch, not once per element
 constexpr int kSolveThreads = 256;
 constexpr int kSolveWarps = kSolveThreads / 32;
 constexpr int LDB = SB + 1;  // leading dimension of a staged block Lb[c * LDB + r]
 constexpr int kDiagPer = SB * SB / kSolveThreads;  // entries of a staged block per thread
-template <typename T>
-__device__ __forceinline__ void fetch_diag_block(const SolveNode<T>& sn, int j0, int jb,
-                                                 T (&v)[kDiagPer]) {
-#pragma unroll
-  for (int k = 0; k < kDiagPer; ++k) {
-    const int e = threadIdx.x + k * kSolveThreads;
-    const int c = e / SB, r = e % SB;
-    v[k] = (r > c && r < jb && c < jb) ? sn.L[(int64_t)(j0 + c) * sn.ld + j0 + r] : T(0);
-  }
-}
-template <typename T>
-__device__ __forceinline__ void store_diag_block(const T (&v)[kDiagPer], T* Lb) {
-#pragma unroll
-  for (int k = 0; k < kDiagPer; ++k) {
-    const int e = threadIdx.x + k * kSolveThreads;
-    Lb[(e / SB) * LDB + e % SB] = v[k];
-  }
-}
-// the same staging with asynchronous copies (cp.async), so that a CTA can
-// start it, do other work, and wait for it with cp_async_wait_all() and a
-// barrier before the block is read
+
+// stage the jb x jb diagonal block (strictly lower part) into shared memory
+// with asynchronous copies (cp.async): a CTA starts it, does other work, and
+// waits for it with cp_async_wait_all() and a barrier before the block is
+// read; the entries outside the strictly lower part are zeroed
 template <typename T>
 __device__ __forceinline__ void prefetch_diag_block(const SolveNode<T>& sn, int j0, int jb, T* Lb) {
 #pragma unroll
@@ -120,228 +101,255 @@ __device__ __forceinline__ void prefetch_diag_block(const SolveNode<T>& sn, int 
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
-template <typename T>
-__device__ __forceinline__ void load_diag_block(const SolveNode<T>& sn, int j0, int jb, T* Lb) {
-  T v[kDiagPer];
-  fetch_diag_block(sn, j0, jb, v);
-  store_diag_block(v, Lb);
-}
 
-// Unit lower (FWD) or unit upper L^T (!FWD) triangular solve of rows
-// [j0, j0+jb) of xloc in place, with the block staged in Lb (Lb[c*LDB + r] =
-// L(j0+r, j0+c), zero on and above the diagonal).  Warp w solves the
-// right-hand sides w, w + 8, ...; lane l holds rows l, l + 32, ...  The
-// caller has synchronised the CTA after staging Lb; nothing follows.
-template <typename T, int NR, bool FWD>
-__device__ __forceinline__ void diag_block_solve(const SolveNode<T>& sn, int j0, int jb,
-                                                 int nrhs, const T* Lb) {
-  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
-  constexpr int G = SB / 32;  // rows per lane
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (warp >= nrhs) return;
-  T x[R][G];
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const int q = warp + r * kSolveWarps;
-#pragma unroll
-    for (int g = 0; g < G; ++g)
-      x[r][g] = (q < nrhs && lane + 32 * g < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + lane + 32 * g]
-                                                 : T(0);
-  }
-  if (FWD) {
+// Unit lower (FWD) or unit upper L^T (!FWD) triangular solve of a jb x jb
+// diagonal block staged in Lb (Lb[c*LDB + r] = L(j0+r, j0+c), zero on and
+// above the diagonal) for values held in registers: warp w holds the
+// right-hand sides w, w + 8, ...; lane l holds rows l and l + 32.  Pivot k
+// changes only the rows after it (FWD) or before it (!FWD), so once the
+// chain has passed a group of 32 rows that group is left out.
+static_assert(SB == 64, "the register layout below holds two row groups per lane");
+template <typename T, int R, bool FWD>
+__device__ __forceinline__ void solve_in_regs(int jb, const T* Lb, T (&x)[R][2]) {
+  const int lane = threadIdx.x & 31;
+  if (jb <= 32) {
+    // one row group: the second holds no rows of the block
     for (int k = 0; k < jb - 1; ++k) {
-      T l[G];
-#pragma unroll
-      for (int g = 0; g < G; ++g) l[g] = Lb[k * LDB + lane + 32 * g];
-      const int kg = k >> 5;
+      const T l0 = FWD ? Lb[k * LDB + lane] : Lb[lane * LDB + (jb - 1 - k)];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        T src = x[r][0];
+        const T v = __shfl_sync(0xffffffffu, x[r][0], FWD ? k : jb - 1 - k);
+        x[r][0] -= l0 * v;
+      }
+    }
+    return;
+  }
+  if (FWD) {
+    const int k1 = min(jb - 1, 32);
+    for (int k = 0; k < k1; ++k) {
+      const T l0 = Lb[k * LDB + lane], l1 = Lb[k * LDB + lane + 32];
 #pragma unroll
-        for (int g = 1; g < G; ++g) src = (kg == g) ? x[r][g] : src;
-        const T xk = __shfl_sync(0xffffffffu, src, k & 31);
+      for (int r = 0; r < R; ++r) {
+        const T xk = __shfl_sync(0xffffffffu, x[r][0], k);
+        x[r][0] -= l0 * xk;
+        x[r][1] -= l1 * xk;
+      }
+    }
+    for (int k = 32; k < jb - 1; ++k) {
+      const T l1 = Lb[k * LDB + lane + 32];
 #pragma unroll
-        for (int g = 0; g < G; ++g) x[r][g] -= l[g] * xk;
+      for (int r = 0; r < R; ++r) {
+        const T xk = __shfl_sync(0xffffffffu, x[r][1], k & 31);
+        x[r][1] -= l1 * xk;
       }
     }
   } else {
-    // (L^T y)_r = y_r + sum_{c > r} L(c, r) y_c ; process c from the bottom.
-    // L(c, r) = Lb[r*LDB + c] is zero unless c > r, so no lane masks are needed.
-    for (int c = jb - 1; c > 0; --c) {
-      T l[G];
-#pragma unroll
-      for (int g = 0; g < G; ++g) l[g] = Lb[(lane + 32 * g) * LDB + c];
-      const int cg = c >> 5;
+    // (L^T y)_r = y_r + sum_{c > r} L(c, r) y_c, c from the bottom
+    for (int c = jb - 1; c >= 32; --c) {
+      const T l0 = Lb[lane * LDB + c], l1 = Lb[(lane + 32) * LDB + c];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        T src = x[r][0];
-#pragma unroll
-        for (int g = 1; g < G; ++g) src = (cg == g) ? x[r][g] : src;
-        const T yc = __shfl_sync(0xffffffffu, src, c & 31);
-#pragma unroll
-        for (int g = 0; g < G; ++g) x[r][g] -= l[g] * yc;
+        const T yc = __shfl_sync(0xffffffffu, x[r][1], c & 31);
+        x[r][0] -= l0 * yc;
+        x[r][1] -= l1 * yc;
       }
     }
-  }
+    for (int c = min(jb - 1, 31); c > 0; --c) {
+      const T l0 = Lb[lane * LDB + c];
 #pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const int q = warp + r * kSolveWarps;
-#pragma unroll
-    for (int g = 0; g < G; ++g)
-      if (q < nrhs && lane + 32 * g < jb) sn.xloc[(int64_t)q * sn.m + j0 + lane + 32 * g] = x[r][g];
+      for (int r = 0; r < R; ++r) {
+        const T yc = __shfl_sync(0xffffffffu, x[r][0], c);
+        x[r][0] -= l0 * yc;
+      }
+    }
   }
 }
 
 // dynamic shared memory of the solve kernels: the staged block, the
 // block's solved values yb[r * NR + q], then the partial sums of the
-// update passes red[(qq * NR + q) * 64 + t] (qq = 0..3)
+// update passes red[(qq * NR + q) * PR + t] (256 NR values for any pass width)
 template <typename T, int NR>
 constexpr size_t solve_smem_bytes() {
   return sizeof(T) * ((size_t)SB * LDB + (size_t)SB * NR + (size_t)4 * NR * 64);
 }
 
+// Solve of diagonal block [j0, j0+jb) inside a block step, after the CTA
+// started staging it with prefetch_diag_block.  Every CTA of the step solves
+// the block itself: its solution feeds that CTA's share of the update, so
+// no CTA waits for another.  The solution goes to yb (yb[r*NR + q], zero
+// outside the block and for absent right-hand sides) and CTA 0 writes it to
+// the output vector x through perm (times sqrt(D^{-1}) for the posdef
+// forward solve, L_chol = L D^(1/2)).  The local vector keeps the unsolved
+// values (other CTAs of the step may still be reading them) unless to_xloc
+// is set by a CTA that is alone on its node.  Ends with a barrier.
+template <typename T, int NR, bool FWD>
+__device__ __forceinline__ void block_solve(const SolveNode<T>& sn, int j0, int jb, int nrhs,
+                                            const T* Lb, T* yb, double* x, int ldx,
+                                            bool scale_sqrt, bool to_xloc) {
+  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T xr[R][2];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int q = warp + r * kSolveWarps;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      const int row = lane + 32 * g;
+      xr[r][g] = (q < nrhs && row < jb) ? sn.xloc[(int64_t)q * sn.m + j0 + row] : T(0);
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  if (warp < nrhs) solve_in_regs<T, R, FWD>(jb, Lb, xr);
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int q = warp + r * kSolveWarps;
+    if (q >= NR) continue;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      const int row = lane + 32 * g;
+      const bool ok = q < nrhs && row < jb;
+      yb[row * NR + q] = ok ? xr[r][g] : T(0);
+      if (ok && to_xloc) sn.xloc[(int64_t)q * sn.m + j0 + row] = xr[r][g];
+      if (ok && blockIdx.x == 0) {
+        double v = (double)xr[r][g];
+        if (scale_sqrt) v *= sqrt(sn.D[2 * (j0 + row)]);
+        x[(int64_t)q * ldx + sn.perm[j0 + row]] = v;
+      }
+    }
+  }
+  __syncthreads();
+}
+
 // ---- forward ----
 // Gather every node of the level into its local vector (final positions:
-// xloc[i] = value of assembly position opos[i] for i < n), then solve the
-// first diagonal block.  CTA 0 of a node gathers rows [0, SB) and solves
-// block 0 from them; CTAs 1.. gather the rows after it (CTA 0 gathers all
-// rows when it is alone).
-template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveThreads)
-    k_fwd_gather_diag(const SolveNode<T>* sns, const int* nodes, const int* children,
-                      const int2* pairs, const double* x, int ldx, int nrhs) {
+// xloc[i] = value of assembly position opos[i] for i < n), all CTAs of a
+// node grid-striding over its entries.
+template <typename T>
+__global__ void k_fwd_gather(const SolveNode<T>* sns, const int* nodes, const int* children,
+                             const int2* pairs, const double* x, int ldx, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];  // written by the host before the launch
   pdl_wait();
   pdl_trigger();
   const int m = sn.m;
-  const int h = (gridDim.x == 1) ? m : min(m, SB);
-  int lo, len, e0, stride;
-  if (blockIdx.x == 0) {
-    lo = 0; len = h; e0 = threadIdx.x; stride = blockDim.x;
-  } else {
-    lo = h; len = m - h; e0 = (blockIdx.x - 1) * blockDim.x + threadIdx.x;
-    stride = (gridDim.x - 1) * blockDim.x;
-  }
-  for (int e = e0; e < len * nrhs; e += stride) {
-    const int i = lo + e % len, q = e / len;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < m * nrhs;
+       e += gridDim.x * blockDim.x) {
+    const int i = e % m, q = e / m;
     const int pos = (i < sn.n) ? sn.opos[i] : i;
     sn.xloc[(int64_t)q * m + i] = gather_value(sn, sns, children, pairs, x, ldx, q, pos);
   }
-  if (blockIdx.x != 0 || sn.nelim == 0) return;
-  extern __shared__ __align__(16) unsigned char solve_smem[];
-  T* Lb = reinterpret_cast<T*>(solve_smem);
-  __syncthreads();  // rows [0, h) written by this CTA
-  const int jb = min(SB, sn.nelim);
-  load_diag_block(sn, 0, jb, Lb);
-  __syncthreads();
-  diag_block_solve<T, NR, true>(sn, 0, jb, nrhs, Lb);
 }
 
-// Update kernels of the block steps: a CTA pass covers 64 rows (forward) or
-// columns (backward); thread (t, qq) = (threadIdx.x % 64, threadIdx.x / 64)
+// Update passes of the block steps: a CTA pass covers PR rows (forward) or
+// columns (backward); thread (t, qq) = (threadIdx.x % PR, threadIdx.x / PR)
 // forms the partial dot products of entry t over the block columns
-// [qq SB/4, (qq+1) SB/4) for every right-hand side, with those loads issued
-// together, and the four partial sums are added through shared memory.
-constexpr int kPassRows = 64;
-constexpr int kQuarter = SB / 4;
+// [qq CW, (qq+1) CW), CW = SB PR / 256, for every right-hand side, with
+// those loads issued together, and the 256 / PR partial sums are added
+// through shared memory in qq order.  FP32 passes cover 64 entries; FP64
+// passes 16, because a 64-entry pass is 32k FP64 FMAs for 8 right-hand
+// sides, which on GB300's FP64 pipe (about 1.7 per clock per SM) would
+// keep one SM busy for about 9 us.
+template <typename T>
+constexpr int pass_rows() { return sizeof(T) == 8 ? 16 : 64; }
 
-template <typename T, int NR>
+template <typename T, int NR, int CW>
 __device__ __forceinline__ void partial_dots(const T* p, int64_t stride, int cq, int jb,
                                              const T* yb, T (&acc)[NR]) {
-  T lv[kQuarter];
+  T lv[CW];
 #pragma unroll
-  for (int k = 0; k < kQuarter; ++k) lv[k] = (cq + k < jb) ? p[(int64_t)k * stride] : T(0);
+  for (int k = 0; k < CW; ++k) lv[k] = (cq + k < jb) ? p[(int64_t)k * stride] : T(0);
 #pragma unroll
   for (int q = 0; q < NR; ++q) acc[q] = T(0);
 #pragma unroll
-  for (int k = 0; k < kQuarter; ++k)
+  for (int k = 0; k < CW; ++k)
 #pragma unroll
     for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(cq + k) * NR + q];
 }
 
-// red[(qq * NR + q) * 64 + t] holds the partial sums; entry t of the pass
-// (global index base + t < lim) gets x -= the sum of its four partials
-template <typename T, int NR>
+// red[(qq * NR + q) * PR + t] holds the partial sums; entry t of the pass
+// (global index base + t < lim) gets x -= the sum of its partials
+template <typename T, int NR, int PR>
 __device__ __forceinline__ void apply_partials(const SolveNode<T>& sn, const T* red, int base,
                                                int lim, int nrhs) {
-  for (int e = threadIdx.x; e < kPassRows * NR; e += blockDim.x) {
-    const int t = e % kPassRows, q = e / kPassRows;
+  constexpr int QN = kSolveThreads / PR;
+  for (int e = threadIdx.x; e < PR * NR; e += blockDim.x) {
+    const int t = e % PR, q = e / PR;
     const int idx = base + t;
     if (q < nrhs && idx < lim) {
-      const T v = red[(0 * NR + q) * kPassRows + t] + red[(1 * NR + q) * kPassRows + t] +
-                  red[(2 * NR + q) * kPassRows + t] + red[(3 * NR + q) * kPassRows + t];
+      T v = red[q * PR + t];
+#pragma unroll
+      for (int qq = 1; qq < QN; ++qq) v += red[(qq * NR + q) * PR + t];
       sn.xloc[(int64_t)q * sn.m + idx] -= v;
     }
   }
 }
 
 // the solved rows [j0, j0+jb) of every right-hand side into yb[r*NR + q]
+// (zero outside the block), then a barrier
 template <typename T, int NR>
 __device__ __forceinline__ void load_y(const SolveNode<T>& sn, int j0, int jb, int nrhs, T* yb) {
   for (int e = threadIdx.x; e < SB * NR; e += blockDim.x) {
     const int r = e % SB, q = e / SB;
     yb[r * NR + q] = (r < jb && q < nrhs) ? sn.xloc[(int64_t)q * sn.m + j0 + r] : T(0);
   }
+  __syncthreads();
 }
 
-// Block step st: rows i >= i0 = j0 + jb get x_i -= sum_c L(i, j0+c) y_c with
-// y = the solved rows [j0, j0+jb).  CTA 0 updates the next block's rows
-// [i0, i0 + SB) and then solves that block; CTAs 1.. update the rows after
-// it (CTA 0 as well when it is alone).
-template <typename T, int NR>
+// Block step kernels, three shapes (MODE):
+//   kStepFused  solve block st in every CTA (block_solve), then update;
+//   kStepSolve  one CTA per node solves block st and stores it in xloc;
+//   kStepUpdate update only, y read back from xloc.
+// The FP32 path always runs fused steps.  The FP64 path runs fused steps on
+// levels with few nodes (their large fronts spread over many CTAs, where the
+// latency of a step matters) and solve + update pairs on levels with many
+// nodes, where the FP64 pipe is the limit and a repeated diagonal solve in
+// every CTA would add FP64 work.
+// All shapes use the same pass width, so a node's arithmetic (and result)
+// does not depend on the level it shares with other nodes.
+constexpr int kStepFused = 0, kStepSolve = 1, kStepUpdate = 2;
+
+// Forward block step st: solve block st, then the rows i >= j0 + jb take
+// x_i -= sum_c L(i, j0+c) y_c, PR rows per pass, the passes spread over the
+// CTAs.
+template <typename T, int NR, int MODE>
 __global__ void __launch_bounds__(kSolveThreads)
-    k_fwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
+    k_fwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs, double* x, int ldx,
+               bool scale_sqrt) {
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];  // written by the host before the launch
   pdl_wait();
   pdl_trigger();
   const int j0 = step * SB;
   if (j0 >= sn.nelim) return;
   const int jb = min(SB, sn.nelim - j0);
-  const int i0 = j0 + jb;
-  if (i0 >= sn.m) return;
   extern __shared__ __align__(16) unsigned char solve_smem[];
   T* Lb = reinterpret_cast<T*>(solve_smem);
   T* yb = Lb + SB * LDB;
   T* red = yb + SB * NR;
-  // CTA 0 starts staging the next diagonal block first: the copies overlap
-  // the update passes (L is read-only here)
-  const bool solve_next = blockIdx.x == 0 && i0 < sn.nelim;
-  const int jb1 = solve_next ? min(SB, sn.nelim - i0) : 0;
-  if (solve_next) prefetch_diag_block(sn, i0, jb1, Lb);
-  load_y<T, NR>(sn, j0, jb, nrhs, yb);
-  __syncthreads();
-  const int t = threadIdx.x % kPassRows, qq = threadIdx.x / kPassRows;
-  const int ih = min(sn.m, i0 + SB);  // end of the next block's rows
-  auto pass = [&](int base) {
+  if (MODE == kStepUpdate) {
+    load_y<T, NR>(sn, j0, jb, nrhs, yb);
+  } else {
+    prefetch_diag_block(sn, j0, jb, Lb);
+    block_solve<T, NR, true>(sn, j0, jb, nrhs, Lb, yb, x, ldx, scale_sqrt, MODE == kStepSolve);
+    if (MODE == kStepSolve) return;
+  }
+  constexpr int PR = pass_rows<T>(), CW = SB * PR / kSolveThreads;
+  const int t = threadIdx.x % PR, qq = threadIdx.x / PR;
+  for (int base = j0 + jb + blockIdx.x * PR; base < sn.m; base += gridDim.x * PR) {
     const int i = base + t;
     T acc[NR];
     if (i < sn.m) {
-      partial_dots<T, NR>(sn.L + (int64_t)(j0 + qq * kQuarter) * sn.ld + i, sn.ld, qq * kQuarter,
-                          jb, yb, acc);
+      partial_dots<T, NR, CW>(sn.L + (int64_t)(j0 + qq * CW) * sn.ld + i, sn.ld, qq * CW, jb, yb,
+                              acc);
     } else {
 #pragma unroll
       for (int q = 0; q < NR; ++q) acc[q] = T(0);
     }
 #pragma unroll
-    for (int q = 0; q < NR; ++q) red[(qq * NR + q) * kPassRows + t] = acc[q];
+    for (int q = 0; q < NR; ++q) red[(qq * NR + q) * PR + t] = acc[q];
     __syncthreads();
-    apply_partials<T, NR>(sn, red, base, sn.m, nrhs);
+    apply_partials<T, NR, PR>(sn, red, base, sn.m, nrhs);
     __syncthreads();
-  };
-  if (blockIdx.x == 0) {
-    for (int base = i0; base < ih; base += kPassRows) pass(base);
   }
-  if (gridDim.x == 1) {
-    for (int base = ih; base < sn.m; base += kPassRows) pass(base);
-  } else if (blockIdx.x > 0) {
-    for (int base = ih + (blockIdx.x - 1) * kPassRows; base < sn.m;
-         base += (gridDim.x - 1) * kPassRows)
-      pass(base);
-  }
-  if (!solve_next) return;
-  cp_async_wait_all();
-  __syncthreads();
-  diag_block_solve<T, NR, true>(sn, i0, jb1, nrhs, Lb);
 }
 
 template <typename T>
@@ -427,18 +435,29 @@ __device__ __forceinline__ void bwd_l21_partial(const SolveNode<T>& sn, int j, i
   }
 }
 
+// warps that share one column of the L21^T product, from the node's own
+// rows below its pivots (so a node is computed the same way whatever level
+// it shares)
+__device__ __forceinline__ int l21_warps(int rows_below) {
+  return rows_below <= 128 ? 1 : rows_below <= 512 ? 2 : rows_below <= 1024 ? 4 : 8;
+}
+inline int l21_warps_host(int rows_below) {
+  return rows_below <= 128 ? 1 : rows_below <= 512 ? 2 : rows_below <= 1024 ? 4 : 8;
+}
+
 // L21^T part of the backward solve for every eliminated column:
 // xloc[j] -= sum_{i in [nelim, m)} L(i, j) xloc[i].  W warps share a column
 // (rows strided over their 32 W lanes); their partial sums are added in
-// shared memory in warp order, so the result does not depend on the grid.
-template <typename T, int NR, int W>
+// shared memory in warp order.
+template <typename T, int NR>
 __global__ void __launch_bounds__(kSolveThreads)
     k_bwd_l21(const SolveNode<T>* sns, const int* nodes, int nrhs) {
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];  // written by the host before the launch
   pdl_wait();
   pdl_trigger();
   if (sn.m <= sn.nelim) return;
-  constexpr int CPB = kSolveWarps / W;  // columns per CTA round
+  const int W = l21_warps(sn.m - sn.nelim);
+  const int CPB = kSolveWarps / W;  // columns per CTA round
   __shared__ T part[kSolveWarps][NR];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int cw = warp / W, wi = warp % W;
@@ -458,7 +477,6 @@ __global__ void __launch_bounds__(kSolveThreads)
     __syncthreads();
     if (wi == 0 && lane < nrhs && j < sn.nelim) {
       T v = part[warp][lane];
-#pragma unroll
       for (int w = 1; w < W; ++w) v += part[warp + w][lane];
       sn.xloc[(int64_t)lane * sn.m + j] -= v;
     }
@@ -466,76 +484,55 @@ __global__ void __launch_bounds__(kSolveThreads)
   }
 }
 
-// the last diagonal block of each node (one CTA per node)
-template <typename T, int NR>
+// Backward block step st, from the last block down: solve block st, then the
+// columns j < j0 take x_j -= sum_c L(j0+c, j) y_c, PR columns per pass,
+// spread over the CTAs (shapes as for the forward steps).
+template <typename T, int NR, int MODE>
 __global__ void __launch_bounds__(kSolveThreads)
-    k_bwd_diag_last(const SolveNode<T>* sns, const int* nodes, int nrhs) {
-  const SolveNode<T> sn = sns[nodes[blockIdx.x]];  // written by the host before the launch
-  pdl_wait();
-  pdl_trigger();
-  if (sn.nelim == 0) return;
-  const int jl = ((sn.nelim - 1) / SB) * SB;
-  extern __shared__ __align__(16) unsigned char solve_smem[];
-  T* Lb = reinterpret_cast<T*>(solve_smem);
-  load_diag_block(sn, jl, sn.nelim - jl, Lb);
-  __syncthreads();
-  diag_block_solve<T, NR, false>(sn, jl, sn.nelim - jl, nrhs, Lb);
-}
-
-// Block step st (> 0) of the backward solve: the columns j left of block st
-// take x_j -= sum_c L(j0+c, j) y_c with y = its solved rows.  CTA 0 updates
-// the columns of block st-1 and then solves that block; CTAs 1.. update the
-// columns before it (CTA 0 as well when it is alone), 64 per pass.
-template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveThreads)
-    k_bwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs) {
+    k_bwd_step(const SolveNode<T>* sns, const int* nodes, int step, int nrhs, double* x,
+               int ldx) {
   const SolveNode<T> sn = sns[nodes[blockIdx.y]];  // written by the host before the launch
   pdl_wait();
   pdl_trigger();
   const int j0 = step * SB;
-  if (j0 >= sn.nelim || j0 == 0) return;
+  if (j0 >= sn.nelim) return;
   const int jb = min(SB, sn.nelim - j0);
   extern __shared__ __align__(16) unsigned char solve_smem[];
   T* Lb = reinterpret_cast<T*>(solve_smem);
   T* yb = Lb + SB * LDB;
   T* red = yb + SB * NR;
-  const int jp = j0 - SB;  // first column of block st-1 (a full block)
-  if (blockIdx.x == 0) prefetch_diag_block(sn, jp, SB, Lb);  // overlaps the passes
-  load_y<T, NR>(sn, j0, jb, nrhs, yb);
-  __syncthreads();
-  const int t = threadIdx.x % kPassRows, qq = threadIdx.x / kPassRows;
-  auto pass = [&](int base, int lim) {
+  if (MODE == kStepUpdate) {
+    load_y<T, NR>(sn, j0, jb, nrhs, yb);
+  } else {
+    prefetch_diag_block(sn, j0, jb, Lb);
+    block_solve<T, NR, false>(sn, j0, jb, nrhs, Lb, yb, x, ldx, false, MODE == kStepSolve);
+    if (MODE == kStepSolve) return;
+  }
+  constexpr int PR = pass_rows<T>(), CW = SB * PR / kSolveThreads;
+  const int t = threadIdx.x % PR, qq = threadIdx.x / PR;
+  for (int base = blockIdx.x * PR; base < j0; base += gridDim.x * PR) {
     const int j = base + t;
     T acc[NR];
-    if (j < lim) {
-      partial_dots<T, NR>(sn.L + (int64_t)j * sn.ld + j0 + qq * kQuarter, 1, qq * kQuarter, jb,
-                          yb, acc);
+    if (j < j0) {
+      partial_dots<T, NR, CW>(sn.L + (int64_t)j * sn.ld + j0 + qq * CW, 1, qq * CW, jb, yb, acc);
     } else {
 #pragma unroll
       for (int q = 0; q < NR; ++q) acc[q] = T(0);
     }
 #pragma unroll
-    for (int q = 0; q < NR; ++q) red[(qq * NR + q) * kPassRows + t] = acc[q];
+    for (int q = 0; q < NR; ++q) red[(qq * NR + q) * PR + t] = acc[q];
     __syncthreads();
-    apply_partials<T, NR>(sn, red, base, lim, nrhs);
+    apply_partials<T, NR, PR>(sn, red, base, j0, nrhs);
     __syncthreads();
-  };
-  if (blockIdx.x == 0) {
-    for (int base = jp; base < j0; base += kPassRows) pass(base, j0);
   }
-  if (gridDim.x == 1) {
-    for (int base = 0; base < jp; base += kPassRows) pass(base, jp);
-  } else if (blockIdx.x > 0) {
-    for (int base = (blockIdx.x - 1) * kPassRows; base < jp; base += (gridDim.x - 1) * kPassRows)
-      pass(base, jp);
-  }
-  if (blockIdx.x != 0) return;
-  cp_async_wait_all();
-  __syncthreads();
-  diag_block_solve<T, NR, false>(sn, jp, SB, nrhs, Lb);
 }
 
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
+
+// CTAs per node of a block step: every CTA repeats the step's diagonal
+// solve, so a level with many nodes gets about one wave of CTAs in total
+// (one per node once the level has 152 nodes or more)
+inline int cta_cap(int nn) { return std::max(1, 152 / std::max(nn, 1)); }
 
 // call f(std::integral_constant<int, NR>) with the smallest NR in
 // {1, 2, 4, 8, 16} that holds q right-hand sides
@@ -550,51 +547,51 @@ void with_nr(int q, F&& f) {
 
 }  // namespace
 
-// gather plus the first diagonal block of every node of the level
 template <typename T>
 void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const int* children,
                        const int2* pairs, const double* x, int ldx, int nrhs, int max_m,
                        cudaStream_t s) {
   if (nn <= 0) return;
-  const int rest = std::max(0, max_m - SB) * nrhs;
-  const int gx = rest > 0 ? 1 + std::min(cdiv(rest, kSolveThreads), 151) : 1;
-  with_nr(nrhs, [&](auto nrc) {
-    constexpr int NR = decltype(nrc)::value;
-    launch_pdl(k_fwd_gather_diag<T, NR>, dim3(gx, nn), kSolveThreads, solve_smem_bytes<T, NR>(),
-               s, sn, nodes, children, pairs, x, ldx, nrhs);
-    note_launches(1);
-  });
+  const int gx = std::max(1, std::min(cdiv(max_m * nrhs, 256), 152));
+  launch_pdl(k_fwd_gather<T>, dim3(gx, nn), 256, 0, s, sn, nodes, children, pairs, x, ldx, nrhs);
+  note_launches(1);
 }
 
-// block steps: update below block st, then solve block st + 1
+// levels with at least this many nodes run FP64 block steps as solve +
+// update pairs (see kStepSolve)
+constexpr int kSplitNodes = 8;
+
+// block steps: solve block st, update the rows below it; the solution goes
+// straight to x (pivot order)
 template <typename T>
 void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_nelim,
-                      int max_m, int nrhs, cudaStream_t s, PhaseTimer* tm) {
+                      int max_m, int nrhs, double* x, int ldx, bool scale_sqrt, cudaStream_t s,
+                      PhaseTimer* tm) {
   if (nn <= 0) return;
   const int steps = cdiv(max_nelim, SB);
+  const bool split = sizeof(T) == 8 && nn >= kSplitNodes;
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
+    constexpr size_t sm = solve_smem_bytes<T, NR>();
     for (int st = 0; st < steps; ++st) {
-      const int rows = max_m - st * SB;  // upper bound; the kernel derives the exact range
-      if (rows <= 0) break;
-      // CTA 0 takes the next block's rows, the others the rows after it
-      const int tail = rows - SB - 1;
-      const int gx = tail > 0 ? 1 + std::min(cdiv(tail, kPassRows), 151) : 1;
+      const int below = std::max(max_m - (st + 1) * SB, 1);  // upper bound on rows to update
       pmark(tm, kPhFwdUpdate, s);
-      launch_pdl(k_fwd_step<T, NR>, dim3(gx, nn), kSolveThreads, solve_smem_bytes<T, NR>(), s,
-                 sn, nodes, st, nrhs);
-      note_launches(1);
+      if (split) {
+        launch_pdl(k_fwd_step<T, NR, kStepSolve>, dim3(1, nn), kSolveThreads, sm, s, sn, nodes, st,
+                   nrhs, x, ldx, scale_sqrt);
+        const int gx = std::max(1, std::min(cdiv(below, pass_rows<T>()), 152));
+        launch_pdl(k_fwd_step<T, NR, kStepUpdate>, dim3(gx, nn), kSolveThreads, sm, s, sn, nodes,
+                   st, nrhs, x, ldx, scale_sqrt);
+        note_launches(2);
+      } else {
+        const int cap = sizeof(T) == 8 ? cta_cap(nn) : 152;
+        const int gx = std::max(1, std::min(cdiv(below, pass_rows<T>()), cap));
+        launch_pdl(k_fwd_step<T, NR, kStepFused>, dim3(gx, nn), kSolveThreads, sm, s, sn, nodes,
+                   st, nrhs, x, ldx, scale_sqrt);
+        note_launches(1);
+      }
     }
   });
-}
-
-template <typename T>
-void launch_fwd_scatter(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx,
-                        int nrhs, int max_nelim, cudaStream_t s, bool scale_sqrt) {
-  if (nn <= 0) return;
-  int gx = std::max(1, std::min(cdiv(max_nelim * nrhs, 256), 64));
-  launch_pdl(k_fwd_scatter<T>, dim3(gx, nn), 256, 0, s, sn, nodes, x, ldx, nrhs, scale_sqrt);
-  note_launches(1);
 }
 
 template <typename T>
@@ -602,47 +599,53 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
                 int max_m, int max_nelim, int diag_mode, bool do_bwd, cudaStream_t s,
                 PhaseTimer* tm) {
   if (nn <= 0) return;
-  int gx = std::max(1, std::min(cdiv(max_m * nrhs, 256), 64));
+  int gx = std::max(1, std::min(cdiv(max_m * nrhs, 256), 152));
   pmark(tm, kPhBwdGather, s);
   launch_pdl(k_bwd_gather<T>, dim3(gx, nn), 256, 0, s, sn, nodes, x, ldx, nrhs, diag_mode,
              do_bwd);
   note_launches(1);
-  if (do_bwd) {
-    with_nr(nrhs, [&](auto nrc) {
-      constexpr int NR = decltype(nrc)::value;
-      // warps per column from the level's largest front (rows below the
-      // pivots <= max_m), columns spread over up to 4 CTAs per SM
-      auto l21 = [&](auto wc) {
-        constexpr int W = decltype(wc)::value;
-        const int gw = std::max(1, std::min(cdiv(max_nelim, kSolveWarps / W), 4 * 152));
-        launch_pdl(k_bwd_l21<T, NR, W>, dim3(gw, nn), kSolveThreads, 0, s, sn, nodes, nrhs);
-      };
-      pmark(tm, kPhBwdL21, s);
-      if (max_m <= 128) l21(std::integral_constant<int, 1>());
-      else if (max_m <= 512) l21(std::integral_constant<int, 2>());
-      else if (max_m <= 1024) l21(std::integral_constant<int, 4>());
-      else l21(std::integral_constant<int, 8>());
-      note_launches(1);
-      pmark(tm, kPhBwdDiag, s);
-      launch_pdl(k_bwd_diag_last<T, NR>, nn, kSolveThreads, solve_smem_bytes<T, NR>(), s, sn,
-                 nodes, nrhs);
-      note_launches(1);
-      const int steps = cdiv(max_nelim, SB);
-      for (int st = steps - 1; st >= 1; --st) {
-        // CTA 0 takes block st-1, the others the columns before it
-        const int jp = (st - 1) * SB;
-        const int gu = jp > 0 ? std::min(cdiv(jp, kPassRows), 151) : 0;
-        pmark(tm, kPhBwdUpdate, s);
-        launch_pdl(k_bwd_step<T, NR>, dim3(1 + gu, nn), kSolveThreads,
-                   solve_smem_bytes<T, NR>(), s, sn, nodes, st, nrhs);
+  if (!do_bwd) {
+    // diagonal solve only: D^{-1} x was applied by the gather
+    int gs = std::max(1, std::min(cdiv(max_nelim * nrhs, 256), 64));
+    pmark(tm, kPhBwdScatter, s);
+    launch_pdl(k_fwd_scatter<T>, dim3(gs, nn), 256, 0, s, sn, nodes, x, ldx, nrhs, false);
+    note_launches(1);
+    return;
+  }
+  with_nr(nrhs, [&](auto nrc) {
+    constexpr int NR = decltype(nrc)::value;
+    // enough CTAs for the level's widest node at the most warps per column
+    // any of its nodes can use (rows below the pivots <= max_m), up to 4 per SM
+    const int gw = std::max(
+        1, std::min(cdiv(max_nelim, kSolveWarps / l21_warps_host(max_m)), 4 * 152));
+    pmark(tm, kPhBwdL21, s);
+    launch_pdl(k_bwd_l21<T, NR>, dim3(gw, nn), kSolveThreads, 0, s, sn, nodes, nrhs);
+    note_launches(1);
+    const int steps = cdiv(max_nelim, SB);
+    const bool split = sizeof(T) == 8 && nn >= kSplitNodes;
+    constexpr size_t sm = solve_smem_bytes<T, NR>();
+    for (int st = steps - 1; st >= 0; --st) {
+      const int left = std::max(st * SB, 1);  // columns to update
+      pmark(tm, kPhBwdUpdate, s);
+      if (split) {
+        launch_pdl(k_bwd_step<T, NR, kStepSolve>, dim3(1, nn), kSolveThreads, sm, s, sn, nodes, st,
+                   nrhs, x, ldx);
+        note_launches(1);
+        if (st > 0) {
+          const int gx = std::max(1, std::min(cdiv(left, pass_rows<T>()), 152));
+          launch_pdl(k_bwd_step<T, NR, kStepUpdate>, dim3(gx, nn), kSolveThreads, sm, s, sn,
+                     nodes, st, nrhs, x, ldx);
+          note_launches(1);
+        }
+      } else {
+        const int cap = sizeof(T) == 8 ? cta_cap(nn) : 152;
+        const int gx = std::max(1, std::min(cdiv(left, pass_rows<T>()), cap));
+        launch_pdl(k_bwd_step<T, NR, kStepFused>, dim3(gx, nn), kSolveThreads, sm, s, sn, nodes,
+                   st, nrhs, x, ldx);
         note_launches(1);
       }
-    });
-  }
-  int gs = std::max(1, std::min(cdiv(max_nelim * nrhs, 256), 64));
-  pmark(tm, kPhBwdScatter, s);
-  launch_pdl(k_fwd_scatter<T>, dim3(gs, nn), 256, 0, s, sn, nodes, x, ldx, nrhs, false);
-  note_launches(1);
+    }
+  });
 }
 
 // the dynamic shared memory limit of every solve kernel instantiation; called
@@ -657,10 +660,12 @@ void solve_init() {
     for (int q : {1, 2, 4, 8, 16}) {
       with_nr(q, [&](auto nrc) {
         constexpr int NR = decltype(nrc)::value;
-        set(k_fwd_gather_diag<T, NR>, solve_smem_bytes<T, NR>());
-        set(k_fwd_step<T, NR>, solve_smem_bytes<T, NR>());
-        set(k_bwd_diag_last<T, NR>, solve_smem_bytes<T, NR>());
-        set(k_bwd_step<T, NR>, solve_smem_bytes<T, NR>());
+        set(k_fwd_step<T, NR, kStepFused>, solve_smem_bytes<T, NR>());
+        set(k_fwd_step<T, NR, kStepSolve>, solve_smem_bytes<T, NR>());
+        set(k_fwd_step<T, NR, kStepUpdate>, solve_smem_bytes<T, NR>());
+        set(k_bwd_step<T, NR, kStepFused>, solve_smem_bytes<T, NR>());
+        set(k_bwd_step<T, NR, kStepSolve>, solve_smem_bytes<T, NR>());
+        set(k_bwd_step<T, NR, kStepUpdate>, solve_smem_bytes<T, NR>());
       });
     }
   });
@@ -671,9 +676,7 @@ void solve_init() {
   template void launch_fwd_gather<T>(const SolveNode<T>*, const int*, int, const int*,         \
                                      const int2*, const double*, int, int, int, cudaStream_t); \
   template void launch_fwd_steps<T>(const SolveNode<T>*, const int*, int, int, int, int,       \
-                                    cudaStream_t, PhaseTimer*);                                \
-  template void launch_fwd_scatter<T>(const SolveNode<T>*, const int*, int, double*, int, int, \
-                                      int, cudaStream_t, bool);                                \
+                                    double*, int, bool, cudaStream_t, PhaseTimer*);            \
   template void launch_bwd<T>(const SolveNode<T>*, const int*, int, double*, int, int, int, int, \
                               int, bool, cudaStream_t, PhaseTimer*);
 INST(double)

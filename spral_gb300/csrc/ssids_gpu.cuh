@@ -243,13 +243,11 @@ void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const i
                        cudaStream_t s);
 template <typename T>
 void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_nelim,
-                      int max_m, int nrhs, cudaStream_t s, PhaseTimer* tm);
+                      int max_m, int nrhs, double* x, int ldx, bool scale_sqrt, cudaStream_t s,
+                      PhaseTimer* tm);
 // sets the solve kernels' dynamic shared memory limits (once per process)
 template <typename T>
 void solve_init();
-template <typename T>
-void launch_fwd_scatter(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx,
-                        int nrhs, int max_nelim, cudaStream_t s, bool scale_sqrt);
 template <typename T>
 // diag_mode: 0 none, 1 D^{-1}, 2 sqrt(D^{-1}) (posdef backward solve)
 void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int ldx, int nrhs,
