@@ -668,9 +668,18 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
   const int nrows = fd.m - r0;
   if (nrows <= 0) return;
   // X = A21 L11^{-T} in the factor precision T; D^{-1} application and the
-  // a-posteriori test in FP64
-  __shared__ T l11[kBlk][kBlk + 1];  // l11[j][k] = L(j,k), row-major for broadcast
+  // a-posteriori test in FP64.  Few warps run this kernel on an SM, so its
+  // code is kept short: L11 is staged transposed (l11t[k][j] = L(j, k),
+  // rows 16-byte aligned) for vector loads in the unrolled solve, and the
+  // per-column epilogue is a rolled loop over X staged in shared memory,
+  // driven by the pivot kind of each column.
+  constexpr int VW = 16 / sizeof(T);  // elements per 16-byte vector
+  constexpr int LT = kBlk + VW;       // padded row of l11t
+  __shared__ __align__(16) T l11t[kBlk][LT];
+  __shared__ T xs[kBlk][kApplyRows];
   __shared__ double dd[2 * kBlk + 2];
+  __shared__ float ddf[kBlk];  // FP32 copies of the 1x1 D^{-1} entries
+  __shared__ int kind[kBlk];   // 0 1x1, 1 first of a 2x2, 2 second of a 2x2, 3 zero pivot
   __shared__ int lp[kBlk];
   {
     // all loads first (one latency), then the shared-memory stores
@@ -685,15 +694,24 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
       const int i = threadIdx.x + k * kApplyRows;
-      l11[i % kBlk][i / kBlk] = (T)v[k];
+      l11t[i / kBlk][i % kBlk] = (T)v[k];
     }
   }
   for (int i = threadIdx.x; i < 2 * kBlk + 2; i += blockDim.x)
     dd[i] = (i < 2 * bs) ? fd.step[kBlk * kBlk + i] : 0.0;
-  __shared__ float ddf[kBlk];  // FP32 copies of the 1x1 D^{-1} entries
-  for (int i = threadIdx.x; i < kBlk; i += blockDim.x)
-    ddf[i] = (i < bs) ? (float)fd.step[kBlk * kBlk + 2 * i] : 0.f;
-  if (threadIdx.x < kBlk) lp[threadIdx.x] = (threadIdx.x < bs) ? fd.lperm[threadIdx.x] : 0;
+  __syncthreads();
+  if (threadIdx.x < kBlk) {
+    const int j = threadIdx.x;
+    ddf[j] = (j < bs) ? (float)dd[2 * j] : 0.f;
+    lp[j] = (j < bs) ? fd.lperm[j] : 0;
+    int kd = 0;
+    if (j < bs) {
+      if (isinf(dd[2 * j])) kd = 2;
+      else if (j + 1 < bs && isinf(dd[2 * j + 2])) kd = 1;
+      else if (dd[2 * j] == 0.0) kd = 3;
+    }
+    kind[j] = kd;
+  }
   __syncthreads();
   const double thresh = 1.0 / u;
   // FP32 guard band of the threshold test (FP32 factors)
@@ -705,8 +723,9 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
     return b > tkey && b <= 0x7ff0000000000000LL;
   };
   int myfail = bs;
+  const int t = threadIdx.x;
   for (int tile = blockIdx.x; tile * kApplyRows < nrows; tile += napply) {
-    const int rr = tile * kApplyRows + threadIdx.x;
+    const int rr = tile * kApplyRows + t;
     const bool valid = rr < nrows;
     const int r = r0 + rr;
     T x[kBlk];
@@ -714,59 +733,70 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
     for (int j = 0; j < kBlk; ++j)
       x[j] = (valid && j < bs) ? fd.L[(int64_t)(p + lp[j]) * fd.ld + r] : T(0);
     // right-looking: after x[k] is final, the updates of x[k+1..] are
-    // independent FMAs (instruction-level parallelism for the FP64 pipe)
+    // independent FMAs; L(j, k) for j > k comes in 16-byte vectors (the
+    // zero entries on and above the diagonal change nothing)
 #pragma unroll
     for (int k = 0; k < kBlk - 1; ++k) {
       if (k + 1 < bs) {
         const T xk = x[k];
 #pragma unroll
-        for (int j = k + 1; j < kBlk; ++j) x[j] -= xk * l11[j][k];
+        for (int j0 = ((k + 1) / VW) * VW; j0 < kBlk; j0 += VW) {
+          T lv[VW];
+          if constexpr (sizeof(T) == 4) {
+            const float4 q = *reinterpret_cast<const float4*>(&l11t[k][j0]);
+            lv[0] = q.x; lv[1] = q.y; lv[2] = q.z; lv[3] = q.w;
+          } else {
+            const double2 q = *reinterpret_cast<const double2*>(&l11t[k][j0]);
+            lv[0] = q.x; lv[1] = q.y;
+          }
+#pragma unroll
+          for (int v = 0; v < VW; ++v)
+            if (j0 + v > k) x[j0 + v] -= xk * lv[v];
+        }
       }
     }
+#pragma unroll
+    for (int j = 0; j < kBlk; ++j) xs[j][t] = x[j];  // column t is this thread's
     if (valid) {
       T* W = fd.W + rr;
-#pragma unroll
-      for (int j = 0; j < kBlk; ++j) {
-        if (j < bs) {
-          const double dj = dd[2 * j];
-          if (!isinf(dj)) {  // (second half of a 2x2 is handled with the first)
-            if (j + 1 < bs && isinf(dd[2 * j + 2])) {
-              const double d21 = dd[2 * j + 1], d22 = dd[2 * j + 3];
-              const double x1 = (double)x[j], x2 = (double)x[j + 1 < kBlk ? j + 1 : kBlk - 1];
-              const double l1 = dj * x1 + d21 * x2, l2 = d21 * x1 + d22 * x2;
-              fd.L[(int64_t)(p + j) * fd.ld + r] = (T)l1;
-              fd.L[(int64_t)(p + j + 1) * fd.ld + r] = (T)l2;
-              W[(int64_t)j * fd.ld] = (T)x1;
-              W[(int64_t)(j + 1) * fd.ld] = (T)x2;
-              int cand = over(l1) ? j : (over(l2) ? j + 1 : bs);
-              myfail = min(myfail, cand);
-            } else if (sizeof(T) == 4 && dj != 0.0) {
-              // FP32 factors: L in FP32; the a-posteriori test |l| <= 1/u is
-              // decided in FP32 outside a relative guard band of 1e-6 around
-              // the threshold and in FP64 inside it, so every decision is
-              // the FP64 one
-              const float lf = (float)x[j] * ddf[j];
-              fd.L[(int64_t)(p + j) * fd.ld + r] = (T)lf;
-              W[(int64_t)j * fd.ld] = x[j];
-              const float al = fabsf(lf);
-              if (!(al <= thr_lo)) {  // above the band, in it, or NaN
-                if (al > thr_hi || over((double)x[j] * dj)) myfail = min(myfail, j);
-              }
-            } else {
-              double l, w;
-              if (dj == 0.0) {
-                const double v = (double)x[j];
-                l = (fabs(v) < small) ? 0.0 : dinf() * v;
-                w = 0.0;
-              } else {
-                l = (double)x[j] * dj;
-                w = (double)x[j];
-              }
-              fd.L[(int64_t)(p + j) * fd.ld + r] = (T)l;
-              W[(int64_t)j * fd.ld] = (T)w;
-              if (over(l)) myfail = min(myfail, j);
-            }
+#pragma unroll 1
+      for (int j = 0; j < bs; ++j) {
+        const int kd = kind[j];
+        if (kd == 2) continue;  // second half of a 2x2: handled with the first
+        const T xj = xs[j][t];
+        if (kd == 1) {
+          const double dj = dd[2 * j], d21 = dd[2 * j + 1], d22 = dd[2 * j + 3];
+          const double x1 = (double)xj, x2 = (double)xs[j + 1][t];
+          const double l1 = dj * x1 + d21 * x2, l2 = d21 * x1 + d22 * x2;
+          fd.L[(int64_t)(p + j) * fd.ld + r] = (T)l1;
+          fd.L[(int64_t)(p + j + 1) * fd.ld + r] = (T)l2;
+          W[(int64_t)j * fd.ld] = (T)x1;
+          W[(int64_t)(j + 1) * fd.ld] = (T)x2;
+          const int cand = over(l1) ? j : (over(l2) ? j + 1 : bs);
+          myfail = min(myfail, cand);
+        } else if (kd == 3) {
+          const double v = (double)xj;
+          const double l = (fabs(v) < small) ? 0.0 : dinf() * v;
+          fd.L[(int64_t)(p + j) * fd.ld + r] = (T)l;
+          W[(int64_t)j * fd.ld] = T(0);
+          if (over(l)) myfail = min(myfail, j);
+        } else if (sizeof(T) == 4) {
+          // FP32 factors: L in FP32; the a-posteriori test |l| <= 1/u is
+          // decided in FP32 outside a relative guard band of 1e-6 around
+          // the threshold and in FP64 inside it, so every decision is the
+          // FP64 one
+          const float lf = (float)xj * ddf[j];
+          fd.L[(int64_t)(p + j) * fd.ld + r] = (T)lf;
+          W[(int64_t)j * fd.ld] = xj;
+          const float al = fabsf(lf);
+          if (!(al <= thr_lo)) {  // above the band, in it, or NaN
+            if (al > thr_hi || over((double)xj * dd[2 * j])) myfail = min(myfail, j);
           }
+        } else {
+          const double l = (double)xj * dd[2 * j];
+          fd.L[(int64_t)(p + j) * fd.ld + r] = (T)l;
+          W[(int64_t)j * fd.ld] = xj;
+          if (over(l)) myfail = min(myfail, j);
         }
       }
     }
