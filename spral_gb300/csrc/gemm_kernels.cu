@@ -53,12 +53,77 @@ __global__ void __launch_bounds__(256) k_syrk(FrontDesc<T>* fds, const FrontStat
   const FrontState st = sts[f];
   SyrkJob<T> j;
   if (!make_job<T, MODE>(fd, st, j)) return;
-  __shared__ T As[TK][TM + 4];
-  __shared__ T Bs[TK][TM + 4];
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const int tc = (j.N + TM - 1) / TM, tr = (j.M + TM - 1) / TM;
   const int total = tc * tr - tc * (tc - 1) / 2;
+  if (MODE == 0) {
+    // Panel update, K <= kBlk: a tile stages all of its A and B columns and
+    // reads its C entries in one batch of loads (one memory round trip per
+    // tile instead of one per k-chunk plus one for C).
+    __shared__ T Ap[kBlk][TM + 4];
+    __shared__ T Bp[kBlk][TM + 4];
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+      int tj = 0, rem = t;
+      while (rem >= tr - tj) { rem -= tr - tj; ++tj; }
+      const int ti = tj + rem;
+      const int row0 = ti * TM, col0 = tj * TM;
+      T cv[4][4];
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        const int c = col0 + ty + 16 * y;
+#pragma unroll
+        for (int x = 0; x < 4; ++x) {
+          const int r = row0 + tx + 16 * x;
+          cv[x][y] = (r < j.M && c < j.N && r >= c) ? j.C[(int64_t)c * j.ldc + r] : T(0);
+        }
+      }
+      T av[(TM * kBlk) / 256], bv[(TM * kBlk) / 256];
+#pragma unroll
+      for (int q = 0; q < (TM * kBlk) / 256; ++q) {
+        const int idx = tid + 256 * q;
+        const int rr = idx % TM, kk = idx / TM;
+        const int r = row0 + rr, c = col0 + rr;
+        av[q] = (r < j.M && kk < j.K) ? j.A[(int64_t)kk * j.lda + r] : T(0);
+        bv[q] = (c < j.N && kk < j.K) ? j.B[(int64_t)kk * j.ldb + c] : T(0);
+      }
+#pragma unroll
+      for (int q = 0; q < (TM * kBlk) / 256; ++q) {
+        const int idx = tid + 256 * q;
+        Ap[idx / TM][idx % TM] = av[q];
+        Bp[idx / TM][idx % TM] = bv[q];
+      }
+      __syncthreads();
+      T acc[4][4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+#pragma unroll 8
+      for (int kk = 0; kk < kBlk; ++kk) {
+        T a[4], b[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) { a[q] = Ap[kk][tx + 16 * q]; b[q] = Bp[kk][ty + 16 * q]; }
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int y = 0; y < 4; ++y) acc[x][y] += a[x] * b[y];
+      }
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        const int c = col0 + ty + 16 * y;
+#pragma unroll
+        for (int x = 0; x < 4; ++x) {
+          const int r = row0 + tx + 16 * x;
+          if (r < j.M && c < j.N && r >= c) j.C[(int64_t)c * j.ldc + r] = cv[x][y] - acc[x][y];
+        }
+      }
+      __syncthreads();  // Ap/Bp are rewritten by the next tile
+    }
+    return;
+  }
+  __shared__ T As[TK][TM + 4];
+  __shared__ T Bs[TK][TM + 4];
   for (int t = blockIdx.x; t < total; t += gridDim.x) {
     int tj = 0, rem = t;
     while (rem >= tr - tj) { rem -= tr - tj; ++tj; }
