@@ -162,6 +162,16 @@ int spral_ssids_gpu_debug_front(const void* numeric, int node, int* info, double
 int spral_ssids_gpu_solve_refined_dev(void* numeric, int nrhs, const double* b_dev, double* x_dev,
                                       int ld, int* iters, double* bwd_err);
 
+/* No counterpart in the reference.  Number of FP64 refactorisations taken by
+ * the refined solves of an FP32-factor handle (precision = 1) since it was
+ * created: when the FP32 factors cannot bring a refined solve to the
+ * backward-error target (refinement stalls or runs out of steps), the same
+ * values are factored in FP64 on the GPU, once per factorisation, and the
+ * solve is finished with those factors.  stats (may be NULL) receives the
+ * handle's current statistics, which are the FP64 factorisation's after a
+ * fallback.  Returns -1 for a NULL handle. */
+int spral_ssids_gpu_fp64_fallbacks(const void* numeric, struct spral_ssids_thread_stats* stats);
+
 /* Benchmark support (no reference counterpart): kernels launched by this
  * library so far; per-factor timing of the contribution-block update with
  * CUDA events on the library's stream (out[0] ms, out[1] algorithmic flops,

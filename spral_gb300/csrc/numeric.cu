@@ -424,6 +424,8 @@ struct NumericBase {
   virtual int node_inertia(int* out) = 0;
   virtual cudaStream_t get_stream() const = 0;
   DevBuf<double> hsolve;  // device copy of host right-hand sides (host-buffer solves)
+  // FP64 refactorisations taken by the FP32-factor path's refined solves
+  int fallbacks = 0;
 };
 
 template <typename T>
@@ -887,6 +889,12 @@ struct Numeric : NumericBase {
 
   const double* cur_aval = nullptr;  // device values of the last factor
   double last_bwd_err = 0.0;
+  // FP32-factor path: an FP64 factorisation of the same values, formed on the
+  // GPU when the FP32 factors cannot reach the refinement target (see
+  // fp64_fallback); stale after every factorisation of this handle
+  std::unique_ptr<NumericBase> fb;
+  bool fb_stale = true, fb_ok = false;
+  bool last_scaled = false;
   std::vector<cudaEvent_t> pev;
 
   explicit Numeric(Symbolic* s) : S(s) {
@@ -939,6 +947,8 @@ struct Numeric : NumericBase {
              cudaStream_t user_stream) override {
     if (user_stream) CK(cudaStreamSynchronize(user_stream));
     solve_ready = false;
+    fb_stale = true;
+    last_scaled = scaling != nullptr;
     if (use_graphs && !profile && last_zero_delay) {
       stats = spral_ssids_thread_stats{};
       const int r = factor_graph(aval, on_device, scaling);
@@ -1310,6 +1320,13 @@ struct Numeric : NumericBase {
                          cudaMemcpyDeviceToDevice, s));
       solve_dev(0, q, xbuf.p, n, nullptr);
       int it = refine_dev(q, xbuf.p, bbuf.p, n);
+      if (NumericBase* f64 = fp64_fallback()) {
+        int it64 = 0;
+        double bwd64 = 0;
+        f64->solve_refined_dev(q, bbuf.p, xbuf.p, n, &it64, &bwd64);
+        it += it64;
+        last_bwd_err = bwd64;
+      }
       itmax = std::max(itmax, it);
       for (int r = 0; r < q; ++r)
         CK(cudaMemcpyAsync(xh + (size_t)(r0 + r) * ldx, xbuf.p + (size_t)r * n,
@@ -1332,12 +1349,52 @@ struct Numeric : NumericBase {
       CK(cudaMemcpy2DAsync(xp, ld * sizeof(double), bp, ld * sizeof(double),
                            S->n * sizeof(double), q, cudaMemcpyDeviceToDevice, stream));
       solve_dev(0, q, xp, ld, nullptr);
-      itmax = std::max(itmax, refine_dev(q, xp, bp, ld));
+      int it = refine_dev(q, xp, bp, ld);
+      if (NumericBase* f64 = fp64_fallback()) {
+        int it64 = 0;
+        double bwd64 = 0;
+        f64->solve_refined_dev(q, bp, xp, ld, &it64, &bwd64);
+        it += it64;
+        last_bwd_err = bwd64;
+      }
+      itmax = std::max(itmax, it);
       worst = std::max(worst, last_bwd_err);
     }
     if (iters) *iters = itmax;
     if (bwd) *bwd = worst;
     return 0;
+  }
+
+  // FP64 fallback of the FP32-factor path.  When FP32 factors cannot bring
+  // the backward error of a refined solve to the target (the refinement
+  // stalled or ran out of steps: the matrix is too ill-conditioned for FP32
+  // factors), the same values are factored again in FP64 on the GPU, once
+  // per factorisation of this handle, and the right-hand sides are solved
+  // and refined with those factors.  The FP64 factorisation's statistics
+  // (inertia, delays) replace the FP32 ones.  Returns the FP64 handle to
+  // solve with, or nullptr when no fallback is needed (FP64 handles, or the
+  // target was met).
+  NumericBase* fp64_fallback() {
+    if (!std::is_same<T, float>::value) return nullptr;
+    if (!(last_bwd_err > S->gopts.refine_tol)) return nullptr;
+    if (!fb) {
+      fb.reset(new Numeric<double>(S));
+      fb->posdef = posdef;
+      fb->precision = 0;
+    }
+    if (fb_stale) {
+      std::vector<double> sc;
+      if (last_scaled) {
+        sc.resize(S->n);
+        CK(cudaMemcpy(sc.data(), scale_buf.p, S->n * sizeof(double), cudaMemcpyDeviceToHost));
+      }
+      const int r = fb->factor(cur_aval, true, last_scaled ? sc.data() : nullptr, nullptr);
+      fb_stale = false;
+      fb_ok = r >= 0;
+      ++fallbacks;
+      stats = fb->stats;  // its flag tells a failed FP64 factorisation
+    }
+    return fb_ok ? fb.get() : nullptr;
   }
 
   // refinement of x (device, n x q, ld) against b; returns steps taken
@@ -1359,8 +1416,11 @@ struct Numeric : NumericBase {
       if (profile) ptimer.flush();
       double worst = 0;
       for (int r = 0; r < q; ++r) worst = std::max(worst, h[r]);
+      // stop at the target, after max_refine steps, or when a step did not
+      // halve the backward error (the factors' precision cannot reach it)
+      const bool stalled = it > 0 && !(worst < 0.5 * last_bwd_err);
       last_bwd_err = worst;
-      if (!(worst > S->gopts.refine_tol) || it >= maxit) break;
+      if (!(worst > S->gopts.refine_tol) || it >= maxit || stalled) break;
       solve_dev(0, q, rbuf.p, ld, nullptr);
       pmark(tm(), kPhAxpy, s);
       launch_axpy(n, q, ld, x, rbuf.p, s);
@@ -1744,6 +1804,13 @@ int spral_ssids_gpu_solve_refined_dev(void* numeric, int nrhs, const double* b_d
   } catch (ssids300::CudaFail const& e) {
     return map_cuda_error(e, nullptr);
   }
+}
+
+int spral_ssids_gpu_fp64_fallbacks(const void* numeric, struct spral_ssids_thread_stats* stats) {
+  const auto* N = static_cast<const NumericBase*>(numeric);
+  if (!N) return -1;
+  if (stats) *stats = N->stats;
+  return N->fallbacks;
 }
 
 int spral_ssids_gpu_recip_probe(const double* x_dev, double* y_dev, int n) {

@@ -277,14 +277,28 @@ class Fkeep:
         invp = self.akeep.invp
         xp = np.asfortranarray(B[invp, :])
         it = ctypes.c_int(0)
+        nfb = self.fallbacks
         fl = L.spral_ssids_gpu_solve_refined(self.num, xp.shape[1], _P(xp), xp.shape[0],
                                              ctypes.byref(it))
         if fl != 0:
             raise RuntimeError(f"spral_gb300 refined solve failed, flag {fl}")
         self.last_refine_iters = it.value
+        if self.fallbacks != nfb:
+            # FP32 factors could not reach the target: the solve was finished
+            # with an FP64 factorisation, whose statistics now apply
+            st = ThreadStats()
+            L.spral_ssids_gpu_fp64_fallbacks(self.num, ctypes.byref(st))
+            self.stats = {k: getattr(st, k) for k, _ in ThreadStats._fields_}
+            self.inform = self._inform(st)
         x = np.empty_like(B)
         x[invp, :] = xp
         return x[:, 0] if one else x
+
+    @property
+    def fallbacks(self):
+        """FP64 refactorisations the refined solves of an FP32-factor handle
+        have taken (always 0 for FP64 factors)."""
+        return _native.lib().spral_ssids_gpu_fp64_fallbacks(self.num, None)
 
     def enquire_posdef(self):
         """Diagonal entries of the Cholesky factor of a posdef factorisation,

@@ -193,6 +193,41 @@ def test_gpu_mixed_precision_refined(k):
     assert _rel(x, xd.solve(b)) < SOL_TOL
 
 
+def test_gpu_mixed_falls_back_to_fp64_when_refinement_cannot_converge():
+    """A shifted 2D Laplacian with one eigenvalue 3e-9 away from zero
+    (condition number ~3e9): FP32 factors cannot drive the refinement to the
+    target (kappa * eps32 >> 1), so the refined solve refactors in FP64 on the
+    GPU once and finishes there; the result meets the FP64 bar and the
+    statistics (inertia) are the FP64 factorisation's."""
+    nx, ny = 30, 34
+    lam = (2 - 2 * np.cos(np.pi * 3 / (nx + 1))) + (2 - 2 * np.cos(np.pi * 5 / (ny + 1)))
+    shift = 3e-9 - lam
+    p, r, v = M.laplacian_2d(nx, ny, shift)
+    ak = ssids.analyse(p, r, M.nd_order_grid(nx, ny))
+    opts = ssids.Options(precision=ssids.PRECISION_MIXED, max_refine=20, refine_tol=1e-14)
+    fk, _ = ssids.factor(ak, v, opts)
+    assert fk.fallbacks == 0
+    b = np.random.default_rng(3).uniform(-1, 1, (nx * ny, 2))
+    x = fk.solve_refined(b)
+    assert fk.fallbacks == 1
+    assert M.scaled_bwd_error(p, r, v, x, b).max() <= 1e-14
+    neg, _, _ = M.laplacian_eig_count_2d(nx, ny, shift)
+    assert fk.inform.num_neg == neg
+    xd, _ = ssids.factor(ak, v, ssids.Options(max_refine=10, refine_tol=1e-14))
+    assert _rel(x, xd.solve_refined(b)) < 1e-5  # kappa ~3e9: agreement limited by conditioning
+    # a second solve reuses the FP64 factors; a refactorisation makes them stale
+    x2 = fk.solve_refined(b)
+    assert fk.fallbacks == 1 and np.array_equal(x, x2)
+    fk.refactor(v)
+    fk.solve_refined(b)
+    assert fk.fallbacks == 2
+    # a well-conditioned matrix never falls back
+    p2, r2, v2 = M.laplacian_2d(nx, ny, -0.5)
+    fk2, _ = ssids.factor(ssids.analyse(p2, r2, M.nd_order_grid(nx, ny)), v2, opts)
+    fk2.solve_refined(b)
+    assert fk2.fallbacks == 0
+
+
 def test_gpu_recip_within_one_ulp():
     """The Newton reciprocal on the pivot-decision path agrees with IEEE
     division to one unit in the last place (and exactly at special values)."""
