@@ -172,6 +172,16 @@ int spral_ssids_gpu_solve_refined_dev(void* numeric, int nrhs, const double* b_d
  * fallback.  Returns -1 for a NULL handle. */
 int spral_ssids_gpu_fp64_fallbacks(const void* numeric, struct spral_ssids_thread_stats* stats);
 
+/* No counterpart in the reference.  Row groups for the refined solves of
+ * every numeric handle of this symbolic subtree: row_group[i] (pivot order,
+ * n entries) in [0, ngroups) names the group of row i, e.g. the matrix of a
+ * batch of independent matrices stacked into one subtree.  The scaled
+ * backward error that stops the refinement is then the largest over the
+ * groups, each with its own norms (||A_g||, ||x_g||, ||b_g||), so every
+ * group meets the target.  ngroups <= 0 or row_group == NULL removes the
+ * groups.  Returns 0, -1 (NULL handle), -2 (a group out of range) or -51. */
+int spral_ssids_gpu_set_row_groups(void* symbolic, int ngroups, const int* row_group);
+
 /* Benchmark support (no reference counterpart): kernels launched by this
  * library so far; per-factor timing of the contribution-block update with
  * CUDA events on the library's stream (out[0] ms, out[1] algorithmic flops,

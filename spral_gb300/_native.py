@@ -89,6 +89,7 @@ def _declare(L):
     f("spral_ssids_gpu_debug_front", I, P, I, P, P, P, P)
     f("spral_ssids_gpu_solve_refined_dev", I, P, I, P, P, I, P, P)
     f("spral_ssids_gpu_fp64_fallbacks", I, P, P)
+    f("spral_ssids_gpu_set_row_groups", I, P, I, P)
     f("spral_ssids_gpu_solve_refined", I, P, I, P, I, P)
     f("spral_ssids_gpu_launch_count", ctypes.c_longlong)
     f("spral_ssids_gpu_node_inertia", I, P, P)

@@ -13,6 +13,8 @@ the launch.
 The reference has no batched interface; a caller of the reference factors
 the matrices one ssids_analyse/ssids_factor/ssids_solve sequence at a time.
 """
+import ctypes
+
 import numpy as np
 
 from . import ssids
@@ -48,6 +50,8 @@ class BatchAkeep:
         mat_of_var = np.repeat(np.arange(self.nmat), sizes)
         first = self.akeep.invp[self.akeep.sptr[:-1] - 1]  # first pivot of each node
         self.mat_of_node = mat_of_var[first]
+        # matrix of each pivot position: the refinement's row groups
+        self.mat_of_pivot = np.ascontiguousarray(mat_of_var[self.akeep.invp], dtype=np.int32)
 
     @property
     def n(self):
@@ -78,6 +82,13 @@ class BatchFkeep:
     def __init__(self, bakeep, vals, options=None):
         self.bak = bakeep
         self.fk = ssids.Fkeep(bakeep.akeep, bakeep.stack_values(vals), options)
+        # refinement judges the backward error matrix by matrix (each with its
+        # own norms), so every matrix of the batch meets the target
+        from . import _native
+        fl = _native.lib().spral_ssids_gpu_set_row_groups(
+            self.fk.sym, bakeep.nmat, bakeep.mat_of_pivot.ctypes.data_as(ctypes.c_void_p))
+        if fl != 0:
+            raise RuntimeError(f"spral_gb300: row groups rejected, flag {fl}")
 
     @property
     def inform(self):
@@ -104,7 +115,8 @@ class BatchFkeep:
 
     def solve_refined(self, bs):
         """Solve with FP64 iterative refinement of the whole batch against its
-        FP64 values (options max_refine / refine_tol)."""
+        FP64 values (options max_refine / refine_tol), until every matrix's
+        scaled backward error meets the target."""
         B, two = self.bak.stack_rhs(bs)
         return self.bak.split(self.fk.solve_refined(B), two)
 

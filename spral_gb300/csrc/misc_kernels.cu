@@ -37,10 +37,15 @@ __device__ __forceinline__ void atomic_max_pos(double* a, double v) {
 // (||x||, ||b||, ||r||) at 1 + 3q (maxima, order-independent).
 constexpr int kResG = 4;
 constexpr int kResQC = 4;
+// With row groups (row_group != nullptr: the group of each row, e.g. the
+// matrix of a batch it belongs to) the maxima are kept per group, at
+// work[g * kResStride ...], so the backward error can be judged per group.
+constexpr int kResStride = 1 + 3 * kSolveRhs;
 __global__ void __launch_bounds__(256) k_resid_norms(const int64_t* aptr, const int* acol,
                                                      const int64_t* asrc, const double* aval,
                                                      int n, const double* x, const double* b,
-                                                     double* r, int nrhs, int ld, double* work) {
+                                                     double* r, int nrhs, int ld, double* work,
+                                                     const int* row_group) {
   constexpr int G = kResG, QC = kResQC, RPW = 32 / G;
   const int lane = threadIdx.x & 31, sub = lane & (G - 1);
   const int q0 = blockIdx.y * QC;
@@ -73,6 +78,58 @@ __global__ void __launch_bounds__(256) k_resid_norms(const int64_t* aptr, const 
 #pragma unroll
       for (int q = 0; q < QC; ++q) s[q] += __shfl_xor_sync(0xffffffffu, s[q], off);
     }
+    if (row_group) {
+      // grouped maxima: a warp whose rows share one group reduces them and
+      // makes one atomic per value; otherwise each row makes its own
+      double vx[QC], vb[QC], vr[QC];
+#pragma unroll
+      for (int q = 0; q < QC; ++q) vx[q] = vb[q] = vr[q] = 0.0;
+      const int g = ok ? row_group[i] : -1;
+      if (ok && sub == 0) {
+#pragma unroll
+        for (int q = 0; q < QC; ++q) {
+          if (q < nq) {
+            const int64_t e = (int64_t)(q0 + q) * ld + i;
+            const double bi = b[e], ri = bi - s[q];
+            r[e] = ri;
+            vx[q] = fabs(x[e]);
+            vb[q] = fabs(bi);
+            vr[q] = fabs(ri);
+          }
+        }
+      }
+      const double va = ok ? ra : 0.0;
+      const int g0 = __shfl_sync(0xffffffffu, g, 0);
+      if (__all_sync(0xffffffffu, g == g0 || g < 0)) {
+        double wa = va;
+        for (int off = 16; off > 0; off >>= 1) wa = fmax(wa, __shfl_xor_sync(0xffffffffu, wa, off));
+#pragma unroll
+        for (int q = 0; q < QC; ++q)
+          for (int off = 16; off > 0; off >>= 1) {
+            vx[q] = fmax(vx[q], __shfl_xor_sync(0xffffffffu, vx[q], off));
+            vb[q] = fmax(vb[q], __shfl_xor_sync(0xffffffffu, vb[q], off));
+            vr[q] = fmax(vr[q], __shfl_xor_sync(0xffffffffu, vr[q], off));
+          }
+        if (lane == 0 && g0 >= 0) {
+          double* w = work + (int64_t)g0 * kResStride;
+          if (blockIdx.y == 0) atomic_max_pos(&w[0], wa);
+          for (int q = 0; q < nq; ++q) {
+            atomic_max_pos(&w[1 + 3 * (q0 + q)], vx[q]);
+            atomic_max_pos(&w[2 + 3 * (q0 + q)], vb[q]);
+            atomic_max_pos(&w[3 + 3 * (q0 + q)], vr[q]);
+          }
+        }
+      } else if (ok && sub == 0) {
+        double* w = work + (int64_t)g * kResStride;
+        if (blockIdx.y == 0) atomic_max_pos(&w[0], va);
+        for (int q = 0; q < nq; ++q) {
+          atomic_max_pos(&w[1 + 3 * (q0 + q)], vx[q]);
+          atomic_max_pos(&w[2 + 3 * (q0 + q)], vb[q]);
+          atomic_max_pos(&w[3 + 3 * (q0 + q)], vr[q]);
+        }
+      }
+      continue;
+    }
     if (ok && sub == 0) {
       an = fmax(an, ra);
 #pragma unroll
@@ -88,6 +145,7 @@ __global__ void __launch_bounds__(256) k_resid_norms(const int64_t* aptr, const 
       }
     }
   }
+  if (row_group) return;
   // warp maxima -> block maxima in shared memory -> one atomic per value
   // and block (same-address atomics from every warp would serialise)
   constexpr int NV = 1 + 3 * QC;
@@ -122,11 +180,25 @@ __global__ void __launch_bounds__(256) k_resid_norms(const int64_t* aptr, const 
   }
 }
 
-__global__ void k_bwd_finish(const double* work, int nrhs, double* out) {
-  int q = threadIdx.x;
-  if (q < nrhs) {
-    double den = work[0] * work[1 + 3 * q] + work[1 + 3 * q + 1];
-    out[q] = (den > 0) ? work[1 + 3 * q + 2] / den : 0.0;
+// out[q] = the largest scaled backward error of right-hand side q over the
+// groups (one group when rows are not grouped)
+__global__ void k_bwd_finish(const double* work, int nrhs, int ngroups, double* out) {
+  __shared__ double red[256];
+  for (int q = 0; q < nrhs; ++q) {
+    double m = 0.0;
+    for (int g = threadIdx.x; g < ngroups; g += blockDim.x) {
+      const double* w = work + (int64_t)g * kResStride;
+      const double den = w[0] * w[1 + 3 * q] + w[2 + 3 * q];
+      m = fmax(m, den > 0 ? w[3 + 3 * q] / den : 0.0);
+    }
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+      if ((int)threadIdx.x < h) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + h]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[q] = red[0];
+    __syncthreads();
   }
 }
 
@@ -150,19 +222,22 @@ void launch_zero_fronts(FrontDesc<T>* fd, const int* fronts, int nf, int max_ele
 template void launch_zero_fronts<double>(FrontDesc<double>*, const int*, int, int, cudaStream_t);
 template void launch_zero_fronts<float>(FrontDesc<float>*, const int*, int, int, cudaStream_t);
 
-// r = b - A x and the scaled backward error of each right-hand side (work
-// must hold nrhs + 1 + 3*kSolveRhs doubles; the result per rhs is written
-// to work[0 .. nrhs)).
+// r = b - A x and the scaled backward error of each right-hand side, the
+// largest over the row groups when row_group is given (work must hold
+// nrhs + max(ngroups, 1) * (1 + 3*kSolveRhs) doubles; the result per rhs is
+// written to work[0 .. nrhs)).
 void launch_resid_bwd_err(const int64_t* aptr, const int* acol, const int64_t* asrc,
                           const double* aval, int n, const double* x, const double* b, double* r,
-                          int nrhs, int ld, double* work, cudaStream_t s) {
+                          int nrhs, int ld, double* work, const int* row_group, int ngroups,
+                          cudaStream_t s) {
   double* acc = work + nrhs;
-  cudaMemsetAsync(acc, 0, (1 + 3 * kSolveRhs) * sizeof(double), s);
+  const int ng = row_group ? std::max(ngroups, 1) : 1;
+  cudaMemsetAsync(acc, 0, (size_t)ng * kResStride * sizeof(double), s);
   const int rows_per_block = 256 / 32 * (32 / kResG);
   const int bx = std::max(1, std::min((n + rows_per_block - 1) / rows_per_block, 4 * 152));
   const int by = (nrhs + kResQC - 1) / kResQC;
-  { k_resid_norms<<<dim3(bx, by), 256, 0, s>>>(aptr, acol, asrc, aval, n, x, b, r, nrhs, ld, acc); note_launches(1); }
-  { k_bwd_finish<<<1, 32, 0, s>>>(acc, nrhs, work); note_launches(1); }
+  { k_resid_norms<<<dim3(bx, by), 256, 0, s>>>(aptr, acol, asrc, aval, n, x, b, r, nrhs, ld, acc, row_group); note_launches(1); }
+  { k_bwd_finish<<<1, 256, 0, s>>>(acc, nrhs, ng, work); note_launches(1); }
 }
 
 void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s) {

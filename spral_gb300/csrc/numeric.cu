@@ -188,6 +188,9 @@ struct Symbolic {
   int4* d_cols = nullptr;
   int2* d_pairs = nullptr;
   int* d_gp = nullptr;        // per front, nrow + 1 offsets into d_pairs by parent position
+  // optional row groups of the refinement's backward error (pivot order)
+  int ngroups = 0;
+  int* d_row_group = nullptr;
   std::vector<int64_t> gp_off;
   // FP64 matrix in pivot order (full CSR, both triangles) for refinement
   int64_t* d_aptr = nullptr;
@@ -198,7 +201,7 @@ struct Symbolic {
   ~Symbolic() {
     cudaFree(d_nptr); cudaFree(d_nlist); cudaFree(d_sptr); cudaFree(d_rlist); cudaFree(d_rptr);
     cudaFree(d_rdir); cudaFree(d_rdir_ptr); cudaFree(d_fronts); cudaFree(d_cols);
-    cudaFree(d_pairs); cudaFree(d_gp); cudaFree(d_aptr); cudaFree(d_acol); cudaFree(d_asrc);
+    cudaFree(d_pairs); cudaFree(d_gp); cudaFree(d_row_group); cudaFree(d_aptr); cudaFree(d_acol); cudaFree(d_asrc);
   }
 };
 
@@ -433,7 +436,8 @@ void launch_zero_fronts(FrontDesc<T>* fd, const int* fronts, int nf, int max_ele
                         cudaStream_t s);
 void launch_resid_bwd_err(const int64_t* aptr, const int* acol, const int64_t* asrc,
                           const double* aval, int n, const double* x, const double* b, double* r,
-                          int nrhs, int ld, double* work, cudaStream_t s);
+                          int nrhs, int ld, double* work, const int* row_group, int ngroups,
+                          cudaStream_t s);
 void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
@@ -1312,7 +1316,7 @@ struct Numeric : NumericBase {
       bbuf.ensure((size_t)n * q + 1);
       xbuf.ensure((size_t)n * q + 1);
       rbuf.ensure((size_t)n * q + 1);
-      nbuf.ensure(q + 1 + 3 * kSolveRhs + 8);
+      nbuf.ensure(q + (size_t)std::max(S->ngroups, 1) * (1 + 3 * kSolveRhs) + 8);
       for (int r = 0; r < q; ++r)
         CK(cudaMemcpyAsync(bbuf.p + (size_t)r * n, xh + (size_t)(r0 + r) * ldx,
                            n * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -1402,14 +1406,14 @@ struct Numeric : NumericBase {
     const int n = S->n;
     cudaStream_t s = stream;
     rbuf.ensure((size_t)ld * q + 1);
-    nbuf.ensure(q + 1 + 3 * kSolveRhs + 8);
+    nbuf.ensure(q + (size_t)std::max(S->ngroups, 1) * (1 + 3 * kSolveRhs) + 8);
     std::vector<double> h(q);
     int it = 0;
     const int maxit = S->gopts.max_refine;
     for (;; ++it) {
       pmark(tm(), kPhResid, s);
       launch_resid_bwd_err(S->d_aptr, S->d_acol, S->d_asrc, cur_aval, n, x, b, rbuf.p, q, ld,
-                           nbuf.p, s);
+                           nbuf.p, S->d_row_group, S->ngroups, s);
       pmark(tm(), kPhHost, s);
       CK(cudaMemcpyAsync(h.data(), nbuf.p, q * sizeof(double), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
@@ -1803,6 +1807,32 @@ int spral_ssids_gpu_solve_refined_dev(void* numeric, int nrhs, const double* b_d
     return N->solve_refined_dev(nrhs, b_dev, x_dev, ld, iters, bwd_err);
   } catch (ssids300::CudaFail const& e) {
     return map_cuda_error(e, nullptr);
+  }
+}
+
+int spral_ssids_gpu_set_row_groups(void* symbolic, int ngroups, const int* row_group) {
+  Symbolic* S = static_cast<Symbolic*>(symbolic);
+  if (!S) return -1;
+  try {
+    CK(cudaSetDevice(S->device));
+    if (ngroups <= 0 || !row_group) {
+      cudaFree(S->d_row_group);
+      S->d_row_group = nullptr;
+      S->ngroups = 0;
+      return 0;
+    }
+    for (int i = 0; i < S->n; ++i)
+      if (row_group[i] < 0 || row_group[i] >= ngroups) return -2;
+    int* d = nullptr;
+    CK(cudaMalloc(&d, std::max(S->n, 1) * sizeof(int)));
+    const cudaError_t e = cudaMemcpy(d, row_group, S->n * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { cudaFree(d); CK(e); }
+    cudaFree(S->d_row_group);
+    S->d_row_group = d;
+    S->ngroups = ngroups;
+    return 0;
+  } catch (CudaFail const& e) {
+    return -51;
   }
 }
 

@@ -70,3 +70,23 @@ def test_gpu_batch_refactor_replays_graph():
         for i, (p, r, _) in enumerate(mats):
             assert M.scaled_bwd_error(p, r, vals[i], xs[i], bs[i]).max() <= 1e-14
     bf.free()
+
+
+@pytest.mark.parametrize("precision", [ssids.PRECISION_FP64, ssids.PRECISION_MIXED])
+def test_gpu_batch_refined_meets_target_per_matrix(precision):
+    """Refinement of a batch stops only when every matrix's own scaled
+    backward error (its own norms) meets the target, not the stacked
+    system's."""
+    sides, shifts, mats, orders = _batch(32, 8, 64, 6)
+    bak = batch.BatchAkeep([(p, r) for p, r, _ in mats], orders)
+    opts = ssids.Options(precision=precision, max_refine=20, refine_tol=1e-14)
+    bf = batch.BatchFkeep(bak, [v for _, _, v in mats], opts)
+    rng = np.random.default_rng(11)
+    # right-hand sides of very different sizes per matrix, so that the
+    # stacked system's norms say little about the small ones
+    bs = [rng.uniform(-1, 1, len(p) - 1) * 10.0 ** rng.integers(-6, 3) for p, _, _ in mats]
+    xs = bf.solve_refined(bs)
+    worst = max(float(M.scaled_bwd_error(p, r, v, xs[i], bs[i]).max())
+                for i, (p, r, v) in enumerate(mats))
+    assert worst <= 1e-14
+    bf.free()
