@@ -1297,6 +1297,9 @@ __global__ void k_stats(const FrontDesc<T>* fds, const FrontState* sts, const in
 }  // namespace
 
 // ---------------- syrk kernel entry points (gemm_kernels.cu) --------------
+// tile edge of the panel update for factor type T (gemm_kernels.cu)
+template <typename T>
+int panel_tile();
 template <typename T>
 void launch_syrk_panel(FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
                        int max_tiles, cudaStream_t s);
@@ -1335,7 +1338,8 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
   // tile estimate assumes no failed columns so far; after failures the
   // trailing region is wider and the kernel's grid-stride loop covers it, so
   // the launch is never skipped
-  int tr = std::max(0, cdiv(max_trail_rows, kGemmTile)), tc = std::max(0, cdiv(max_trail_cols, kGemmTile));
+  const int tp = panel_tile<T>();
+  int tr = std::max(0, cdiv(max_trail_rows, tp)), tc = std::max(0, cdiv(max_trail_cols, tp));
   int tiles = tc * tr - tc * (tc - 1) / 2;
   pmark(tm, kPhPanel, s);
   launch_syrk_panel<T>(fd, st, fronts, nf, std::max(tiles, 1), s);
