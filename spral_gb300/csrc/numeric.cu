@@ -586,6 +586,15 @@ struct Numeric : NumericBase {
   bool use_tc = false;
   int tc_chunk = kTcChunk;
   int tc_min_cm = 192;  // smallest contribution block formed on the tensor cores
+  // fewest fully-summed columns (the update's depth K) of a front formed on
+  // the tensor cores.  Shallower updates stream their contribution block
+  // through HBM with little arithmetic per byte, so the tensor cores gain
+  // little there, while their 3xTF32 products (about 22-bit operands) cost
+  // the FP64 refinement a step: on the 48^3 and 32^3 Laplacians the
+  // factor + refined solve was fastest with K >= 256 (48^3: 26.7 ms against
+  // 28.9 ms with every front of >= 192 contribution rows on the tensor cores
+  // and 28.1 ms with none).
+  int tc_min_k = 256;
   TcBuffers tcbuf;
   DevBuf<char> tc_scratch;
   int* d_tc_status = nullptr;
@@ -714,7 +723,7 @@ struct Numeric : NumericBase {
         d.LD = ws_LD.p + oL; oL += (size_t)d.cm * d.n;
         d.step = ws_step.p + (size_t)(f - f0) * (kBlk * kBlk + 2 * kBlk + 64);
         d.lperm = ws_lperm.p + (size_t)(f - f0) * kBlk;
-        d.tc = (use_tc && d.cm >= tc_min_cm) ? 1 : 0;
+        d.tc = (use_tc && d.cm >= tc_min_cm && d.n >= tc_min_k) ? 1 : 0;
       }
     }
     fg_hfd = hfd;
@@ -928,6 +937,8 @@ struct Numeric : NumericBase {
       const char* mc = getenv("SPRAL_GB300_TC_MIN_CM");
       if (mc) tc_min_cm = std::max(1, atoi(mc));
       else if (use_tc) tc_min_cm = autotune_tc_min_cm();
+      const char* mk = getenv("SPRAL_GB300_TC_MIN_K");
+      if (mk) tc_min_k = std::max(0, atoi(mk));
     }
     contrib.ensure(std::max<int64_t>(S->contrib_total, 1));
     // factor storage estimate (no delays) + 10%
@@ -1058,7 +1069,7 @@ struct Numeric : NumericBase {
         d.LD = ws_LD.p + oL; oL += (size_t)d.cm * n;
         d.step = ws_step.p + (size_t)(f - f0) * (kBlk * kBlk + 2 * kBlk + 64);
         d.lperm = ws_lperm.p + (size_t)(f - f0) * kBlk;
-        d.tc = (use_tc && d.cm >= tc_min_cm) ? 1 : 0;
+        d.tc = (use_tc && d.cm >= tc_min_cm && d.n >= tc_min_k) ? 1 : 0;
       }
       CK(cudaMemcpyAsync(d_fd + f0, hfd.data() + f0, nf * sizeof(FrontDesc<T>),
                          cudaMemcpyHostToDevice, s));
