@@ -11,11 +11,11 @@
 //                   ldlt_app.cxx:316-436); X (= L21 D) is kept for the update;
 //                   extra CTAs apply the block permutation to the eliminated
 //                   L rows
-//   k_app_fixup     Column::adjust (ldlt_app.cxx:112-130) and, for failed
-//                   columns, the restore-and-update of restore_if_required +
-//                   update, computed as X_f L_ff^T (rows below) and
-//                   L_ff D_f L_ff^T (diagonal block)
-//   k_syrk (panel)  trailing update of the candidate columns (gemm_kernels.cu)
+//   k_app_panel     trailing update of the candidate columns and, in extra
+//                   CTAs, the fixup: Column::adjust (ldlt_app.cxx:112-130)
+//                   and, for failed columns, the restore-and-update of
+//                   restore_if_required + update, computed as X_f L_ff^T
+//                   (rows below) and L_ff D_f L_ff^T (diagonal block)
 //   k_app_swap      failed columns are moved to the end of the APP range
 // After ceil(n/32) steps k_app_finish records nelim; k_tpp finishes failed
 // columns with threshold partial pivoting (ldlt_tpp.cxx:166-270) where the
@@ -815,25 +815,20 @@ __device__ __forceinline__ int adjust_npass(int np, int bs, int p, const double*
 }
 
 // ------------------------------------------------------------------------
-// k_app_fixup: adjust npass; restore + update failed columns
+// Fixup of a block step (one of nfix CTAs, index fix): CTA 0 stores npass
+// (Column::adjust, ldlt_app.cxx:112-130); for failed columns the
+// restore-and-update of restore_if_required + update, computed as
+// X_f L_ff^T (rows below, blockDim.x rows per tile) and L_ff D_f L_ff^T
+// (diagonal block, CTA 0).  Failed columns are rare, so this path keeps few
+// registers rather than being fast.
 // ------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(kApplyRows) k_app_fixup(FrontDesc<T>* fds, FrontState* sts,
-                                                          const int* fronts) {
-  const int f = fronts[blockIdx.y];
-  pdl_wait();
-  pdl_trigger();
-  FrontState* st = &sts[f];
-  const int bs = st->bs;
-  if (bs == 0) return;
-  const int p = st->p;
-  FrontDesc<T> fd = fds[f];
-  const int np = adjust_npass(st->npass_raw, bs, p, fd.D);
-  if (blockIdx.x == 0 && threadIdx.x == 0) st->npass = np;
+__device__ void app_fixup_cta(const FrontDesc<T>& fd, FrontState* st, int p, int bs, int np,
+                              int fix, int nfix, double (*l11)[kBlk + 1],
+                              double (*ldf)[kBlk + 1]) {
+  if (fix == 0 && threadIdx.x == 0) st->npass = np;
   const int nf = bs - np;
   if (nf == 0) return;
-  __shared__ double l11[kBlk][kBlk + 1];
-  __shared__ double ldf[kBlk][kBlk + 1];
   for (int i = threadIdx.x; i < kBlk * kBlk; i += blockDim.x) {
     int c = i / kBlk, r = i % kBlk;
     double v = (r < bs && c < bs) ? ((r == c) ? 1.0 : (r > c ? fd.step[c * kBlk + r] : 0.0)) : 0.0;
@@ -842,23 +837,18 @@ __global__ void __launch_bounds__(kApplyRows) k_app_fixup(FrontDesc<T>* fds, Fro
   __syncthreads();
   const int r0 = p + bs, nrows = fd.m - r0;
   // rows below: A(r, p+np+i) = sum_{k<=i} X(r, np+k) * L(np+i, np+k)
-  for (int tile = blockIdx.x; tile * kApplyRows < nrows; tile += gridDim.x) {
-    int rr = tile * kApplyRows + threadIdx.x;
+  for (int tile = fix; tile * (int)blockDim.x < nrows; tile += nfix) {
+    const int rr = tile * blockDim.x + threadIdx.x;
     if (rr < nrows) {
       const T* W = fd.W + rr;
-      double xf[kBlk];
-#pragma unroll
-      for (int i = 0; i < kBlk; ++i) xf[i] = (i < nf) ? (double)W[(int64_t)(np + i) * fd.ld] : 0.0;
       for (int i = 0; i < nf; ++i) {
         double s = 0.0;
-#pragma unroll
-        for (int k = 0; k < kBlk; ++k)
-          if (k <= i) s += xf[k] * l11[np + i][np + k];
+        for (int k = 0; k <= i; ++k) s += (double)W[(int64_t)(np + k) * fd.ld] * l11[np + i][np + k];
         fd.L[(int64_t)(p + np + i) * fd.ld + r0 + rr] = (T)s;
       }
     }
   }
-  if (blockIdx.x == 0) {
+  if (fix == 0) {
     // diagonal failed block S = L_ff D_f L_ff^T
     const double* d = fd.step + kBlk * kBlk;
     // LD = L_ff * D_f  (D_f = inverse of stored inverse)
@@ -867,7 +857,7 @@ __global__ void __launch_bounds__(kApplyRows) k_app_fixup(FrontDesc<T>* fds, Fro
       ldf[r][c] = 0.0;
     }
     __syncthreads();
-    if (threadIdx.x < nf) {
+    if ((int)threadIdx.x < nf) {
       int r = threadIdx.x;
       for (int c = 0; c < nf;) {
         int cc = np + c;
@@ -895,6 +885,119 @@ __global__ void __launch_bounds__(kApplyRows) k_app_fixup(FrontDesc<T>* fds, Fro
       for (int k = 0; k < nf; ++k) s += l11[np + r][np + k] * ldf[c][k];
       fd.L[(int64_t)(p + np + c) * fd.ld + p + np + r] = (T)s;
     }
+  }
+}
+
+// ------------------------------------------------------------------------
+// k_app_panel: the block step's trailing update of the candidate columns
+// (ldlt_app.cxx:1082-1165 Block::update) in CTAs [0, ptiles) and its fixup
+// in CTAs [ptiles, gridDim.x).  The two touch disjoint columns (the update
+// reads the passed pivots' columns and writes the columns after the block;
+// the fixup rewrites the failed columns of the block), so one launch serves
+// both.  Every CTA derives npass from the apply's result itself.
+//
+// Update C -= A B^T (lower part) with K = npass <= kBlk: a TP x TP tile per
+// CTA round, thread (tx, ty) = (tid % 16, tid / 16) computing (TP/16)^2
+// entries; a tile stages all of its A and B columns and reads its C entries
+// in one batch of loads (one memory round trip per tile).  FP32 uses 64 x 64
+// tiles (latency bound); FP64 32 x 32 tiles: a 64 x 64 tile is about 37 us
+// of work for one SM's FP64 pipe, and finer tiles balance the last wave.
+// ------------------------------------------------------------------------
+template <typename T>
+constexpr int panel_tile() { return sizeof(T) == 8 ? 32 : 64; }
+
+template <typename T, int TP>
+__global__ void __launch_bounds__(256) k_app_panel(FrontDesc<T>* fds, FrontState* sts,
+                                                   const int* fronts, int ptiles) {
+  constexpr int RT = TP / 16;            // entries per thread and direction
+  constexpr int PER = TP * kBlk / 256;   // A (and B) loads per thread
+  // update CTAs use Ap/Bp, fixup CTAs l11/ldf: one buffer serves both
+  constexpr size_t kUpd = 2 * sizeof(T) * kBlk * (TP + 4);
+  constexpr size_t kFix = 2 * sizeof(double) * kBlk * (kBlk + 1);
+  __shared__ __align__(16) unsigned char sbuf[kUpd > kFix ? kUpd : kFix];
+  T (*Ap)[TP + 4] = reinterpret_cast<T (*)[TP + 4]>(sbuf);
+  T (*Bp)[TP + 4] = Ap + kBlk;
+  double (*l11)[kBlk + 1] = reinterpret_cast<double (*)[kBlk + 1]>(sbuf);
+  double (*ldf)[kBlk + 1] = l11 + kBlk;
+  const int f = fronts[blockIdx.y];
+  const FrontDesc<T> fd = fds[f];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
+  FrontState* stp = &sts[f];
+  const int bs = stp->bs;
+  if (bs == 0) return;
+  const int p = stp->p;
+  const int np = adjust_npass(stp->npass_raw, bs, p, fd.D);
+  if ((int)blockIdx.x >= ptiles) {
+    app_fixup_cta<T>(fd, stp, p, bs, np, blockIdx.x - ptiles, gridDim.x - ptiles, l11, ldf);
+    return;
+  }
+  const int M = fd.m - (p + bs), N = fd.n - (p + bs), K = np;
+  if (K <= 0 || M <= 0 || N <= 0) return;
+  T* C = fd.L + (int64_t)(p + bs) * fd.ld + (p + bs);
+  const T* A = fd.L + (int64_t)p * fd.ld + (p + bs);
+  const T* B = fd.W;
+  const int ld = fd.ld;
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int tc = (N + TP - 1) / TP, tr = (M + TP - 1) / TP;
+  const int total = tc * tr - tc * (tc - 1) / 2;
+  for (int t = blockIdx.x; t < total; t += ptiles) {
+    int tj = 0, rem = t;
+    while (rem >= tr - tj) { rem -= tr - tj; ++tj; }
+    const int ti = tj + rem;
+    const int row0 = ti * TP, col0 = tj * TP;
+    T cv[RT][RT];
+#pragma unroll
+    for (int y = 0; y < RT; ++y) {
+      const int c = col0 + ty + 16 * y;
+#pragma unroll
+      for (int x = 0; x < RT; ++x) {
+        const int r = row0 + tx + 16 * x;
+        cv[x][y] = (r < M && c < N && r >= c) ? C[(int64_t)c * ld + r] : T(0);
+      }
+    }
+    T av[PER], bv[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int idx = tid + 256 * q;
+      const int rr = idx % TP, kk = idx / TP;
+      const int r = row0 + rr, c = col0 + rr;
+      av[q] = (r < M && kk < K) ? A[(int64_t)kk * ld + r] : T(0);
+      bv[q] = (c < N && kk < K) ? B[(int64_t)kk * ld + c] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+      const int idx = tid + 256 * q;
+      Ap[idx / TP][idx % TP] = av[q];
+      Bp[idx / TP][idx % TP] = bv[q];
+    }
+    __syncthreads();
+    T acc[RT][RT];
+#pragma unroll
+    for (int a = 0; a < RT; ++a)
+#pragma unroll
+      for (int b = 0; b < RT; ++b) acc[a][b] = T(0);
+#pragma unroll 8
+    for (int kk = 0; kk < kBlk; ++kk) {
+      T a[RT], b[RT];
+#pragma unroll
+      for (int q = 0; q < RT; ++q) { a[q] = Ap[kk][tx + 16 * q]; b[q] = Bp[kk][ty + 16 * q]; }
+#pragma unroll
+      for (int x = 0; x < RT; ++x)
+#pragma unroll
+        for (int y = 0; y < RT; ++y) acc[x][y] += a[x] * b[y];
+    }
+#pragma unroll
+    for (int y = 0; y < RT; ++y) {
+      const int c = col0 + ty + 16 * y;
+#pragma unroll
+      for (int x = 0; x < RT; ++x) {
+        const int r = row0 + tx + 16 * x;
+        if (r < M && c < N && r >= c) C[(int64_t)c * ld + r] = cv[x][y] - acc[x][y];
+      }
+    }
+    __syncthreads();  // Ap/Bp are rewritten by the next tile
   }
 }
 
@@ -1297,12 +1400,6 @@ __global__ void k_stats(const FrontDesc<T>* fds, const FrontState* sts, const in
 }  // namespace
 
 // ---------------- syrk kernel entry points (gemm_kernels.cu) --------------
-// tile edge of the panel update for factor type T (gemm_kernels.cu)
-template <typename T>
-int panel_tile();
-template <typename T>
-void launch_syrk_panel(FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
-                       int max_tiles, cudaStream_t s);
 template <typename T>
 void launch_syrk_contrib(FrontDesc<T>* fd, const FrontState* st, const int* fronts, int nf,
                          int max_tiles, cudaStream_t s);
@@ -1332,17 +1429,16 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
   launch_pdl(k_app_apply<T>, dim3(napply + nperm, nf), kApplyRows, 0, s, fd, st, fronts, u, small,
              napply);
   note_launches(1);
-  pmark(tm, kPhFixup, s);
-  launch_pdl(k_app_fixup<T>, dim3(napply, nf), kApplyRows, 0, s, fd, st, fronts);
-  note_launches(1);
-  // tile estimate assumes no failed columns so far; after failures the
-  // trailing region is wider and the kernel's grid-stride loop covers it, so
-  // the launch is never skipped
-  const int tp = panel_tile<T>();
+  // trailing update and fixup in one launch (tile estimate assumes no failed
+  // columns so far; after failures the trailing region is wider and the
+  // kernel's tile loop covers it, so the launch is never skipped)
+  constexpr int tp = panel_tile<T>();
   int tr = std::max(0, cdiv(max_trail_rows, tp)), tc = std::max(0, cdiv(max_trail_cols, tp));
-  int tiles = tc * tr - tc * (tc - 1) / 2;
+  const int ptiles = std::max(1, std::min(tc * tr - tc * (tc - 1) / 2, 4096));
+  const int nfix = std::max(1, cdiv(max_rows, 256));
   pmark(tm, kPhPanel, s);
-  launch_syrk_panel<T>(fd, st, fronts, nf, std::max(tiles, 1), s);
+  launch_pdl(k_app_panel<T, tp>, dim3(ptiles + nfix, nf), 256, 0, s, fd, st, fronts, ptiles);
+  note_launches(1);
   pmark(tm, kPhSwap, s);
   launch_pdl(k_app_swap<T>, nf, 256, 0, s, fd, st, fronts);
   note_launches(1);
