@@ -267,9 +267,15 @@ int spral_ssids_gpu_node_inertia(const void* numeric, int* out);
 int spral_ssids_gpu_tc_crossover(void);
 
 /* Free and total memory of the current device (cudaMemGetInfo), for
- * callers that admit work by device memory.  No reference counterpart.
- * Returns 0 or -51. */
+ * callers that admit work by device memory; free includes the blocks this
+ * library keeps cached for reuse by numeric handles.  No reference
+ * counterpart.  Returns 0 or -51. */
 int spral_ssids_gpu_mem_info(size_t* free_bytes, size_t* total_bytes);
+
+/* No counterpart in the reference.  Returns the device blocks that numeric
+ * handles of this process gave back (kept for reuse by later handles, up to
+ * a quarter of the device's memory) to the driver, for the current device. */
+void spral_ssids_gpu_release_cache(void);
 
 /* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
 int spral_ssids_gpu_device_count(void);

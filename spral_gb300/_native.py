@@ -94,6 +94,7 @@ def _declare(L):
     f("spral_ssids_gpu_launch_count", ctypes.c_longlong)
     f("spral_ssids_gpu_node_inertia", I, P, P)
     f("spral_ssids_gpu_mem_info", I, P, P)
+    f("spral_ssids_gpu_release_cache", None)
     f("spral_ssids_gpu_tc_crossover", I)
     f("spral_ssids_gpu_set_profiling", None, P, I)
     f("spral_ssids_gpu_profile_stats", None, P, P)

@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <new>
 #include <stdexcept>
@@ -99,12 +100,142 @@ void launch_recip_probe(const double* x, double* y, int n, cudaStream_t s);
   } while (0)
 
 // ---------------------------------------------------------------------------
+// Device block cache.  Numeric handles take their large buffers (factor
+// arena chunks, contribution blocks, workspaces, solve vectors) from here
+// and give them back when they grow them or are destroyed, so a caller that
+// factors one matrix after another with a new handle each time (as
+// ssids_factor does) does not pay cudaMalloc and cudaFree, and the device
+// synchronisation of cudaFree, for every handle.  Blocks of 4 KiB or more
+// are kept per device in size classes (4 KiB steps up to 64 KiB, 64 KiB
+// steps up to 2 MiB, 2 MiB steps above), up to a quarter of the device's
+// memory; a request takes the
+// smallest cached block of its class or at most a quarter larger.
+// spral_ssids_gpu_mem_info counts cached bytes as free, and
+// spral_ssids_gpu_release_cache returns them to the driver.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kCacheDevices = 64;
+struct BlockCache {
+  std::mutex mu;
+  std::multimap<size_t, void*> blocks[kCacheDevices];
+  size_t bytes[kCacheDevices] = {0};
+  size_t limit[kCacheDevices] = {0};
+};
+BlockCache& block_cache() {
+  static BlockCache* c = new BlockCache();  // never destroyed: blocks outlive static teardown
+  return *c;
+}
+constexpr size_t kCacheMin = size_t(4) << 10;  // smaller blocks are not cached
+size_t cache_class(size_t bytes) {
+  const size_t g = bytes < (size_t(64) << 10)  ? (size_t(4) << 10)
+                   : bytes < (size_t(2) << 20) ? (size_t(64) << 10)
+                                               : (size_t(2) << 20);
+  return (bytes + g - 1) / g * g;
+}
+}  // namespace
+
+// allocate `bytes` on the current device; *cls receives the block's size
+void* cache_alloc(size_t bytes, size_t* cls, int* dev_out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  *dev_out = dev;
+  const size_t c = cache_class(std::max<size_t>(bytes, 1));
+  *cls = c;
+  if (c >= kCacheMin && dev >= 0 && dev < kCacheDevices) {
+    BlockCache& bc = block_cache();
+    std::lock_guard<std::mutex> lock(bc.mu);
+    auto it = bc.blocks[dev].lower_bound(c);
+    if (it != bc.blocks[dev].end() && it->first <= c + c / 4) {
+      void* p = it->second;
+      *cls = it->first;
+      bc.bytes[dev] -= it->first;
+      bc.blocks[dev].erase(it);
+      return p;
+    }
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, c);
+  if (e == cudaErrorMemoryAllocation && dev >= 0 && dev < kCacheDevices) {
+    // give the cached blocks back and retry once
+    cudaGetLastError();
+    BlockCache& bc = block_cache();
+    {
+      std::lock_guard<std::mutex> lock(bc.mu);
+      for (auto& kv : bc.blocks[dev]) cudaFree(kv.second);
+      bc.blocks[dev].clear();
+      bc.bytes[dev] = 0;
+    }
+    e = cudaMalloc(&p, c);
+  }
+  CK(e);
+  return p;
+}
+
+// return a block of size cls (from cache_alloc) allocated on device dev
+void cache_free(void* p, size_t cls, int dev) {
+  if (!p) return;
+  if (cls >= kCacheMin && dev >= 0 && dev < kCacheDevices) {
+    BlockCache& bc = block_cache();
+    std::lock_guard<std::mutex> lock(bc.mu);
+    if (bc.limit[dev] == 0) {
+      size_t fr = 0, tot = 0;
+      int cur = -1;
+      cudaGetDevice(&cur);
+      if (cur != dev) cudaSetDevice(dev);
+      if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { cudaGetLastError(); tot = 0; }
+      if (cur != dev && cur >= 0) cudaSetDevice(cur);
+      bc.limit[dev] = std::max<size_t>(tot / 4, 1);
+    }
+    if (bc.bytes[dev] + cls <= bc.limit[dev]) {
+      bc.blocks[dev].emplace(cls, p);
+      bc.bytes[dev] += cls;
+      return;
+    }
+  }
+  int cur = -1;
+  cudaGetDevice(&cur);
+  if (cur != dev && dev >= 0) cudaSetDevice(dev);
+  cudaFree(p);
+  if (cur != dev && cur >= 0) cudaSetDevice(cur);
+}
+
+// cudaFree on the block's device (not cached)
+void release_now(void* p, int dev) {
+  int cur = -1;
+  cudaGetDevice(&cur);
+  if (cur != dev && dev >= 0) cudaSetDevice(dev);
+  cudaFree(p);
+  if (cur != dev && cur >= 0) cudaSetDevice(cur);
+}
+
+size_t cache_bytes(int dev) {
+  if (dev < 0 || dev >= kCacheDevices) return 0;
+  BlockCache& bc = block_cache();
+  std::lock_guard<std::mutex> lock(bc.mu);
+  return bc.bytes[dev];
+}
+
+void cache_release(int dev) {
+  if (dev < 0 || dev >= kCacheDevices) return;
+  BlockCache& bc = block_cache();
+  std::lock_guard<std::mutex> lock(bc.mu);
+  int cur = -1;
+  cudaGetDevice(&cur);
+  if (cur != dev) cudaSetDevice(dev);
+  for (auto& kv : bc.blocks[dev]) cudaFree(kv.second);
+  bc.blocks[dev].clear();
+  bc.bytes[dev] = 0;
+  if (cur != dev && cur >= 0) cudaSetDevice(cur);
+}
+
+// ---------------------------------------------------------------------------
 // device arena: chunked bump allocator that can be rewound for refactorisation
 // ---------------------------------------------------------------------------
 struct DevArena {
   struct Chunk {
     char* p;
     size_t cap;
+    int dev;
   };
   std::vector<Chunk> chunks;
   size_t ci = 0, used = 0;
@@ -123,32 +254,38 @@ struct DevArena {
       used = 0;
     }
     size_t cap = std::max(bytes, min_chunk);
-    void* p = nullptr;
-    CK(cudaMalloc(&p, cap));
-    chunks.push_back({(char*)p, cap});
+    int dev = 0;
+    void* p = cache_alloc(cap, &cap, &dev);
+    chunks.push_back({(char*)p, cap, dev});
     ci = chunks.size() - 1;
     used = bytes;
     return p;
   }
   ~DevArena() {
-    for (auto& c : chunks) cudaFree(c.p);
+    for (auto& c : chunks) cache_free(c.p, c.cap, c.dev);
   }
 };
 
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
-  size_t cap = 0;
+  size_t cap = 0;    // elements
+  size_t bytes = 0;  // size of the cache block
+  int dev = -1;
   void ensure(size_t n) {
     if (n <= cap) return;
-    if (p) cudaFree(p);
+    // kernels already queued may still use the old block: give it to the
+    // driver (cudaFree waits for them) rather than to the cache
+    if (p) release_now(p, dev);
     p = nullptr;
     size_t nc = std::max(n, cap + cap / 2);
-    CK(cudaMalloc(&p, std::max<size_t>(nc, 1) * sizeof(T)));
-    cap = nc;
+    p = static_cast<T*>(cache_alloc(std::max<size_t>(nc, 1) * sizeof(T), &bytes, &dev));
+    cap = bytes / sizeof(T);
   }
+  // the owner has finished all work that uses the block (Numeric's
+  // destructor synchronises its stream first)
   ~DevBuf() {
-    if (p) cudaFree(p);
+    if (p) cache_free(p, bytes, dev);
   }
 };
 
@@ -563,7 +700,9 @@ struct Numeric : NumericBase {
   bool solve_ready = false;
   SolveNode<T>* d_sn = nullptr;
   int* d_children = nullptr;
-  size_t sn_cap = 0, ch_cap = 0;
+  DevBuf<SolveNode<T>> sn_buf;
+  DevBuf<int> ch_buf;
+  DevBuf<char> small_buf;  // d_fd, d_st, d_stats, d_dwork, d_tc_status, d_ncount
   // Captured solve sequences (CUDA graphs), replayed while the launch
   // sequence and every pointer it uses are unchanged (solve_sig).
   struct SolveGraph {
@@ -919,12 +1058,22 @@ struct Numeric : NumericBase {
     hst.resize(nn);
     nelim_.assign(nn, 0); ndin_.assign(nn, 0); m_.assign(nn, 0); n_.assign(nn, 0);
     ld_.assign(nn, 0); doff_.assign(nn, 0); napp_.assign(nn, 0);
-    CK(cudaMalloc(&d_fd, std::max(nn, 1) * sizeof(FrontDesc<T>)));
-    CK(cudaMalloc(&d_st, std::max(nn, 1) * sizeof(FrontState)));
-    CK(cudaMalloc(&d_stats, sizeof(Stats)));
-    CK(cudaMalloc(&d_dwork, std::max(nn, 1) * sizeof(int4)));
-    CK(cudaMalloc(&d_tc_status, sizeof(int)));
-    CK(cudaMalloc(&d_ncount, 3 * (size_t)std::max(nn, 1) * sizeof(int)));
+    {
+      // the per-front descriptor, state and count arrays share one block
+      auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+      const size_t nn1 = std::max(nn, 1);
+      const size_t b_fd = al(nn1 * sizeof(FrontDesc<T>)), b_st = al(nn1 * sizeof(FrontState));
+      const size_t b_stats = al(sizeof(Stats)), b_dw = al(nn1 * sizeof(int4));
+      const size_t b_tcs = al(sizeof(int)), b_nc = al(3 * nn1 * sizeof(int));
+      small_buf.ensure(b_fd + b_st + b_stats + b_dw + b_tcs + b_nc);
+      char* q = small_buf.p;
+      d_fd = reinterpret_cast<FrontDesc<T>*>(q); q += b_fd;
+      d_st = reinterpret_cast<FrontState*>(q); q += b_st;
+      d_stats = reinterpret_cast<Stats*>(q); q += b_stats;
+      d_dwork = reinterpret_cast<int4*>(q); q += b_dw;
+      d_tc_status = reinterpret_cast<int*>(q); q += b_tcs;
+      d_ncount = reinterpret_cast<int*>(q);
+    }
     {
       const char* gr = getenv("SPRAL_GB300_GRAPHS");
       use_graphs = !(gr && gr[0] == '0');
@@ -947,12 +1096,12 @@ struct Numeric : NumericBase {
     farena.min_chunk = std::max<size_t>(est * sizeof(T) * 11 / 10, size_t(16) << 20);
   }
   ~Numeric() override {
+    // every kernel of this handle has finished before its blocks go back to
+    // the device block cache (member destructors)
+    if (stream) cudaStreamSynchronize(stream);
     for (auto e : pev) cudaEventDestroy(e);
-    cudaFree(d_fd); cudaFree(d_st); cudaFree(d_stats); cudaFree(d_dwork); cudaFree(d_tc_status);
-    cudaFree(d_ncount);
     drop_graphs();
     drop_fgraph();
-    cudaFree(d_sn); cudaFree(d_children);
     for (auto& e : ev) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -1207,18 +1356,10 @@ struct Numeric : NumericBase {
       q.doff = doff_[f];
     }
     // the tables keep their device addresses across refactorisations
-    if (sn.size() > sn_cap) {
-      cudaFree(d_sn);
-      d_sn = nullptr;
-      CK(cudaMalloc(&d_sn, sn.size() * sizeof(SolveNode<T>)));
-      sn_cap = sn.size();
-    }
-    if (std::max<size_t>(ch.size(), 1) > ch_cap) {
-      cudaFree(d_children);
-      d_children = nullptr;
-      CK(cudaMalloc(&d_children, std::max<size_t>(ch.size(), 1) * sizeof(int)));
-      ch_cap = std::max<size_t>(ch.size(), 1);
-    }
+    sn_buf.ensure(std::max<size_t>(sn.size(), 1));
+    ch_buf.ensure(std::max<size_t>(ch.size(), 1));
+    d_sn = sn_buf.p;
+    d_children = ch_buf.p;
     CK(cudaMemcpyAsync(d_sn, sn.data(), sn.size() * sizeof(SolveNode<T>), cudaMemcpyHostToDevice,
                        stream));
     if (!ch.empty())
@@ -1782,7 +1923,15 @@ int spral_ssids_gpu_mem_info(size_t* free_bytes, size_t* total_bytes) {
     cudaGetLastError();
     return -51;
   }
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) *free_bytes += ssids300::cache_bytes(dev);
   return 0;
+}
+
+void spral_ssids_gpu_release_cache(void) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) ssids300::cache_release(dev);
+  else cudaGetLastError();
 }
 
 /* Per-node inertia of the last factorisation: out[3*node + {0, 1, 2}] =
