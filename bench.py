@@ -53,11 +53,18 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--mixed-only", action="store_true",
                     help="profiling aid: time only the mixed-precision path and print its object")
-    ap.add_argument("--workload", default="lap3d", choices=["lap3d", "batch", "serve", "tc-gemm"],
+    ap.add_argument("--workload", default="lap3d",
+                    choices=["lap3d", "batch", "serve", "tc-gemm", "kkt"],
                     help="lap3d: the headline 48^3 Laplacian; batch: many small 2D Laplacians "
                          "factored and solved as one forest; serve: a Poisson stream of factor "
                          "and refactor requests through the request loop; tc-gemm: the "
-                         "tensor-core Schur update kernel alone")
+                         "tensor-core Schur update kernel alone; kkt: a KKT saddle point "
+                         "(random sparse H and A, -1e-8 I block) in mixed precision with FP64 "
+                         "refinement against the FP64 path")
+    ap.add_argument("--kkt-nh", type=int, default=10000)
+    ap.add_argument("--kkt-na", type=int, default=5000)
+    ap.add_argument("--kkt-cpu", action="store_true",
+                    help="also time the CPU port on the kkt workload (about a minute)")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-count", type=int, default=96)
     ap.add_argument("--serve-rate", type=float, default=8.0)
@@ -713,6 +720,133 @@ def run_tc_gemm(args):
                       "peak": peak, "peak_source": src, "cases": out}), flush=True)
 
 
+def run_kkt(args):
+    """KKT saddle point [[H, A^T], [A, -1e-8 I]] with the benchmark
+    definition's structure (H SPD with a random symmetric pattern of about 7
+    entries per row, N(0,1) off-diagonals and diagonal = row abs-sum + 1; A
+    with 4 N(0,1) entries per row at uniform columns) at nh x na = 10,000 x
+    5,000 by default (the definition's 200,000 x 100,000 has no small
+    separators: its root front would be ~1.9e5 wide).  Minimum-degree order,
+    8 right-hand sides N(0,1).  One step = numeric factor + 8-RHS solve
+    refined to bwd err <= 1e-14; `value` is the mixed-precision path (FP32
+    factors, 2x2 pivots and delays decided in FP64), `fp64` the FP64 path."""
+    import torch
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    from spral_gb300 import _native, matrices as M, ssids
+    L = _native.lib()
+    nh, na = args.kkt_nh, args.kkt_na
+    ptr, row, val = M.kkt(nh, na, seed=2026)
+    ak = ssids.analyse(ptr, row)
+    n, nrhs = ak.n, args.nrhs
+    b = np.random.default_rng(2027).standard_normal((n, nrhs))
+    dev = torch.device("cuda", local)
+    aval_d = torch.tensor(val, dtype=torch.float64, device=dev)
+    b_d = torch.tensor(np.ascontiguousarray(b[ak.invp, :].T), dtype=torch.float64, device=dev)
+    x_d = torch.empty_like(b_d)
+
+    def measure(prec, steps):
+        fk = ssids.Fkeep(ak, val, ssids.Options(precision=prec, max_refine=20,
+                                                 refine_tol=REFINE_TOL))
+        it = ctypes.c_int(0)
+        bw = ctypes.c_double(0)
+
+        def step():
+            fk.refactor_dev(aval_d.data_ptr())
+            L.spral_ssids_gpu_solve_refined_dev(fk.num, nrhs, ctypes.c_void_p(b_d.data_ptr()),
+                                                ctypes.c_void_p(x_d.data_ptr()), n,
+                                                ctypes.byref(it), ctypes.byref(bw))
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        lc0 = L.spral_ssids_gpu_launch_count()
+        clk = Clocks(local) if rank == 0 else None
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        clocks = clk.stop() if clk else None
+        ms = e0.elapsed_time(e1) / steps
+        x = x_d.cpu().numpy().T
+        xu = np.empty_like(x)
+        xu[ak.invp, :] = x
+        out = {"value": 1000.0 / ms, "unit": "solves/s", "ms_per_step": ms,
+               "factor_ms": float(fk.timing()[0]),
+               "bwd_err": float(M.scaled_bwd_error(ptr, row, val, xu, b).max()),
+               "refine_iters": it.value, "num_neg": fk.inform.num_neg,
+               "num_two": fk.inform.num_two, "num_delay": fk.inform.num_delay,
+               "fp64_fallbacks": fk.fallbacks, "num_flops": fk.inform.num_flops,
+               "gpu_launches": int(L.spral_ssids_gpu_launch_count() - lc0), "clocks": clocks}
+        return fk, out
+
+    fm, mixed = measure(ssids.PRECISION_MIXED, args.steps)
+    roof = tensor_roofline(L, fm, aval_d)
+    # end to end through the C-ABI with host buffers (mixed precision)
+    g = ssids.Options(precision=ssids.PRECISION_MIXED, max_refine=20, refine_tol=REFINE_TOL)
+    copts = g.cpu_options()
+    xh = np.asfortranarray(b[ak.invp, :])
+    e2e_t = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        st = _native.ThreadStats()
+        num = L.spral_ssids_gpu_create_num_subtree_dbl(False, fm.sym,
+                                                       val.ctypes.data_as(ctypes.c_void_p), None,
+                                                       None, ctypes.byref(copts), ctypes.byref(st))
+        xw = xh.copy(order="F")
+        its = ctypes.c_int(0)
+        L.spral_ssids_gpu_solve_refined(num, nrhs, xw.ctypes.data_as(ctypes.c_void_p), n,
+                                        ctypes.byref(its))
+        L.spral_ssids_gpu_destroy_num_subtree_dbl(False, num)
+        if i >= args.warmup:
+            e2e_t.append(time.perf_counter() - t0)
+    fm.free()
+    f64, fp64 = measure(ssids.PRECISION_FP64, max(1, min(args.steps, 3)))
+    f64.free()
+    cpu = None
+    if rank == 0 and args.kkt_cpu:
+        import oracle
+        oracle.build()
+        t0 = time.perf_counter()
+        F = oracle.OracleFactor(ak, val, blas=True)
+        xc = F.solve(b)
+        tc = time.perf_counter() - t0
+        cpu = {"value": 1.0 / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "one full factor+solve (OpenBLAS threads = all cores)",
+               "bwd_err": float(M.scaled_bwd_error(ptr, row, val, xc, b).max()),
+               "num_neg": F.stats["num_neg"]}
+    if rank == 0:
+        e2e_ms = 1000.0 * sum(e2e_t) / len(e2e_t)
+        line = {"metric": METRIC, "workload": "kkt", "value": mixed["value"],
+                "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": mixed["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32 factors, f64 refinement",
+                "data": "synthetic (seeded KKT values and RHS)",
+                "config": {"workload": f"KKT [[H, A^T], [A, -1e-8 I]], H {nh}x{nh} SPD (7 "
+                                       f"nnz/row), A {na}x{nh} (4 nnz/row), n={n}, "
+                                       f"minimum-degree order, {nrhs} RHS N(0,1); one solve = "
+                                       f"numeric factor + {nrhs}-RHS solve refined to bwd err "
+                                       f"<= 1e-14",
+                           "n": n, "nnz_lower": ak.nnz, "predicted_flops": ak.nflops,
+                           "maxfront": int(ak.front_sizes()[0].max()),
+                           "num_neg_expected": na,
+                           "l2": "inputs larger than L2 (factors ~%.0f MB in FP32)"
+                                 % (ak.nfact * 4 / 1e6)},
+                "mixed": mixed, "fp64": fp64,
+                "speedup_mixed_vs_fp64_gpu": mixed["value"] / fp64["value"],
+                "e2e": {"value": 1000.0 / e2e_ms, "unit": "solves/s",
+                        "h2d_bytes_per_step": int(val.nbytes + n * nrhs * 8),
+                        "d2h_bytes_per_step": int(n * nrhs * 8),
+                        "path": "spral_ssids_gpu_create_num_subtree_dbl + "
+                                "spral_ssids_gpu_solve_refined (host aval and x, FP32 factors)"},
+                "gpu_launches": mixed["gpu_launches"], "roofline": roof, "cpu_baseline": cpu,
+                "clocks": mixed["clocks"]}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "tc-gemm":
@@ -724,6 +858,8 @@ def main():
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "kkt":
+        run_kkt(args)
     else:
         run_gpu(args)
 
