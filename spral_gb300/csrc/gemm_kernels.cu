@@ -43,6 +43,71 @@ __global__ void __launch_bounds__(256) k_syrk(FrontDesc<T>* fds, const FrontStat
   const int tx = tid & 15, ty = tid >> 4;
   const int tc = (j.N + TM - 1) / TM, tr = (j.M + TM - 1) / TM;
   const int total = tc * tr - tc * (tc - 1) / 2;
+  if constexpr (sizeof(T) == 4) {
+    // FP32: a tile reads its C entries with the first 32 columns of A and B
+    // in one batch of loads, then one batch per further 32 columns.  (Thin
+    // supernodes update large contribution blocks with depth 32, where the
+    // update is a stream of C through HBM.)
+    constexpr int KC = 32, PER = TM * KC / 256;
+    __shared__ T Ap[KC][TM + 4];
+    __shared__ T Bp[KC][TM + 4];
+    for (int t = blockIdx.x; t < total; t += gridDim.x) {
+      int tj = 0, rem = t;
+      while (rem >= tr - tj) { rem -= tr - tj; ++tj; }
+      const int ti = tj + rem;
+      const int row0 = ti * TM, col0 = tj * TM;
+      T cv[4][4], acc[4][4];
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        const int c = col0 + ty + 16 * y;
+#pragma unroll
+        for (int x = 0; x < 4; ++x) {
+          const int r = row0 + tx + 16 * x;
+          cv[x][y] = (r < j.M && c < j.N && r >= c) ? j.C[(int64_t)c * j.ldc + r] : T(0);
+          acc[x][y] = T(0);
+        }
+      }
+      for (int k0 = 0; k0 < j.K; k0 += KC) {
+        T av[PER], bv[PER];
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+          const int idx = tid + 256 * q;
+          const int rr = idx % TM, kk = k0 + idx / TM;
+          const int r = row0 + rr, c = col0 + rr;
+          av[q] = (r < j.M && kk < j.K) ? j.A[(int64_t)kk * j.lda + r] : T(0);
+          bv[q] = (c < j.N && kk < j.K) ? j.B[(int64_t)kk * j.ldb + c] : T(0);
+        }
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+          const int idx = tid + 256 * q;
+          Ap[idx / TM][idx % TM] = av[q];
+          Bp[idx / TM][idx % TM] = bv[q];
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < KC; ++kk) {
+          T a[4], b[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) { a[q] = Ap[kk][tx + 16 * q]; b[q] = Bp[kk][ty + 16 * q]; }
+#pragma unroll
+          for (int x = 0; x < 4; ++x)
+#pragma unroll
+            for (int y = 0; y < 4; ++y) acc[x][y] += a[x] * b[y];
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        const int c = col0 + ty + 16 * y;
+#pragma unroll
+        for (int x = 0; x < 4; ++x) {
+          const int r = row0 + tx + 16 * x;
+          if (r < j.M && c < j.N && r >= c) j.C[(int64_t)c * j.ldc + r] = cv[x][y] - acc[x][y];
+        }
+      }
+    }
+    return;
+  }
   __shared__ T As[TK][TM + 4];
   __shared__ T Bs[TK][TM + 4];
   for (int t = blockIdx.x; t < total; t += gridDim.x) {

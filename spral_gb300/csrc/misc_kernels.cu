@@ -11,16 +11,35 @@ namespace ssids300 {
 
 namespace {
 
+// zero n elements from p (16-byte aligned) with 16-byte stores
+template <typename T>
+__device__ __forceinline__ void zero_range(T* p, int64_t n, int64_t i0, int64_t stride) {
+  constexpr int V = 16 / sizeof(T);
+  const int64_t nv = n / V;
+  int4* q = reinterpret_cast<int4*>(p);
+  for (int64_t i = i0; i < nv; i += stride) q[i] = make_int4(0, 0, 0, 0);
+  for (int64_t i = nv * V + i0; i < n; i += stride) p[i] = T(0);
+}
+
+// Zero a level's fronts: L (ld x n, contiguous), the contribution block
+// (cm x cm; contiguous when ldc == cm, as for the tree's own blocks) and D.
+// Fronts and contribution blocks start 256-byte aligned, so the stores are
+// 16 bytes wide: this pass writes each front's storage once per
+// factorisation, at HBM speed.
 template <typename T>
 __global__ void k_zero_fronts(FrontDesc<T>* fds, const int* fronts) {
   const FrontDesc<T> fd = fds[fronts[blockIdx.y]];
   const int64_t nl = (int64_t)fd.ld * fd.n;
   const int64_t nc = (int64_t)fd.cm * fd.cm;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl; i += stride) fd.L[i] = T(0);
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nc; i += stride)
-    fd.C[(i / fd.cm) * fd.ldc + i % fd.cm] = T(0);
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 2 * fd.n; i += stride) fd.D[i] = 0.0;
+  const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  zero_range(fd.L, nl, i0, stride);
+  if (fd.ldc == fd.cm) {
+    zero_range(fd.C, nc, i0, stride);
+  } else {
+    for (int64_t i = i0; i < nc; i += stride) fd.C[(i / fd.cm) * fd.ldc + i % fd.cm] = T(0);
+  }
+  zero_range(fd.D, 2 * (int64_t)fd.n, i0, stride);
 }
 
 __device__ __forceinline__ void atomic_max_pos(double* a, double v) {
@@ -216,7 +235,9 @@ template <typename T>
 void launch_zero_fronts(FrontDesc<T>* fd, const int* fronts, int nf, int max_elems,
                         cudaStream_t s) {
   if (nf <= 0) return;
-  int gx = std::max(1, std::min((max_elems + 1023) / 1024, 256));
+  // 16-byte stores: one thread per 8 elements (FP32) or 4 (FP64) per round
+  const int per = 256 * (16 / (int)sizeof(T)) * 4;
+  int gx = std::max(1, std::min((max_elems + per - 1) / per, 4 * 152));
   { k_zero_fronts<T><<<dim3(gx, nf), 256, 0, s>>>(fd, fronts); note_launches(1); }
 }
 template void launch_zero_fronts<double>(FrontDesc<double>*, const int*, int, int, cudaStream_t);
