@@ -54,11 +54,13 @@ def parse():
     ap.add_argument("--mixed-only", action="store_true",
                     help="profiling aid: time only the mixed-precision path and print its object")
     ap.add_argument("--workload", default="lap3d",
-                    choices=["lap3d", "batch", "serve", "tc-gemm", "kkt"],
+                    choices=["lap3d", "batch", "serve", "tc-gemm", "kkt", "contrib"],
                     help="lap3d: the headline 48^3 Laplacian; batch: many small 2D Laplacians "
                          "factored and solved as one forest; serve: a Poisson stream of factor "
                          "and refactor requests through the request loop; tc-gemm: the "
-                         "tensor-core Schur update kernel alone; kkt: a KKT saddle point "
+                         "tensor-core Schur update kernel alone; contrib: the SIMT "
+                         "contribution update of one thin wide front alone (HBM roofline); "
+                         "kkt: a KKT saddle point "
                          "(random sparse H and A, -1e-8 I block) in mixed precision with FP64 "
                          "refinement against the FP64 path")
     ap.add_argument("--kkt-nh", type=int, default=10000)
@@ -720,6 +722,66 @@ def run_tc_gemm(args):
                       "peak": peak, "peak_source": src, "cases": out}), flush=True)
 
 
+def run_contrib(args):
+    """The SIMT contribution update of one front alone, C -= L21 (L21 D)^T on
+    the lower triangle, through spral_ssids_gpu_contrib_update: the thin
+    supernodes of the KKT workload's chain (k = 32 and 64 eliminated columns
+    against a contribution block 9,728 rows wide) in FP32, where the update
+    streams C through HBM, and the same in FP64.  Algorithmic bytes = the
+    lower triangle of C read and written once (cm(cm+1)/2 entries x 2);
+    C (190-380 MB) exceeds L2, so no flush between repetitions.  Timed with
+    CUDA events on the stream of the launches; the first call's result is
+    checked against an FP64 product on the host."""
+    import torch
+    from spral_gb300 import _native
+    L = _native.lib()
+    peak, src = hbm_peak_gbs()
+    stream = torch.cuda.current_stream()
+    out = []
+    for dbl, cm, k in ((0, 9728, 32), (0, 9728, 64), (1, 9728, 32)):
+        dt = torch.float64 if dbl else torch.float32
+        npdt = np.float64 if dbl else np.float32
+        rng = np.random.default_rng(cm + k + dbl)
+        ld = cm + k
+        Lh = (rng.standard_normal((ld, k)) * 0.1).astype(npdt)
+        LDh = (rng.standard_normal((cm, k)) * 0.1).astype(npdt)
+        Ch = np.tril(rng.standard_normal((cm, cm))).astype(npdt)
+        dL = torch.tensor(Lh.ravel(order="F"), device="cuda")
+        dLD = torch.tensor(LDh.ravel(order="F"), device="cuda")
+        dC = torch.tensor(Ch.ravel(order="F"), device="cuda")
+        h = stream.cuda_stream
+
+        def call(reps):
+            rc = L.spral_ssids_gpu_contrib_update(dbl, dL.data_ptr(), ld, dLD.data_ptr(),
+                                                  dC.data_ptr(), cm, k, reps, h)
+            assert rc == 0, rc
+
+        call(1)
+        got = dC.cpu().numpy().reshape(cm, cm, order="F").astype(np.float64)
+        ref = Ch.astype(np.float64) - Lh[k:, :].astype(np.float64) @ LDh.astype(np.float64).T
+        low = np.tril(np.ones((cm, cm), bool))
+        err = float(np.abs(got - ref)[low].max())
+        call(max(args.warmup, 3))
+        reps = max(args.steps, 3)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        call(reps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        ent = cm * (cm + 1) / 2
+        gbs = ent * 2 * (8 if dbl else 4) / (ms * 1e-3) / 1e9
+        out.append({"dtype": "f64" if dbl else "f32", "cm": cm, "k": k, "ms": ms,
+                    "achieved_gbs": gbs, "frac_hbm": gbs / peak,
+                    "gflops": 2.0 * k * ent / (ms * 1e-3) / 1e9, "max_abs_err": err})
+        del dL, dLD, dC
+    print(json.dumps({"metric": "SIMT contribution update GB/s (lower C read + write)",
+                      "workload": "contrib", "value": out[0]["achieved_gbs"], "unit": "GB/s",
+                      "peak": peak, "peak_source": src, "cases": out}), flush=True)
+
+
 def run_kkt(args):
     """KKT saddle point [[H, A^T], [A, -1e-8 I]] with the benchmark
     definition's structure (H SPD with a random symmetric pattern of about 7
@@ -851,6 +913,9 @@ def main():
     args = parse()
     if args.workload == "tc-gemm":
         run_tc_gemm(args)
+        return
+    if args.workload == "contrib":
+        run_contrib(args)
         return
     if args.impl == "reference":
         run_reference(args)

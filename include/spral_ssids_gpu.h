@@ -266,6 +266,20 @@ int spral_ssids_gpu_node_inertia(const void* numeric, int* out);
  * the size, or -51 on a CUDA error. */
 int spral_ssids_gpu_tc_crossover(void);
 
+/* The contribution update of one front, C -= L21 (L21 D)^T on the lower
+ * triangle of the cm x cm block C, on the SIMT kernel of the numeric
+ * factorisation, applied reps times on the caller's device buffers and
+ * stream (L: the front's (cm + k) x k columns, leading dimension ld >=
+ * cm + k; LD = L21 D: cm x k, leading dimension cm; C: a full cm x cm
+ * array, whose upper part may be read but is never written; FP64 when
+ * dbl != 0, else FP32).  Serves timing the kernel alone.  No
+ * reference counterpart (the reference forms this block inside its
+ * factorisation: form_contrib, src/ssids/gpu/factor.f90:945, with the
+ * kernel cu_multisyrk_lc_r4x4, src/ssids/gpu/kernels/syrk.cu:185).
+ * Returns 0, -1 on a bad argument or -51 on a CUDA error. */
+int spral_ssids_gpu_contrib_update(int dbl, const void* l, int ld, const void* l21d, void* c,
+                                   int cm, int k, int reps, void* stream);
+
 /* Free and total memory of the current device (cudaMemGetInfo), for
  * callers that admit work by device memory; free includes the blocks this
  * library keeps cached for reuse by numeric handles.  No reference

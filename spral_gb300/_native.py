@@ -96,6 +96,7 @@ def _declare(L):
     f("spral_ssids_gpu_mem_info", I, P, P)
     f("spral_ssids_gpu_release_cache", None)
     f("spral_ssids_gpu_tc_crossover", I)
+    f("spral_ssids_gpu_contrib_update", I, I, P, I, P, P, I, I, I, P)
     f("spral_ssids_gpu_set_profiling", None, P, I)
     f("spral_ssids_gpu_profile_stats", None, P, P)
     f("spral_ssids_gpu_fp64_peak_tflops", D, I)

@@ -1916,6 +1916,46 @@ int spral_ssids_gpu_tc_crossover(void) {
   }
 }
 
+/* The contribution update of one front on the SIMT kernel, on the caller's
+ * device buffers and stream: C -= L21 (L21 D)^T on the lower triangle of
+ * the cm x cm block C (leading dimension cm), where the front's L is
+ * (cm + k) x k with leading dimension ld (rows 0..k-1 the pivots, rows k..
+ * the L21 block) and LD = L21 D is cm x k with leading dimension cm.  dbl
+ * selects FP64 (1) or FP32 (0) buffers; the update is applied reps times
+ * back to back (reps >= 1).  Returns 0, -1 on a bad argument or -51 on a
+ * CUDA error. */
+int spral_ssids_gpu_contrib_update(int dbl, const void* l, int ld, const void* l21d, void* c,
+                                   int cm, int k, int reps, void* stream) {
+  using namespace ssids300;
+  if (cm < 0 || k < 0 || reps < 1 || ld < cm + k || !l || !l21d || !c) return -1;
+  if (cm == 0 || k == 0) return 0;
+  auto s = static_cast<cudaStream_t>(stream);
+  auto run = [&](auto* tag) -> int {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    struct Blk {
+      FrontDesc<T> fd;
+      FrontState st;
+      int front;
+    } h{};
+    h.fd.L = const_cast<T*>(static_cast<const T*>(l));
+    h.fd.LD = const_cast<T*>(static_cast<const T*>(l21d));
+    h.fd.C = static_cast<T*>(c);
+    h.fd.m = cm + k; h.fd.n = k; h.fd.ld = ld; h.fd.cm = cm; h.fd.ldc = cm;
+    h.fd.nrow = cm + k; h.fd.ncol = k;
+    h.st.nelim = k;
+    h.front = 0;
+    Blk* d = nullptr;
+    if (cudaMallocAsync(reinterpret_cast<void**>(&d), sizeof(Blk), s) != cudaSuccess) return -51;
+    cudaMemcpyAsync(d, &h, sizeof(Blk), cudaMemcpyHostToDevice, s);
+    for (int r = 0; r < reps; ++r) launch_contrib_gemm<T>(&d->fd, &d->st, &d->front, 1, cm, s);
+    cudaFreeAsync(d, s);
+    // h is read by the copy above before the stream drains
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -51;
+    return cudaGetLastError() == cudaSuccess ? 0 : -51;
+  };
+  return dbl ? run(static_cast<double*>(nullptr)) : run(static_cast<float*>(nullptr));
+}
+
 /* Free and total device memory of the current device (cudaMemGetInfo);
  * used by callers that admit work by memory.  Returns 0 or -51. */
 int spral_ssids_gpu_mem_info(size_t* free_bytes, size_t* total_bytes) {
