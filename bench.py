@@ -214,8 +214,9 @@ def hbm_rooflines(ak, L, fk, ph_ms, b_d, x_d, n, nrhs):
     algorithmic byte counts: solve = 2 sum_nodes m*nelim*8 (L read in the
     forward and the backward pass) + sum_nodes 2*nelim*8 (D) + 2 sum_nodes
     m*nrhs*8*2 (local vectors gathered and scattered); assembly = sum over
-    children cm(cm+1)/2 * (8 read + 16 parent read-modify-write) + 4 cm
-    (row map) plus loading A: nnz * (8 value + 16 index pair + 8 front)."""
+    children cm(cm+1)/2 * (8 read + 8 parent write: the extend-add zeroes
+    the parent's contribution columns in L2 before adding) + 4 cm (row map)
+    plus loading A: nnz * (8 value + 16 index pair + 8 front)."""
     import torch
     peak, src = hbm_peak_gbs()
     nrow, ncol = ak.front_sizes()
@@ -232,7 +233,7 @@ def hbm_rooflines(ak, L, fk, ph_ms, b_d, x_d, n, nrhs):
     cm = nrow - ncol
     parent = ak.sparent[:ak.nnodes] - 1
     has_parent = parent < ak.nnodes
-    asm_bytes = float((cm[has_parent] * (cm[has_parent] + 1) / 2 * 24 + 4 * cm[has_parent]).sum()
+    asm_bytes = float((cm[has_parent] * (cm[has_parent] + 1) / 2 * 16 + 4 * cm[has_parent]).sum()
                       + ak.nnz * 32)
     t_asm = (ph_ms[1] + ph_ms[4]) * 1e-3  # load A + extend-add phases
     return {"peak": peak, "unit": "GB/s", "peak_source": src,
@@ -257,11 +258,15 @@ def tf32_peak_tflops():
         return 1900.0 / 2.0, "fallback 1.9 PF/s bf16 / 2"
 
 
-def tensor_roofline(L, fk, aval_d):
+def tensor_roofline(L, fk, aval_d, ak=None):
     """Roofline of the tensor-core Schur update (k_tc_gemm) inside one
     mixed-precision factorization, each launch timed with CUDA events on
     the library's stream.  Tensor flops = 3 x the FP32 update's flops
-    (3xTF32 split products)."""
+    (3xTF32 split products).  When no front takes the tensor cores (thin
+    supernodes, below the depth rule) and ak is given, the roofline of the
+    SIMT contribution update instead: HBM-bound, algorithmic bytes = the
+    lower triangle of every contribution block read and written once in
+    FP32, sum cm(cm+1)/2 * 8."""
     L.spral_ssids_gpu_set_profiling(fk.num, 1)
     fk.refactor_dev(aval_d.data_ptr())
     ps = np.zeros(6)
@@ -269,7 +274,24 @@ def tensor_roofline(L, fk, aval_d):
     L.spral_ssids_gpu_set_profiling(fk.num, 0)
     peak, src = tf32_peak_tflops()
     if ps[3] <= 0:
-        return None
+        if ak is None or ps[0] <= 0:
+            return None
+        nrow, ncol = ak.front_sizes()
+        cm = (nrow - ncol).astype(np.float64)
+        nbytes = float((cm * (cm + 1) / 2 * 8).sum())
+        hpk, hsrc = hbm_peak_gbs()
+        gbs = nbytes / (ps[0] * 1e-3) / 1e9
+        traffic = None
+        tfile = os.path.join(HERE, "profiles", "contrib_f32_thin_front.md")
+        if os.path.exists(tfile):
+            import re
+            m = re.search(r"dram_bytes_per_byte:\s*([0-9.eE+]+)", open(tfile).read())
+            traffic = float(m.group(1)) * nbytes / max(int(ps[2]), 1) if m else None
+        return {"bound": "hbm", "kernel": "k_syrk<float, 1> (SIMT contribution update)",
+                "achieved": gbs, "peak": hpk, "unit": "GB/s", "frac": gbs / hpk,
+                "traffic": traffic, "peak_source": hsrc, "launches": int(ps[2]),
+                "bytes_per_step": nbytes, "contrib_update_ms": ps[0],
+                "fp32_update_tflops": ps[1] / (ps[0] * 1e-3) / 1e12}
     alg = ps[4] / (ps[3] * 1e-3) / 1e12
     return {"bound": "tensor", "kernel": "k_tc_gemm (tcgen05 kind::tf32, 3xTF32 split)",
             "achieved": 3.0 * alg, "achieved_fp32_update": alg, "peak": peak,
@@ -846,7 +868,7 @@ def run_kkt(args):
         return fk, out
 
     fm, mixed = measure(ssids.PRECISION_MIXED, args.steps)
-    roof = tensor_roofline(L, fm, aval_d)
+    roof = tensor_roofline(L, fm, aval_d, ak)
     # end to end through the C-ABI with host buffers (mixed precision)
     g = ssids.Options(precision=ssids.PRECISION_MIXED, max_refine=20, refine_tol=REFINE_TOL)
     copts = g.cpu_options()

@@ -15,7 +15,12 @@
 //                     that column are added in a fixed order, each child
 //                     column read contiguously and scattered through the
 //                     child->parent row map (rdir), so the result is
-//                     deterministic without atomics.
+//                     deterministic without atomics.  The contribution
+//                     block receives nothing else (A and the delayed
+//                     columns go to the fully-summed part), so every one of
+//                     its columns has a CTA that first zeroes the column's
+//                     lower part and then adds: the zeros stay in L2 for the
+//                     adds, and each entry crosses HBM once as a write.
 #include "ssids_gpu.cuh"
 
 namespace ssids300 {
@@ -92,6 +97,10 @@ __global__ void k_assemble_contrib(const FrontDesc<T>* fds, const int4* cols, co
   const int P = cw.y;
   const bool into_l = P < fp.ncol;
   T* dst = into_l ? fp.L + (int64_t)P * fp.ld : fp.C + (int64_t)(P - fp.ncol) * fp.ldc;
+  if (!into_l) {
+    for (int r = P - fp.ncol + threadIdx.x; r < fp.cm; r += blockDim.x) dst[r] = T(0);
+    __syncthreads();
+  }
   for (int q = cw.z; q < cw.w; ++q) {
     const int2 pr = pairs[q];
     const FrontDesc<T> fc = fds[pr.x];

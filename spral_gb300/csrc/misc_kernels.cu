@@ -21,13 +21,9 @@ __device__ __forceinline__ void zero_range(T* p, int64_t n, int64_t i0, int64_t 
   for (int64_t i = nv * V + i0; i < n; i += stride) p[i] = T(0);
 }
 
-// Zero a level's fronts: L (ld x n, contiguous), the lower triangle of the
-// contribution block (every reader of C -- the extend-add, the SIMT and
-// tensor-core updates -- touches only entries with row >= column) and D.
-// Fronts start 256-byte aligned, so L and D take 16-byte stores; C is
-// cleared one column per warp, each store instruction a contiguous run of
-// 32 entries.  The pass writes each front's storage once per
-// factorisation, at HBM speed.
+// Zero a level's fronts: L (ld x n, contiguous) and D.  Fronts start
+// 256-byte aligned, so the stores are 16 bytes wide.  The contribution
+// blocks are zeroed column by column by the extend-add, which owns them.
 template <typename T>
 __global__ void k_zero_fronts(FrontDesc<T>* fds, const int* fronts) {
   const FrontDesc<T> fd = fds[fronts[blockIdx.y]];
@@ -36,12 +32,6 @@ __global__ void k_zero_fronts(FrontDesc<T>* fds, const int* fronts) {
   const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   zero_range(fd.L, nl, i0, stride);
   zero_range(fd.D, 2 * (int64_t)fd.n, i0, stride);
-  const int lane = threadIdx.x & 31;
-  const int nwarp = (gridDim.x * blockDim.x) >> 5;
-  for (int c = (int)(i0 >> 5); c < fd.cm; c += nwarp) {
-    T* col = fd.C + (int64_t)c * fd.ldc;
-    for (int r = c + lane; r < fd.cm; r += 32) col[r] = T(0);
-  }
 }
 
 __device__ __forceinline__ void atomic_max_pos(double* a, double v) {

@@ -476,7 +476,9 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
       }
       for (int P = 0; P < S->nrow[p]; ++P) {
         gp[S->gp_off[f] + P] = (int)pairs.size();
-        if (per[P].empty()) continue;
+        // every column of the contribution block gets a CTA (the extend-add
+        // also zeroes it), those of the fully-summed part only with children
+        if (per[P].empty() && P < S->ncol[p]) continue;
         int beg = (int)pairs.size();
         for (auto& q : per[P]) pairs.push_back(q);
         cols.push_back(make_int4(f, P, beg, (int)pairs.size()));
@@ -909,8 +911,7 @@ struct Numeric : NumericBase {
           max_n = std::max(max_n, n_[f]);
           max_cm = std::max(max_cm, hfd[f].cm);
           max_ent = std::max<int>(max_ent, (int)(S->nptr[node + 1] - S->nptr[node]));
-          maxz = std::max(maxz, std::max<int64_t>((int64_t)ld_[f] * n_[f],
-                                                  (int64_t)hfd[f].cm * hfd[f].cm));
+          maxz = std::max(maxz, (int64_t)ld_[f] * n_[f]);
         }
         const int* fr = S->d_fronts + f0;
         launch_zero_fronts<T>(d_fd, fr, nf, (int)std::min<int64_t>(maxz, 1 << 30), s);
@@ -1229,8 +1230,7 @@ struct Numeric : NumericBase {
       // assembly
       int64_t maxz = 0;
       for (int f = f0; f < f1; ++f) {
-        int64_t z = std::max<int64_t>((int64_t)ld_[f] * n_[f], (int64_t)hfd[f].cm * hfd[f].cm);
-        maxz = std::max(maxz, z);
+        maxz = std::max(maxz, (int64_t)ld_[f] * n_[f]);
       }
       pmark(tm(), kPhZero, s);
       launch_zero_fronts<T>(d_fd, fr, nf, (int)std::min<int64_t>(maxz, 1 << 30), s);
