@@ -101,6 +101,11 @@ __global__ void k_assemble_contrib(const FrontDesc<T>* fds, const int4* cols, co
     for (int r = P - fp.ncol + threadIdx.x; r < fp.cm; r += blockDim.x) dst[r] = T(0);
     __syncthreads();
   }
+  // A contribution-block column fed by one child receives each entry at most
+  // once: it is stored (v + 0 has the bits of 0 + v, -0 included) instead of
+  // read back and added.
+  const bool store = !into_l && cw.w - cw.z == 1;
+  constexpr int U = 8;  // entries per thread in flight
   for (int q = cw.z; q < cw.w; ++q) {
     const int2 pr = pairs[q];
     const FrontDesc<T> fc = fds[pr.x];
@@ -108,12 +113,24 @@ __global__ void k_assemble_contrib(const FrontDesc<T>* fds, const int4* cols, co
     const int cmc = fc.cm;
     const T* src = fc.C + (int64_t)jc * fc.ldc;
     const int* rd = rdir + rdir_ptr[fc.node];
-    for (int ic = jc + threadIdx.x; ic < cmc; ic += blockDim.x) {
-      const int Q = rd[ic];
-      int r;
-      if (into_l) r = (Q < fp.ncol) ? Q : Q + fp.ndelay_in;
-      else r = Q - fp.ncol;
-      dst[r] += src[ic];
+    for (int ic0 = jc + threadIdx.x; ic0 < cmc; ic0 += U * blockDim.x) {
+      int Q[U];
+      T v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int ic = ic0 + u * blockDim.x;
+        Q[u] = ic < cmc ? rd[ic] : -1;
+        v[u] = ic < cmc ? src[ic] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (Q[u] < 0) continue;
+        int r;
+        if (into_l) r = (Q[u] < fp.ncol) ? Q[u] : Q[u] + fp.ndelay_in;
+        else r = Q[u] - fp.ncol;
+        if (store) dst[r] = v[u] + T(0);
+        else dst[r] += v[u];
+      }
     }
     __syncthreads();
   }
