@@ -208,8 +208,6 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
       if (mine && lo >= q) key = DiagKey<T>::make(blk[C][R], lo * 32 + hi);
       key = warp_max_u64(key);
       if (lane == 0) wkey[warp] = key;
-      // FP64 factors: reciprocals of the trailing diagonal, ready for a 1x1
-      if (kF64 && mine && R == C && lo >= q) rdiag[C] = recip_nr((double)blk[C][C]);
     }
     __syncthreads();
     // ---- decision and the pivot's L column(s) (warp 0; every lane takes the
@@ -262,7 +260,9 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
           const int P = pb;
           T dT;
           if (kF64) {
-            const double d11 = rdiag[P];
+            // the chosen pivot's reciprocal only: FP64 instructions issue
+            // slowly, so the other warps compute none
+            const double d11 = POSDEF ? rdiag[P] : recip_nr((double)blk[P][P]);
             dT = (T)d11;
             if (lane == 0) { dd[2 * q] = d11; dd[2 * q + 1] = 0.0; }
           } else {
