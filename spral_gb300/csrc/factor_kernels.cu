@@ -113,13 +113,13 @@ struct DiagKey<float> {
   }
 };
 
+// unsigned 64-bit maximum over the warp as two 32-bit redux.sync: the high
+// halves, then the low halves of the lanes holding the high maximum
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long k) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const unsigned long long o = __shfl_xor_sync(0xffffffffu, k, off);
-    k = o > k ? o : k;
-  }
-  return k;
+  const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+  const unsigned mh = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? lo : 0u);
+  return ((unsigned long long)mh << 32) | ml;
 }
 
 // 17 warps: thread t < 528 owns the pair {R, C}, R >= C, t = R(R+1)/2 + C
@@ -372,14 +372,6 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
 // ------------------------------------------------------------------------
 constexpr int kDiagWarps = kDiagThreads / 32;
 
-// lexicographic maximum of 64-bit keys over the warp
-__device__ __forceinline__ unsigned long long warp_max_key(unsigned long long k) {
-  const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
-  const unsigned mh = __reduce_max_sync(0xffffffffu, hi);
-  const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? lo : 0u);
-  return ((unsigned long long)mh << 32) | ml;
-}
-
 // key of entry value v at logical (lo, hi), lo <= hi, physical (plo, phi):
 // magnitude, then the inverted column-major position, then the physical
 // indices (never decisive: positions are distinct)
@@ -458,7 +450,7 @@ __global__ void __launch_bounds__(kDiagThreads)
     psz[tid] = 0;
   }
   {
-    const unsigned long long k0 = warp_max_key(mine ? diag_key_f32(a, C, R, C, R) : 0ULL);
+    const unsigned long long k0 = warp_max_u64(mine ? diag_key_f32(a, C, R, C, R) : 0ULL);
     if (lane == 0) wkey[0][warp] = k0;
   }
   int li = R, lj = C;  // logical indices of physical R and C
@@ -468,7 +460,7 @@ __global__ void __launch_bounds__(kDiagThreads)
   for (int q = 0; q < bs;) {
     __syncthreads();
     const int nxt = cur ^ 1;
-    const unsigned long long gk = warp_max_key(lane < kDiagWarps ? wkey[cur][lane] : 0ULL);
+    const unsigned long long gk = warp_max_u64(lane < kDiagWarps ? wkey[cur][lane] : 0ULL);
     const unsigned lo32 = (unsigned)gk;
     const int pos = 1023 - (int)(lo32 >> 10);
     const int bj = pos >> 5, bi = pos & 31;                   // logical column, row
@@ -559,7 +551,7 @@ __global__ void __launch_bounds__(kDiagThreads)
         (mine && lo >= qn)
             ? diag_key_f32(a, lo, hi, li <= lj ? R : C, li <= lj ? C : R)
             : 0ULL;
-    const unsigned long long wk = warp_max_key(k);
+    const unsigned long long wk = warp_max_u64(k);
     if (lane == 0) wkey[nxt][warp] = wk;
     if (warp == 0) {
       int v = mp[lane];
