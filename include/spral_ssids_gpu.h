@@ -120,6 +120,27 @@ void spral_ssids_gpu_subtree_enquire_dbl(bool posdef, const void* numeric, int* 
  * cf. spral_ssids_cpu_subtree_alter_dbl (NumericSubtree.cxx:204). */
 void spral_ssids_gpu_subtree_alter_dbl(bool posdef, void* numeric, const double* d);
 
+/* Replaces gpu_numeric_subtree%get_contrib (src/ssids/gpu/subtree.f90:522)
+ * with the copy of transfer_contrib (src/ssids/gpu/factor.f90:155-221);
+ * arguments of spral_ssids_cpu_subtree_get_contrib_dbl
+ * (src/ssids/cpu/NumericSubtree.cxx:218).  For a subtree whose root has a
+ * parent in another subtree: the root's contribution block (n x n, full
+ * symmetric, ldval = n), its 1-based rows (rlist), and the root's delayed
+ * columns (delay_perm: 1-based variables; delay_val: each column from its
+ * diagonal down, the ndelay x ndelay block then the n contribution rows,
+ * leading dimension lddelay = n + ndelay).  Pointers are NULL when empty and
+ * stay valid until free_contrib or the handle's destruction; FP32 factors
+ * are widened to FP64.  Returns 0 or -51 (a CUDA error; the reference's
+ * function returns nothing, so a Fortran subroutine binding may ignore it). */
+int spral_ssids_gpu_subtree_get_contrib_dbl(bool posdef, void* numeric, int* n,
+                                            const double** val, int* ldval, const int** rlist,
+                                            int* ndelay, const int** delay_perm,
+                                            const double** delay_val, int* lddelay);
+
+/* Replaces gpu_free_contrib (src/ssids/gpu/subtree.f90:540); cf.
+ * spral_ssids_cpu_subtree_free_contrib_dbl (NumericSubtree.cxx:248). */
+void spral_ssids_gpu_subtree_free_contrib_dbl(bool posdef, void* numeric);
+
 /* Same-pattern refactorisation with values already in device memory (no
  * reference counterpart: the reference re-creates the numeric subtree and
  * copies aval host-to-device each time, src/ssids/gpu/subtree.f90:375). */

@@ -80,6 +80,8 @@ def _declare(L):
         f(f"spral_ssids_gpu_subtree_solve_{nm}_dbl", I, B, P, I, P, I)
     f("spral_ssids_gpu_subtree_enquire_dbl", None, B, P, P, P)
     f("spral_ssids_gpu_subtree_alter_dbl", None, B, P, P)
+    f("spral_ssids_gpu_subtree_get_contrib_dbl", I, B, P, P, P, P, P, P, P, P, P)
+    f("spral_ssids_gpu_subtree_free_contrib_dbl", None, B, P)
     f("spral_ssids_gpu_set_options", I, P, ctypes.POINTER(GpuOptions))
     f("spral_ssids_gpu_refactor_dev", I, P, P, ctypes.POINTER(ThreadStats), P)
     f("spral_ssids_gpu_refactor", I, P, P, P, ctypes.POINTER(ThreadStats))

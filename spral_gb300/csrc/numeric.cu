@@ -565,6 +565,12 @@ struct NumericBase {
   virtual int debug_front(int node, int* info, double* L, double* D, int* perm) = 0;
   virtual int node_inertia(int* out) = 0;
   virtual cudaStream_t get_stream() const = 0;
+  virtual int get_contrib() = 0;
+  // the subtree root's contribution for a parent outside the subtree, host
+  // copies filled by get_contrib() and kept until free_contrib
+  std::vector<double> contrib_val, contrib_delay;
+  std::vector<int> contrib_rlist, contrib_perm;
+  int contrib_n = 0, contrib_ndelay = 0, contrib_lddelay = 0;
   DevBuf<double> hsolve;  // device copy of host right-hand sides (host-buffer solves)
   // FP64 refactorisations taken by the FP32-factor path's refined solves
   int fallbacks = 0;
@@ -1029,9 +1035,14 @@ struct Numeric : NumericBase {
     stats.not_first_pass = nfp;
     stats.not_second_pass = nsp;
     stats.flag = 0;
-    // delays left at a root are unrecoverable
-    for (int f = 0; f < S->nnodes; ++f)
-      if (S->parent[S->node_of[f]] < 0 && nelim_[f] < n_[f]) stats.flag = -5;
+    // delays left at a root of the tree are unrecoverable; a subtree root
+    // with rows beyond its columns has its parent in another subtree, which
+    // takes the delays with the contribution block (get_contrib)
+    for (int f = 0; f < S->nnodes; ++f) {
+      const int node = S->node_of[f];
+      if (S->parent[node] < 0 && S->nrow[node] == S->ncol[node] && nelim_[f] < n_[f])
+        stats.flag = -5;
+    }
     if (stats.num_zero > 0 && stats.flag == 0) stats.flag = 7;
     if (posdef) {
       if (stats.num_neg > 0 || stats.num_zero > 0 || stats.num_two > 0) stats.flag = -6;
@@ -1613,6 +1624,63 @@ struct Numeric : NumericBase {
     CK(cudaMemcpy(P.data(), hfd[f].perm, P.size() * sizeof(int), cudaMemcpyDeviceToHost));
   }
 
+  // The subtree root's generalised element for a parent in another subtree,
+  // as transfer_contrib (src/ssids/gpu/factor.f90:155-221) hands it over and
+  // NumericSubtree::get_contrib (src/ssids/cpu/NumericSubtree.hxx:518-532)
+  // describes it: the cm x cm contribution block (full, leading dimension
+  // cm; the device holds its lower triangle, mirrored here), the 1-based
+  // rows it belongs to, and the delayed columns (1-based perm entries; each
+  // column from its diagonal down: the ndelay x ndelay block, then the cm
+  // contribution rows; leading dimension cm + ndelay).  FP32 factors are
+  // widened to FP64.  Returns 0 or -51.
+  int get_contrib() override {
+    contrib_val.clear(); contrib_delay.clear(); contrib_rlist.clear(); contrib_perm.clear();
+    contrib_n = contrib_ndelay = contrib_lddelay = 0;
+    const int root = S->nnodes - 1;
+    if (root < 0 || nelim_.empty()) return 0;
+    const int f = S->front_of[root];
+    const int cm = S->nrow[root] - S->ncol[root];
+    const int nel = nelim_[f], nd = n_[f] - nel;
+    if (cudaStreamSynchronize(stream) != cudaSuccess) { cudaGetLastError(); return -51; }
+    contrib_n = cm;
+    if (cm > 0) {
+      std::vector<T> c((size_t)cm * cm);
+      if (cudaMemcpy(c.data(), hfd[f].C, c.size() * sizeof(T), cudaMemcpyDeviceToHost) !=
+          cudaSuccess) { cudaGetLastError(); return -51; }
+      contrib_val.resize((size_t)cm * cm);
+      for (int j = 0; j < cm; ++j)
+        for (int i = j; i < cm; ++i) {
+          const double v = (double)c[(size_t)j * hfd[f].ldc + i];
+          contrib_val[(size_t)j * cm + i] = v;
+          contrib_val[(size_t)i * cm + j] = v;
+        }
+      contrib_rlist.resize(cm);
+      const int64_t r0 = S->rptr[root] + S->ncol[root];
+      for (int i = 0; i < cm; ++i) contrib_rlist[i] = S->rlist[r0 + i] + 1;
+    }
+    if (nd > 0) {
+      std::vector<int> P(n_[f]);
+      std::vector<T> Lc((size_t)ld_[f] * nd);
+      if (cudaMemcpy(P.data(), hfd[f].perm, P.size() * sizeof(int), cudaMemcpyDeviceToHost) !=
+              cudaSuccess ||
+          cudaMemcpy(Lc.data(), hfd[f].L + (size_t)nel * ld_[f], Lc.size() * sizeof(T),
+                     cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return -51;
+      }
+      contrib_ndelay = nd;
+      contrib_lddelay = cm + nd;
+      contrib_perm.resize(nd);
+      contrib_delay.resize((size_t)contrib_lddelay * nd);
+      for (int i = 0; i < nd; ++i) {
+        contrib_perm[i] = P[nel + i] + 1;
+        for (int r = 0; r < contrib_lddelay; ++r)
+          contrib_delay[(size_t)i * contrib_lddelay + r] = (double)Lc[(size_t)i * ld_[f] + nel + r];
+      }
+    }
+    return 0;
+  }
+
   // node order as the CPU enquire (NumericSubtree.hxx:402-445)
   void enquire(int* piv_order, double* d) override {
     std::vector<double> D;
@@ -1859,6 +1927,36 @@ void spral_ssids_gpu_subtree_alter_dbl(bool posdef, void* numeric, const double*
   } catch (CudaFail const& e) {
     map_cuda_error(e, nullptr);
   }
+}
+
+int spral_ssids_gpu_subtree_get_contrib_dbl(bool posdef, void* numeric, int* n,
+                                            const double** val, int* ldval, const int** rlist,
+                                            int* ndelay, const int** delay_perm,
+                                            const double** delay_val, int* lddelay) {
+  (void)posdef;
+  auto* N = static_cast<NumericBase*>(numeric);
+  if (!N) return -1;
+  const int rc = N->get_contrib();
+  *n = N->contrib_n;
+  *ldval = N->contrib_n;
+  *val = N->contrib_val.empty() ? nullptr : N->contrib_val.data();
+  *rlist = N->contrib_rlist.empty() ? nullptr : N->contrib_rlist.data();
+  *ndelay = N->contrib_ndelay;
+  *delay_perm = N->contrib_perm.empty() ? nullptr : N->contrib_perm.data();
+  *delay_val = N->contrib_delay.empty() ? nullptr : N->contrib_delay.data();
+  *lddelay = N->contrib_lddelay;
+  return rc;
+}
+
+void spral_ssids_gpu_subtree_free_contrib_dbl(bool posdef, void* numeric) {
+  (void)posdef;
+  auto* N = static_cast<NumericBase*>(numeric);
+  if (!N) return;
+  std::vector<double>().swap(N->contrib_val);
+  std::vector<double>().swap(N->contrib_delay);
+  std::vector<int>().swap(N->contrib_rlist);
+  std::vector<int>().swap(N->contrib_perm);
+  N->contrib_n = N->contrib_ndelay = N->contrib_lddelay = 0;
 }
 
 int spral_ssids_gpu_debug_front(const void* numeric, int node, int* info, double* L, double* D,
