@@ -136,8 +136,6 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
                                                            bool action, double small) {
   constexpr bool kF64 = sizeof(T) == 8;
   const int f = fronts[blockIdx.x];
-  pdl_wait();
-  pdl_trigger();
   FrontState* st = &sts[f];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // owned pair (physical R >= C)
@@ -156,8 +154,10 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
   __shared__ int s_state[2];
   __shared__ FrontDesc<T> fd;
 
+  if (tid == 0) fd = fds[f];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
   if (tid == 0) {
-    fd = fds[f];
     int p, end;
     if (step == 0) {
       p = 0;
@@ -387,8 +387,6 @@ __global__ void __launch_bounds__(kDiagThreads)
     k_app_diag_f32(FrontDesc<float>* fds, FrontState* sts, const int* fronts, int step,
                    bool action, double small) {
   const int f = fronts[blockIdx.x];
-  pdl_wait();
-  pdl_trigger();
   FrontState* st = &sts[f];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int R = (int)((sqrtf(8.0f * tid + 1.0f) - 1.0f) * 0.5f);
@@ -407,8 +405,10 @@ __global__ void __launch_bounds__(kDiagThreads)
   __shared__ int s_state[2];
   __shared__ FrontDesc<float> fd;
 
+  if (tid == 0) fd = fds[f];  // written by the host before the launch
+  pdl_wait();
+  pdl_trigger();
   if (tid == 0) {
-    fd = fds[f];
     int p, end;
     if (step == 0) {
       p = 0;
@@ -629,13 +629,13 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
                                                           const int* fronts, double u,
                                                           double small, int napply) {
   const int f = fronts[blockIdx.y];
+  FrontDesc<T> fd = fds[f];  // written by the host before the launch
   pdl_wait();
   pdl_trigger();
   FrontState* st = &sts[f];
   const int bs = st->bs;
   if (bs == 0) return;
   const int p = st->p;
-  FrontDesc<T> fd = fds[f];
   if ((int)blockIdx.x >= napply) {
     // block permutation of rows [p, p+bs) in the eliminated columns [0, p)
     if (p == 0) return;
@@ -1022,11 +1022,11 @@ __device__ __forceinline__ int swap_partner(const SwapRanges& s, int x) {
 template <typename T>
 __global__ void k_app_swap(FrontDesc<T>* fds, const FrontState* sts, const int* fronts) {
   const int f = fronts[blockIdx.x];
+  FrontDesc<T> fd = fds[f];  // written by the host before the launch
   pdl_wait();
   pdl_trigger();
   const FrontState st = sts[f];
   if (st.bs == 0 || st.bs == st.npass) return;
-  FrontDesc<T> fd = fds[f];
   SwapRanges sr = swap_ranges(st);
   const int nl = 2 * sr.npairs;
   int* ib = reinterpret_cast<int*>(fd.swapbuf + (int64_t)nl * fd.ld);
