@@ -624,8 +624,15 @@ constexpr int kPermCols = 8;
 // ------------------------------------------------------------------------
 // k_app_apply: rows below the block; solve, scale, threshold test
 // ------------------------------------------------------------------------
+// threads per apply CTA and rows per tile: FP32, one row per thread (64);
+// FP64, 32 rows shared by 4 warps (column blocks, see the solve below)
 template <typename T>
-__global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, FrontState* sts,
+__host__ __device__ constexpr int apply_threads() { return sizeof(T) == 8 ? 128 : kApplyRows; }
+template <typename T>
+__host__ __device__ constexpr int apply_rows() { return sizeof(T) == 8 ? 32 : kApplyRows; }
+
+template <typename T>
+__global__ void __launch_bounds__(apply_threads<T>()) k_app_apply(FrontDesc<T>* fds, FrontState* sts,
                                                           const int* fronts, double u,
                                                           double small, int napply) {
   const int f = fronts[blockIdx.y];
@@ -667,25 +674,26 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
   // driven by the pivot kind of each column.
   constexpr int VW = 16 / sizeof(T);  // elements per 16-byte vector
   constexpr int LT = kBlk + VW;       // padded row of l11t
+  constexpr int NT = apply_threads<T>(), RT = apply_rows<T>();
   __shared__ __align__(16) T l11t[kBlk][LT];
-  __shared__ T xs[kBlk][kApplyRows];
+  __shared__ T xs[kBlk][RT];
   __shared__ double dd[2 * kBlk + 2];
   __shared__ float ddf[kBlk];  // FP32 copies of the 1x1 D^{-1} entries
   __shared__ int kind[kBlk];   // 0 1x1, 1 first of a 2x2, 2 second of a 2x2, 3 zero pivot
   __shared__ int lp[kBlk];
   {
     // all loads first (one latency), then the shared-memory stores
-    constexpr int PER = kBlk * kBlk / kApplyRows;  // 16
+    constexpr int PER = kBlk * kBlk / NT;  // 16 (FP32) or 8 (FP64)
     double v[PER];
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-      const int i = threadIdx.x + k * kApplyRows;
+      const int i = threadIdx.x + k * NT;
       const int c = i / kBlk, r = i % kBlk;
       v[k] = (r > c && r < bs && c < bs) ? fd.step[c * kBlk + r] : 0.0;
     }
 #pragma unroll
     for (int k = 0; k < PER; ++k) {
-      const int i = threadIdx.x + k * kApplyRows;
+      const int i = threadIdx.x + k * NT;
       l11t[i / kBlk][i % kBlk] = (T)v[k];
     }
   }
@@ -715,44 +723,86 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
     return b > tkey && b <= 0x7ff0000000000000LL;
   };
   int myfail = bs;
-  const int t = threadIdx.x;
-  for (int tile = blockIdx.x; tile * kApplyRows < nrows; tile += napply) {
-    const int rr = tile * kApplyRows + t;
+  // row of the tile: FP32, thread t; FP64, lane t of each of the 4 warps,
+  // warp w owning columns [8w, 8w+8)
+  const int t = (sizeof(T) == 8) ? (threadIdx.x & 31) : threadIdx.x;
+  for (int tile = blockIdx.x; tile * RT < nrows; tile += napply) {
+    const int rr = tile * RT + t;
     const bool valid = rr < nrows;
     const int r = r0 + rr;
-    T x[kBlk];
+    if constexpr (sizeof(T) == 8) {
+      // FP64: one warp's chain of 496 dependent FMAs per row tile waits on
+      // the FP64 pipe of its SM sub-partition (~75 cycles a warp
+      // instruction), so the columns are split over 4 warps in blocks of 8
+      // and solved block by block: warp b solves its diagonal block, then
+      // the warps right of it subtract block b.  Each x[j] still takes its
+      // terms in the order k = 0, 1, ..., j-1 (the single-warp result, bit
+      // for bit); the critical path is 4 x 28 + 3 x 64 FMAs.
+      constexpr int CB = 8;
+      const int w = threadIdx.x >> 5, c0 = CB * w;
+      T x[CB];
 #pragma unroll
-    for (int j = 0; j < kBlk; ++j)
-      x[j] = (valid && j < bs) ? fd.L[(int64_t)(p + lp[j]) * fd.ld + r] : T(0);
-    // right-looking: after x[k] is final, the updates of x[k+1..] are
-    // independent FMAs; L(j, k) for j > k comes in 16-byte vectors (the
-    // zero entries on and above the diagonal change nothing)
+      for (int i = 0; i < CB; ++i)
+        x[i] = (valid && c0 + i < bs) ? fd.L[(int64_t)(p + lp[c0 + i]) * fd.ld + r] : T(0);
+      for (int b = 0; b < kBlk / CB && CB * b < bs; ++b) {
+        if (w == b) {
 #pragma unroll
-    for (int k = 0; k < kBlk - 1; ++k) {
-      if (k + 1 < bs) {
-        const T xk = x[k];
+          for (int k = 0; k < CB - 1; ++k) {
+            const T xk = x[k];
 #pragma unroll
-        for (int j0 = ((k + 1) / VW) * VW; j0 < kBlk; j0 += VW) {
-          T lv[VW];
-          if constexpr (sizeof(T) == 4) {
-            const float4 q = *reinterpret_cast<const float4*>(&l11t[k][j0]);
-            lv[0] = q.x; lv[1] = q.y; lv[2] = q.z; lv[3] = q.w;
-          } else {
-            const double2 q = *reinterpret_cast<const double2*>(&l11t[k][j0]);
-            lv[0] = q.x; lv[1] = q.y;
+            for (int i = k + 1; i < CB; ++i) x[i] -= xk * l11t[c0 + k][c0 + i];
           }
 #pragma unroll
-          for (int v = 0; v < VW; ++v)
-            if (j0 + v > k) x[j0 + v] -= xk * lv[v];
+          for (int i = 0; i < CB; ++i) xs[c0 + i][t] = x[i];
+        }
+        __syncthreads();
+        if (w > b) {
+#pragma unroll
+          for (int k = 0; k < CB; ++k) {
+            const T xk = xs[CB * b + k][t];
+#pragma unroll
+            for (int i = 0; i < CB; i += 2) {
+              const double2 q = *reinterpret_cast<const double2*>(&l11t[CB * b + k][c0 + i]);
+              x[i] -= xk * (T)q.x;
+              x[i + 1] -= xk * (T)q.y;
+            }
+          }
         }
       }
-    }
+      // blocks past bs were never solved: their columns are not used
+    } else {
+      T x[kBlk];
 #pragma unroll
-    for (int j = 0; j < kBlk; ++j) xs[j][t] = x[j];  // column t is this thread's
+      for (int j = 0; j < kBlk; ++j)
+        x[j] = (valid && j < bs) ? fd.L[(int64_t)(p + lp[j]) * fd.ld + r] : T(0);
+      // right-looking: after x[k] is final, the updates of x[k+1..] are
+      // independent FMAs; L(j, k) for j > k comes in 16-byte vectors (the
+      // zero entries on and above the diagonal change nothing)
+#pragma unroll
+      for (int k = 0; k < kBlk - 1; ++k) {
+        if (k + 1 < bs) {
+          const T xk = x[k];
+#pragma unroll
+          for (int j0 = ((k + 1) / VW) * VW; j0 < kBlk; j0 += VW) {
+            T lv[VW];
+            const float4 q = *reinterpret_cast<const float4*>(&l11t[k][j0]);
+            lv[0] = q.x; lv[1] = q.y; lv[2] = q.z; lv[3] = q.w;
+#pragma unroll
+            for (int v = 0; v < VW; ++v)
+              if (j0 + v > k) x[j0 + v] -= xk * lv[v];
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kBlk; ++j) xs[j][t] = x[j];  // column t is this thread's
+    }
     if (valid) {
       T* W = fd.W + rr;
+      // FP32: every column of the row; FP64: the warp's 8 columns
+      const int jb = (sizeof(T) == 8) ? 8 * (threadIdx.x >> 5) : 0;
+      const int je = (sizeof(T) == 8) ? min(jb + 8, bs) : bs;
 #pragma unroll 1
-      for (int j = 0; j < bs; ++j) {
+      for (int j = jb; j < je; ++j) {
         const int kd = kind[j];
         if (kd == 2) continue;  // second half of a 2x2: handled with the first
         const T xj = xs[j][t];
@@ -792,6 +842,7 @@ __global__ void __launch_bounds__(kApplyRows) k_app_apply(FrontDesc<T>* fds, Fro
         }
       }
     }
+    if constexpr (sizeof(T) == 8) __syncthreads();  // the next tile rewrites xs
   }
   // block min -> atomicMin
   for (int off = 16; off > 0; off >>= 1) myfail = min(myfail, __shfl_xor_sync(0xffffffffu, myfail, off));
@@ -1413,13 +1464,14 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
   }
   note_launches(1);
   // apply (+ row permutation of the eliminated part in extra CTAs)
-  const int napply = std::max(1, cdiv(max_rows, kApplyRows));
+  const int napply = std::max(1, cdiv(max_rows, apply_rows<T>()));
   const int pcols = step * kBlk;  // upper bound on p
   const int nperm =
-      pcols > 0 ? std::max(1, std::min(cdiv(pcols, (kApplyRows / 32) * kPermCols), 128)) : 0;
+      pcols > 0 ? std::max(1, std::min(cdiv(pcols, (apply_threads<T>() / 32) * kPermCols), 128))
+                : 0;
   pmark(tm, kPhApply, s);
-  launch_pdl(k_app_apply<T>, dim3(napply + nperm, nf), kApplyRows, 0, s, fd, st, fronts, u, small,
-             napply);
+  launch_pdl(k_app_apply<T>, dim3(napply + nperm, nf), apply_threads<T>(), 0, s, fd, st, fronts,
+             u, small, napply);
   note_launches(1);
   // trailing update and fixup in one launch (tile estimate assumes no failed
   // columns so far; after failures the trailing region is wider and the
