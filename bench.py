@@ -145,6 +145,23 @@ def dist_setup(args):
     return world, rank, local
 
 
+def max_over_ranks(ms, dist, device):
+    """The job's time per step: the slowest rank's (all_reduce MAX); `dist`
+    is None on one rank."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, ms):
+    """Whole-job throughput of `world` independent replicas: all ranks'
+    solves over the slowest rank's time per step (ms)."""
+    return world * 1000.0 / ms
+
+
 def cpu_reference_step_fn(ak, val, b, use_ref):
     import oracle
     if use_ref:
@@ -360,10 +377,7 @@ def run_gpu(args):
         barrier()
         ms = ev0.elapsed_time(ev1) / args.steps
         launches = L.spral_ssids_gpu_launch_count() - lc0
-        if dist is not None:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, dist, dev)
         x = x_d.cpu().numpy().T
         xu = np.empty_like(x)
         xu[ak.invp, :] = x
@@ -386,7 +400,7 @@ def run_gpu(args):
     fk = ssids.Fkeep(ak, val, opts64)
     inform = fk.inform
     ms, per, launches, clocks, bwd, fp64_iters = measure(fk, mixed=False)
-    value = world * 1000.0 / ms
+    value = replica_value(world, ms)
     factor_tflops = inform.num_flops / (fk.timing()[0] * 1e-3) / 1e12
 
     # roofline of the dominant kernel: contribution GEMM, timed per launch
@@ -433,11 +447,8 @@ def run_gpu(args):
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
     e2e_ms = 1000.0 * sum(e2e_times) / len(e2e_times)
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e = {"value": world * 1000.0 / e2e_ms, "unit": "solves/s",
+    e2e_ms = max_over_ranks(e2e_ms, dist, dev)
+    e2e = {"value": replica_value(world, e2e_ms), "unit": "solves/s",
            "h2d_bytes_per_step": int(val.nbytes + n * nrhs * 8),
            "d2h_bytes_per_step": int(n * nrhs * 8),
            "path": "spral_ssids_gpu_create_num_subtree_dbl + spral_ssids_gpu_solve_refined "
