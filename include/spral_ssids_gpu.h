@@ -9,7 +9,7 @@
  * src/ssids/cpu/NumericSubtree.cxx:29-262), so that a Fortran binding can
  * call them the way src/ssids/cpu/subtree.f90 calls the CPU ones.
  *
- * Conventions (as at the reference boundary, SURVEYed in
+ * Conventions (as at the reference boundary, described in
  * src/ssids/cpu/SymbolicSubtree.hxx:20-48): all index arrays are 1-based and
  * Fortran-ordered; x is column-major n x nrhs in pivot order (already
  * permuted by invp and scaled by the caller, src/ssids/fkeep.F90:252-266).
