@@ -223,6 +223,12 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def rel_diff(x, xref):
+    """max |x - xref| / max |xref| (the solution's error against the FP64
+    CPU solution of the same right-hand sides)."""
+    return float(np.abs(x - xref).max() / max(np.abs(xref).max(), 1e-300))
+
+
 def hbm_peak_gbs():
     try:
         pk = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
@@ -382,6 +388,7 @@ def run_gpu(args):
         xu = np.empty_like(x)
         xu[ak.invp, :] = x
         bwd = float(M.scaled_bwd_error(ptr, row, val, xu, b).max())
+        measure.x = xu
         return ms, per, launches, clocks, bwd, it.value
 
     if args.mixed_only:
@@ -400,6 +407,7 @@ def run_gpu(args):
     fk = ssids.Fkeep(ak, val, opts64)
     inform = fk.inform
     ms, per, launches, clocks, bwd, fp64_iters = measure(fk, mixed=False)
+    x_fp64 = measure.x
     value = replica_value(world, ms)
     factor_tflops = inform.num_flops / (fk.timing()[0] * 1e-3) / 1e12
 
@@ -459,6 +467,7 @@ def run_gpu(args):
         fm = ssids.Fkeep(ak, val, ssids.Options(precision=ssids.PRECISION_MIXED, max_refine=20,
                                                  refine_tol=REFINE_TOL))
         mms, mper, mlaunch, _, mbwd, mit = measure(fm, mixed=True)
+        x_mixed = measure.x
         mixed = {"value": world * 1000.0 / mms, "unit": "solves/s", "ms_per_step": mms,
                  "bwd_err": mbwd, "refine_iters": mit, "num_neg": fm.inform.num_neg,
                  "factor_ms": float(fm.timing()[0]),
@@ -470,6 +479,7 @@ def run_gpu(args):
         fm.free()
 
     cpu = None
+    rel_fp64 = rel_mixed = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
         oracle.build()
@@ -481,6 +491,12 @@ def run_gpu(args):
                "sample": "one full factor+solve of the workload (OpenBLAS threads = all cores)",
                "bwd_err": float(M.scaled_bwd_error(ptr, row, val, xc, b).max()),
                "num_neg": stc["num_neg"]}
+        # each arm's solution against the FP64 CPU solution of the same b:
+        # max |x - x_cpu| / max |x_cpu| over all right-hand sides
+        rel_fp64 = rel_diff(x_fp64, xc)
+        if mixed is not None:
+            rel_mixed = rel_diff(x_mixed, xc)
+            mixed["rel_vs_oracle"] = rel_mixed
 
     if rank == 0:
         neg_exact, _, _ = M.laplacian_eig_count_3d(args.grid, args.grid, args.grid, args.shift)
@@ -492,7 +508,8 @@ def run_gpu(args):
                                             "num_neg_exact": neg_exact,
                                             "num_delay": inform.num_delay,
                                             "refine_iters": fp64_iters,
-                                            "num_flops": inform.num_flops}),
+                                            "num_flops": inform.num_flops,
+                                            "rel_vs_oracle": rel_fp64}),
                 "factor_tflops": factor_tflops,
                 "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99)),
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,

@@ -245,8 +245,11 @@ int spral_ssids_gpu_ldlt_app_factor(int m, int n, int* perm_dev, double* a_dev, 
  * can stall the device): the workspace is a fixed 3 MiB device array inside
  * the library, present on every GPU that loads it until the process exits.
  * lda <= 1024 (so m <= 1024); larger fronts return
- * SPRAL_SSIDS_GPU_NOALLOC_TOO_LARGE.  The first call on a device looks up
- * the array's device address and should come before any stream capture.
+ * SPRAL_SSIDS_GPU_NOALLOC_TOO_LARGE (n = 0 returns 0 whatever lda is, as
+ * the allocating call does).  The first call on a device looks up the
+ * array's device address and keeps it; a process that resets the device
+ * (cudaDeviceReset) must not call this entry point on it again.  Like the
+ * allocating call, it synchronises its stream before returning.
  * All calls share the array: calls that overlap on the GPU race and must be
  * serialised by the caller.  Calls no cudaMalloc, cudaFree or allocating
  * library routine. */

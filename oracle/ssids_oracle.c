@@ -520,12 +520,43 @@ void* oracle_factor(int n, int nnodes, const int* sptr, const int* sparent, cons
     nd->rlist = &rlist[rptr[i] - 1];
     nd->parent = sparent[i] - 1;
   }
-  /* child lists in reverse so they come off in increasing order */
-  for (int i = nnodes - 1; i >= 0; --i) {
+  /* child lists built as SymbolicSubtree.hxx:42-47 builds them (each node
+   * is pushed onto its parent's list in increasing order), so children come
+   * off in decreasing order: delayed columns are appended, and contributions
+   * added, last child first */
+  for (int i = 0; i < nnodes; ++i) {
     int par = F->nodes[i].parent;
     if (par > nnodes) par = nnodes;
     F->nodes[i].next_child = F->nodes[par].first_child;
     F->nodes[par].first_child = i;
+  }
+  /* Small leaf subtrees (SymbolicSubtree.hxx:56-82): subtrees below
+   * small_subtree_threshold flops are factored node by node with TPP only
+   * (SmallLeafNumericSubtree.hxx:345-375, ldlt_tpp_factor from column 0). */
+  char* insl = (char*)calloc((size_t)nnodes + 1, 1);
+  {
+    int64_t* fl = (int64_t*)calloc((size_t)nnodes + 1, sizeof(int64_t));
+    for (int ni = 0; ni < nnodes; ++ni) {
+      const int64_t nr = F->nodes[ni].nrow;
+      for (int k = 0; k < F->nodes[ni].ncol; ++k) fl[ni] += (nr - k) * (nr - k);
+      int par = F->nodes[ni].parent;
+      if (par > nnodes || par < 0) par = nnodes;
+      fl[par] += fl[ni];
+    }
+    for (int ni = 0; ni < nnodes;) {
+      if (F->nodes[ni].first_child != -1) { ++ni; continue; }
+      int last = ni;
+      for (int cur = ni; cur < nnodes;) {
+        if (fl[cur] >= opt->small_subtree_threshold) break;
+        last = cur;
+        int par = F->nodes[cur].parent;
+        cur = (par > nnodes || par < 0) ? nnodes : par;
+      }
+      if (last == ni) { ++ni; continue; }
+      for (int i = ni; i <= last; ++i) insl[i] = 1;
+      ni = last + 1;
+    }
+    free(fl);
   }
   int* map = (int*)malloc(sizeof(int) * ((size_t)n + 1));
   int maxm = 1;
@@ -602,11 +633,18 @@ void* oracle_factor(int n, int nnodes, const int* sptr, const int* sparent, cons
       ldw = (double*)malloc(sizeof(double) * scratch);
     }
     int nelim = 0, napp = 0;
-    if (opt->pivot_method != 3) {
+    if (insl[ni]) {
+      double* l0 = (double*)malloc(sizeof(double) * (size_t)m);
+      double* l1 = (double*)malloc(sizeof(double) * (size_t)m);
+      int got = tpp_factor(0, m, nn, L, ld, D, nd->perm, opt->action, opt->u, opt->small, l0, l1);
+      free(l0); free(l1);
+      if (got < 0) { stats->flag = -5; break; }
+      nelim = got;
+    } else if (opt->pivot_method != 3) {
       nelim = app_factor(m, nn, L, ld, D, nd->perm, opt->action, opt->u, opt->small, bk, xw, ldw, &napp);
       if (nelim < 0) { stats->flag = -5; break; }
     }
-    if (nelim < nn) {
+    if (nelim < nn && !insl[ni]) {
       if (opt->pivot_method != 3) stats->not_first_pass += nn - nelim;
       if (m == nn || opt->pivot_method == 3 || opt->failed_pivot_method == 1) {
         double* l0 = (double*)malloc(sizeof(double) * (size_t)m);
@@ -638,7 +676,7 @@ void* oracle_factor(int n, int nnodes, const int* sptr, const int* sparent, cons
     if (m > stats->maxfront) stats->maxfront = m;
     if (nn > stats->maxsupernode) stats->maxsupernode = nn;
   }
-  free(map); free(bk); free(xw); free(ldw);
+  free(map); free(bk); free(xw); free(ldw); free(insl);
   if (stats->flag < 0) { F->stats = *stats; return F; }
   /* inertia (NumericSubtree.hxx:249-280) */
   for (int ni = 0; ni < nnodes; ++ni) {

@@ -187,7 +187,11 @@ void* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
 
 // Device address of the scratch array on the current device.  The host-side
 // symbol g_noalloc_scratch is only a stand-in and must never reach a kernel;
-// the address is looked up once per device, with that device current.
+// the address is looked up once per device, with that device current, and
+// kept for the life of the process.  cudaDeviceReset (or anything else that
+// destroys the device's primary context) unloads the module, after which the
+// array may come back at another address: a process that resets a device
+// must not call this entry point on it again.
 int noalloc_scratch_address(void** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return -51; }
@@ -218,8 +222,9 @@ extern "C" {
 //  * lda must be at most 1024 (so m <= 1024); larger fronts are refused with
 //    SPRAL_SSIDS_GPU_NOALLOC_TOO_LARGE (-60) and a message on stderr.
 //  * The first call on each device looks up the scratch array's device
-//    address (with that device current); make that first call before any
-//    stream capture begins.
+//    address (with that device current) and keeps it for later calls.
+//  * Like spral_ssids_gpu_ldlt_app_factor, the call synchronises its stream
+//    and reads the front's elimination count back before it returns.
 //  * All calls share the one array and it keeps the previous call's contents;
 //    the per-call state that must start from zero is cleared by each call.
 //    Calls whose GPU work overlaps (different host threads or streams at the
@@ -233,13 +238,13 @@ int spral_ssids_gpu_ldlt_app_factor_noalloc(int m, int n, int* perm_dev, double*
   if (m < n || n < 0) return -1;
   if (lda < m) return -4;
   if (m > n && upd_dev && ldupd < m - n) return -9;
+  if (n == 0) return 0;  // nothing to factor: the same result as the allocating call
   if (lda > kNoAllocMaxLda || dense_workspace_bytes(m, n, lda) > kNoAllocScratchBytes) {
     fprintf(stderr,
             "spral_gb300: front too large for the fixed scratch (lda=%d, limit %d)\n", lda,
             kNoAllocMaxLda);
     return -60;
   }
-  if (n == 0) return 0;
   void* base = nullptr;
   const int st = noalloc_scratch_address(&base);
   if (st != 0) return st;

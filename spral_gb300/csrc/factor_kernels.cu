@@ -21,6 +21,7 @@
 // columns with threshold partial pivoting (ldlt_tpp.cxx:166-270) where the
 // reference does (root fronts or failed_pivot_method = tpp); k_calc_ld and
 // k_syrk (contrib) form the contribution block; k_stats counts inertia.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -1229,25 +1230,20 @@ __device__ void tpp_apply(FrontDesc<T>& fd, int nel, int ps, double d11, double 
   __syncthreads();
 }
 
+// The TPP loop of ldlt_tpp_factor on the columns [nel, n) of the front
+// described by fd (whose L and W may point to global or shared memory).
+// Returns the number of columns eliminated in total, or -1 for a singular
+// front with action == false.
 template <typename T>
-__global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontState* sts,
-                                                     const int* fronts, bool action, double u,
-                                                     double small, bool all_fronts) {
-  const int f = fronts[blockIdx.x];
-  FrontState* st = &sts[f];
-  FrontDesc<T> fd = fds[f];
-  if (st->status != kDevOk) return;
-  if (st->nelim >= fd.n) return;
-  if (!(all_fronts || fd.m == fd.n)) return;
-  __shared__ double red[kTppThreads / 32];
-  __shared__ int s_t;
-  int nel = st->nelim;
+__device__ int tpp_body(FrontDesc<T>& fd, int nel, bool action, double u, double small,
+                        double* red, int* s_t_ptr) {
+  int& s_t = *s_t_ptr;
   const int n = fd.n, m = fd.m;
   const T* L = fd.L;
   const int ld = fd.ld;
   while (nel < n) {
     if (tpp_col_small(fd, nel, nel, small, red)) {
-      if (!action) { if (threadIdx.x == 0) st->status = kDevSingular; return; }
+      if (!action) return -1;
       tpp_zero_col(fd, nel);
       nel++;
       continue;
@@ -1256,7 +1252,7 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontSta
     bool done = false;
     for (p = nel + 1; p < n; ++p) {
       if (tpp_col_small(fd, p, nel, small, red)) {
-        if (!action) { if (threadIdx.x == 0) st->status = kDevSingular; return; }
+        if (!action) return -1;
         tpp_sym_swap(fd, p, nel);
         tpp_zero_col(fd, nel);
         nel++;
@@ -1330,8 +1326,78 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontSta
       }
     }
   }
-  if (threadIdx.x == 0) { st->nelim = nel; st->p = nel; }
   (void)m;
+  return nel;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontState* sts,
+                                                     const int* fronts, bool action, double u,
+                                                     double small, bool all_fronts) {
+  const int f = fronts[blockIdx.x];
+  FrontState* st = &sts[f];
+  FrontDesc<T> fd = fds[f];
+  if (st->status != kDevOk) return;
+  if (st->nelim >= fd.n) return;
+  if (!(all_fronts || fd.m == fd.n)) return;
+  __shared__ double red[kTppThreads / 32];
+  __shared__ int s_t;
+  const int nel = tpp_body(fd, st->nelim, action, u, small, red, &s_t);
+  if (threadIdx.x == 0) {
+    if (nel < 0) st->status = kDevSingular;
+    else { st->nelim = nel; st->p = nel; }
+  }
+}
+
+// ------------------------------------------------------------------------
+// k_tpp_small: the fronts of small leaf subtrees, factored with TPP from
+// their first column as the reference's CPU path does for every node of a
+// subtree below small_subtree_threshold flops (SymbolicSubtree.hxx:56-82;
+// SmallLeafNumericSubtree.hxx:345-375 calls ldlt_tpp_factor on the whole
+// front).  One CTA per front.  A front whose m x n block (plus two columns
+// of workspace) fits the launch's dynamic shared memory is copied there,
+// factored and copied back, so the many reductions of the pivot search read
+// shared memory; a larger one (delays can grow a front) is factored in place
+// in global memory.  The elimination count is stored as the APP count's
+// successor would be (p = nelim; step = 0: no APP pass ran).
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, FrontState* sts,
+                                                           const int* fronts, bool action,
+                                                           double u, double small,
+                                                           int smem_bytes) {
+  extern __shared__ __align__(16) unsigned char tpp_smem[];
+  const int f = fronts[blockIdx.x];
+  FrontState* st = &sts[f];
+  FrontDesc<T> fd = fds[f];
+  if (st->status != kDevOk) return;
+  __shared__ double red[kTppThreads / 32];
+  __shared__ int s_t;
+  const int m = fd.m, n = fd.n;
+  const int ldS = (m + 1) & ~1;
+  const size_t need = ((size_t)ldS * (n + 2)) * sizeof(T);
+  int nel;
+  if (n > 0 && need <= (size_t)smem_bytes) {
+    T* S = reinterpret_cast<T*>(tpp_smem);
+    for (int c = 0; c < n; ++c)
+      for (int r = threadIdx.x; r < m; r += blockDim.x) S[(size_t)c * ldS + r] = fd.L[(int64_t)c * fd.ld + r];
+    __syncthreads();
+    FrontDesc<T> sd = fd;
+    sd.L = S;
+    sd.ld = ldS;
+    sd.W = S + (size_t)ldS * n;  // two columns: unscaled pivot copies
+    nel = tpp_body(sd, 0, action, u, small, red, &s_t);
+    __syncthreads();
+    if (nel >= 0)
+      for (int c = 0; c < n; ++c)
+        for (int r = threadIdx.x; r < m; r += blockDim.x) fd.L[(int64_t)c * fd.ld + r] = S[(size_t)c * ldS + r];
+  } else {
+    nel = tpp_body(fd, 0, action, u, small, red, &s_t);
+  }
+  if (threadIdx.x == 0) {
+    if (nel < 0) st->status = kDevSingular;
+    else { st->nelim = nel; st->p = nel; st->step = 0; }
+  }
 }
 
 // ------------------------------------------------------------------------
@@ -1502,6 +1568,27 @@ void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, boo
   { k_tpp<T><<<nf, kTppThreads, 0, s>>>(fd, st, fronts, action, u, small, all_fronts); note_launches(1); }
 }
 
+// Largest dynamic shared memory of k_tpp_small: the fronts of small leaf
+// subtrees hold m * n < ~26k entries (their flops are below 4e6), about
+// 205 KB in FP64.
+constexpr int kTppSmallSmem = 220 * 1024;
+
+template <typename T>
+void launch_tpp_small(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
+                      double u, double small, int max_elems, cudaStream_t s) {
+  if (nf <= 0) return;
+  static bool attr_set = false;  // per template instance, once per process
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_tpp_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kTppSmallSmem);
+    attr_set = true;
+  }
+  const size_t want = (size_t)max_elems * sizeof(T);
+  const int smem = (int)std::min<size_t>(want, kTppSmallSmem);
+  k_tpp_small<T><<<nf, kTppThreads, smem, s>>>(fd, st, fronts, action, u, small, smem);
+  note_launches(1);
+}
+
 template <typename T>
 void launch_calc_ld(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
                     int max_n, cudaStream_t s) {
@@ -1533,6 +1620,8 @@ void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* front
   template void launch_app_finish<T>(FrontDesc<T>*, FrontState*, const int*, int, cudaStream_t); \
   template void launch_tpp<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double, double, \
                               bool, cudaStream_t);                                              \
+  template void launch_tpp_small<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double,  \
+                                    double, int, cudaStream_t);                                 \
   template void launch_calc_ld<T>(FrontDesc<T>*, FrontState*, const int*, int, int, int,        \
                                   cudaStream_t);                                                 \
   template void launch_contrib_gemm<T>(FrontDesc<T>*, FrontState*, const int*, int, int,        \

@@ -305,8 +305,14 @@ struct Symbolic {
   std::vector<int> sptr, ncol, nrow, parent;  // per node (0-based; parent -1 = root)
   std::vector<int64_t> rptr, nptr;
   std::vector<int> rlist;
-  std::vector<std::vector<int>> children;  // node ids, increasing
+  std::vector<std::vector<int>> children;  // node ids, decreasing (reference order)
   std::vector<int> front_of, node_of, lvl_start;
+  // Small leaf subtrees (SymbolicSubtree.hxx:56-82): per front, 1 when its
+  // node lies in a leaf subtree below small_subtree_threshold flops, which
+  // the reference's CPU path factors with TPP only; per level, the number of
+  // other (APP) fronts, listed first in the level's part of d_fronts.
+  std::vector<char> tpp_only;
+  std::vector<int> lvl_napp;
   std::vector<int> cols_start;  // per level into cols
   std::vector<int64_t> contrib_off;  // per front, elements
   int64_t contrib_total = 0;
@@ -385,8 +391,12 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
     maxsrc = std::max(maxsrc, nl[2 * k]);
   }
   S->nnz = maxsrc + 1;
+  // children in decreasing order, the order in which the reference's CPU
+  // path visits them (SymbolicSubtree.hxx:42-47 pushes each node onto its
+  // parent's list): delayed columns are appended, and contributions added,
+  // last child first
   S->children.assign(nn, {});
-  for (int i = 0; i < nn; ++i)
+  for (int i = nn - 1; i >= 0; --i)
     if (S->parent[i] >= 0) S->children[S->parent[i]].push_back(i);
   // levels (leaves = 0)
   std::vector<int> lev(nn, 0);
@@ -520,8 +530,41 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
     S->d_acol = upload(acol);
     S->d_asrc = upload(asrc);
   }
+  // small leaf subtrees: flops below each node, then from every leaf up
+  // while the subtree stays below the threshold (a single node is not a
+  // subtree)
+  {
+    const int64_t thr = opts ? opts->small_subtree_threshold : int64_t(4000000);
+    std::vector<int64_t> fl(nn + 1, 0);
+    for (int i = 0; i < nn; ++i) {
+      for (int k = 0; k < S->ncol[i]; ++k) fl[i] += (int64_t)(S->nrow[i] - k) * (S->nrow[i] - k);
+      fl[S->parent[i] >= 0 ? S->parent[i] : nn] += fl[i];
+    }
+    std::vector<char> insl(nn, 0);
+    for (int i = 0; i < nn;) {
+      if (!S->children[i].empty()) { ++i; continue; }
+      int last = i;
+      for (int cur = i; cur >= 0 && cur < nn; cur = S->parent[cur]) {
+        if (fl[cur] >= thr) break;
+        last = cur;
+      }
+      if (last == i) { ++i; continue; }
+      for (int j = i; j <= last; ++j) insl[j] = 1;
+      i = last + 1;
+    }
+    S->tpp_only.assign(nn, 0);
+    for (int i = 0; i < nn; ++i) S->tpp_only[S->front_of[i]] = insl[i];
+  }
   std::vector<int> fronts(nn);
-  for (int f = 0; f < nn; ++f) fronts[f] = f;
+  S->lvl_napp.assign(nlev, 0);
+  for (int l = 0; l < nlev; ++l) {
+    int k = S->lvl_start[l];
+    for (int f = S->lvl_start[l]; f < S->lvl_start[l + 1]; ++f)
+      if (!S->tpp_only[f]) fronts[k++] = f;
+    S->lvl_napp[l] = k - S->lvl_start[l];
+    for (int f = S->lvl_start[l]; f < S->lvl_start[l + 1]; ++f)
+      if (S->tpp_only[f]) fronts[k++] = f;
+  }
   std::vector<int> sp(S->sptr.begin(), S->sptr.end());
   S->d_nptr = upload(S->nptr);
   S->d_nlist = upload(nl);
@@ -747,6 +790,21 @@ struct Numeric : NumericBase {
   int* d_tc_status = nullptr;
   int* d_ncount = nullptr;  // per-node inertia counts (neg, two, zero)
 
+  // Fronts of small leaf subtrees are factored by TPP alone (as the
+  // reference's CPU path does), except in the positive-definite case, whose
+  // small leaf subtrees use the same unpivoted factorisation as the rest,
+  // and with pivot_method = tpp, where every front takes TPP after an empty
+  // APP pass.  The level's APP fronts come first in d_fronts.
+  bool tpp_front(int f) const {
+    return !posdef && S->copts.pivot_method != 3 && S->tpp_only[f];
+  }
+  int app_fronts(int l) const {
+    if (posdef || S->copts.pivot_method == 3) return S->lvl_start[l + 1] - S->lvl_start[l];
+    return S->lvl_napp[l];
+  }
+  // shared-memory staging size of a small leaf front, elements
+  int tpp_elems(int f) const { return ((m_[f] + 1) & ~1) * (n_[f] + 2); }
+
   std::vector<TcProblem> tc_problems(int f0, int f1) const {
     std::vector<TcProblem> ps;
     for (int f = f0; f < f1; ++f) {
@@ -909,7 +967,8 @@ struct Numeric : NumericBase {
       CK(cudaMemsetAsync(d_ncount, 0, 3 * (size_t)nn * sizeof(int), s));
       for (int l = 0; l < S->nlev; ++l) {
         const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1], nf = f1 - f0;
-        int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0;
+        const int napp = app_fronts(l);
+        int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0, max_app_n = 0, max_tpp = 0;
         int64_t maxz = 0;
         for (int f = f0; f < f1; ++f) {
           const int node = S->node_of[f];
@@ -918,6 +977,8 @@ struct Numeric : NumericBase {
           max_cm = std::max(max_cm, hfd[f].cm);
           max_ent = std::max<int>(max_ent, (int)(S->nptr[node + 1] - S->nptr[node]));
           maxz = std::max(maxz, (int64_t)ld_[f] * n_[f]);
+          if (tpp_front(f)) max_tpp = std::max(max_tpp, tpp_elems(f));
+          else max_app_n = std::max(max_app_n, n_[f]);
         }
         const int* fr = S->d_fronts + f0;
         launch_zero_fronts<T>(d_fd, fr, nf, (int)std::min<int64_t>(maxz, 1 << 30), s);
@@ -927,20 +988,23 @@ struct Numeric : NumericBase {
         launch_assemble_contrib<T>(d_fd, S->d_cols + S->cols_start[l],
                                    S->cols_start[l + 1] - S->cols_start[l], S->d_pairs,
                                    S->d_rdir, S->d_rdir_ptr, s);
-        const int steps = (max_n + kBlk - 1) / kBlk;
+        const int steps = (max_app_n + kBlk - 1) / kBlk;
         for (int st = 0; st < steps; ++st) {
           int mr = 0, tr = 0, tc = 0;
           for (int f = f0; f < f1; ++f) {
+            if (tpp_front(f)) continue;
             mr = std::max(mr, m_[f] - kBlk * st);
             tr = std::max(tr, m_[f] - kBlk * (st + 1));
             tc = std::max(tc, n_[f] - kBlk * (st + 1));
           }
-          launch_app_step<T>(d_fd, d_st, fr, nf, st, std::max(mr, 1), tr, tc, co.action,
+          launch_app_step<T>(d_fd, d_st, fr, napp, st, std::max(mr, 1), tr, tc, co.action,
                              posdef ? 0.0 : co.u, co.small, s, nullptr, posdef);
         }
         launch_app_finish<T>(d_fd, d_st, fr, nf, s);
         const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
-        launch_tpp<T>(d_fd, d_st, fr, nf, co.action, co.u, co.small, tpp_all, s);
+        launch_tpp<T>(d_fd, d_st, fr, napp, co.action, co.u, co.small, tpp_all, s);
+        launch_tpp_small<T>(d_fd, d_st, fr + napp, nf - napp, co.action, co.u, co.small, max_tpp,
+                            s);
         launch_calc_ld<T>(d_fd, d_st, fr, nf, max_cm, max_n, s);
         launch_contrib_gemm<T>(d_fd, d_st, fr, nf, max_cm, s);
         if (tblob[l] && tc_gemm_launch(tplans[l], tblob[l], d_tc_status, s, tc_chunk) != 0)
@@ -1012,6 +1076,7 @@ struct Numeric : NumericBase {
         napp_[f] = hst[f].step;
         lvl_max_m[l] = std::max(lvl_max_m[l], m_[f]);
         lvl_max_nelim[l] = std::max(lvl_max_nelim[l], nelim_[f]);
+        if (tpp_front(f)) continue;  // small leaf fronts: no pass counts
         if (use_app && napp_[f] < n_[f]) nfp += n_[f] - napp_[f];
         const bool tpp_ran = tpp_all || (m_[f] == n_[f]);
         if (!use_app) nfp += n_[f] - nelim_[f];
@@ -1177,8 +1242,9 @@ struct Numeric : NumericBase {
     std::vector<int4> dwork;
     for (int l = 0; l < S->nlev; ++l) {
       const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1], nf = f1 - f0;
+      const int napp = app_fronts(l);
       dwork.clear();
-      int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0;
+      int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0, max_app_n = 0, max_tpp = 0;
       size_t wsW = 0, wsSwap = 0, wsLD = 0;
       for (int f = f0; f < f1; ++f) {
         const int node = S->node_of[f];
@@ -1203,6 +1269,10 @@ struct Numeric : NumericBase {
         wsLD += (size_t)cm * n;
         maxfront = std::max(maxfront, m);
         maxsn = std::max(maxsn, n);
+      }
+      for (int f = f0; f < f1; ++f) {
+        if (tpp_front(f)) max_tpp = std::max(max_tpp, tpp_elems(f));
+        else max_app_n = std::max(max_app_n, n_[f]);
       }
       ws_W.ensure(wsW + 64);
       ws_swap.ensure(wsSwap + 64);
@@ -1260,15 +1330,16 @@ struct Numeric : NumericBase {
       // dense factorisation
       const bool use_app = co.pivot_method != 3;
       if (use_app) {
-        const int steps = (max_n + kBlk - 1) / kBlk;
+        const int steps = (max_app_n + kBlk - 1) / kBlk;
         for (int st = 0; st < steps; ++st) {
           int mr = 0, tr = 0, tc = 0;
           for (int f = f0; f < f1; ++f) {
+            if (tpp_front(f)) continue;
             mr = std::max(mr, m_[f] - kBlk * st);
             tr = std::max(tr, m_[f] - kBlk * (st + 1));
             tc = std::max(tc, n_[f] - kBlk * (st + 1));
           }
-          launch_app_step<T>(d_fd, d_st, fr, nf, st, std::max(mr, 1), tr, tc, co.action,
+          launch_app_step<T>(d_fd, d_st, fr, napp, st, std::max(mr, 1), tr, tc, co.action,
                              posdef ? 0.0 : co.u, co.small, s, tm(), posdef);
         }
       }
@@ -1276,7 +1347,8 @@ struct Numeric : NumericBase {
       launch_app_finish<T>(d_fd, d_st, fr, nf, s);
       pmark(tm(), kPhTpp, s);
       const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
-      launch_tpp<T>(d_fd, d_st, fr, nf, co.action, co.u, co.small, tpp_all, s);
+      launch_tpp<T>(d_fd, d_st, fr, napp, co.action, co.u, co.small, tpp_all, s);
+      launch_tpp_small<T>(d_fd, d_st, fr + napp, nf - napp, co.action, co.u, co.small, max_tpp, s);
       pmark(tm(), kPhCalcLd, s);
       launch_calc_ld<T>(d_fd, d_st, fr, nf, max_cm, max_n, s);
       pmark(tm(), kPhContrib, s);
@@ -1300,6 +1372,7 @@ struct Numeric : NumericBase {
         napp_[f] = hst[f].step;
         lvl_max_m[l] = std::max(lvl_max_m[l], m_[f]);
         lvl_max_nelim[l] = std::max(lvl_max_nelim[l], nelim_[f]);
+        if (tpp_front(f)) continue;  // small leaf fronts: no pass counts
         if (use_app && napp_[f] < n_[f]) nfp += n_[f] - napp_[f];
         bool tpp_ran = tpp_all || (m_[f] == n_[f]);
         if (!use_app) nfp += n_[f] - nelim_[f];

@@ -51,6 +51,25 @@ def test_oracle_matches_golden(path):
     assert rel < 1e-10
 
 
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_oracle_pivots_match_reference_fixture(path):
+    """The oracle takes the reference's pivots: small leaf subtrees by TPP,
+    children visited last first, so the pivot order, D^{-1} and the partial
+    solves equal the reference's own outputs stored in the fixture."""
+    g = np.load(path)
+    ak = ssids.analyse(g["ptr"], g["row"], g["order"])
+    F = oracle.OracleFactor(ak, g["val"])
+    for k in ("num_neg", "num_two", "num_delay", "num_zero", "not_first_pass",
+              "not_second_pass"):
+        assert F.stats[k] == int(g["stat_" + k]), k
+    piv, d = F.enquire_indef()
+    assert np.array_equal(piv, g["piv_order"])
+    assert np.abs(d - g["d"]).max() <= 1e-12 * np.abs(g["d"]).max()
+    for job, key in ((1, "x_fwd"), (2, "x_diag"), (0, "x")):
+        x = F.solve(g["b"], job=job)
+        assert np.abs(x - g[key]).max() <= 1e-10 * np.abs(g[key]).max(), key
+
+
 @pytest.mark.skipif(not oracle.ref_available(), reason="reference CPU core not built here")
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_oracle_vs_reference_random(seed):

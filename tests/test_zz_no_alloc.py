@@ -55,6 +55,42 @@ def test_noalloc_matches_allocating_entry_point_twice():
         assert np.abs(l2[low] - l1[low]).max() <= TOL * max(np.abs(l1[low]).max(), 1.0)
 
 
+def test_noalloc_leaves_device_memory_untouched():
+    """After one warm-up call, a further call changes neither the device's
+    free memory nor torch's allocations: nothing is allocated or freed."""
+    torch = pytest.importorskip("torch")
+    from spral_gb300 import _native
+    import oracle
+    lib = _native.lib()
+    opts = oracle.default_options()
+    m, n = 600, 200
+    a = gen_sym_indef(m, np.random.default_rng(31))
+    a_d = torch.tensor(np.asfortranarray(a).ravel(order="F"), dtype=torch.float64, device="cuda")
+    a0 = a_d.clone()
+    d_d = torch.zeros(2 * n + 2, dtype=torch.float64, device="cuda")
+    p_d = torch.arange(n, dtype=torch.int32, device="cuda")
+    p0 = p_d.clone()
+
+    def call():
+        a_d.copy_(a0)
+        p_d.copy_(p0)
+        torch.cuda.synchronize()
+        return lib.spral_ssids_gpu_ldlt_app_factor_noalloc(
+            m, n, ctypes.c_void_p(p_d.data_ptr()), ctypes.c_void_p(a_d.data_ptr()), m,
+            ctypes.c_void_p(d_d.data_ptr()), 1.0, ctypes.c_void_p(a_d.data_ptr() + 8 * (n * m + n)),
+            m, ctypes.byref(opts), None)
+
+    assert call() >= 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0 = torch.cuda.memory_allocated()
+    assert call() >= 0
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_allocated() == alloc0
+
+
 def test_noalloc_rejects_front_beyond_fixed_scratch():
     torch = pytest.importorskip("torch")
     from spral_gb300 import _native
@@ -68,3 +104,15 @@ def test_noalloc_rejects_front_beyond_fixed_scratch():
         m, n, ctypes.c_void_p(p_d.data_ptr()), ctypes.c_void_p(a_d.data_ptr()), m,
         ctypes.c_void_p(d_d.data_ptr()), 1.0, None, 0, ctypes.byref(oracle.default_options()), None)
     assert rc == -60
+    # the leading dimension alone is limited too (a small front stored in a
+    # taller array), while an empty front succeeds whatever its lda
+    m, n, lda = 64, 32, 1100
+    a2 = torch.zeros(lda * n, dtype=torch.float64, device="cuda")
+    rc = lib.spral_ssids_gpu_ldlt_app_factor_noalloc(
+        m, n, ctypes.c_void_p(p_d.data_ptr()), ctypes.c_void_p(a2.data_ptr()), lda,
+        ctypes.c_void_p(d_d.data_ptr()), 1.0, None, 0, ctypes.byref(oracle.default_options()), None)
+    assert rc == -60
+    rc = lib.spral_ssids_gpu_ldlt_app_factor_noalloc(
+        m, 0, ctypes.c_void_p(p_d.data_ptr()), ctypes.c_void_p(a2.data_ptr()), lda,
+        ctypes.c_void_p(d_d.data_ptr()), 1.0, None, 0, ctypes.byref(oracle.default_options()), None)
+    assert rc == 0
