@@ -65,6 +65,10 @@ def parse():
                          "refinement against the FP64 path")
     ap.add_argument("--kkt-nh", type=int, default=10000)
     ap.add_argument("--kkt-na", type=int, default=5000)
+    ap.add_argument("--kkt-order", default="amd", choices=["amd", "natural"],
+                    help="KKT pivot order: approximate minimum degree (interleaves the "
+                         "constraint rows with H, so 2x2 pivots and delays occur) or the "
+                         "natural order (H first: no 2x2 pivot is needed)")
     ap.add_argument("--kkt-cpu", action="store_true",
                     help="also time the CPU port on the kkt workload (about a minute)")
     ap.add_argument("--batch-count", type=int, default=4096)
@@ -842,9 +846,11 @@ def run_kkt(args):
     definition's structure (H SPD with a random symmetric pattern of about 7
     entries per row, N(0,1) off-diagonals and diagonal = row abs-sum + 1; A
     with 4 N(0,1) entries per row at uniform columns) at nh x na = 10,000 x
-    5,000 by default (the definition's 200,000 x 100,000 has no small
-    separators: its root front would be ~1.9e5 wide).  Minimum-degree order,
-    8 right-hand sides N(0,1).  One step = numeric factor + 8-RHS solve
+    5,000 by default (the definition's 200,000 x 100,000 under the same
+    approximate minimum-degree order has a dense root front of 105,834 rows
+    and 4.1e14 predicted flops).  Approximate minimum-degree order (which
+    interleaves constraint rows with H, so 2x2 pivots and delays occur), 8
+    right-hand sides N(0,1).  One step = numeric factor + 8-RHS solve
     refined to bwd err <= 1e-14; `value` is the mixed-precision path (FP32
     factors, 2x2 pivots and delays decided in FP64), `fp64` the FP64 path."""
     import torch
@@ -854,7 +860,8 @@ def run_kkt(args):
     L = _native.lib()
     nh, na = args.kkt_nh, args.kkt_na
     ptr, row, val = M.kkt(nh, na, seed=2026)
-    ak = ssids.analyse(ptr, row)
+    order = ssids.order_amd(ptr, row) if args.kkt_order == "amd" else None
+    ak = ssids.analyse(ptr, row, order)
     n, nrhs = ak.n, args.nrhs
     b = np.random.default_rng(2027).standard_normal((n, nrhs))
     dev = torch.device("cuda", local)
@@ -891,6 +898,10 @@ def run_kkt(args):
         x = x_d.cpu().numpy().T
         xu = np.empty_like(x)
         xu[ak.invp, :] = x
+        if prec == ssids.PRECISION_MIXED:
+            measure.x_mixed = xu
+        else:
+            measure.x_fp64 = xu
         out = {"value": 1000.0 / ms, "unit": "solves/s", "ms_per_step": ms,
                "factor_ms": float(fk.timing()[0]),
                "bwd_err": float(M.scaled_bwd_error(ptr, row, val, xu, b).max()),
@@ -934,7 +945,10 @@ def run_kkt(args):
         cpu = {"value": 1.0 / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
                "sample": "one full factor+solve (OpenBLAS threads = all cores)",
                "bwd_err": float(M.scaled_bwd_error(ptr, row, val, xc, b).max()),
-               "num_neg": F.stats["num_neg"]}
+               "num_neg": F.stats["num_neg"], "num_two": F.stats["num_two"],
+               "num_delay": F.stats["num_delay"]}
+        mixed["rel_vs_oracle"] = rel_diff(measure.x_mixed, xc)
+        fp64["rel_vs_oracle"] = rel_diff(measure.x_fp64, xc)
     if rank == 0:
         e2e_ms = 1000.0 * sum(e2e_t) / len(e2e_t)
         line = {"metric": METRIC, "workload": "kkt", "value": mixed["value"],
@@ -944,7 +958,8 @@ def run_kkt(args):
                 "data": "synthetic (seeded KKT values and RHS)",
                 "config": {"workload": f"KKT [[H, A^T], [A, -1e-8 I]], H {nh}x{nh} SPD (7 "
                                        f"nnz/row), A {na}x{nh} (4 nnz/row), n={n}, "
-                                       f"minimum-degree order, {nrhs} RHS N(0,1); one solve = "
+                                       f"{'approximate minimum-degree' if args.kkt_order == 'amd' else 'natural'} "
+                                       f"order, {nrhs} RHS N(0,1); one solve = "
                                        f"numeric factor + {nrhs}-RHS solve refined to bwd err "
                                        f"<= 1e-14",
                            "n": n, "nnz_lower": ak.nnz, "predicted_flops": ak.nflops,

@@ -70,6 +70,7 @@ def _declare(L):
     f("spral_gb300_akeep_arrays", None, P, P, P, P, P, P, P, P)
     f("spral_gb300_akeep_free", None, P)
     f("spral_gb300_order_mindeg", I, I, P, P, P)
+    f("spral_gb300_order_amd", I, I, P, P, P)
     f("spral_ssids_gpu_create_symbolic_subtree", P, I, I, I, I, P, P, P, P, P, P,
       ctypes.POINTER(CpuFactorOptions))
     f("spral_ssids_gpu_destroy_symbolic_subtree", None, P)

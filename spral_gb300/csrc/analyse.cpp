@@ -426,4 +426,184 @@ int spral_gb300_order_mindeg(int n, const int64_t* ptr, const int* row, int* ord
   }
 }
 
+
+// Approximate minimum degree ordering, written from the published algorithm
+// (P. R. Amestoy, T. A. Davis, I. S. Duff, "An approximate minimum degree
+// ordering algorithm", SIAM J. Matrix Anal. Appl. 17(4), 1996): elimination
+// on the quotient graph (variables, and elements formed by eliminated
+// pivots), approximate external degrees from |Le \ Lp|, element absorption
+// (including elements that Lp covers), and supervariables of
+// indistinguishable variables found by hashing their adjacency, which also
+// collapses the dense end of the elimination into one pivot block.  Input:
+// lower CSC, 0-based.  Output: order[i] = pivot position of variable i.  The
+// reference takes its orderings from METIS, which is not part of this path;
+// this ordering serves general sparse matrices here (KKT systems).
+int spral_gb300_order_amd(int n, const int64_t* ptr, const int* row, int* order) {
+  try {
+    std::vector<int64_t> fptr;
+    std::vector<int> frow;
+    full_pattern(n, ptr, row, fptr, frow);
+    std::vector<std::vector<int>> A(n), E(n), Le(n);
+    for (int v = 0; v < n; ++v) {
+      A[v].assign(frow.begin() + fptr[v], frow.begin() + fptr[v + 1]);
+      std::sort(A[v].begin(), A[v].end());
+      A[v].erase(std::unique(A[v].begin(), A[v].end()), A[v].end());
+    }
+    std::vector<int64_t>().swap(fptr);
+    std::vector<int>().swap(frow);
+    enum : char { kVar = 0, kElt = 1, kMerged = 2, kDead = 3 };
+    std::vector<char> status(n, kVar);
+    std::vector<int> nv(n, 1), deg(n), chain_next(n, -1), chain_last(n);
+    for (int v = 0; v < n; ++v) { deg[v] = (int)A[v].size(); chain_last[v] = v; }
+    // degree buckets (doubly linked)
+    std::vector<int> head(n + 1, -1), nxt(n, -1), prv(n, -1);
+    auto bucket_insert = [&](int v) {
+      const int d = std::min(std::max(deg[v], 0), n);
+      nxt[v] = head[d];
+      prv[v] = -1;
+      if (head[d] >= 0) prv[head[d]] = v;
+      head[d] = v;
+    };
+    auto bucket_remove = [&](int v) {
+      const int d = std::min(std::max(deg[v], 0), n);
+      if (prv[v] >= 0) nxt[prv[v]] = nxt[v];
+      else head[d] = nxt[v];
+      if (nxt[v] >= 0) prv[nxt[v]] = prv[v];
+      nxt[v] = prv[v] = -1;
+    };
+    for (int v = n - 1; v >= 0; --v) bucket_insert(v);
+    std::vector<int> mark(n, 0), wstamp(n, 0);
+    std::vector<long long> w(n, 0);
+    int tag = 0, wtag = 0, mindeg = 0, nel = 0;
+    std::vector<int> pivots;
+    std::vector<int> Lp;
+    std::vector<std::pair<unsigned long long, int>> hv;
+    while (nel < n) {
+      while (mindeg <= n && head[mindeg] < 0) ++mindeg;
+      if (mindeg > n) return -1;  // inconsistent state
+      const int p = head[mindeg];
+      bucket_remove(p);
+      // the new element Lp: p's elements' variables and p's variable neighbours
+      ++tag;
+      mark[p] = tag;
+      Lp.clear();
+      long long lpw = 0;
+      for (int e : E[p]) {
+        if (status[e] != kElt) continue;
+        for (int j : Le[e])
+          if (status[j] == kVar && mark[j] != tag) { mark[j] = tag; Lp.push_back(j); lpw += nv[j]; }
+        status[e] = kDead;  // absorbed into p
+        std::vector<int>().swap(Le[e]);
+      }
+      for (int j : A[p])
+        if (status[j] == kVar && mark[j] != tag) { mark[j] = tag; Lp.push_back(j); lpw += nv[j]; }
+      std::vector<int>().swap(E[p]);
+      std::vector<int>().swap(A[p]);
+      status[p] = kElt;
+      nel += nv[p];
+      pivots.push_back(p);
+      for (int i : Lp) bucket_remove(i);
+      // adjacency of the variables of Lp: element p replaces what it covers
+      for (int i : Lp) {
+        auto& Ei = E[i];
+        size_t k = 0;
+        for (int e : Ei) if (status[e] == kElt && e != p) Ei[k++] = e;
+        Ei.resize(k);
+        Ei.push_back(p);
+        auto& Ai = A[i];
+        k = 0;
+        for (int j : Ai) if (status[j] == kVar && mark[j] != tag) Ai[k++] = j;
+        Ai.resize(k);
+      }
+      // w(e) = |Le \ Lp| (weighted) for the other elements next to Lp
+      ++wtag;
+      for (int i : Lp)
+        for (int e : E[i]) {
+          if (e == p) continue;
+          if (wstamp[e] != wtag) {
+            wstamp[e] = wtag;
+            auto& L = Le[e];
+            size_t k = 0;
+            long long s = 0;
+            for (int j : L) if (status[j] == kVar) { L[k++] = j; s += nv[j]; }
+            L.resize(k);
+            w[e] = s;
+          }
+          w[e] -= nv[i];
+        }
+      // approximate external degrees; elements covered by Lp are absorbed
+      for (int i : Lp) {
+        long long dext = 0;
+        auto& Ei = E[i];
+        size_t k = 0;
+        for (int e : Ei) {
+          if (e == p) { Ei[k++] = e; continue; }
+          if (status[e] != kElt) continue;
+          if (w[e] <= 0) { status[e] = kDead; std::vector<int>().swap(Le[e]); continue; }
+          dext += w[e];
+          Ei[k++] = e;
+        }
+        Ei.resize(k);
+        for (int j : A[i]) dext += nv[j];
+        long long d = std::min<long long>((long long)deg[i] + lpw - nv[i], dext + lpw - nv[i]);
+        d = std::min<long long>(d, (long long)(n - nel) - nv[i]);
+        deg[i] = (int)std::max<long long>(d, 0);
+      }
+      // supervariables: variables of Lp with equal element and variable lists
+      hv.clear();
+      for (int i : Lp) {
+        auto& Ei = E[i];
+        size_t k = 0;
+        for (int e : Ei) if (status[e] == kElt) Ei[k++] = e;
+        Ei.resize(k);
+        std::sort(Ei.begin(), Ei.end());
+        std::sort(A[i].begin(), A[i].end());
+        unsigned long long h = 1469598103934665603ull;
+        for (int e : Ei) h = (h ^ (unsigned long long)e) * 1099511628211ull;
+        h = (h ^ 0x9e3779b97f4a7c15ull) * 1099511628211ull;
+        for (int j : A[i]) h = (h ^ (unsigned long long)j) * 1099511628211ull;
+        hv.push_back({h, i});
+      }
+      std::sort(hv.begin(), hv.end());
+      for (size_t a = 0; a < hv.size();) {
+        size_t b = a;
+        while (b < hv.size() && hv[b].first == hv[a].first) ++b;
+        for (size_t x = a; x < b; ++x) {
+          const int i = hv[x].second;
+          if (status[i] != kVar) continue;
+          for (size_t y = x + 1; y < b; ++y) {
+            const int j = hv[y].second;
+            if (status[j] != kVar) continue;
+            if (E[i] != E[j] || A[i] != A[j]) continue;
+            // j is indistinguishable from i: merge
+            nv[i] += nv[j];
+            deg[i] -= nv[j];
+            nv[j] = 0;
+            status[j] = kMerged;
+            chain_next[chain_last[i]] = j;
+            chain_last[i] = chain_last[j];
+            std::vector<int>().swap(E[j]);
+            std::vector<int>().swap(A[j]);
+          }
+        }
+        a = b;
+      }
+      auto& Lnew = Le[p];
+      for (int i : Lp) {
+        if (status[i] != kVar) continue;
+        deg[i] = std::max(deg[i], 0);
+        bucket_insert(i);
+        mindeg = std::min(mindeg, std::min(deg[i], n));
+        Lnew.push_back(i);
+      }
+    }
+    int pos = 0;
+    for (int p : pivots)
+      for (int v = p; v >= 0; v = chain_next[v]) order[v] = pos++;
+    return pos == n ? 0 : -1;
+  } catch (std::bad_alloc const&) {
+    return -50;
+  }
+}
+
 }  // extern "C"

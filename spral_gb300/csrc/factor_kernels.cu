@@ -1354,18 +1354,139 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontSta
 // their first column as the reference's CPU path does for every node of a
 // subtree below small_subtree_threshold flops (SymbolicSubtree.hxx:56-82;
 // SmallLeafNumericSubtree.hxx:345-375 calls ldlt_tpp_factor on the whole
-// front).  One CTA per front.  A front whose m x n block (plus two columns
-// of workspace) fits the launch's dynamic shared memory is copied there,
-// factored and copied back, so the many reductions of the pivot search read
-// shared memory; a larger one (delays can grow a front) is factored in place
-// in global memory.  The elimination count is stored as the APP count's
-// successor would be (p = nelim; step = 0: no APP pass ran).
+// front).  One CTA per front, the front (m x n), two workspace columns and
+// its perm/opos held in shared memory.  Each pivot: warp 0 alone runs the
+// pivot search of ldlt_tpp_factor (ldlt_tpp.cxx:166-270; every reduction a
+// warp shuffle over shared memory), performs the symmetric swaps, writes
+// D^{-1} and keeps unscaled copies of the pivot column(s); after one barrier
+// every warp scales the pivot column(s) and updates the trailing
+// fully-summed columns (rows of the front's contribution part included);
+// one more barrier ends the pivot.  A front too large for the launch's
+// shared memory (delays can grow one) is factored in global memory by the
+// block-wide TPP of k_tpp.  step = 0 records that no APP pass ran.
 // ------------------------------------------------------------------------
+namespace tpps {
+enum Kind : int { kStop = 0, kZeroNel, kZeroSwap, kTwo, kOne, kSingular };
+struct Decision {
+  int kind, t, p;
+  double d0, d1, d3;
+};
+
+// warp-wide maximum of |a| over a strided set, NaN-free inputs assumed
+__device__ __forceinline__ double wmax(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ bool wall(bool b) { return __all_sync(0xffffffffu, b); }
+
+// all |entries| of row/column idx (row part from `from`) below small
+// (check_col_small, ldlt_tpp.cxx:21-28)
+template <typename T>
+__device__ bool col_small(const T* S, int ld, int idx, int from, int m, double small) {
+  const int lane = threadIdx.x & 31;
+  bool ok = true;
+  for (int c = from + lane; c < idx; c += 32) ok = ok && (fabs((double)S[(size_t)c * ld + idx]) < small);
+  for (int r = idx + lane; r < m; r += 32) ok = ok && (fabs((double)S[(size_t)idx * ld + r]) < small);
+  return wall(ok);
+}
+// largest |entry| of row/column col excluding position excl and the
+// diagonal (find_rc_abs_max_exclude, ldlt_tpp.cxx:80-92)
+template <typename T>
+__device__ double rc_max(const T* S, int ld, int col, int nel, int m, int excl) {
+  const int lane = threadIdx.x & 31;
+  double v = 0.0;
+  for (int c = nel + lane; c < col; c += 32)
+    if (c != excl) v = fmax(v, fabs((double)S[(size_t)c * ld + col]));
+  for (int r = col + 1 + lane; r < m; r += 32)
+    if (r != excl) v = fmax(v, fabs((double)S[(size_t)col * ld + r]));
+  return wmax(v);
+}
+// first column of the largest |a(p, c)|, c in [from, p) (find_row_abs_max)
+template <typename T>
+__device__ int row_argmax(const T* S, int ld, int p, int from) {
+  const int lane = threadIdx.x & 31;
+  double bv = -1.0;
+  int bi = 0x7fffffff;
+  for (int c = from + lane; c < p; c += 32) {
+    const double v = fabs((double)S[(size_t)c * ld + p]);
+    if (v > bv) { bv = v; bi = c; }
+  }
+  const double mx = wmax(bv);
+  int cand = (bv == mx) ? bi : 0x7fffffff;
+  for (int o = 16; o > 0; o >>= 1) cand = min(cand, __shfl_xor_sync(0xffffffffu, cand, o));
+  return cand;
+}
+// symmetric swap of positions i < j over the whole front (swap_cols,
+// ldlt_tpp.cxx:44-72), perm and opos included; warp-wide
+template <typename T>
+__device__ void sym_swap(T* S, int ld, int m, int i, int j, int* perm, int* opos) {
+  if (i == j) return;
+  if (j < i) { const int t = i; i = j; j = t; }
+  const int lane = threadIdx.x & 31;
+  for (int c = lane; c < i; c += 32) {
+    const T t = S[(size_t)c * ld + i]; S[(size_t)c * ld + i] = S[(size_t)c * ld + j]; S[(size_t)c * ld + j] = t;
+  }
+  for (int r = i + 1 + lane; r < j; r += 32) {
+    const T t = S[(size_t)i * ld + r]; S[(size_t)i * ld + r] = S[(size_t)r * ld + j]; S[(size_t)r * ld + j] = t;
+  }
+  for (int r = j + 1 + lane; r < m; r += 32) {
+    const T t = S[(size_t)i * ld + r]; S[(size_t)i * ld + r] = S[(size_t)j * ld + r]; S[(size_t)j * ld + r] = t;
+  }
+  if (lane == 0) {
+    const T t = S[(size_t)i * ld + i]; S[(size_t)i * ld + i] = S[(size_t)j * ld + j]; S[(size_t)j * ld + j] = t;
+    const int pt = perm[i]; perm[i] = perm[j]; perm[j] = pt;
+    const int ot = opos[i]; opos[i] = opos[j]; opos[j] = ot;
+  }
+  __syncwarp();
+}
+// the pivot search of one step of ldlt_tpp_factor, in warp 0
+template <typename T>
+__device__ Decision decide(const T* S, int ld, int nel, int m, int n, bool action, double u,
+                           double small) {
+  Decision d{kStop, 0, 0, 0.0, 0.0, 0.0};
+  if (col_small(S, ld, nel, nel, m, small)) { d.kind = action ? kZeroNel : kSingular; return d; }
+  for (int p = nel + 1; p < n; ++p) {
+    if (col_small(S, ld, p, nel, m, small)) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return d; }
+    const int t = row_argmax(S, ld, p, nel);
+    const double maxt = rc_max(S, ld, t, nel, m, p);
+    double maxp = rc_max(S, ld, p, nel, m, t);
+    const double a11 = (double)S[(size_t)t * ld + t], a21 = (double)S[(size_t)t * ld + p];
+    const double a22 = (double)S[(size_t)p * ld + p];
+    // test_2x2 (ldlt_tpp.cxx:95-126)
+    const double maxpiv = fmax(fabs(a11), fmax(fabs(a21), fabs(a22)));
+    if (!(maxpiv < small)) {
+      const double detscale = 1 / maxpiv;
+      const double det0 = (a11 * detscale) * a22, det1 = (a21 * detscale) * a21;
+      const double detpiv = det0 - det1;
+      if (!(fabs(detpiv) < fmax(small, fmax(fabs(det0 / 2), fabs(det1 / 2))))) {
+        const double d0 = (a22 * detscale) / detpiv, d1 = (-a21 * detscale) / detpiv;
+        const double d3 = (a11 * detscale) / detpiv;
+        bool ok;
+        if (fmax(maxp, maxt) < small) ok = true;
+        else {
+          const double x1 = fabs(d0) * maxt + fabs(d1) * maxp;
+          const double x2 = fabs(d1) * maxt + fabs(d3) * maxp;
+          ok = (u * fmax(x1, x2) < 1.0);
+        }
+        if (ok) { d.kind = kTwo; d.t = t; d.p = p; d.d0 = d0; d.d1 = d1; d.d3 = d3; return d; }
+      }
+    }
+    maxp = fmax(maxp, fabs(a21));
+    if (fabs(a22) >= u * maxp) { d.kind = kOne; d.p = p; return d; }
+  }
+  // last resort: nel itself as a 1x1 pivot
+  const double maxp = rc_max(S, ld, nel, nel, m, -1);
+  if (fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp) { d.kind = kOne; d.p = nel; }
+  return d;
+}
+}  // namespace tpps
+
 template <typename T>
 __global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, FrontState* sts,
                                                            const int* fronts, bool action,
                                                            double u, double small,
                                                            int smem_bytes) {
+  using namespace tpps;
   extern __shared__ __align__(16) unsigned char tpp_smem[];
   const int f = fronts[blockIdx.x];
   FrontState* st = &sts[f];
@@ -1373,29 +1494,119 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, Fr
   if (st->status != kDevOk) return;
   __shared__ double red[kTppThreads / 32];
   __shared__ int s_t;
+  __shared__ Decision s_dec;
   const int m = fd.m, n = fd.n;
   const int ldS = (m + 1) & ~1;
-  const size_t need = ((size_t)ldS * (n + 2)) * sizeof(T);
-  int nel;
-  if (n > 0 && need <= (size_t)smem_bytes) {
-    T* S = reinterpret_cast<T*>(tpp_smem);
+  const size_t need = (size_t)ldS * (n + 2) * sizeof(T) + 2 * (size_t)n * sizeof(int);
+  if (n == 0) {
+    if (threadIdx.x == 0) { st->nelim = 0; st->p = 0; st->step = 0; }
+    return;
+  }
+  if (need > (size_t)smem_bytes) {
+    const int nel = tpp_body(fd, 0, action, u, small, red, &s_t);
+    if (threadIdx.x == 0) {
+      if (nel < 0) st->status = kDevSingular;
+      else { st->nelim = nel; st->p = nel; st->step = 0; }
+    }
+    return;
+  }
+  T* S = reinterpret_cast<T*>(tpp_smem);
+  T* W0 = S + (size_t)ldS * n;
+  T* W1 = W0 + ldS;
+  int* sperm = reinterpret_cast<int*>(W1 + ldS);
+  int* sopos = sperm + n;
+  for (int c = 0; c < n; ++c)
+    for (int r = threadIdx.x; r < m; r += blockDim.x) S[(size_t)c * ldS + r] = fd.L[(int64_t)c * fd.ld + r];
+  for (int i = threadIdx.x; i < n; i += blockDim.x) { sperm[i] = fd.perm[i]; sopos[i] = fd.opos[i]; }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  int nel = 0;
+  bool singular = false;
+  while (nel < n) {
+    if (warp == 0) {
+      Decision d = decide(S, ldS, nel, m, n, action, u, small);
+      if (d.kind == kZeroSwap) sym_swap(S, ldS, m, d.p, nel, sperm, sopos);
+      if (d.kind == kZeroNel || d.kind == kZeroSwap) {
+        for (int r = nel + lane; r < m; r += 32) S[(size_t)nel * ldS + r] = T(0);
+        if (lane == 0) { fd.D[2 * nel] = 0.0; fd.D[2 * nel + 1] = 0.0; }
+      } else if (d.kind == kTwo) {
+        sym_swap(S, ldS, m, d.t, nel, sperm, sopos);
+        sym_swap(S, ldS, m, d.p, nel + 1, sperm, sopos);
+        for (int r = nel + 2 + lane; r < m; r += 32) {
+          W0[r] = S[(size_t)nel * ldS + r];
+          W1[r] = S[(size_t)(nel + 1) * ldS + r];
+        }
+        if (lane == 0) {
+          S[(size_t)nel * ldS + nel] = T(1);
+          S[(size_t)nel * ldS + nel + 1] = T(0);
+          S[(size_t)(nel + 1) * ldS + nel + 1] = T(1);
+          fd.D[2 * nel] = d.d0; fd.D[2 * nel + 1] = d.d1;
+          fd.D[2 * nel + 2] = dinf(); fd.D[2 * nel + 3] = d.d3;
+        }
+      } else if (d.kind == kOne) {
+        sym_swap(S, ldS, m, d.p, nel, sperm, sopos);
+        const double d11 = 1.0 / (double)S[(size_t)nel * ldS + nel];
+        d.d0 = d11;
+        for (int r = nel + 1 + lane; r < m; r += 32) W0[r] = S[(size_t)nel * ldS + r];
+        if (lane == 0) {
+          S[(size_t)nel * ldS + nel] = T(1);
+          fd.D[2 * nel] = d11; fd.D[2 * nel + 1] = 0.0;
+        }
+      }
+      __syncwarp();
+      if (lane == 0) s_dec = d;
+    }
+    __syncthreads();
+    const Decision d = s_dec;
+    if (d.kind == kStop) break;
+    if (d.kind == kSingular) { singular = true; break; }
+    if (d.kind == kZeroNel || d.kind == kZeroSwap) {
+      nel += 1;
+      __syncthreads();  // every warp has read s_dec before warp 0 rewrites it
+      continue;
+    }
+    const int ps = (d.kind == kTwo) ? 2 : 1;
+    // scale the pivot column(s) (apply_1x1 / apply_2x2) and update the
+    // trailing fully-summed columns, rows [c, m), with the unscaled copies
+    const int c0 = nel + ps;
+    if (ps == 1) {
+      const double d11 = d.d0;
+      for (int r = c0 + threadIdx.x; r < m; r += blockDim.x)
+        S[(size_t)nel * ldS + r] = (T)((double)W0[r] * d11);
+      for (int c = c0 + warp; c < n; c += nw) {
+        const T wc = W0[c];
+        T* col = S + (size_t)c * ldS;
+        for (int r = c + lane; r < m; r += 32) {
+          const T l = (T)((double)W0[r] * d11);
+          col[r] -= l * wc;
+        }
+      }
+    } else {
+      for (int r = c0 + threadIdx.x; r < m; r += blockDim.x) {
+        const double a1 = (double)W0[r], a2 = (double)W1[r];
+        S[(size_t)nel * ldS + r] = (T)(d.d0 * a1 + d.d1 * a2);
+        S[(size_t)(nel + 1) * ldS + r] = (T)(d.d1 * a1 + d.d3 * a2);
+      }
+      for (int c = c0 + warp; c < n; c += nw) {
+        const T w0 = W0[c], w1 = W1[c];
+        T* col = S + (size_t)c * ldS;
+        for (int r = c + lane; r < m; r += 32) {
+          const double a1 = (double)W0[r], a2 = (double)W1[r];
+          const T l1 = (T)(d.d0 * a1 + d.d1 * a2), l2 = (T)(d.d1 * a1 + d.d3 * a2);
+          col[r] -= l1 * w0 + l2 * w1;
+        }
+      }
+    }
+    __syncthreads();
+    nel += ps;
+  }
+  if (!singular) {
     for (int c = 0; c < n; ++c)
-      for (int r = threadIdx.x; r < m; r += blockDim.x) S[(size_t)c * ldS + r] = fd.L[(int64_t)c * fd.ld + r];
-    __syncthreads();
-    FrontDesc<T> sd = fd;
-    sd.L = S;
-    sd.ld = ldS;
-    sd.W = S + (size_t)ldS * n;  // two columns: unscaled pivot copies
-    nel = tpp_body(sd, 0, action, u, small, red, &s_t);
-    __syncthreads();
-    if (nel >= 0)
-      for (int c = 0; c < n; ++c)
-        for (int r = threadIdx.x; r < m; r += blockDim.x) fd.L[(int64_t)c * fd.ld + r] = S[(size_t)c * ldS + r];
-  } else {
-    nel = tpp_body(fd, 0, action, u, small, red, &s_t);
+      for (int r = threadIdx.x; r < m; r += blockDim.x) fd.L[(int64_t)c * fd.ld + r] = S[(size_t)c * ldS + r];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) { fd.perm[i] = sperm[i]; fd.opos[i] = sopos[i]; }
   }
   if (threadIdx.x == 0) {
-    if (nel < 0) st->status = kDevSingular;
+    if (singular) st->status = kDevSingular;
     else { st->nelim = nel; st->p = nel; st->step = 0; }
   }
 }
@@ -1571,11 +1782,11 @@ void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, boo
 // Largest dynamic shared memory of k_tpp_small: the fronts of small leaf
 // subtrees hold m * n < ~26k entries (their flops are below 4e6), about
 // 205 KB in FP64.
-constexpr int kTppSmallSmem = 220 * 1024;
+constexpr int kTppSmallSmem = 222 * 1024;
 
 template <typename T>
 void launch_tpp_small(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
-                      double u, double small, int max_elems, cudaStream_t s) {
+                      double u, double small, int max_bytes, cudaStream_t s) {
   if (nf <= 0) return;
   static bool attr_set = false;  // per template instance, once per process
   if (!attr_set) {
@@ -1583,8 +1794,7 @@ void launch_tpp_small(FrontDesc<T>* fd, FrontState* st, const int* fronts, int n
                          kTppSmallSmem);
     attr_set = true;
   }
-  const size_t want = (size_t)max_elems * sizeof(T);
-  const int smem = (int)std::min<size_t>(want, kTppSmallSmem);
+  const int smem = std::min(std::max(max_bytes, 0), kTppSmallSmem);
   k_tpp_small<T><<<nf, kTppThreads, smem, s>>>(fd, st, fronts, action, u, small, smem);
   note_launches(1);
 }

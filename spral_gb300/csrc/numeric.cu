@@ -802,8 +802,11 @@ struct Numeric : NumericBase {
     if (posdef || S->copts.pivot_method == 3) return S->lvl_start[l + 1] - S->lvl_start[l];
     return S->lvl_napp[l];
   }
-  // shared-memory staging size of a small leaf front, elements
-  int tpp_elems(int f) const { return ((m_[f] + 1) & ~1) * (n_[f] + 2); }
+  // shared-memory staging of a small leaf front (k_tpp_small): the front,
+  // two workspace columns, perm and opos, bytes
+  int tpp_bytes(int f) const {
+    return ((m_[f] + 1) & ~1) * (n_[f] + 2) * (int)sizeof(T) + 8 * n_[f];
+  }
 
   std::vector<TcProblem> tc_problems(int f0, int f1) const {
     std::vector<TcProblem> ps;
@@ -977,7 +980,7 @@ struct Numeric : NumericBase {
           max_cm = std::max(max_cm, hfd[f].cm);
           max_ent = std::max<int>(max_ent, (int)(S->nptr[node + 1] - S->nptr[node]));
           maxz = std::max(maxz, (int64_t)ld_[f] * n_[f]);
-          if (tpp_front(f)) max_tpp = std::max(max_tpp, tpp_elems(f));
+          if (tpp_front(f)) max_tpp = std::max(max_tpp, tpp_bytes(f));
           else max_app_n = std::max(max_app_n, n_[f]);
         }
         const int* fr = S->d_fronts + f0;
@@ -1271,7 +1274,7 @@ struct Numeric : NumericBase {
         maxsn = std::max(maxsn, n);
       }
       for (int f = f0; f < f1; ++f) {
-        if (tpp_front(f)) max_tpp = std::max(max_tpp, tpp_elems(f));
+        if (tpp_front(f)) max_tpp = std::max(max_tpp, tpp_bytes(f));
         else max_app_n = std::max(max_app_n, n_[f]);
       }
       ws_W.ensure(wsW + 64);

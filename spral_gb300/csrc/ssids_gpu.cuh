@@ -148,11 +148,12 @@ void launch_app_finish(FrontDesc<T>* fd, FrontState* st, const int* fronts, int 
 template <typename T>
 void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
                 double u, double small, bool root_only_or_all, cudaStream_t s);
-// fronts of small leaf subtrees: TPP from the first column; max_elems bounds
-// ((m + 1) & ~1) * (n + 2) over the listed fronts (shared-memory staging)
+// fronts of small leaf subtrees: TPP from the first column; max_bytes is
+// the largest shared-memory staging of the listed fronts,
+// ((m + 1) & ~1) * (n + 2) * sizeof(T) + 8 n
 template <typename T>
 void launch_tpp_small(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
-                      double u, double small, int max_elems, cudaStream_t s);
+                      double u, double small, int max_bytes, cudaStream_t s);
 template <typename T>
 void launch_calc_ld(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
                     int max_n, cudaStream_t s);

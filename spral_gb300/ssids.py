@@ -138,6 +138,20 @@ def order_mindeg(ptr, row):
     return order
 
 
+def order_amd(ptr, row):
+    """Approximate minimum-degree ordering (order[i] = pivot position of
+    variable i) for general sparse matrices, e.g. KKT systems."""
+    L = _native.lib()
+    n = len(ptr) - 1
+    ptr = np.ascontiguousarray(ptr, dtype=np.int64)
+    row = np.ascontiguousarray(row, dtype=np.int32)
+    order = np.zeros(n, dtype=np.int32)
+    st = L.spral_gb300_order_amd(n, _P(ptr), _P(row), _P(order))
+    if st != 0:
+        raise RuntimeError(f"order_amd failed ({st})")
+    return order
+
+
 def analyse(ptr, row, order=None, options=None):
     """Symbolic analyse (ssids_analyse, src/ssids/ssids.f90:148), host-side."""
     options = options or Options()

@@ -33,7 +33,10 @@ def test_gpu_batch_matches_individual_factorisations(precision):
     rng = np.random.default_rng(9)
     bs = [rng.uniform(-1, 1, len(p) - 1) for p, _, _ in mats]
     xs = bf.solve(bs)
-    tol = 1e-14 if precision == ssids.PRECISION_FP64 else 1e-5
+    # direct solves without refinement: the FP64 bound is 5e-14, as for the
+    # reference fixtures (the reference's TPP in small leaf subtrees takes
+    # 2x2 pivots whose growth bound is 1/u)
+    tol = 5e-14 if precision == ssids.PRECISION_FP64 else 1e-5
     for i, (p, r, v) in enumerate(mats):
         assert M.scaled_bwd_error(p, r, v, xs[i], bs[i]).max() <= tol
     # alone: the same kernels on the same data give the same bits
