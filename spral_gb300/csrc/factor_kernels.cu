@@ -71,6 +71,44 @@ __device__ __forceinline__ double sym_at(const T* L, int ld, int r, int c) {
 }
 
 // ------------------------------------------------------------------------
+// Start of APP block step `step` for one front (one thread): fold the
+// previous step's result (npass eliminated, the rest moved to the end of the
+// candidate range) and take the next block of at most 32 candidates.  A
+// front with fd.panel > 0 and more columns than that starts with the panel
+// [0, panel): its candidate range ends there (see FrontState).
+// ------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void app_step_begin(const FrontDesc<T>& fd, FrontState* st, int step,
+                                               int& p_out, int& bs_out) {
+  int p, end;
+  if (step == 0) {
+    p = 0;
+    end = (fd.panel > 0 && fd.n > fd.panel) ? fd.panel : fd.n;
+    st->pstart = 0;
+    st->qend = end;
+    st->gend = fd.n;
+    st->pk = 0;
+  } else {
+    p = st->p;
+    end = st->end;
+    if (st->bs > 0) {
+      p += st->npass;
+      end -= st->bs - st->npass;
+    }
+  }
+  int bs = min(kBlk, end - p);
+  if (bs < 0) bs = 0;
+  st->p = p;
+  st->end = end;
+  st->bs = bs;
+  st->npass_raw = bs;
+  st->npass = bs;
+  st->step = step;
+  p_out = p;
+  bs_out = bs;
+}
+
+// ------------------------------------------------------------------------
 // k_app_diag: advance state, factor the diagonal block with complete pivoting.
 // 1024 threads, thread (R, C) = (warp, lane) owns entry (R, C) of the block,
 // which is stored full-symmetric and kept exactly symmetric: for R > C the
@@ -159,26 +197,8 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
   pdl_wait();
   pdl_trigger();
   if (tid == 0) {
-    int p, end;
-    if (step == 0) {
-      p = 0;
-      end = fd.n;
-    } else {
-      p = st->p;
-      end = st->end;
-      if (st->bs > 0) {
-        p += st->npass;
-        end -= st->bs - st->npass;
-      }
-    }
-    int bs = min(kBlk, end - p);
-    if (bs < 0) bs = 0;
-    st->p = p;
-    st->end = end;
-    st->bs = bs;
-    st->npass_raw = bs;
-    st->npass = bs;
-    st->step = step;
+    int p, bs;
+    app_step_begin(fd, st, step, p, bs);
     s_state[0] = p;
     s_state[1] = bs;
   }
@@ -410,26 +430,8 @@ __global__ void __launch_bounds__(kDiagThreads)
   pdl_wait();
   pdl_trigger();
   if (tid == 0) {
-    int p, end;
-    if (step == 0) {
-      p = 0;
-      end = fd.n;
-    } else {
-      p = st->p;
-      end = st->end;
-      if (st->bs > 0) {
-        p += st->npass;
-        end -= st->bs - st->npass;
-      }
-    }
-    int bs = min(kBlk, end - p);
-    if (bs < 0) bs = 0;
-    st->p = p;
-    st->end = end;
-    st->bs = bs;
-    st->npass_raw = bs;
-    st->npass = bs;
-    st->step = step;
+    int p, bs;
+    app_step_begin(fd, st, step, p, bs);
     s_state[0] = p;
     s_state[1] = bs;
   }
@@ -976,7 +978,9 @@ __global__ void __launch_bounds__(256) k_app_panel(FrontDesc<T>* fds, FrontState
     app_fixup_cta<T>(fd, stp, p, bs, np, blockIdx.x - ptiles, gridDim.x - ptiles, l11, ldf);
     return;
   }
-  const int M = fd.m - (p + bs), N = fd.n - (p + bs), K = np;
+  // the candidate columns of the current panel (all of them for a front
+  // without panels), including failed columns moved behind its candidates
+  const int M = fd.m - (p + bs), N = stp->qend - (p + bs), K = np;
   if (K <= 0 || M <= 0 || N <= 0) return;
   T* C = fd.L + (int64_t)(p + bs) * fd.ld + (p + bs);
   const T* A = fd.L + (int64_t)p * fd.ld + (p + bs);
@@ -1069,8 +1073,47 @@ __device__ __forceinline__ int swap_partner(const SwapRanges& s, int x) {
   return x;
 }
 
-// One CTA per front (failures are rare): gather the affected symmetric lines
-// into the front's scratch, barrier, scatter them permuted.
+// columns per CTA of the L D kernels (k_panel_ld, k_calc_ld)
+constexpr int kLdCols = 16;
+
+// Symmetric swap of the position pairs (a0 + k, b0 + k), k < npairs, over
+// the whole front (every line: eliminated L rows, columns, diagonal; perm
+// and opos), by one CTA, 32 pairs at a time: gather the affected lines into
+// the front's swap buffer (64 lines), barrier, scatter them permuted.
+template <typename T>
+__device__ void swap_lines(const FrontDesc<T>& fd, int a0, int b0, int npairs) {
+  for (int base = 0; base < npairs; base += 32) {
+    SwapRanges sr;
+    sr.a0 = a0 + base;
+    sr.b0 = b0 + base;
+    sr.npairs = min(32, npairs - base);
+    const int nl = 2 * sr.npairs;
+    int* ib = reinterpret_cast<int*>(fd.swapbuf + (int64_t)nl * fd.ld);
+    for (int li = 0; li < nl; ++li) {
+      const int s = (li < sr.npairs) ? sr.a0 + li : sr.b0 + (li - sr.npairs);
+      T* line = fd.swapbuf + (int64_t)li * fd.ld;
+      for (int x = threadIdx.x; x < fd.m; x += blockDim.x) line[x] = (T)sym_at(fd.L, fd.ld, x, s);
+      if (threadIdx.x == 0) { ib[2 * li] = fd.perm[s]; ib[2 * li + 1] = fd.opos[s]; }
+    }
+    __syncthreads();
+    for (int li = 0; li < nl; ++li) {
+      const int s = (li < sr.npairs) ? sr.a0 + li : sr.b0 + (li - sr.npairs);
+      const int ps = swap_partner(sr, s);
+      const int pli =
+          (ps >= sr.a0 && ps < sr.a0 + sr.npairs) ? ps - sr.a0 : sr.npairs + (ps - sr.b0);
+      const T* line = fd.swapbuf + (int64_t)pli * fd.ld;
+      for (int x = threadIdx.x; x < fd.m; x += blockDim.x) {
+        const T v = line[swap_partner(sr, x)];
+        if (x <= s) fd.L[(int64_t)x * fd.ld + s] = v;
+        else fd.L[(int64_t)s * fd.ld + x] = v;
+      }
+      if (threadIdx.x == 0) { fd.perm[s] = ib[2 * pli]; fd.opos[s] = ib[2 * pli + 1]; }
+    }
+    __syncthreads();  // the buffer is refilled by the next 32 pairs
+  }
+}
+
+// One CTA per front (failures are rare)
 template <typename T>
 __global__ void k_app_swap(FrontDesc<T>* fds, const FrontState* sts, const int* fronts) {
   const int f = fronts[blockIdx.x];
@@ -1079,27 +1122,102 @@ __global__ void k_app_swap(FrontDesc<T>* fds, const FrontState* sts, const int* 
   pdl_trigger();
   const FrontState st = sts[f];
   if (st.bs == 0 || st.bs == st.npass) return;
-  SwapRanges sr = swap_ranges(st);
-  const int nl = 2 * sr.npairs;
-  int* ib = reinterpret_cast<int*>(fd.swapbuf + (int64_t)nl * fd.ld);
-  for (int li = 0; li < nl; ++li) {
-    const int s = (li < sr.npairs) ? sr.a0 + li : sr.b0 + (li - sr.npairs);
-    T* line = fd.swapbuf + (int64_t)li * fd.ld;
-    for (int x = threadIdx.x; x < fd.m; x += blockDim.x) line[x] = (T)sym_at(fd.L, fd.ld, x, s);
-    if (threadIdx.x == 0) { ib[2 * li] = fd.perm[s]; ib[2 * li + 1] = fd.opos[s]; }
+  const SwapRanges sr = swap_ranges(st);
+  swap_lines(fd, sr.a0, sr.b0, sr.npairs);
+}
+
+// ------------------------------------------------------------------------
+// Panel end (fronts with panels): fold the panel's last block step, record
+// pk = p - pstart, and form LD = L D of the trailing rows [qend, n) for the
+// panel's pivots [pstart, p), column k at fd.LD + k * n (2x2 pivots never
+// straddle a panel: Column::adjust keeps them whole).  The tensor-core
+// update C[qend:m, qend:n] -= L[qend:m, pstart:p] LD^T follows.
+// ------------------------------------------------------------------------
+__global__ void k_panel_fold(FrontState* sts, const int* fronts, int nf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nf) return;
+  FrontState* st = &sts[fronts[i]];
+  if (st->bs > 0) {
+    st->p += st->npass;
+    st->end -= st->bs - st->npass;
+    st->bs = 0;
+  }
+  st->pk = st->p - st->pstart;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_panel_ld(FrontDesc<T>* fds, const FrontState* sts,
+                                                  const int* fronts) {
+  const int f = fronts[blockIdx.z];
+  const FrontDesc<T> fd = fds[f];
+  const FrontState st = sts[f];
+  const int K = st.pk, c0 = blockIdx.y * kLdCols;
+  const int q = st.qend, rows = fd.n - q;
+  if (c0 >= K || rows <= 0 || st.status != kDevOk) return;
+  const int nc = min(kLdCols, K - c0);
+  const int pe = st.pstart + K;  // end of the panel's pivots
+  __shared__ double alpha[kLdCols], beta[kLdCols];
+  __shared__ int partner[kLdCols];
+  if ((int)threadIdx.x < nc) {
+    const int c = st.pstart + c0 + threadIdx.x;
+    const double d11 = fd.D[2 * c];
+    if (isinf(d11)) {  // second column of a 2x2
+      const double a = fd.D[2 * (c - 1)], b = fd.D[2 * (c - 1) + 1], d = fd.D[2 * c + 1];
+      const double det = a * d - b * b;
+      alpha[threadIdx.x] = a / det; beta[threadIdx.x] = -b / det; partner[threadIdx.x] = c - 1;
+    } else if (c + 1 < pe && isinf(fd.D[2 * c + 2])) {  // first column of a 2x2
+      const double b = fd.D[2 * c + 1], d = fd.D[2 * c + 3];
+      const double det = d11 * d - b * b;
+      alpha[threadIdx.x] = d / det; beta[threadIdx.x] = -b / det; partner[threadIdx.x] = c + 1;
+    } else {
+      alpha[threadIdx.x] = (d11 != 0.0) ? 1.0 / d11 : 0.0; beta[threadIdx.x] = 0.0;
+      partner[threadIdx.x] = c;
+    }
   }
   __syncthreads();
-  for (int li = 0; li < nl; ++li) {
-    const int s = (li < sr.npairs) ? sr.a0 + li : sr.b0 + (li - sr.npairs);
-    const int ps = swap_partner(sr, s);
-    const int pli = (ps >= sr.a0 && ps < sr.a0 + sr.npairs) ? ps - sr.a0 : sr.npairs + (ps - sr.b0);
-    const T* line = fd.swapbuf + (int64_t)pli * fd.ld;
-    for (int x = threadIdx.x; x < fd.m; x += blockDim.x) {
-      const T v = line[swap_partner(sr, x)];
-      if (x <= s) fd.L[(int64_t)x * fd.ld + s] = v;
-      else fd.L[(int64_t)s * fd.ld + x] = v;
+  for (int rr = blockIdx.x * blockDim.x + threadIdx.x; rr < rows; rr += gridDim.x * blockDim.x) {
+    const T* Lr = fd.L + q + rr;
+    T lv[kLdCols], lp[kLdCols];
+#pragma unroll
+    for (int k = 0; k < kLdCols; ++k) {
+      lv[k] = (k < nc) ? Lr[(int64_t)(st.pstart + c0 + k) * fd.ld] : T(0);
+      lp[k] = (k < nc && beta[k] != 0.0) ? Lr[(int64_t)partner[k] * fd.ld] : T(0);
     }
-    if (threadIdx.x == 0) { fd.perm[s] = ib[2 * pli]; fd.opos[s] = ib[2 * pli + 1]; }
+#pragma unroll
+    for (int k = 0; k < kLdCols; ++k)
+      if (k < nc)
+        fd.LD[(int64_t)(c0 + k) * fd.n + rr] = (T)(alpha[k] * (double)lv[k] + beta[k] * (double)lp[k]);
+  }
+}
+
+// Panel close (one CTA per front): the panel's failed columns [end, qend)
+// (kept up to date by every pivot of the panel, and now also complete with
+// respect to the trailing update) trade places with the last candidates of
+// the front [gend - nf, gend), which have all of the panel's updates too;
+// the candidate range shrinks by nf and the next panel [p, min(p + panel,
+// gend)) opens.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_panel_close(FrontDesc<T>* fds, FrontState* sts,
+                                                      const int* fronts) {
+  const int f = fronts[blockIdx.x];
+  const FrontDesc<T> fd = fds[f];
+  FrontState* st = &sts[f];
+  const int p = st->p, end = st->end, qend = st->qend, gend = st->gend;
+  if (st->status != kDevOk) return;
+  const int nf = qend - end;
+  if (nf > 0) {
+    const int fs = end, fe = qend, ts = gend - nf;
+    const int b0 = max(ts, fe);
+    const int npairs = max(0, min(fe, ts) - fs);
+    swap_lines(fd, fs, b0, npairs);
+  }
+  if (threadIdx.x == 0) {
+    const int g = gend - max(nf, 0);
+    st->gend = g;
+    st->pstart = p;
+    st->qend = min(p + fd.panel, g);
+    st->end = st->qend;
+    st->bs = 0;
   }
 }
 
@@ -1619,7 +1737,6 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, Fr
 // Grid: (row blocks of 128, column chunks of kLdCols, fronts).  Each thread
 // issues the loads of all of its chunk's columns before the first store, so
 // one memory round trip covers kLdCols columns.
-constexpr int kLdCols = 16;
 template <typename T>
 __global__ void __launch_bounds__(128) k_calc_ld(FrontDesc<T>* fds, const FrontState* sts,
                                                  const int* fronts) {
@@ -1773,6 +1890,25 @@ void launch_app_finish(FrontDesc<T>* fd, FrontState* st, const int* fronts, int 
 }
 
 template <typename T>
+void launch_panel_end(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_n,
+                      int panel, cudaStream_t s) {
+  if (nf <= 0) return;
+  k_panel_fold<<<cdiv(nf, 128), 128, 0, s>>>(st, fronts, nf);
+  const int gx = std::max(1, std::min(cdiv(max_n, 128), 64));
+  const int gy = std::max(1, cdiv(panel, kLdCols));
+  k_panel_ld<T><<<dim3(gx, gy, nf), 128, 0, s>>>(fd, st, fronts);
+  note_launches(2);
+}
+
+template <typename T>
+void launch_panel_close(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf,
+                        cudaStream_t s) {
+  if (nf <= 0) return;
+  k_panel_close<T><<<nf, 1024, 0, s>>>(fd, st, fronts);
+  note_launches(1);
+}
+
+template <typename T>
 void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
                 double u, double small, bool all_fronts, cudaStream_t s) {
   if (nf <= 0) return;
@@ -1828,6 +1964,9 @@ void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* front
   template void launch_app_step<T>(FrontDesc<T>*, FrontState*, const int*, int, int, int, int,  \
                                    int, bool, double, double, cudaStream_t, PhaseTimer*, bool); \
   template void launch_app_finish<T>(FrontDesc<T>*, FrontState*, const int*, int, cudaStream_t); \
+  template void launch_panel_end<T>(FrontDesc<T>*, FrontState*, const int*, int, int, int,      \
+                                    cudaStream_t);                                              \
+  template void launch_panel_close<T>(FrontDesc<T>*, FrontState*, const int*, int, cudaStream_t); \
   template void launch_tpp<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double, double, \
                               bool, cudaStream_t);                                              \
   template void launch_tpp_small<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double,  \

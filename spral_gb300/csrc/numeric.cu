@@ -787,6 +787,8 @@ struct Numeric : NumericBase {
   int tc_min_k = 256;
   TcBuffers tcbuf;
   DevBuf<char> tc_scratch;
+  int panel_nb = 256;       // APP panel width (FP32 fronts with tensor cores)
+  DevBuf<int> panel_list;   // fronts ending a panel (eager mode)
   int* d_tc_status = nullptr;
   int* d_ncount = nullptr;  // per-node inertia counts (neg, two, zero)
 
@@ -802,6 +804,78 @@ struct Numeric : NumericBase {
     if (posdef || S->copts.pivot_method == 3) return S->lvl_start[l + 1] - S->lvl_start[l];
     return S->lvl_napp[l];
   }
+  // APP panels (FP32 factors with tensor cores): a front with more than
+  // panel_nb fully-summed columns is factored in panels of panel_nb columns;
+  // the block steps of a panel update only the panel, and the panel's
+  // trailing update (all later fully-summed columns and their rows below)
+  // runs once per panel on the tensor cores with the panel's pivots as its
+  // depth.  Returns the panel width of front f, or 0.
+  int panel_cols(int f) const {
+    if (!std::is_same<T, float>::value || !use_tc || panel_nb <= 0) return 0;
+    if (tpp_front(f) || S->copts.pivot_method == 3) return 0;
+    return n_[f] > panel_nb ? panel_nb : 0;
+  }
+  // fronts of [f0, f1) whose current panel ends with block step st
+  void panel_boundary(int f0, int f1, int st, std::vector<int>& out) const {
+    out.clear();
+    const int per = panel_nb / kBlk;
+    for (int f = f0; f < f1; ++f) {
+      if (!hfd[f].panel) continue;
+      const int steps_f = (n_[f] + kBlk - 1) / kBlk;
+      if (st + 1 > steps_f) continue;
+      if ((st + 1) % per == 0 || st + 1 == steps_f) out.push_back(f);
+    }
+  }
+  // the tensor-core trailing update of a closed panel: pivots [pstart,
+  // pstart + k) of front f, trailing block [q, m) x [q, n)
+  TcProblem panel_problem(int f, int pstart, int q, int k) const {
+    const FrontDesc<T>& d = hfd[f];
+    TcProblem pr;
+    pr.A = reinterpret_cast<const float*>(d.L + (int64_t)pstart * d.ld + q);
+    pr.lda = d.ld;
+    pr.B = reinterpret_cast<const float*>(d.LD);
+    pr.ldb = d.n;
+    pr.C = reinterpret_cast<float*>(d.L + (int64_t)q * d.ld + q);
+    pr.ldc = d.ld;
+    pr.M = d.m - q;
+    pr.N = d.n - q;
+    pr.kmax = k;
+    pr.kval_dev = &d_st[f].pk;
+    pr.lower = 1;
+    return pr;
+  }
+  // end of panels in eager mode: the panels' geometry is read back (failed
+  // columns move panel boundaries), then the trailing updates and the close
+  void panel_end_eager(const std::vector<int>& fl, cudaStream_t s) {
+    const int nfl = (int)fl.size();
+    panel_list.ensure(nfl);
+    CK(cudaMemcpyAsync(panel_list.p, fl.data(), nfl * sizeof(int), cudaMemcpyHostToDevice, s));
+    int max_n = 0;
+    for (int f : fl) max_n = std::max(max_n, n_[f]);
+    launch_panel_end<T>(d_fd, d_st, panel_list.p, nfl, max_n, panel_nb, s);
+    for (int f : fl)
+      CK(cudaMemcpyAsync(&hst[f], &d_st[f], sizeof(FrontState), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<TcProblem> ps;
+    double fl_tc = 0;
+    for (int f : fl) {
+      const FrontState& q = hst[f];
+      if (q.status != kDevOk || q.pk <= 0 || q.qend >= n_[f]) continue;
+      ps.push_back(panel_problem(f, q.pstart, q.qend, q.pk));
+      const double M = m_[f] - q.qend, N = n_[f] - q.qend;
+      fl_tc += 2.0 * q.pk * (N * (N + 1) / 2 + (M - N) * N);
+    }
+    if (!ps.empty()) {
+      tc_scratch.ensure(tc_gemm_scratch_bytes(ps));
+      float ms_split = 0, ms_gemm = 0;
+      if (tc_gemm_run(ps, tc_scratch.p, tcbuf, d_tc_status, s, tc_chunk,
+                      profile ? &ms_split : nullptr, profile ? &ms_gemm : nullptr) != 0)
+        throw CudaFail{cudaErrorUnknown, __LINE__};
+      if (profile) { prof_tc_ms += ms_gemm; prof_tc_launches += 1; prof_tc_flops += fl_tc; }
+    }
+    launch_panel_close<T>(d_fd, d_st, panel_list.p, nfl, s);
+  }
+
   // shared-memory staging of a small leaf front (k_tpp_small): the front,
   // two workspace columns, perm and opos, bytes
   int tpp_bytes(int f) const {
@@ -891,7 +965,7 @@ struct Numeric : NumericBase {
         ndin_[f] = 0; m_[f] = m; n_[f] = n; ld_[f] = ld;
         w1 += (size_t)ld * kBlk;
         w2 += (size_t)ld * 64 + 256;
-        w3 += (size_t)cm * n;
+        w3 += (size_t)std::max(cm, panel_cols(f)) * n;
         fg_maxfront = std::max(fg_maxfront, m);
         fg_maxsn = std::max(fg_maxsn, n);
         for (int c : S->children[node]) doff_[S->front_of[c]] = 0;
@@ -928,17 +1002,59 @@ struct Numeric : NumericBase {
         d.C = d.cm > 0 ? contrib.p + S->contrib_off[f] : nullptr;
         d.W = ws_W.p + oW; oW += (size_t)d.ld * kBlk;
         d.swapbuf = ws_swap.p + oS; oS += (size_t)d.ld * 64 + 256;
-        d.LD = ws_LD.p + oL; oL += (size_t)d.cm * d.n;
+        d.LD = ws_LD.p + oL; oL += (size_t)std::max(d.cm, panel_cols(f)) * d.n;
         d.step = ws_step.p + (size_t)(f - f0) * (kBlk * kBlk + 2 * kBlk + 64);
         d.lperm = ws_lperm.p + (size_t)(f - f0) * kBlk;
         d.tc = (use_tc && d.cm >= tc_min_cm && d.n >= tc_min_k) ? 1 : 0;
+        d.panel = panel_cols(f);
       }
     }
     fg_hfd = hfd;
     CK(cudaMemcpy(d_fd, hfd.data(), nn * sizeof(FrontDesc<T>), cudaMemcpyHostToDevice));
-    // tensor-core job tables, one device blob per level
-    std::vector<TcPlan> tplans(S->nlev);
-    std::vector<const void*> tblob(S->nlev, nullptr);
+    // panel ends of the fronts with panels, with the static geometry of a
+    // factorisation without failed columns (panel j covers [j nb, (j+1) nb))
+    struct PanelStep {
+      int l, st, off, nl, max_n, pp;  // pp: index into pps (-1: no update)
+    };
+    std::vector<PanelStep> psteps;
+    std::vector<int> plist;
+    std::vector<std::vector<TcProblem>> pps;
+    {
+      const int per = std::max(panel_nb / kBlk, 1);
+      std::vector<int> pfl;
+      for (int l = 0; l < S->nlev; ++l) {
+        const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1];
+        int mx = 0;
+        for (int f = f0; f < f1; ++f) if (hfd[f].panel) mx = std::max(mx, n_[f]);
+        if (mx == 0) continue;
+        for (int st = 0; st < (mx + kBlk - 1) / kBlk; ++st) {
+          panel_boundary(f0, f1, st, pfl);
+          if (pfl.empty()) continue;
+          PanelStep ps{l, st, (int)plist.size(), (int)pfl.size(), 0, -1};
+          std::vector<TcProblem> pr;
+          for (int f : pfl) {
+            plist.push_back(f);
+            ps.max_n = std::max(ps.max_n, n_[f]);
+            const int j = st / per, pstart = j * panel_nb;
+            const int q = std::min((j + 1) * panel_nb, n_[f]);
+            if (q < n_[f]) pr.push_back(panel_problem(f, pstart, q, q - pstart));
+          }
+          if (!pr.empty()) { ps.pp = (int)pps.size(); pps.push_back(pr); }
+          psteps.push_back(ps);
+        }
+      }
+    }
+    const int* d_plist = nullptr;
+    if (!plist.empty()) {
+      void* b = nullptr;
+      CK(cudaMalloc(&b, plist.size() * sizeof(int)));
+      fgraph_blobs.push_back(b);
+      CK(cudaMemcpy(b, plist.data(), plist.size() * sizeof(int), cudaMemcpyHostToDevice));
+      d_plist = static_cast<const int*>(b);
+    }
+    // tensor-core job tables, one device blob per level and per panel end
+    std::vector<TcPlan> tplans(S->nlev), pplans(pps.size());
+    std::vector<const void*> tblob(S->nlev, nullptr), pblob(pps.size(), nullptr);
     if (use_tc) {
       size_t scr = 0;
       std::vector<std::vector<TcProblem>> lps(S->nlev);
@@ -946,18 +1062,22 @@ struct Numeric : NumericBase {
         lps[l] = tc_problems(S->lvl_start[l], S->lvl_start[l + 1]);
         if (!lps[l].empty()) scr = std::max(scr, tc_gemm_scratch_bytes(lps[l]));
       }
+      for (auto& pr : pps) scr = std::max(scr, tc_gemm_scratch_bytes(pr));
       if (scr > 0) tc_scratch.ensure(scr);
-      for (int l = 0; l < S->nlev; ++l) {
-        if (lps[l].empty()) continue;
-        if (tc_gemm_prepare(lps[l], tc_scratch.p, tplans[l]) != 0)
+      auto upload_plan = [&](const std::vector<TcProblem>& pr, TcPlan& plan) -> const void* {
+        if (tc_gemm_prepare(pr, tc_scratch.p, plan) != 0)
           throw CudaFail{cudaErrorUnknown, __LINE__};
         void* b = nullptr;
-        CK(cudaMalloc(&b, tplans[l].blob.size()));
+        CK(cudaMalloc(&b, plan.blob.size()));
         fgraph_blobs.push_back(b);
-        CK(cudaMemcpy(b, tplans[l].blob.data(), tplans[l].blob.size(), cudaMemcpyHostToDevice));
-        tblob[l] = b;
-      }
+        CK(cudaMemcpy(b, plan.blob.data(), plan.blob.size(), cudaMemcpyHostToDevice));
+        return b;
+      };
+      for (int l = 0; l < S->nlev; ++l)
+        if (!lps[l].empty()) tblob[l] = upload_plan(lps[l], tplans[l]);
+      for (size_t i = 0; i < pps.size(); ++i) pblob[i] = upload_plan(pps[i], pplans[i]);
     }
+    size_t pstep_i = 0;
     const double* d_scale = scaled ? scale_buf.p : nullptr;
     std::lock_guard<std::mutex> lock(g_capture_mutex);
     const long long l0 = t_launches;
@@ -998,10 +1118,19 @@ struct Numeric : NumericBase {
             if (tpp_front(f)) continue;
             mr = std::max(mr, m_[f] - kBlk * st);
             tr = std::max(tr, m_[f] - kBlk * (st + 1));
-            tc = std::max(tc, n_[f] - kBlk * (st + 1));
+            const int cols = n_[f] - kBlk * (st + 1);
+            tc = std::max(tc, hfd[f].panel ? std::min(cols, hfd[f].panel) : cols);
           }
           launch_app_step<T>(d_fd, d_st, fr, napp, st, std::max(mr, 1), tr, tc, co.action,
                              posdef ? 0.0 : co.u, co.small, s, nullptr, posdef);
+          if (pstep_i < psteps.size() && psteps[pstep_i].l == l && psteps[pstep_i].st == st) {
+            const PanelStep& ps = psteps[pstep_i++];
+            launch_panel_end<T>(d_fd, d_st, d_plist + ps.off, ps.nl, ps.max_n, panel_nb, s);
+            if (ps.pp >= 0 &&
+                tc_gemm_launch(pplans[ps.pp], pblob[ps.pp], d_tc_status, s, tc_chunk) != 0)
+              throw CudaFail{cudaErrorUnknown, __LINE__};
+            launch_panel_close<T>(d_fd, d_st, d_plist + ps.off, ps.nl, s);
+          }
         }
         launch_app_finish<T>(d_fd, d_st, fr, nf, s);
         const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
@@ -1168,6 +1297,8 @@ struct Numeric : NumericBase {
       else if (use_tc) tc_min_cm = autotune_tc_min_cm();
       const char* mk = getenv("SPRAL_GB300_TC_MIN_K");
       if (mk) tc_min_k = std::max(0, atoi(mk));
+      const char* pn = getenv("SPRAL_GB300_PANEL");
+      if (pn) panel_nb = std::max(0, atoi(pn)) / kBlk * kBlk;
     }
     contrib.ensure(std::max<int64_t>(S->contrib_total, 1));
     // factor storage estimate (no delays) + 10%
@@ -1269,7 +1400,7 @@ struct Numeric : NumericBase {
         max_ent = std::max<int>(max_ent, (int)(S->nptr[node + 1] - S->nptr[node]));
         wsW += (size_t)ld * kBlk;
         wsSwap += (size_t)ld * 64 + 256;
-        wsLD += (size_t)cm * n;
+        wsLD += (size_t)std::max(cm, panel_cols(f)) * n;
         maxfront = std::max(maxfront, m);
         maxsn = std::max(maxsn, n);
       }
@@ -1300,10 +1431,11 @@ struct Numeric : NumericBase {
         d.C = d.cm > 0 ? contrib.p + S->contrib_off[f] : nullptr;
         d.W = ws_W.p + oW; oW += (size_t)ld * kBlk;
         d.swapbuf = ws_swap.p + oS; oS += (size_t)ld * 64 + 256;
-        d.LD = ws_LD.p + oL; oL += (size_t)d.cm * n;
+        d.LD = ws_LD.p + oL; oL += (size_t)std::max(d.cm, panel_cols(f)) * n;
         d.step = ws_step.p + (size_t)(f - f0) * (kBlk * kBlk + 2 * kBlk + 64);
         d.lperm = ws_lperm.p + (size_t)(f - f0) * kBlk;
         d.tc = (use_tc && d.cm >= tc_min_cm && d.n >= tc_min_k) ? 1 : 0;
+        d.panel = panel_cols(f);
       }
       CK(cudaMemcpyAsync(d_fd + f0, hfd.data() + f0, nf * sizeof(FrontDesc<T>),
                          cudaMemcpyHostToDevice, s));
@@ -1332,6 +1464,9 @@ struct Numeric : NumericBase {
                                  S->d_rdir_ptr, s);
       // dense factorisation
       const bool use_app = co.pivot_method != 3;
+      bool any_panel = false;
+      for (int f = f0; f < f1; ++f) any_panel = any_panel || hfd[f].panel > 0;
+      std::vector<int> pfl;
       if (use_app) {
         const int steps = (max_app_n + kBlk - 1) / kBlk;
         for (int st = 0; st < steps; ++st) {
@@ -1340,10 +1475,18 @@ struct Numeric : NumericBase {
             if (tpp_front(f)) continue;
             mr = std::max(mr, m_[f] - kBlk * st);
             tr = std::max(tr, m_[f] - kBlk * (st + 1));
-            tc = std::max(tc, n_[f] - kBlk * (st + 1));
+            const int cols = n_[f] - kBlk * (st + 1);
+            tc = std::max(tc, hfd[f].panel ? std::min(cols, hfd[f].panel) : cols);
           }
           launch_app_step<T>(d_fd, d_st, fr, napp, st, std::max(mr, 1), tr, tc, co.action,
                              posdef ? 0.0 : co.u, co.small, s, tm(), posdef);
+          if (any_panel) {
+            panel_boundary(f0, f1, st, pfl);
+            if (!pfl.empty()) {
+              pmark(tm(), kPhPanel, s);
+              panel_end_eager(pfl, s);
+            }
+          }
         }
       }
       pmark(tm(), kPhFinish, s);

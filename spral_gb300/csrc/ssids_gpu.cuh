@@ -76,18 +76,29 @@ struct FrontDesc {
   int node;
   int ldc;       // leading dimension of C (cm for the tree's own blocks)
   int tc;        // contribution block formed by the tensor-core GEMM
-  int pad2;
+  int panel;     // > 0: APP in panels of this many candidate columns (see below)
 };
 
+// Panels (FP32 factors, fronts wider than FrontDesc::panel): the APP block
+// steps draw their candidates from a panel of `panel` columns [pstart, qend)
+// and update only the panel's columns; at the panel's end the trailing
+// fully-summed columns [qend, n) take the panel's pk pivots in one
+// tensor-core update, and the panel's failed columns move to the end of the
+// front's candidate range [.., gend).  Other fronts have one panel with
+// qend = gend = n.
 struct FrontState {
   int p;          // number eliminated so far (APP)
-  int end;        // end of the APP candidate range
+  int end;        // end of the APP candidate range (of the current panel)
   int bs;         // current block width (0 = done)
   int npass_raw;  // first failing column from the threshold test
   int npass;      // adjusted (2x2 not split)
   int nelim;      // final
   int status;     // DevStatus
   int step;       // step counter (sanity)
+  int pstart;     // first position of the current panel
+  int qend;       // end of the current panel's columns (bound of its updates)
+  int gend;       // end of the front's candidate range
+  int pk;         // pivots of the last closed panel
 };
 
 struct Stats {  // device-side reduction target (integers only -> deterministic)
@@ -145,6 +156,17 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
 template <typename T>
 void launch_app_finish(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf,
                        cudaStream_t s);
+// End of a panel for the listed fronts: fold the last block step and form
+// LD = L D for the trailing rows [qend, n) of the panel's pivots into fd.LD
+// (column k at fd.LD + k * n); max_n bounds n over the listed fronts.
+template <typename T>
+void launch_panel_end(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_n,
+                      int panel, cudaStream_t s);
+// After the panel's trailing update: move its failed columns to the end of
+// the candidate range and open the next panel.
+template <typename T>
+void launch_panel_close(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf,
+                        cudaStream_t s);
 template <typename T>
 void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
                 double u, double small, bool root_only_or_all, cudaStream_t s);
