@@ -60,11 +60,13 @@ __global__ void k_init_perm(const FrontDesc<T>* fds, const int* fronts, const in
   }
 }
 
-// work[i] = (parent front, child front, first delay column in parent, 0)
+// work[i] = (parent front, child front, first delay column in parent, 0);
+// grid (column groups, work items): CTA x takes the child's delayed columns
+// x, x + gridDim.x, ... (each column independent of the others)
 template <typename T>
 __global__ void k_assemble_delays(const FrontDesc<T>* fds, const FrontState* sts, const int4* work,
                                   const int* rdir, const int64_t* rdir_ptr) {
-  const int4 w = work[blockIdx.x];
+  const int4 w = work[blockIdx.y];
   const FrontDesc<T> fp = fds[w.x];
   const FrontDesc<T> fc = fds[w.y];
   const int nel = sts[w.y].nelim;
@@ -72,7 +74,7 @@ __global__ void k_assemble_delays(const FrontDesc<T>* fds, const FrontState* sts
   const int dcol0 = w.z;
   const int* rd = rdir + rdir_ptr[fc.node];
   const int cmc = fc.m - fc.n;
-  for (int i = 0; i < nd; ++i) {
+  for (int i = blockIdx.x; i < nd; i += gridDim.x) {
     const int sc = nel + i, dcol = dcol0 + i;
     const T* src = fc.L + (int64_t)sc * fc.ld;
     for (int j = i + threadIdx.x; j < nd; j += blockDim.x)
@@ -157,9 +159,11 @@ void launch_init_perm(const FrontDesc<T>* fd, const int* fronts, int nf, const i
 }
 template <typename T>
 void launch_assemble_delays(const FrontDesc<T>* fd, const FrontState* st, const int4* work,
-                            int nwork, const int* rdir, const int64_t* rdir_ptr, cudaStream_t s) {
+                            int nwork, int max_nd, const int* rdir, const int64_t* rdir_ptr,
+                            cudaStream_t s) {
   if (nwork <= 0) return;
-  { k_assemble_delays<T><<<nwork, 128, 0, s>>>(fd, st, work, rdir, rdir_ptr); note_launches(1); }
+  const int gx = std::max(1, std::min(max_nd, 256));
+  { k_assemble_delays<T><<<dim3(gx, nwork), 128, 0, s>>>(fd, st, work, rdir, rdir_ptr); note_launches(1); }
 }
 template <typename T>
 void launch_assemble_contrib(const FrontDesc<T>* fd, const int4* cols, int ncols,
@@ -176,7 +180,7 @@ void launch_assemble_contrib(const FrontDesc<T>* fd, const int4* cols, int ncols
   template void launch_init_perm<T>(const FrontDesc<T>*, const int*, int, const int*, int,      \
                                     cudaStream_t);                                               \
   template void launch_assemble_delays<T>(const FrontDesc<T>*, const FrontState*, const int4*,  \
-                                          int, const int*, const int64_t*, cudaStream_t);        \
+                                          int, int, const int*, const int64_t*, cudaStream_t);   \
   template void launch_assemble_contrib<T>(const FrontDesc<T>*, const int4*, int, const int2*,  \
                                            const int*, const int64_t*, cudaStream_t);
 INST(double)

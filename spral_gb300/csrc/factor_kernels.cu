@@ -1113,17 +1113,66 @@ __device__ void swap_lines(const FrontDesc<T>& fd, int a0, int b0, int npairs) {
   }
 }
 
-// One CTA per front (failures are rare)
+// The block step's failed columns trade places with the last candidates
+// (at most 32 disjoint transpositions (a0 + i, b0 + i)).  For a line x
+// outside the swapped set, the transposition only exchanges the entries
+// (x, a0 + i) and (x, b0 + i): CTAs 1.. take the lines x, one thread per
+// line, which touch disjoint entries (a row of contiguous entries when x
+// lies left of the set, coalesced columns when it lies right of it).  CTA 0
+// permutes the block of entries between the swapped lines themselves, and
+// perm and opos, through shared memory.  No barrier across CTAs is needed.
 template <typename T>
-__global__ void k_app_swap(FrontDesc<T>* fds, const FrontState* sts, const int* fronts) {
-  const int f = fronts[blockIdx.x];
+__device__ __forceinline__ T* sym_ptr(T* L, int ld, int r, int c) {
+  return r >= c ? L + (int64_t)c * ld + r : L + (int64_t)r * ld + c;
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_app_swap(FrontDesc<T>* fds, const FrontState* sts,
+                                                  const int* fronts) {
+  const int f = fronts[blockIdx.y];
   FrontDesc<T> fd = fds[f];  // written by the host before the launch
   pdl_wait();
   pdl_trigger();
   const FrontState st = sts[f];
   if (st.bs == 0 || st.bs == st.npass) return;
   const SwapRanges sr = swap_ranges(st);
-  swap_lines(fd, sr.a0, sr.b0, sr.npairs);
+  const int np = sr.npairs;
+  if (np <= 0) return;
+  const int nl = 2 * np;
+  auto line = [&](int i) { return i < np ? sr.a0 + i : sr.b0 + (i - np); };
+  if (blockIdx.x == 0) {
+    __shared__ T blk[2 * kBlk][2 * kBlk + 1];
+    __shared__ int pp[2 * kBlk], oo[2 * kBlk];
+    for (int e = threadIdx.x; e < nl * nl; e += blockDim.x) {
+      const int i = e / nl, j = e % nl;
+      blk[i][j] = *sym_ptr(fd.L, fd.ld, line(i), line(j));
+    }
+    for (int i = threadIdx.x; i < nl; i += blockDim.x) { pp[i] = fd.perm[line(i)]; oo[i] = fd.opos[line(i)]; }
+    __syncthreads();
+    // new(s_i, s_j) = old(partner(s_i), partner(s_j)); partner swaps halves
+    for (int e = threadIdx.x; e < nl * nl; e += blockDim.x) {
+      const int i = e / nl, j = e % nl;
+      if (line(i) < line(j)) continue;  // each stored entry once
+      const int pi = i < np ? i + np : i - np, pj = j < np ? j + np : j - np;
+      *sym_ptr(fd.L, fd.ld, line(i), line(j)) = blk[pi][pj];
+    }
+    for (int i = threadIdx.x; i < nl; i += blockDim.x) {
+      const int pi = i < np ? i + np : i - np;
+      fd.perm[line(i)] = pp[pi];
+      fd.opos[line(i)] = oo[pi];
+    }
+    return;
+  }
+  for (int x = (blockIdx.x - 1) * blockDim.x + threadIdx.x; x < fd.m;
+       x += (gridDim.x - 1) * blockDim.x) {
+    if ((x >= sr.a0 && x < sr.a0 + np) || (x >= sr.b0 && x < sr.b0 + np)) continue;
+    for (int i = 0; i < np; ++i) {
+      T* pa = sym_ptr(fd.L, fd.ld, x, sr.a0 + i);
+      T* pb = sym_ptr(fd.L, fd.ld, x, sr.b0 + i);
+      const T va = *pa, vb = *pb;
+      *pa = vb;
+      *pb = va;
+    }
+  }
 }
 
 // ------------------------------------------------------------------------
@@ -1241,231 +1290,6 @@ __global__ void k_app_finish(FrontDesc<T>* fds, FrontState* sts, const int* fron
 // ------------------------------------------------------------------------
 constexpr int kTppThreads = 256;
 
-__device__ __forceinline__ double block_max(double v, double* red) {
-  for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double r = red[0];
-  for (int i = 1; i < (int)(blockDim.x >> 5); ++i) r = fmax(r, red[i]);
-  __syncthreads();
-  return r;
-}
-
-template <typename T>
-__device__ void tpp_sym_swap(FrontDesc<T>& fd, int i, int j) {
-  if (i == j) return;
-  if (j < i) { int t = i; i = j; j = t; }
-  T* L = fd.L;
-  const int ld = fd.ld;
-  for (int c = threadIdx.x; c < i; c += blockDim.x) {
-    T t = L[(int64_t)c * ld + i]; L[(int64_t)c * ld + i] = L[(int64_t)c * ld + j]; L[(int64_t)c * ld + j] = t;
-  }
-  for (int r = i + 1 + threadIdx.x; r < j; r += blockDim.x) {
-    T t = L[(int64_t)i * ld + r]; L[(int64_t)i * ld + r] = L[(int64_t)r * ld + j]; L[(int64_t)r * ld + j] = t;
-  }
-  if (threadIdx.x == 0) {
-    T t = L[(int64_t)i * ld + i]; L[(int64_t)i * ld + i] = L[(int64_t)j * ld + j]; L[(int64_t)j * ld + j] = t;
-    int pt = fd.perm[i]; fd.perm[i] = fd.perm[j]; fd.perm[j] = pt;
-    int ot = fd.opos[i]; fd.opos[i] = fd.opos[j]; fd.opos[j] = ot;
-  }
-  for (int r = j + 1 + threadIdx.x; r < fd.m; r += blockDim.x) {
-    T t = L[(int64_t)i * ld + r]; L[(int64_t)i * ld + r] = L[(int64_t)j * ld + r]; L[(int64_t)j * ld + r] = t;
-  }
-  __syncthreads();
-}
-
-template <typename T>
-__device__ bool tpp_col_small(const FrontDesc<T>& fd, int idx, int from, double small, double* red) {
-  double v = 0.0;
-  for (int c = from + threadIdx.x; c < idx; c += blockDim.x) v = fmax(v, fabs((double)fd.L[(int64_t)c * fd.ld + idx]));
-  for (int r = idx + threadIdx.x; r < fd.m; r += blockDim.x) v = fmax(v, fabs((double)fd.L[(int64_t)idx * fd.ld + r]));
-  return block_max(v, red) < small;
-}
-
-template <typename T>
-__device__ double tpp_rc_max_excl(const FrontDesc<T>& fd, int col, int nel, int excl, double* red) {
-  double v = 0.0;
-  for (int c = nel + threadIdx.x; c < col; c += blockDim.x)
-    if (c != excl) v = fmax(v, fabs((double)fd.L[(int64_t)c * fd.ld + col]));
-  for (int r = col + 1 + threadIdx.x; r < fd.m; r += blockDim.x)
-    if (r != excl) v = fmax(v, fabs((double)fd.L[(int64_t)col * fd.ld + r]));
-  return block_max(v, red);
-}
-
-template <typename T>
-__device__ void tpp_zero_col(FrontDesc<T>& fd, int col) {
-  for (int r = col + threadIdx.x; r < fd.m; r += blockDim.x) fd.L[(int64_t)col * fd.ld + r] = T(0);
-  if (threadIdx.x == 0) { fd.D[2 * col] = 0.0; fd.D[2 * col + 1] = 0.0; }
-  __syncthreads();
-}
-
-// scale pivot column(s) at nel, keep unscaled copy in W, update trailing
-template <typename T>
-__device__ void tpp_apply(FrontDesc<T>& fd, int nel, int ps, double d11, double d21, double d22) {
-  T* L = fd.L;
-  const int ld = fd.ld, m = fd.m, n = fd.n;
-  T* w0 = fd.W;            // unscaled copies indexed by row
-  T* w1 = fd.W + fd.ld;
-  if (ps == 1) {
-    for (int r = nel + 1 + threadIdx.x; r < m; r += blockDim.x) {
-      double a = (double)L[(int64_t)nel * ld + r];
-      w0[r] = (T)a;
-      L[(int64_t)nel * ld + r] = (T)(a * d11);
-    }
-    if (threadIdx.x == 0) { L[(int64_t)nel * ld + nel] = T(1); fd.D[2 * nel] = d11; fd.D[2 * nel + 1] = 0.0; }
-  } else {
-    for (int r = nel + 2 + threadIdx.x; r < m; r += blockDim.x) {
-      double a1 = (double)L[(int64_t)nel * ld + r], a2 = (double)L[(int64_t)(nel + 1) * ld + r];
-      w0[r] = (T)a1; w1[r] = (T)a2;
-      L[(int64_t)nel * ld + r] = (T)(d11 * a1 + d21 * a2);
-      L[(int64_t)(nel + 1) * ld + r] = (T)(d21 * a1 + d22 * a2);
-    }
-    if (threadIdx.x == 0) {
-      L[(int64_t)nel * ld + nel] = T(1);
-      L[(int64_t)nel * ld + nel + 1] = T(0);
-      L[(int64_t)(nel + 1) * ld + nel + 1] = T(1);
-      fd.D[2 * nel] = d11; fd.D[2 * nel + 1] = d21;
-      fd.D[2 * nel + 2] = dinf(); fd.D[2 * nel + 3] = d22;
-    }
-  }
-  __syncthreads();
-  // trailing update of fully-summed columns [nel+ps, n), rows [c, m)
-  const int c0 = nel + ps;
-  const int ncols = n - c0;
-  if (ncols > 0) {
-    const int64_t rows = m - c0;
-    const int64_t total = rows * ncols;
-    for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
-      int c = c0 + (int)(e / rows);
-      int r = c0 + (int)(e % rows);
-      if (r < c) continue;
-      double v = (double)w0[c] * (double)L[(int64_t)nel * ld + r];
-      if (ps == 2) v += (double)w1[c] * (double)L[(int64_t)(nel + 1) * ld + r];
-      L[(int64_t)c * ld + r] = (T)((double)L[(int64_t)c * ld + r] - v);
-    }
-  }
-  __syncthreads();
-}
-
-// The TPP loop of ldlt_tpp_factor on the columns [nel, n) of the front
-// described by fd (whose L and W may point to global or shared memory).
-// Returns the number of columns eliminated in total, or -1 for a singular
-// front with action == false.
-template <typename T>
-__device__ int tpp_body(FrontDesc<T>& fd, int nel, bool action, double u, double small,
-                        double* red, int* s_t_ptr) {
-  int& s_t = *s_t_ptr;
-  const int n = fd.n, m = fd.m;
-  const T* L = fd.L;
-  const int ld = fd.ld;
-  while (nel < n) {
-    if (tpp_col_small(fd, nel, nel, small, red)) {
-      if (!action) return -1;
-      tpp_zero_col(fd, nel);
-      nel++;
-      continue;
-    }
-    int p;
-    bool done = false;
-    for (p = nel + 1; p < n; ++p) {
-      if (tpp_col_small(fd, p, nel, small, red)) {
-        if (!action) return -1;
-        tpp_sym_swap(fd, p, nel);
-        tpp_zero_col(fd, nel);
-        nel++;
-        done = true;
-        break;
-      }
-      // t = argmax_{c in [nel, p)} |a(p, c)| (first maximum)
-      if (threadIdx.x == 0) {
-        int t = nel;
-        double bv = fabs((double)L[(int64_t)nel * ld + p]);
-        for (int c = nel + 1; c < p; ++c) {
-          double v = fabs((double)L[(int64_t)c * ld + p]);
-          if (v > bv) { bv = v; t = c; }
-        }
-        s_t = t;
-      }
-      __syncthreads();
-      const int t = s_t;
-      double maxt = tpp_rc_max_excl(fd, t, nel, p, red);
-      double maxp = tpp_rc_max_excl(fd, p, nel, t, red);
-      {
-        double a11 = (double)L[(int64_t)t * ld + t], a21 = (double)L[(int64_t)t * ld + p];
-        double a22 = (double)L[(int64_t)p * ld + p];
-        double maxpiv = fmax(fabs(a11), fmax(fabs(a21), fabs(a22)));
-        bool ok = false;
-        double d0 = 0, d1 = 0, d3 = 0;
-        if (!(maxpiv < small)) {
-          double detscale = 1 / maxpiv;
-          double det0 = (a11 * detscale) * a22, det1 = (a21 * detscale) * a21;
-          double detpiv = det0 - det1;
-          if (!(fabs(detpiv) < fmax(small, fmax(fabs(det0 / 2), fabs(det1 / 2))))) {
-            d0 = (a22 * detscale) / detpiv;
-            d1 = (-a21 * detscale) / detpiv;
-            d3 = (a11 * detscale) / detpiv;
-            if (fmax(maxp, maxt) < small) ok = true;
-            else {
-              double x1 = fabs(d0) * maxt + fabs(d1) * maxp;
-              double x2 = fabs(d1) * maxt + fabs(d3) * maxp;
-              ok = (u * fmax(x1, x2) < 1.0);
-            }
-          }
-        }
-        if (ok) {
-          tpp_sym_swap(fd, t, nel);
-          tpp_sym_swap(fd, p, nel + 1);
-          tpp_apply(fd, nel, 2, d0, d1, d3);
-          nel += 2;
-          done = true;
-          break;
-        }
-      }
-      maxp = fmax(maxp, fabs((double)L[(int64_t)t * ld + p]));
-      if (fabs((double)L[(int64_t)p * ld + p]) >= u * maxp) {
-        tpp_sym_swap(fd, p, nel);
-        double d11 = 1.0 / (double)L[(int64_t)nel * ld + nel];
-        tpp_apply(fd, nel, 1, d11, 0, 0);
-        nel += 1;
-        done = true;
-        break;
-      }
-    }
-    if (!done) {
-      p = nel;
-      double maxp = tpp_rc_max_excl(fd, p, nel, -1, red);
-      if (fabs((double)L[(int64_t)p * ld + p]) >= u * maxp) {
-        double d11 = 1.0 / (double)L[(int64_t)nel * ld + nel];
-        tpp_apply(fd, nel, 1, d11, 0, 0);
-        nel += 1;
-      } else {
-        break;
-      }
-    }
-  }
-  (void)m;
-  return nel;
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontState* sts,
-                                                     const int* fronts, bool action, double u,
-                                                     double small, bool all_fronts) {
-  const int f = fronts[blockIdx.x];
-  FrontState* st = &sts[f];
-  FrontDesc<T> fd = fds[f];
-  if (st->status != kDevOk) return;
-  if (st->nelim >= fd.n) return;
-  if (!(all_fronts || fd.m == fd.n)) return;
-  __shared__ double red[kTppThreads / 32];
-  __shared__ int s_t;
-  const int nel = tpp_body(fd, st->nelim, action, u, small, red, &s_t);
-  if (threadIdx.x == 0) {
-    if (nel < 0) st->status = kDevSingular;
-    else { st->nelim = nel; st->p = nel; }
-  }
-}
 
 // ------------------------------------------------------------------------
 // k_tpp_small: the fronts of small leaf subtrees, factored with TPP from
@@ -1473,15 +1297,16 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontSta
 // subtree below small_subtree_threshold flops (SymbolicSubtree.hxx:56-82;
 // SmallLeafNumericSubtree.hxx:345-375 calls ldlt_tpp_factor on the whole
 // front).  One CTA per front, the front (m x n), two workspace columns and
-// its perm/opos held in shared memory.  Each pivot: warp 0 alone runs the
-// pivot search of ldlt_tpp_factor (ldlt_tpp.cxx:166-270; every reduction a
-// warp shuffle over shared memory), performs the symmetric swaps, writes
+// its perm/opos held in shared memory.  The TPP itself (tpp_fast, which
+// k_tpp also runs on the failed columns of APP fronts): each pivot, warp 0
+// alone runs the pivot search of ldlt_tpp_factor (ldlt_tpp.cxx:166-270;
+// every reduction a warp shuffle), performs the symmetric swaps, writes
 // D^{-1} and keeps unscaled copies of the pivot column(s); after one barrier
 // every warp scales the pivot column(s) and updates the trailing
 // fully-summed columns (rows of the front's contribution part included);
 // one more barrier ends the pivot.  A front too large for the launch's
-// shared memory (delays can grow one) is factored in global memory by the
-// block-wide TPP of k_tpp.  step = 0 records that no APP pass ran.
+// shared memory (delays can grow one) is factored the same way in global
+// memory.  step = 0 records that no APP pass ran.
 // ------------------------------------------------------------------------
 namespace tpps {
 enum Kind : int { kStop = 0, kZeroNel, kZeroSwap, kTwo, kOne, kSingular };
@@ -1599,76 +1424,48 @@ __device__ Decision decide(const T* S, int ld, int nel, int m, int n, bool actio
 }
 }  // namespace tpps
 
+// The TPP loop of ldlt_tpp_factor on columns [nel, n), rows [nel, m), of
+// the front held at S (leading dimension ld; shared or global memory), with
+// two workspace columns W0, W1 (>= m entries) and the front's perm, opos
+// and D^{-1}.  Swaps cover whole lines (the rows of the eliminated columns
+// to the left included, as swap_cols with aleft, ldlt_tpp.cxx:44-72).
+// Returns the number of columns eliminated in total, or -1 for a singular
+// front with action == false.  Called by all threads of the CTA.
 template <typename T>
-__global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, FrontState* sts,
-                                                           const int* fronts, bool action,
-                                                           double u, double small,
-                                                           int smem_bytes) {
+__device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* perm, int* opos,
+                        double* D, bool action, double u, double small) {
   using namespace tpps;
-  extern __shared__ __align__(16) unsigned char tpp_smem[];
-  const int f = fronts[blockIdx.x];
-  FrontState* st = &sts[f];
-  FrontDesc<T> fd = fds[f];
-  if (st->status != kDevOk) return;
-  __shared__ double red[kTppThreads / 32];
-  __shared__ int s_t;
   __shared__ Decision s_dec;
-  const int m = fd.m, n = fd.n;
-  const int ldS = (m + 1) & ~1;
-  const size_t need = (size_t)ldS * (n + 2) * sizeof(T) + 2 * (size_t)n * sizeof(int);
-  if (n == 0) {
-    if (threadIdx.x == 0) { st->nelim = 0; st->p = 0; st->step = 0; }
-    return;
-  }
-  if (need > (size_t)smem_bytes) {
-    const int nel = tpp_body(fd, 0, action, u, small, red, &s_t);
-    if (threadIdx.x == 0) {
-      if (nel < 0) st->status = kDevSingular;
-      else { st->nelim = nel; st->p = nel; st->step = 0; }
-    }
-    return;
-  }
-  T* S = reinterpret_cast<T*>(tpp_smem);
-  T* W0 = S + (size_t)ldS * n;
-  T* W1 = W0 + ldS;
-  int* sperm = reinterpret_cast<int*>(W1 + ldS);
-  int* sopos = sperm + n;
-  for (int c = 0; c < n; ++c)
-    for (int r = threadIdx.x; r < m; r += blockDim.x) S[(size_t)c * ldS + r] = fd.L[(int64_t)c * fd.ld + r];
-  for (int i = threadIdx.x; i < n; i += blockDim.x) { sperm[i] = fd.perm[i]; sopos[i] = fd.opos[i]; }
-  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  int nel = 0;
-  bool singular = false;
   while (nel < n) {
     if (warp == 0) {
-      Decision d = decide(S, ldS, nel, m, n, action, u, small);
-      if (d.kind == kZeroSwap) sym_swap(S, ldS, m, d.p, nel, sperm, sopos);
+      Decision d = decide(S, ld, nel, m, n, action, u, small);
+      if (d.kind == kZeroSwap) sym_swap(S, ld, m, d.p, nel, perm, opos);
       if (d.kind == kZeroNel || d.kind == kZeroSwap) {
-        for (int r = nel + lane; r < m; r += 32) S[(size_t)nel * ldS + r] = T(0);
-        if (lane == 0) { fd.D[2 * nel] = 0.0; fd.D[2 * nel + 1] = 0.0; }
+        for (int r = nel + lane; r < m; r += 32) S[(size_t)nel * ld + r] = T(0);
+        if (lane == 0) { D[2 * nel] = 0.0; D[2 * nel + 1] = 0.0; }
       } else if (d.kind == kTwo) {
-        sym_swap(S, ldS, m, d.t, nel, sperm, sopos);
-        sym_swap(S, ldS, m, d.p, nel + 1, sperm, sopos);
+        sym_swap(S, ld, m, d.t, nel, perm, opos);
+        sym_swap(S, ld, m, d.p, nel + 1, perm, opos);
         for (int r = nel + 2 + lane; r < m; r += 32) {
-          W0[r] = S[(size_t)nel * ldS + r];
-          W1[r] = S[(size_t)(nel + 1) * ldS + r];
+          W0[r] = S[(size_t)nel * ld + r];
+          W1[r] = S[(size_t)(nel + 1) * ld + r];
         }
         if (lane == 0) {
-          S[(size_t)nel * ldS + nel] = T(1);
-          S[(size_t)nel * ldS + nel + 1] = T(0);
-          S[(size_t)(nel + 1) * ldS + nel + 1] = T(1);
-          fd.D[2 * nel] = d.d0; fd.D[2 * nel + 1] = d.d1;
-          fd.D[2 * nel + 2] = dinf(); fd.D[2 * nel + 3] = d.d3;
+          S[(size_t)nel * ld + nel] = T(1);
+          S[(size_t)nel * ld + nel + 1] = T(0);
+          S[(size_t)(nel + 1) * ld + nel + 1] = T(1);
+          D[2 * nel] = d.d0; D[2 * nel + 1] = d.d1;
+          D[2 * nel + 2] = dinf(); D[2 * nel + 3] = d.d3;
         }
       } else if (d.kind == kOne) {
-        sym_swap(S, ldS, m, d.p, nel, sperm, sopos);
-        const double d11 = 1.0 / (double)S[(size_t)nel * ldS + nel];
+        sym_swap(S, ld, m, d.p, nel, perm, opos);
+        const double d11 = 1.0 / (double)S[(size_t)nel * ld + nel];
         d.d0 = d11;
-        for (int r = nel + 1 + lane; r < m; r += 32) W0[r] = S[(size_t)nel * ldS + r];
+        for (int r = nel + 1 + lane; r < m; r += 32) W0[r] = S[(size_t)nel * ld + r];
         if (lane == 0) {
-          S[(size_t)nel * ldS + nel] = T(1);
-          fd.D[2 * nel] = d11; fd.D[2 * nel + 1] = 0.0;
+          S[(size_t)nel * ld + nel] = T(1);
+          D[2 * nel] = d11; D[2 * nel + 1] = 0.0;
         }
       }
       __syncwarp();
@@ -1677,7 +1474,7 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, Fr
     __syncthreads();
     const Decision d = s_dec;
     if (d.kind == kStop) break;
-    if (d.kind == kSingular) { singular = true; break; }
+    if (d.kind == kSingular) return -1;
     if (d.kind == kZeroNel || d.kind == kZeroSwap) {
       nel += 1;
       __syncthreads();  // every warp has read s_dec before warp 0 rewrites it
@@ -1690,10 +1487,10 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, Fr
     if (ps == 1) {
       const double d11 = d.d0;
       for (int r = c0 + threadIdx.x; r < m; r += blockDim.x)
-        S[(size_t)nel * ldS + r] = (T)((double)W0[r] * d11);
+        S[(size_t)nel * ld + r] = (T)((double)W0[r] * d11);
       for (int c = c0 + warp; c < n; c += nw) {
         const T wc = W0[c];
-        T* col = S + (size_t)c * ldS;
+        T* col = S + (size_t)c * ld;
         for (int r = c + lane; r < m; r += 32) {
           const T l = (T)((double)W0[r] * d11);
           col[r] -= l * wc;
@@ -1702,12 +1499,12 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, Fr
     } else {
       for (int r = c0 + threadIdx.x; r < m; r += blockDim.x) {
         const double a1 = (double)W0[r], a2 = (double)W1[r];
-        S[(size_t)nel * ldS + r] = (T)(d.d0 * a1 + d.d1 * a2);
-        S[(size_t)(nel + 1) * ldS + r] = (T)(d.d1 * a1 + d.d3 * a2);
+        S[(size_t)nel * ld + r] = (T)(d.d0 * a1 + d.d1 * a2);
+        S[(size_t)(nel + 1) * ld + r] = (T)(d.d1 * a1 + d.d3 * a2);
       }
       for (int c = c0 + warp; c < n; c += nw) {
         const T w0 = W0[c], w1 = W1[c];
-        T* col = S + (size_t)c * ldS;
+        T* col = S + (size_t)c * ld;
         for (int r = c + lane; r < m; r += 32) {
           const double a1 = (double)W0[r], a2 = (double)W1[r];
           const T l1 = (T)(d.d0 * a1 + d.d1 * a2), l2 = (T)(d.d1 * a1 + d.d3 * a2);
@@ -1718,13 +1515,66 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, Fr
     __syncthreads();
     nel += ps;
   }
-  if (!singular) {
+  return nel;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontState* sts,
+                                                     const int* fronts, bool action, double u,
+                                                     double small, bool all_fronts) {
+  const int f = fronts[blockIdx.x];
+  FrontState* st = &sts[f];
+  FrontDesc<T> fd = fds[f];
+  if (st->status != kDevOk) return;
+  if (st->nelim >= fd.n) return;
+  if (!(all_fronts || fd.m == fd.n)) return;
+  const int nel = tpp_fast(fd.L, fd.ld, fd.m, fd.n, st->nelim, fd.W, fd.W + fd.ld, fd.perm,
+                           fd.opos, fd.D, action, u, small);
+  if (threadIdx.x == 0) {
+    if (nel < 0) st->status = kDevSingular;
+    else { st->nelim = nel; st->p = nel; }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, FrontState* sts,
+                                                           const int* fronts, bool action,
+                                                           double u, double small,
+                                                           int smem_bytes) {
+  extern __shared__ __align__(16) unsigned char tpp_smem[];
+  const int f = fronts[blockIdx.x];
+  FrontState* st = &sts[f];
+  FrontDesc<T> fd = fds[f];
+  if (st->status != kDevOk) return;
+  const int m = fd.m, n = fd.n;
+  const int ldS = (m + 1) & ~1;
+  const size_t need = (size_t)ldS * (n + 2) * sizeof(T) + 2 * (size_t)n * sizeof(int);
+  int nel;
+  if (n == 0) {
+    nel = 0;
+  } else if (need > (size_t)smem_bytes) {
+    nel = tpp_fast(fd.L, fd.ld, m, n, 0, fd.W, fd.W + fd.ld, fd.perm, fd.opos, fd.D, action, u,
+                   small);
+  } else {
+    T* S = reinterpret_cast<T*>(tpp_smem);
+    T* W0 = S + (size_t)ldS * n;
+    T* W1 = W0 + ldS;
+    int* sperm = reinterpret_cast<int*>(W1 + ldS);
+    int* sopos = sperm + n;
     for (int c = 0; c < n; ++c)
-      for (int r = threadIdx.x; r < m; r += blockDim.x) fd.L[(int64_t)c * fd.ld + r] = S[(size_t)c * ldS + r];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) { fd.perm[i] = sperm[i]; fd.opos[i] = sopos[i]; }
+      for (int r = threadIdx.x; r < m; r += blockDim.x) S[(size_t)c * ldS + r] = fd.L[(int64_t)c * fd.ld + r];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) { sperm[i] = fd.perm[i]; sopos[i] = fd.opos[i]; }
+    __syncthreads();
+    nel = tpp_fast(S, ldS, m, n, 0, W0, W1, sperm, sopos, fd.D, action, u, small);
+    __syncthreads();
+    if (nel >= 0) {
+      for (int c = 0; c < n; ++c)
+        for (int r = threadIdx.x; r < m; r += blockDim.x) fd.L[(int64_t)c * fd.ld + r] = S[(size_t)c * ldS + r];
+      for (int i = threadIdx.x; i < n; i += blockDim.x) { fd.perm[i] = sperm[i]; fd.opos[i] = sopos[i]; }
+    }
   }
   if (threadIdx.x == 0) {
-    if (singular) st->status = kDevSingular;
+    if (nel < 0) st->status = kDevSingular;
     else { st->nelim = nel; st->p = nel; st->step = 0; }
   }
 }
@@ -1878,7 +1728,8 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
   launch_pdl(k_app_panel<T, tp>, dim3(ptiles + nfix, nf), 256, 0, s, fd, st, fronts, ptiles);
   note_launches(1);
   pmark(tm, kPhSwap, s);
-  launch_pdl(k_app_swap<T>, nf, 256, 0, s, fd, st, fronts);
+  const int sx = 1 + std::max(1, std::min(cdiv(max_rows + step * kBlk, 256), 64));
+  launch_pdl(k_app_swap<T>, dim3(sx, nf), 256, 0, s, fd, st, fronts);
   note_launches(1);
 }
 

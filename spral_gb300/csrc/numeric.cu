@@ -788,6 +788,11 @@ struct Numeric : NumericBase {
   TcBuffers tcbuf;
   DevBuf<char> tc_scratch;
   int panel_nb = 256;       // APP panel width (FP32 fronts with tensor cores)
+  // fewest fully-summed columns of a front factored in panels: narrower
+  // fronts keep the block steps' SIMT updates, which are exact in FP32
+  // (the 3xTF32 products carry about 22 bits and can cost the FP64
+  // refinement a step)
+  int panel_min_n = 1024;
   DevBuf<int> panel_list;   // fronts ending a panel (eager mode)
   int* d_tc_status = nullptr;
   int* d_ncount = nullptr;  // per-node inertia counts (neg, two, zero)
@@ -813,7 +818,7 @@ struct Numeric : NumericBase {
   int panel_cols(int f) const {
     if (!std::is_same<T, float>::value || !use_tc || panel_nb <= 0) return 0;
     if (tpp_front(f) || S->copts.pivot_method == 3) return 0;
-    return n_[f] > panel_nb ? panel_nb : 0;
+    return n_[f] >= std::max(panel_min_n, panel_nb + 1) ? panel_nb : 0;
   }
   // fronts of [f0, f1) whose current panel ends with block step st
   void panel_boundary(int f0, int f1, int st, std::vector<int>& out) const {
@@ -1299,6 +1304,8 @@ struct Numeric : NumericBase {
       if (mk) tc_min_k = std::max(0, atoi(mk));
       const char* pn = getenv("SPRAL_GB300_PANEL");
       if (pn) panel_nb = std::max(0, atoi(pn)) / kBlk * kBlk;
+      const char* pm = getenv("SPRAL_GB300_PANEL_MIN_N");
+      if (pm) panel_min_n = std::max(0, atoi(pm));
     }
     contrib.ensure(std::max<int64_t>(S->contrib_total, 1));
     // factor storage estimate (no delays) + 10%
@@ -1456,7 +1463,9 @@ struct Numeric : NumericBase {
       pmark(tm(), kPhInitPerm, s);
       launch_init_perm<T>(d_fd, fr, nf, S->d_sptr, max_n, s);
       pmark(tm(), kPhDelays, s);
-      launch_assemble_delays<T>(d_fd, d_st, d_dwork, (int)dwork.size(), S->d_rdir,
+      int max_nd = 0;
+      for (const int4& w : dwork) max_nd = std::max(max_nd, n_[w.y] - nelim_[w.y]);
+      launch_assemble_delays<T>(d_fd, d_st, d_dwork, (int)dwork.size(), max_nd, S->d_rdir,
                                 S->d_rdir_ptr, s);
       pmark(tm(), kPhAssemble, s);
       launch_assemble_contrib<T>(d_fd, S->d_cols + S->cols_start[l],

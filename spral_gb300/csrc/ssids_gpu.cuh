@@ -142,9 +142,11 @@ void launch_load_a(const FrontDesc<T>* fd, const int* fronts, int nf, const int6
 template <typename T>
 void launch_init_perm(const FrontDesc<T>* fd, const int* fronts, int nf, const int* sptr,
                       int max_n, cudaStream_t s);
+// max_nd bounds the delayed columns of any child in the work list
 template <typename T>
 void launch_assemble_delays(const FrontDesc<T>* fd, const FrontState* st, const int4* work,
-                            int nwork, const int* rdir, const int64_t* rdir_ptr, cudaStream_t s);
+                            int nwork, int max_nd, const int* rdir, const int64_t* rdir_ptr,
+                            cudaStream_t s);
 template <typename T>
 void launch_assemble_contrib(const FrontDesc<T>* fd, const int4* cols, int ncols,
                              const int2* pairs, const int* rdir, const int64_t* rdir_ptr,

@@ -23,6 +23,7 @@ def _mixed():
 
 @pytest.mark.parametrize("kind", ["lap3d", "kkt"])
 def test_gpu_panels_match_unpaneled_and_oracle(kind, monkeypatch):
+    monkeypatch.setenv("SPRAL_GB300_PANEL_MIN_N", "257")
     if kind == "lap3d":
         k = 24
         p, r, v = M.laplacian_3d(k, shift=-0.3)
@@ -51,7 +52,8 @@ def test_gpu_panels_match_unpaneled_and_oracle(kind, monkeypatch):
     f0.free()
 
 
-def test_gpu_panels_captured_refactorisation_matches_eager():
+def test_gpu_panels_captured_refactorisation_matches_eager(monkeypatch):
+    monkeypatch.setenv("SPRAL_GB300_PANEL_MIN_N", "257")
     k = 24
     p, r, v = M.laplacian_3d(k, shift=-0.3)
     ak = ssids.analyse(p, r, M.nd_order_grid(k, k, k))
