@@ -94,17 +94,30 @@ typedef void (*dgemm_fn)(const char*, const char*, const int*, const int*, const
                          const double*, const double*, const int*, const double*,
                          const int*, const double*, double*, const int*);
 static dgemm_fn g_dgemm = NULL;
+typedef void (*dtrsm_fn)(const char*, const char*, const char*, const char*, const int*,
+                         const int*, const double*, const double*, const int*, double*,
+                         const int*);
+static dtrsm_fn g_dtrsm = NULL;
 
 /* Load a Fortran-ABI dgemm from the shared library at `path` under symbol
  * `sym` (e.g. scipy's bundled OpenBLAS "scipy_dgemm_").  Returns 0 on
  * success.  Without it, the naive loops below are used. */
 int oracle_set_blas(const char* path, const char* sym) {
-  if (!path) { g_dgemm = NULL; return 0; }
+  if (!path) { g_dgemm = NULL; g_dtrsm = NULL; return 0; }
   void* h = dlopen(path, RTLD_NOW | RTLD_GLOBAL);
   if (!h) return -1;
   void* f = dlsym(h, sym);
   if (!f) return -2;
   g_dgemm = (dgemm_fn)f;
+  /* dtrsm under the same prefix (the solves, as ldlt_app_solve_* use it) */
+  char tsym[128];
+  size_t len = strlen(sym);
+  g_dtrsm = NULL;
+  if (len >= 6 && len < sizeof(tsym) && strcmp(sym + len - 6, "dgemm_") == 0) {
+    memcpy(tsym, sym, len + 1);
+    memcpy(tsym + len - 6, "dtrsm_", 6);
+    g_dtrsm = (dtrsm_fn)dlsym(h, tsym);
+  }
   return 0;
 }
 
@@ -722,62 +735,93 @@ void oracle_node_data(void* h, int node, double* L, double* D, int* perm) {
 
 /* Solve in pivot order (x already permuted by invp), nrhs columns, ldx.
  * job: 0 full, 1 fwd, 2 diag, 3 bwd (no D), 4 diag_bwd
- * (NumericSubtree.hxx:284-400; ldlt_app.cxx:2538-2589). */
+ * (NumericSubtree.hxx:284-400; ldlt_app.cxx:2538-2589: per node, all
+ * right-hand sides at once; with BLAS loaded, dtrsm for the triangle and
+ * dgemm for the rectangle, as ldlt_app_solve_fwd/bwd do). */
 int oracle_solve(void* h, int job, int nrhs, double* x, int ldx) {
   ofactors* F = (ofactors*)h;
   int n = F->n;
-  double* xl = (double*)malloc(sizeof(double) * (size_t)n);
-  int* map = (int*)malloc(sizeof(int) * (size_t)n);
+  int maxm = 1;
+  for (int ni = 0; ni < F->nnodes; ++ni) if (F->nodes[ni].m > maxm) maxm = F->nodes[ni].m;
+  double* xl = (double*)malloc(sizeof(double) * (size_t)maxm * (nrhs > 0 ? nrhs : 1));
+  int* map = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
   bool fwd = (job == 0 || job == 1);
   bool diag = (job == 0 || job == 2 || job == 4);
   bool bwd = (job == 0 || job == 3 || job == 4);
-  for (int r = 0; r < nrhs; ++r) {
-    double* xr = &x[(int64_t)r * ldx];
-    if (fwd) {
-      for (int ni = 0; ni < F->nnodes; ++ni) {
-        onode* nd = &F->nodes[ni];
-        int m = nd->m, nn = nd->n, ne = nd->nelim;
-        for (int i = 0; i < nn; ++i) map[i] = nd->perm[i];
-        for (int i = nd->ncol; i < nd->nrow; ++i) map[i + nd->ndelay_in] = nd->rlist[i];
-        for (int i = 0; i < m; ++i) xl[i] = xr[map[i] - 1];
-        const double* L = nd->l;
-        for (int j = 0; j < ne; ++j) {
-          double v = xl[j];
-          for (int i = j + 1; i < m; ++i) xl[i] -= L[(int64_t)j * m + i] * v;
+  const double one = 1.0, mone = -1.0;
+  if (fwd) {
+    for (int ni = 0; ni < F->nnodes; ++ni) {
+      onode* nd = &F->nodes[ni];
+      int m = nd->m, nn = nd->n, ne = nd->nelim;
+      for (int i = 0; i < nn; ++i) map[i] = nd->perm[i];
+      for (int i = nd->ncol; i < nd->nrow; ++i) map[i + nd->ndelay_in] = nd->rlist[i];
+      for (int r = 0; r < nrhs; ++r)
+        for (int i = 0; i < m; ++i) xl[(size_t)r * m + i] = x[(size_t)r * ldx + map[i] - 1];
+      const double* L = nd->l;
+      if (ne > 0) {
+        if (g_dtrsm && g_dgemm) {
+          g_dtrsm("L", "L", "N", "U", &ne, &nrhs, &one, L, &m, xl, &m);
+          int rows = m - ne;
+          if (rows > 0)
+            g_dgemm("N", "N", &rows, &nrhs, &ne, &mone, L + ne, &m, xl, &m, &one, xl + ne, &m);
+        } else {
+          for (int r = 0; r < nrhs; ++r) {
+            double* xr = xl + (size_t)r * m;
+            for (int j = 0; j < ne; ++j) {
+              double v = xr[j];
+              for (int i = j + 1; i < m; ++i) xr[i] -= L[(int64_t)j * m + i] * v;
+            }
+          }
         }
-        for (int i = 0; i < m; ++i) xr[map[i] - 1] = xl[i];
       }
+      for (int r = 0; r < nrhs; ++r)
+        for (int i = 0; i < m; ++i) x[(size_t)r * ldx + map[i] - 1] = xl[(size_t)r * m + i];
     }
-    if (diag || bwd) {
-      for (int ni = F->nnodes - 1; ni >= 0; --ni) {
-        onode* nd = &F->nodes[ni];
-        int m = nd->m, nn = nd->n, ne = nd->nelim;
-        for (int i = 0; i < nn; ++i) map[i] = nd->perm[i];
-        for (int i = nd->ncol; i < nd->nrow; ++i) map[i + nd->ndelay_in] = nd->rlist[i];
-        int blkm = bwd ? m : ne;
-        for (int i = 0; i < blkm; ++i) xl[i] = xr[map[i] - 1];
-        const double* L = nd->l;
-        const double* d = &L[(int64_t)nn * m];
-        if (diag) {
+  }
+  if (diag || bwd) {
+    for (int ni = F->nnodes - 1; ni >= 0; --ni) {
+      onode* nd = &F->nodes[ni];
+      int m = nd->m, nn = nd->n, ne = nd->nelim;
+      for (int i = 0; i < nn; ++i) map[i] = nd->perm[i];
+      for (int i = nd->ncol; i < nd->nrow; ++i) map[i + nd->ndelay_in] = nd->rlist[i];
+      int blkm = bwd ? m : ne;
+      for (int r = 0; r < nrhs; ++r)
+        for (int i = 0; i < blkm; ++i) xl[(size_t)r * m + i] = x[(size_t)r * ldx + map[i] - 1];
+      const double* L = nd->l;
+      const double* d = &L[(int64_t)nn * m];
+      if (diag) {
+        for (int r = 0; r < nrhs; ++r) {
+          double* xr = xl + (size_t)r * m;
           for (int i = 0; i < ne;) {
-            if (i + 1 == ne || isfinite(d[2 * i + 2])) { xl[i] *= d[2 * i]; i++; }
+            if (i + 1 == ne || isfinite(d[2 * i + 2])) { xr[i] *= d[2 * i]; i++; }
             else {
-              double x1 = xl[i], x2 = xl[i + 1];
-              xl[i] = d[2 * i] * x1 + d[2 * i + 1] * x2;
-              xl[i + 1] = d[2 * i + 1] * x1 + d[2 * i + 3] * x2;
+              double x1 = xr[i], x2 = xr[i + 1];
+              xr[i] = d[2 * i] * x1 + d[2 * i + 1] * x2;
+              xr[i + 1] = d[2 * i + 1] * x1 + d[2 * i + 3] * x2;
               i += 2;
             }
           }
         }
-        if (bwd) {
-          for (int j = ne - 1; j >= 0; --j) {
-            double s = xl[j];
-            for (int i = j + 1; i < m; ++i) s -= L[(int64_t)j * m + i] * xl[i];
-            xl[j] = s;
+      }
+      if (bwd && ne > 0) {
+        if (g_dtrsm && g_dgemm) {
+          int rows = m - ne;
+          if (rows > 0)
+            g_dgemm("T", "N", &ne, &nrhs, &rows, &mone, L + ne, &m, xl + ne, &m, &one, xl, &m);
+          g_dtrsm("L", "L", "T", "U", &ne, &nrhs, &one, L, &m, xl, &m);
+        } else {
+          for (int r = 0; r < nrhs; ++r) {
+            double* xr = xl + (size_t)r * m;
+            for (int j = ne - 1; j >= 0; --j) {
+              double sacc = xr[j];
+              for (int i = j + 1; i < m; ++i) sacc -= L[(int64_t)j * m + i] * xr[i];
+              xr[j] = sacc;
+            }
           }
         }
-        for (int i = 0; i < ne; ++i) xr[map[i] - 1] = xl[i];
       }
+      for (int r = 0; r < nrhs; ++r)
+        for (int i = 0; i < ne; ++i) x[(size_t)r * ldx + map[i] - 1] = xl[(size_t)r * m + i];
     }
   }
   free(xl); free(map);
