@@ -772,6 +772,22 @@ struct Numeric : NumericBase {
   }
   DevBuf<T> xloc;
   DevBuf<double> xbuf, rbuf, dbuf, bbuf, nbuf;
+  // wavefront solves: per level, the forward and backward item lists (one
+  // device array), the completion flags of every pivot block, and the ints
+  // [status, forward counters (nlev), backward counters (nlev)]
+  bool use_wave = true;
+  DevBuf<int2> wave_items;
+  DevBuf<int> wave_flags, wave_ints;
+  std::vector<int> wave_fwd_off, wave_bwd_off;  // per level, into wave_items (+1 end)
+  size_t wave_nflags = 0;
+  WaveLevel wave_level(bool fwd, int l) const {
+    const std::vector<int>& off = fwd ? wave_fwd_off : wave_bwd_off;
+    WaveLevel w;
+    w.items = wave_items.p + off[l];
+    w.nitems = off[l + 1] - off[l];
+    w.counter = wave_ints.p + 1 + (fwd ? 0 : S->nlev) + l;
+    return w;
+  }
   // tensor-core contribution GEMM (FP32 factors only)
   bool use_tc = false;
   int tc_chunk = kTcChunk;
@@ -1291,6 +1307,8 @@ struct Numeric : NumericBase {
     {
       const char* gr = getenv("SPRAL_GB300_GRAPHS");
       use_graphs = !(gr && gr[0] == '0');
+      const char* wv = getenv("SPRAL_GB300_SOLVE_WAVE");
+      use_wave = !(wv && wv[0] == '0');
     }
     if (std::is_same<T, float>::value) {
       const char* env = getenv("SPRAL_GB300_TENSOR_CORES");
@@ -1577,9 +1595,51 @@ struct Numeric : NumericBase {
     std::vector<size_t> xoff(nn);
     for (int f = 0; f < nn; ++f) { xoff[f] = xl; xl += (size_t)m_[f] * kSolveRhs; }
     xloc.ensure(xl + 1);
+    std::vector<size_t> flag_off(nn + 1, 0);
+    for (int f = 0; f < nn; ++f) flag_off[f + 1] = flag_off[f] + (nelim_[f] + kSolveBlk - 1) / kSolveBlk;
+    wave_nflags = flag_off[nn];
+    wave_flags.ensure(std::max<size_t>(wave_nflags, 1));
+    wave_ints.ensure(1 + 2 * (size_t)S->nlev);
+    {
+      // forward: pivot blocks by block index across the level's nodes, then
+      // the contribution row blocks; backward: pivot blocks from the last
+      std::vector<int2> items;
+      wave_fwd_off.assign(S->nlev + 1, 0);
+      wave_bwd_off.assign(S->nlev + 1, 0);
+      for (int l = 0; l < S->nlev; ++l) {
+        wave_fwd_off[l] = (int)items.size();
+        const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1];
+        int mb = 0;
+        for (int f = f0; f < f1; ++f) mb = std::max(mb, (nelim_[f] + kSolveBlk - 1) / kSolveBlk);
+        for (int b = 0; b < mb; ++b)
+          for (int f = f0; f < f1; ++f)
+            if (b * kSolveBlk < nelim_[f]) items.push_back(make_int2(f, b));
+        for (int f = f0; f < f1; ++f)
+          for (int r = nelim_[f], k = 0; r < m_[f]; r += kSolveBlk, ++k)
+            items.push_back(make_int2(f, kWaveContrib + k));
+      }
+      wave_fwd_off[S->nlev] = (int)items.size();
+      for (int l = 0; l < S->nlev; ++l) {
+        wave_bwd_off[l] = (int)items.size();
+        const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1];
+        int mb = 0;
+        for (int f = f0; f < f1; ++f) mb = std::max(mb, (nelim_[f] + kSolveBlk - 1) / kSolveBlk);
+        for (int b = mb - 1; b >= 0; --b)
+          for (int f = f0; f < f1; ++f)
+            if (b * kSolveBlk < nelim_[f]) items.push_back(make_int2(f, b));
+      }
+      wave_bwd_off[S->nlev] = (int)items.size();
+      wave_items.ensure(std::max<size_t>(items.size(), 1));
+      if (!items.empty())
+        CK(cudaMemcpyAsync(wave_items.p, items.data(), items.size() * sizeof(int2),
+                           cudaMemcpyHostToDevice, stream));
+      CK(cudaMemsetAsync(wave_ints.p, 0, sizeof(int), stream));  // status
+    }
     for (int f = 0; f < nn; ++f) {
       const int node = S->node_of[f];
       SolveNode<T>& q = sn[f];
+      q.flag = wave_flags.p + flag_off[f];
+      q.pad_ = 0;
       q.L = hfd[f].L; q.D = hfd[f].D; q.perm = hfd[f].perm; q.opos = hfd[f].opos;
       q.rows = S->d_rlist + S->rptr[node];
       q.rdir = S->d_rdir + S->rdir_ptr_h[node];
@@ -1611,6 +1671,10 @@ struct Numeric : NumericBase {
     for (int l = 0; l < S->nlev; ++l) { mix((uint64_t)lvl_max_m[l]); mix((uint64_t)lvl_max_nelim[l]); }
     mix((uint64_t)(uintptr_t)d_sn); mix((uint64_t)(uintptr_t)d_children);
     mix((uint64_t)(uintptr_t)xloc.p);
+    mix((uint64_t)(uintptr_t)wave_items.p); mix((uint64_t)(uintptr_t)wave_flags.p);
+    mix((uint64_t)(uintptr_t)wave_ints.p);
+    for (int v : wave_fwd_off) mix((uint64_t)v);
+    for (int v : wave_bwd_off) mix((uint64_t)v);
     if (h != solve_sig) drop_graphs();
     solve_sig = h;
     solve_ready = true;
@@ -1624,21 +1688,41 @@ struct Numeric : NumericBase {
     const bool diag = (job == 0 || job == 2 || job == 4);
     const bool bwd = (job == 0 || job == 3 || job == 4 || job == 6);
     const int diag_mode = diag ? 1 : (job == 6 ? 2 : 0);
+    int* wstatus = wave_ints.p;
     if (fwd) {
+      if (use_wave) {
+        CK(cudaMemsetAsync(wave_flags.p, 0, std::max<size_t>(wave_nflags, 1) * sizeof(int), s));
+        CK(cudaMemsetAsync(wave_ints.p + 1, 0, S->nlev * sizeof(int), s));
+      }
       for (int l = 0; l < S->nlev; ++l) {
         const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
         const int* fr = S->d_fronts + f0;
         pmark(tm(), kPhFwdGather, s);
         launch_fwd_gather<T>(d_sn, fr, nf, d_children, S->d_pairs, xp, ldx, q, lvl_max_m[l], s);
-        launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, xp, ldx, job == 5, s,
-                            tm());
+        if (use_wave) {
+          pmark(tm(), kPhFwdUpdate, s);
+          launch_fwd_wave<T>(d_sn, wave_level(true, l), q, xp, ldx, job == 5, wstatus, s);
+        } else {
+          launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, xp, ldx, job == 5,
+                              s, tm());
+        }
       }
     }
     if (diag || bwd) {
+      if (use_wave && bwd) {
+        CK(cudaMemsetAsync(wave_flags.p, 0, std::max<size_t>(wave_nflags, 1) * sizeof(int), s));
+        CK(cudaMemsetAsync(wave_ints.p + 1 + S->nlev, 0, S->nlev * sizeof(int), s));
+      }
       for (int l = S->nlev - 1; l >= 0; --l) {
         const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
-        launch_bwd<T>(d_sn, S->d_fronts + f0, nf, xp, ldx, q, lvl_max_m[l], lvl_max_nelim[l],
-                      diag_mode, bwd, s, tm());
+        if (use_wave && bwd) {
+          pmark(tm(), kPhBwdUpdate, s);
+          launch_bwd_wave<T>(d_sn, S->d_fronts + f0, nf, wave_level(false, l), xp, ldx, q,
+                             lvl_max_m[l], diag_mode, wstatus, s);
+        } else {
+          launch_bwd<T>(d_sn, S->d_fronts + f0, nf, xp, ldx, q, lvl_max_m[l], lvl_max_nelim[l],
+                        diag_mode, bwd, s, tm());
+        }
       }
     }
   }
@@ -1694,6 +1778,15 @@ struct Numeric : NumericBase {
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
     if (profile) ptimer.flush();
+    if (use_wave) {
+      // a wavefront wait that gave up (never expected) fails the solve
+      int wst = 0;
+      CK(cudaMemcpy(&wst, wave_ints.p, sizeof(int), cudaMemcpyDeviceToHost));
+      if (wst != 0) {
+        CK(cudaMemset(wave_ints.p, 0, sizeof(int)));
+        throw CudaFail{cudaErrorLaunchTimeout, __LINE__};
+      }
+    }
     return 0;
   }
 

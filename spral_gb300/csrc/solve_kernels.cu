@@ -527,6 +527,263 @@ __global__ void __launch_bounds__(kSolveThreads)
   }
 }
 
+// ---- wavefront solves (one persistent launch per level) ----
+// try rounds of a flag wait before it gives up (each round sleeps briefly);
+// no legitimate wait comes close
+constexpr long long kWaveSpinLimit = 1LL << 25;
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// every thread: wait until *flag is set by the CTA that owns that block
+// (thread 0 polls); false once the wait, or another CTA's wait, gave up
+__device__ __forceinline__ bool wave_wait(const int* flag, int* status, int* s_fail) {
+  if (threadIdx.x == 0) {
+    bool ok = true;
+    for (long long it = 0; ld_acquire(flag) == 0; ++it) {
+      if (it >= kWaveSpinLimit || *(volatile int*)status != 0) { ok = false; break; }
+      __nanosleep(20);
+    }
+    if (!ok) atomicExch(status, 1);
+    *s_fail = ok ? 0 : 1;
+  }
+  __syncthreads();
+  return *s_fail == 0;
+}
+
+// the next item of the level for this CTA (kept in shared memory)
+__device__ __forceinline__ int wave_next(const WaveLevel& wl, int* s_item) {
+  __syncthreads();  // every thread is done with the previous item
+  if (threadIdx.x == 0) *s_item = atomicAdd(wl.counter, 1);
+  __syncthreads();
+  return *s_item;
+}
+
+// Forward wave: a pivot block b takes x_b -= sum_{j < b} L(b, j) y_j, block
+// by block as the flags of blocks j arrive (thread (r, cq): row r, columns
+// [16 cq, 16 cq + 16) of each 64-column block), adds the four column
+// quarters in shared memory, solves its unit lower diagonal block in
+// registers (warp per right-hand side), writes y to the local vector and to
+// x, and sets its flag.  A contribution row block takes the whole
+// L21 y product the same way.
+template <typename T, int NR>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_fwd_wave(const SolveNode<T>* sns, WaveLevel wl, int nrhs, double* x, int ldx,
+               bool scale_sqrt, int* status) {
+  extern __shared__ __align__(16) unsigned char solve_smem[];
+  T* Lb = reinterpret_cast<T*>(solve_smem);
+  T* yb = Lb + SB * LDB;
+  T* red = yb + SB * NR;
+  __shared__ int s_item, s_fail;
+  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
+  const int tid = threadIdx.x, r = tid % SB, cq = tid / SB;
+  const int warp = tid >> 5, lane = tid & 31;
+  for (;;) {
+    const int it = wave_next(wl, &s_item);
+    if (it >= wl.nitems) break;
+    const int2 w = wl.items[it];
+    const SolveNode<T>& sn = sns[w.x];
+    const int m = sn.m, nelim = sn.nelim;
+    const bool piv = w.y < kWaveContrib;
+    const int r0 = piv ? w.y * SB : nelim + (w.y - kWaveContrib) * SB;
+    const int rows = min(SB, (piv ? nelim : m) - r0);
+    const int ncb = piv ? w.y : (nelim + SB - 1) / SB;
+    if (piv) prefetch_diag_block(sn, r0, rows, Lb);
+    T acc[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
+    bool ok = true;
+    for (int j = 0; j < ncb && ok; ++j) {
+      ok = wave_wait(&sn.flag[j], status, &s_fail);
+      if (!ok) break;
+      const int c0 = j * SB, jb = min(SB, nelim - c0);
+      for (int e = tid; e < SB * NR; e += kSolveThreads) {
+        const int c = e % SB, q = e / SB;
+        yb[c * NR + q] = (c < jb && q < nrhs) ? sn.xloc[(int64_t)q * m + c0 + c] : T(0);
+      }
+      __syncthreads();
+      if (r < rows) {
+        const T* Lp = sn.L + (int64_t)(c0 + cq * 16) * sn.ld + r0 + r;
+        T lv[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) lv[k] = (cq * 16 + k < jb) ? Lp[(int64_t)k * sn.ld] : T(0);
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+#pragma unroll
+          for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(cq * 16 + k) * NR + q];
+      }
+      __syncthreads();
+    }
+    if (!ok) {
+      if (piv) cp_async_wait_all();
+      continue;
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q) red[(cq * NR + q) * SB + r] = acc[q];
+    __syncthreads();
+    if (piv) {
+      T xr[R][2];
+#pragma unroll
+      for (int rr = 0; rr < R; ++rr) {
+        const int q = warp + rr * kSolveWarps;
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          const int row = lane + 32 * g;
+          T v = T(0);
+          if (q < nrhs && q < NR && row < rows)
+            v = sn.xloc[(int64_t)q * m + r0 + row] -
+                (red[q * SB + row] + red[(NR + q) * SB + row] + red[(2 * NR + q) * SB + row] +
+                 red[(3 * NR + q) * SB + row]);
+          xr[rr][g] = v;
+        }
+      }
+      cp_async_wait_all();
+      __syncthreads();
+      if (warp < nrhs) solve_in_regs<T, R, true>(rows, Lb, xr);
+#pragma unroll
+      for (int rr = 0; rr < R; ++rr) {
+        const int q = warp + rr * kSolveWarps;
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          const int row = lane + 32 * g;
+          if (q < nrhs && q < NR && row < rows) {
+            sn.xloc[(int64_t)q * m + r0 + row] = xr[rr][g];
+            double v = (double)xr[rr][g];
+            if (scale_sqrt) v *= sqrt(sn.D[2 * (r0 + row)]);
+            x[(int64_t)q * ldx + sn.perm[r0 + row]] = v;
+          }
+        }
+      }
+      __syncthreads();
+      if (tid == 0) {
+        __threadfence();
+        st_release(&sn.flag[w.y], 1);
+      }
+    } else {
+      for (int e = tid; e < SB * NR; e += kSolveThreads) {
+        const int row = e % SB, q = e / SB;
+        if (row < rows && q < nrhs)
+          sn.xloc[(int64_t)q * m + r0 + row] -=
+              red[q * SB + row] + red[(NR + q) * SB + row] + red[(2 * NR + q) * SB + row] +
+              red[(3 * NR + q) * SB + row];
+      }
+    }
+  }
+}
+
+// Backward wave: a pivot block b takes x_b -= sum L(i, b)^T x_i over the
+// rows i below the block: the contribution rows first (their values come
+// from the level's gather), then the pivot blocks j > b as their flags
+// arrive (thread (c, rq): column c, rows [16 rq, 16 rq + 16) of each
+// 64-row tile), adds the four row quarters, solves L_bb^T in registers,
+// writes y to the local vector and to x, and sets its flag.
+template <typename T, int NR>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_bwd_wave(const SolveNode<T>* sns, WaveLevel wl, int nrhs, double* x, int ldx,
+               int* status) {
+  extern __shared__ __align__(16) unsigned char solve_smem[];
+  T* Lb = reinterpret_cast<T*>(solve_smem);
+  T* yb = Lb + SB * LDB;
+  T* red = yb + SB * NR;
+  __shared__ int s_item, s_fail;
+  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
+  const int tid = threadIdx.x, c = tid % SB, rq = tid / SB;
+  const int warp = tid >> 5, lane = tid & 31;
+  for (;;) {
+    const int it = wave_next(wl, &s_item);
+    if (it >= wl.nitems) break;
+    const int2 w = wl.items[it];
+    const SolveNode<T>& sn = sns[w.x];
+    const int m = sn.m, nelim = sn.nelim;
+    const int c0 = w.y * SB, jb = min(SB, nelim - c0);
+    const int npb = (nelim + SB - 1) / SB;
+    prefetch_diag_block(sn, c0, jb, Lb);
+    T acc[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
+    // tiles of rows: contribution rows [nelim, m) first, then pivot blocks
+    // npb-1 .. b+1
+    const int ntile_c = (m - nelim + SB - 1) / SB;
+    bool ok = true;
+    for (int t = 0; t < ntile_c + (npb - 1 - w.y) && ok; ++t) {
+      int R0, nr;
+      if (t < ntile_c) {
+        R0 = nelim + t * SB;
+        nr = min(SB, m - R0);
+      } else {
+        const int j = npb - 1 - (t - ntile_c);
+        ok = wave_wait(&sn.flag[j], status, &s_fail);
+        if (!ok) break;
+        R0 = j * SB;
+        nr = min(SB, nelim - R0);
+      }
+      for (int e = tid; e < SB * NR; e += kSolveThreads) {
+        const int rr = e % SB, q = e / SB;
+        yb[rr * NR + q] = (rr < nr && q < nrhs) ? sn.xloc[(int64_t)q * m + R0 + rr] : T(0);
+      }
+      __syncthreads();
+      if (c < jb) {
+        const T* Lp = sn.L + (int64_t)(c0 + c) * sn.ld + R0 + rq * 16;
+        T lv[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) lv[k] = (rq * 16 + k < nr) ? Lp[k] : T(0);
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+#pragma unroll
+          for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(rq * 16 + k) * NR + q];
+      }
+      __syncthreads();
+    }
+    if (!ok) {
+      cp_async_wait_all();
+      continue;
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q) red[(rq * NR + q) * SB + c] = acc[q];
+    __syncthreads();
+    T xr[R][2];
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+      const int q = warp + rr * kSolveWarps;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int col = lane + 32 * g;
+        T v = T(0);
+        if (q < nrhs && q < NR && col < jb)
+          v = sn.xloc[(int64_t)q * m + c0 + col] -
+              (red[q * SB + col] + red[(NR + q) * SB + col] + red[(2 * NR + q) * SB + col] +
+               red[(3 * NR + q) * SB + col]);
+        xr[rr][g] = v;
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (warp < nrhs) solve_in_regs<T, R, false>(jb, Lb, xr);
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+      const int q = warp + rr * kSolveWarps;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int col = lane + 32 * g;
+        if (q < nrhs && q < NR && col < jb) {
+          sn.xloc[(int64_t)q * m + c0 + col] = xr[rr][g];
+          x[(int64_t)q * ldx + sn.perm[c0 + col]] = (double)xr[rr][g];
+        }
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      st_release(&sn.flag[w.y], 1);
+    }
+  }
+}
+
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 
 // CTAs per node of a block step: every CTA repeats the step's diagonal
@@ -648,6 +905,39 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
   });
 }
 
+// persistent CTAs of a wave launch: at most two per SM (each may hold an
+// item that waits), never more than there are items
+inline int wave_grid(int nitems) { return std::max(1, std::min(nitems, 2 * 152)); }
+
+template <typename T>
+void launch_fwd_wave(const SolveNode<T>* sn, const WaveLevel& wl, int nrhs, double* x, int ldx,
+                     bool scale_sqrt, int* status, cudaStream_t s) {
+  if (wl.nitems <= 0) return;
+  with_nr(nrhs, [&](auto nrc) {
+    constexpr int NR = decltype(nrc)::value;
+    k_fwd_wave<T, NR><<<wave_grid(wl.nitems), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
+        sn, wl, nrhs, x, ldx, scale_sqrt, status);
+  });
+  note_launches(1);
+}
+
+template <typename T>
+void launch_bwd_wave(const SolveNode<T>* sn, const int* nodes, int nn, const WaveLevel& wl,
+                     double* x, int ldx, int nrhs, int max_m, int diag_mode, int* status,
+                     cudaStream_t s) {
+  if (nn <= 0) return;
+  const int gx = std::max(1, std::min(cdiv(max_m * nrhs, 256), 152));
+  launch_pdl(k_bwd_gather<T>, dim3(gx, nn), 256, 0, s, sn, nodes, x, ldx, nrhs, diag_mode, true);
+  note_launches(1);
+  if (wl.nitems <= 0) return;
+  with_nr(nrhs, [&](auto nrc) {
+    constexpr int NR = decltype(nrc)::value;
+    k_bwd_wave<T, NR><<<wave_grid(wl.nitems), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
+        sn, wl, nrhs, x, ldx, status);
+  });
+  note_launches(1);
+}
+
 // the dynamic shared memory limit of every solve kernel instantiation; called
 // before solves are enqueued (never during a stream capture)
 template <typename T>
@@ -666,6 +956,8 @@ void solve_init() {
         set(k_bwd_step<T, NR, kStepFused>, solve_smem_bytes<T, NR>());
         set(k_bwd_step<T, NR, kStepSolve>, solve_smem_bytes<T, NR>());
         set(k_bwd_step<T, NR, kStepUpdate>, solve_smem_bytes<T, NR>());
+        set(k_fwd_wave<T, NR>, solve_smem_bytes<T, NR>());
+        set(k_bwd_wave<T, NR>, solve_smem_bytes<T, NR>());
       });
     }
   });
@@ -678,7 +970,11 @@ void solve_init() {
   template void launch_fwd_steps<T>(const SolveNode<T>*, const int*, int, int, int, int,       \
                                     double*, int, bool, cudaStream_t, PhaseTimer*);            \
   template void launch_bwd<T>(const SolveNode<T>*, const int*, int, double*, int, int, int, int, \
-                              int, bool, cudaStream_t, PhaseTimer*);
+                              int, bool, cudaStream_t, PhaseTimer*);                           \
+  template void launch_fwd_wave<T>(const SolveNode<T>*, const WaveLevel&, int, double*, int,   \
+                                   bool, int*, cudaStream_t);                                  \
+  template void launch_bwd_wave<T>(const SolveNode<T>*, const int*, int, const WaveLevel&,     \
+                                   double*, int, int, int, int, int*, cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

@@ -262,6 +262,23 @@ struct SolveNode {
   int sptr0;         // first own pivot
   int child_beg, child_end;  // into the child arrays
   int doff;          // offset of this node's delays inside its parent's delay block
+  int* flag;         // ceil(nelim / 64) completion flags of the wavefront solves
+  int pad_;
+};
+
+// Wavefront solves: one persistent launch per level.  The level's work
+// items, items[i] = (front, block), are taken in list order from an atomic
+// counter; a pivot block waits (bounded) for the flags of the blocks it
+// needs, which come earlier in the list, so every awaited item is held by a
+// running CTA.  Forward: pivot blocks (rows [64 b, 64 b + 64) of the
+// eliminated part) in increasing block order, then the contribution row
+// blocks (block >= 0x10000: rows nelim + 64 (block - 0x10000)).  Backward:
+// pivot blocks in decreasing order.  A wait that gives up sets *status.
+constexpr int kWaveContrib = 0x10000;
+struct WaveLevel {
+  const int2* items;
+  int nitems;
+  int* counter;  // zeroed before the launch
 };
 
 constexpr int kSolveBlk = 64;   // diagonal block of the blocked triangular solves
@@ -275,6 +292,14 @@ template <typename T>
 void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_nelim,
                       int max_m, int nrhs, double* x, int ldx, bool scale_sqrt, cudaStream_t s,
                       PhaseTimer* tm);
+template <typename T>
+void launch_fwd_wave(const SolveNode<T>* sn, const WaveLevel& wl, int nrhs, double* x, int ldx,
+                     bool scale_sqrt, int* status, cudaStream_t s);
+// backward wave after the level's gather (launch_bwd with do_bwd)
+template <typename T>
+void launch_bwd_wave(const SolveNode<T>* sn, const int* nodes, int nn, const WaveLevel& wl,
+                     double* x, int ldx, int nrhs, int max_m, int diag_mode, int* status,
+                     cudaStream_t s);
 // sets the solve kernels' dynamic shared memory limits (once per process)
 template <typename T>
 void solve_init();
