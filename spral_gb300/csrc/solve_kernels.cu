@@ -530,7 +530,7 @@ __global__ void __launch_bounds__(kSolveThreads)
 // ---- wavefront solves (one persistent launch per level) ----
 // try rounds of a flag wait before it gives up (each round sleeps briefly);
 // no legitimate wait comes close
-constexpr long long kWaveSpinLimit = 1LL << 25;
+constexpr long long kWaveSpinLimit = 1LL << 22;
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
   int v;
@@ -604,7 +604,8 @@ __global__ void __launch_bounds__(kSolveThreads)
       const int c0 = j * SB, jb = min(SB, nelim - c0);
       for (int e = tid; e < SB * NR; e += kSolveThreads) {
         const int c = e % SB, q = e / SB;
-        yb[c * NR + q] = (c < jb && q < nrhs) ? sn.xloc[(int64_t)q * m + c0 + c] : T(0);
+        // another CTA wrote these values: read them from L2, past this SM's L1
+        yb[c * NR + q] = (c < jb && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + c0 + c]) : T(0);
       }
       __syncthreads();
       if (r < rows) {
@@ -724,7 +725,8 @@ __global__ void __launch_bounds__(kSolveThreads)
       }
       for (int e = tid; e < SB * NR; e += kSolveThreads) {
         const int rr = e % SB, q = e / SB;
-        yb[rr * NR + q] = (rr < nr && q < nrhs) ? sn.xloc[(int64_t)q * m + R0 + rr] : T(0);
+        // another CTA wrote the pivot blocks' values: read them from L2
+        yb[rr * NR + q] = (rr < nr && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + R0 + rr]) : T(0);
       }
       __syncthreads();
       if (c < jb) {
