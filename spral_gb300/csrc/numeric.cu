@@ -808,7 +808,7 @@ struct Numeric : NumericBase {
   // fronts keep the block steps' SIMT updates, which are exact in FP32
   // (the 3xTF32 products carry about 22 bits and can cost the FP64
   // refinement a step)
-  int panel_min_n = 1024;
+  int panel_min_n = 4096;
   DevBuf<int> panel_list;   // fronts ending a panel (eager mode)
   int* d_tc_status = nullptr;
   int* d_ncount = nullptr;  // per-node inertia counts (neg, two, zero)
