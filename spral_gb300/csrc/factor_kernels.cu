@@ -1422,7 +1422,118 @@ __device__ Decision decide(const T* S, int ld, int nel, int m, int n, bool actio
   if (fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp) { d.kind = kOne; d.p = nel; }
   return d;
 }
+// ---- the same pivot search with every warp of the CTA (tall fronts) ----
+// Per line (row part [nel, idx) then column part [idx, m) of line idx):
+// all |v| < small, the first largest |v| of the row part, and the two
+// largest |v| off the diagonal with their positions; reduced over the CTA
+// in warp order (shuffles, then shared memory), so the result is the same
+// for every thread and every launch shape.
+struct LineInfo {
+  int all_small;
+  double rv; int ri;           // row part: first maximum
+  double v1; int i1;           // off-diagonal: largest ...
+  double v2; int i2;           // ... and second largest (positions differ)
+};
+__device__ __forceinline__ bool better(double va, int ia, double vb, int ib) {
+  return va > vb || (va == vb && ia < ib);
+}
+__device__ __forceinline__ void top2_add(LineInfo& a, double v, int i) {
+  if (better(v, i, a.v1, a.i1)) { a.v2 = a.v1; a.i2 = a.i1; a.v1 = v; a.i1 = i; }
+  else if (better(v, i, a.v2, a.i2)) { a.v2 = v; a.i2 = i; }
+}
+__device__ __forceinline__ void line_merge(LineInfo& a, const LineInfo& b) {
+  a.all_small = a.all_small && b.all_small;
+  if (better(b.rv, b.ri, a.rv, a.ri)) { a.rv = b.rv; a.ri = b.ri; }
+  top2_add(a, b.v1, b.i1);
+  top2_add(a, b.v2, b.i2);
+}
+__device__ __forceinline__ LineInfo line_shfl(const LineInfo& a, int o) {
+  LineInfo b;
+  b.all_small = __shfl_xor_sync(0xffffffffu, a.all_small, o);
+  b.rv = __shfl_xor_sync(0xffffffffu, a.rv, o); b.ri = __shfl_xor_sync(0xffffffffu, a.ri, o);
+  b.v1 = __shfl_xor_sync(0xffffffffu, a.v1, o); b.i1 = __shfl_xor_sync(0xffffffffu, a.i1, o);
+  b.v2 = __shfl_xor_sync(0xffffffffu, a.v2, o); b.i2 = __shfl_xor_sync(0xffffffffu, a.i2, o);
+  return b;
+}
+template <typename T>
+__device__ LineInfo line_info(const T* S, int ld, int idx, int nel, int m, double small,
+                              LineInfo* sh) {
+  LineInfo a{1, -1.0, 0x7fffffff, -1.0, 0x7fffffff, -1.0, 0x7fffffff};
+  for (int c = nel + (int)threadIdx.x; c < idx; c += blockDim.x) {
+    const double v = fabs((double)S[(size_t)c * ld + idx]);
+    a.all_small = a.all_small && (v < small);
+    if (better(v, c, a.rv, a.ri)) { a.rv = v; a.ri = c; }
+    top2_add(a, v, c);
+  }
+  for (int r = idx + (int)threadIdx.x; r < m; r += blockDim.x) {
+    const double v = fabs((double)S[(size_t)idx * ld + r]);
+    a.all_small = a.all_small && (v < small);
+    if (r != idx) top2_add(a, v, r);
+  }
+  for (int o = 1; o < 32; o <<= 1) {
+    const LineInfo b = line_shfl(a, o);
+    line_merge(a, b);
+  }
+  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();  // sh may still be read from the previous reduction
+  if ((threadIdx.x & 31) == 0) sh[warp] = a;
+  __syncthreads();
+  LineInfo r = sh[0];
+  for (int w = 1; w < nw; ++w) line_merge(r, sh[w]);
+  return r;
+}
+// the pivot search of one step of ldlt_tpp_factor with all threads (each
+// gets the same Decision)
+template <typename T>
+__device__ Decision decide_cta(const T* S, int ld, int nel, int m, int n, bool action, double u,
+                               double small, LineInfo* sh) {
+  Decision d{kStop, 0, 0, 0.0, 0.0, 0.0};
+  if (line_info(S, ld, nel, nel, m, small, sh).all_small) {
+    d.kind = action ? kZeroNel : kSingular;
+    return d;
+  }
+  for (int p = nel + 1; p < n; ++p) {
+    const LineInfo lp = line_info(S, ld, p, nel, m, small, sh);
+    if (lp.all_small) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return d; }
+    const int t = lp.ri;
+    double maxp = (lp.i1 == t) ? lp.v2 : lp.v1;
+    if (maxp < 0) maxp = 0.0;
+    const LineInfo lt = line_info(S, ld, t, nel, m, small, sh);
+    // largest |entry| of line t off its diagonal, excluding position p
+    double maxt = (lt.i1 == p) ? lt.v2 : lt.v1;
+    if (maxt < 0) maxt = 0.0;
+    const double a11 = (double)S[(size_t)t * ld + t], a21 = (double)S[(size_t)t * ld + p];
+    const double a22 = (double)S[(size_t)p * ld + p];
+    const double maxpiv = fmax(fabs(a11), fmax(fabs(a21), fabs(a22)));
+    if (!(maxpiv < small)) {
+      const double detscale = 1 / maxpiv;
+      const double det0 = (a11 * detscale) * a22, det1 = (a21 * detscale) * a21;
+      const double detpiv = det0 - det1;
+      if (!(fabs(detpiv) < fmax(small, fmax(fabs(det0 / 2), fabs(det1 / 2))))) {
+        const double d0 = (a22 * detscale) / detpiv, d1 = (-a21 * detscale) / detpiv;
+        const double d3 = (a11 * detscale) / detpiv;
+        bool ok;
+        if (fmax(maxp, maxt) < small) ok = true;
+        else {
+          const double x1 = fabs(d0) * maxt + fabs(d1) * maxp;
+          const double x2 = fabs(d1) * maxt + fabs(d3) * maxp;
+          ok = (u * fmax(x1, x2) < 1.0);
+        }
+        if (ok) { d.kind = kTwo; d.t = t; d.p = p; d.d0 = d0; d.d1 = d1; d.d3 = d3; return d; }
+      }
+    }
+    maxp = fmax(maxp, fabs(a21));
+    if (fabs(a22) >= u * maxp) { d.kind = kOne; d.p = p; return d; }
+  }
+  const LineInfo ln = line_info(S, ld, nel, nel, m, small, sh);
+  const double maxp = ln.v1 < 0 ? 0.0 : ln.v1;
+  if (fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp) { d.kind = kOne; d.p = nel; }
+  return d;
+}
 }  // namespace tpps
+
+// rows of a front above which the TPP pivot search uses every warp
+constexpr int kTppWideRows = 1024;
 
 // The TPP loop of ldlt_tpp_factor on columns [nel, n), rows [nel, m), of
 // the front held at S (leading dimension ld; shared or global memory), with
@@ -1436,10 +1547,14 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
                         double* D, bool action, double u, double small) {
   using namespace tpps;
   __shared__ Decision s_dec;
+  __shared__ LineInfo s_line[kTppThreads / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   while (nel < n) {
+    Decision dw;
+    const bool wide = m - nel > kTppWideRows;
+    if (wide) dw = decide_cta(S, ld, nel, m, n, action, u, small, s_line);
     if (warp == 0) {
-      Decision d = decide(S, ld, nel, m, n, action, u, small);
+      Decision d = wide ? dw : decide(S, ld, nel, m, n, action, u, small);
       if (d.kind == kZeroSwap) sym_swap(S, ld, m, d.p, nel, perm, opos);
       if (d.kind == kZeroNel || d.kind == kZeroSwap) {
         for (int r = nel + lane; r < m; r += 32) S[(size_t)nel * ld + r] = T(0);
