@@ -315,6 +315,23 @@ int spral_ssids_gpu_mem_info(size_t* free_bytes, size_t* total_bytes);
  * a quarter of the device's memory) to the driver, for the current device. */
 void spral_ssids_gpu_release_cache(void);
 
+/* Failure detection (testing aids, no reference counterpart).  Every wait
+ * of this library's kernels on another CTA or on an mbarrier is bounded:
+ * when it gives up, the kernel records an error status and returns, and the
+ * host reports SSIDS_ERROR_CUDA_UNKNOWN (-51) with the context still usable
+ * (the reference's inter-CTA spins, src/ssids/gpu/kernels/assemble.cu:208-211,
+ * are unbounded).  These probes run one such wait on a barrier or flag that
+ * nothing completes, bounded to `rounds` polls, and return -51 when it gave
+ * up (0 otherwise); the first is the tensor-core pipeline's mbarrier wait,
+ * the second the wavefront solves' flag wait. */
+int spral_ssids_gpu_mbar_timeout_probe(int rounds);
+int spral_ssids_gpu_wave_timeout_probe(int rounds);
+/* Testing aid: after `after` further successful device-block allocations
+ * of numeric handles, the next one fails as an out-of-memory cudaMalloc
+ * does (the factorization then reports SSIDS_ERROR_ALLOCATION, -50); a
+ * negative value switches the injection off. */
+void spral_ssids_gpu_inject_alloc_failure(int after);
+
 /* Number of CUDA devices visible (hw_topology/guess_topology.cxx:65). */
 int spral_ssids_gpu_device_count(void);
 

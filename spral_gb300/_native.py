@@ -108,5 +108,8 @@ def _declare(L):
     f("spral_ssids_gpu_ldlt_app_factor", I, I, I, P, P, I, P, D, P, I,
       ctypes.POINTER(CpuFactorOptions), P)
     f("spral_ssids_gpu_tc_gemm_f32", I, I, I, I, P, I, P, I, P, I, I, I, I, P)
+    f("spral_ssids_gpu_mbar_timeout_probe", I, I)
+    f("spral_ssids_gpu_wave_timeout_probe", I, I)
+    f("spral_ssids_gpu_inject_alloc_failure", None, I)
     f("spral_ssids_gpu_ldlt_app_factor_noalloc", I, I, I, P, P, I, P, D, P, I,
       ctypes.POINTER(CpuFactorOptions), P)

@@ -134,10 +134,17 @@ size_t cache_class(size_t bytes) {
 }
 }  // namespace
 
+// Allocation-failure injection for tests (spral_ssids_gpu_inject_alloc_failure):
+// when >= 0, the number of cache_alloc calls that still succeed; the call
+// after them fails as cudaMalloc does when the device is out of memory.
+static std::atomic<int> g_alloc_fail_after{-1};
+
 // allocate `bytes` on the current device; *cls receives the block's size
 void* cache_alloc(size_t bytes, size_t* cls, int* dev_out) {
   int dev = 0;
   CK(cudaGetDevice(&dev));
+  if (g_alloc_fail_after.load() >= 0 && g_alloc_fail_after.fetch_sub(1) == 0)
+    throw CudaFail{cudaErrorMemoryAllocation, __LINE__};
   *dev_out = dev;
   const size_t c = cache_class(std::max<size_t>(bytes, 1));
   *cls = c;
@@ -2070,6 +2077,10 @@ int map_cuda_error(const CudaFail& e, spral_ssids_thread_stats* st) {
 }  // namespace
 
 extern "C" {
+
+void spral_ssids_gpu_inject_alloc_failure(int after) { g_alloc_fail_after.store(after); }
+
+int spral_ssids_gpu_wave_timeout_probe(int rounds) { return wave_timeout_probe(rounds); }
 
 int spral_ssids_gpu_device_count(void) {
   int n = 0;

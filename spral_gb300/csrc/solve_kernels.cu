@@ -556,6 +556,21 @@ __device__ __forceinline__ bool wave_wait(const int* flag, int* status, int* s_f
   return *s_fail == 0;
 }
 
+// Failure-detection probe: one CTA waits on a completion flag that no
+// item will ever set, with the wait bounded to `rounds` polls; the wait
+// gives up and sets *status, as a wavefront solve does.
+__global__ void k_wave_timeout_probe(const int* flag, long long rounds, int* status) {
+  __shared__ int s_fail;
+  if (threadIdx.x == 0) {
+    bool ok = true;
+    for (long long it = 0; ld_acquire(flag) == 0; ++it)
+      if (it >= rounds) { ok = false; break; }
+    if (!ok) atomicExch(status, 1);
+    s_fail = ok ? 0 : 1;
+  }
+  __syncthreads();
+}
+
 // the next item of the level for this CTA (kept in shared memory)
 __device__ __forceinline__ int wave_next(const WaveLevel& wl, int* s_item) {
   __syncthreads();  // every thread is done with the previous item
@@ -905,6 +920,20 @@ void launch_bwd(const SolveNode<T>* sn, const int* nodes, int nn, double* x, int
       }
     }
   });
+}
+
+// returns -51 (SSIDS_ERROR_CUDA_UNKNOWN) when the bounded wait gave up, as
+// it must: nothing sets the flag
+int wave_timeout_probe(int rounds) {
+  int* d = nullptr;
+  if (cudaMalloc(&d, 2 * sizeof(int)) != cudaSuccess) { cudaGetLastError(); return -50; }
+  cudaMemset(d, 0, 2 * sizeof(int));
+  k_wave_timeout_probe<<<1, 32>>>(d, (long long)std::max(rounds, 1), d + 1);
+  int h = 0;
+  const cudaError_t e = cudaMemcpy(&h, d + 1, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) { cudaGetLastError(); return -51; }
+  return h ? -51 : 0;
 }
 
 // persistent CTAs of a wave launch: at most two per SM (each may hold an

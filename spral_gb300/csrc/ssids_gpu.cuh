@@ -300,6 +300,9 @@ template <typename T>
 void launch_bwd_wave(const SolveNode<T>* sn, const int* nodes, int nn, const WaveLevel& wl,
                      double* x, int ldx, int nrhs, int max_m, int diag_mode, int* status,
                      cudaStream_t s);
+// failure-detection probe of the wavefront solves' bounded flag wait
+// (solve_kernels.cu): -51 when the wait gave up
+int wave_timeout_probe(int rounds);
 // sets the solve kernels' dynamic shared memory limits (once per process)
 template <typename T>
 void solve_init();

@@ -596,6 +596,25 @@ int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf,
   return rc;
 }
 
+// Failure-detection probe: one CTA waits on an mbarrier that nothing will
+// ever complete, with the pipeline's bounded-wait loop cut to `limit`
+// rounds; the wait gives up, records kDevBadState in *status and the CTA
+// returns normally, leaving the context usable.
+__global__ void k_mbar_timeout_probe(long long limit, int* status) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t a = smem_u32(&bar);
+    bool done = false;
+    for (long long it = 0; it < limit && !done; ++it) done = mbar_try(a, 0);
+    if (!done) atomicExch(status, kDevBadState);
+  }
+}
+
 }  // namespace ssids300
 
 // ---------------------------------------------------------------------------
@@ -605,6 +624,18 @@ int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf,
 // reps > 0 and ms != nullptr the update is repeated reps times and
 // ms[0], ms[1] receive the mean split and GEMM times of the repetitions.
 // ---------------------------------------------------------------------------
+extern "C" int spral_ssids_gpu_mbar_timeout_probe(int rounds) {
+  int* d = nullptr;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) { cudaGetLastError(); return -50; }
+  int h = 0;
+  cudaMemset(d, 0, sizeof(int));
+  ssids300::k_mbar_timeout_probe<<<1, 32>>>((long long)std::max(rounds, 1), d);
+  const cudaError_t e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) { cudaGetLastError(); return -51; }
+  return h == ssids300::kDevBadState ? -51 : 0;  // a wait that gave up: SSIDS_ERROR_CUDA_UNKNOWN
+}
+
 extern "C" int spral_ssids_gpu_tc_gemm_f32(int M, int N, int K, const float* A, int lda,
                                            const float* B, int ldb, float* C, int ldc, int lower,
                                            int chunk, int reps, float* ms) {
