@@ -14,8 +14,10 @@ def _rel(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
 
+# FP32 factors: the two summation orders differ by FP32 rounding, amplified
+# by the matrices' condition numbers (~1e3)
 @pytest.mark.parametrize("precision,tol", [(ssids.PRECISION_FP64, 1e-12),
-                                           (ssids.PRECISION_MIXED, 1e-5)], ids=["fp64", "mixed"])
+                                           (ssids.PRECISION_MIXED, 1e-3)], ids=["fp64", "mixed"])
 @pytest.mark.parametrize("case", ["lap3d", "kkt"])
 def test_gpu_wave_solves_match_block_steps(case, precision, tol, monkeypatch):
     if case == "lap3d":
