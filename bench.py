@@ -13,7 +13,9 @@ Arms:
                      with inputs resident in HBM (value), the same through the
                      C-ABI with host buffers (e2e), the mixed-precision path
                      (FP32 factors + FP64 refinement) as a second line item,
-                     the contribution-GEMM roofline, and the CPU baseline
+                     the KKT saddle point (n = 15,000, AMD order: 2x2 pivots
+                     and delays; mixed against FP64) as a third, the
+                     contribution-GEMM roofline, and the CPU baseline
   --impl reference   the reference's CPU numeric path on the host cores:
                      the reference's own C++ core where it was compiled here,
                      else the oracle's C restatement (with OpenBLAS)
@@ -51,6 +53,8 @@ def parse():
     ap.add_argument("--nrhs", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-kkt", action="store_true",
+                    help="leave the KKT saddle-point object out of the default line")
     ap.add_argument("--mixed-only", action="store_true",
                     help="profiling aid: time only the mixed-precision path and print its object")
     ap.add_argument("--workload", default="lap3d",
@@ -502,6 +506,24 @@ def run_gpu(args):
             rel_mixed = rel_diff(x_mixed, xc)
             mixed["rel_vs_oracle"] = rel_mixed
 
+    # the KKT saddle point (mixed precision against FP64), a compact object
+    # of the same line
+    kkt = None
+    if not args.no_kkt and world == 1:
+        import copy
+        ka = copy.copy(args)
+        ka.steps, ka.warmup, ka.kkt_cpu = 3, 2, not args.no_cpu_baseline
+        kl = kkt_line(ka)
+        if kl is not None:
+            kkt = {"workload": kl["config"]["workload"], "n": kl["config"]["n"],
+                   "maxfront": kl["config"]["maxfront"],
+                   "num_neg_expected": kl["config"]["num_neg_expected"],
+                   "value": kl["value"], "unit": "solves/s", "dtype": kl["dtype"],
+                   "mixed": kl["mixed"], "fp64": kl["fp64"],
+                   "speedup_mixed_vs_fp64_gpu": kl["speedup_mixed_vs_fp64_gpu"],
+                   "e2e": kl["e2e"], "roofline": kl["roofline"],
+                   "cpu_baseline": kl["cpu_baseline"]}
+
     if rank == 0:
         neg_exact, _, _ = M.laplacian_eig_count_3d(args.grid, args.grid, args.grid, args.shift)
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
@@ -518,7 +540,8 @@ def run_gpu(args):
                 "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99)),
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
                 "bandwidth": bandwidth,
-                "cpu_baseline": cpu, "clocks": clocks, "mixed_precision": mixed}
+                "cpu_baseline": cpu, "clocks": clocks, "mixed_precision": mixed,
+                "kkt": kkt}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
@@ -842,6 +865,12 @@ def run_contrib(args):
 
 
 def run_kkt(args):
+    line = kkt_line(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def kkt_line(args):
     """KKT saddle point [[H, A^T], [A, -1e-8 I]] with the benchmark
     definition's structure (H SPD with a random symmetric pattern of about 7
     entries per row, N(0,1) off-diagonals and diagonal = row abs-sum + 1; A
@@ -976,7 +1005,8 @@ def run_kkt(args):
                                 "spral_ssids_gpu_solve_refined (host aval and x, FP32 factors)"},
                 "gpu_launches": mixed["gpu_launches"], "roofline": roof, "cpu_baseline": cpu,
                 "clocks": mixed["clocks"]}
-        print(json.dumps(line), flush=True)
+        return line
+    return None
 
 
 def main():
