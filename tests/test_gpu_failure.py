@@ -33,8 +33,14 @@ def test_gpu_injected_allocation_failure_reports_minus_50():
     lib = _native.lib()
     p, r, v = M.laplacian_3d(10, shift=-0.3)
     ak = ssids.analyse(p, r, M.nd_order_grid(10, 10, 10))
+    # the first allocation fails: no handle at all (create_num_subtree
+    # returns NULL with stats.flag = -50)
     lib.spral_ssids_gpu_inject_alloc_failure(0)
     try:
+        with pytest.raises(RuntimeError, match="flag -50"):
+            ssids.factor(ak, v)
+        # a later one fails inside the factorisation: the handle reports -50
+        lib.spral_ssids_gpu_inject_alloc_failure(2)
         fk, inf = ssids.factor(ak, v)
         assert inf.flag == ssids.SSIDS_ERROR_ALLOCATION
         fk.free()
