@@ -1314,8 +1314,12 @@ struct Numeric : NumericBase {
     {
       const char* gr = getenv("SPRAL_GB300_GRAPHS");
       use_graphs = !(gr && gr[0] == '0');
+      // wavefront solves for FP32 factors; FP64 factors keep the block-step
+      // chain, which spreads each step's FP64 update over many SMs (in a
+      // wave a pivot block's FP64 products stay in one CTA, about 9 us per
+      // 64 x 64 tile for 8 right-hand sides on GB300's FP64 pipe)
       const char* wv = getenv("SPRAL_GB300_SOLVE_WAVE");
-      use_wave = !(wv && wv[0] == '0');
+      use_wave = wv ? wv[0] != '0' : std::is_same<T, float>::value;
     }
     if (std::is_same<T, float>::value) {
       const char* env = getenv("SPRAL_GB300_TENSOR_CORES");
@@ -1725,7 +1729,7 @@ struct Numeric : NumericBase {
         if (use_wave && bwd) {
           pmark(tm(), kPhBwdUpdate, s);
           launch_bwd_wave<T>(d_sn, S->d_fronts + f0, nf, wave_level(false, l), xp, ldx, q,
-                             lvl_max_m[l], diag_mode, wstatus, s);
+                             lvl_max_m[l], lvl_max_nelim[l], diag_mode, wstatus, s);
         } else {
           launch_bwd<T>(d_sn, S->d_fronts + f0, nf, xp, ldx, q, lvl_max_m[l], lvl_max_nelim[l],
                         diag_mode, bwd, s, tm());

@@ -614,25 +614,28 @@ __global__ void __launch_bounds__(kSolveThreads)
     for (int q = 0; q < NR; ++q) acc[q] = T(0);
     bool ok = true;
     for (int j = 0; j < ncb && ok; ++j) {
+      const int c0 = j * SB, jb = min(SB, nelim - c0);
+      // the tile of L does not depend on block j's result: its loads are
+      // in flight while the flag is awaited
+      T lv[16];
+      {
+        const T* Lp = sn.L + (int64_t)(c0 + cq * 16) * sn.ld + r0 + r;
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+          lv[k] = (r < rows && cq * 16 + k < jb) ? Lp[(int64_t)k * sn.ld] : T(0);
+      }
       ok = wave_wait(&sn.flag[j], status, &s_fail);
       if (!ok) break;
-      const int c0 = j * SB, jb = min(SB, nelim - c0);
       for (int e = tid; e < SB * NR; e += kSolveThreads) {
         const int c = e % SB, q = e / SB;
         // another CTA wrote these values: read them from L2, past this SM's L1
         yb[c * NR + q] = (c < jb && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + c0 + c]) : T(0);
       }
       __syncthreads();
-      if (r < rows) {
-        const T* Lp = sn.L + (int64_t)(c0 + cq * 16) * sn.ld + r0 + r;
-        T lv[16];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) lv[k] = (cq * 16 + k < jb) ? Lp[(int64_t)k * sn.ld] : T(0);
+      for (int k = 0; k < 16; ++k)
 #pragma unroll
-        for (int k = 0; k < 16; ++k)
-#pragma unroll
-          for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(cq * 16 + k) * NR + q];
-      }
+        for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(cq * 16 + k) * NR + q];
       __syncthreads();
     }
     if (!ok) {
@@ -692,9 +695,9 @@ __global__ void __launch_bounds__(kSolveThreads)
   }
 }
 
-// Backward wave: a pivot block b takes x_b -= sum L(i, b)^T x_i over the
-// rows i below the block: the contribution rows first (their values come
-// from the level's gather), then the pivot blocks j > b as their flags
+// Backward wave (after k_bwd_l21 has subtracted L21^T x of the contribution
+// rows from every eliminated entry): a pivot block b takes
+// x_b -= sum_{j > b} L(j, b)^T y_j as the flags of the pivot blocks j
 // arrive (thread (c, rq): column c, rows [16 rq, 16 rq + 16) of each
 // 64-row tile), adds the four row quarters, solves L_bb^T in registers,
 // writes y to the local vector and to x, and sets its flag.
@@ -722,38 +725,29 @@ __global__ void __launch_bounds__(kSolveThreads)
     T acc[NR];
 #pragma unroll
     for (int q = 0; q < NR; ++q) acc[q] = T(0);
-    // tiles of rows: contribution rows [nelim, m) first, then pivot blocks
-    // npb-1 .. b+1
-    const int ntile_c = (m - nelim + SB - 1) / SB;
+    // the pivot blocks npb-1 .. b+1, as their flags arrive (the contribution
+    // rows' L21^T x was subtracted by k_bwd_l21 before this launch)
     bool ok = true;
-    for (int t = 0; t < ntile_c + (npb - 1 - w.y) && ok; ++t) {
-      int R0, nr;
-      if (t < ntile_c) {
-        R0 = nelim + t * SB;
-        nr = min(SB, m - R0);
-      } else {
-        const int j = npb - 1 - (t - ntile_c);
-        ok = wave_wait(&sn.flag[j], status, &s_fail);
-        if (!ok) break;
-        R0 = j * SB;
-        nr = min(SB, nelim - R0);
+    for (int j = npb - 1; j > w.y && ok; --j) {
+      const int R0 = j * SB, nr = min(SB, nelim - R0);
+      T lv[16];
+      {
+        const T* Lp = sn.L + (int64_t)(c0 + c) * sn.ld + R0 + rq * 16;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) lv[k] = (c < jb && rq * 16 + k < nr) ? Lp[k] : T(0);
       }
+      ok = wave_wait(&sn.flag[j], status, &s_fail);
+      if (!ok) break;
       for (int e = tid; e < SB * NR; e += kSolveThreads) {
         const int rr = e % SB, q = e / SB;
         // another CTA wrote the pivot blocks' values: read them from L2
         yb[rr * NR + q] = (rr < nr && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + R0 + rr]) : T(0);
       }
       __syncthreads();
-      if (c < jb) {
-        const T* Lp = sn.L + (int64_t)(c0 + c) * sn.ld + R0 + rq * 16;
-        T lv[16];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) lv[k] = (rq * 16 + k < nr) ? Lp[k] : T(0);
+      for (int k = 0; k < 16; ++k)
 #pragma unroll
-        for (int k = 0; k < 16; ++k)
-#pragma unroll
-          for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(rq * 16 + k) * NR + q];
-      }
+        for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(rq * 16 + k) * NR + q];
       __syncthreads();
     }
     if (!ok) {
@@ -954,8 +948,8 @@ void launch_fwd_wave(const SolveNode<T>* sn, const WaveLevel& wl, int nrhs, doub
 
 template <typename T>
 void launch_bwd_wave(const SolveNode<T>* sn, const int* nodes, int nn, const WaveLevel& wl,
-                     double* x, int ldx, int nrhs, int max_m, int diag_mode, int* status,
-                     cudaStream_t s) {
+                     double* x, int ldx, int nrhs, int max_m, int max_nelim, int diag_mode,
+                     int* status, cudaStream_t s) {
   if (nn <= 0) return;
   const int gx = std::max(1, std::min(cdiv(max_m * nrhs, 256), 152));
   launch_pdl(k_bwd_gather<T>, dim3(gx, nn), 256, 0, s, sn, nodes, x, ldx, nrhs, diag_mode, true);
@@ -963,10 +957,14 @@ void launch_bwd_wave(const SolveNode<T>* sn, const int* nodes, int nn, const Wav
   if (wl.nitems <= 0) return;
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
+    // L21^T x of the contribution rows, every eliminated column in parallel
+    const int gw = std::max(1, std::min(cdiv(max_nelim, kSolveWarps / l21_warps_host(max_m)),
+                                        4 * 152));
+    launch_pdl(k_bwd_l21<T, NR>, dim3(gw, nn), kSolveThreads, 0, s, sn, nodes, nrhs);
     k_bwd_wave<T, NR><<<wave_grid(wl.nitems), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
         sn, wl, nrhs, x, ldx, status);
   });
-  note_launches(1);
+  note_launches(2);
 }
 
 // the dynamic shared memory limit of every solve kernel instantiation; called
@@ -1005,7 +1003,7 @@ void solve_init() {
   template void launch_fwd_wave<T>(const SolveNode<T>*, const WaveLevel&, int, double*, int,   \
                                    bool, int*, cudaStream_t);                                  \
   template void launch_bwd_wave<T>(const SolveNode<T>*, const int*, int, const WaveLevel&,     \
-                                   double*, int, int, int, int, int*, cudaStream_t);
+                                   double*, int, int, int, int, int, int*, cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

@@ -298,8 +298,8 @@ void launch_fwd_wave(const SolveNode<T>* sn, const WaveLevel& wl, int nrhs, doub
 // backward wave after the level's gather (launch_bwd with do_bwd)
 template <typename T>
 void launch_bwd_wave(const SolveNode<T>* sn, const int* nodes, int nn, const WaveLevel& wl,
-                     double* x, int ldx, int nrhs, int max_m, int diag_mode, int* status,
-                     cudaStream_t s);
+                     double* x, int ldx, int nrhs, int max_m, int max_nelim, int diag_mode,
+                     int* status, cudaStream_t s);
 // failure-detection probe of the wavefront solves' bounded flag wait
 // (solve_kernels.cu): -51 when the wait gave up
 int wave_timeout_probe(int rounds);

@@ -1,7 +1,8 @@
 """The wavefront solves (one persistent launch per level, pivot blocks
-waiting on the flags of the blocks they need) against the chain of block
-step launches (SPRAL_GB300_SOLVE_WAVE=0): every job, several right-hand
-side counts, FP64 and FP32 factors, a tree with delayed columns."""
+waiting on the flags of the blocks they need; the default for FP32
+factors) against the chain of block step launches (the default for FP64
+factors): every job, several right-hand side counts, FP64 and FP32
+factors, a tree with delayed columns."""
 import numpy as np
 import pytest
 
@@ -29,6 +30,7 @@ def test_gpu_wave_solves_match_block_steps(case, precision, tol, monkeypatch):
         ak = ssids.analyse(p, r, ssids.order_amd(p, r))
     n = len(p) - 1
     opts = ssids.Options(precision=precision)
+    monkeypatch.setenv("SPRAL_GB300_SOLVE_WAVE", "1")  # FP64 factors default to the steps
     fw, infw = ssids.factor(ak, v, opts)
     monkeypatch.setenv("SPRAL_GB300_SOLVE_WAVE", "0")
     fs, infs = ssids.factor(ak, v, opts)
@@ -48,7 +50,8 @@ def test_gpu_wave_solves_match_block_steps(case, precision, tol, monkeypatch):
     fs.free()
 
 
-def test_gpu_wave_posdef_solves():
+def test_gpu_wave_posdef_solves(monkeypatch):
+    monkeypatch.setenv("SPRAL_GB300_SOLVE_WAVE", "1")
     k = 16
     p, r, v = M.laplacian_3d(k, shift=0.5)  # positive definite
     ak = ssids.analyse(p, r, M.nd_order_grid(k, k, k))
