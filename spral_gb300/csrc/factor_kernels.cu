@@ -1482,48 +1482,114 @@ __device__ LineInfo line_info(const T* S, int ld, int idx, int nel, int m, doubl
   for (int w = 1; w < nw; ++w) line_merge(r, sh[w]);
   return r;
 }
+// the line information of lines [l0, l1) (one warp per line) into
+// out[idx - nel], then a barrier
+template <typename T>
+__device__ void line_info_batch(const T* S, int ld, int l0, int l1, int nel, int m, double small,
+                                LineInfo* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int idx = l0 + warp; idx < l1; idx += nw) {
+    LineInfo a{1, -1.0, 0x7fffffff, -1.0, 0x7fffffff, -1.0, 0x7fffffff};
+    for (int c = nel + lane; c < idx; c += 32) {
+      const double v = fabs((double)S[(size_t)c * ld + idx]);
+      a.all_small = a.all_small && (v < small);
+      if (better(v, c, a.rv, a.ri)) { a.rv = v; a.ri = c; }
+      top2_add(a, v, c);
+    }
+    for (int r = idx + lane; r < m; r += 32) {
+      const double v = fabs((double)S[(size_t)idx * ld + r]);
+      a.all_small = a.all_small && (v < small);
+      if (r != idx) top2_add(a, v, r);
+    }
+    for (int o = 1; o < 32; o <<= 1) {
+      const LineInfo b = line_shfl(a, o);
+      line_merge(a, b);
+    }
+    if (lane == 0) out[idx - nel] = a;
+  }
+  __syncthreads();
+}
+
+// One candidate p of ldlt_tpp_factor's search (ldlt_tpp.cxx:196-236), from
+// the line information of p and of t = the first largest entry of row p:
+// returns true with d set when p is taken (as a zero column, a 2x2 pivot
+// (t, p) or a 1x1 pivot).
+template <typename T>
+__device__ bool try_candidate(const T* S, int ld, int p, const LineInfo& lp, const LineInfo& lt,
+                              bool action, double u, double small, Decision& d) {
+  if (lp.all_small) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return true; }
+  const int t = lp.ri;
+  double maxp = (lp.i1 == t) ? lp.v2 : lp.v1;
+  if (maxp < 0) maxp = 0.0;
+  // largest |entry| of line t off its diagonal, excluding position p
+  double maxt = (lt.i1 == p) ? lt.v2 : lt.v1;
+  if (maxt < 0) maxt = 0.0;
+  const double a11 = (double)S[(size_t)t * ld + t], a21 = (double)S[(size_t)t * ld + p];
+  const double a22 = (double)S[(size_t)p * ld + p];
+  const double maxpiv = fmax(fabs(a11), fmax(fabs(a21), fabs(a22)));
+  if (!(maxpiv < small)) {
+    const double detscale = 1 / maxpiv;
+    const double det0 = (a11 * detscale) * a22, det1 = (a21 * detscale) * a21;
+    const double detpiv = det0 - det1;
+    if (!(fabs(detpiv) < fmax(small, fmax(fabs(det0 / 2), fabs(det1 / 2))))) {
+      const double d0 = (a22 * detscale) / detpiv, d1 = (-a21 * detscale) / detpiv;
+      const double d3 = (a11 * detscale) / detpiv;
+      bool ok;
+      if (fmax(maxp, maxt) < small) ok = true;
+      else {
+        const double x1 = fabs(d0) * maxt + fabs(d1) * maxp;
+        const double x2 = fabs(d1) * maxt + fabs(d3) * maxp;
+        ok = (u * fmax(x1, x2) < 1.0);
+      }
+      if (ok) { d.kind = kTwo; d.t = t; d.p = p; d.d0 = d0; d.d1 = d1; d.d3 = d3; return true; }
+    }
+  }
+  maxp = fmax(maxp, fabs(a21));
+  if (fabs(a22) >= u * maxp) { d.kind = kOne; d.p = p; return true; }
+  return false;
+}
+
 // the pivot search of one step of ldlt_tpp_factor with all threads (each
-// gets the same Decision)
+// gets the same Decision).  The first candidate is tested from two line
+// scans; when it fails and `batch` (>= n - nel line records of global
+// scratch) is given, the information of every remaining line is gathered
+// in one pass, one warp per line, and the other candidates are tested from
+// it: a search that runs through many candidates (failed columns, as in KKT
+// systems) reads each line once instead of twice per candidate.  The
+// records equal line_info's, so the decision is the same either way.
 template <typename T>
 __device__ Decision decide_cta(const T* S, int ld, int nel, int m, int n, bool action, double u,
-                               double small, LineInfo* sh) {
+                               double small, LineInfo* sh, LineInfo* batch) {
   Decision d{kStop, 0, 0, 0.0, 0.0, 0.0};
   if (line_info(S, ld, nel, nel, m, small, sh).all_small) {
     d.kind = action ? kZeroNel : kSingular;
     return d;
   }
-  for (int p = nel + 1; p < n; ++p) {
+  int p = nel + 1;
+  if (p < n) {
+    const LineInfo lp = line_info(S, ld, p, nel, m, small, sh);
+    const LineInfo lt = line_info(S, ld, lp.ri, nel, m, small, sh);
+    if (try_candidate(S, ld, p, lp, lt, action, u, small, d)) return d;
+    ++p;
+  }
+  if (batch != nullptr && p < n) {
+    line_info_batch(S, ld, nel, n, nel, m, small, batch);
+    for (; p < n; ++p) {
+      const LineInfo lp = batch[p - nel];
+      if (try_candidate(S, ld, p, lp, batch[(lp.all_small ? p : lp.ri) - nel], action, u, small,
+                        d))
+        return d;
+    }
+    const LineInfo ln = batch[0];
+    const double maxp = ln.v1 < 0 ? 0.0 : ln.v1;
+    if (fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp) { d.kind = kOne; d.p = nel; }
+    return d;
+  }
+  for (; p < n; ++p) {
     const LineInfo lp = line_info(S, ld, p, nel, m, small, sh);
     if (lp.all_small) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return d; }
-    const int t = lp.ri;
-    double maxp = (lp.i1 == t) ? lp.v2 : lp.v1;
-    if (maxp < 0) maxp = 0.0;
-    const LineInfo lt = line_info(S, ld, t, nel, m, small, sh);
-    // largest |entry| of line t off its diagonal, excluding position p
-    double maxt = (lt.i1 == p) ? lt.v2 : lt.v1;
-    if (maxt < 0) maxt = 0.0;
-    const double a11 = (double)S[(size_t)t * ld + t], a21 = (double)S[(size_t)t * ld + p];
-    const double a22 = (double)S[(size_t)p * ld + p];
-    const double maxpiv = fmax(fabs(a11), fmax(fabs(a21), fabs(a22)));
-    if (!(maxpiv < small)) {
-      const double detscale = 1 / maxpiv;
-      const double det0 = (a11 * detscale) * a22, det1 = (a21 * detscale) * a21;
-      const double detpiv = det0 - det1;
-      if (!(fabs(detpiv) < fmax(small, fmax(fabs(det0 / 2), fabs(det1 / 2))))) {
-        const double d0 = (a22 * detscale) / detpiv, d1 = (-a21 * detscale) / detpiv;
-        const double d3 = (a11 * detscale) / detpiv;
-        bool ok;
-        if (fmax(maxp, maxt) < small) ok = true;
-        else {
-          const double x1 = fabs(d0) * maxt + fabs(d1) * maxp;
-          const double x2 = fabs(d1) * maxt + fabs(d3) * maxp;
-          ok = (u * fmax(x1, x2) < 1.0);
-        }
-        if (ok) { d.kind = kTwo; d.t = t; d.p = p; d.d0 = d0; d.d1 = d1; d.d3 = d3; return d; }
-      }
-    }
-    maxp = fmax(maxp, fabs(a21));
-    if (fabs(a22) >= u * maxp) { d.kind = kOne; d.p = p; return d; }
+    const LineInfo lt = line_info(S, ld, lp.ri, nel, m, small, sh);
+    if (try_candidate(S, ld, p, lp, lt, action, u, small, d)) return d;
   }
   const LineInfo ln = line_info(S, ld, nel, nel, m, small, sh);
   const double maxp = ln.v1 < 0 ? 0.0 : ln.v1;
@@ -1535,6 +1601,14 @@ __device__ Decision decide_cta(const T* S, int ld, int nel, int m, int n, bool a
 // rows of a front above which the TPP pivot search uses every warp
 constexpr int kTppWideRows = 1024;
 
+// line records of the batched pivot search: the front's workspace W (ld x 32
+// entries; the first two columns hold the pivot copies), 56 n <= 30 ld
+// sizeof(T) bytes
+template <typename T>
+__device__ __forceinline__ tpps::LineInfo* tpp_batch(const FrontDesc<T>& fd) {
+  return reinterpret_cast<tpps::LineInfo*>(fd.W + 2 * (size_t)fd.ld);
+}
+
 // The TPP loop of ldlt_tpp_factor on columns [nel, n), rows [nel, m), of
 // the front held at S (leading dimension ld; shared or global memory), with
 // two workspace columns W0, W1 (>= m entries) and the front's perm, opos
@@ -1544,7 +1618,7 @@ constexpr int kTppWideRows = 1024;
 // front with action == false.  Called by all threads of the CTA.
 template <typename T>
 __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* perm, int* opos,
-                        double* D, bool action, double u, double small) {
+                        double* D, bool action, double u, double small, tpps::LineInfo* batch) {
   using namespace tpps;
   __shared__ Decision s_dec;
   __shared__ LineInfo s_line[kTppThreads / 32];
@@ -1552,7 +1626,7 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
   while (nel < n) {
     Decision dw;
     const bool wide = m - nel > kTppWideRows;
-    if (wide) dw = decide_cta(S, ld, nel, m, n, action, u, small, s_line);
+    if (wide) dw = decide_cta(S, ld, nel, m, n, action, u, small, s_line, batch);
     if (warp == 0) {
       Decision d = wide ? dw : decide(S, ld, nel, m, n, action, u, small);
       if (d.kind == kZeroSwap) sym_swap(S, ld, m, d.p, nel, perm, opos);
@@ -1644,7 +1718,7 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontSta
   if (st->nelim >= fd.n) return;
   if (!(all_fronts || fd.m == fd.n)) return;
   const int nel = tpp_fast(fd.L, fd.ld, fd.m, fd.n, st->nelim, fd.W, fd.W + fd.ld, fd.perm,
-                           fd.opos, fd.D, action, u, small);
+                           fd.opos, fd.D, action, u, small, tpp_batch(fd));
   if (threadIdx.x == 0) {
     if (nel < 0) st->status = kDevSingular;
     else { st->nelim = nel; st->p = nel; }
@@ -1669,7 +1743,7 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, Fr
     nel = 0;
   } else if (need > (size_t)smem_bytes) {
     nel = tpp_fast(fd.L, fd.ld, m, n, 0, fd.W, fd.W + fd.ld, fd.perm, fd.opos, fd.D, action, u,
-                   small);
+                   small, tpp_batch(fd));
   } else {
     T* S = reinterpret_cast<T*>(tpp_smem);
     T* W0 = S + (size_t)ldS * n;
@@ -1680,7 +1754,7 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, Fr
       for (int r = threadIdx.x; r < m; r += blockDim.x) S[(size_t)c * ldS + r] = fd.L[(int64_t)c * fd.ld + r];
     for (int i = threadIdx.x; i < n; i += blockDim.x) { sperm[i] = fd.perm[i]; sopos[i] = fd.opos[i]; }
     __syncthreads();
-    nel = tpp_fast(S, ldS, m, n, 0, W0, W1, sperm, sopos, fd.D, action, u, small);
+    nel = tpp_fast(S, ldS, m, n, 0, W0, W1, sperm, sopos, fd.D, action, u, small, nullptr);
     __syncthreads();
     if (nel >= 0) {
       for (int c = 0; c < n; ++c)
