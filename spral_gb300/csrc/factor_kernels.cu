@@ -621,233 +621,6 @@ __global__ void __launch_bounds__(kDiagThreads)
   if (tid < bs) { fd.perm[p + tid] = oldp; fd.opos[p + tid] = oldo; }
 }
 
-// ------------------------------------------------------------------------
-// k_app_diag_w32: the indefinite diagonal block for FP32 factors in ONE warp.
-// Lane j holds physical column j of the block (all 32 physical rows, the
-// block kept full-symmetric) in registers; the logical <-> physical maps
-// live in shared memory.  Each pivot: every lane keys the entries of its
-// column that lie in the logical lower triangle (the same 64-bit keys as
-// k_app_diag_f32: magnitude, then the reference's column-major order), one
-// warp maximum picks the pivot, the 1x1 / 2x2 decision is taken by every
-// lane alike, the pivot column(s) are broadcast by shuffles and each lane
-// applies the rank-1/2 update to its column.  The update is written in a
-// form symmetric in the two indices (e11 (x1 y1) + e21 (x1 y2 + x2 y1) +
-// e22 (x2 y2), x and y the pivot-column entries of the two indices), so
-// the two copies of every entry stay bitwise equal.  No block barrier, no
-// second reduction level: the per-pivot chain is a warp's instruction
-// stream.  Outputs as k_app_diag_f32 (L11, D^{-1} in FP64, step buffer,
-// lperm, perm/opos).
-// ------------------------------------------------------------------------
-__device__ __forceinline__ float sel32(const float (&c)[kBlk], int k) {
-  float v = c[0];
-#pragma unroll
-  for (int i = 1; i < kBlk; ++i) v = (k == i) ? c[i] : v;
-  return v;
-}
-
-__global__ void __launch_bounds__(32)
-    k_app_diag_w32(FrontDesc<float>* fds, FrontState* sts, const int* fronts, int step,
-                   bool action, double small) {
-  constexpr unsigned FULL = 0xffffffffu;
-  const int f = fronts[blockIdx.x];
-  FrontState* st = &sts[f];
-  const int lane = threadIdx.x;
-  __shared__ float outb[kBlk][kBlk + 1];  // outb[j][X] = L(logical row of X, j)
-  __shared__ int map[kBlk];               // logical -> physical
-  __shared__ int lgs[kBlk];               // physical -> logical
-  __shared__ float pv[kBlk][3];           // pivot entries: a11 (1x1: d), a21, a22
-  __shared__ int psz[kBlk];               // 1: 1x1, 2: first of a 2x2, 3: second, 0: zero
-  __shared__ double dd[2 * kBlk + 2];
-  __shared__ FrontDesc<float> fd;
-  if (lane == 0) fd = fds[f];  // written by the host before the launch
-  pdl_wait();
-  pdl_trigger();
-  int p = 0, bs = 0;
-  if (lane == 0) app_step_begin(fd, st, step, p, bs);
-  p = __shfl_sync(FULL, p, 0);
-  bs = __shfl_sync(FULL, bs, 0);
-  __syncwarp();
-  if (bs == 0) return;
-  float fsmall = (float)small;
-  if ((double)fsmall < small) fsmall = nextafterf(fsmall, INFINITY);
-  const float* Lb = fd.L + (int64_t)p * fd.ld + p;
-  float c[kBlk];
-#pragma unroll
-  for (int r = 0; r < kBlk; ++r) {
-    float v = 0.f;
-    if (r < bs && lane < bs) v = (r >= lane) ? Lb[(int64_t)lane * fd.ld + r] : Lb[(int64_t)r * fd.ld + lane];
-    c[r] = v;
-  }
-  for (int e = lane; e < kBlk * (kBlk + 1); e += 32) (&outb[0][0])[e] = 0.f;
-  map[lane] = lane;
-  lgs[lane] = lane;
-  psz[lane] = 0;
-  if (lane < 2 * kBlk + 2 - 64) dd[64 + lane] = 0.0;
-  dd[lane] = 0.0;
-  dd[32 + lane] = 0.0;
-  __syncwarp();
-  int lg = lane;  // logical index of this lane's physical column
-  bool singular = false;
-  for (int q = 0; q < bs;) {
-    unsigned long long key = 0ULL;
-    if (lane < bs && lg >= q) {
-#pragma unroll
-      for (int r = 0; r < kBlk; ++r) {
-        const int lr = lgs[r];
-        if (r < bs && lr >= lg) {
-          const unsigned long long k = diag_key_f32(c[r], lg, lr, lane, r);
-          key = k > key ? k : key;
-        }
-      }
-    }
-    key = warp_max_u64(key);
-    const unsigned lo32 = (unsigned)key;
-    const int pos = 1023 - (int)(lo32 >> 10);
-    const int bj = pos >> 5, bi = pos & 31;                         // logical column, row
-    const int pj = (int)((lo32 >> 5) & 31), pi = (int)(lo32 & 31);  // their physical
-    const float bv = __uint_as_float((unsigned)(key >> 32) & 0x7fffffffu);
-    int pivsiz = 1, i1 = bi, i2 = -1;
-    float e11 = 0.f, e21 = 0.f, e22 = 0.f, a11 = 0.f, a21 = 0.f, a22 = 0.f;
-    if (key == 0ULL || bv < fsmall) {
-      pivsiz = 0;
-    } else if (bi != bj) {
-      // A(pj, pj), A(pi, pi), A(pi, pj) from the lanes that hold them
-      a11 = __shfl_sync(FULL, sel32(c, pj), pj);
-      a22 = __shfl_sync(FULL, sel32(c, pi), pi);
-      a21 = __shfl_sync(FULL, sel32(c, pi), pj);
-      const float aa21 = fabsf(a21);
-      const float detscale = __frcp_rn(aa21);
-      const float detpiv = (a11 * detscale) * a22 - aa21;
-      if (fabsf(detpiv) >= aa21 * 0.5f) {
-        pivsiz = 2; i1 = bj; i2 = bi;
-        const float rdet = __frcp_rn(detpiv);
-        e11 = (a22 * detscale) * rdet;
-        e21 = (-a21 * detscale) * rdet;
-        e22 = (a11 * detscale) * rdet;
-      } else if (fabsf(a11) > fabsf(a22)) {
-        i1 = bj;
-      } else {
-        i1 = bi;
-      }
-    }
-    if (pivsiz == 0) {
-      // the remaining logical columns are zero pivots (psz 0): L columns and
-      // D^{-1} stay zero
-      if (!action) singular = true;
-      break;
-    }
-    const int pa = map[q], pb = map[i1];
-    const int cq1 = (pivsiz == 2) ? ((i1 == q + 1) ? pa : map[q + 1]) : -1;
-    const int ci2 = (pivsiz == 2) ? map[i2] : -1;
-    // swaps q <-> i1, then q+1 <-> i2, applied to logical indices
-    auto relabel = [&](int x) {
-      x = (x == q) ? i1 : (x == i1) ? q : x;
-      if (pivsiz == 2) x = (x == q + 1) ? i2 : (x == i2) ? q + 1 : x;
-      return x;
-    };
-    const int qn = q + pivsiz;
-    const int lgn = relabel(lg);
-    __syncwarp();  // every lane has read map / lgs of this pivot
-    // new maps: lane x updates entry x of each
-    {
-      int v = map[lane];
-      if (lane == q) v = pb; else if (lane == i1) v = pa;
-      if (pivsiz == 2) {
-        if (lane == q + 1) v = ci2; else if (lane == i2) v = cq1;
-      }
-      map[lane] = v;
-      lgs[lane] = lgn;
-    }
-    __syncwarp();
-    if (pivsiz == 1) {
-      const int P = pb;
-      const float app = __shfl_sync(FULL, sel32(c, P), P);
-      const float dT = __frcp_rn(app);
-      const float y = sel32(c, P);  // A(P, this column)
-      if (lgn > q && lane < bs) outb[q][lane] = y * dT;
-#pragma unroll
-      for (int r = 0; r < kBlk; ++r) {
-        const float x = __shfl_sync(FULL, c[r], P);  // A(r, P), every lane takes part
-        if (lgn >= qn && lgs[r] >= qn) c[r] = c[r] - (x * y) * dT;
-      }
-      if (lane == 0) { psz[q] = 1; pv[q][0] = app; }
-    } else {
-      const int P1 = pb, P2 = ci2;
-      const float y1 = sel32(c, P1), y2 = sel32(c, P2);  // A(P1, this), A(P2, this)
-      if (lgn > q + 1 && lane < bs) {
-        outb[q][lane] = e11 * y1 + e21 * y2;
-        outb[q + 1][lane] = e21 * y1 + e22 * y2;
-      }
-#pragma unroll
-      for (int r = 0; r < kBlk; ++r) {
-        const float x1 = __shfl_sync(FULL, c[r], P1), x2 = __shfl_sync(FULL, c[r], P2);
-        if (lgn >= qn && lgs[r] >= qn)
-          c[r] = c[r] - (e11 * (x1 * y1) + e21 * (x1 * y2 + x2 * y1) + e22 * (x2 * y2));
-      }
-      if (lane == 0) {
-        psz[q] = 2;
-        psz[q + 1] = 3;
-        pv[q][0] = a11;
-        pv[q][1] = a21;
-        pv[q][2] = a22;
-      }
-    }
-    lg = lgn;
-    q = qn;
-    __syncwarp();
-  }
-  __syncwarp();
-  if (singular) {
-    if (lane == 0) { st->status = kDevSingular; st->bs = 0; }
-    return;
-  }
-  // D^{-1} in FP64 from the recorded pivots (as k_app_diag_f32)
-  if (lane < bs) {
-    const int ps = psz[lane];
-    if (ps == 1) {
-      dd[2 * lane] = recip_nr((double)pv[lane][0]);
-      dd[2 * lane + 1] = 0.0;
-    } else if (ps == 2) {
-      const double d11 = pv[lane][0], d21 = pv[lane][1], d22 = pv[lane][2];
-      const double detscale = recip_nr(fabs(d21));
-      const double detpiv = (d11 * detscale) * d22 - fabs(d21);
-      const double rdet = recip_nr(detpiv);
-      dd[2 * lane] = (d22 * detscale) * rdet;
-      dd[2 * lane + 1] = (-d21 * detscale) * rdet;
-      dd[2 * lane + 2] = dinf();
-      dd[2 * lane + 3] = (d11 * detscale) * rdet;
-    } else if (ps == 0) {
-      dd[2 * lane] = 0.0;
-      dd[2 * lane + 1] = 0.0;
-    }
-  }
-  __syncwarp();
-  // ---- write L11 (logical lower part, unit diagonal), D, step buffer, perm
-  for (int e = lane; e < kBlk * kBlk; e += 32) {
-    const int j = e >> 5, X = e & 31;  // logical column, physical row
-    if (j < bs && X < bs) {
-      const int i = lgs[X];
-      if (i >= j) {
-        const float v = (i == j) ? 1.f : outb[j][X];
-        fd.L[(int64_t)(p + j) * fd.ld + p + i] = v;
-        fd.step[j * kBlk + i] = (double)v;
-      }
-    }
-  }
-  int oldp = 0, oldo = 0;
-  if (lane < bs) {
-    fd.D[2 * (p + lane)] = dd[2 * lane];
-    fd.D[2 * (p + lane) + 1] = dd[2 * lane + 1];
-    fd.step[kBlk * kBlk + 2 * lane] = dd[2 * lane];
-    fd.step[kBlk * kBlk + 2 * lane + 1] = dd[2 * lane + 1];
-    fd.lperm[lane] = map[lane];
-    oldp = fd.perm[p + map[lane]];
-    oldo = fd.opos[p + map[lane]];
-  }
-  __syncwarp();
-  if (lane < bs) { fd.perm[p + lane] = oldp; fd.opos[p + lane] = oldo; }
-}
-
 // columns of the eliminated part that one warp of k_app_apply's permutation
 // CTAs moves per round
 constexpr int kPermCols = 8;
@@ -2110,16 +1883,6 @@ void launch_syrk_contrib(FrontDesc<T>* fd, const FrontState* st, const int* fron
 
 static inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 
-// the one-warp FP32 diagonal-block kernel (SPRAL_GB300_DIAG_WARP=0 selects
-// the 17-warp k_app_diag_f32)
-static bool diag_one_warp() {
-  static const bool on = [] {
-    const char* e = getenv("SPRAL_GB300_DIAG_WARP");
-    return !(e && e[0] == '0');
-  }();
-  return on;
-}
-
 template <typename T>
 void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int step,
                      int max_rows, int max_trail_rows, int max_trail_cols, bool action,
@@ -2129,10 +1892,7 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
   if (posdef) {
     launch_pdl(k_app_diag<T, true>, nf, kDiagThreads, 0, s, fd, st, fronts, step, action, small);
   } else if constexpr (std::is_same<T, float>::value) {
-    if (diag_one_warp())
-      launch_pdl(k_app_diag_w32, nf, 32, 0, s, fd, st, fronts, step, action, small);
-    else
-      launch_pdl(k_app_diag_f32, nf, kDiagThreads, 0, s, fd, st, fronts, step, action, small);
+    launch_pdl(k_app_diag_f32, nf, kDiagThreads, 0, s, fd, st, fronts, step, action, small);
   } else {
     launch_pdl(k_app_diag<T, false>, nf, kDiagThreads, 0, s, fd, st, fronts, step, action, small);
   }
