@@ -285,6 +285,48 @@ def test_gpu_mixed_falls_back_to_fp64_when_refinement_cannot_converge():
     assert fk2.fallbacks == 0
 
 
+def _stack_lower_csc(mats, orders):
+    """Block-diagonal stacking of lower-CSC matrices (and their orders)."""
+    ptr, row, val, order = [np.zeros(1, dtype=np.int64)], [], [], []
+    off = 0
+    for (p, r, v), o in zip(mats, orders):
+        ptr.append(p[1:] + ptr[-1][-1])
+        row.append(r + off)
+        val.append(v)
+        order.append(o + off)
+        off += len(p) - 1
+    return (np.concatenate(ptr), np.concatenate(row).astype(np.int32), np.concatenate(val),
+            np.concatenate(order).astype(np.int32))
+
+
+def test_gpu_mixed_fallback_on_a_front_local_failure():
+    """Two independent blocks in one tree (a forest): a well-conditioned 3D
+    Laplacian and a 2D Laplacian with an eigenvalue 3e-9 from zero.  Only the
+    fronts of the second block carry the ill-conditioning; the FP32 refinement
+    stalls and the refined solve refactors the whole matrix in FP64 (the
+    fallback is per matrix, not per front), after which both blocks meet the
+    FP64 bar and the inertia is exact."""
+    nx, ny = 30, 34
+    lam = (2 - 2 * np.cos(np.pi * 3 / (nx + 1))) + (2 - 2 * np.cos(np.pi * 5 / (ny + 1)))
+    shift = 3e-9 - lam
+    k = 16
+    good = M.laplacian_3d(k, shift=-0.3)
+    bad = M.laplacian_2d(nx, ny, shift)
+    p, r, v, order = _stack_lower_csc([good, bad], [M.nd_order_grid(k, k, k),
+                                                     M.nd_order_grid(nx, ny)])
+    ak = ssids.analyse(p, r, order)
+    opts = ssids.Options(precision=ssids.PRECISION_MIXED, max_refine=20, refine_tol=1e-14)
+    fk, _ = ssids.factor(ak, v, opts)
+    b = np.random.default_rng(7).uniform(-1, 1, (len(p) - 1, 2))
+    x = fk.solve_refined(b)
+    assert fk.fallbacks == 1
+    assert M.scaled_bwd_error(p, r, v, x, b).max() <= 1e-14
+    neg3, _, _ = M.laplacian_eig_count_3d(k, k, k, -0.3)
+    neg2, _, _ = M.laplacian_eig_count_2d(nx, ny, shift)
+    assert fk.inform.num_neg == neg3 + neg2
+    fk.free()
+
+
 def test_gpu_recip_within_one_ulp():
     """The Newton reciprocal on the pivot-decision path agrees with IEEE
     division to one unit in the last place (and exactly at special values)."""
