@@ -333,7 +333,21 @@ def tensor_roofline(L, fk, aval_d, ak=None):
             "achieved": 3.0 * alg, "achieved_fp32_update": alg, "peak": peak,
             "unit": "TFLOP/s", "frac": 3.0 * alg / peak, "traffic": None,
             "peak_source": src, "launches": int(ps[5]), "flops_per_step": ps[4],
-            "contrib_update_ms": ps[0], "tc_gemm_ms": ps[3]}
+            "contrib_update_ms": ps[0], "tc_gemm_ms": ps[3], "autotuner": tune_table()}
+
+
+def tune_table():
+    """The library's autotuner table for this GPU: the SIMT / tensor-core
+    crossover and the tile width per size class (largest contribution block
+    of a launch, rows)."""
+    from spral_gb300 import _native
+    tab = np.zeros(32, dtype=np.int32)
+    n = _native.lib().spral_ssids_gpu_tune_table(tab.ctypes.data_as(ctypes.c_void_p), 32)
+    if n <= 0:
+        return None
+    t = tab[:n].tolist()
+    return {"tc_min_cm": t[0],
+            "tile_width_by_max_rows": {str(m): w for m, w in zip(t[2::2], t[3::2])}}
 
 
 def run_gpu(args):
@@ -795,13 +809,23 @@ def run_tc_gemm(args):
                                              max(args.steps, 3), ms) == 0
         flops = 2.0 * K_ * mask.sum()
         alg = flops / (ms[1] * 1e-3) / 1e12
+        # every tile width of the kernel, beside the autotuned one above
+        widths = {}
+        for bn in (64, 128, 256):
+            mw = (ctypes.c_float * 2)()
+            assert L.spral_ssids_gpu_tc_gemm_f32_bn(M_, N_, K_, dA.data_ptr(), M_, dB.data_ptr(),
+                                                    N_, dC.data_ptr(), M_, lower, -1,
+                                                    max(args.steps, 3), mw, bn) == 0
+            widths[str(bn)] = {"gemm_ms": mw[1], "tensor_tflops": 3 * flops / (mw[1] * 1e-3) / 1e12}
         out.append({"shape": f"{M_}x{N_}x{K_}" + (" lower" if lower else ""),
                     "gemm_ms": ms[1], "split_ms": ms[0], "fp32_update_tflops": alg,
                     "tensor_tflops": 3 * alg, "frac": 3 * alg / peak,
-                    "rms_err_over_sqrtK": rms})
+                    "rms_err_over_sqrtK": rms, "tile_widths": widths})
+    tune = tune_table()
     print(json.dumps({"metric": "tensor-core Schur update TFLOP/s (3xTF32)", "workload": "tc-gemm",
                       "value": out[-1]["tensor_tflops"], "unit": "TFLOP/s",
-                      "peak": peak, "peak_source": src, "cases": out}), flush=True)
+                      "peak": peak, "peak_source": src, "autotuner": tune, "cases": out}),
+          flush=True)
 
 
 def run_contrib(args):

@@ -275,6 +275,12 @@ int spral_ssids_gpu_tc_gemm_f32(int M, int N, int K, const float* A, int lda, co
                                 int ldb, float* C, int ldc, int lower, int chunk, int reps,
                                 float* ms);
 
+/* The same with an explicit tile width bn (64, 128 or 256; 0: the
+ * autotuned width).  Returns -4 for another width. */
+int spral_ssids_gpu_tc_gemm_f32_bn(int M, int N, int K, const float* A, int lda, const float* B,
+                                   int ldb, float* C, int ldc, int lower, int chunk, int reps,
+                                   float* ms, int bn);
+
 /* Per-node inertia of the last factorisation: out[3*node + {0, 1, 2}] =
  * (negative eigenvalues, 2x2 pivots, zero pivots) of each node's D, nodes
  * numbered 0-based as in the symbolic subtree.  Batched factorisations of
@@ -289,6 +295,39 @@ int spral_ssids_gpu_node_inertia(const void* numeric, int* out);
  * SPRAL_GB300_TC_MIN_CM overrides it).  No reference counterpart.  Returns
  * the size, or -51 on a CUDA error. */
 int spral_ssids_gpu_tc_crossover(void);
+
+/* The autotuner's table for the current device: the crossover above and,
+ * per size class of a launch (its largest contribution block, m rows or
+ * fewer), the fastest tile width of the tensor-core update (128 x 64,
+ * 128 x 128 or 128 x 256), all measured once per device, or read from the
+ * tune cache file named by the environment variable SPRAL_GB300_TUNE_CACHE
+ * when it holds a line for this device (and written there after a
+ * measurement).  out = [tc_min_cm, nb, m_0, bn_0, ..., m_{nb-1}, bn_{nb-1}].
+ * Returns the number of ints written, -1 if nout is too small, -51 on a
+ * CUDA error.  No reference counterpart (the reference's kernel shapes are
+ * fixed at compile time). */
+int spral_ssids_gpu_tune_table(int* out, int nout);
+
+/* The current device's key in the tune cache (device name with '_' for
+ * spaces, "-sm<multiprocessors>-cc<major><minor>").  Returns its length, or
+ * -1 (no device, or cap too small). */
+int spral_ssids_gpu_tune_device_key(char* buf, int cap);
+
+/* Tune-cache helpers (host only, no GPU needed).  A cache line reads
+ *   spral_gb300-tune v1 <key> tc_min_cm=<int> bn=<m>:<bn>,<m>:<bn>,...
+ * with strictly increasing m and bn in {64, 128, 256}; tables are passed as
+ * the ints of spral_ssids_gpu_tune_table.
+ * _parse: parses one line into key (key_cap bytes) and out; returns the
+ *   number of ints, or -1 for a malformed line or too little room.
+ * _format: writes the line of (key, table) into buf; returns its length or -1.
+ * _cache_lookup: the last line for key in the file at path; returns the
+ *   number of ints, 0 if the file or the key is absent, -1 if out is too small.
+ * _cache_store: replaces (or adds) the line for key, keeping the others;
+ *   the file is replaced by a rename.  Returns 0 or -1. */
+int spral_ssids_gpu_tune_parse(const char* line, char* key, int key_cap, int* out, int nout);
+int spral_ssids_gpu_tune_format(const char* key, const int* in, int nin, char* buf, int cap);
+int spral_ssids_gpu_tune_cache_lookup(const char* path, const char* key, int* out, int nout);
+int spral_ssids_gpu_tune_cache_store(const char* path, const char* key, const int* in, int nin);
 
 /* The contribution update of one front, C -= L21 (L21 D)^T on the lower
  * triangle of the cm x cm block C, on the SIMT kernel of the numeric

@@ -108,6 +108,13 @@ def _declare(L):
     f("spral_ssids_gpu_ldlt_app_factor", I, I, I, P, P, I, P, D, P, I,
       ctypes.POINTER(CpuFactorOptions), P)
     f("spral_ssids_gpu_tc_gemm_f32", I, I, I, I, P, I, P, I, P, I, I, I, I, P)
+    f("spral_ssids_gpu_tc_gemm_f32_bn", I, I, I, I, P, I, P, I, P, I, I, I, I, P, I)
+    f("spral_ssids_gpu_tune_table", I, P, I)
+    f("spral_ssids_gpu_tune_device_key", I, ctypes.c_char_p, I)
+    f("spral_ssids_gpu_tune_parse", I, ctypes.c_char_p, ctypes.c_char_p, I, P, I)
+    f("spral_ssids_gpu_tune_format", I, ctypes.c_char_p, P, I, ctypes.c_char_p, I)
+    f("spral_ssids_gpu_tune_cache_lookup", I, ctypes.c_char_p, ctypes.c_char_p, P, I)
+    f("spral_ssids_gpu_tune_cache_store", I, ctypes.c_char_p, ctypes.c_char_p, P, I)
     f("spral_ssids_gpu_mbar_timeout_probe", I, I)
     f("spral_ssids_gpu_wave_timeout_probe", I, I)
     f("spral_ssids_gpu_inject_alloc_failure", None, I)

@@ -30,6 +30,7 @@
 
 #include "spral_ssids_gpu.h"
 #include "ssids_gpu.cuh"
+#include "tune.h"
 
 namespace ssids300 {
 
@@ -636,25 +637,42 @@ void launch_resid_bwd_err(const int64_t* aptr, const int* acol, const int64_t* a
 void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
-// Crossover of the FP32 contribution update between the SIMT kernel and the
-// tensor cores, measured once per device: the kernels of both are timed
-// (CUDA events, best of three; the tensor path's host-side job tables are
-// built beforehand, as they are when the factorisation is replayed from its
-// graph) on synthetic fronts with contribution blocks of cm rows and cm/2
-// eliminated columns; the threshold is the smallest cm from which the tensor
-// cores are faster for every larger size of the grid.
+// Autotuner, run once per device (or read from the tune cache named by
+// SPRAL_GB300_TUNE_CACHE, see tune.cpp).  It times, with CUDA events (best of
+// five after a warm-up run; the tensor path's host-side job tables are built
+// beforehand, as they are when the factorisation is replayed from its
+// graph), synthetic fronts with contribution blocks of cm rows and
+// max(32, cm / 2) eliminated columns (at least 256 for the tile classes):
+//  * the SIMT contribution kernel against the tensor-core update at its best
+//    tile width: the crossover is the smallest cm of the grid from which the
+//    tensor cores are faster for every larger size of the grid;
+//  * each tile width of the tensor-core kernel (128 x 64, 128 x 128,
+//    128 x 256) at the size classes cm = 256 .. 4096: a launch whose largest
+//    contribution block has at most cm rows takes that class's fastest width.
 // ---------------------------------------------------------------------------
 static std::mutex g_tune_mutex;
-static int g_tuned_min_cm[64];  // 0: not measured yet
 
-static int autotune_tc_min_cm() {
-  int dev = 0;
-  CK(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lock(g_tune_mutex);
-  if (dev >= 0 && dev < 64 && g_tuned_min_cm[dev] > 0) return g_tuned_min_cm[dev];
-  const int grid[] = {64, 96, 128, 192, 256, 384, 512};
-  constexpr int ng = sizeof(grid) / sizeof(grid[0]);
-  const int maxcm = grid[ng - 1], k = maxcm / 2;  // storage for the deepest case
+static std::string tune_device_key(int dev) {
+  cudaDeviceProp pr{};
+  if (cudaGetDeviceProperties(&pr, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return "unknown";
+  }
+  std::string name = pr.name;
+  for (auto& c : name)
+    if (c == ' ' || c == '\t') c = '_';
+  return name + "-sm" + std::to_string(pr.multiProcessorCount) + "-cc" +
+         std::to_string(pr.major) + std::to_string(pr.minor);
+}
+
+static TuneTable measure_tune_table() {
+  const int xgrid[] = {64, 96, 128, 192, 256, 384, 512};
+  constexpr int nx = sizeof(xgrid) / sizeof(xgrid[0]);
+  const int cgrid[] = {256, 512, 1024, 2048, 4096};
+  constexpr int ncls = sizeof(cgrid) / sizeof(cgrid[0]);
+  const int widths[] = {64, 128, 256};
+  constexpr int nw = sizeof(widths) / sizeof(widths[0]);
+  const int maxcm = cgrid[ncls - 1], maxk = 1024;  // storage for the largest case
   cudaStream_t s;
   CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   DevBuf<float> L, LD, C;
@@ -663,9 +681,9 @@ static int autotune_tc_min_cm() {
   FrontDesc<float>* d_fd = nullptr;
   FrontState* d_st = nullptr;
   int* d_status = nullptr;
-  const int ld = ((maxcm + k) + 3) / 4 * 4;
-  L.ensure((size_t)ld * k);
-  LD.ensure((size_t)maxcm * k);
+  const int ld = ((maxcm + maxk) + 3) / 4 * 4;
+  L.ensure((size_t)ld * maxk);
+  LD.ensure((size_t)maxcm * maxk);
   C.ensure((size_t)maxcm * maxcm);
   fr.ensure(1);
   CK(cudaMalloc(&d_fd, sizeof(FrontDesc<float>)));
@@ -682,7 +700,7 @@ static int autotune_tc_min_cm() {
   CK(cudaEventCreate(&e1));
   auto best = [&](auto&& run) {
     float b = 1e30f;
-    for (int r = 0; r < 4; ++r) {  // first run warms up
+    for (int r = 0; r < 6; ++r) {  // first run warms up
       CK(cudaEventRecord(e0, s));
       run();
       CK(cudaEventRecord(e1, s));
@@ -693,10 +711,24 @@ static int autotune_tc_min_cm() {
     }
     return b;
   };
-  bool tc_wins[ng];
   void* blob = nullptr;
-  for (int g = 0; g < ng; ++g) {
-    const int cm = grid[g], kk = std::max(32, cm / 2);
+  // tensor-core time of one (cm, k) front at tile width bn
+  auto time_tc = [&](int cm, int kk, int bn) {
+    std::vector<TcProblem> ps(1);
+    ps[0] = {L.p + kk, ld, LD.p, cm, C.p, cm, cm, cm, kk, &d_st->nelim, 1};
+    scratch.ensure(tc_gemm_scratch_bytes(ps));
+    TcPlan plan;
+    if (tc_gemm_prepare(ps, scratch.p, plan, bn) != 0) throw CudaFail{cudaErrorUnknown, __LINE__};
+    cudaFree(blob);
+    blob = nullptr;
+    CK(cudaMalloc(&blob, plan.blob.size()));
+    CK(cudaMemcpy(blob, plan.blob.data(), plan.blob.size(), cudaMemcpyHostToDevice));
+    return best([&] {
+      if (tc_gemm_launch(plan, blob, d_status, s, kTcChunk) != 0)
+        throw CudaFail{cudaErrorUnknown, __LINE__};
+    });
+  };
+  auto set_front = [&](int cm, int kk) {
     FrontDesc<float> h{};
     h.L = L.p; h.LD = LD.p; h.C = C.p;
     h.m = cm + kk; h.n = kk; h.ld = ld; h.cm = cm; h.ldc = cm;
@@ -705,25 +737,34 @@ static int autotune_tc_min_cm() {
     hs.nelim = kk;
     CK(cudaMemcpyAsync(d_fd, &h, sizeof(h), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(d_st, &hs, sizeof(hs), cudaMemcpyHostToDevice, s));
+  };
+  TuneTable t;
+  // tile width per size class
+  for (int c = 0; c < ncls; ++c) {
+    const int cm = cgrid[c], kk = std::max(256, std::min(cm / 2, maxk));
+    set_front(cm, kk);
+    float bt = 1e30f;
+    int bw = kTuneDefaultBn;
+    for (int w = 0; w < nw; ++w) {
+      const float tt = time_tc(cm, kk, widths[w]);
+      if (tt < bt) { bt = tt; bw = widths[w]; }
+    }
+    t.bucket_m[c] = cm;
+    t.bn[c] = bw;
+  }
+  t.nb = ncls;
+  // SIMT / tensor-core crossover, the tensor cores at the tuned width
+  bool tc_wins[nx];
+  for (int g = 0; g < nx; ++g) {
+    const int cm = xgrid[g], kk = std::max(32, cm / 2);
+    set_front(cm, kk);
     const float t_simt = best([&] { launch_contrib_gemm<float>(d_fd, d_st, fr.p, 1, cm, s); });
-    std::vector<TcProblem> ps(1);
-    ps[0] = {L.p + kk, ld, LD.p, cm, C.p, cm, cm, cm, kk, &d_st->nelim, 1};
-    scratch.ensure(tc_gemm_scratch_bytes(ps));
-    TcPlan plan;
-    if (tc_gemm_prepare(ps, scratch.p, plan) != 0) throw CudaFail{cudaErrorUnknown, __LINE__};
-    cudaFree(blob);
-    blob = nullptr;
-    CK(cudaMalloc(&blob, plan.blob.size()));
-    CK(cudaMemcpy(blob, plan.blob.data(), plan.blob.size(), cudaMemcpyHostToDevice));
-    const float t_tc = best([&] {
-      if (tc_gemm_launch(plan, blob, d_status, s, kTcChunk) != 0)
-        throw CudaFail{cudaErrorUnknown, __LINE__};
-    });
-    tc_wins[g] = t_tc < t_simt;
+    tc_wins[g] = time_tc(cm, kk, tune_bn_for(t, cm)) < t_simt;
   }
   cudaFree(blob);
-  int pick = grid[ng - 1] + 1;
-  for (int g = ng - 1; g >= 0 && tc_wins[g]; --g) pick = grid[g];
+  int pick = xgrid[nx - 1] + 1;
+  for (int g = nx - 1; g >= 0 && tc_wins[g]; --g) pick = xgrid[g];
+  t.tc_min_cm = pick;
   CK(cudaStreamSynchronize(s));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -731,8 +772,39 @@ static int autotune_tc_min_cm() {
   cudaFree(d_st);
   cudaFree(d_status);
   cudaStreamDestroy(s);
-  if (dev >= 0 && dev < 64) g_tuned_min_cm[dev] = pick;
-  return pick;
+  return t;
+}
+
+static TuneTable autotune_device() {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  TuneTable t;
+  if (tune_get(dev, t)) return t;
+  const char* cache = getenv("SPRAL_GB300_TUNE_CACHE");
+  const std::string key = tune_device_key(dev);
+  if (!(cache && *cache && tune_cache_lookup(cache, key, t))) {
+    t = measure_tune_table();
+    if (cache && *cache) (void)tune_cache_store(cache, key, t);  // best effort
+  }
+  tune_set(dev, t);
+  return t;
+}
+
+static int autotune_tc_min_cm() { return autotune_device().tc_min_cm; }
+
+int tc_tile_width(const std::vector<TcProblem>& ps) {
+  if (const char* e = getenv("SPRAL_GB300_TC_BN")) {
+    const int bn = atoi(e);
+    if (tc_tile_width_ok(bn)) return bn;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return kTuneDefaultBn; }
+  TuneTable t;
+  if (!tune_get(dev, t)) return kTuneDefaultBn;
+  int mm = 0;
+  for (auto& p : ps) mm = std::max(mm, std::max(p.M, p.N));
+  return tune_bn_for(t, mm);
 }
 
 template <typename T>
@@ -785,15 +857,52 @@ struct Numeric : NumericBase {
   bool use_wave = true;
   DevBuf<int2> wave_items;
   DevBuf<int> wave_flags, wave_ints;
-  std::vector<int> wave_fwd_off, wave_bwd_off;  // per level, into wave_items (+1 end)
+  DevBuf<T> wave_l21p;  // backward L21^T partial sums of the wavefront pass
+  int wave_nfwd = 0, wave_nbwd = 0;  // items of the forward pass, then of the backward pass
   size_t wave_nflags = 0;
-  WaveLevel wave_level(bool fwd, int l) const {
-    const std::vector<int>& off = fwd ? wave_fwd_off : wave_bwd_off;
+  // optional trace of the wavefront passes (SPRAL_GB300_WAVE_TRACE = path
+  // prefix): per item four stamps (taken, last wait over, finished, SM),
+  // written with the item list after every pass; passes then run without
+  // graphs
+  std::string wave_trace;
+  DevBuf<unsigned long long> wave_trace_buf;
+  WaveLevel wave_pass(bool fwd) {
     WaveLevel w;
-    w.items = wave_items.p + off[l];
-    w.nitems = off[l + 1] - off[l];
-    w.counter = wave_ints.p + 1 + (fwd ? 0 : S->nlev) + l;
+    w.items = wave_items.p + (fwd ? 0 : wave_nfwd);
+    w.nitems = fwd ? wave_nfwd : wave_nbwd;
+    w.counter = wave_ints.p + (fwd ? 1 : 2);
+    w.trace = nullptr;
+    if (!wave_trace.empty()) {
+      wave_trace_buf.ensure(4 * (size_t)(wave_nfwd + wave_nbwd) + 4);
+      w.trace = wave_trace_buf.p + (fwd ? 0 : 4 * (size_t)wave_nfwd);
+    }
     return w;
+  }
+  void dump_wave_trace(cudaStream_t s) {
+    CK(cudaStreamSynchronize(s));
+    const size_t ni = (size_t)wave_nfwd + wave_nbwd;
+    std::vector<int2> items(ni);
+    std::vector<unsigned long long> tr(4 * ni);
+    if (ni) {
+      CK(cudaMemcpy(items.data(), wave_items.p, ni * sizeof(int2), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(tr.data(), wave_trace_buf.p, tr.size() * 8, cudaMemcpyDeviceToHost));
+    }
+    if (FILE* f = fopen((wave_trace + ".items").c_str(), "wb")) {
+      fwrite(items.data(), sizeof(int2), ni, f);
+      fclose(f);
+    }
+    if (FILE* f = fopen((wave_trace + ".trace").c_str(), "wb")) {
+      fwrite(tr.data(), 8, tr.size(), f);
+      fclose(f);
+    }
+    if (FILE* f = fopen((wave_trace + ".meta").c_str(), "w")) {
+      fprintf(f, "%d %d\n", wave_nfwd, wave_nbwd);
+      // per front: level, m, nelim
+      for (int l = 0; l < S->nlev; ++l)
+        for (int fr = S->lvl_start[l]; fr < S->lvl_start[l + 1]; ++fr)
+          fprintf(f, "%d %d %d\n", l, m_[fr], nelim_[fr]);
+      fclose(f);
+    }
   }
   // tensor-core contribution GEMM (FP32 factors only)
   bool use_tc = false;
@@ -1320,6 +1429,8 @@ struct Numeric : NumericBase {
       // 64 x 64 tile for 8 right-hand sides on GB300's FP64 pipe)
       const char* wv = getenv("SPRAL_GB300_SOLVE_WAVE");
       use_wave = wv ? wv[0] != '0' : std::is_same<T, float>::value;
+      const char* wt = getenv("SPRAL_GB300_WAVE_TRACE");
+      if (wt && *wt) wave_trace = wt;
     }
     if (std::is_same<T, float>::value) {
       const char* env = getenv("SPRAL_GB300_TENSOR_CORES");
@@ -1606,40 +1717,72 @@ struct Numeric : NumericBase {
     std::vector<size_t> xoff(nn);
     for (int f = 0; f < nn; ++f) { xoff[f] = xl; xl += (size_t)m_[f] * kSolveRhs; }
     xloc.ensure(xl + 1);
-    std::vector<size_t> flag_off(nn + 1, 0);
-    for (int f = 0; f < nn; ++f) flag_off[f + 1] = flag_off[f] + (nelim_[f] + kSolveBlk - 1) / kSolveBlk;
+    // per front: the pivot blocks' flags, the gathered-chunk counter and the
+    // finished-item counter of the wavefront passes
+    auto nblk_of = [&](int f) { return (nelim_[f] + kSolveBlk - 1) / kSolveBlk; };
+    auto small_of = [&](int f) { return nblk_of(f) <= 1 && m_[f] - nelim_[f] <= kWaveSmallRows; };
+    auto ngat_of = [&](int f) {
+      return small_of(f) ? 0 : (m_[f] + kWaveGatherRows - 1) / kWaveGatherRows;
+    };
+    auto ncon_of = [&](int f) { return (m_[f] - nelim_[f] + kSolveBlk - 1) / kSolveBlk; };
+    auto nch_of = [&](int f) {
+      return small_of(f) ? 0 : (m_[f] - nelim_[f] + kWaveL21Rows - 1) / kWaveL21Rows;
+    };
+    std::vector<size_t> flag_off(nn + 1, 0), l21_off(nn + 1, 0);
+    for (int f = 0; f < nn; ++f) {
+      flag_off[f + 1] = flag_off[f] + 2 * nblk_of(f) + 2;
+      l21_off[f + 1] = l21_off[f] + (size_t)nblk_of(f) * nch_of(f) * kSolveBlk * kSolveRhs;
+    }
+    wave_l21p.ensure(std::max<size_t>(l21_off[nn], 1));
     wave_nflags = flag_off[nn];
     wave_flags.ensure(std::max<size_t>(wave_nflags, 1));
-    wave_ints.ensure(1 + 2 * (size_t)S->nlev);
+    wave_ints.ensure(3);
     {
-      // forward: pivot blocks by block index across the level's nodes, then
-      // the contribution row blocks; backward: pivot blocks from the last
+      // forward: levels from the leaves; per level the gathers and small
+      // fronts, the pivot blocks by block index across the level's fronts,
+      // then the contribution row blocks.  Backward: levels from the root;
+      // the gathers and small fronts, then the pivot blocks from the last.
       std::vector<int2> items;
-      wave_fwd_off.assign(S->nlev + 1, 0);
-      wave_bwd_off.assign(S->nlev + 1, 0);
       for (int l = 0; l < S->nlev; ++l) {
-        wave_fwd_off[l] = (int)items.size();
         const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1];
         int mb = 0;
-        for (int f = f0; f < f1; ++f) mb = std::max(mb, (nelim_[f] + kSolveBlk - 1) / kSolveBlk);
+        for (int f = f0; f < f1; ++f) {
+          if (small_of(f)) {
+            items.push_back(make_int2(f, kWaveSmall));
+            continue;
+          }
+          for (int g = 0; g < ngat_of(f); ++g) items.push_back(make_int2(f, kWaveGather + g));
+          mb = std::max(mb, nblk_of(f));
+        }
         for (int b = 0; b < mb; ++b)
           for (int f = f0; f < f1; ++f)
-            if (b * kSolveBlk < nelim_[f]) items.push_back(make_int2(f, b));
+            if (!small_of(f) && b < nblk_of(f)) items.push_back(make_int2(f, b));
         for (int f = f0; f < f1; ++f)
-          for (int r = nelim_[f], k = 0; r < m_[f]; r += kSolveBlk, ++k)
-            items.push_back(make_int2(f, kWaveContrib + k));
+          if (!small_of(f))
+            for (int k = 0; k < ncon_of(f); ++k) items.push_back(make_int2(f, kWaveContrib + k));
       }
-      wave_fwd_off[S->nlev] = (int)items.size();
-      for (int l = 0; l < S->nlev; ++l) {
-        wave_bwd_off[l] = (int)items.size();
+      wave_nfwd = (int)items.size();
+      for (int l = S->nlev - 1; l >= 0; --l) {
         const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1];
         int mb = 0;
-        for (int f = f0; f < f1; ++f) mb = std::max(mb, (nelim_[f] + kSolveBlk - 1) / kSolveBlk);
+        for (int f = f0; f < f1; ++f) {
+          if (small_of(f)) {
+            items.push_back(make_int2(f, kWaveSmall));
+            continue;
+          }
+          for (int g = 0; g < ngat_of(f); ++g) items.push_back(make_int2(f, kWaveGather + g));
+          mb = std::max(mb, nblk_of(f));
+        }
         for (int b = mb - 1; b >= 0; --b)
           for (int f = f0; f < f1; ++f)
-            if (b * kSolveBlk < nelim_[f]) items.push_back(make_int2(f, b));
+            if (b < nblk_of(f))
+              for (int c = 0; c < nch_of(f); ++c)
+                items.push_back(make_int2(f, kWaveL21 + b * nch_of(f) + c));
+        for (int b = mb - 1; b >= 0; --b)
+          for (int f = f0; f < f1; ++f)
+            if (!small_of(f) && b < nblk_of(f)) items.push_back(make_int2(f, b));
       }
-      wave_bwd_off[S->nlev] = (int)items.size();
+      wave_nbwd = (int)items.size() - wave_nfwd;
       wave_items.ensure(std::max<size_t>(items.size(), 1));
       if (!items.empty())
         CK(cudaMemcpyAsync(wave_items.p, items.data(), items.size() * sizeof(int2),
@@ -1650,7 +1793,13 @@ struct Numeric : NumericBase {
       const int node = S->node_of[f];
       SolveNode<T>& q = sn[f];
       q.flag = wave_flags.p + flag_off[f];
-      q.pad_ = 0;
+      q.l21p = wave_l21p.p + l21_off[f];
+      q.nblk = nblk_of(f);
+      q.ngat = ngat_of(f);
+      q.nch = nch_of(f);
+      q.nitf = small_of(f) ? 1 : q.ngat + q.nblk + ncon_of(f);
+      q.nitb = small_of(f) ? 1 : q.ngat + q.nblk * (1 + q.nch);
+      q.parent = S->parent[node] >= 0 ? S->front_of[S->parent[node]] : -1;
       q.L = hfd[f].L; q.D = hfd[f].D; q.perm = hfd[f].perm; q.opos = hfd[f].opos;
       q.rows = S->d_rlist + S->rptr[node];
       q.rdir = S->d_rdir + S->rdir_ptr_h[node];
@@ -1683,9 +1832,8 @@ struct Numeric : NumericBase {
     mix((uint64_t)(uintptr_t)d_sn); mix((uint64_t)(uintptr_t)d_children);
     mix((uint64_t)(uintptr_t)xloc.p);
     mix((uint64_t)(uintptr_t)wave_items.p); mix((uint64_t)(uintptr_t)wave_flags.p);
-    mix((uint64_t)(uintptr_t)wave_ints.p);
-    for (int v : wave_fwd_off) mix((uint64_t)v);
-    for (int v : wave_bwd_off) mix((uint64_t)v);
+    mix((uint64_t)(uintptr_t)wave_ints.p); mix((uint64_t)(uintptr_t)wave_l21p.p);
+    mix((uint64_t)wave_nfwd); mix((uint64_t)wave_nbwd);
     if (h != solve_sig) drop_graphs();
     solve_sig = h;
     solve_ready = true;
@@ -1703,17 +1851,17 @@ struct Numeric : NumericBase {
     if (fwd) {
       if (use_wave) {
         CK(cudaMemsetAsync(wave_flags.p, 0, std::max<size_t>(wave_nflags, 1) * sizeof(int), s));
-        CK(cudaMemsetAsync(wave_ints.p + 1, 0, S->nlev * sizeof(int), s));
-      }
-      for (int l = 0; l < S->nlev; ++l) {
-        const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
-        const int* fr = S->d_fronts + f0;
-        pmark(tm(), kPhFwdGather, s);
-        launch_fwd_gather<T>(d_sn, fr, nf, d_children, S->d_pairs, xp, ldx, q, lvl_max_m[l], s);
-        if (use_wave) {
-          pmark(tm(), kPhFwdUpdate, s);
-          launch_fwd_wave<T>(d_sn, wave_level(true, l), q, xp, ldx, job == 5, wstatus, s);
-        } else {
+        CK(cudaMemsetAsync(wave_ints.p + 1, 0, sizeof(int), s));
+        pmark(tm(), kPhFwdUpdate, s);
+        launch_fwd_tree<T>(d_sn, d_children, S->d_pairs, wave_pass(true), q, xp, ldx, job == 5,
+                           wstatus, s);
+      } else {
+        for (int l = 0; l < S->nlev; ++l) {
+          const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
+          const int* fr = S->d_fronts + f0;
+          pmark(tm(), kPhFwdGather, s);
+          launch_fwd_gather<T>(d_sn, fr, nf, d_children, S->d_pairs, xp, ldx, q, lvl_max_m[l],
+                               s);
           launch_fwd_steps<T>(d_sn, fr, nf, lvl_max_nelim[l], lvl_max_m[l], q, xp, ldx, job == 5,
                               s, tm());
         }
@@ -1722,15 +1870,12 @@ struct Numeric : NumericBase {
     if (diag || bwd) {
       if (use_wave && bwd) {
         CK(cudaMemsetAsync(wave_flags.p, 0, std::max<size_t>(wave_nflags, 1) * sizeof(int), s));
-        CK(cudaMemsetAsync(wave_ints.p + 1 + S->nlev, 0, S->nlev * sizeof(int), s));
-      }
-      for (int l = S->nlev - 1; l >= 0; --l) {
-        const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
-        if (use_wave && bwd) {
-          pmark(tm(), kPhBwdUpdate, s);
-          launch_bwd_wave<T>(d_sn, S->d_fronts + f0, nf, wave_level(false, l), xp, ldx, q,
-                             lvl_max_m[l], lvl_max_nelim[l], diag_mode, wstatus, s);
-        } else {
+        CK(cudaMemsetAsync(wave_ints.p + 2, 0, sizeof(int), s));
+        pmark(tm(), kPhBwdUpdate, s);
+        launch_bwd_tree<T>(d_sn, wave_pass(false), xp, ldx, q, diag_mode, wstatus, s);
+      } else {
+        for (int l = S->nlev - 1; l >= 0; --l) {
+          const int f0 = S->lvl_start[l], nf = S->lvl_start[l + 1] - f0;
           launch_bwd<T>(d_sn, S->d_fronts + f0, nf, xp, ldx, q, lvl_max_m[l], lvl_max_nelim[l],
                         diag_mode, bwd, s, tm());
         }
@@ -1740,6 +1885,11 @@ struct Numeric : NumericBase {
 
   // the same pass through a captured graph (captured on first use)
   void run_solve(int job, int q, double* xp, int ldx, cudaStream_t s) {
+    if (!wave_trace.empty()) {
+      enqueue_solve(job, q, xp, ldx, s);
+      dump_wave_trace(s);
+      return;
+    }
     if (profile || !use_graphs) { enqueue_solve(job, q, xp, ldx, s); return; }
     for (auto& g : sgraphs)
       if (g.job == job && g.q == q && g.x == xp && g.ldx == ldx && g.sig == solve_sig) {
@@ -2348,6 +2498,33 @@ int spral_ssids_gpu_tc_crossover(void) {
   } catch (...) {
     return -51;
   }
+}
+
+/* The autotuner's table for the current device (measured on first use, or
+ * read from the tune cache): out = [tc_min_cm, nb, m_0, bn_0, ...].  Returns
+ * the number of ints written, -1 if nout is too small, -51 on a CUDA error. */
+int spral_ssids_gpu_tune_table(int* out, int nout) {
+  try {
+    const ssids300::TuneTable t = ssids300::autotune_device();
+    const int need = 2 + 2 * t.nb;
+    if (!out || nout < need) return -1;
+    out[0] = t.tc_min_cm;
+    out[1] = t.nb;
+    for (int i = 0; i < t.nb; ++i) { out[2 + 2 * i] = t.bucket_m[i]; out[3 + 2 * i] = t.bn[i]; }
+    return need;
+  } catch (...) {
+    return -51;
+  }
+}
+
+/* The current device's key in the tune cache.  Returns its length, or -1. */
+int spral_ssids_gpu_tune_device_key(char* buf, int cap) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return -1; }
+  const std::string k = ssids300::tune_device_key(dev);
+  if (!buf || cap <= (int)k.size()) return -1;
+  std::snprintf(buf, (size_t)cap, "%s", k.c_str());
+  return (int)k.size();
 }
 
 /* The contribution update of one front on the SIMT kernel, on the caller's

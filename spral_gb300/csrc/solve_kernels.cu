@@ -1,5 +1,5 @@
-// Forward, diagonal and backward solves over the assembly tree, level by
-// level, many right-hand sides at once (the reference GPU path solves one
+// Forward, diagonal and backward solves over the assembly tree, many
+// right-hand sides at once (the reference GPU path solves one
 // right-hand side per call, src/ssids/gpu/subtree.f90:570-579).
 //
 // Semantics follow the CPU subtree solves (src/ssids/cpu/NumericSubtree.hxx:
@@ -11,16 +11,26 @@
 // never update the same entry: each node gathers b for its own pivots plus
 // its children's local vectors (fixed order, no atomics), solves, and leaves
 // rows [nelim, m) of its local vector for its parent.  The triangular solves
-// are blocked by 64 rows, one kernel per block step: every CTA of the step
-// stages the step's diagonal block in shared memory (cp.async) and solves it
-// itself, each right-hand side in its own warp (values in registers, the
-// pivot row broadcast by shuffles), then takes its share of the block's
-// update (rows below the block in the forward pass, columns left of it in
-// the backward pass).  No CTA waits for another and the solution is written
-// to the output vector by CTA 0 of the step, so a level needs no scatter
-// launch.  Arithmetic is in the factor precision T; the number of
-// right-hand sides per pass NR is a template parameter so that no work is
-// spent on absent columns.
+// are blocked by 64 rows.  Two schedules:
+//  * wavefront passes (FP32 factors by default): one persistent launch per
+//    pass over the whole tree; CTAs take work items (gathers, pivot blocks,
+//    contribution row blocks, or a small front whole) in a fixed order from
+//    an atomic counter and wait, with bounded polls, on completion flags and
+//    counters of earlier items only, so fronts of different levels overlap
+//    and no level boundary drains the GPU (k_fwd_tree, k_bwd_tree);
+//  * block steps (FP64 factors by default): per level a gather launch, then
+//    one kernel per block step: every CTA of the step stages the step's
+//    diagonal block in shared memory (cp.async) and solves it itself, each
+//    right-hand side in its own warp (values in registers, the pivot row
+//    broadcast by shuffles), then takes its share of the block's update
+//    (rows below the block in the forward pass, columns left of it in the
+//    backward pass).  No CTA waits for another and the solution is written
+//    to the output vector by CTA 0 of the step, so a level needs no scatter
+//    launch.
+// Arithmetic is in the factor precision T; the number of right-hand sides
+// per pass NR is a template parameter so that no work is spent on absent
+// columns.  Every sum runs in a fixed order, so results do not depend on
+// which CTA takes which item.
 #include <mutex>
 #include <type_traits>
 
@@ -39,10 +49,13 @@ constexpr int SB = kSolveBlk;
 // function of b and the children's local vectors, so any number of CTAs can
 // gather one node; the additions run in child order, so the sums do not
 // depend on the launch shape.
-template <typename T>
+// With CG the children's values are read from L2 (__ldcg): in a wavefront
+// pass they were written by other CTAs of the same launch.
+template <typename T, bool CG = false>
 __device__ __forceinline__ T gather_value(const SolveNode<T>& sn, const SolveNode<T>* sns,
                                           const int* children, const int2* pairs,
                                           const double* x, int ldx, int q, int pos) {
+  auto ld = [](const T* p) { return CG ? __ldcg(p) : *p; };
   T v = T(0);
   int P;
   if (pos < sn.ncol) {
@@ -54,7 +67,7 @@ __device__ __forceinline__ T gather_value(const SolveNode<T>& sn, const SolveNod
       const SolveNode<T>& cn = sns[children[ci]];
       const int nd = cn.n - cn.nelim;
       if (k >= cn.doff && k < cn.doff + nd)
-        return cn.xloc[(int64_t)q * cn.m + cn.nelim + (k - cn.doff)];
+        return ld(&cn.xloc[(int64_t)q * cn.m + cn.nelim + (k - cn.doff)]);
     }
     return v;
   } else {
@@ -64,7 +77,7 @@ __device__ __forceinline__ T gather_value(const SolveNode<T>& sn, const SolveNod
   for (int k = sn.gp[P]; k < k1; ++k) {
     const int2 pr = pairs[k];
     const SolveNode<T>& cn = sns[pr.x];
-    v += cn.xloc[(int64_t)q * cn.m + cn.n + pr.y];
+    v += ld(&cn.xloc[(int64_t)q * cn.m + cn.n + pr.y]);
   }
   return v;
 }
@@ -370,6 +383,36 @@ __global__ void k_fwd_scatter(const SolveNode<T>* sns, const int* nodes, double*
 // ---- backward ----
 // diag_mode: 0 none, 1 apply D^{-1} (1x1 and 2x2), 2 apply sqrt(D^{-1}) (the
 // posdef backward solve with L_chol^T = D^(1/2) L^T)
+// Value of local position i for right-hand side q at the start of the
+// backward pass: x at the position's pivot (for i < nelim times D^{-1}
+// with 2x2 blocks, or sqrt(D^{-1}) for diag_mode 2).  With CG, x is read
+// from L2 (ancestors' values written by other CTAs of the same launch).
+template <bool CG, typename T>
+__device__ __forceinline__ double bwd_gather_value(const SolveNode<T>& sn, const double* x,
+                                                   int ldx, int diag_mode, int q, int i) {
+  auto ld = [](const double* p) { return CG ? __ldcg(p) : *p; };
+  const int src = (i < sn.n) ? sn.perm[i] : sn.rows[sn.ncol + i - sn.n];
+  double v = ld(&x[(int64_t)q * ldx + src]);
+  if (diag_mode == 2 && i < sn.nelim) {
+    v *= sqrt(sn.D[2 * i]);
+  } else if (diag_mode == 1 && i < sn.nelim) {
+    const double di = sn.D[2 * i];
+    if (isinf(di)) {
+      // second half of a 2x2: d21*x1 + d22*x2
+      const double d21 = sn.D[2 * (i - 1) + 1], d22 = sn.D[2 * i + 1];
+      const double x1 = ld(&x[(int64_t)q * ldx + sn.perm[i - 1]]);
+      v = d21 * x1 + d22 * v;
+    } else if (i + 1 < sn.nelim && isinf(sn.D[2 * i + 2])) {
+      const double d21 = sn.D[2 * i + 1];
+      const double x2 = ld(&x[(int64_t)q * ldx + sn.perm[i + 1]]);
+      v = di * v + d21 * x2;
+    } else {
+      v = di * v;
+    }
+  }
+  return v;
+}
+
 template <typename T>
 __global__ void k_bwd_gather(const SolveNode<T>* sns, const int* nodes, const double* x, int ldx,
                              int nrhs, int diag_mode, bool do_bwd) {
@@ -380,26 +423,7 @@ __global__ void k_bwd_gather(const SolveNode<T>* sns, const int* nodes, const do
   const int tot = mm * nrhs;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
     const int i = e % mm, q = e / mm;
-    const int src = (i < sn.n) ? sn.perm[i] : sn.rows[sn.ncol + i - sn.n];
-    double v = x[(int64_t)q * ldx + src];
-    if (diag_mode == 2 && i < sn.nelim) {
-      v *= sqrt(sn.D[2 * i]);
-    } else if (diag_mode == 1 && i < sn.nelim) {
-      const double di = sn.D[2 * i];
-      if (isinf(di)) {
-        // second half of a 2x2: d21*x1 + d22*x2
-        const double d21 = sn.D[2 * (i - 1) + 1], d22 = sn.D[2 * i + 1];
-        const double x1 = x[(int64_t)q * ldx + sn.perm[i - 1]];
-        v = d21 * x1 + d22 * v;
-      } else if (i + 1 < sn.nelim && isinf(sn.D[2 * i + 2])) {
-        const double d21 = sn.D[2 * i + 1];
-        const double x2 = x[(int64_t)q * ldx + sn.perm[i + 1]];
-        v = di * v + d21 * x2;
-      } else {
-        v = di * v;
-      }
-    }
-    sn.xloc[(int64_t)q * sn.m + i] = (T)v;
+    sn.xloc[(int64_t)q * sn.m + i] = (T)bwd_gather_value<false>(sn, x, ldx, diag_mode, q, i);
   }
 }
 
@@ -527,7 +551,7 @@ __global__ void __launch_bounds__(kSolveThreads)
   }
 }
 
-// ---- wavefront solves (one persistent launch per level) ----
+// ---- wavefront solves (one persistent launch per pass, whole tree) ----
 // try rounds of a flag wait before it gives up (each round sleeps briefly);
 // no legitimate wait comes close
 constexpr long long kWaveSpinLimit = 1LL << 22;
@@ -540,12 +564,14 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-// every thread: wait until *flag is set by the CTA that owns that block
-// (thread 0 polls); false once the wait, or another CTA's wait, gave up
-__device__ __forceinline__ bool wave_wait(const int* flag, int* status, int* s_fail) {
+// every thread: wait until *ctr >= target, the counter being advanced by
+// other CTAs (thread 0 polls); false once the wait, or another CTA's wait,
+// gave up
+__device__ __forceinline__ bool wave_wait_count(const int* ctr, int target, int* status,
+                                                int* s_fail) {
   if (threadIdx.x == 0) {
     bool ok = true;
-    for (long long it = 0; ld_acquire(flag) == 0; ++it) {
+    for (long long it = 0; ld_acquire(ctr) < target; ++it) {
       if (it >= kWaveSpinLimit || *(volatile int*)status != 0) { ok = false; break; }
       __nanosleep(20);
     }
@@ -554,6 +580,20 @@ __device__ __forceinline__ bool wave_wait(const int* flag, int* status, int* s_f
   }
   __syncthreads();
   return *s_fail == 0;
+}
+// completion flag of one pivot block
+__device__ __forceinline__ bool wave_wait(const int* flag, int* status, int* s_fail) {
+  return wave_wait_count(flag, 1, status, s_fail);
+}
+// after every thread of the CTA has written its part of an item: publish
+// (all writes before the counter advances, as seen by any CTA)
+__device__ __forceinline__ void wave_signal(int* ctr_a, int* ctr_b) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (ctr_a) atomicAdd(ctr_a, 1);
+    if (ctr_b) atomicAdd(ctr_b, 1);
+  }
 }
 
 // Failure-detection probe: one CTA waits on a completion flag that no
@@ -571,7 +611,24 @@ __global__ void k_wave_timeout_probe(const int* flag, long long rounds, int* sta
   __syncthreads();
 }
 
-// the next item of the level for this CTA (kept in shared memory)
+__device__ __forceinline__ unsigned long long global_timer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// trace stamp k of item it (thread 0; no-op without a trace buffer)
+__device__ __forceinline__ void wave_stamp(const WaveLevel& wl, int it, int k) {
+  if (wl.trace && threadIdx.x == 0) {
+    wl.trace[4 * (size_t)it + k] = global_timer();
+    if (k == 0) {
+      unsigned sm;
+      asm volatile("mov.u32 %0, %%smid;" : "=r"(sm));
+      wl.trace[4 * (size_t)it + 3] = sm;
+    }
+  }
+}
+
+// the next item of the pass for this CTA (kept in shared memory)
 __device__ __forceinline__ int wave_next(const WaveLevel& wl, int* s_item) {
   __syncthreads();  // every thread is done with the previous item
   if (threadIdx.x == 0) *s_item = atomicAdd(wl.counter, 1);
@@ -579,169 +636,359 @@ __device__ __forceinline__ int wave_next(const WaveLevel& wl, int* s_item) {
   return *s_item;
 }
 
-// Forward wave: a pivot block b takes x_b -= sum_{j < b} L(b, j) y_j, block
-// by block as the flags of blocks j arrive (thread (r, cq): row r, columns
-// [16 cq, 16 cq + 16) of each 64-column block), adds the four column
-// quarters in shared memory, solves its unit lower diagonal block in
-// registers (warp per right-hand side), writes y to the local vector and to
-// x, and sets its flag.  A contribution row block takes the whole
-// L21 y product the same way.
+template <typename T>
+__device__ __forceinline__ int* wave_l21done(const SolveNode<T>& sn, int b) {
+  return sn.flag + sn.nblk + b;
+}
+template <typename T>
+__device__ __forceinline__ int* wave_gathered(const SolveNode<T>& sn) {
+  return sn.flag + 2 * sn.nblk;
+}
+template <typename T>
+__device__ __forceinline__ int* wave_finished(const SolveNode<T>& sn) {
+  return sn.flag + 2 * sn.nblk + 1;
+}
+
+// Forward gather of rows [r0, r1) of a front's local vector, one row per
+// thread with every right-hand side (the row's index lookups once, its
+// children's values, from L2, all in flight together).  The additions run
+// in the same order as gather_value's.
 template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveThreads)
-    k_fwd_wave(const SolveNode<T>* sns, WaveLevel wl, int nrhs, double* x, int ldx,
-               bool scale_sqrt, int* status) {
-  extern __shared__ __align__(16) unsigned char solve_smem[];
-  T* Lb = reinterpret_cast<T*>(solve_smem);
-  T* yb = Lb + SB * LDB;
-  T* red = yb + SB * NR;
-  __shared__ int s_item, s_fail;
-  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
-  const int tid = threadIdx.x, r = tid % SB, cq = tid / SB;
-  const int warp = tid >> 5, lane = tid & 31;
-  for (;;) {
-    const int it = wave_next(wl, &s_item);
-    if (it >= wl.nitems) break;
-    const int2 w = wl.items[it];
-    const SolveNode<T>& sn = sns[w.x];
-    const int m = sn.m, nelim = sn.nelim;
-    const bool piv = w.y < kWaveContrib;
-    const int r0 = piv ? w.y * SB : nelim + (w.y - kWaveContrib) * SB;
-    const int rows = min(SB, (piv ? nelim : m) - r0);
-    const int ncb = piv ? w.y : (nelim + SB - 1) / SB;
-    if (piv) prefetch_diag_block(sn, r0, rows, Lb);
-    T acc[NR];
+__device__ __forceinline__ void fwd_gather_rows(const SolveNode<T>& sn, const SolveNode<T>* sns,
+                                                const int* children, const int2* pairs,
+                                                const double* x, int ldx, int nrhs, int r0,
+                                                int r1) {
+  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+    const int pos = (i < sn.n) ? sn.opos[i] : i;
+    T v[NR];
 #pragma unroll
-    for (int q = 0; q < NR; ++q) acc[q] = T(0);
-    bool ok = true;
-    for (int j = 0; j < ncb && ok; ++j) {
-      const int c0 = j * SB, jb = min(SB, nelim - c0);
-      // the tile of L does not depend on block j's result: its loads are
-      // in flight while the flag is awaited
-      T lv[16];
-      {
-        const T* Lp = sn.L + (int64_t)(c0 + cq * 16) * sn.ld + r0 + r;
+    for (int q = 0; q < NR; ++q) v[q] = T(0);
+    int P = -1;
+    if (pos < sn.ncol) {
 #pragma unroll
-        for (int k = 0; k < 16; ++k)
-          lv[k] = (r < rows && cq * 16 + k < jb) ? Lp[(int64_t)k * sn.ld] : T(0);
-      }
-      ok = wave_wait(&sn.flag[j], status, &s_fail);
-      if (!ok) break;
-      for (int e = tid; e < SB * NR; e += kSolveThreads) {
-        const int c = e % SB, q = e / SB;
-        // another CTA wrote these values: read them from L2, past this SM's L1
-        yb[c * NR + q] = (c < jb && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + c0 + c]) : T(0);
-      }
-      __syncthreads();
+      for (int q = 0; q < NR; ++q)
+        if (q < nrhs) v[q] = (T)x[(int64_t)q * ldx + sn.sptr0 + pos];
+      P = pos;
+    } else if (pos < sn.ncol + sn.ndelay_in) {
+      const int k = pos - sn.ncol;
+      for (int ci = sn.child_beg; ci < sn.child_end; ++ci) {
+        const SolveNode<T>& cn = sns[children[ci]];
+        const int nd = cn.n - cn.nelim;
+        if (k >= cn.doff && k < cn.doff + nd) {
+          const T* src = cn.xloc + cn.nelim + (k - cn.doff);
 #pragma unroll
-      for (int k = 0; k < 16; ++k)
-#pragma unroll
-        for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(cq * 16 + k) * NR + q];
-      __syncthreads();
-    }
-    if (!ok) {
-      if (piv) cp_async_wait_all();
-      continue;
-    }
-#pragma unroll
-    for (int q = 0; q < NR; ++q) red[(cq * NR + q) * SB + r] = acc[q];
-    __syncthreads();
-    if (piv) {
-      T xr[R][2];
-#pragma unroll
-      for (int rr = 0; rr < R; ++rr) {
-        const int q = warp + rr * kSolveWarps;
-#pragma unroll
-        for (int g = 0; g < 2; ++g) {
-          const int row = lane + 32 * g;
-          T v = T(0);
-          if (q < nrhs && q < NR && row < rows)
-            v = sn.xloc[(int64_t)q * m + r0 + row] -
-                (red[q * SB + row] + red[(NR + q) * SB + row] + red[(2 * NR + q) * SB + row] +
-                 red[(3 * NR + q) * SB + row]);
-          xr[rr][g] = v;
+          for (int q = 0; q < NR; ++q)
+            if (q < nrhs) v[q] = __ldcg(src + (int64_t)q * cn.m);
+          break;
         }
-      }
-      cp_async_wait_all();
-      __syncthreads();
-      if (warp < nrhs) solve_in_regs<T, R, true>(rows, Lb, xr);
-#pragma unroll
-      for (int rr = 0; rr < R; ++rr) {
-        const int q = warp + rr * kSolveWarps;
-#pragma unroll
-        for (int g = 0; g < 2; ++g) {
-          const int row = lane + 32 * g;
-          if (q < nrhs && q < NR && row < rows) {
-            sn.xloc[(int64_t)q * m + r0 + row] = xr[rr][g];
-            double v = (double)xr[rr][g];
-            if (scale_sqrt) v *= sqrt(sn.D[2 * (r0 + row)]);
-            x[(int64_t)q * ldx + sn.perm[r0 + row]] = v;
-          }
-        }
-      }
-      __syncthreads();
-      if (tid == 0) {
-        __threadfence();
-        st_release(&sn.flag[w.y], 1);
       }
     } else {
-      for (int e = tid; e < SB * NR; e += kSolveThreads) {
-        const int row = e % SB, q = e / SB;
-        if (row < rows && q < nrhs)
-          sn.xloc[(int64_t)q * m + r0 + row] -=
-              red[q * SB + row] + red[(NR + q) * SB + row] + red[(2 * NR + q) * SB + row] +
-              red[(3 * NR + q) * SB + row];
+      P = pos - sn.ndelay_in;
+    }
+    if (P >= 0) {
+      const int k1 = sn.gp[P + 1];
+      for (int k = sn.gp[P]; k < k1; ++k) {
+        const int2 pr = pairs[k];
+        const SolveNode<T>& cn = sns[pr.x];
+        const T* src = cn.xloc + cn.n + pr.y;
+#pragma unroll
+        for (int q = 0; q < NR; ++q)
+          if (q < nrhs) v[q] += __ldcg(src + (int64_t)q * cn.m);
       }
     }
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+      if (q < nrhs) sn.xloc[(int64_t)q * sn.m + i] = v[q];
   }
 }
 
-// Backward wave (after k_bwd_l21 has subtracted L21^T x of the contribution
-// rows from every eliminated entry): a pivot block b takes
-// x_b -= sum_{j > b} L(j, b)^T y_j as the flags of the pivot blocks j
-// arrive (thread (c, rq): column c, rows [16 rq, 16 rq + 16) of each
-// 64-row tile), adds the four row quarters, solves L_bb^T in registers,
-// writes y to the local vector and to x, and sets its flag.
+// Backward gather of rows [r0, r1), one row per thread (x from L2)
+template <typename T, int NR>
+__device__ __forceinline__ void bwd_gather_rows(const SolveNode<T>& sn, const double* x, int ldx,
+                                                int nrhs, int diag_mode, int r0, int r1) {
+  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < NR; ++q)
+      if (q < nrhs)
+        sn.xloc[(int64_t)q * sn.m + i] = (T)bwd_gather_value<true>(sn, x, ldx, diag_mode, q, i);
+  }
+}
+
+// Forward block item.  A pivot block b takes x_b -= sum_{j < b} L(b, j) y_j,
+// block by block as the flags of blocks j arrive (thread (r, cq): row r,
+// columns [16 cq, 16 cq + 16) of each 64-column block), adds the four column
+// quarters in shared memory, solves its unit lower diagonal block in
+// registers (warp per right-hand side), writes y to the local vector and to
+// x, and sets its flag.  A contribution row block takes the whole L21 y
+// product the same way.  False if a wait gave up.
+template <typename T, int NR>
+__device__ bool fwd_block(const SolveNode<T>& sn, int code, int nrhs, double* x, int ldx,
+                          bool scale_sqrt, int* status, T* Lb, T* yb, T* red, int* s_fail,
+                          const WaveLevel& wl, int it) {
+  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
+  const int tid = threadIdx.x, r = tid % SB, cq = tid / SB;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int m = sn.m, nelim = sn.nelim;
+  const bool piv = code < kWaveContrib;
+  const int r0 = piv ? code * SB : nelim + (code - kWaveContrib) * SB;
+  const int rows = min(SB, (piv ? nelim : m) - r0);
+  const int ncb = piv ? code : sn.nblk;
+  T own[R][2];  // a pivot block's gathered values, final before any wait below
+  if (piv) {
+    prefetch_diag_block(sn, r0, rows, Lb);
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+      const int q = warp + rr * kSolveWarps;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int row = lane + 32 * g;
+        own[rr][g] = (q < nrhs && q < NR && row < rows) ? __ldcg(&sn.xloc[(int64_t)q * m + r0 + row])
+                                                        : T(0);
+      }
+    }
+  }
+  T acc[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) acc[q] = T(0);
+  bool ok = true;
+  for (int j = 0; j < ncb && ok; ++j) {
+    const int c0 = j * SB, jb = min(SB, nelim - c0);
+    // the tile of L does not depend on block j's result: its loads are
+    // in flight while the flag is awaited
+    T lv[16];
+    {
+      const T* Lp = sn.L + (int64_t)(c0 + cq * 16) * sn.ld + r0 + r;
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        lv[k] = (r < rows && cq * 16 + k < jb) ? Lp[(int64_t)k * sn.ld] : T(0);
+    }
+    ok = wave_wait(&sn.flag[j], status, s_fail);
+    if (!ok) break;
+    for (int e = tid; e < SB * NR; e += kSolveThreads) {
+      const int c = e % SB, q = e / SB;
+      // another CTA wrote these values: read them from L2, past this SM's L1
+      yb[c * NR + q] = (c < jb && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + c0 + c]) : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+#pragma unroll
+      for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(cq * 16 + k) * NR + q];
+    __syncthreads();
+  }
+  if (!ok) {
+    if (piv) cp_async_wait_all();
+    return false;
+  }
+  wave_stamp(wl, it, 1);
+#pragma unroll
+  for (int q = 0; q < NR; ++q) red[(cq * NR + q) * SB + r] = acc[q];
+  __syncthreads();
+  if (piv) {
+    T xr[R][2];
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+      const int q = warp + rr * kSolveWarps;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int row = lane + 32 * g;
+        T v = T(0);
+        if (q < nrhs && q < NR && row < rows)
+          v = own[rr][g] - (red[q * SB + row] + red[(NR + q) * SB + row] +
+                            red[(2 * NR + q) * SB + row] + red[(3 * NR + q) * SB + row]);
+        xr[rr][g] = v;
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (warp < nrhs) solve_in_regs<T, R, true>(rows, Lb, xr);
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+      const int q = warp + rr * kSolveWarps;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int row = lane + 32 * g;
+        if (q < nrhs && q < NR && row < rows) {
+          sn.xloc[(int64_t)q * m + r0 + row] = xr[rr][g];
+          double v = (double)xr[rr][g];
+          if (scale_sqrt) v *= sqrt(sn.D[2 * (r0 + row)]);
+          x[(int64_t)q * ldx + sn.perm[r0 + row]] = v;
+        }
+      }
+    }
+    __syncthreads();
+    // the release orders every thread's writes above (ordered before it by
+    // the barrier) before the flag, for any CTA that acquires the flag
+    if (tid == 0) st_release(&sn.flag[code], 1);
+  } else {
+    for (int e = tid; e < SB * NR; e += kSolveThreads) {
+      const int row = e % SB, q = e / SB;
+      if (row < rows && q < nrhs) {
+        T* p = &sn.xloc[(int64_t)q * m + r0 + row];
+        *p = __ldcg(p) - (red[q * SB + row] + red[(NR + q) * SB + row] +
+                          red[(2 * NR + q) * SB + row] + red[(3 * NR + q) * SB + row]);
+      }
+    }
+  }
+  return true;
+}
+
+// Forward pass over the whole tree (item list and waits: see WaveLevel).
 template <typename T, int NR>
 __global__ void __launch_bounds__(kSolveThreads)
-    k_bwd_wave(const SolveNode<T>* sns, WaveLevel wl, int nrhs, double* x, int ldx,
-               int* status) {
+    k_fwd_tree(const SolveNode<T>* sns, const int* children, const int2* pairs, WaveLevel wl,
+               int nrhs, double* x, int ldx, bool scale_sqrt, int* status) {
   extern __shared__ __align__(16) unsigned char solve_smem[];
   T* Lb = reinterpret_cast<T*>(solve_smem);
   T* yb = Lb + SB * LDB;
   T* red = yb + SB * NR;
   __shared__ int s_item, s_fail;
-  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
-  const int tid = threadIdx.x, c = tid % SB, rq = tid / SB;
-  const int warp = tid >> 5, lane = tid & 31;
   for (;;) {
     const int it = wave_next(wl, &s_item);
     if (it >= wl.nitems) break;
+    wave_stamp(wl, it, 0);
     const int2 w = wl.items[it];
     const SolveNode<T>& sn = sns[w.x];
-    const int m = sn.m, nelim = sn.nelim;
-    const int c0 = w.y * SB, jb = min(SB, nelim - c0);
-    const int npb = (nelim + SB - 1) / SB;
-    prefetch_diag_block(sn, c0, jb, Lb);
-    T acc[NR];
-#pragma unroll
-    for (int q = 0; q < NR; ++q) acc[q] = T(0);
-    // the pivot blocks npb-1 .. b+1, as their flags arrive (the contribution
-    // rows' L21^T x was subtracted by k_bwd_l21 before this launch)
+    const int code = w.y;
     bool ok = true;
-    for (int j = npb - 1; j > w.y && ok; --j) {
-      const int R0 = j * SB, nr = min(SB, nelim - R0);
+    if (code >= kWaveGather) {
+      // the children's contribution rows (and delayed entries) are final
+      // once every item of theirs has finished
+      for (int ci = sn.child_beg; ci < sn.child_end && ok; ++ci) {
+        const SolveNode<T>& cn = sns[children[ci]];
+        ok = wave_wait_count(wave_finished(cn), cn.nitf, status, &s_fail);
+      }
+      if (!ok) continue;
+      wave_stamp(wl, it, 1);
+      if (code == kWaveSmall) {
+        fwd_gather_rows<T, NR>(sn, sns, children, pairs, x, ldx, nrhs, 0, sn.m);
+        __syncthreads();
+        if (sn.nelim > 0)
+          ok = fwd_block<T, NR>(sn, 0, nrhs, x, ldx, scale_sqrt, status, Lb, yb, red, &s_fail, wl,
+                               it);
+        for (int k = 0; ok && sn.nelim + k * SB < sn.m; ++k)
+          ok = fwd_block<T, NR>(sn, kWaveContrib + k, nrhs, x, ldx, scale_sqrt, status, Lb, yb,
+                                red, &s_fail, wl, it);
+        if (ok) wave_signal(wave_finished(sn), nullptr);
+      } else {
+        const int g0 = (code - kWaveGather) * kWaveGatherRows;
+        fwd_gather_rows<T, NR>(sn, sns, children, pairs, x, ldx, nrhs, g0,
+                        min(sn.m, g0 + kWaveGatherRows));
+        wave_signal(wave_gathered(sn), wave_finished(sn));
+      }
+    } else {
+      ok = wave_wait_count(wave_gathered(sn), sn.ngat, status, &s_fail);
+      if (ok)
+        ok = fwd_block<T, NR>(sn, code, nrhs, x, ldx, scale_sqrt, status, Lb, yb, red, &s_fail,
+                              wl, it);
+      if (ok) wave_signal(wave_finished(sn), nullptr);
+    }
+    wave_stamp(wl, it, 2);
+  }
+}
+
+// Backward L21^T partial item t = b nch + c: for pivot block b, the
+// products sum_i L(i, 64 b + col) x_i over the contribution rows
+// [nelim + 256 c, ...) of the front (thread (col, rq): rows
+// [64 rq, 64 rq + 64) of the chunk), the four row groups added in order,
+// into l21p[b][c][col][q].  The rows' values (gathered, from L2) are staged
+// in xs (256 NR values).
+template <typename T, int NR>
+__device__ void bwd_l21_item(const SolveNode<T>& sn, int t, int nrhs, T* xs, T* red) {
+  static_assert(kWaveL21Rows * NR <= SB * LDB, "the staged rows fit the diagonal block's space");
+  static_assert(kWaveL21Rows == 4 * 64, "four row groups of 64 per chunk");
+  const int b = t / sn.nch, c = t % sn.nch;
+  const int m = sn.m, nelim = sn.nelim;
+  const int c0 = b * SB, jb = min(SB, nelim - c0);
+  const int R0 = nelim + c * kWaveL21Rows, nr = min(kWaveL21Rows, m - R0);
+  const int tid = threadIdx.x, col = tid % SB, rq = tid / SB;
+  for (int e = tid; e < kWaveL21Rows * NR; e += kSolveThreads) {
+    const int rr = e % kWaveL21Rows, q = e / kWaveL21Rows;
+    xs[rr * NR + q] = (rr < nr && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + R0 + rr]) : T(0);
+  }
+  __syncthreads();
+  T acc[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) acc[q] = T(0);
+  const T* Lp = sn.L + (int64_t)(c0 + col) * sn.ld + R0 + rq * 64;
+  for (int kb = 0; kb < 64; kb += 16) {
+    T lv[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+      lv[k] = (col < jb && rq * 64 + kb + k < nr) ? Lp[kb + k] : T(0);
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+#pragma unroll
+      for (int q = 0; q < NR; ++q) acc[q] += lv[k] * xs[(rq * 64 + kb + k) * NR + q];
+  }
+#pragma unroll
+  for (int q = 0; q < NR; ++q) red[(rq * NR + q) * SB + col] = acc[q];
+  __syncthreads();
+  T* out = sn.l21p + (size_t)(b * sn.nch + c) * SB * kSolveRhs;
+  for (int e = tid; e < SB * NR; e += kSolveThreads) {
+    const int cc = e % SB, q = e / SB;
+    out[cc * kSolveRhs + q] = red[q * SB + cc] + red[(NR + q) * SB + cc] +
+                              red[(2 * NR + q) * SB + cc] + red[(3 * NR + q) * SB + cc];
+  }
+}
+
+// Backward block item for pivot block b: x_b -= L21(:, b)^T x(rows below
+// the pivots), from the block's partial items (their sums in chunk order)
+// or, for a front without them (a small front taken whole), over its
+// contribution rows here; then x_b -= sum_{j > b} L(j, b)^T y_j as the
+// flags of the pivot blocks j arrive (thread (c, rq): column c, rows
+// [16 rq, 16 rq + 16) of each 64-row tile), the four row quarters added in
+// shared memory, L_bb^T solved in registers, y written to the local vector
+// and to x, and the flag set.  False if a wait gave up.
+template <typename T, int NR>
+__device__ bool bwd_block(const SolveNode<T>& sn, int b, int nrhs, double* x, int ldx,
+                          int* status, T* Lb, T* yb, T* red, int* s_fail, const WaveLevel& wl,
+                          int it) {
+  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
+  const int tid = threadIdx.x, c = tid % SB, rq = tid / SB;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int m = sn.m, nelim = sn.nelim;
+  const int c0 = b * SB, jb = min(SB, nelim - c0);
+  prefetch_diag_block(sn, c0, jb, Lb);
+  // the block's gathered values (D^{-1} applied), final before any wait
+  T own[R][2];
+#pragma unroll
+  for (int rr = 0; rr < R; ++rr) {
+    const int q = warp + rr * kSolveWarps;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      const int col = lane + 32 * g;
+      own[rr][g] = (q < nrhs && q < NR && col < jb) ? __ldcg(&sn.xloc[(int64_t)q * m + c0 + col])
+                                                    : T(0);
+    }
+  }
+  T acc[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) acc[q] = T(0);
+  bool ok = true;
+  if (sn.nch > 0) {
+    ok = wave_wait_count(wave_l21done(sn, b), sn.nch, status, s_fail);
+    if (ok && rq == 0) {
+      const T* pp = sn.l21p + (size_t)b * sn.nch * SB * kSolveRhs + c * kSolveRhs;
+      for (int k = 0; k < sn.nch; ++k)
+#pragma unroll
+        for (int q = 0; q < NR; ++q)
+          if (q < nrhs) acc[q] += __ldcg(pp + (size_t)k * SB * kSolveRhs + q);
+    }
+  } else {
+    // the contribution rows, 64-row tiles
+    for (int R0 = nelim; R0 < m; R0 += SB) {
+      const int nr = min(SB, m - R0);
       T lv[16];
       {
         const T* Lp = sn.L + (int64_t)(c0 + c) * sn.ld + R0 + rq * 16;
 #pragma unroll
         for (int k = 0; k < 16; ++k) lv[k] = (c < jb && rq * 16 + k < nr) ? Lp[k] : T(0);
       }
-      ok = wave_wait(&sn.flag[j], status, &s_fail);
-      if (!ok) break;
       for (int e = tid; e < SB * NR; e += kSolveThreads) {
         const int rr = e % SB, q = e / SB;
-        // another CTA wrote the pivot blocks' values: read them from L2
-        yb[rr * NR + q] = (rr < nr && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + R0 + rr]) : T(0);
+        yb[rr * NR + q] =
+            (rr < nr && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + R0 + rr]) : T(0);
       }
       __syncthreads();
 #pragma unroll
@@ -750,48 +997,124 @@ __global__ void __launch_bounds__(kSolveThreads)
         for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(rq * 16 + k) * NR + q];
       __syncthreads();
     }
-    if (!ok) {
-      cp_async_wait_all();
-      continue;
-    }
+  }
+  // the pivot blocks sn.nblk-1 .. b+1, as their flags arrive
+  for (int j = sn.nblk - 1; j > b && ok; --j) {
+    const int R0 = j * SB, nr = min(SB, nelim - R0);
+    T lv[16];
+    {
+      const T* Lp = sn.L + (int64_t)(c0 + c) * sn.ld + R0 + rq * 16;
 #pragma unroll
-    for (int q = 0; q < NR; ++q) red[(rq * NR + q) * SB + c] = acc[q];
+      for (int k = 0; k < 16; ++k) lv[k] = (c < jb && rq * 16 + k < nr) ? Lp[k] : T(0);
+    }
+    ok = wave_wait(&sn.flag[j], status, s_fail);
+    if (!ok) break;
+    for (int e = tid; e < SB * NR; e += kSolveThreads) {
+      const int rr = e % SB, q = e / SB;
+      // another CTA wrote the pivot blocks' values: read them from L2
+      yb[rr * NR + q] = (rr < nr && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + R0 + rr]) : T(0);
+    }
     __syncthreads();
-    T xr[R][2];
 #pragma unroll
-    for (int rr = 0; rr < R; ++rr) {
-      const int q = warp + rr * kSolveWarps;
+    for (int k = 0; k < 16; ++k)
 #pragma unroll
-      for (int g = 0; g < 2; ++g) {
-        const int col = lane + 32 * g;
-        T v = T(0);
-        if (q < nrhs && q < NR && col < jb)
-          v = sn.xloc[(int64_t)q * m + c0 + col] -
-              (red[q * SB + col] + red[(NR + q) * SB + col] + red[(2 * NR + q) * SB + col] +
-               red[(3 * NR + q) * SB + col]);
-        xr[rr][g] = v;
-      }
-    }
+      for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(rq * 16 + k) * NR + q];
+    __syncthreads();
+  }
+  if (!ok) {
     cp_async_wait_all();
-    __syncthreads();
-    if (warp < nrhs) solve_in_regs<T, R, false>(jb, Lb, xr);
+    return false;
+  }
+  wave_stamp(wl, it, 1);
 #pragma unroll
-    for (int rr = 0; rr < R; ++rr) {
-      const int q = warp + rr * kSolveWarps;
+  for (int q = 0; q < NR; ++q) red[(rq * NR + q) * SB + c] = acc[q];
+  __syncthreads();
+  T xr[R][2];
 #pragma unroll
-      for (int g = 0; g < 2; ++g) {
-        const int col = lane + 32 * g;
-        if (q < nrhs && q < NR && col < jb) {
-          sn.xloc[(int64_t)q * m + c0 + col] = xr[rr][g];
-          x[(int64_t)q * ldx + sn.perm[c0 + col]] = (double)xr[rr][g];
-        }
+  for (int rr = 0; rr < R; ++rr) {
+    const int q = warp + rr * kSolveWarps;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      const int col = lane + 32 * g;
+      T v = T(0);
+      if (q < nrhs && q < NR && col < jb)
+        v = own[rr][g] - (red[q * SB + col] + red[(NR + q) * SB + col] +
+                          red[(2 * NR + q) * SB + col] + red[(3 * NR + q) * SB + col]);
+      xr[rr][g] = v;
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  if (warp < nrhs) solve_in_regs<T, R, false>(jb, Lb, xr);
+#pragma unroll
+  for (int rr = 0; rr < R; ++rr) {
+    const int q = warp + rr * kSolveWarps;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      const int col = lane + 32 * g;
+      if (q < nrhs && q < NR && col < jb) {
+        sn.xloc[(int64_t)q * m + c0 + col] = xr[rr][g];
+        x[(int64_t)q * ldx + sn.perm[c0 + col]] = (double)xr[rr][g];
       }
     }
-    __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      st_release(&sn.flag[w.y], 1);
+  }
+  __syncthreads();
+  // the release orders every thread's writes above (ordered before it by
+  // the barrier) before the flag, for any CTA that acquires the flag
+  if (tid == 0) st_release(&sn.flag[b], 1);
+  return true;
+}
+
+// Backward pass over the whole tree (item list and waits: see WaveLevel).
+template <typename T, int NR>
+__global__ void __launch_bounds__(kSolveThreads)
+    k_bwd_tree(const SolveNode<T>* sns, WaveLevel wl, int nrhs, double* x, int ldx, int diag_mode,
+               int* status) {
+  extern __shared__ __align__(16) unsigned char solve_smem[];
+  T* Lb = reinterpret_cast<T*>(solve_smem);
+  T* yb = Lb + SB * LDB;
+  T* red = yb + SB * NR;
+  __shared__ int s_item, s_fail;
+  for (;;) {
+    const int it = wave_next(wl, &s_item);
+    if (it >= wl.nitems) break;
+    wave_stamp(wl, it, 0);
+    const int2 w = wl.items[it];
+    const SolveNode<T>& sn = sns[w.x];
+    const int code = w.y;
+    bool ok = true;
+    if (code >= kWaveL21) {
+      ok = wave_wait_count(wave_gathered(sn), sn.ngat, status, &s_fail);
+      if (ok) wave_stamp(wl, it, 1);
+      const int t = code - kWaveL21;
+      if (ok) bwd_l21_item<T, NR>(sn, t, nrhs, Lb, red);
+      if (ok) wave_signal(wave_l21done(sn, t / sn.nch), wave_finished(sn));
+    } else if (code >= kWaveGather) {
+      // the rows below the pivots are solved at the ancestors, which are
+      // final once the parent has finished (it waited for its own parent)
+      if (sn.parent >= 0) {
+        const SolveNode<T>& pn = sns[sn.parent];
+        ok = wave_wait_count(wave_finished(pn), pn.nitb, status, &s_fail);
+      }
+      if (!ok) continue;
+      wave_stamp(wl, it, 1);
+      const int g0 = code == kWaveSmall ? 0 : (code - kWaveGather) * kWaveGatherRows;
+      const int g1 = code == kWaveSmall ? sn.m : min(sn.m, g0 + kWaveGatherRows);
+      bwd_gather_rows<T, NR>(sn, x, ldx, nrhs, diag_mode, g0, g1);
+      if (code == kWaveSmall) {
+        __syncthreads();
+        if (sn.nelim > 0)
+          ok = bwd_block<T, NR>(sn, 0, nrhs, x, ldx, status, Lb, yb, red, &s_fail, wl, it);
+        if (ok) wave_signal(wave_finished(sn), nullptr);
+      } else {
+        wave_signal(wave_gathered(sn), wave_finished(sn));
+      }
+    } else {
+      ok = wave_wait_count(wave_gathered(sn), sn.ngat, status, &s_fail);
+      if (ok) ok = bwd_block<T, NR>(sn, code, nrhs, x, ldx, status, Lb, yb, red, &s_fail, wl, it);
+      if (ok) wave_signal(wave_finished(sn), nullptr);
     }
+    wave_stamp(wl, it, 2);
   }
 }
 
@@ -935,36 +1258,28 @@ int wave_timeout_probe(int rounds) {
 inline int wave_grid(int nitems) { return std::max(1, std::min(nitems, 2 * 152)); }
 
 template <typename T>
-void launch_fwd_wave(const SolveNode<T>* sn, const WaveLevel& wl, int nrhs, double* x, int ldx,
-                     bool scale_sqrt, int* status, cudaStream_t s) {
+void launch_fwd_tree(const SolveNode<T>* sn, const int* children, const int2* pairs,
+                     const WaveLevel& wl, int nrhs, double* x, int ldx, bool scale_sqrt,
+                     int* status, cudaStream_t s) {
   if (wl.nitems <= 0) return;
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
-    k_fwd_wave<T, NR><<<wave_grid(wl.nitems), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
-        sn, wl, nrhs, x, ldx, scale_sqrt, status);
+    k_fwd_tree<T, NR><<<wave_grid(wl.nitems), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
+        sn, children, pairs, wl, nrhs, x, ldx, scale_sqrt, status);
   });
   note_launches(1);
 }
 
 template <typename T>
-void launch_bwd_wave(const SolveNode<T>* sn, const int* nodes, int nn, const WaveLevel& wl,
-                     double* x, int ldx, int nrhs, int max_m, int max_nelim, int diag_mode,
-                     int* status, cudaStream_t s) {
-  if (nn <= 0) return;
-  const int gx = std::max(1, std::min(cdiv(max_m * nrhs, 256), 152));
-  launch_pdl(k_bwd_gather<T>, dim3(gx, nn), 256, 0, s, sn, nodes, x, ldx, nrhs, diag_mode, true);
-  note_launches(1);
+void launch_bwd_tree(const SolveNode<T>* sn, const WaveLevel& wl, double* x, int ldx, int nrhs,
+                     int diag_mode, int* status, cudaStream_t s) {
   if (wl.nitems <= 0) return;
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
-    // L21^T x of the contribution rows, every eliminated column in parallel
-    const int gw = std::max(1, std::min(cdiv(max_nelim, kSolveWarps / l21_warps_host(max_m)),
-                                        4 * 152));
-    launch_pdl(k_bwd_l21<T, NR>, dim3(gw, nn), kSolveThreads, 0, s, sn, nodes, nrhs);
-    k_bwd_wave<T, NR><<<wave_grid(wl.nitems), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
-        sn, wl, nrhs, x, ldx, status);
+    k_bwd_tree<T, NR><<<wave_grid(wl.nitems), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
+        sn, wl, nrhs, x, ldx, diag_mode, status);
   });
-  note_launches(2);
+  note_launches(1);
 }
 
 // the dynamic shared memory limit of every solve kernel instantiation; called
@@ -985,8 +1300,8 @@ void solve_init() {
         set(k_bwd_step<T, NR, kStepFused>, solve_smem_bytes<T, NR>());
         set(k_bwd_step<T, NR, kStepSolve>, solve_smem_bytes<T, NR>());
         set(k_bwd_step<T, NR, kStepUpdate>, solve_smem_bytes<T, NR>());
-        set(k_fwd_wave<T, NR>, solve_smem_bytes<T, NR>());
-        set(k_bwd_wave<T, NR>, solve_smem_bytes<T, NR>());
+        set(k_fwd_tree<T, NR>, solve_smem_bytes<T, NR>());
+        set(k_bwd_tree<T, NR>, solve_smem_bytes<T, NR>());
       });
     }
   });
@@ -1000,10 +1315,11 @@ void solve_init() {
                                     double*, int, bool, cudaStream_t, PhaseTimer*);            \
   template void launch_bwd<T>(const SolveNode<T>*, const int*, int, double*, int, int, int, int, \
                               int, bool, cudaStream_t, PhaseTimer*);                           \
-  template void launch_fwd_wave<T>(const SolveNode<T>*, const WaveLevel&, int, double*, int,   \
-                                   bool, int*, cudaStream_t);                                  \
-  template void launch_bwd_wave<T>(const SolveNode<T>*, const int*, int, const WaveLevel&,     \
-                                   double*, int, int, int, int, int, int*, cudaStream_t);
+  template void launch_fwd_tree<T>(const SolveNode<T>*, const int*, const int2*,               \
+                                   const WaveLevel&, int, double*, int, bool, int*,            \
+                                   cudaStream_t);                                              \
+  template void launch_bwd_tree<T>(const SolveNode<T>*, const WaveLevel&, double*, int, int,   \
+                                   int, int*, cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

@@ -223,15 +223,23 @@ struct TcPlan {
   std::vector<char> blob;
   size_t o_jobs = 0, o_tiles = 0, o_maps = 0;
   int nsplit = 0, ntiles = 0, maxr = 0, maxk = 0, grid = 0;
+  int bn = 256;  // tile width (N) of the GEMM kernel
 };
-int tc_gemm_prepare(const std::vector<TcProblem>& ps, void* scratch, TcPlan& plan);
+// Tile widths of k_tc_gemm (128 x bn tiles): 64, 128 or 256.
+bool tc_tile_width_ok(int bn);
+// The autotuned tile width for a launch over ps on the current device
+// (256 before the device has been tuned; SPRAL_GB300_TC_BN overrides it).
+int tc_tile_width(const std::vector<TcProblem>& ps);
+// bn = 0: the autotuned width; returns -4 for a width the kernel lacks.
+int tc_gemm_prepare(const std::vector<TcProblem>& ps, void* scratch, TcPlan& plan, int bn = 0);
 int tc_gemm_launch(const TcPlan& plan, const void* d_blob, int* status, cudaStream_t s,
                    int chunk);
 // Returns 0, or a negative code: -1 allocation, -2 tensor-map encoding,
-// -3 launch error.  Device-side pipeline timeouts are reported in *status.
+// -3 launch error, -4 unknown tile width.  Device-side pipeline timeouts are
+// reported in *status.
 int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf, int* status,
                 cudaStream_t s, int chunk = kTcChunk, float* ms_split = nullptr,
-                float* ms_gemm = nullptr);
+                float* ms_gemm = nullptr, int bn = 0);
 
 // syrk-like lower update C(r,c) -= sum_k A(r,k) B(c,k), r >= c
 template <typename T>
@@ -262,23 +270,60 @@ struct SolveNode {
   int sptr0;         // first own pivot
   int child_beg, child_end;  // into the child arrays
   int doff;          // offset of this node's delays inside its parent's delay block
-  int* flag;         // ceil(nelim / 64) completion flags of the wavefront solves
-  int pad_;
+  // wavefront solves: flag[0, nblk) completion flags of the pivot blocks,
+  // flag[nblk, 2 nblk) finished L21^T partial items of each pivot block,
+  // flag[2 nblk] gathered row chunks, flag[2 nblk + 1] finished items of
+  // the pass
+  int* flag;
+  T* l21p;           // backward L21^T partial sums: [nblk][nch][64][kSolveRhs]
+  int nblk;          // ceil(nelim / 64) pivot blocks
+  int ngat;          // gather items (0: the front is one small item)
+  int nch;           // L21^T partial items per pivot block (0: none)
+  int nitf, nitb;    // items of the forward and of the backward pass
+  int parent;        // front index of the parent, -1 at a root
 };
 
-// Wavefront solves: one persistent launch per level.  The level's work
-// items, items[i] = (front, block), are taken in list order from an atomic
-// counter; a pivot block waits (bounded) for the flags of the blocks it
-// needs, which come earlier in the list, so every awaited item is held by a
-// running CTA.  Forward: pivot blocks (rows [64 b, 64 b + 64) of the
-// eliminated part) in increasing block order, then the contribution row
-// blocks (block >= 0x10000: rows nelim + 64 (block - 0x10000)).  Backward:
-// pivot blocks in decreasing order.  A wait that gives up sets *status.
+// Wavefront solves: one persistent launch per pass over the whole tree.
+// The work items, items[i] = (front, code), are taken in list order from an
+// atomic counter; an item waits (bounded) only for items earlier in the
+// list, so every awaited item is held by a running CTA.  Codes:
+//   [0, 0x10000)        pivot block b (rows [64 b, 64 b + 64) of the
+//                       eliminated part);
+//   [0x10000, 0x20000)  forward only: contribution row block k (rows
+//                       nelim + 64 k ...);
+//   [0x20000, 0x30000)  gather chunk c: rows [256 c, 256 c + 256) of the
+//                       front's local vector;
+//   0x30000             a small front whole (gather, its one pivot block
+//                       and, forward, its contribution rows) in one item;
+//   >= 0x100000         backward only: L21^T partial item t = b nch + c,
+//                       the product over contribution rows
+//                       [nelim + 256 c, nelim + 256 c + 256) for pivot
+//                       block b.
+// Forward list: levels from the leaves; per level the gathers (and small
+// fronts), then the pivot blocks in increasing block order, then the
+// contribution row blocks.  A gather waits until every child has finished
+// all its items; pivot and contribution blocks wait for their front's
+// gathers and for the pivot blocks before them.  Backward list: levels from
+// the root; per level the gathers, then the pivot blocks in decreasing
+// order, each after its block's L21^T partial items (which wait for their
+// front's gathers); a gather waits until the parent has finished.  A wait
+// that gives up sets *status.
 constexpr int kWaveContrib = 0x10000;
+constexpr int kWaveGather = 0x20000;
+constexpr int kWaveSmall = 0x30000;
+constexpr int kWaveL21 = 0x100000;
+constexpr int kWaveGatherRows = 256;
+constexpr int kWaveL21Rows = 256;
+// a front is one small item when it has at most one pivot block and at most
+// this many rows below its pivots
+constexpr int kWaveSmallRows = 256;
 struct WaveLevel {
   const int2* items;
   int nitems;
   int* counter;  // zeroed before the launch
+  // optional trace (nullptr: off): per item, the global timer when a CTA
+  // took it, when its last wait was over, when it finished, and the SM
+  unsigned long long* trace;
 };
 
 constexpr int kSolveBlk = 64;   // diagonal block of the blocked triangular solves
@@ -292,14 +337,16 @@ template <typename T>
 void launch_fwd_steps(const SolveNode<T>* sn, const int* nodes, int nn, int max_nelim,
                       int max_m, int nrhs, double* x, int ldx, bool scale_sqrt, cudaStream_t s,
                       PhaseTimer* tm);
+// one forward pass over the whole tree (gathers included)
 template <typename T>
-void launch_fwd_wave(const SolveNode<T>* sn, const WaveLevel& wl, int nrhs, double* x, int ldx,
-                     bool scale_sqrt, int* status, cudaStream_t s);
-// backward wave after the level's gather (launch_bwd with do_bwd)
-template <typename T>
-void launch_bwd_wave(const SolveNode<T>* sn, const int* nodes, int nn, const WaveLevel& wl,
-                     double* x, int ldx, int nrhs, int max_m, int max_nelim, int diag_mode,
+void launch_fwd_tree(const SolveNode<T>* sn, const int* children, const int2* pairs,
+                     const WaveLevel& wl, int nrhs, double* x, int ldx, bool scale_sqrt,
                      int* status, cudaStream_t s);
+// one backward pass over the whole tree (gathers, D^{-1} by diag_mode and
+// the L21^T products included)
+template <typename T>
+void launch_bwd_tree(const SolveNode<T>* sn, const WaveLevel& wl, double* x, int ldx, int nrhs,
+                     int diag_mode, int* status, cudaStream_t s);
 // failure-detection probe of the wavefront solves' bounded flag wait
 // (solve_kernels.cu): -51 when the wait gave up
 int wave_timeout_probe(int rounds);

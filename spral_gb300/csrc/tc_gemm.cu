@@ -9,11 +9,12 @@
 // which is ONE TF32 GEMM over a 3K-deep operand pair
 //   A' = [Ahi | Ahi | Alo],  B' = [Bhi | Blo | Bhi]   (interleaved per k).
 // k_split builds A' and B' K-major (row-major, ld = kpad); k_tc_gemm is a
-// persistent kernel that computes 128 x 256 tiles of the result: it streams
-// 32-deep k-tiles of A' (128 rows) and B' (256 rows) with TMA (128-byte
-// swizzle) through a 4-stage mbarrier pipeline into tcgen05.mma.kind::tf32
-// (M = 128, N = 256, FP32 accumulators in TMEM) and subtracts the result
-// from C.
+// persistent kernel that computes 128 x BN tiles of the result (BN = 256,
+// 128 or 64, chosen per launch by the autotuner): it streams 32-deep k-tiles
+// of A' (128 rows) and B' (BN rows) with TMA (128-byte swizzle) through an
+// mbarrier pipeline of 192 KiB (4, 6 or 8 stages) into
+// tcgen05.mma.kind::tf32 (M = 128, N = BN, FP32 accumulators in TMEM) and
+// subtracts the result from C.
 //
 // Accumulation: the tensor cores accumulate at most `chunk` k-tiles
 // (32 * chunk split products) in TMEM; the epilogue warps then add that
@@ -32,17 +33,25 @@
 #include <cstring>
 #include <vector>
 
+#include "spral_ssids_gpu.h"
 #include "ssids_gpu.cuh"
 
 namespace ssids300 {
 
 namespace {
 
-constexpr int TC_M = 128, TC_N = 256, TC_K = 32;  // K = 32 fp32 = 128 bytes
-constexpr int TC_STAGES = 4;
+constexpr int TC_M = 128, TC_K = 32;  // K = 32 fp32 = 128 bytes
 constexpr int TC_A_BYTES = TC_M * TC_K * 4;  // 16 KiB of A' per stage
-constexpr int TC_B_BYTES = TC_N * TC_K * 4;  // 32 KiB of B' per stage
-constexpr uint32_t TC_TMEM_COLS = 2 * TC_N;  // two FP32 accumulators = all of TMEM
+constexpr int TC_RING_BYTES = 192 << 10;     // the k-tile ring of every tile width
+// tile width BN: B' bytes per stage, stages, TMEM columns (two FP32
+// accumulators of BN columns; a power of two >= 32 as tcgen05.alloc needs)
+template <int BN>
+struct TcShape {
+  static_assert(BN == 64 || BN == 128 || BN == 256, "tile widths of the kernel");
+  static constexpr int B_BYTES = BN * TC_K * 4;
+  static constexpr int STAGES = TC_RING_BYTES / (TC_A_BYTES + B_BYTES);
+  static constexpr uint32_t TMEM_COLS = 2 * BN;
+};
 constexpr int TC_EPI_WARPS = 8;              // two per TMEM lane quarter
 constexpr int TC_EPI_THREADS = 32 * TC_EPI_WARPS;
 constexpr int TC_THREADS = 64 + TC_EPI_THREADS;
@@ -142,9 +151,10 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
   return d;
 }
 
-// instruction descriptor: D = F32, A = B = TF32, both K-major, N = TC_N, M = 128
+// instruction descriptor: D = F32, A = B = TF32, both K-major, N = BN, M = 128
+template <int BN>
 __host__ __device__ constexpr uint32_t idesc_tf32() {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
          ((uint32_t)(TC_M >> 4) << 24);
 }
 
@@ -215,7 +225,7 @@ __device__ __forceinline__ int tile_ktiles(const TcJob& j) {
 }
 
 // Persistent kernel, one CTA per SM, 320 threads:
-//   warp 0 lane 0   TMA producer (A' and B' k-tiles into a TC_STAGES ring)
+//   warp 0 lane 0   TMA producer (A' and B' k-tiles into a ring of STAGES)
 //   warp 1 lane 0   MMA issuer (tcgen05.mma into one of two TMEM accumulators)
 //   warps 2..9      accumulate / epilogue (warp w reads TMEM lanes 32*(w%4)..)
 // The k range of a tile is cut into chunks of `chunk` k-tiles (0 = one chunk).
@@ -224,9 +234,14 @@ __device__ __forceinline__ int tile_ktiles(const TcJob& j) {
 // row of the tile, so the tensor cores' own accumulation spans at most
 // 32 * chunk products.  Two accumulators let the MMAs of the next chunk (or
 // tile) run while the previous one is drained.
+template <int BN>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_gemm(const TcJob* jobs, const int4* tiles, int ntiles, const CUtensorMap* maps,
               int chunk, int* status) {
+  constexpr int TC_STAGES = TcShape<BN>::STAGES;
+  constexpr int TC_B_BYTES = TcShape<BN>::B_BYTES;
+  constexpr uint32_t TC_TMEM_COLS = TcShape<BN>::TMEM_COLS;
+  constexpr int HALF = BN / 2;  // columns of a tile per epilogue warp
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* sA = smem;
@@ -280,7 +295,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           }
           mbar_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
           tma_load_2d(sA + s * TC_A_BYTES, mapA, kt * TC_K, tl.y * TC_M, &full[s]);
-          tma_load_2d(sB + s * TC_B_BYTES, mapB, kt * TC_K, tl.z * TC_N, &full[s]);
+          tma_load_2d(sB + s * TC_B_BYTES, mapB, kt * TC_K, tl.z * BN, &full[s]);
         }
       }
       *s_issued = (int)it;
@@ -288,7 +303,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       // ---- MMA issuer ----
-      const uint32_t idesc = idesc_tf32();
+      const uint32_t idesc = idesc_tf32<BN>();
       uint32_t it = 0, ch = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
@@ -301,7 +316,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;");
-          const uint32_t dacc = tmem + b * TC_N;
+          const uint32_t dacc = tmem + b * BN;
           const int k1 = min(nk, k0 + per);
           for (int kt = k0; kt < k1; ++kt, ++it) {
             const uint32_t s = it % TC_STAGES;
@@ -331,8 +346,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else {
     // ---- accumulate + epilogue ----
-    // warp w (2..9) reads TMEM lane quarter w % 4 and owns the 128-column
-    // half (w - 2) / 4 of the tile: one register row of 128 sums per thread
+    // warp w (2..9) reads TMEM lane quarter w % 4 and owns the column half
+    // (w - 2) / 4 of the tile: one register row of BN / 2 sums per thread
     const int q = warp & 3;
     const int half = (warp - 2) >> 2;
     uint32_t ch = 0;
@@ -343,18 +358,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int nk = tile_ktiles(job);
       if (nk == 0) continue;
       const int per = chunk > 0 ? chunk : nk;
-      float acc[128];
+      float acc[HALF];
 #pragma unroll
-      for (int j = 0; j < 128; ++j) acc[j] = 0.f;
+      for (int j = 0; j < HALF; ++j) acc[j] = 0.f;
       for (int k0 = 0; k0 < nk; k0 += per, ++ch) {
         const uint32_t b = ch & 1;
         // the TMEM loads below are warp-collective: decide as a warp
         const bool got = mbar_wait(&accf[b], (ch >> 1) & 1, abort_flag);
         if (!__all_sync(0xffffffffu, got)) { *abort_flag = 1; ok = false; break; }
         asm volatile("tcgen05.fence::after_thread_sync;");
-        const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + b * TC_N + half * 128;
+        const uint32_t base = tmem + ((uint32_t)(q * 32) << 16) + b * BN + half * HALF;
 #pragma unroll
-        for (int cb = 0; cb < 128; cb += 16) {
+        for (int cb = 0; cb < HALF; cb += 16) {
           uint32_t v[16];
           tmem_ld16(base + (uint32_t)cb, v);
 #pragma unroll
@@ -366,13 +381,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if (!ok) break;
       const int r = tl.y * TC_M + q * 32 + lane;
       if (r < job.M) {
-        const int col0 = tl.z * TC_N + half * 128;
+        const int col0 = tl.z * BN + half * HALF;
         float* crow = job.C + r;
         // 8 columns at a time: all loads in flight before the stores
         const int64_t ldc = job.ldc;
         const float* cbase = crow + col0 * ldc;
 #pragma unroll
-        for (int cb = 0; cb < 128; cb += 8) {
+        for (int cb = 0; cb < HALF; cb += 8) {
           float cv[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
@@ -445,8 +460,35 @@ static CUresult encode_kmajor(CUtensorMap* map, const float* base, int rows, int
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 }
 
-size_t tc_gemm_smem_bytes() {
-  return 1024 + TC_STAGES * (TC_A_BYTES + TC_B_BYTES) + (2 * TC_STAGES + 5) * 8 + 16;
+// dynamic shared memory of k_tc_gemm<BN>: alignment slack, the ring, the
+// barriers (full and empty per stage, two accumulator pairs, drain) and the
+// TMEM slot and flags
+template <int BN>
+static size_t tc_gemm_smem_bytes() {
+  constexpr int st = TcShape<BN>::STAGES;
+  return 1024 + (size_t)st * (TC_A_BYTES + TcShape<BN>::B_BYTES) + (2 * st + 5) * 8 + 16;
+}
+static size_t tc_gemm_smem_bytes(int bn) {
+  return bn == 64 ? tc_gemm_smem_bytes<64>()
+                  : bn == 128 ? tc_gemm_smem_bytes<128>() : tc_gemm_smem_bytes<256>();
+}
+
+bool tc_tile_width_ok(int bn) { return bn == 64 || bn == 128 || bn == 256; }
+
+// one launch of k_tc_gemm with the plan's tile width
+static void launch_tc_kernel(const TcPlan& plan, const char* d, int chunk, int* status,
+                             cudaStream_t s) {
+  const TcJob* jobs = reinterpret_cast<const TcJob*>(d + plan.o_jobs);
+  const int4* tiles = reinterpret_cast<const int4*>(d + plan.o_tiles);
+  const CUtensorMap* maps = reinterpret_cast<const CUtensorMap*>(d + plan.o_maps);
+  const size_t sm = tc_gemm_smem_bytes(plan.bn);
+  if (plan.bn == 64)
+    k_tc_gemm<64><<<plan.grid, TC_THREADS, sm, s>>>(jobs, tiles, plan.ntiles, maps, chunk, status);
+  else if (plan.bn == 128)
+    k_tc_gemm<128><<<plan.grid, TC_THREADS, sm, s>>>(jobs, tiles, plan.ntiles, maps, chunk, status);
+  else
+    k_tc_gemm<256><<<plan.grid, TC_THREADS, sm, s>>>(jobs, tiles, plan.ntiles, maps, chunk, status);
+  note_launches(1);
 }
 
 
@@ -469,8 +511,11 @@ TcBuffers::~TcBuffers() {
 
 static size_t up64(size_t b) { return (b + 63) & ~size_t(63); }
 
-int tc_gemm_prepare(const std::vector<TcProblem>& ps, void* scratch, TcPlan& plan) {
+int tc_gemm_prepare(const std::vector<TcProblem>& ps, void* scratch, TcPlan& plan, int bn) {
   plan = TcPlan{};
+  if (bn == 0) bn = tc_tile_width(ps);
+  if (!tc_tile_width_ok(bn)) return -4;
+  plan.bn = bn;
   if (ps.empty()) return 0;
   std::vector<SplitJob> sj;
   std::vector<TcJob> jobs;
@@ -490,14 +535,14 @@ int tc_gemm_prepare(const std::vector<TcProblem>& ps, void* scratch, TcPlan& pla
     maxk = std::max(maxk, (kpad + 2) / 3);  // split columns 3k..3k+2 cover [0, kpad)
     CUtensorMap ma, mb;
     if (encode_kmajor(&ma, a2, p.M, kpad, kpad, TC_M) != CUDA_SUCCESS) return -2;
-    if (encode_kmajor(&mb, b2, p.N, kpad, kpad, TC_N) != CUDA_SUCCESS) return -2;
+    if (encode_kmajor(&mb, b2, p.N, kpad, kpad, bn) != CUDA_SUCCESS) return -2;
     maps.push_back(ma);
     maps.push_back(mb);
     jobs.push_back({p.C, p.ldc, p.M, p.N, kpad, p.lower, p.kval_dev});
-    const int tm = (p.M + TC_M - 1) / TC_M, tn = (p.N + TC_N - 1) / TC_N;
+    const int tm = (p.M + TC_M - 1) / TC_M, tn = (p.N + bn - 1) / bn;
     for (int ti = 0; ti < tm; ++ti)
       for (int tj = 0; tj < tn; ++tj) {
-        if (p.lower && (tj * TC_N > ti * TC_M + TC_M - 1)) continue;  // tile above diagonal
+        if (p.lower && (tj * bn > ti * TC_M + TC_M - 1)) continue;  // tile above diagonal
         tiles.push_back(make_int4((int)i, ti, tj, kpad));
       }
   }
@@ -522,10 +567,17 @@ int tc_gemm_prepare(const std::vector<TcProblem>& ps, void* scratch, TcPlan& pla
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   plan.grid = std::min(plan.ntiles, std::max(nsm, 1));
-  if (cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)tc_gemm_smem_bytes()) != cudaSuccess)
-    return -3;
-  return 0;
+  cudaError_t e;
+  if (bn == 64)
+    e = cudaFuncSetAttribute(k_tc_gemm<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tc_gemm_smem_bytes<64>());
+  else if (bn == 128)
+    e = cudaFuncSetAttribute(k_tc_gemm<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tc_gemm_smem_bytes<128>());
+  else
+    e = cudaFuncSetAttribute(k_tc_gemm<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tc_gemm_smem_bytes<256>());
+  return e == cudaSuccess ? 0 : -3;
 }
 
 int tc_gemm_launch(const TcPlan& plan, const void* d_blob, int* status, cudaStream_t s, int chunk) {
@@ -534,21 +586,15 @@ int tc_gemm_launch(const TcPlan& plan, const void* d_blob, int* status, cudaStre
   dim3 sg((plan.maxr + 31) / 32, (plan.maxk + 31) / 32, (unsigned)plan.nsplit);
   k_split<<<sg, 256, 0, s>>>(reinterpret_cast<const SplitJob*>(d));
   note_launches(1);
-  if (plan.ntiles > 0) {
-    k_tc_gemm<<<plan.grid, TC_THREADS, tc_gemm_smem_bytes(), s>>>(
-        reinterpret_cast<const TcJob*>(d + plan.o_jobs),
-        reinterpret_cast<const int4*>(d + plan.o_tiles), plan.ntiles,
-        reinterpret_cast<const CUtensorMap*>(d + plan.o_maps), chunk, status);
-    note_launches(1);
-  }
+  if (plan.ntiles > 0) launch_tc_kernel(plan, d, chunk, status, s);
   return cudaGetLastError() == cudaSuccess ? 0 : -3;
 }
 
 int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf, int* status,
-                cudaStream_t s, int chunk, float* ms_split, float* ms_gemm) {
+                cudaStream_t s, int chunk, float* ms_split, float* ms_gemm, int bn) {
   if (ps.empty()) return 0;
   TcPlan plan;
-  const int rp = tc_gemm_prepare(ps, scratch, plan);
+  const int rp = tc_gemm_prepare(ps, scratch, plan, bn);
   if (rp != 0) return rp;
   // one upload of all descriptors through a pinned staging buffer
   const size_t total = plan.blob.size();
@@ -580,12 +626,7 @@ int tc_gemm_run(const std::vector<TcProblem>& ps, void* scratch, TcBuffers& buf,
   int rc = tc_gemm_launch(only_split, buf.d_stage, status, s, chunk);
   cudaEventRecord(ev[1], s);
   if (rc == 0 && plan.ntiles > 0) {
-    const char* d = static_cast<const char*>(buf.d_stage);
-    k_tc_gemm<<<plan.grid, TC_THREADS, tc_gemm_smem_bytes(), s>>>(
-        reinterpret_cast<const TcJob*>(d + plan.o_jobs),
-        reinterpret_cast<const int4*>(d + plan.o_tiles), plan.ntiles,
-        reinterpret_cast<const CUtensorMap*>(d + plan.o_maps), chunk, status);
-    note_launches(1);
+    launch_tc_kernel(plan, static_cast<const char*>(buf.d_stage), chunk, status, s);
     rc = cudaGetLastError() == cudaSuccess ? 0 : -3;
   }
   cudaEventRecord(ev[2], s);
@@ -639,8 +680,16 @@ extern "C" int spral_ssids_gpu_mbar_timeout_probe(int rounds) {
 extern "C" int spral_ssids_gpu_tc_gemm_f32(int M, int N, int K, const float* A, int lda,
                                            const float* B, int ldb, float* C, int ldc, int lower,
                                            int chunk, int reps, float* ms) {
+  return spral_ssids_gpu_tc_gemm_f32_bn(M, N, K, A, lda, B, ldb, C, ldc, lower, chunk, reps, ms,
+                                        0);
+}
+
+extern "C" int spral_ssids_gpu_tc_gemm_f32_bn(int M, int N, int K, const float* A, int lda,
+                                              const float* B, int ldb, float* C, int ldc,
+                                              int lower, int chunk, int reps, float* ms, int bn) {
   using namespace ssids300;
   if (M < 0 || N < 0 || K < 0 || lda < M || ldb < N || ldc < M) return -1;
+  if (bn != 0 && !tc_tile_width_ok(bn)) return -4;
   if (chunk < 0) chunk = kTcChunk;
   std::vector<TcProblem> ps(1);
   ps[0] = {A, lda, B, ldb, C, ldc, M, N, K, nullptr, lower};
@@ -657,7 +706,8 @@ extern "C" int spral_ssids_gpu_tc_gemm_f32(int M, int N, int K, const float* A, 
     double tsplit = 0, tgemm = 0;
     for (int i = 0; i < n && rc == 0; ++i) {
       float a = 0, b = 0;
-      rc = tc_gemm_run(ps, scratch, buf, status, 0, chunk, ms ? &a : nullptr, ms ? &b : nullptr);
+      rc = tc_gemm_run(ps, scratch, buf, status, 0, chunk, ms ? &a : nullptr, ms ? &b : nullptr,
+                       bn);
       tsplit += a;
       tgemm += b;
     }

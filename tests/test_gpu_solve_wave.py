@@ -1,8 +1,8 @@
-"""The wavefront solves (one persistent launch per level, pivot blocks
-waiting on the flags of the blocks they need; the default for FP32
-factors) against the chain of block step launches (the default for FP64
-factors): every job, several right-hand side counts, FP64 and FP32
-factors, a tree with delayed columns."""
+"""The wavefront solves (one persistent launch per pass over the whole tree,
+items waiting on the flags and counters of the items they need; the default
+for FP32 factors) against the chain of block step launches (the default for
+FP64 factors): every job, several right-hand side counts, FP64 and FP32
+factors, a tree with delayed columns, a forest of many small matrices."""
 import numpy as np
 import pytest
 
@@ -63,3 +63,29 @@ def test_gpu_wave_posdef_solves(monkeypatch):
     y = fk.solve(b, job=1)
     assert _rel(fk.solve(y, job=3), x) < 1e-12
     fk.free()
+
+
+@pytest.mark.parametrize("precision,tol", [(ssids.PRECISION_FP64, 1e-12),
+                                           (ssids.PRECISION_MIXED, 1e-3)], ids=["fp64", "mixed"])
+def test_gpu_wave_solves_on_a_forest(precision, tol, monkeypatch):
+    """A batch of 40 small indefinite 2D Laplacians (one forest whose levels
+    hold many small fronts, taken whole by one item each): the wavefront
+    passes against the block steps, matrix by matrix."""
+    from spral_gb300 import batch
+    rng = np.random.default_rng(40)
+    sides = rng.integers(4, 40, 40)
+    mats = [M.laplacian_2d(int(k), int(k), float(s))
+            for k, s in zip(sides, rng.uniform(-1, 0, 40))]
+    bak = batch.BatchAkeep([(p, r) for p, r, _ in mats],
+                           [M.nd_order_grid(int(k), int(k)) for k in sides])
+    vals = [v for _, _, v in mats]
+    opts = ssids.Options(precision=precision)
+    monkeypatch.setenv("SPRAL_GB300_SOLVE_WAVE", "1")
+    bw = batch.BatchFkeep(bak, vals, opts)
+    monkeypatch.setenv("SPRAL_GB300_SOLVE_WAVE", "0")
+    bs_ = batch.BatchFkeep(bak, vals, opts)
+    b = [rng.standard_normal((len(p) - 1, 3)) for p, _, _ in mats]
+    for xw, xs in zip(bw.solve(b), bs_.solve(b)):
+        assert _rel(xw, xs) < tol
+    bw.free()
+    bs_.free()

@@ -6,7 +6,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _run(M, N, K, lower, chunk, seed):
+def _run(M, N, K, lower, chunk, seed, bn=None):
     torch = pytest.importorskip("torch")
     from spral_gb300 import _native
     rng = np.random.default_rng(seed)
@@ -16,8 +16,13 @@ def _run(M, N, K, lower, chunk, seed):
     dA = torch.tensor(A.ravel(order="F"), device="cuda")
     dB = torch.tensor(B.ravel(order="F"), device="cuda")
     dC = torch.tensor(C.ravel(order="F"), device="cuda")
-    rc = _native.lib().spral_ssids_gpu_tc_gemm_f32(M, N, K, dA.data_ptr(), M, dB.data_ptr(), N,
-                                                    dC.data_ptr(), M, lower, chunk, 0, None)
+    if bn is None:
+        rc = _native.lib().spral_ssids_gpu_tc_gemm_f32(M, N, K, dA.data_ptr(), M, dB.data_ptr(),
+                                                        N, dC.data_ptr(), M, lower, chunk, 0, None)
+    else:
+        rc = _native.lib().spral_ssids_gpu_tc_gemm_f32_bn(M, N, K, dA.data_ptr(), M,
+                                                           dB.data_ptr(), N, dC.data_ptr(), M,
+                                                           lower, chunk, 0, None, bn)
     assert rc == 0
     got = dC.cpu().numpy().reshape(M, N, order="F")
     ref = C.astype(np.float64) - A.astype(np.float64) @ B.astype(np.float64).T
@@ -55,3 +60,22 @@ def test_tc_crossover_is_measured_once_per_device():
     b = L.spral_ssids_gpu_tc_crossover()
     assert a == b  # cached per device
     assert 64 <= a <= 513  # a size of the grid, or "never" (one past the largest)
+
+
+@pytest.mark.parametrize("bn", [64, 128, 256])
+@pytest.mark.parametrize("M,N,K,lower", [(300, 200, 100, 0), (513, 513, 300, 1),
+                                         (129, 1000, 33, 0), (700, 700, 64, 1)])
+def test_tc_gemm_tile_widths_match_fp64(bn, M, N, K, lower):
+    """Every tile width the autotuner may pick gives the same FP32-class result."""
+    C, got, ref = _run(M, N, K, lower, -1, M + 3 * N + K + bn, bn=bn)
+    if lower:
+        mask = np.tril(np.ones((M, N), dtype=bool))
+        assert np.array_equal(got[~mask], C[~mask])
+        got, ref = got[mask], ref[mask]
+    assert np.abs(got - ref).max() <= 2e-5 * np.sqrt(K)
+
+
+def test_tc_gemm_rejects_unknown_tile_width():
+    from spral_gb300 import _native
+    assert _native.lib().spral_ssids_gpu_tc_gemm_f32_bn(128, 128, 32, None, 128, None, 128, None,
+                                                        128, 0, -1, 0, None, 96) == -4
