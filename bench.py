@@ -67,6 +67,8 @@ def parse():
                          "kkt: a KKT saddle point "
                          "(random sparse H and A, -1e-8 I block) in mixed precision with FP64 "
                          "refinement against the FP64 path")
+    ap.add_argument("--nemin", type=int, default=32,
+                    help="supernode amalgamation parameter of the analyse (options%%nemin)")
     ap.add_argument("--kkt-nh", type=int, default=10000)
     ap.add_argument("--kkt-na", type=int, default=5000)
     ap.add_argument("--kkt-order", default="amd", choices=["amd", "natural"],
@@ -87,7 +89,7 @@ def problem(args):
     k = args.grid
     ptr, row, val = M.laplacian_3d(k, shift=args.shift)
     order = M.nd_order_grid(k, k, k)
-    ak = ssids.analyse(ptr, row, order)
+    ak = ssids.analyse(ptr, row, order, ssids.Options(nemin=getattr(args, "nemin", 32)))
     rng = np.random.default_rng(2024)
     b = rng.standard_normal((len(ptr) - 1, args.nrhs))
     return ptr, row, val, ak, b
@@ -97,7 +99,7 @@ def config(args, ak, extra=None):
     c = {"workload": f"3D 7-point Laplacian {args.grid}^3 (n={ak.n}), shift {args.shift}, "
                      f"nested-dissection order, {args.nrhs} RHS N(0,1); one solve = numeric "
                      f"factor + {args.nrhs}-RHS solve",
-         "n": ak.n, "nnz_lower": ak.nnz, "nrhs": args.nrhs, "nemin": 32,
+         "n": ak.n, "nnz_lower": ak.nnz, "nrhs": args.nrhs, "nemin": args.nemin,
          "predicted_flops": ak.nflops, "nfactor": ak.nfact,
          "l2": "inputs larger than L2 (factors ~%.0f MB)" % (ak.nfact * 8 / 1e6),
          "parallelism": f"replicas x{args.gpus}"}
@@ -576,7 +578,11 @@ def batch_problem(args):
 
 def run_batch(args):
     """One step = numeric factorisation of every matrix of the batch plus the
-    solve of each one's right-hand side, FP64 factors."""
+    solve of each one's right-hand side, refined in FP64 until every matrix's
+    own scaled backward error is <= 1e-14.  Measured with FP64 factors
+    (`value`) and with FP32 factors (`mixed`): the batch is one handle, so
+    when FP32 factors cannot reach the target for some of its matrices (a
+    shift near an eigenvalue) the whole batch is refactored in FP64."""
     import torch
     world, rank, local = dist_setup(args)
     torch.cuda.set_device(local)
@@ -585,8 +591,6 @@ def run_batch(args):
     sides, shifts, mats, orders, bs = batch_problem(args)
     bak = batch.BatchAkeep([(p, r) for p, r, _ in mats], orders)
     vals = bak.stack_values([v for _, _, v in mats])
-    bf = batch.BatchFkeep(bak, [v for _, _, v in mats],
-                          ssids.Options(max_refine=10, refine_tol=REFINE_TOL))
     n = bak.n
     B, _ = bak.stack_rhs(bs)
     invp = bak.akeep.invp
@@ -595,56 +599,74 @@ def run_batch(args):
     bp_d = torch.tensor(np.ascontiguousarray(B[invp, 0]), dtype=torch.float64, device=dev)
     x_d = torch.empty_like(bp_d)
 
-    it = ctypes.c_int(0)
-    bw = ctypes.c_double(0)
+    def measure(precision):
+        bf = batch.BatchFkeep(bak, [v for _, _, v in mats],
+                              ssids.Options(precision=precision, max_refine=10,
+                                            refine_tol=REFINE_TOL))
+        it = ctypes.c_int(0)
+        bw = ctypes.c_double(0)
 
-    def step():
-        bf.fk.refactor_dev(vals_d.data_ptr())
-        # solve plus FP64 refinement of the whole batch to bwd err <= 1e-14
-        L.spral_ssids_gpu_solve_refined_dev(bf.fk.num, 1, ctypes.c_void_p(bp_d.data_ptr()),
-                                            ctypes.c_void_p(x_d.data_ptr()), n,
-                                            ctypes.byref(it), ctypes.byref(bw))
+        def step():
+            bf.fk.refactor_dev(vals_d.data_ptr())
+            # solve plus FP64 refinement of the whole batch to bwd err <= 1e-14
+            L.spral_ssids_gpu_solve_refined_dev(bf.fk.num, 1, ctypes.c_void_p(bp_d.data_ptr()),
+                                                ctypes.c_void_p(x_d.data_ptr()), n,
+                                                ctypes.byref(it), ctypes.byref(bw))
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    lc0 = L.spral_ssids_gpu_launch_count()
-    clk = Clocks(local) if rank == 0 else None
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    per = []
-    e0.record()
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        step()
+        for _ in range(args.warmup):
+            step()
         torch.cuda.synchronize()
-        per.append((time.perf_counter() - t0) * 1e3)
-    e1.record()
-    torch.cuda.synchronize()
-    clocks = clk.stop() if clk else None
-    ms = e0.elapsed_time(e1) / args.steps
-    launches = L.spral_ssids_gpu_launch_count() - lc0
-    x = np.empty(n)
-    x[invp] = x_d.cpu().numpy()
-    xs = bak.split(x[:, None], True)
-    bwd = max(float(M.scaled_bwd_error(p, r, v, xs[i], bs[i][:, None]).max())
-              for i, (p, r, v) in enumerate(mats))
-    inert = bf.inertia()
-    exact = all(inert[i, 0] == M.laplacian_eig_count_2d(int(k), int(k), float(sh))[0]
-                for i, (k, sh) in enumerate(zip(sides, shifts)))
-    # end to end: host values and right-hand sides through the batch API
-    e2e_t = []
-    for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        bf.refactor([v for _, _, v in mats])
-        bf.solve_refined(bs)
-        if i >= args.warmup:
-            e2e_t.append(time.perf_counter() - t0)
-    e2e_ms = 1000.0 * sum(e2e_t) / len(e2e_t)
+        lc0 = L.spral_ssids_gpu_launch_count()
+        clk = Clocks(local) if rank == 0 else None
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        per = []
+        e0.record()
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            step()
+            torch.cuda.synchronize()
+            per.append((time.perf_counter() - t0) * 1e3)
+        e1.record()
+        torch.cuda.synchronize()
+        clocks = clk.stop() if clk else None
+        ms = e0.elapsed_time(e1) / args.steps
+        launches = L.spral_ssids_gpu_launch_count() - lc0
+        x = np.empty(n)
+        x[invp] = x_d.cpu().numpy()
+        xs = bak.split(x[:, None], True)
+        bwd = max(float(M.scaled_bwd_error(p, r, v, xs[i], bs[i][:, None]).max())
+                  for i, (p, r, v) in enumerate(mats))
+        inert = bf.inertia()
+        exact = all(inert[i, 0] == M.laplacian_eig_count_2d(int(k), int(k), float(sh))[0]
+                    for i, (k, sh) in enumerate(zip(sides, shifts)))
+        # end to end: host values and right-hand sides through the batch API
+        e2e_t = []
+        for i in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            bf.refactor([v for _, _, v in mats])
+            bf.solve_refined(bs)
+            if i >= args.warmup:
+                e2e_t.append(time.perf_counter() - t0)
+        e2e_ms = 1000.0 * sum(e2e_t) / len(e2e_t)
+        fb = bf.fk.fallbacks
+        bf.free()
+        return {"value": world * args.batch_count * 1000.0 / ms, "unit": "matrices/s",
+                "ms_per_step": ms, "p50_ms": float(np.percentile(per, 50)),
+                "p99_ms": float(np.percentile(per, 99)), "bwd_err": bwd,
+                "refine_iters": it.value, "inertia_exact": bool(exact), "fp64_fallbacks": fb,
+                "gpu_launches": int(launches), "clocks": clocks,
+                "e2e": {"value": args.batch_count * 1000.0 / e2e_ms, "unit": "matrices/s",
+                        "h2d_bytes_per_step": int(vals.nbytes + n * 8),
+                        "d2h_bytes_per_step": int(n * 8),
+                        "path": "BatchFkeep.refactor + BatchFkeep.solve_refined (host values "
+                                "and RHS)"}}
+
+    fp64 = measure(ssids.PRECISION_FP64)
+    mixed = measure(ssids.PRECISION_MIXED)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         import oracle
-        from spral_gb300 import ssids
         oracle.build()
         t_all, done = 0.0, 0
         for i in range(len(mats)):  # a bounded sample, in batch order
@@ -663,28 +685,26 @@ def run_batch(args):
                          f"all cores)"}
     if rank == 0:
         line = {"metric": "matrices factored+solved per second (batched)", "workload": "batch",
-                "value": world * args.batch_count * 1000.0 / ms, "unit": "matrices/s",
-                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "value": fp64["value"], "unit": "matrices/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": fp64["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64",
                 "data": "synthetic (seeded 2D Laplacians and right-hand sides)",
                 "config": {"workload": f"{args.batch_count} indefinite 2D 5-point Laplacians, "
                                        "side log-uniform in [8,128], shift uniform[-1,0], "
-                                       "nested-dissection order, 1 RHS uniform[-1,1] each; one "
-                                       "step = factor + solve of every matrix refined to bwd "
-                                       "err <= 1e-14",
-                           "total_n": n, "nnodes": bak.akeep.nnodes, "bwd_err": bwd,
-                           "refine_iters": it.value,
-                           "inertia_exact": bool(exact),
+                                       "nested-dissection order, FP64 values, 1 RHS "
+                                       "uniform[-1,1] each; one step = factor + solve of every "
+                                       "matrix refined to bwd err <= 1e-14",
+                           "total_n": n, "nnodes": bak.akeep.nnodes,
+                           "nflops": int(bak.akeep.nflops),
+                           "bwd_err": fp64["bwd_err"], "refine_iters": fp64["refine_iters"],
+                           "inertia_exact": fp64["inertia_exact"],
                            "l2": "inputs larger than L2"},
-                "p50_ms": float(np.percentile(per, 50)), "p99_ms": float(np.percentile(per, 99)),
-                "e2e": {"value": args.batch_count * 1000.0 / e2e_ms, "unit": "matrices/s",
-                        "h2d_bytes_per_step": int(vals.nbytes + n * 8),
-                        "d2h_bytes_per_step": int(n * 8),
-                        "path": "BatchFkeep.refactor + BatchFkeep.solve_refined (host values "
-                                "and RHS)"},
-                "gpu_launches": int(launches), "cpu_baseline": cpu, "clocks": clocks}
+                "p50_ms": fp64["p50_ms"], "p99_ms": fp64["p99_ms"], "e2e": fp64["e2e"],
+                "gpu_launches": fp64["gpu_launches"], "mixed": mixed, "cpu_baseline": cpu,
+                "clocks": fp64["clocks"]}
         print(json.dumps(line), flush=True)
-    bf.free()
 
 
 def run_serve(args):
@@ -914,7 +934,7 @@ def kkt_line(args):
     nh, na = args.kkt_nh, args.kkt_na
     ptr, row, val = M.kkt(nh, na, seed=2026)
     order = ssids.order_amd(ptr, row) if args.kkt_order == "amd" else None
-    ak = ssids.analyse(ptr, row, order)
+    ak = ssids.analyse(ptr, row, order, ssids.Options(nemin=args.nemin))
     n, nrhs = ak.n, args.nrhs
     b = np.random.default_rng(2027).standard_normal((n, nrhs))
     dev = torch.device("cuda", local)
@@ -1016,7 +1036,7 @@ def kkt_line(args):
                                        f"numeric factor + {nrhs}-RHS solve refined to bwd err "
                                        f"<= 1e-14",
                            "n": n, "nnz_lower": ak.nnz, "predicted_flops": ak.nflops,
-                           "maxfront": int(ak.front_sizes()[0].max()),
+                           "maxfront": int(ak.front_sizes()[0].max()), "nemin": args.nemin,
                            "num_neg_expected": na,
                            "l2": "inputs larger than L2 (factors ~%.0f MB in FP32)"
                                  % (ak.nfact * 4 / 1e6)},

@@ -1726,46 +1726,118 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp(FrontDesc<T>* fds, FrontSta
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kTppThreads) k_tpp_small(FrontDesc<T>* fds, FrontState* sts,
-                                                           const int* fronts, bool action,
-                                                           double u, double small,
-                                                           int smem_bytes) {
-  extern __shared__ __align__(16) unsigned char tpp_smem[];
-  const int f = fronts[blockIdx.x];
-  FrontState* st = &sts[f];
-  FrontDesc<T> fd = fds[f];
-  if (st->status != kDevOk) return;
-  const int m = fd.m, n = fd.n;
-  const int ldS = (m + 1) & ~1;
-  const size_t need = (size_t)ldS * (n + 2) * sizeof(T) + 2 * (size_t)n * sizeof(int);
-  int nel;
-  if (n == 0) {
-    nel = 0;
-  } else if (need > (size_t)smem_bytes) {
-    nel = tpp_fast(fd.L, fd.ld, m, n, 0, fd.W, fd.W + fd.ld, fd.perm, fd.opos, fd.D, action, u,
-                   small, tpp_batch(fd));
+// ------------------------------------------------------------------------
+// k_tpp_level: the fronts of the small leaf subtrees in one level set, one
+// persistent launch per size class (the multinode_ldlt role of the
+// reference's GPU path, src/ssids/gpu/kernels/dense_factor.cu, with the CPU
+// path's pivoting for these fronts, ldlt_tpp_factor).  CTAs take fronts
+// i = blockIdx.x, blockIdx.x + gridDim.x, ... of the class's list (largest
+// first); per front: the TPP factorisation (in shared memory when the front
+// fits the launch's dynamic shared memory, else in place in global memory),
+// then, fused, the front's contribution: LD = L21 D (the front's LD
+// workspace) and C -= L21 LD^T on the lower triangle of its contribution
+// block, warp per column of C and lane per row, k in increasing order.  So
+// a level set of small fronts takes one or two launches instead of a TPP
+// launch, an LD launch and a contribution launch, and small fronts run many
+// CTAs per SM (the tiny class launches one warp per CTA).
+// ------------------------------------------------------------------------
+// (alpha, beta, partner) of eliminated column c: column c of D = (D^{-1})^{-1}
+// is alpha e_c + beta e_partner (1x1: partner = c, beta = 0)
+__device__ __forceinline__ void d_column(const double* D, int c, int nel, double& alpha,
+                                         double& beta, int& partner) {
+  const double d11 = D[2 * c];
+  if (isinf(d11)) {  // second column of a 2x2
+    const double a = D[2 * (c - 1)], b = D[2 * (c - 1) + 1], d = D[2 * c + 1];
+    const double det = a * d - b * b;
+    alpha = a / det; beta = -b / det; partner = c - 1;
+  } else if (c + 1 < nel && isinf(D[2 * c + 2])) {  // first column of a 2x2
+    const double b = D[2 * c + 1], d = D[2 * c + 3];
+    const double det = d11 * d - b * b;
+    alpha = d / det; beta = -b / det; partner = c + 1;
   } else {
-    T* S = reinterpret_cast<T*>(tpp_smem);
-    T* W0 = S + (size_t)ldS * n;
-    T* W1 = W0 + ldS;
-    int* sperm = reinterpret_cast<int*>(W1 + ldS);
-    int* sopos = sperm + n;
-    for (int c = 0; c < n; ++c)
-      for (int r = threadIdx.x; r < m; r += blockDim.x) S[(size_t)c * ldS + r] = fd.L[(int64_t)c * fd.ld + r];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) { sperm[i] = fd.perm[i]; sopos[i] = fd.opos[i]; }
-    __syncthreads();
-    nel = tpp_fast(S, ldS, m, n, 0, W0, W1, sperm, sopos, fd.D, action, u, small, nullptr);
-    __syncthreads();
-    if (nel >= 0) {
-      for (int c = 0; c < n; ++c)
-        for (int r = threadIdx.x; r < m; r += blockDim.x) fd.L[(int64_t)c * fd.ld + r] = S[(size_t)c * ldS + r];
-      for (int i = threadIdx.x; i < n; i += blockDim.x) { fd.perm[i] = sperm[i]; fd.opos[i] = sopos[i]; }
+    alpha = (d11 != 0.0) ? 1.0 / d11 : 0.0; beta = 0.0; partner = c;
+  }
+}
+
+// the fused contribution of one front whose factor is at S (leading
+// dimension ldS); all threads of the CTA
+template <typename T>
+__device__ void tpp_front_contrib(const FrontDesc<T>& fd, const T* S, int ldS, int nel) {
+  const int n = fd.n, cm = fd.m - fd.n;
+  if (cm <= 0 || nel <= 0) return;
+  for (int e = threadIdx.x; e < cm * nel; e += blockDim.x) {
+    const int rr = e % cm, c = e / cm;
+    double alpha, beta;
+    int partner;
+    d_column(fd.D, c, nel, alpha, beta, partner);
+    const T lv = S[(size_t)c * ldS + n + rr];
+    const T lp = (beta != 0.0) ? S[(size_t)partner * ldS + n + rr] : T(0);
+    fd.LD[(int64_t)c * cm + rr] = (T)(alpha * (double)lv + beta * (double)lp);
+  }
+  __syncthreads();  // LD (global) is read back by other threads of this CTA
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int c = warp; c < cm; c += nw) {
+    const T* ldc = fd.LD + c;
+    for (int r = c + lane; r < cm; r += 32) {
+      const T* lr = S + n + r;
+      T acc = T(0);
+      for (int k = 0; k < nel; ++k) acc += lr[(size_t)k * ldS] * ldc[(int64_t)k * cm];
+      fd.C[(int64_t)c * fd.ldc + r] -= acc;
     }
   }
-  if (threadIdx.x == 0) {
-    if (nel < 0) st->status = kDevSingular;
-    else { st->nelim = nel; st->p = nel; st->step = 0; }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTppThreads) k_tpp_level(FrontDesc<T>* fds, FrontState* sts,
+                                                           const int* fronts, int nf,
+                                                           bool action, double u, double small,
+                                                           int smem_bytes) {
+  extern __shared__ __align__(16) unsigned char tpp_smem[];
+  for (int i = blockIdx.x; i < nf; i += gridDim.x) {
+    const int f = fronts[i];
+    FrontState* st = &sts[f];
+    const FrontDesc<T> fd = fds[f];
+    __syncthreads();  // the previous front is done with shared memory and st
+    if (st->status != kDevOk) continue;
+    const int m = fd.m, n = fd.n;
+    const int ldS = (m + 1) & ~1;
+    const size_t need = (size_t)ldS * (n + 2) * sizeof(T) + 2 * (size_t)n * sizeof(int);
+    int nel;
+    const T* F = fd.L;  // where the factor is when the contribution is formed
+    int ldF = fd.ld;
+    if (n == 0) {
+      nel = 0;
+    } else if (need > (size_t)smem_bytes) {
+      nel = tpp_fast(fd.L, fd.ld, m, n, 0, fd.W, fd.W + fd.ld, fd.perm, fd.opos, fd.D, action, u,
+                     small, tpp_batch(fd));
+    } else {
+      T* S = reinterpret_cast<T*>(tpp_smem);
+      T* W0 = S + (size_t)ldS * n;
+      T* W1 = W0 + ldS;
+      int* sperm = reinterpret_cast<int*>(W1 + ldS);
+      int* sopos = sperm + n;
+      for (int c = 0; c < n; ++c)
+        for (int r = threadIdx.x; r < m; r += blockDim.x)
+          S[(size_t)c * ldS + r] = fd.L[(int64_t)c * fd.ld + r];
+      for (int k = threadIdx.x; k < n; k += blockDim.x) { sperm[k] = fd.perm[k]; sopos[k] = fd.opos[k]; }
+      __syncthreads();
+      nel = tpp_fast(S, ldS, m, n, 0, W0, W1, sperm, sopos, fd.D, action, u, small, nullptr);
+      __syncthreads();
+      if (nel >= 0) {
+        for (int c = 0; c < n; ++c)
+          for (int r = threadIdx.x; r < m; r += blockDim.x)
+            fd.L[(int64_t)c * fd.ld + r] = S[(size_t)c * ldS + r];
+        for (int k = threadIdx.x; k < n; k += blockDim.x) { fd.perm[k] = sperm[k]; fd.opos[k] = sopos[k]; }
+      }
+      F = S;
+      ldF = ldS;
+    }
+    if (threadIdx.x == 0) {
+      if (nel < 0) st->status = kDevSingular;
+      else { st->nelim = nel; st->p = nel; st->step = 0; }
+    }
+    __syncthreads();  // D and the factor are complete
+    if (nel > 0) tpp_front_contrib(fd, F, ldF, nel);
   }
 }
 
@@ -1962,17 +2034,25 @@ void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, boo
 constexpr int kTppSmallSmem = 222 * 1024;
 
 template <typename T>
-void launch_tpp_small(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
-                      double u, double small, int max_bytes, cudaStream_t s) {
+void launch_tpp_level(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
+                      double u, double small, int max_bytes, int threads, cudaStream_t s) {
   if (nf <= 0) return;
   static bool attr_set = false;  // per template instance, once per process
   if (!attr_set) {
-    cudaFuncSetAttribute(k_tpp_small<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_tpp_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kTppSmallSmem);
     attr_set = true;
   }
   const int smem = std::min(std::max(max_bytes, 0), kTppSmallSmem);
-  k_tpp_small<T><<<nf, kTppThreads, smem, s>>>(fd, st, fronts, action, u, small, smem);
+  threads = threads <= 32 ? 32 : threads <= 64 ? 64 : kTppThreads;
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_tpp_level<T>, threads, smem) !=
+      cudaSuccess)
+    occ = 1;
+  const int grid = std::max(1, std::min(nf, std::max(nsm, 1) * std::max(occ, 1)));
+  k_tpp_level<T><<<grid, threads, smem, s>>>(fd, st, fronts, nf, action, u, small, smem);
   note_launches(1);
 }
 
@@ -2010,8 +2090,8 @@ void launch_stats(const FrontDesc<T>* fd, const FrontState* st, const int* front
   template void launch_panel_close<T>(FrontDesc<T>*, FrontState*, const int*, int, cudaStream_t); \
   template void launch_tpp<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double, double, \
                               bool, cudaStream_t);                                              \
-  template void launch_tpp_small<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double,  \
-                                    double, int, cudaStream_t);                                 \
+  template void launch_tpp_level<T>(FrontDesc<T>*, FrontState*, const int*, int, bool, double,  \
+                                    double, int, int, cudaStream_t);                            \
   template void launch_calc_ld<T>(FrontDesc<T>*, FrontState*, const int*, int, int, int,        \
                                   cudaStream_t);                                                 \
   template void launch_contrib_gemm<T>(FrontDesc<T>*, FrontState*, const int*, int, int,        \

@@ -297,6 +297,15 @@ struct DevBuf {
   }
 };
 
+// Size classes of the small leaf subtrees' fronts for the level-set kernel
+// (launch_tpp_level): rows <= 32 one warp per front, <= 96 two warps, more
+// 256 threads; a class launch stages fronts up to its cap in shared memory
+// and factors larger ones in place.
+constexpr int kTppClasses = 3;
+inline int tpp_class(int rows) { return rows <= 32 ? 0 : rows <= 96 ? 1 : 2; }
+inline int tpp_class_threads(int c) { return c == 0 ? 32 : c == 1 ? 64 : 256; }
+inline int tpp_class_smem_cap(int c) { return c == 2 ? (100 << 10) : (64 << 10); }
+
 template <typename T>
 static T* upload(const std::vector<T>& v) {
   T* p = nullptr;
@@ -321,6 +330,10 @@ struct Symbolic {
   // other (APP) fronts, listed first in the level's part of d_fronts.
   std::vector<char> tpp_only;
   std::vector<int> lvl_napp;
+  // the level's TPP fronts by size class for the level-set kernel
+  // (kTppClasses classes of rows, largest first within a class):
+  // d_tpp[tpp_off[kTppClasses * l + c] .. tpp_off[kTppClasses * l + c + 1])
+  std::vector<int> tpp_off, tpp_list;
   std::vector<int> cols_start;  // per level into cols
   std::vector<int64_t> contrib_off;  // per front, elements
   int64_t contrib_total = 0;
@@ -336,6 +349,7 @@ struct Symbolic {
   int* d_rdir = nullptr;
   int64_t* d_rdir_ptr = nullptr;
   int* d_fronts = nullptr;
+  int* d_tpp = nullptr;
   int4* d_cols = nullptr;
   int2* d_pairs = nullptr;
   int* d_gp = nullptr;        // per front, nrow + 1 offsets into d_pairs by parent position
@@ -351,7 +365,7 @@ struct Symbolic {
   spral_ssids_cpu_factor_options copts{};
   ~Symbolic() {
     cudaFree(d_nptr); cudaFree(d_nlist); cudaFree(d_sptr); cudaFree(d_rlist); cudaFree(d_rptr);
-    cudaFree(d_rdir); cudaFree(d_rdir_ptr); cudaFree(d_fronts); cudaFree(d_cols);
+    cudaFree(d_rdir); cudaFree(d_rdir_ptr); cudaFree(d_fronts); cudaFree(d_cols); cudaFree(d_tpp);
     cudaFree(d_pairs); cudaFree(d_gp); cudaFree(d_row_group); cudaFree(d_aptr); cudaFree(d_acol); cudaFree(d_asrc);
   }
 };
@@ -573,6 +587,21 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
     for (int f = S->lvl_start[l]; f < S->lvl_start[l + 1]; ++f)
       if (S->tpp_only[f]) fronts[k++] = f;
   }
+  // size classes of the TPP fronts (rows at analysis)
+  S->tpp_off.assign((size_t)kTppClasses * nlev + 1, 0);
+  S->tpp_list.clear();
+  for (int l = 0; l < nlev; ++l)
+    for (int c = 0; c < kTppClasses; ++c) {
+      S->tpp_off[(size_t)kTppClasses * l + c] = (int)S->tpp_list.size();
+      std::vector<int> cls;
+      for (int f = S->lvl_start[l]; f < S->lvl_start[l + 1]; ++f)
+        if (S->tpp_only[f] && tpp_class(S->nrow[S->node_of[f]]) == c) cls.push_back(f);
+      std::stable_sort(cls.begin(), cls.end(), [&](int a, int b) {
+        return S->nrow[S->node_of[a]] > S->nrow[S->node_of[b]];
+      });
+      S->tpp_list.insert(S->tpp_list.end(), cls.begin(), cls.end());
+    }
+  S->tpp_off[(size_t)kTppClasses * nlev] = (int)S->tpp_list.size();
   std::vector<int> sp(S->sptr.begin(), S->sptr.end());
   S->d_nptr = upload(S->nptr);
   S->d_nlist = upload(nl);
@@ -582,6 +611,7 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
   S->d_rdir = upload(S->rdir_h);
   S->d_rdir_ptr = upload(S->rdir_ptr_h);
   S->d_fronts = upload(fronts);
+  if (!S->tpp_list.empty()) S->d_tpp = upload(S->tpp_list);
   S->d_cols = upload(cols);
   S->d_pairs = upload(pairs);
   S->d_gp = upload(gp);
@@ -858,6 +888,12 @@ struct Numeric : NumericBase {
   DevBuf<int2> wave_items;
   DevBuf<int> wave_flags, wave_ints;
   DevBuf<T> wave_l21p;  // backward L21^T partial sums of the wavefront pass
+  // inverses of the pivot blocks' unit lower diagonal blocks (FP32 factors'
+  // wavefront passes; SPRAL_GB300_SOLVE_BINV=0 keeps the substitution),
+  // formed once per factorisation before the first solve
+  bool use_binv = false;
+  DevBuf<T> wave_binv;
+  DevBuf<int2> binv_blocks;
   int wave_nfwd = 0, wave_nbwd = 0;  // items of the forward pass, then of the backward pass
   size_t wave_nflags = 0;
   // optional trace of the wavefront passes (SPRAL_GB300_WAVE_TRACE = path
@@ -1017,6 +1053,21 @@ struct Numeric : NumericBase {
   // two workspace columns, perm and opos, bytes
   int tpp_bytes(int f) const {
     return ((m_[f] + 1) & ~1) * (n_[f] + 2) * (int)sizeof(T) + 8 * n_[f];
+  }
+  // the level-set kernel over level l's small-subtree fronts, one launch
+  // per non-empty size class, shared memory sized for the class's largest
+  // front (current sizes, delays included) up to the class cap
+  void launch_tpp_levels(int l, cudaStream_t s) {
+    const auto& co = S->copts;
+    for (int c = 0; c < kTppClasses; ++c) {
+      const int o0 = S->tpp_off[(size_t)kTppClasses * l + c];
+      const int o1 = S->tpp_off[(size_t)kTppClasses * l + c + 1];
+      if (o1 <= o0) continue;
+      int mx = 0;
+      for (int k = o0; k < o1; ++k) mx = std::max(mx, tpp_bytes(S->tpp_list[k]));
+      launch_tpp_level<T>(d_fd, d_st, S->d_tpp + o0, o1 - o0, co.action, co.u, co.small,
+                          std::min(mx, tpp_class_smem_cap(c)), tpp_class_threads(c), s);
+    }
   }
 
   std::vector<TcProblem> tc_problems(int f0, int f1) const {
@@ -1228,7 +1279,7 @@ struct Numeric : NumericBase {
       for (int l = 0; l < S->nlev; ++l) {
         const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1], nf = f1 - f0;
         const int napp = app_fronts(l);
-        int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0, max_app_n = 0, max_tpp = 0;
+        int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0, max_app_n = 0, max_app_cm = 0;
         int64_t maxz = 0;
         for (int f = f0; f < f1; ++f) {
           const int node = S->node_of[f];
@@ -1237,8 +1288,10 @@ struct Numeric : NumericBase {
           max_cm = std::max(max_cm, hfd[f].cm);
           max_ent = std::max<int>(max_ent, (int)(S->nptr[node + 1] - S->nptr[node]));
           maxz = std::max(maxz, (int64_t)ld_[f] * n_[f]);
-          if (tpp_front(f)) max_tpp = std::max(max_tpp, tpp_bytes(f));
-          else max_app_n = std::max(max_app_n, n_[f]);
+          if (!tpp_front(f)) {
+            max_app_n = std::max(max_app_n, n_[f]);
+            max_app_cm = std::max(max_app_cm, hfd[f].cm);
+          }
         }
         const int* fr = S->d_fronts + f0;
         launch_zero_fronts<T>(d_fd, fr, nf, (int)std::min<int64_t>(maxz, 1 << 30), s);
@@ -1272,10 +1325,9 @@ struct Numeric : NumericBase {
         launch_app_finish<T>(d_fd, d_st, fr, nf, s);
         const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
         launch_tpp<T>(d_fd, d_st, fr, napp, co.action, co.u, co.small, tpp_all, s);
-        launch_tpp_small<T>(d_fd, d_st, fr + napp, nf - napp, co.action, co.u, co.small, max_tpp,
-                            s);
-        launch_calc_ld<T>(d_fd, d_st, fr, nf, max_cm, max_n, s);
-        launch_contrib_gemm<T>(d_fd, d_st, fr, nf, max_cm, s);
+        if (napp < nf) launch_tpp_levels(l, s);
+        launch_calc_ld<T>(d_fd, d_st, fr, napp, max_app_cm, max_app_n, s);
+        launch_contrib_gemm<T>(d_fd, d_st, fr, napp, max_app_cm, s);
         if (tblob[l] && tc_gemm_launch(tplans[l], tblob[l], d_tc_status, s, tc_chunk) != 0)
           throw CudaFail{cudaErrorUnknown, __LINE__};
         launch_stats<T>(d_fd, d_st, fr, nf, max_n, d_stats, d_ncount, s);
@@ -1431,6 +1483,8 @@ struct Numeric : NumericBase {
       use_wave = wv ? wv[0] != '0' : std::is_same<T, float>::value;
       const char* wt = getenv("SPRAL_GB300_WAVE_TRACE");
       if (wt && *wt) wave_trace = wt;
+      const char* bi = getenv("SPRAL_GB300_SOLVE_BINV");
+      use_binv = std::is_same<T, float>::value && !(bi && bi[0] == '0');
     }
     if (std::is_same<T, float>::value) {
       const char* env = getenv("SPRAL_GB300_TENSOR_CORES");
@@ -1525,7 +1579,7 @@ struct Numeric : NumericBase {
       const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1], nf = f1 - f0;
       const int napp = app_fronts(l);
       dwork.clear();
-      int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0, max_app_n = 0, max_tpp = 0;
+      int max_m = 0, max_n = 0, max_cm = 0, max_ent = 0, max_app_n = 0, max_app_cm = 0;
       size_t wsW = 0, wsSwap = 0, wsLD = 0;
       for (int f = f0; f < f1; ++f) {
         const int node = S->node_of[f];
@@ -1552,8 +1606,9 @@ struct Numeric : NumericBase {
         maxsn = std::max(maxsn, n);
       }
       for (int f = f0; f < f1; ++f) {
-        if (tpp_front(f)) max_tpp = std::max(max_tpp, tpp_bytes(f));
-        else max_app_n = std::max(max_app_n, n_[f]);
+        if (tpp_front(f)) continue;
+        max_app_n = std::max(max_app_n, n_[f]);
+        max_app_cm = std::max(max_app_cm, S->nrow[S->node_of[f]] - S->ncol[S->node_of[f]]);
       }
       ws_W.ensure(wsW + 64);
       ws_swap.ensure(wsSwap + 64);
@@ -1643,12 +1698,12 @@ struct Numeric : NumericBase {
       pmark(tm(), kPhTpp, s);
       const bool tpp_all = (co.pivot_method == 3) || (co.failed_pivot_method == 1);
       launch_tpp<T>(d_fd, d_st, fr, napp, co.action, co.u, co.small, tpp_all, s);
-      launch_tpp_small<T>(d_fd, d_st, fr + napp, nf - napp, co.action, co.u, co.small, max_tpp, s);
+      if (napp < nf) launch_tpp_levels(l, s);
       pmark(tm(), kPhCalcLd, s);
-      launch_calc_ld<T>(d_fd, d_st, fr, nf, max_cm, max_n, s);
+      launch_calc_ld<T>(d_fd, d_st, fr, napp, max_app_cm, max_app_n, s);
       pmark(tm(), kPhContrib, s);
       if (profile) CK(cudaEventRecord(pev[2 * l], s));
-      launch_contrib_gemm<T>(d_fd, d_st, fr, nf, max_cm, s);
+      launch_contrib_gemm<T>(d_fd, d_st, fr, napp, max_app_cm, s);
       run_tc_contrib(f0, f1, s);
       if (profile) CK(cudaEventRecord(pev[2 * l + 1], s));
       pmark(tm(), kPhStats, s);
@@ -1676,8 +1731,11 @@ struct Numeric : NumericBase {
       if (profile) {
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, pev[2 * l], pev[2 * l + 1]));
+        // the contribution launches' fronts (the small-subtree fronts form
+        // theirs inside the level-set kernel)
         double fl = 0;
         for (int f = f0; f < f1; ++f) {
+          if (tpp_front(f)) continue;
           const double cm = hfd[f].cm;
           fl += (double)nelim_[f] * cm * (cm + 1.0);
         }
@@ -1734,6 +1792,20 @@ struct Numeric : NumericBase {
       l21_off[f + 1] = l21_off[f] + (size_t)nblk_of(f) * nch_of(f) * kSolveBlk * kSolveRhs;
     }
     wave_l21p.ensure(std::max<size_t>(l21_off[nn], 1));
+    const bool binv = use_wave && use_binv;
+    std::vector<size_t> binv_off(nn + 1, 0);
+    std::vector<int2> bblocks;
+    if (binv) {
+      for (int f = 0; f < nn; ++f) {
+        binv_off[f + 1] = binv_off[f] + (size_t)nblk_of(f) * kSolveBlk * kSolveBlk;
+        for (int b = 0; b < nblk_of(f); ++b) bblocks.push_back(make_int2(f, b));
+      }
+      wave_binv.ensure(std::max<size_t>(binv_off[nn], 1));
+      binv_blocks.ensure(std::max<size_t>(bblocks.size(), 1));
+      if (!bblocks.empty())
+        CK(cudaMemcpyAsync(binv_blocks.p, bblocks.data(), bblocks.size() * sizeof(int2),
+                           cudaMemcpyHostToDevice, stream));
+    }
     wave_nflags = flag_off[nn];
     wave_flags.ensure(std::max<size_t>(wave_nflags, 1));
     wave_ints.ensure(3);
@@ -1794,6 +1866,7 @@ struct Numeric : NumericBase {
       SolveNode<T>& q = sn[f];
       q.flag = wave_flags.p + flag_off[f];
       q.l21p = wave_l21p.p + l21_off[f];
+      q.binv = binv ? wave_binv.p + binv_off[f] : nullptr;
       q.nblk = nblk_of(f);
       q.ngat = ngat_of(f);
       q.nch = nch_of(f);
@@ -1821,6 +1894,7 @@ struct Numeric : NumericBase {
     d_children = ch_buf.p;
     CK(cudaMemcpyAsync(d_sn, sn.data(), sn.size() * sizeof(SolveNode<T>), cudaMemcpyHostToDevice,
                        stream));
+    if (binv) launch_diag_inv<T>(d_sn, binv_blocks.p, (int)bblocks.size(), stream);
     if (!ch.empty())
       CK(cudaMemcpyAsync(d_children, ch.data(), ch.size() * sizeof(int), cudaMemcpyHostToDevice,
                          stream));
@@ -1833,6 +1907,7 @@ struct Numeric : NumericBase {
     mix((uint64_t)(uintptr_t)xloc.p);
     mix((uint64_t)(uintptr_t)wave_items.p); mix((uint64_t)(uintptr_t)wave_flags.p);
     mix((uint64_t)(uintptr_t)wave_ints.p); mix((uint64_t)(uintptr_t)wave_l21p.p);
+    mix((uint64_t)(uintptr_t)wave_binv.p); mix((uint64_t)binv);
     mix((uint64_t)wave_nfwd); mix((uint64_t)wave_nbwd);
     if (h != solve_sig) drop_graphs();
     solve_sig = h;

@@ -734,8 +734,15 @@ __device__ bool fwd_block(const SolveNode<T>& sn, int code, int nrhs, double* x,
   const int rows = min(SB, (piv ? nelim : m) - r0);
   const int ncb = piv ? code : sn.nblk;
   T own[R][2];  // a pivot block's gathered values, final before any wait below
+  T bv[16];     // with inverses: row r, columns [16 cq, 16 cq + 16) of the block's
   if (piv) {
-    prefetch_diag_block(sn, r0, rows, Lb);
+    if (sn.binv) {
+      const T* bp = sn.binv + (size_t)code * SB * SB + r * SB + cq * 16;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) bv[k] = bp[k];
+    } else {
+      prefetch_diag_block(sn, r0, rows, Lb);
+    }
 #pragma unroll
     for (int rr = 0; rr < R; ++rr) {
       const int q = warp + rr * kSolveWarps;
@@ -777,14 +784,55 @@ __device__ bool fwd_block(const SolveNode<T>& sn, int code, int nrhs, double* x,
     __syncthreads();
   }
   if (!ok) {
-    if (piv) cp_async_wait_all();
+    if (piv && !sn.binv) cp_async_wait_all();
     return false;
   }
   wave_stamp(wl, it, 1);
 #pragma unroll
   for (int q = 0; q < NR; ++q) red[(cq * NR + q) * SB + r] = acc[q];
   __syncthreads();
-  if (piv) {
+  if (piv && sn.binv) {
+    // y = L_bb^{-1} (b - sum): the right-hand side into yb, then the
+    // block inverse's row r times it over column quarter cq, the quarters
+    // added in order
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+      const int q = warp + rr * kSolveWarps;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int row = lane + 32 * g;
+        if (q < NR)
+          yb[row * NR + q] = (q < nrhs && row < rows)
+                                 ? own[rr][g] - (red[q * SB + row] + red[(NR + q) * SB + row] +
+                                                 red[(2 * NR + q) * SB + row] +
+                                                 red[(3 * NR + q) * SB + row])
+                                 : T(0);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+#pragma unroll
+      for (int q = 0; q < NR; ++q) acc[q] += bv[k] * yb[(cq * 16 + k) * NR + q];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) red[(cq * NR + q) * SB + r] = acc[q];
+    __syncthreads();
+    for (int e = tid; e < SB * NR; e += kSolveThreads) {
+      const int row = e % SB, q = e / SB;
+      if (row < rows && q < nrhs) {
+        const T y = red[q * SB + row] + red[(NR + q) * SB + row] + red[(2 * NR + q) * SB + row] +
+                    red[(3 * NR + q) * SB + row];
+        sn.xloc[(int64_t)q * m + r0 + row] = y;
+        double v = (double)y;
+        if (scale_sqrt) v *= sqrt(sn.D[2 * (r0 + row)]);
+        x[(int64_t)q * ldx + sn.perm[r0 + row]] = v;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) st_release(&sn.flag[code], 1);
+  } else if (piv) {
     T xr[R][2];
 #pragma unroll
     for (int rr = 0; rr < R; ++rr) {
@@ -949,7 +997,14 @@ __device__ bool bwd_block(const SolveNode<T>& sn, int b, int nrhs, double* x, in
   const int warp = tid >> 5, lane = tid & 31;
   const int m = sn.m, nelim = sn.nelim;
   const int c0 = b * SB, jb = min(SB, nelim - c0);
-  prefetch_diag_block(sn, c0, jb, Lb);
+  T bv[16];  // with inverses: column c, rows [16 rq, 16 rq + 16) of the block's
+  if (sn.binv) {
+    const T* bp = sn.binv + (size_t)b * SB * SB + (rq * 16) * SB + c;
+#pragma unroll
+    for (int k = 0; k < 16; ++k) bv[k] = bp[k * SB];
+  } else {
+    prefetch_diag_block(sn, c0, jb, Lb);
+  }
   // the block's gathered values (D^{-1} applied), final before any wait
   T own[R][2];
 #pragma unroll
@@ -1022,13 +1077,53 @@ __device__ bool bwd_block(const SolveNode<T>& sn, int b, int nrhs, double* x, in
     __syncthreads();
   }
   if (!ok) {
-    cp_async_wait_all();
+    if (!sn.binv) cp_async_wait_all();
     return false;
   }
   wave_stamp(wl, it, 1);
 #pragma unroll
   for (int q = 0; q < NR; ++q) red[(rq * NR + q) * SB + c] = acc[q];
   __syncthreads();
+  if (sn.binv) {
+    // y = L_bb^{-T} (b - sum): the right-hand side into yb, then column c
+    // of the block inverse times it over row quarter rq, quarters in order
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+      const int q = warp + rr * kSolveWarps;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int col = lane + 32 * g;
+        if (q < NR)
+          yb[col * NR + q] = (q < nrhs && col < jb)
+                                 ? own[rr][g] - (red[q * SB + col] + red[(NR + q) * SB + col] +
+                                                 red[(2 * NR + q) * SB + col] +
+                                                 red[(3 * NR + q) * SB + col])
+                                 : T(0);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
+#pragma unroll
+    for (int k = 0; k < 16; ++k)
+#pragma unroll
+      for (int q = 0; q < NR; ++q) acc[q] += bv[k] * yb[(rq * 16 + k) * NR + q];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) red[(rq * NR + q) * SB + c] = acc[q];
+    __syncthreads();
+    for (int e = tid; e < SB * NR; e += kSolveThreads) {
+      const int col = e % SB, q = e / SB;
+      if (col < jb && q < nrhs) {
+        const T y = red[q * SB + col] + red[(NR + q) * SB + col] + red[(2 * NR + q) * SB + col] +
+                    red[(3 * NR + q) * SB + col];
+        sn.xloc[(int64_t)q * m + c0 + col] = y;
+        x[(int64_t)q * ldx + sn.perm[c0 + col]] = (double)y;
+      }
+    }
+    __syncthreads();
+    if (tid == 0) st_release(&sn.flag[b], 1);
+    return true;
+  }
   T xr[R][2];
 #pragma unroll
   for (int rr = 0; rr < R; ++rr) {
@@ -1116,6 +1211,37 @@ __global__ void __launch_bounds__(kSolveThreads)
     }
     wave_stamp(wl, it, 2);
   }
+}
+
+// Inverse of a 64 x 64 unit lower diagonal block of the FP32 factors,
+// blocks[i] = (front, block): Binv(i, j) for the block's jb x jb part, zero
+// elsewhere, row-major.  64 threads; thread j forms column j by forward
+// substitution in FP32, the factors' precision.
+__global__ void __launch_bounds__(64) k_diag_inv(const SolveNode<float>* sns, const int2* blocks) {
+  using T = float;
+  __shared__ T Ls[SB][SB + 1];  // Ls[r][c] = L(r, c), strictly lower
+  __shared__ T X[SB][SB + 1];
+  const int2 w = blocks[blockIdx.x];
+  const SolveNode<float>& sn = sns[w.x];
+  const int c0 = w.y * SB, jb = min(SB, sn.nelim - c0);
+  const int t = threadIdx.x;
+  for (int e = t; e < SB * SB; e += blockDim.x) {
+    const int r = e % SB, c = e / SB;
+    Ls[r][c] = (r > c && r < jb) ? sn.L[(int64_t)(c0 + c) * sn.ld + c0 + r] : T(0);
+  }
+  for (int i = 0; i < SB; ++i) X[i][t] = T(0);
+  __syncthreads();
+  if (t < jb) {
+    X[t][t] = T(1);
+    for (int i = t + 1; i < jb; ++i) {
+      T acc = T(0);
+      for (int k = t; k < i; ++k) acc += Ls[i][k] * X[k][t];
+      X[i][t] = -acc;
+    }
+  }
+  __syncthreads();
+  T* out = const_cast<T*>(sn.binv) + (size_t)w.y * SB * SB;
+  for (int e = t; e < SB * SB; e += blockDim.x) out[e] = X[e / SB][e % SB];
 }
 
 inline int cdiv(int a, int b) { return (a + b - 1) / b; }
@@ -1257,6 +1383,16 @@ int wave_timeout_probe(int rounds) {
 // item that waits), never more than there are items
 inline int wave_grid(int nitems) { return std::max(1, std::min(nitems, 2 * 152)); }
 
+// FP32 factors only (FP64 factors keep the substitution in the passes)
+template <typename T>
+void launch_diag_inv(const SolveNode<T>* sn, const int2* blocks, int nblocks, cudaStream_t s) {
+  if (nblocks <= 0) return;
+  if constexpr (std::is_same<T, float>::value) {
+    k_diag_inv<<<nblocks, SB, 0, s>>>(sn, blocks);
+    note_launches(1);
+  }
+}
+
 template <typename T>
 void launch_fwd_tree(const SolveNode<T>* sn, const int* children, const int2* pairs,
                      const WaveLevel& wl, int nrhs, double* x, int ldx, bool scale_sqrt,
@@ -1319,7 +1455,8 @@ void solve_init() {
                                    const WaveLevel&, int, double*, int, bool, int*,            \
                                    cudaStream_t);                                              \
   template void launch_bwd_tree<T>(const SolveNode<T>*, const WaveLevel&, double*, int, int,   \
-                                   int, int*, cudaStream_t);
+                                   int, int*, cudaStream_t);                                   \
+  template void launch_diag_inv<T>(const SolveNode<T>*, const int2*, int, cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

@@ -172,12 +172,14 @@ void launch_panel_close(FrontDesc<T>* fd, FrontState* st, const int* fronts, int
 template <typename T>
 void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
                 double u, double small, bool root_only_or_all, cudaStream_t s);
-// fronts of small leaf subtrees: TPP from the first column; max_bytes is
-// the largest shared-memory staging of the listed fronts,
-// ((m + 1) & ~1) * (n + 2) * sizeof(T) + 8 n
+// fronts of small leaf subtrees, one persistent launch: TPP from the first
+// column, then each front's contribution block (LD and C -= L21 LD^T);
+// max_bytes is the dynamic shared memory of the launch (fronts whose
+// staging, ((m + 1) & ~1) * (n + 2) * sizeof(T) + 8 n bytes, exceeds it
+// are factored in place); threads: 32 (one warp per front) or 256
 template <typename T>
-void launch_tpp_small(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
-                      double u, double small, int max_bytes, cudaStream_t s);
+void launch_tpp_level(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
+                      double u, double small, int max_bytes, int threads, cudaStream_t s);
 template <typename T>
 void launch_calc_ld(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int max_cm,
                     int max_n, cudaStream_t s);
@@ -276,6 +278,9 @@ struct SolveNode {
   // the pass
   int* flag;
   T* l21p;           // backward L21^T partial sums: [nblk][nch][64][kSolveRhs]
+  // inverses of the 64 x 64 unit lower diagonal blocks, [nblk][64][64]
+  // row-major (FP32 factors' wavefront passes), or nullptr
+  const T* binv;
   int nblk;          // ceil(nelim / 64) pivot blocks
   int ngat;          // gather items (0: the front is one small item)
   int nch;           // L21^T partial items per pivot block (0: none)
@@ -347,6 +352,10 @@ void launch_fwd_tree(const SolveNode<T>* sn, const int* children, const int2* pa
 template <typename T>
 void launch_bwd_tree(const SolveNode<T>* sn, const WaveLevel& wl, double* x, int ldx, int nrhs,
                      int diag_mode, int* status, cudaStream_t s);
+// the inverses of the 64 x 64 unit lower diagonal blocks blocks[i] =
+// (front, block) into each front's SolveNode::binv
+template <typename T>
+void launch_diag_inv(const SolveNode<T>* sn, const int2* blocks, int nblocks, cudaStream_t s);
 // failure-detection probe of the wavefront solves' bounded flag wait
 // (solve_kernels.cu): -51 when the wait gave up
 int wave_timeout_probe(int rounds);
