@@ -753,6 +753,28 @@ def run_serve(args):
     t_alone = time.perf_counter() - ta
     alone.close()
     same = all(a.error is None and np.array_equal(a.x, b.x) for a, b in zip(res, ref))
+    # where the latency goes: waiting for a slot or memory (admitted -
+    # arrival) against being served (done - admitted), and what the slowest
+    # requests were; the service time alone is each request's time in the
+    # one-at-a-time run
+    ok = [(q, r, a) for q, r, a in zip(reqs, res, ref) if r.error is None and a.error is None]
+    queue_ms = np.array([r.admitted - r.arrival for _, r, _ in ok]) * 1e3
+    service_ms = np.array([r.done - r.admitted for _, r, _ in ok]) * 1e3
+    alone_ms = np.array([a.done - a.admitted for _, _, a in ok]) * 1e3
+
+    def pct(v, p):
+        return float(np.percentile(v, p)) if v.size else None
+
+    slow = sorted(ok, key=lambda t: -(t[1].done - t[1].arrival))[:3]
+    breakdown = {
+        "queue_ms": {"p50": pct(queue_ms, 50), "p99": pct(queue_ms, 99)},
+        "service_ms": {"p50": pct(service_ms, 50), "p99": pct(service_ms, 99)},
+        "service_alone_ms": {"p50": pct(alone_ms, 50), "p99": pct(alone_ms, 99)},
+        "slowest": [{"kind": q.kind, "n": int(q.b.shape[0]), "nrhs": int(q.b.shape[1]),
+                     "latency_ms": (r.done - r.arrival) * 1e3,
+                     "queue_ms": (r.admitted - r.arrival) * 1e3,
+                     "service_ms": (r.done - r.admitted) * 1e3,
+                     "service_alone_ms": (a.done - a.admitted) * 1e3} for q, r, a in slow]}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         import oracle
@@ -790,6 +812,7 @@ def run_serve(args):
                            "same_alone_and_in_mix": bool(same)},
                 "p50_ms": float(np.percentile(lat, 50)) if lat.size else None,
                 "p99_ms": float(np.percentile(lat, 99)) if lat.size else None,
+                "latency_breakdown": breakdown,
                 "alone": {"value": len(reqs) / t_alone, "unit": "requests/s",
                           "note": "same stream, one request at a time, no arrival waits"},
                 "e2e": {"value": len(reqs) / span, "unit": "requests/s",
@@ -975,13 +998,19 @@ def kkt_line(args):
             measure.x_mixed = xu
         else:
             measure.x_fp64 = xu
+        # the statistics that apply after the solves: an FP32-factor handle
+        # whose refinement could not reach the target was refactored in FP64
+        st = _native.ThreadStats()
+        nfb = L.spral_ssids_gpu_fp64_fallbacks(fk.num, ctypes.byref(st))
         out = {"value": 1000.0 / ms, "unit": "solves/s", "ms_per_step": ms,
                "factor_ms": float(fk.timing()[0]),
                "bwd_err": float(M.scaled_bwd_error(ptr, row, val, xu, b).max()),
-               "refine_iters": it.value, "num_neg": fk.inform.num_neg,
-               "num_two": fk.inform.num_two, "num_delay": fk.inform.num_delay,
-               "fp64_fallbacks": fk.fallbacks, "num_flops": fk.inform.num_flops,
+               "refine_iters": it.value, "num_neg": int(st.num_neg),
+               "num_two": int(st.num_two), "num_delay": int(st.num_delay),
+               "fp64_fallbacks": int(nfb), "num_flops": fk.inform.num_flops,
                "gpu_launches": int(L.spral_ssids_gpu_launch_count() - lc0), "clocks": clocks}
+        if nfb > 0:
+            out["fp32_factor_num_neg"] = fk.inform.num_neg
         return fk, out
 
     fm, mixed = measure(ssids.PRECISION_MIXED, args.steps)

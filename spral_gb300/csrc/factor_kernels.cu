@@ -1316,21 +1316,52 @@ struct Decision {
   double d0, d1, d3;
 };
 
-// warp-wide maximum of |a| over a strided set, NaN-free inputs assumed
-__device__ __forceinline__ double wmax(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
 __device__ __forceinline__ bool wall(bool b) { return __all_sync(0xffffffffu, b); }
+
+// Magnitude keys: |v|'s bits as an unsigned integer order non-negative
+// floating-point values (no NaN) as their values do, so the pivot search
+// compares and reduces entries with integer instructions (on GB300 every
+// FP64 instruction, conversions and maxima included, issues slowly) and
+// takes exactly the decisions of the FP64 comparisons it replaces.
+__device__ __forceinline__ unsigned long long mag_key(float v) {
+  return __float_as_uint(v) & 0x7fffffffu;
+}
+__device__ __forceinline__ unsigned long long mag_key(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+}
+template <typename T>
+__device__ __forceinline__ double key_value(unsigned long long k) {
+  if constexpr (sizeof(T) == 4) return (double)__uint_as_float((unsigned)k);
+  else return __longlong_as_double((long long)k);
+}
+// the key below which an entry's magnitude is < s (s >= 0): the key of the
+// smallest T not below s
+template <typename T>
+__device__ __forceinline__ unsigned long long below_key(double s) {
+  if constexpr (sizeof(T) == 4) {
+    float f = (float)s;
+    if ((double)f < s) f = nextafterf(f, INFINITY);
+    return mag_key(f);
+  } else {
+    return mag_key(s);
+  }
+}
+// warp-wide maximum of a key
+template <typename T>
+__device__ __forceinline__ unsigned long long warp_key_max(unsigned long long k) {
+  if constexpr (sizeof(T) == 4) return __reduce_max_sync(0xffffffffu, (unsigned)k);
+  else return warp_max_u64(k);
+}
 
 // all |entries| of row/column idx (row part from `from`) below small
 // (check_col_small, ldlt_tpp.cxx:21-28)
 template <typename T>
 __device__ bool col_small(const T* S, int ld, int idx, int from, int m, double small) {
   const int lane = threadIdx.x & 31;
+  const unsigned long long sk = below_key<T>(small);
   bool ok = true;
-  for (int c = from + lane; c < idx; c += 32) ok = ok && (fabs((double)S[(size_t)c * ld + idx]) < small);
-  for (int r = idx + lane; r < m; r += 32) ok = ok && (fabs((double)S[(size_t)idx * ld + r]) < small);
+  for (int c = from + lane; c < idx; c += 32) ok = ok && (mag_key(S[(size_t)c * ld + idx]) < sk);
+  for (int r = idx + lane; r < m; r += 32) ok = ok && (mag_key(S[(size_t)idx * ld + r]) < sk);
   return wall(ok);
 }
 // largest |entry| of row/column col excluding position excl and the
@@ -1338,27 +1369,26 @@ __device__ bool col_small(const T* S, int ld, int idx, int from, int m, double s
 template <typename T>
 __device__ double rc_max(const T* S, int ld, int col, int nel, int m, int excl) {
   const int lane = threadIdx.x & 31;
-  double v = 0.0;
+  unsigned long long k = 0;
   for (int c = nel + lane; c < col; c += 32)
-    if (c != excl) v = fmax(v, fabs((double)S[(size_t)c * ld + col]));
+    if (c != excl) k = max(k, mag_key(S[(size_t)c * ld + col]));
   for (int r = col + 1 + lane; r < m; r += 32)
-    if (r != excl) v = fmax(v, fabs((double)S[(size_t)col * ld + r]));
-  return wmax(v);
+    if (r != excl) k = max(k, mag_key(S[(size_t)col * ld + r]));
+  return key_value<T>(warp_key_max<T>(k));
 }
 // first column of the largest |a(p, c)|, c in [from, p) (find_row_abs_max)
 template <typename T>
 __device__ int row_argmax(const T* S, int ld, int p, int from) {
   const int lane = threadIdx.x & 31;
-  double bv = -1.0;
+  unsigned long long bk = 0;
   int bi = 0x7fffffff;
   for (int c = from + lane; c < p; c += 32) {
-    const double v = fabs((double)S[(size_t)c * ld + p]);
-    if (v > bv) { bv = v; bi = c; }
+    const unsigned long long k = mag_key(S[(size_t)c * ld + p]);
+    if (k > bk || bi == 0x7fffffff) { bk = k; bi = c; }
   }
-  const double mx = wmax(bv);
-  int cand = (bv == mx) ? bi : 0x7fffffff;
-  for (int o = 16; o > 0; o >>= 1) cand = min(cand, __shfl_xor_sync(0xffffffffu, cand, o));
-  return cand;
+  const unsigned long long mx = warp_key_max<T>(bi == 0x7fffffff ? 0ULL : bk);
+  const unsigned cand = (bi != 0x7fffffff && bk == mx) ? (unsigned)bi : 0x7fffffffu;
+  return (int)__reduce_min_sync(0xffffffffu, cand);
 }
 // symmetric swap of positions i < j over the whole front (swap_cols,
 // ldlt_tpp.cxx:44-72), perm and opos included; warp-wide
@@ -1429,16 +1459,19 @@ __device__ Decision decide(const T* S, int ld, int nel, int m, int n, bool actio
 // largest |v| off the diagonal with their positions; reduced over the CTA
 // in warp order (shuffles, then shared memory), so the result is the same
 // for every thread and every launch shape.
+// Magnitudes are kept as keys (mag_key); an empty record holds key 0 at
+// position 0x7fffffff, which any entry beats.
 struct LineInfo {
   int all_small;
-  double rv; int ri;           // row part: first maximum
-  double v1; int i1;           // off-diagonal: largest ...
-  double v2; int i2;           // ... and second largest (positions differ)
+  unsigned long long rv; int ri;  // row part: first maximum
+  unsigned long long v1; int i1;  // off-diagonal: largest ...
+  unsigned long long v2; int i2;  // ... and second largest (positions differ)
 };
-__device__ __forceinline__ bool better(double va, int ia, double vb, int ib) {
+__device__ __forceinline__ bool better(unsigned long long va, int ia, unsigned long long vb,
+                                       int ib) {
   return va > vb || (va == vb && ia < ib);
 }
-__device__ __forceinline__ void top2_add(LineInfo& a, double v, int i) {
+__device__ __forceinline__ void top2_add(LineInfo& a, unsigned long long v, int i) {
   if (better(v, i, a.v1, a.i1)) { a.v2 = a.v1; a.i2 = a.i1; a.v1 = v; a.i1 = i; }
   else if (better(v, i, a.v2, a.i2)) { a.v2 = v; a.i2 = i; }
 }
@@ -1459,16 +1492,17 @@ __device__ __forceinline__ LineInfo line_shfl(const LineInfo& a, int o) {
 template <typename T>
 __device__ LineInfo line_info(const T* S, int ld, int idx, int nel, int m, double small,
                               LineInfo* sh) {
-  LineInfo a{1, -1.0, 0x7fffffff, -1.0, 0x7fffffff, -1.0, 0x7fffffff};
+  LineInfo a{1, 0, 0x7fffffff, 0, 0x7fffffff, 0, 0x7fffffff};
+  const unsigned long long sk = below_key<T>(small);
   for (int c = nel + (int)threadIdx.x; c < idx; c += blockDim.x) {
-    const double v = fabs((double)S[(size_t)c * ld + idx]);
-    a.all_small = a.all_small && (v < small);
+    const unsigned long long v = mag_key(S[(size_t)c * ld + idx]);
+    a.all_small = a.all_small && (v < sk);
     if (better(v, c, a.rv, a.ri)) { a.rv = v; a.ri = c; }
     top2_add(a, v, c);
   }
   for (int r = idx + (int)threadIdx.x; r < m; r += blockDim.x) {
-    const double v = fabs((double)S[(size_t)idx * ld + r]);
-    a.all_small = a.all_small && (v < small);
+    const unsigned long long v = mag_key(S[(size_t)idx * ld + r]);
+    a.all_small = a.all_small && (v < sk);
     if (r != idx) top2_add(a, v, r);
   }
   for (int o = 1; o < 32; o <<= 1) {
@@ -1489,17 +1523,18 @@ template <typename T>
 __device__ void line_info_batch(const T* S, int ld, int l0, int l1, int nel, int m, double small,
                                 LineInfo* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned long long sk = below_key<T>(small);
   for (int idx = l0 + warp; idx < l1; idx += nw) {
-    LineInfo a{1, -1.0, 0x7fffffff, -1.0, 0x7fffffff, -1.0, 0x7fffffff};
+    LineInfo a{1, 0, 0x7fffffff, 0, 0x7fffffff, 0, 0x7fffffff};
     for (int c = nel + lane; c < idx; c += 32) {
-      const double v = fabs((double)S[(size_t)c * ld + idx]);
-      a.all_small = a.all_small && (v < small);
+      const unsigned long long v = mag_key(S[(size_t)c * ld + idx]);
+      a.all_small = a.all_small && (v < sk);
       if (better(v, c, a.rv, a.ri)) { a.rv = v; a.ri = c; }
       top2_add(a, v, c);
     }
     for (int r = idx + lane; r < m; r += 32) {
-      const double v = fabs((double)S[(size_t)idx * ld + r]);
-      a.all_small = a.all_small && (v < small);
+      const unsigned long long v = mag_key(S[(size_t)idx * ld + r]);
+      a.all_small = a.all_small && (v < sk);
       if (r != idx) top2_add(a, v, r);
     }
     for (int o = 1; o < 32; o <<= 1) {
@@ -1520,11 +1555,9 @@ __device__ bool try_candidate(const T* S, int ld, int p, const LineInfo& lp, con
                               bool action, double u, double small, Decision& d) {
   if (lp.all_small) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return true; }
   const int t = lp.ri;
-  double maxp = (lp.i1 == t) ? lp.v2 : lp.v1;
-  if (maxp < 0) maxp = 0.0;
+  double maxp = key_value<T>((lp.i1 == t) ? lp.v2 : lp.v1);
   // largest |entry| of line t off its diagonal, excluding position p
-  double maxt = (lt.i1 == p) ? lt.v2 : lt.v1;
-  if (maxt < 0) maxt = 0.0;
+  double maxt = key_value<T>((lt.i1 == p) ? lt.v2 : lt.v1);
   const double a11 = (double)S[(size_t)t * ld + t], a21 = (double)S[(size_t)t * ld + p];
   const double a22 = (double)S[(size_t)p * ld + p];
   const double maxpiv = fmax(fabs(a11), fmax(fabs(a21), fabs(a22)));
@@ -1582,7 +1615,7 @@ __device__ Decision decide_cta(const T* S, int ld, int nel, int m, int n, bool a
         return d;
     }
     const LineInfo ln = batch[0];
-    const double maxp = ln.v1 < 0 ? 0.0 : ln.v1;
+    const double maxp = key_value<T>(ln.v1);
     if (fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp) { d.kind = kOne; d.p = nel; }
     return d;
   }
@@ -1593,7 +1626,7 @@ __device__ Decision decide_cta(const T* S, int ld, int nel, int m, int n, bool a
     if (try_candidate(S, ld, p, lp, lt, action, u, small, d)) return d;
   }
   const LineInfo ln = line_info(S, ld, nel, nel, m, small, sh);
-  const double maxp = ln.v1 < 0 ? 0.0 : ln.v1;
+  const double maxp = key_value<T>(ln.v1);
   if (fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp) { d.kind = kOne; d.p = nel; }
   return d;
 }
@@ -1672,32 +1705,34 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
     }
     const int ps = (d.kind == kTwo) ? 2 : 1;
     // scale the pivot column(s) (apply_1x1 / apply_2x2) and update the
-    // trailing fully-summed columns, rows [c, m), with the unscaled copies
+    // trailing fully-summed columns, rows [c, m), with the unscaled copies.
+    // The multipliers are taken in the factor precision (FP32 factors: the
+    // FP32 D^{-1} entries, as the APP path's L columns; D^{-1} itself stays
+    // FP64), so the update issues no FP64 instruction for FP32 factors.
     const int c0 = nel + ps;
+    const T e0 = (T)d.d0, e1 = (T)d.d1, e3 = (T)d.d3;
     if (ps == 1) {
-      const double d11 = d.d0;
-      for (int r = c0 + threadIdx.x; r < m; r += blockDim.x)
-        S[(size_t)nel * ld + r] = (T)((double)W0[r] * d11);
+      for (int r = c0 + threadIdx.x; r < m; r += blockDim.x) S[(size_t)nel * ld + r] = W0[r] * e0;
       for (int c = c0 + warp; c < n; c += nw) {
         const T wc = W0[c];
         T* col = S + (size_t)c * ld;
         for (int r = c + lane; r < m; r += 32) {
-          const T l = (T)((double)W0[r] * d11);
+          const T l = W0[r] * e0;
           col[r] -= l * wc;
         }
       }
     } else {
       for (int r = c0 + threadIdx.x; r < m; r += blockDim.x) {
-        const double a1 = (double)W0[r], a2 = (double)W1[r];
-        S[(size_t)nel * ld + r] = (T)(d.d0 * a1 + d.d1 * a2);
-        S[(size_t)(nel + 1) * ld + r] = (T)(d.d1 * a1 + d.d3 * a2);
+        const T a1 = W0[r], a2 = W1[r];
+        S[(size_t)nel * ld + r] = e0 * a1 + e1 * a2;
+        S[(size_t)(nel + 1) * ld + r] = e1 * a1 + e3 * a2;
       }
       for (int c = c0 + warp; c < n; c += nw) {
         const T w0 = W0[c], w1 = W1[c];
         T* col = S + (size_t)c * ld;
         for (int r = c + lane; r < m; r += 32) {
-          const double a1 = (double)W0[r], a2 = (double)W1[r];
-          const T l1 = (T)(d.d0 * a1 + d.d1 * a2), l2 = (T)(d.d1 * a1 + d.d3 * a2);
+          const T a1 = W0[r], a2 = W1[r];
+          const T l1 = e0 * a1 + e1 * a2, l2 = e1 * a1 + e3 * a2;
           col[r] -= l1 * w0 + l2 * w1;
         }
       }
@@ -1775,14 +1810,27 @@ __device__ void tpp_front_contrib(const FrontDesc<T>& fd, const T* S, int ldS, i
     fd.LD[(int64_t)c * cm + rr] = (T)(alpha * (double)lv + beta * (double)lp);
   }
   __syncthreads();  // LD (global) is read back by other threads of this CTA
+  // lane l of a warp takes rows c + l + 32 t, t < 4, of column c: four
+  // independent sums per k (the FP64 pipe's latency is long) sharing one
+  // load of LD(c, k)
+  constexpr int U = 4;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int c = warp; c < cm; c += nw) {
     const T* ldc = fd.LD + c;
-    for (int r = c + lane; r < cm; r += 32) {
-      const T* lr = S + n + r;
-      T acc = T(0);
-      for (int k = 0; k < nel; ++k) acc += lr[(size_t)k * ldS] * ldc[(int64_t)k * cm];
-      fd.C[(int64_t)c * fd.ldc + r] -= acc;
+    for (int r0 = c + lane; r0 < cm; r0 += 32 * U) {
+      T acc[U];
+#pragma unroll
+      for (int t = 0; t < U; ++t) acc[t] = T(0);
+      for (int k = 0; k < nel; ++k) {
+        const T b = ldc[(int64_t)k * cm];
+        const T* lk = S + (size_t)k * ldS + n;
+#pragma unroll
+        for (int t = 0; t < U; ++t)
+          if (r0 + 32 * t < cm) acc[t] += lk[r0 + 32 * t] * b;
+      }
+#pragma unroll
+      for (int t = 0; t < U; ++t)
+        if (r0 + 32 * t < cm) fd.C[(int64_t)c * fd.ldc + r0 + 32 * t] -= acc[t];
     }
   }
 }
