@@ -374,16 +374,17 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
 }
 
 // ------------------------------------------------------------------------
-// k_app_diag_f32: the indefinite diagonal block for FP32 factors with one
-// barrier per pivot.  Pair ownership, keys and pivot semantics as
-// k_app_diag; the pivot loop is restructured so that no warp waits on a
-// serial decision phase:
-//   * every warp reduces the 17 warp maxima itself (two 32-bit redux.sync
+// k_app_diag_f32<NW>: the indefinite diagonal block for FP32 factors with
+// one barrier per pivot, NW warps.  Pair ownership, keys and pivot
+// semantics as k_app_diag; thread t owns the pairs t, t + 32 NW, ... of the
+// lower triangle (NW = 17: one pair each).  The pivot loop is restructured
+// so that no warp waits on a serial decision phase:
+//   * every warp reduces the NW warp maxima itself (two 32-bit redux.sync
 //     per reduction) and takes the same pivot decision;
 //   * the key of an entry also carries the physical row and column of its
 //     logical column and row, so the decision reads the pivot entries
 //     directly;
-//   * each thread keeps the logical indices of its pair in registers and
+//   * each thread keeps the logical indices of its pairs in registers and
 //     applies the pivot's swaps to them;
 //   * the block, the logical -> physical map and the warp maxima are double
 //     buffered: pivot q reads buffer q&1 and writes the other, and the key
@@ -391,6 +392,11 @@ __global__ void __launch_bounds__(kDiagThreads) k_app_diag(FrontDesc<T>* fds, Fr
 //   * the 2x2 test and the L columns are FP32; D^{-1} is formed in FP64
 //     after the loop, for all pivots at once, from the recorded pivot
 //     entries (the same formulas as k_app_diag).
+// Every pair's update is the same arithmetic whatever NW, and the key
+// maxima do not depend on the grouping, so all NW give the same bits.
+// Fewer warps issue fewer redundant decisions per pivot but chain a
+// thread's pair updates; on GB300 one pair per thread (17 warps) is the
+// fastest.
 // ------------------------------------------------------------------------
 constexpr int kDiagWarps = kDiagThreads / 32;
 
@@ -405,22 +411,32 @@ __device__ __forceinline__ unsigned long long diag_key_f32(float v, int lo, int 
   return (1ULL << 63) | ((unsigned long long)mag << 32) | low;
 }
 
-__global__ void __launch_bounds__(kDiagThreads)
+template <int NW>
+__global__ void __launch_bounds__(NW * 32)
     k_app_diag_f32(FrontDesc<float>* fds, FrontState* sts, const int* fronts, int step,
                    bool action, double small) {
+  constexpr int NT = NW * 32;
+  constexpr int PP = (kDiagPairs + NT - 1) / NT;  // pairs per thread
   const int f = fronts[blockIdx.x];
   FrontState* st = &sts[f];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  int R = (int)((sqrtf(8.0f * tid + 1.0f) - 1.0f) * 0.5f);
-  while ((R + 1) * (R + 2) / 2 <= tid) ++R;
-  while (R * (R + 1) / 2 > tid) --R;
-  const int C = tid - R * (R + 1) / 2;
-  const bool pair = tid < kDiagPairs;
+  int R[PP], C[PP];
+  bool pair[PP];
+#pragma unroll
+  for (int k = 0; k < PP; ++k) {
+    const int e = tid + k * NT;
+    int r = (int)((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
+    while ((r + 1) * (r + 2) / 2 <= e) ++r;
+    while (r * (r + 1) / 2 > e) --r;
+    pair[k] = e < kDiagPairs;
+    R[k] = pair[k] ? r : 0;
+    C[k] = pair[k] ? e - r * (r + 1) / 2 : 0;
+  }
   __shared__ float blk[2][kBlk][kBlk + 1];   // blk[b][c][r] = A(r, c), physical, symmetric
   __shared__ float outb[kBlk][kBlk + 1];     // outb[j][X] = L(inv[X], j)
   __shared__ int map[2][kBlk];               // logical -> physical
   __shared__ int inv[kBlk];                  // physical -> logical (after the loop)
-  __shared__ unsigned long long wkey[2][kDiagWarps];
+  __shared__ unsigned long long wkey[2][NW];
   __shared__ float pv[kBlk][3];              // pivot entries: a11 (1x1: d), a21, a22
   __shared__ int psz[kBlk];                  // 1: 1x1, 2: first of a 2x2, 3: second, 0: zero
   __shared__ double dd[2 * kBlk + 2];
@@ -442,29 +458,40 @@ __global__ void __launch_bounds__(kDiagThreads)
   // FP32 threshold with (bv < fsmall) == ((double)bv < small) for every float bv
   float fsmall = (float)small;
   if ((double)fsmall < small) fsmall = nextafterf(fsmall, INFINITY);
-  const bool mine = pair && R < bs;  // (C <= R < bs)
-  float a = mine ? fd.L[(int64_t)(p + C) * fd.ld + p + R] : 0.f;  // the owned entry
-  if (pair) {
-    blk[0][C][R] = a;
-    blk[0][R][C] = a;
+  float a[PP];  // the owned entries
+  bool mine[PP];
+#pragma unroll
+  for (int k = 0; k < PP; ++k) {
+    mine[k] = pair[k] && R[k] < bs;  // (C <= R < bs)
+    a[k] = mine[k] ? fd.L[(int64_t)(p + C[k]) * fd.ld + p + R[k]] : 0.f;
+    if (pair[k]) {
+      blk[0][C[k]][R[k]] = a[k];
+      blk[0][R[k]][C[k]] = a[k];
+    }
   }
-  for (int e = tid; e < kBlk * (kBlk + 1); e += kDiagThreads) (&outb[0][0])[e] = 0.f;
+  for (int e = tid; e < kBlk * (kBlk + 1); e += NT) (&outb[0][0])[e] = 0.f;
   if (tid < kBlk) {
     map[0][tid] = tid;
     psz[tid] = 0;
   }
   {
-    const unsigned long long k0 = warp_max_u64(mine ? diag_key_f32(a, C, R, C, R) : 0ULL);
+    unsigned long long k0 = 0ULL;
+#pragma unroll
+    for (int k = 0; k < PP; ++k)
+      if (mine[k]) k0 = max(k0, diag_key_f32(a[k], C[k], R[k], C[k], R[k]));
+    k0 = warp_max_u64(k0);
     if (lane == 0) wkey[0][warp] = k0;
   }
-  int li = R, lj = C;  // logical indices of physical R and C
+  int li[PP], lj[PP];  // logical indices of physical R and C
+#pragma unroll
+  for (int k = 0; k < PP; ++k) { li[k] = R[k]; lj[k] = C[k]; }
   int lx = lane;       // warp 0: logical index of physical row `lane`
   int cur = 0;
   bool singular = false;
   for (int q = 0; q < bs;) {
     __syncthreads();
     const int nxt = cur ^ 1;
-    const unsigned long long gk = warp_max_u64(lane < kDiagWarps ? wkey[cur][lane] : 0ULL);
+    const unsigned long long gk = warp_max_u64(lane < NW ? wkey[cur][lane] : 0ULL);
     const unsigned lo32 = (unsigned)gk;
     const int pos = 1023 - (int)(lo32 >> 10);
     const int bj = pos >> 5, bi = pos & 31;                   // logical column, row
@@ -509,14 +536,16 @@ __global__ void __launch_bounds__(kDiagThreads)
       if (pivsiz == 2) x = (x == q + 1) ? i2 : (x == i2) ? q + 1 : x;
       return x;
     };
-    li = relabel(li);
-    lj = relabel(lj);
+#pragma unroll
+    for (int k = 0; k < PP; ++k) { li[k] = relabel(li[k]); lj[k] = relabel(lj[k]); }
     const int qn = q + pivsiz;
-    const int lo = min(li, lj), hi = max(li, lj);
     if (pivsiz == 1) {
       const int P = pb;
       const float dT = __frcp_rn(blk[cur][P][P]);
-      if (mine && lo >= qn) a = a - blk[cur][P][R] * (blk[cur][P][C] * dT);
+#pragma unroll
+      for (int k = 0; k < PP; ++k)
+        if (mine[k] && min(li[k], lj[k]) >= qn)
+          a[k] = a[k] - blk[cur][P][R[k]] * (blk[cur][P][C[k]] * dT);
       if (warp == 0) {
         lx = relabel(lx);
         if (lane < bs && lx > q) outb[q][lane] = blk[cur][P][lane] * dT;
@@ -527,10 +556,13 @@ __global__ void __launch_bounds__(kDiagThreads)
       }
     } else {
       const int P1 = pb, P2 = ci2;
-      if (mine && lo >= qn) {
-        const float v1 = blk[cur][P1][C], v2 = blk[cur][P2][C];
-        a = a - (blk[cur][P1][R] * (e11 * v1 + e21 * v2) + blk[cur][P2][R] * (e21 * v1 + e22 * v2));
-      }
+#pragma unroll
+      for (int k = 0; k < PP; ++k)
+        if (mine[k] && min(li[k], lj[k]) >= qn) {
+          const float v1 = blk[cur][P1][C[k]], v2 = blk[cur][P2][C[k]];
+          a[k] = a[k] - (blk[cur][P1][R[k]] * (e11 * v1 + e21 * v2) +
+                         blk[cur][P2][R[k]] * (e21 * v1 + e22 * v2));
+        }
       if (warp == 0) {
         lx = relabel(lx);
         if (lane < bs && lx > q + 1) {
@@ -547,15 +579,19 @@ __global__ void __launch_bounds__(kDiagThreads)
         pv[q][2] = a22;
       }
     }
-    if (pair) {
-      blk[nxt][C][R] = a;
-      blk[nxt][R][C] = a;
+    unsigned long long key = 0ULL;
+#pragma unroll
+    for (int k = 0; k < PP; ++k) {
+      if (pair[k]) {
+        blk[nxt][C[k]][R[k]] = a[k];
+        blk[nxt][R[k]][C[k]] = a[k];
+      }
+      const int lo = min(li[k], lj[k]), hi = max(li[k], lj[k]);
+      if (mine[k] && lo >= qn)
+        key = max(key, diag_key_f32(a[k], lo, hi, li[k] <= lj[k] ? R[k] : C[k],
+                                    li[k] <= lj[k] ? C[k] : R[k]));
     }
-    const unsigned long long k =
-        (mine && lo >= qn)
-            ? diag_key_f32(a, lo, hi, li <= lj ? R : C, li <= lj ? C : R)
-            : 0ULL;
-    const unsigned long long wk = warp_max_u64(k);
+    const unsigned long long wk = warp_max_u64(key);
     if (lane == 0) wkey[nxt][warp] = wk;
     if (warp == 0) {
       int v = mp[lane];
@@ -597,7 +633,7 @@ __global__ void __launch_bounds__(kDiagThreads)
   __syncthreads();
   // ---- write L11 (logical lower part, unit diagonal), D, step buffer, perm
   const int* fmap = map[cur];
-  for (int e = tid; e < kBlk * kBlk; e += kDiagThreads) {
+  for (int e = tid; e < kBlk * kBlk; e += NT) {
     const int j = e >> 5, X = e & 31;  // logical column, physical row
     if (j < bs && X < bs) {
       const int i = inv[X];
@@ -1810,27 +1846,14 @@ __device__ void tpp_front_contrib(const FrontDesc<T>& fd, const T* S, int ldS, i
     fd.LD[(int64_t)c * cm + rr] = (T)(alpha * (double)lv + beta * (double)lp);
   }
   __syncthreads();  // LD (global) is read back by other threads of this CTA
-  // lane l of a warp takes rows c + l + 32 t, t < 4, of column c: four
-  // independent sums per k (the FP64 pipe's latency is long) sharing one
-  // load of LD(c, k)
-  constexpr int U = 4;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int c = warp; c < cm; c += nw) {
     const T* ldc = fd.LD + c;
-    for (int r0 = c + lane; r0 < cm; r0 += 32 * U) {
-      T acc[U];
-#pragma unroll
-      for (int t = 0; t < U; ++t) acc[t] = T(0);
-      for (int k = 0; k < nel; ++k) {
-        const T b = ldc[(int64_t)k * cm];
-        const T* lk = S + (size_t)k * ldS + n;
-#pragma unroll
-        for (int t = 0; t < U; ++t)
-          if (r0 + 32 * t < cm) acc[t] += lk[r0 + 32 * t] * b;
-      }
-#pragma unroll
-      for (int t = 0; t < U; ++t)
-        if (r0 + 32 * t < cm) fd.C[(int64_t)c * fd.ldc + r0 + 32 * t] -= acc[t];
+    for (int r = c + lane; r < cm; r += 32) {
+      const T* lr = S + n + r;
+      T acc = T(0);
+      for (int k = 0; k < nel; ++k) acc += lr[(size_t)k * ldS] * ldc[(int64_t)k * cm];
+      fd.C[(int64_t)c * fd.ldc + r] -= acc;
     }
   }
 }
@@ -2003,6 +2026,15 @@ void launch_syrk_contrib(FrontDesc<T>* fd, const FrontState* st, const int* fron
 
 static inline int cdiv(int a, int b) { return (a + b - 1) / b; }
 
+// warps of the FP32 diagonal-block kernel: 17 (one pair per thread; the
+// fastest on GB300: 24.8 ms per 48^3 mixed step against 25.9 with 8 warps
+// and 27.0 with 4), or 8 or 4 through SPRAL_GB300_DIAG_WARPS
+static int diag_f32_warps() {
+  const char* e = getenv("SPRAL_GB300_DIAG_WARPS");
+  const int v = e ? atoi(e) : 17;
+  return (v == 4 || v == 8) ? v : 17;
+}
+
 template <typename T>
 void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int step,
                      int max_rows, int max_trail_rows, int max_trail_cols, bool action,
@@ -2012,7 +2044,14 @@ void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf
   if (posdef) {
     launch_pdl(k_app_diag<T, true>, nf, kDiagThreads, 0, s, fd, st, fronts, step, action, small);
   } else if constexpr (std::is_same<T, float>::value) {
-    launch_pdl(k_app_diag_f32, nf, kDiagThreads, 0, s, fd, st, fronts, step, action, small);
+    const int nw = diag_f32_warps();
+    if (nw == 4)
+      launch_pdl(k_app_diag_f32<4>, nf, 4 * 32, 0, s, fd, st, fronts, step, action, small);
+    else if (nw == 8)
+      launch_pdl(k_app_diag_f32<8>, nf, 8 * 32, 0, s, fd, st, fronts, step, action, small);
+    else
+      launch_pdl(k_app_diag_f32<kDiagWarps>, nf, kDiagThreads, 0, s, fd, st, fronts, step, action,
+                 small);
   } else {
     launch_pdl(k_app_diag<T, false>, nf, kDiagThreads, 0, s, fd, st, fronts, step, action, small);
   }

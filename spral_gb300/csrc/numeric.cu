@@ -1475,12 +1475,12 @@ struct Numeric : NumericBase {
     {
       const char* gr = getenv("SPRAL_GB300_GRAPHS");
       use_graphs = !(gr && gr[0] == '0');
-      // wavefront solves for FP32 factors; FP64 factors keep the block-step
-      // chain, which spreads each step's FP64 update over many SMs (in a
-      // wave a pivot block's FP64 products stay in one CTA, about 9 us per
-      // 64 x 64 tile for 8 right-hand sides on GB300's FP64 pipe)
+      // wavefront solves (one persistent launch per pass over the tree);
+      // SPRAL_GB300_SOLVE_WAVE=0 selects the per-level block-step chain
+      // (48^3 Laplacian, 8 right-hand sides, FP64 factors: 6.1 ms per pass
+      // against 7.3 ms)
       const char* wv = getenv("SPRAL_GB300_SOLVE_WAVE");
-      use_wave = wv ? wv[0] != '0' : std::is_same<T, float>::value;
+      use_wave = !(wv && wv[0] == '0');
       const char* wt = getenv("SPRAL_GB300_WAVE_TRACE");
       if (wt && *wt) wave_trace = wt;
       const char* bi = getenv("SPRAL_GB300_SOLVE_BINV");

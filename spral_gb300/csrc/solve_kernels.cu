@@ -707,10 +707,42 @@ template <typename T, int NR>
 __device__ __forceinline__ void bwd_gather_rows(const SolveNode<T>& sn, const double* x, int ldx,
                                                 int nrhs, int diag_mode, int r0, int r1) {
   for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+    // the row's pivot positions and D^{-1} coefficients once, then every
+    // right-hand side's loads together (the arithmetic of bwd_gather_value)
+    const int src = (i < sn.n) ? sn.perm[i] : sn.rows[sn.ncol + i - sn.n];
+    int src2 = -1;      // the other half of a 2x2 block
+    double ca = 1.0, cb = 0.0;  // v = ca x(src) + cb x(src2)
+    if (diag_mode == 2 && i < sn.nelim) {
+      ca = sqrt(sn.D[2 * i]);
+    } else if (diag_mode == 1 && i < sn.nelim) {
+      const double di = sn.D[2 * i];
+      if (isinf(di)) {
+        src2 = sn.perm[i - 1];
+        ca = sn.D[2 * i + 1];
+        cb = sn.D[2 * (i - 1) + 1];
+      } else if (i + 1 < sn.nelim && isinf(sn.D[2 * i + 2])) {
+        src2 = sn.perm[i + 1];
+        ca = di;
+        cb = sn.D[2 * i + 1];
+      } else {
+        ca = di;
+      }
+    }
+    double v[NR], w[NR];
 #pragma unroll
-    for (int q = 0; q < NR; ++q)
-      if (q < nrhs)
-        sn.xloc[(int64_t)q * sn.m + i] = (T)bwd_gather_value<true>(sn, x, ldx, diag_mode, q, i);
+    for (int q = 0; q < NR; ++q) {
+      v[q] = (q < nrhs) ? __ldcg(&x[(int64_t)q * ldx + src]) : 0.0;
+      w[q] = (q < nrhs && src2 >= 0) ? __ldcg(&x[(int64_t)q * ldx + src2]) : 0.0;
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      if (q >= nrhs) continue;
+      double r;
+      if (src2 < 0) r = (diag_mode == 0 || i >= sn.nelim) ? v[q] : ca * v[q];
+      else if (isinf(sn.D[2 * i])) r = cb * w[q] + ca * v[q];   // d21 x1 + d22 x2
+      else r = ca * v[q] + cb * w[q];                           // di x + d21 x2
+      sn.xloc[(int64_t)q * sn.m + i] = (T)r;
+    }
   }
 }
 
@@ -883,7 +915,7 @@ __device__ bool fwd_block(const SolveNode<T>& sn, int code, int nrhs, double* x,
 
 // Forward pass over the whole tree (item list and waits: see WaveLevel).
 template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveThreads)
+__global__ void __launch_bounds__(kSolveThreads, 2)
     k_fwd_tree(const SolveNode<T>* sns, const int* children, const int2* pairs, WaveLevel wl,
                int nrhs, double* x, int ldx, bool scale_sqrt, int* status) {
   extern __shared__ __align__(16) unsigned char solve_smem[];
@@ -959,13 +991,14 @@ __device__ void bwd_l21_item(const SolveNode<T>& sn, int t, int nrhs, T* xs, T* 
 #pragma unroll
   for (int q = 0; q < NR; ++q) acc[q] = T(0);
   const T* Lp = sn.L + (int64_t)(c0 + col) * sn.ld + R0 + rq * 64;
-  for (int kb = 0; kb < 64; kb += 16) {
-    T lv[16];
+  // two batches of 32 loads in flight: the item is bound by their latency
+  for (int kb = 0; kb < 64; kb += 32) {
+    T lv[32];
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
+    for (int k = 0; k < 32; ++k)
       lv[k] = (col < jb && rq * 64 + kb + k < nr) ? Lp[kb + k] : T(0);
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
+    for (int k = 0; k < 32; ++k)
 #pragma unroll
       for (int q = 0; q < NR; ++q) acc[q] += lv[k] * xs[(rq * 64 + kb + k) * NR + q];
   }
@@ -1162,7 +1195,7 @@ __device__ bool bwd_block(const SolveNode<T>& sn, int b, int nrhs, double* x, in
 
 // Backward pass over the whole tree (item list and waits: see WaveLevel).
 template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveThreads)
+__global__ void __launch_bounds__(kSolveThreads, 2)
     k_bwd_tree(const SolveNode<T>* sns, WaveLevel wl, int nrhs, double* x, int ldx, int diag_mode,
                int* status) {
   extern __shared__ __align__(16) unsigned char solve_smem[];

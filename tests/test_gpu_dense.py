@@ -64,3 +64,31 @@ def test_gpu_dense_ldlt_app_bwd_error(m, n, delays, singular, seed):
     b = a @ np.ones(m)  # consistent right-hand side (solution of ones), as gen_rhs
     x = full_solve(m, q1, l, d, perm, b)
     assert backward_error(a, x, b) <= 1e-13
+
+
+@pytest.mark.parametrize("case", ["lap3d", "kkt"])
+@pytest.mark.parametrize("warps", ["4", "8", "17"])
+def test_gpu_fp32_diag_block_warp_counts_agree(warps, case, monkeypatch):
+    """The FP32 diagonal-block kernel with 4, 8 or 17 warps (pairs per
+    thread 5, 3, 1) takes the same pivots and gives the same bits (fronts
+    above the small leaf subtrees, so the APP block steps run)."""
+    import numpy as np
+    from spral_gb300 import matrices as M, ssids
+    if case == "lap3d":
+        p, r, v = M.laplacian_3d(20, shift=-0.3)
+        ak = ssids.analyse(p, r, M.nd_order_grid(20, 20, 20))
+    else:
+        p, r, v = M.kkt(4000, 2000, seed=5)
+        ak = ssids.analyse(p, r, ssids.order_amd(p, r))
+    b = np.random.default_rng(3).standard_normal((len(p) - 1, 2))
+    opts = ssids.Options(precision=ssids.PRECISION_MIXED)
+    monkeypatch.setenv("SPRAL_GB300_DIAG_WARPS", "17")
+    f0, i0 = ssids.factor(ak, v, opts)
+    x0 = f0.solve(b)
+    monkeypatch.setenv("SPRAL_GB300_DIAG_WARPS", warps)
+    f1, i1 = ssids.factor(ak, v, opts)
+    x1 = f1.solve(b)
+    assert (i1.num_neg, i1.num_two, i1.num_delay) == (i0.num_neg, i0.num_two, i0.num_delay)
+    assert np.array_equal(x0, x1)
+    f0.free()
+    f1.free()

@@ -30,7 +30,7 @@ def test_gpu_wave_solves_match_block_steps(case, precision, tol, monkeypatch):
         ak = ssids.analyse(p, r, ssids.order_amd(p, r))
     n = len(p) - 1
     opts = ssids.Options(precision=precision)
-    monkeypatch.setenv("SPRAL_GB300_SOLVE_WAVE", "1")  # FP64 factors default to the steps
+    monkeypatch.setenv("SPRAL_GB300_SOLVE_WAVE", "1")
     fw, infw = ssids.factor(ak, v, opts)
     monkeypatch.setenv("SPRAL_GB300_SOLVE_WAVE", "0")
     fs, infs = ssids.factor(ak, v, opts)
