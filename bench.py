@@ -580,9 +580,10 @@ def run_batch(args):
     """One step = numeric factorisation of every matrix of the batch plus the
     solve of each one's right-hand side, refined in FP64 until every matrix's
     own scaled backward error is <= 1e-14.  Measured with FP64 factors
-    (`value`) and with FP32 factors (`mixed`): the batch is one handle, so
-    when FP32 factors cannot reach the target for some of its matrices (a
-    shift near an eigenvalue) the whole batch is refactored in FP64."""
+    (`value`) and with FP32 factors (`mixed`): at most 4 refinement steps,
+    after which the matrices still above the target (shifts near an
+    eigenvalue, too ill-conditioned for FP32 factors) are factored and
+    solved again in FP64 as a sub-batch (BatchFkeep's per-matrix fallback)."""
     import torch
     world, rank, local = dist_setup(args)
     torch.cuda.set_device(local)
@@ -599,19 +600,17 @@ def run_batch(args):
     bp_d = torch.tensor(np.ascontiguousarray(B[invp, 0]), dtype=torch.float64, device=dev)
     x_d = torch.empty_like(bp_d)
 
-    def measure(precision):
+    def measure(precision, max_refine):
         bf = batch.BatchFkeep(bak, [v for _, _, v in mats],
-                              ssids.Options(precision=precision, max_refine=10,
+                              ssids.Options(precision=precision, max_refine=max_refine,
                                             refine_tol=REFINE_TOL))
         it = ctypes.c_int(0)
-        bw = ctypes.c_double(0)
 
         def step():
-            bf.fk.refactor_dev(vals_d.data_ptr())
+            bf.refactor_dev(vals_d.data_ptr())
             # solve plus FP64 refinement of the whole batch to bwd err <= 1e-14
-            L.spral_ssids_gpu_solve_refined_dev(bf.fk.num, 1, ctypes.c_void_p(bp_d.data_ptr()),
-                                                ctypes.c_void_p(x_d.data_ptr()), n,
-                                                ctypes.byref(it), ctypes.byref(bw))
+            # (FP32 factors: the matrices that miss it are refactored in FP64)
+            it.value = bf.solve_refined_dev(bp_d, x_d)
 
         for _ in range(args.warmup):
             step()
@@ -650,11 +649,13 @@ def run_batch(args):
                 e2e_t.append(time.perf_counter() - t0)
         e2e_ms = 1000.0 * sum(e2e_t) / len(e2e_t)
         fb = bf.fk.fallbacks
+        nfail = int(bf.failed.size)
         bf.free()
         return {"value": world * args.batch_count * 1000.0 / ms, "unit": "matrices/s",
                 "ms_per_step": ms, "p50_ms": float(np.percentile(per, 50)),
                 "p99_ms": float(np.percentile(per, 99)), "bwd_err": bwd,
                 "refine_iters": it.value, "inertia_exact": bool(exact), "fp64_fallbacks": fb,
+                "matrices_refactored_in_fp64": nfail,
                 "gpu_launches": int(launches), "clocks": clocks,
                 "e2e": {"value": args.batch_count * 1000.0 / e2e_ms, "unit": "matrices/s",
                         "h2d_bytes_per_step": int(vals.nbytes + n * 8),
@@ -662,8 +663,8 @@ def run_batch(args):
                         "path": "BatchFkeep.refactor + BatchFkeep.solve_refined (host values "
                                 "and RHS)"}}
 
-    fp64 = measure(ssids.PRECISION_FP64)
-    mixed = measure(ssids.PRECISION_MIXED)
+    fp64 = measure(ssids.PRECISION_FP64, 10)
+    mixed = measure(ssids.PRECISION_MIXED, 4)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         import oracle

@@ -63,7 +63,13 @@ struct spral_ssids_gpu_options {
   double refine_tol;
   int small_front_cols;
   int use_graph;
-  int reserved[8];
+  /* 1: an FP32-factor handle whose refined solve cannot reach refine_tol
+   * returns its best refined solution instead of refactoring the matrix in
+   * FP64 (the caller handles the rest, e.g. the matrices of a batch that
+   * missed the target, spral_ssids_gpu_group_bwd_errors); 0: the default
+   * FP64 fallback */
+  int no_fp64_fallback;
+  int reserved[7];
 };
 
 /* Replaces construct_gpu_symbolic_subtree (src/ssids/gpu/subtree.f90:76);
@@ -307,6 +313,13 @@ int spral_ssids_gpu_tc_crossover(void);
  * CUDA error.  No reference counterpart (the reference's kernel shapes are
  * fixed at compile time). */
 int spral_ssids_gpu_tune_table(int* out, int nout);
+
+/* The scaled backward error of each row group (spral_ssids_gpu_set_row_groups:
+ * e.g. the matrices of a batch) after the last refined solve of the handle,
+ * the largest over the right-hand sides of its last chunk of 16.  out holds
+ * ngroups values.  Returns 0, -1 without row groups or refined solve, -51 on
+ * a CUDA error.  No reference counterpart. */
+int spral_ssids_gpu_group_bwd_errors(const void* numeric, double* out, int ngroups);
 
 /* The current device's key in the tune cache (device name with '_' for
  * spaces, "-sm<multiprocessors>-cc<major><minor>").  Returns its length, or

@@ -54,7 +54,8 @@ class ThreadStats(ctypes.Structure):
 class GpuOptions(ctypes.Structure):
     """Out-of-band options of the GPU path (``struct spral_ssids_gpu_options``)."""
     _fields_ = [("precision", I), ("max_refine", I), ("refine_tol", D),
-                ("small_front_cols", I), ("use_graph", I), ("reserved", I * 8)]
+                ("small_front_cols", I), ("use_graph", I), ("no_fp64_fallback", I),
+                ("reserved", I * 7)]
 
 
 def _declare(L):
@@ -110,6 +111,7 @@ def _declare(L):
     f("spral_ssids_gpu_tc_gemm_f32", I, I, I, I, P, I, P, I, P, I, I, I, I, P)
     f("spral_ssids_gpu_tc_gemm_f32_bn", I, I, I, I, P, I, P, I, P, I, I, I, I, P, I)
     f("spral_ssids_gpu_tune_table", I, P, I)
+    f("spral_ssids_gpu_group_bwd_errors", I, P, P, I)
     f("spral_ssids_gpu_tune_device_key", I, ctypes.c_char_p, I)
     f("spral_ssids_gpu_tune_parse", I, ctypes.c_char_p, ctypes.c_char_p, I, P, I)
     f("spral_ssids_gpu_tune_format", I, ctypes.c_char_p, P, I, ctypes.c_char_p, I)

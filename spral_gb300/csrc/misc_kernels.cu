@@ -51,7 +51,6 @@ constexpr int kResQC = 4;
 // With row groups (row_group != nullptr: the group of each row, e.g. the
 // matrix of a batch it belongs to) the maxima are kept per group, at
 // work[g * kResStride ...], so the backward error can be judged per group.
-constexpr int kResStride = 1 + 3 * kSolveRhs;
 __global__ void __launch_bounds__(256) k_resid_norms(const int64_t* aptr, const int* acol,
                                                      const int64_t* asrc, const double* aval,
                                                      int n, const double* x, const double* b,

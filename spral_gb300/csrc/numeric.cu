@@ -645,6 +645,8 @@ struct NumericBase {
   virtual Symbolic* symbolic() = 0;
   virtual int debug_front(int node, int* info, double* L, double* D, int* perm) = 0;
   virtual int node_inertia(int* out) = 0;
+  // per row group, the scaled backward error of the last refined solve
+  virtual int group_bwd_errors(double* out, int ngroups) = 0;
   virtual cudaStream_t get_stream() const = 0;
   virtual int get_contrib() = 0;
   // the subtree root's contribution for a parent outside the subtree, host
@@ -2100,6 +2102,7 @@ struct Numeric : NumericBase {
   // target was met).
   NumericBase* fp64_fallback() {
     if (!std::is_same<T, float>::value) return nullptr;
+    if (S->gopts.no_fp64_fallback) return nullptr;
     if (!(last_bwd_err > S->gopts.refine_tol)) return nullptr;
     if (!fb) {
       fb.reset(new Numeric<double>(S));
@@ -2130,6 +2133,8 @@ struct Numeric : NumericBase {
     std::vector<double> h(q);
     int it = 0;
     const int maxit = S->gopts.max_refine;
+    last_refine_q = q;
+    group_prev.clear();
     for (;; ++it) {
       pmark(tm(), kPhResid, s);
       launch_resid_bwd_err(S->d_aptr, S->d_acol, S->d_asrc, cur_aval, n, x, b, rbuf.p, q, ld,
@@ -2141,8 +2146,22 @@ struct Numeric : NumericBase {
       double worst = 0;
       for (int r = 0; r < q; ++r) worst = std::max(worst, h[r]);
       // stop at the target, after max_refine steps, or when a step did not
-      // halve the backward error (the factors' precision cannot reach it)
-      const bool stalled = it > 0 && !(worst < 0.5 * last_bwd_err);
+      // halve the backward error (the factors' precision cannot reach it).
+      // Row groups whose caller handles the misses itself (no FP64
+      // fallback): stalled only once no group above the target halved its
+      // own error, so the other groups finish their refinement.
+      bool stalled = it > 0 && !(worst < 0.5 * last_bwd_err);
+      if (S->d_row_group && S->gopts.no_fp64_fallback && worst > S->gopts.refine_tol) {
+        last_refine_q = q;
+        std::vector<double> ge(S->ngroups);
+        group_bwd_errors(ge.data(), S->ngroups);
+        if (it > 0 && group_prev.size() == ge.size()) {
+          stalled = true;
+          for (size_t g = 0; g < ge.size() && stalled; ++g)
+            if (ge[g] > S->gopts.refine_tol && ge[g] < 0.5 * group_prev[g]) stalled = false;
+        }
+        group_prev.swap(ge);
+      }
       last_bwd_err = worst;
       if (!(worst > S->gopts.refine_tol) || it >= maxit || stalled) break;
       solve_dev(0, q, rbuf.p, ld, nullptr);
@@ -2154,6 +2173,25 @@ struct Numeric : NumericBase {
   }
 
   cudaStream_t get_stream() const override { return stream; }
+
+  int last_refine_q = 0;  // right-hand sides of the last refinement's residuals in nbuf
+  std::vector<double> group_prev;  // per row group, the previous refinement step's error
+  int group_bwd_errors(double* out, int ngroups) override {
+    if (!S->d_row_group || last_refine_q <= 0 || ngroups != S->ngroups) return -1;
+    std::vector<double> w((size_t)ngroups * kResStride);
+    CK(cudaMemcpy(w.data(), nbuf.p + last_refine_q, w.size() * sizeof(double),
+                  cudaMemcpyDeviceToHost));
+    for (int g = 0; g < ngroups; ++g) {
+      const double* wg = w.data() + (size_t)g * kResStride;
+      double e = 0.0;
+      for (int r = 0; r < last_refine_q; ++r) {
+        const double den = wg[0] * wg[1 + 3 * r] + wg[2 + 3 * r];
+        e = std::max(e, den > 0 ? wg[3 + 3 * r] / den : 0.0);
+      }
+      out[g] = e;
+    }
+    return 0;
+  }
 
   int node_inertia(int* out) override {
     CK(cudaMemcpy(out, d_ncount, 3 * (size_t)S->nnodes * sizeof(int), cudaMemcpyDeviceToHost));
@@ -2578,6 +2616,16 @@ int spral_ssids_gpu_tc_crossover(void) {
 /* The autotuner's table for the current device (measured on first use, or
  * read from the tune cache): out = [tc_min_cm, nb, m_0, bn_0, ...].  Returns
  * the number of ints written, -1 if nout is too small, -51 on a CUDA error. */
+int spral_ssids_gpu_group_bwd_errors(const void* numeric, double* out, int ngroups) {
+  auto* N = const_cast<NumericBase*>(static_cast<const NumericBase*>(numeric));
+  if (!N || !out || ngroups <= 0) return -1;
+  try {
+    return N->group_bwd_errors(out, ngroups);
+  } catch (...) {
+    return -51;
+  }
+}
+
 int spral_ssids_gpu_tune_table(int* out, int nout) {
   try {
     const ssids300::TuneTable t = ssids300::autotune_device();

@@ -333,6 +333,9 @@ struct WaveLevel {
 
 constexpr int kSolveBlk = 64;   // diagonal block of the blocked triangular solves
 constexpr int kSolveRhs = 16;   // right-hand sides per pass
+// doubles per row group in the refinement's residual workspace: ||A||, then
+// (||x||, ||b||, ||r||) per right-hand side of a pass
+constexpr int kResStride = 1 + 3 * kSolveRhs;
 
 template <typename T>
 void launch_fwd_gather(const SolveNode<T>* sn, const int* nodes, int nn, const int* children,

@@ -52,6 +52,7 @@ class Options:
     max_refine: int = 10
     refine_tol: float = 1e-15
     small_front_cols: int = 0      # 0 = library default
+    fp64_fallback: bool = True     # FP32 factors that cannot reach refine_tol: refactor in FP64
 
     def cpu_options(self):
         return CpuFactorOptions(print_level=self.print_level, action=self.action, small=self.small,
@@ -66,6 +67,7 @@ class Options:
         g.refine_tol = self.refine_tol
         g.small_front_cols = self.small_front_cols
         g.use_graph = 0
+        g.no_fp64_fallback = 0 if self.fp64_fallback else 1
         return g
 
 

@@ -93,3 +93,36 @@ def test_gpu_batch_refined_meets_target_per_matrix(precision):
                 for i, (p, r, v) in enumerate(mats))
     assert worst <= 1e-14
     bf.free()
+
+
+def test_gpu_mixed_batch_falls_back_per_matrix():
+    """A batch of FP32 factors in which one matrix is too ill-conditioned for
+    FP32 (a shifted 2D Laplacian with an eigenvalue 3e-9 from zero): only
+    that matrix is refactored in FP64 (a sub-batch of its own), every
+    matrix's refined solve meets 1e-14, the inertia is exact for all, and a
+    refactorisation with the same values repeats the same fallback."""
+    nx, ny = 30, 34
+    lam = (2 - 2 * np.cos(np.pi * 3 / (nx + 1))) + (2 - 2 * np.cos(np.pi * 5 / (ny + 1)))
+    bad_shift = 3e-9 - lam
+    specs = [(12, 12, -0.4), (nx, ny, bad_shift), (20, 17, -0.7), (9, 25, -0.2)]
+    mats = [M.laplacian_2d(a, b, s) for a, b, s in specs]
+    bak = batch.BatchAkeep([(p, r) for p, r, _ in mats],
+                           [M.nd_order_grid(a, b) for a, b, _ in specs])
+    opts = ssids.Options(precision=ssids.PRECISION_MIXED, max_refine=20, refine_tol=1e-14)
+    bf = batch.BatchFkeep(bak, [v for _, _, v in mats], opts)
+    rng = np.random.default_rng(8)
+    bs = [rng.uniform(-1, 1, (a * b, 2)) for a, b, _ in specs]
+    xs = bf.solve_refined(bs)
+    assert list(bf.failed) == [1]
+    assert bf.fk.fallbacks == 0  # the batch handle itself never refactors in FP64
+    for (p, r, v), x, b in zip(mats, xs, bs):
+        assert M.scaled_bwd_error(p, r, v, x, b).max() <= 1e-14
+    inert = bf.inertia()
+    for i, (a, b, s) in enumerate(specs):
+        assert inert[i, 0] == M.laplacian_eig_count_2d(a, b, s)[0]
+    bf.refactor([v for _, _, v in mats])
+    xs2 = bf.solve_refined(bs)
+    assert list(bf.failed) == [1] and bf.fallback_matrices == 2
+    for x, x2 in zip(xs, xs2):
+        assert np.array_equal(x, x2)
+    bf.free()
