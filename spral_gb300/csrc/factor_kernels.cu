@@ -1449,20 +1449,18 @@ __device__ void sym_swap(T* S, int ld, int m, int i, int j, int* perm, int* opos
   }
   __syncwarp();
 }
-// the pivot search of one step of ldlt_tpp_factor, in warp 0
+// The 2x2 test of (t, p) (test_2x2, ldlt_tpp.cxx:95-126), then the 1x1
+// test of p (ldlt_tpp.cxx:216-236): true with d set when p is taken.  FP64
+// factors: FP64 arithmetic as the reference.  FP32 factors: FP32 arithmetic,
+// as the FP32 APP block takes its 2x2 test, so the serial search issues no
+// FP64 instruction (on GB300 a division alone is a long chain of slow FP64
+// instructions); D^{-1} of the chosen pivots is formed in FP64 afterwards
+// (tpp_finish_d), and d0..d3 here only scale the L columns.
 template <typename T>
-__device__ Decision decide(const T* S, int ld, int nel, int m, int n, bool action, double u,
-                           double small) {
-  Decision d{kStop, 0, 0, 0.0, 0.0, 0.0};
-  if (col_small(S, ld, nel, nel, m, small)) { d.kind = action ? kZeroNel : kSingular; return d; }
-  for (int p = nel + 1; p < n; ++p) {
-    if (col_small(S, ld, p, nel, m, small)) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return d; }
-    const int t = row_argmax(S, ld, p, nel);
-    const double maxt = rc_max(S, ld, t, nel, m, p);
-    double maxp = rc_max(S, ld, p, nel, m, t);
-    const double a11 = (double)S[(size_t)t * ld + t], a21 = (double)S[(size_t)t * ld + p];
-    const double a22 = (double)S[(size_t)p * ld + p];
-    // test_2x2 (ldlt_tpp.cxx:95-126)
+__device__ __forceinline__ bool test_pivots(double a11, double a21, double a22, double maxt,
+                                            double maxp, double u, double small, int t, int p,
+                                            Decision& d) {
+  if constexpr (sizeof(T) == 8) {
     const double maxpiv = fmax(fabs(a11), fmax(fabs(a21), fabs(a22)));
     if (!(maxpiv < small)) {
       const double detscale = 1 / maxpiv;
@@ -1478,15 +1476,65 @@ __device__ Decision decide(const T* S, int ld, int nel, int m, int n, bool actio
           const double x2 = fabs(d1) * maxt + fabs(d3) * maxp;
           ok = (u * fmax(x1, x2) < 1.0);
         }
-        if (ok) { d.kind = kTwo; d.t = t; d.p = p; d.d0 = d0; d.d1 = d1; d.d3 = d3; return d; }
+        if (ok) { d.kind = kTwo; d.t = t; d.p = p; d.d0 = d0; d.d1 = d1; d.d3 = d3; return true; }
       }
     }
     maxp = fmax(maxp, fabs(a21));
-    if (fabs(a22) >= u * maxp) { d.kind = kOne; d.p = p; return d; }
+    if (fabs(a22) >= u * maxp) { d.kind = kOne; d.p = p; return true; }
+    return false;
+  } else {
+    // the entries and maxima are FP32 values; thresholds in FP32
+    float fsmall = (float)small;
+    if ((double)fsmall < small) fsmall = nextafterf(fsmall, INFINITY);
+    const float fu = (float)u;
+    const float b11 = (float)a11, b21 = (float)a21, b22 = (float)a22;
+    const float mt = (float)maxt;
+    float mp = (float)maxp;
+    const float maxpiv = fmaxf(fabsf(b11), fmaxf(fabsf(b21), fabsf(b22)));
+    if (!(maxpiv < fsmall)) {
+      const float detscale = 1.0f / maxpiv;
+      const float det0 = (b11 * detscale) * b22, det1 = (b21 * detscale) * b21;
+      const float detpiv = det0 - det1;
+      if (!(fabsf(detpiv) < fmaxf(fsmall, fmaxf(fabsf(det0 * 0.5f), fabsf(det1 * 0.5f))))) {
+        const float d0 = (b22 * detscale) / detpiv, d1 = (-b21 * detscale) / detpiv;
+        const float d3 = (b11 * detscale) / detpiv;
+        bool ok;
+        if (fmaxf(mp, mt) < fsmall) ok = true;
+        else {
+          const float x1 = fabsf(d0) * mt + fabsf(d1) * mp;
+          const float x2 = fabsf(d1) * mt + fabsf(d3) * mp;
+          ok = (fu * fmaxf(x1, x2) < 1.0f);
+        }
+        if (ok) { d.kind = kTwo; d.t = t; d.p = p; d.d0 = d0; d.d1 = d1; d.d3 = d3; return true; }
+      }
+    }
+    mp = fmaxf(mp, fabsf(b21));
+    if (fabsf(b22) >= fu * mp) { d.kind = kOne; d.p = p; return true; }
+    return false;
+  }
+}
+// the pivot search of one step of ldlt_tpp_factor, in warp 0
+template <typename T>
+__device__ Decision decide(const T* S, int ld, int nel, int m, int n, bool action, double u,
+                           double small) {
+  Decision d{kStop, 0, 0, 0.0, 0.0, 0.0};
+  if (col_small(S, ld, nel, nel, m, small)) { d.kind = action ? kZeroNel : kSingular; return d; }
+  for (int p = nel + 1; p < n; ++p) {
+    if (col_small(S, ld, p, nel, m, small)) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return d; }
+    const int t = row_argmax(S, ld, p, nel);
+    const double maxt = rc_max(S, ld, t, nel, m, p);
+    const double maxp = rc_max(S, ld, p, nel, m, t);
+    const double a11 = (double)S[(size_t)t * ld + t], a21 = (double)S[(size_t)t * ld + p];
+    const double a22 = (double)S[(size_t)p * ld + p];
+    if (test_pivots<T>(a11, a21, a22, maxt, maxp, u, small, t, p, d)) return d;
   }
   // last resort: nel itself as a 1x1 pivot
   const double maxp = rc_max(S, ld, nel, nel, m, -1);
-  if (fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp) { d.kind = kOne; d.p = nel; }
+  if (sizeof(T) == 8 ? fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp
+                     : fabsf((float)S[(size_t)nel * ld + nel]) >= (float)u * (float)maxp) {
+    d.kind = kOne;
+    d.p = nel;
+  }
   return d;
 }
 // ---- the same pivot search with every warp of the CTA (tall fronts) ----
@@ -1591,32 +1639,12 @@ __device__ bool try_candidate(const T* S, int ld, int p, const LineInfo& lp, con
                               bool action, double u, double small, Decision& d) {
   if (lp.all_small) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return true; }
   const int t = lp.ri;
-  double maxp = key_value<T>((lp.i1 == t) ? lp.v2 : lp.v1);
+  const double maxp = key_value<T>((lp.i1 == t) ? lp.v2 : lp.v1);
   // largest |entry| of line t off its diagonal, excluding position p
-  double maxt = key_value<T>((lt.i1 == p) ? lt.v2 : lt.v1);
+  const double maxt = key_value<T>((lt.i1 == p) ? lt.v2 : lt.v1);
   const double a11 = (double)S[(size_t)t * ld + t], a21 = (double)S[(size_t)t * ld + p];
   const double a22 = (double)S[(size_t)p * ld + p];
-  const double maxpiv = fmax(fabs(a11), fmax(fabs(a21), fabs(a22)));
-  if (!(maxpiv < small)) {
-    const double detscale = 1 / maxpiv;
-    const double det0 = (a11 * detscale) * a22, det1 = (a21 * detscale) * a21;
-    const double detpiv = det0 - det1;
-    if (!(fabs(detpiv) < fmax(small, fmax(fabs(det0 / 2), fabs(det1 / 2))))) {
-      const double d0 = (a22 * detscale) / detpiv, d1 = (-a21 * detscale) / detpiv;
-      const double d3 = (a11 * detscale) / detpiv;
-      bool ok;
-      if (fmax(maxp, maxt) < small) ok = true;
-      else {
-        const double x1 = fabs(d0) * maxt + fabs(d1) * maxp;
-        const double x2 = fabs(d1) * maxt + fabs(d3) * maxp;
-        ok = (u * fmax(x1, x2) < 1.0);
-      }
-      if (ok) { d.kind = kTwo; d.t = t; d.p = p; d.d0 = d0; d.d1 = d1; d.d3 = d3; return true; }
-    }
-  }
-  maxp = fmax(maxp, fabs(a21));
-  if (fabs(a22) >= u * maxp) { d.kind = kOne; d.p = p; return true; }
-  return false;
+  return test_pivots<T>(a11, a21, a22, maxt, maxp, u, small, t, p, d);
 }
 
 // the pivot search of one step of ldlt_tpp_factor with all threads (each
@@ -1652,7 +1680,11 @@ __device__ Decision decide_cta(const T* S, int ld, int nel, int m, int n, bool a
     }
     const LineInfo ln = batch[0];
     const double maxp = key_value<T>(ln.v1);
-    if (fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp) { d.kind = kOne; d.p = nel; }
+    if (sizeof(T) == 8 ? fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp
+                       : fabsf((float)S[(size_t)nel * ld + nel]) >= (float)u * (float)maxp) {
+      d.kind = kOne;
+      d.p = nel;
+    }
     return d;
   }
   for (; p < n; ++p) {
@@ -1663,7 +1695,11 @@ __device__ Decision decide_cta(const T* S, int ld, int nel, int m, int n, bool a
   }
   const LineInfo ln = line_info(S, ld, nel, nel, m, small, sh);
   const double maxp = key_value<T>(ln.v1);
-  if (fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp) { d.kind = kOne; d.p = nel; }
+  if (sizeof(T) == 8 ? fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp
+                     : fabsf((float)S[(size_t)nel * ld + nel]) >= (float)u * (float)maxp) {
+    d.kind = kOne;
+    d.p = nel;
+  }
   return d;
 }
 }  // namespace tpps
@@ -1677,6 +1713,36 @@ constexpr int kTppWideRows = 1024;
 template <typename T>
 __device__ __forceinline__ tpps::LineInfo* tpp_batch(const FrontDesc<T>& fd) {
   return reinterpret_cast<tpps::LineInfo*>(fd.W + 2 * (size_t)fd.ld);
+}
+
+// FP32 factors: D^{-1} of the pivots [nel0, nel1) in FP64 from the pivot
+// entries the TPP loop recorded in D (1x1: the pivot; 2x2: a11, a21, the
+// second-half marker, a22), with the formulas of test_2x2 and the 1x1
+// reciprocal, one pivot per thread; ends with a barrier.  FP64 factors
+// already hold D^{-1}.
+template <typename T>
+__device__ void tpp_finish_d(double* D, int nel0, int nel1) {
+  if constexpr (sizeof(T) == 4) {
+    __syncthreads();
+    for (int i = nel0 + (int)threadIdx.x; i < nel1; i += blockDim.x) {
+      if (isinf(D[2 * i])) continue;  // second half of a 2x2: its first half converts both
+      if (i + 1 < nel1 && isinf(D[2 * i + 2])) {
+        const double a11 = D[2 * i], a21 = D[2 * i + 1], a22 = D[2 * i + 3];
+        const double maxpiv = fmax(fabs(a11), fmax(fabs(a21), fabs(a22)));
+        const double detscale = 1 / maxpiv;
+        const double det0 = (a11 * detscale) * a22, det1 = (a21 * detscale) * a21;
+        const double detpiv = det0 - det1;
+        D[2 * i] = (a22 * detscale) / detpiv;
+        D[2 * i + 1] = (-a21 * detscale) / detpiv;
+        D[2 * i + 3] = (a11 * detscale) / detpiv;
+      } else {
+        const double a = D[2 * i];
+        D[2 * i] = (a != 0.0) ? 1.0 / a : 0.0;
+        D[2 * i + 1] = 0.0;
+      }
+    }
+  }
+  __syncthreads();
 }
 
 // The TPP loop of ldlt_tpp_factor on columns [nel, n), rows [nel, m), of
@@ -1693,6 +1759,7 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
   __shared__ Decision s_dec;
   __shared__ LineInfo s_line[kTppThreads / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int nel0 = nel;
   while (nel < n) {
     Decision dw;
     const bool wide = m - nel > kTppWideRows;
@@ -1711,20 +1778,31 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
           W1[r] = S[(size_t)(nel + 1) * ld + r];
         }
         if (lane == 0) {
+          if constexpr (sizeof(T) == 4) {
+            // the pivot entries; D^{-1} in FP64 by tpp_finish_d
+            D[2 * nel] = (double)S[(size_t)nel * ld + nel];
+            D[2 * nel + 1] = (double)S[(size_t)nel * ld + nel + 1];
+            D[2 * nel + 3] = (double)S[(size_t)(nel + 1) * ld + nel + 1];
+          } else {
+            D[2 * nel] = d.d0; D[2 * nel + 1] = d.d1; D[2 * nel + 3] = d.d3;
+          }
+          D[2 * nel + 2] = dinf();
           S[(size_t)nel * ld + nel] = T(1);
           S[(size_t)nel * ld + nel + 1] = T(0);
           S[(size_t)(nel + 1) * ld + nel + 1] = T(1);
-          D[2 * nel] = d.d0; D[2 * nel + 1] = d.d1;
-          D[2 * nel + 2] = dinf(); D[2 * nel + 3] = d.d3;
         }
       } else if (d.kind == kOne) {
         sym_swap(S, ld, m, d.p, nel, perm, opos);
-        const double d11 = 1.0 / (double)S[(size_t)nel * ld + nel];
+        const T app = S[(size_t)nel * ld + nel];
+        double d11;
+        if constexpr (sizeof(T) == 4) d11 = (double)(1.0f / app);  // the L column's multiplier
+        else d11 = 1.0 / app;
         d.d0 = d11;
         for (int r = nel + 1 + lane; r < m; r += 32) W0[r] = S[(size_t)nel * ld + r];
         if (lane == 0) {
           S[(size_t)nel * ld + nel] = T(1);
-          D[2 * nel] = d11; D[2 * nel + 1] = 0.0;
+          D[2 * nel] = sizeof(T) == 4 ? (double)app : d11;  // FP32: the pivot, see tpp_finish_d
+          D[2 * nel + 1] = 0.0;
         }
       }
       __syncwarp();
@@ -1733,7 +1811,10 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
     __syncthreads();
     const Decision d = s_dec;
     if (d.kind == kStop) break;
-    if (d.kind == kSingular) return -1;
+    if (d.kind == kSingular) {
+      tpp_finish_d<T>(D, nel0, nel);
+      return -1;
+    }
     if (d.kind == kZeroNel || d.kind == kZeroSwap) {
       nel += 1;
       __syncthreads();  // every warp has read s_dec before warp 0 rewrites it
@@ -1776,6 +1857,7 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
     __syncthreads();
     nel += ps;
   }
+  tpp_finish_d<T>(D, nel0, nel);
   return nel;
 }
 

@@ -1061,14 +1061,27 @@ struct Numeric : NumericBase {
   // front (current sizes, delays included) up to the class cap
   void launch_tpp_levels(int l, cudaStream_t s) {
     const auto& co = S->copts;
-    for (int c = 0; c < kTppClasses; ++c) {
+    int cls[kTppClasses], nc = 0;
+    for (int c = 0; c < kTppClasses; ++c)
+      if (S->tpp_off[(size_t)kTppClasses * l + c + 1] > S->tpp_off[(size_t)kTppClasses * l + c])
+        cls[nc++] = c;
+    // the classes' fronts are independent: the first class on s, the others
+    // on the side streams, joined back into s
+    if (nc > 1) CK(cudaEventRecord(fork_ev, s));
+    for (int k = 0; k < nc; ++k) {
+      const int c = cls[k];
       const int o0 = S->tpp_off[(size_t)kTppClasses * l + c];
       const int o1 = S->tpp_off[(size_t)kTppClasses * l + c + 1];
-      if (o1 <= o0) continue;
       int mx = 0;
-      for (int k = o0; k < o1; ++k) mx = std::max(mx, tpp_bytes(S->tpp_list[k]));
+      for (int j = o0; j < o1; ++j) mx = std::max(mx, tpp_bytes(S->tpp_list[j]));
+      cudaStream_t q = k == 0 ? s : side[k - 1];
+      if (k > 0) CK(cudaStreamWaitEvent(q, fork_ev, 0));
       launch_tpp_level<T>(d_fd, d_st, S->d_tpp + o0, o1 - o0, co.action, co.u, co.small,
-                          std::min(mx, tpp_class_smem_cap(c)), tpp_class_threads(c), s);
+                          std::min(mx, tpp_class_smem_cap(c)), tpp_class_threads(c), q);
+      if (k > 0) {
+        CK(cudaEventRecord(join_ev[k - 1], q));
+        CK(cudaStreamWaitEvent(s, join_ev[k - 1], 0));
+      }
     }
   }
 
@@ -1449,10 +1462,19 @@ struct Numeric : NumericBase {
   bool last_scaled = false;
   std::vector<cudaEvent_t> pev;
 
+  // side streams and events that let the size-class launches of one level's
+  // small-subtree fronts run concurrently (fork from and join back to the
+  // handle's stream; captured into the factorisation graph as branches)
+  cudaStream_t side[kTppClasses - 1] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kTppClasses - 1] = {};
+
   explicit Numeric(Symbolic* s) : S(s) {
     CK(cudaSetDevice(S->device));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     for (auto& e : ev) CK(cudaEventCreate(&e));
+    for (auto& q : side) CK(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    for (auto& e : join_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     const int nn = S->nnodes;
     hfd.resize(nn);
     hst.resize(nn);
@@ -1517,6 +1539,11 @@ struct Numeric : NumericBase {
     drop_graphs();
     drop_fgraph();
     for (auto& e : ev) cudaEventDestroy(e);
+    for (auto q : side)
+      if (q) { cudaStreamSynchronize(q); cudaStreamDestroy(q); }
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    for (auto e : join_ev)
+      if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
   }
   Symbolic* symbolic() override { return S; }
