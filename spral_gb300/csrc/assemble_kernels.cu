@@ -90,18 +90,29 @@ __global__ void k_assemble_delays(const FrontDesc<T>* fds, const FrontState* sts
 }
 
 // cols[i] = (parent front, parent position P, first pair, end pair);
-// pairs[q] = (child front, child contribution column jc)
-template <typename T>
-__global__ void k_assemble_contrib(const FrontDesc<T>* fds, const int4* cols, const int2* pairs,
-                                   const int* rdir, const int64_t* rdir_ptr) {
-  const int4 cw = cols[blockIdx.x];
+// pairs[q] = (child front, child contribution column jc).  One parent
+// column per CTA, or per warp (WARP: levels whose columns are short, so that
+// four columns of small fronts share a CTA instead of one leaving most of
+// its threads idle); the same additions in the same order either way.
+template <typename T, bool WARP>
+__global__ void k_assemble_contrib(const FrontDesc<T>* fds, const int4* cols, int ncols,
+                                   const int2* pairs, const int* rdir, const int64_t* rdir_ptr) {
+  const int col = WARP ? blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) : blockIdx.x;
+  if (col >= ncols) return;  // warp-uniform
+  const int tid = WARP ? (threadIdx.x & 31) : threadIdx.x;
+  const int nt = WARP ? 32 : blockDim.x;
+  auto sync = [] {
+    if (WARP) __syncwarp();
+    else __syncthreads();
+  };
+  const int4 cw = cols[col];
   const FrontDesc<T> fp = fds[cw.x];
   const int P = cw.y;
   const bool into_l = P < fp.ncol;
   T* dst = into_l ? fp.L + (int64_t)P * fp.ld : fp.C + (int64_t)(P - fp.ncol) * fp.ldc;
   if (!into_l) {
-    for (int r = P - fp.ncol + threadIdx.x; r < fp.cm; r += blockDim.x) dst[r] = T(0);
-    __syncthreads();
+    for (int r = P - fp.ncol + tid; r < fp.cm; r += nt) dst[r] = T(0);
+    sync();
   }
   // A contribution-block column fed by one child receives each entry at most
   // once: it is stored (v + 0 has the bits of 0 + v, -0 included) instead of
@@ -115,12 +126,12 @@ __global__ void k_assemble_contrib(const FrontDesc<T>* fds, const int4* cols, co
     const int cmc = fc.cm;
     const T* src = fc.C + (int64_t)jc * fc.ldc;
     const int* rd = rdir + rdir_ptr[fc.node];
-    for (int ic0 = jc + threadIdx.x; ic0 < cmc; ic0 += U * blockDim.x) {
+    for (int ic0 = jc + tid; ic0 < cmc; ic0 += U * nt) {
       int Q[U];
       T v[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int ic = ic0 + u * blockDim.x;
+        const int ic = ic0 + u * nt;
         Q[u] = ic < cmc ? rd[ic] : -1;
         v[u] = ic < cmc ? src[ic] : T(0);
       }
@@ -134,7 +145,7 @@ __global__ void k_assemble_contrib(const FrontDesc<T>* fds, const int4* cols, co
         else dst[r] += v[u];
       }
     }
-    __syncthreads();
+    sync();
   }
 }
 
@@ -165,12 +176,21 @@ void launch_assemble_delays(const FrontDesc<T>* fd, const FrontState* st, const 
   const int gx = std::max(1, std::min(max_nd, 256));
   { k_assemble_delays<T><<<dim3(gx, nwork), 128, 0, s>>>(fd, st, work, rdir, rdir_ptr); note_launches(1); }
 }
+// columns at most this long (rows of the parent's or a child's contribution
+// block) take a warp each
+constexpr int kAssembleWarpRows = 256;
+
 template <typename T>
 void launch_assemble_contrib(const FrontDesc<T>* fd, const int4* cols, int ncols,
                              const int2* pairs, const int* rdir, const int64_t* rdir_ptr,
-                             cudaStream_t s) {
+                             int max_rows, cudaStream_t s) {
   if (ncols <= 0) return;
-  { k_assemble_contrib<T><<<ncols, 128, 0, s>>>(fd, cols, pairs, rdir, rdir_ptr); note_launches(1); }
+  if (max_rows <= kAssembleWarpRows)
+    k_assemble_contrib<T, true><<<cdiv(ncols, 4), 128, 0, s>>>(fd, cols, ncols, pairs, rdir,
+                                                               rdir_ptr);
+  else
+    k_assemble_contrib<T, false><<<ncols, 128, 0, s>>>(fd, cols, ncols, pairs, rdir, rdir_ptr);
+  note_launches(1);
 }
 
 #define INST(T)                                                                                  \
@@ -182,7 +202,7 @@ void launch_assemble_contrib(const FrontDesc<T>* fd, const int4* cols, int ncols
   template void launch_assemble_delays<T>(const FrontDesc<T>*, const FrontState*, const int4*,  \
                                           int, int, const int*, const int64_t*, cudaStream_t);   \
   template void launch_assemble_contrib<T>(const FrontDesc<T>*, const int4*, int, const int2*,  \
-                                           const int*, const int64_t*, cudaStream_t);
+                                           const int*, const int64_t*, int, cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

@@ -335,6 +335,7 @@ struct Symbolic {
   // d_tpp[tpp_off[kTppClasses * l + c] .. tpp_off[kTppClasses * l + c + 1])
   std::vector<int> tpp_off, tpp_list;
   std::vector<int> cols_start;  // per level into cols
+  std::vector<int> lvl_colrows;  // per level, the longest contribution-block column (parent or child)
   std::vector<int64_t> contrib_off;  // per front, elements
   int64_t contrib_total = 0;
   int64_t nnz = 0;
@@ -491,6 +492,7 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
   std::vector<int4> cols;
   std::vector<int2> pairs;
   S->cols_start.assign(nlev + 1, 0);
+  S->lvl_colrows.assign(nlev, 0);
   S->gp_off.assign(nn + 1, 0);
   for (int f = 0; f < nn; ++f) S->gp_off[f + 1] = S->gp_off[f] + S->nrow[S->node_of[f]] + 1;
   std::vector<int> gp(S->gp_off[nn] + 1, 0);
@@ -499,8 +501,10 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
     for (int f = S->lvl_start[l]; f < S->lvl_start[l + 1]; ++f) {
       int p = S->node_of[f];
       std::vector<std::vector<int2>> per(S->nrow[p]);
+      S->lvl_colrows[l] = std::max(S->lvl_colrows[l], S->nrow[p] - S->ncol[p]);
       for (int c : S->children[p]) {
         int cm = S->nrow[c] - S->ncol[c];
+        S->lvl_colrows[l] = std::max(S->lvl_colrows[l], cm);
         for (int jc = 0; jc < cm; ++jc) {
           int P = S->rdir_h[S->rdir_ptr_h[c] + jc];
           per[P].push_back(make_int2(S->front_of[c], jc));
@@ -1315,7 +1319,7 @@ struct Numeric : NumericBase {
         launch_init_perm<T>(d_fd, fr, nf, S->d_sptr, max_n, s);
         launch_assemble_contrib<T>(d_fd, S->d_cols + S->cols_start[l],
                                    S->cols_start[l + 1] - S->cols_start[l], S->d_pairs,
-                                   S->d_rdir, S->d_rdir_ptr, s);
+                                   S->d_rdir, S->d_rdir_ptr, S->lvl_colrows[l], s);
         const int steps = (max_app_n + kBlk - 1) / kBlk;
         for (int st = 0; st < steps; ++st) {
           int mr = 0, tr = 0, tc = 0;
@@ -1694,7 +1698,7 @@ struct Numeric : NumericBase {
       pmark(tm(), kPhAssemble, s);
       launch_assemble_contrib<T>(d_fd, S->d_cols + S->cols_start[l],
                                  S->cols_start[l + 1] - S->cols_start[l], S->d_pairs, S->d_rdir,
-                                 S->d_rdir_ptr, s);
+                                 S->d_rdir_ptr, S->lvl_colrows[l], s);
       // dense factorisation
       const bool use_app = co.pivot_method != 3;
       bool any_panel = false;

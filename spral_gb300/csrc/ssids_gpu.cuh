@@ -147,10 +147,12 @@ template <typename T>
 void launch_assemble_delays(const FrontDesc<T>* fd, const FrontState* st, const int4* work,
                             int nwork, int max_nd, const int* rdir, const int64_t* rdir_ptr,
                             cudaStream_t s);
+// max_rows: the longest contribution-block column (parent or child) of the
+// level: short columns take a warp each, long ones a CTA
 template <typename T>
 void launch_assemble_contrib(const FrontDesc<T>* fd, const int4* cols, int ncols,
                              const int2* pairs, const int* rdir, const int64_t* rdir_ptr,
-                             cudaStream_t s);
+                             int max_rows, cudaStream_t s);
 template <typename T>
 void launch_app_step(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, int step,
                      int max_rows, int max_trail_rows, int max_trail_cols, bool action,
