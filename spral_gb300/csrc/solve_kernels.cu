@@ -552,6 +552,9 @@ __global__ void __launch_bounds__(kSolveThreads)
 }
 
 // ---- wavefront solves (one persistent launch per pass, whole tree) ----
+// persistent CTAs per SM of a pass (registers capped to fit them): more
+// items in flight for trees of many small fronts
+constexpr int kWaveCtasPerSm = 3;
 // try rounds of a flag wait before it gives up (each round sleeps briefly);
 // no legitimate wait comes close
 constexpr long long kWaveSpinLimit = 1LL << 22;
@@ -915,7 +918,7 @@ __device__ bool fwd_block(const SolveNode<T>& sn, int code, int nrhs, double* x,
 
 // Forward pass over the whole tree (item list and waits: see WaveLevel).
 template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveThreads, 2)
+__global__ void __launch_bounds__(kSolveThreads, kWaveCtasPerSm)
     k_fwd_tree(const SolveNode<T>* sns, const int* children, const int2* pairs, WaveLevel wl,
                int nrhs, double* x, int ldx, bool scale_sqrt, int* status) {
   extern __shared__ __align__(16) unsigned char solve_smem[];
@@ -1195,7 +1198,7 @@ __device__ bool bwd_block(const SolveNode<T>& sn, int b, int nrhs, double* x, in
 
 // Backward pass over the whole tree (item list and waits: see WaveLevel).
 template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveThreads, 2)
+__global__ void __launch_bounds__(kSolveThreads, kWaveCtasPerSm)
     k_bwd_tree(const SolveNode<T>* sns, WaveLevel wl, int nrhs, double* x, int ldx, int diag_mode,
                int* status) {
   extern __shared__ __align__(16) unsigned char solve_smem[];
@@ -1412,9 +1415,17 @@ int wave_timeout_probe(int rounds) {
   return h ? -51 : 0;
 }
 
-// persistent CTAs of a wave launch: at most two per SM (each may hold an
-// item that waits), never more than there are items
-inline int wave_grid(int nitems) { return std::max(1, std::min(nitems, 2 * 152)); }
+// persistent CTAs of a wave launch: kWaveCtasPerSm per SM (each may hold
+// an item that waits), never more than there are items
+inline int wave_grid(int nitems) {
+  static const int nsm = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 152;
+  }();
+  return std::max(1, std::min(nitems, kWaveCtasPerSm * nsm));
+}
 
 // FP32 factors only (FP64 factors keep the substitution in the passes)
 template <typename T>
