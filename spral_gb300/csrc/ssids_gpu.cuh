@@ -216,9 +216,10 @@ struct TcBuffers {  // reusable descriptor staging of tc_gemm_run
 }  // namespace ssids300
 #include <vector>
 namespace ssids300 {
-// Default number of 32-deep k-tiles accumulated in TMEM before the partial
-// sum is added (round-to-nearest) into the register accumulator.
-constexpr int kTcChunk = 8;
+// Default number of 32-deep k-tiles (96 split products each) accumulated in
+// TMEM before the partial sum is added (round-to-nearest) into the register
+// accumulator.
+constexpr int kTcChunk = 3;
 size_t tc_gemm_scratch_bytes(const std::vector<TcProblem>& ps);
 // Descriptor tables of one tc_gemm launch pair (split + GEMM), built on the
 // host; tc_gemm_launch only enqueues kernels, so it can be graph-captured

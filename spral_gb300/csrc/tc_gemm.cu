@@ -5,19 +5,21 @@
 // with A = L21 and B = L21 D of a front (FP32 factors of the mixed-precision
 // path).  FP32-class accuracy comes from split products: each FP32 value x is
 // written as x = hi + lo with hi = tf32(x) and lo = tf32(x - hi), and
-//   A B^T ~ Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T,
-// which is ONE TF32 GEMM over a 3K-deep operand pair
-//   A' = [Ahi | Ahi | Alo],  B' = [Bhi | Blo | Bhi]   (interleaved per k).
-// k_split builds A' and B' K-major (row-major, ld = kpad); k_tc_gemm is a
+//   A B^T ~ Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T.
+// k_split writes A' and B' K-major (row-major) with, per 32-deep k-tile, the
+// 32 hi values then the 32 lo values (ld = 64 x k-tiles); k_tc_gemm is a
 // persistent kernel that computes 128 x BN tiles of the result (BN = 256,
-// 128 or 64, chosen per launch by the autotuner): it streams 32-deep k-tiles
-// of A' (128 rows) and B' (BN rows) with TMA (128-byte swizzle) through an
-// mbarrier pipeline of 192 KiB (4, 6 or 8 stages) into
-// tcgen05.mma.kind::tf32 (M = 128, N = BN, FP32 accumulators in TMEM) and
-// subtracts the result from C.
+// 128 or 64, chosen per launch by the autotuner): per k-tile it loads the
+// hi and lo halves of A (128 rows) and B (BN rows) with TMA (128-byte
+// swizzle) through an mbarrier pipeline of 192 KiB (2, 3 or 4 stages) and
+// issues the three products of the tile from them into
+// tcgen05.mma.kind::tf32 (M = 128, N = BN, FP32 accumulators in TMEM), then
+// subtracts the result from C.  Keeping hi and lo once each, instead of the
+// three operand copies of a 3K-deep GEMM, reads two thirds of the operand
+// bytes per tensor flop.
 //
 // Accumulation: the tensor cores accumulate at most `chunk` k-tiles
-// (32 * chunk split products) in TMEM; the epilogue warps then add that
+// (96 * chunk split products) in TMEM; the epilogue warps then add that
 // partial sum into registers with round-to-nearest FP32 adds.  This keeps
 // the tensor cores' internal accumulation short and recovers FP32-class
 // accuracy for deep updates (the contribution of a front with nelim
@@ -41,14 +43,17 @@ namespace ssids300 {
 namespace {
 
 constexpr int TC_M = 128, TC_K = 32;  // K = 32 fp32 = 128 bytes
-constexpr int TC_A_BYTES = TC_M * TC_K * 4;  // 16 KiB of A' per stage
-constexpr int TC_RING_BYTES = 192 << 10;     // the k-tile ring of every tile width
-// tile width BN: B' bytes per stage, stages, TMEM columns (two FP32
-// accumulators of BN columns; a power of two >= 32 as tcgen05.alloc needs)
+constexpr int TC_AH_BYTES = TC_M * TC_K * 4;  // 16 KiB: the hi (or lo) half of A per stage
+constexpr int TC_A_BYTES = 2 * TC_AH_BYTES;   // A hi then A lo
+constexpr int TC_RING_BYTES = 192 << 10;      // the k-tile ring of every tile width
+// tile width BN: B bytes per stage (hi then lo halves of BN * 128 bytes),
+// stages, TMEM columns (two FP32 accumulators of BN columns; a power of two
+// >= 32 as tcgen05.alloc needs)
 template <int BN>
 struct TcShape {
   static_assert(BN == 64 || BN == 128 || BN == 256, "tile widths of the kernel");
-  static constexpr int B_BYTES = BN * TC_K * 4;
+  static constexpr int BH_BYTES = BN * TC_K * 4;
+  static constexpr int B_BYTES = 2 * BH_BYTES;
   static constexpr int STAGES = TC_RING_BYTES / (TC_A_BYTES + B_BYTES);
   static constexpr uint32_t TMEM_COLS = 2 * BN;
 };
@@ -167,9 +172,10 @@ __device__ __forceinline__ float to_tf32(float x) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
-// Split operands.  For row r < rows and k < kval: dst[r*ld + 3k + {0,1,2}] =
-// (hi, hi, lo) of src(r, k) for the A side, (hi, lo, hi) for the B side;
-// columns [3*kval, kpad) are zero.  src is column-major (ld_src).
+// Split operands.  For row r < rows and k < kval, k = 32 t + j: dst[r*ld +
+// 64 t + j] = hi and dst[r*ld + 64 t + 32 + j] = lo of src(r, k) (both
+// sides alike); entries of k >= kval are zero.  src is column-major
+// (ld_src); kpad = 64 x k-tiles.
 // ---------------------------------------------------------------------------
 struct SplitJob {
   const float* src;
@@ -182,7 +188,7 @@ __global__ void k_split(const SplitJob* jobs) {
   const SplitJob j = jobs[blockIdx.z];
   __shared__ float tile[32][33];
   const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
-  if (r0 >= j.rows || 3 * k0 >= j.kpad) return;  // uniform per CTA
+  if (r0 >= j.rows || 2 * k0 >= j.kpad) return;  // uniform per CTA
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
   const int kval = j.kval_dev ? min(j.kval, *j.kval_dev) : j.kval;
   for (int i = ty; i < 32; i += 8) {
@@ -193,16 +199,13 @@ __global__ void k_split(const SplitJob* jobs) {
   for (int i = ty; i < 32; i += 8) {
     const int r = r0 + i;
     if (r >= j.rows) continue;
-    const int k = k0 + tx;
-    if (3 * k >= j.kpad) continue;
     const float x = tile[tx][i];
     const float hi = to_tf32(x);
     const float lo = to_tf32(x - hi);
-    float* d = j.dst + (int64_t)r * j.ld_dst + 3 * k;
-    // columns past kpad belong to the next row: write only inside the row
+    // k0 is a multiple of 32: this CTA's k-tile is k0 / 32
+    float* d = j.dst + (int64_t)r * j.ld_dst + 2 * k0 + tx;
     d[0] = hi;
-    if (3 * k + 1 < j.kpad) d[1] = j.is_b ? lo : hi;
-    if (3 * k + 2 < j.kpad) d[2] = j.is_b ? hi : lo;
+    d[32] = lo;
   }
 }
 
@@ -213,26 +216,29 @@ __global__ void k_split(const SplitJob* jobs) {
 struct TcJob {
   float* C;
   int ldc, M, N;
-  int kpad;        // depth of A', B' (multiple of 32)
+  int kpad;        // row length of A', B': 64 per 32-deep k-tile
   int lower;       // 1: only r >= c is updated
-  const int* kval; // nullptr or device pointer: effective depth = 3 * (*kval)
+  const int* kval; // nullptr or device pointer: effective depth *kval
 };
 
+// 32-deep k-tiles of a job (each: hi and lo halves, three products)
 __device__ __forceinline__ int tile_ktiles(const TcJob& j) {
-  int kd = j.kpad;
-  if (j.kval) kd = min(kd, 3 * max(*j.kval, 0));
-  return (kd + TC_K - 1) / TC_K;
+  int nk = j.kpad / (2 * TC_K);
+  if (j.kval) nk = min(nk, (max(*j.kval, 0) + TC_K - 1) / TC_K);
+  return nk;
 }
 
 // Persistent kernel, one CTA per SM, 320 threads:
-//   warp 0 lane 0   TMA producer (A' and B' k-tiles into a ring of STAGES)
-//   warp 1 lane 0   MMA issuer (tcgen05.mma into one of two TMEM accumulators)
+//   warp 0 lane 0   TMA producer (hi and lo halves of A' and B' per k-tile
+//                   into a ring of STAGES)
+//   warp 1 lane 0   MMA issuer (tcgen05.mma into one of two TMEM
+//                   accumulators, the k-tile's three split products)
 //   warps 2..9      accumulate / epilogue (warp w reads TMEM lanes 32*(w%4)..)
 // The k range of a tile is cut into chunks of `chunk` k-tiles (0 = one chunk).
 // Each chunk is accumulated by the tensor cores in a fresh TMEM accumulator;
 // the epilogue warps add it, rounding to nearest, into a per-thread register
 // row of the tile, so the tensor cores' own accumulation spans at most
-// 32 * chunk products.  Two accumulators let the MMAs of the next chunk (or
+// 96 * chunk products.  Two accumulators let the MMAs of the next chunk (or
 // tile) run while the previous one is drained.
 template <int BN>
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -240,6 +246,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               int chunk, int* status) {
   constexpr int TC_STAGES = TcShape<BN>::STAGES;
   constexpr int TC_B_BYTES = TcShape<BN>::B_BYTES;
+  constexpr int TC_BH_BYTES = TcShape<BN>::BH_BYTES;
   constexpr uint32_t TC_TMEM_COLS = TcShape<BN>::TMEM_COLS;
   constexpr int HALF = BN / 2;  // columns of a tile per epilogue warp
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -294,8 +301,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             break;
           }
           mbar_expect_tx(&full[s], TC_A_BYTES + TC_B_BYTES);
-          tma_load_2d(sA + s * TC_A_BYTES, mapA, kt * TC_K, tl.y * TC_M, &full[s]);
-          tma_load_2d(sB + s * TC_B_BYTES, mapB, kt * TC_K, tl.z * BN, &full[s]);
+          unsigned char* a = sA + s * TC_A_BYTES;
+          unsigned char* b = sB + s * TC_B_BYTES;
+          const int x = kt * 2 * TC_K;  // hi half at x, lo half at x + 32
+          tma_load_2d(a, mapA, x, tl.y * TC_M, &full[s]);
+          tma_load_2d(a + TC_AH_BYTES, mapA, x + TC_K, tl.y * TC_M, &full[s]);
+          tma_load_2d(b, mapB, x, tl.z * BN, &full[s]);
+          tma_load_2d(b + TC_BH_BYTES, mapB, x + TC_K, tl.z * BN, &full[s]);
         }
       }
       *s_issued = (int)it;
@@ -322,17 +334,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const uint32_t s = it % TC_STAGES;
             if (!mbar_wait(&full[s], (it / TC_STAGES) & 1, abort_flag)) { ok = false; break; }
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t a0 = smem_u32(sA + s * TC_A_BYTES);
-            const uint32_t b0 = smem_u32(sB + s * TC_B_BYTES);
+            const uint32_t ahi = smem_u32(sA + s * TC_A_BYTES), alo = ahi + TC_AH_BYTES;
+            const uint32_t bhi = smem_u32(sB + s * TC_B_BYTES), blo = bhi + TC_BH_BYTES;
+            // the three split products Ahi Bhi, Ahi Blo, Alo Bhi of the k-tile
 #pragma unroll
-            for (int kk = 0; kk < TC_K / 8; ++kk) {  // 8 tf32 = 32 bytes per MMA
-              const uint64_t ad = smem_desc_sw128(a0 + kk * 32);
-              const uint64_t bd = smem_desc_sw128(b0 + kk * 32);
-              const uint32_t acc = (kt > k0 || kk > 0) ? 1u : 0u;
-              asm volatile(
-                  "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                  " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dacc),
-                  "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+            for (int pr = 0; pr < 3; ++pr) {
+              const uint32_t a0 = pr == 2 ? alo : ahi, b0 = pr == 1 ? blo : bhi;
+#pragma unroll
+              for (int kk = 0; kk < TC_K / 8; ++kk) {  // 8 tf32 = 32 bytes per MMA
+                const uint64_t ad = smem_desc_sw128(a0 + kk * 32);
+                const uint64_t bd = smem_desc_sw128(b0 + kk * 32);
+                const uint32_t acc = (kt > k0 || pr > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(dacc),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+              }
             }
             // stage s is free once these MMAs have read it
             mma_commit(&empty[s]);
@@ -495,7 +512,7 @@ static void launch_tc_kernel(const TcPlan& plan, const char* d, int chunk, int* 
 size_t tc_gemm_scratch_bytes(const std::vector<TcProblem>& ps) {
   size_t b = 0;
   for (auto& p : ps) {
-    const size_t kpad = (size_t)((3 * p.kmax + TC_K - 1) / TC_K) * TC_K;
+    const size_t kpad = (size_t)((p.kmax + TC_K - 1) / TC_K) * 2 * TC_K;
     b += ((size_t)p.M * kpad * 4 + 255) / 256 * 256;
     b += ((size_t)p.N * kpad * 4 + 255) / 256 * 256;
   }
@@ -526,13 +543,13 @@ int tc_gemm_prepare(const std::vector<TcProblem>& ps, void* scratch, TcPlan& pla
   int maxr = 0, maxk = 0;
   for (size_t i = 0; i < ps.size(); ++i) {
     const TcProblem& p = ps[i];
-    const int kpad = (3 * p.kmax + TC_K - 1) / TC_K * TC_K;
+    const int kpad = (p.kmax + TC_K - 1) / TC_K * 2 * TC_K;  // hi and lo per k-tile
     float* a2 = (float*)sp; sp += ((size_t)p.M * kpad * 4 + 255) / 256 * 256;
     float* b2 = (float*)sp; sp += ((size_t)p.N * kpad * 4 + 255) / 256 * 256;
     sj.push_back({p.A, a2, p.M, p.kmax, kpad, p.lda, kpad, 0, p.kval_dev});
     sj.push_back({p.B, b2, p.N, p.kmax, kpad, p.ldb, kpad, 1, p.kval_dev});
     maxr = std::max(maxr, std::max(p.M, p.N));
-    maxk = std::max(maxk, (kpad + 2) / 3);  // split columns 3k..3k+2 cover [0, kpad)
+    maxk = std::max(maxk, kpad / 2);  // source columns of the split
     CUtensorMap ma, mb;
     if (encode_kmajor(&ma, a2, p.M, kpad, kpad, TC_M) != CUDA_SUCCESS) return -2;
     if (encode_kmajor(&mb, b2, p.N, kpad, kpad, bn) != CUDA_SUCCESS) return -2;
