@@ -901,6 +901,7 @@ struct Numeric : NumericBase {
   DevBuf<T> wave_binv;
   DevBuf<int2> binv_blocks;
   int wave_nfwd = 0, wave_nbwd = 0;  // items of the forward pass, then of the backward pass
+  int wave_nsmall = 0;  // small fronts (one item each per pass)
   size_t wave_nflags = 0;
   // optional trace of the wavefront passes (SPRAL_GB300_WAVE_TRACE = path
   // prefix): per item four stamps (taken, last wait over, finished, SM),
@@ -914,6 +915,9 @@ struct Numeric : NumericBase {
     w.nitems = fwd ? wave_nfwd : wave_nbwd;
     w.counter = wave_ints.p + (fwd ? 1 : 2);
     w.trace = nullptr;
+    // many small-front items: more CTAs in flight; otherwise the widest
+    // fronts' chains set the time and keep their registers
+    w.ctas_per_sm = 2 * wave_nsmall > wave_nfwd ? 3 : 2;
     if (!wave_trace.empty()) {
       wave_trace_buf.ensure(4 * (size_t)(wave_nfwd + wave_nbwd) + 4);
       w.trace = wave_trace_buf.p + (fwd ? 0 : 4 * (size_t)wave_nfwd);
@@ -1867,6 +1871,8 @@ struct Numeric : NumericBase {
             for (int k = 0; k < ncon_of(f); ++k) items.push_back(make_int2(f, kWaveContrib + k));
       }
       wave_nfwd = (int)items.size();
+      wave_nsmall = 0;
+      for (int f = 0; f < nn; ++f) wave_nsmall += small_of(f) ? 1 : 0;
       for (int l = S->nlev - 1; l >= 0; --l) {
         const int f0 = S->lvl_start[l], f1 = S->lvl_start[l + 1];
         int mb = 0;

@@ -552,9 +552,9 @@ __global__ void __launch_bounds__(kSolveThreads)
 }
 
 // ---- wavefront solves (one persistent launch per pass, whole tree) ----
-// persistent CTAs per SM of a pass (registers capped to fit them): more
-// items in flight for trees of many small fronts
-constexpr int kWaveCtasPerSm = 3;
+// persistent CTAs per SM of a pass, CPS (registers capped to fit them):
+// 3 for trees of many small fronts (more items in flight), 2 otherwise (no
+// spilled registers on the chains of the widest fronts); WaveLevel tells
 // try rounds of a flag wait before it gives up (each round sleeps briefly);
 // no legitimate wait comes close
 constexpr long long kWaveSpinLimit = 1LL << 22;
@@ -603,15 +603,12 @@ __device__ __forceinline__ void wave_signal(int* ctr_a, int* ctr_b) {
 // item will ever set, with the wait bounded to `rounds` polls; the wait
 // gives up and sets *status, as a wavefront solve does.
 __global__ void k_wave_timeout_probe(const int* flag, long long rounds, int* status) {
-  __shared__ int s_fail;
   if (threadIdx.x == 0) {
     bool ok = true;
     for (long long it = 0; ld_acquire(flag) == 0; ++it)
       if (it >= rounds) { ok = false; break; }
     if (!ok) atomicExch(status, 1);
-    s_fail = ok ? 0 : 1;
   }
-  __syncthreads();
 }
 
 __device__ __forceinline__ unsigned long long global_timer() {
@@ -917,8 +914,8 @@ __device__ bool fwd_block(const SolveNode<T>& sn, int code, int nrhs, double* x,
 }
 
 // Forward pass over the whole tree (item list and waits: see WaveLevel).
-template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveThreads, kWaveCtasPerSm)
+template <typename T, int NR, int CPS>
+__global__ void __launch_bounds__(kSolveThreads, CPS)
     k_fwd_tree(const SolveNode<T>* sns, const int* children, const int2* pairs, WaveLevel wl,
                int nrhs, double* x, int ldx, bool scale_sqrt, int* status) {
   extern __shared__ __align__(16) unsigned char solve_smem[];
@@ -1197,8 +1194,8 @@ __device__ bool bwd_block(const SolveNode<T>& sn, int b, int nrhs, double* x, in
 }
 
 // Backward pass over the whole tree (item list and waits: see WaveLevel).
-template <typename T, int NR>
-__global__ void __launch_bounds__(kSolveThreads, kWaveCtasPerSm)
+template <typename T, int NR, int CPS>
+__global__ void __launch_bounds__(kSolveThreads, CPS)
     k_bwd_tree(const SolveNode<T>* sns, WaveLevel wl, int nrhs, double* x, int ldx, int diag_mode,
                int* status) {
   extern __shared__ __align__(16) unsigned char solve_smem[];
@@ -1415,16 +1412,16 @@ int wave_timeout_probe(int rounds) {
   return h ? -51 : 0;
 }
 
-// persistent CTAs of a wave launch: kWaveCtasPerSm per SM (each may hold
-// an item that waits), never more than there are items
-inline int wave_grid(int nitems) {
+// persistent CTAs of a wave launch: cps per SM (each may hold an item that
+// waits), never more than there are items
+inline int wave_grid(int nitems, int cps) {
   static const int nsm = [] {
     int dev = 0, n = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
     return n > 0 ? n : 152;
   }();
-  return std::max(1, std::min(nitems, kWaveCtasPerSm * nsm));
+  return std::max(1, std::min(nitems, cps * nsm));
 }
 
 // FP32 factors only (FP64 factors keep the substitution in the passes)
@@ -1444,8 +1441,12 @@ void launch_fwd_tree(const SolveNode<T>* sn, const int* children, const int2* pa
   if (wl.nitems <= 0) return;
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
-    k_fwd_tree<T, NR><<<wave_grid(wl.nitems), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
-        sn, children, pairs, wl, nrhs, x, ldx, scale_sqrt, status);
+    if (wl.ctas_per_sm >= 3)
+      k_fwd_tree<T, NR, 3><<<wave_grid(wl.nitems, 3), kSolveThreads, solve_smem_bytes<T, NR>(),
+                             s>>>(sn, children, pairs, wl, nrhs, x, ldx, scale_sqrt, status);
+    else
+      k_fwd_tree<T, NR, 2><<<wave_grid(wl.nitems, 2), kSolveThreads, solve_smem_bytes<T, NR>(),
+                             s>>>(sn, children, pairs, wl, nrhs, x, ldx, scale_sqrt, status);
   });
   note_launches(1);
 }
@@ -1456,8 +1457,12 @@ void launch_bwd_tree(const SolveNode<T>* sn, const WaveLevel& wl, double* x, int
   if (wl.nitems <= 0) return;
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
-    k_bwd_tree<T, NR><<<wave_grid(wl.nitems), kSolveThreads, solve_smem_bytes<T, NR>(), s>>>(
-        sn, wl, nrhs, x, ldx, diag_mode, status);
+    if (wl.ctas_per_sm >= 3)
+      k_bwd_tree<T, NR, 3><<<wave_grid(wl.nitems, 3), kSolveThreads, solve_smem_bytes<T, NR>(),
+                             s>>>(sn, wl, nrhs, x, ldx, diag_mode, status);
+    else
+      k_bwd_tree<T, NR, 2><<<wave_grid(wl.nitems, 2), kSolveThreads, solve_smem_bytes<T, NR>(),
+                             s>>>(sn, wl, nrhs, x, ldx, diag_mode, status);
   });
   note_launches(1);
 }
@@ -1480,8 +1485,10 @@ void solve_init() {
         set(k_bwd_step<T, NR, kStepFused>, solve_smem_bytes<T, NR>());
         set(k_bwd_step<T, NR, kStepSolve>, solve_smem_bytes<T, NR>());
         set(k_bwd_step<T, NR, kStepUpdate>, solve_smem_bytes<T, NR>());
-        set(k_fwd_tree<T, NR>, solve_smem_bytes<T, NR>());
-        set(k_bwd_tree<T, NR>, solve_smem_bytes<T, NR>());
+        set(k_fwd_tree<T, NR, 2>, solve_smem_bytes<T, NR>());
+        set(k_bwd_tree<T, NR, 2>, solve_smem_bytes<T, NR>());
+        set(k_fwd_tree<T, NR, 3>, solve_smem_bytes<T, NR>());
+        set(k_bwd_tree<T, NR, 3>, solve_smem_bytes<T, NR>());
       });
     }
   });

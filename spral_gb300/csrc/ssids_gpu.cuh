@@ -332,6 +332,7 @@ struct WaveLevel {
   // optional trace (nullptr: off): per item, the global timer when a CTA
   // took it, when its last wait was over, when it finished, and the SM
   unsigned long long* trace;
+  int ctas_per_sm;  // persistent CTAs per SM: 3 when small fronts dominate, else 2
 };
 
 constexpr int kSolveBlk = 64;   // diagonal block of the blocked triangular solves
