@@ -1467,8 +1467,13 @@ __device__ __forceinline__ bool test_pivots(double a11, double a21, double a22, 
       const double det0 = (a11 * detscale) * a22, det1 = (a21 * detscale) * a21;
       const double detpiv = det0 - det1;
       if (!(fabs(detpiv) < fmax(small, fmax(fabs(det0 / 2), fabs(det1 / 2))))) {
-        const double d0 = (a22 * detscale) / detpiv, d1 = (-a21 * detscale) / detpiv;
-        const double d3 = (a11 * detscale) / detpiv;
+        // the three divisions side by side in lanes 0, 1, 2 (the same
+        // operations, so the same bits, in one division's latency)
+        const int lane = threadIdx.x & 31;
+        const double num = lane == 0 ? a22 * detscale : lane == 1 ? -a21 * detscale : a11 * detscale;
+        const double q = num / detpiv;
+        const double d0 = __shfl_sync(0xffffffffu, q, 0), d1 = __shfl_sync(0xffffffffu, q, 1);
+        const double d3 = __shfl_sync(0xffffffffu, q, 2);
         bool ok;
         if (fmax(maxp, maxt) < small) ok = true;
         else {
