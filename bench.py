@@ -247,19 +247,27 @@ def hbm_peak_gbs():
         return 6800.0, "fallback 6.8 TB/s"
 
 
-def hbm_rooflines(ak, L, fk, ph_ms, b_d, x_d, n, nrhs):
+def hbm_rooflines(ak, L, fk, ph_ms, b_d, x_d, n, nrhs, fp64_peak):
     """HBM rooflines of the solve and of the assembly (FP64 path), with the
     algorithmic byte counts: solve = 2 sum_nodes m*nelim*8 (L read in the
     forward and the backward pass) + sum_nodes 2*nelim*8 (D) + 2 sum_nodes
     m*nrhs*8*2 (local vectors gathered and scattered); assembly = sum over
     children cm(cm+1)/2 * (8 read + 8 parent write: the extend-add zeroes
     the parent's contribution columns in L2 before adding) + 4 cm (row map)
-    plus loading A: nnz * (8 value + 16 index pair + 8 front)."""
+    plus loading A: nnz * (8 value + 16 index pair + 8 front).
+
+    The FP64 solve also has a compute roofline: 2 passes x 2 flops x nrhs
+    per strictly-lower entry of L, sum_nodes (m*nelim - nelim(nelim+1)/2),
+    against the FP64 FMA rate.  On this GPU that bound (about 1.7 ms for the
+    48^3 Laplacian's 8 right-hand sides) lies ten times above the HBM one,
+    so the FP64 solve cannot reach a large fraction of HBM bandwidth."""
     import torch
     peak, src = hbm_peak_gbs()
     nrow, ncol = ak.front_sizes()
     solve_bytes = float(2 * (nrow * ncol).sum() * 8 + (2 * ncol * 8).sum()
                         + 2 * (nrow * nrhs * 8 * 2).sum())
+    nrow64, ncol64 = nrow.astype(np.int64), ncol.astype(np.int64)
+    solve_flops = float(2 * 2 * nrhs * (nrow64 * ncol64 - ncol64 * (ncol64 + 1) // 2).sum())
     times = []
     for _ in range(5):
         x_d.copy_(b_d)
@@ -278,12 +286,46 @@ def hbm_rooflines(ak, L, fk, ph_ms, b_d, x_d, n, nrhs):
             "solve": {"bytes": solve_bytes, "ms": t_solve * 1e3,
                       "achieved": solve_bytes / t_solve / 1e9,
                       "frac": solve_bytes / t_solve / 1e9 / peak,
-                      "note": f"one {nrhs}-RHS forward+backward solve, FP64 factors"},
+                      "flops": solve_flops,
+                      "fp64_tflops": solve_flops / t_solve / 1e12,
+                      "fp64_frac": (solve_flops / t_solve / 1e12 / fp64_peak
+                                    if fp64_peak > 0 else None),
+                      "fp64_bound_ms": (solve_flops / fp64_peak / 1e9
+                                        if fp64_peak > 0 else None),
+                      "hbm_bound_ms": solve_bytes / peak / 1e6,
+                      "note": f"one {nrhs}-RHS forward+backward solve, FP64 factors; "
+                              "fp64_* = the same solve against the FP64 FMA rate, "
+                              "its binding roofline on this GPU"},
             "assembly": {"bytes": asm_bytes, "ms": t_asm * 1e3,
                          "achieved": asm_bytes / t_asm / 1e9 if t_asm > 0 else None,
                          "frac": asm_bytes / t_asm / 1e9 / peak if t_asm > 0 else None,
                          "note": "load A + extend-add phases of one factorisation "
                                  "(phase timer, CUDA events)"}}
+
+
+def solve_roofline_f32(ak, fk, b_d, x_d, n, nrhs):
+    """HBM roofline of one forward+backward solve with FP32 factors: the
+    FP64 path's byte count with 4-byte entries of L and of the local
+    vectors (D stays FP64).  Both passes run as one persistent launch each
+    and are bound by the chain of dependent pivot blocks, not by bytes."""
+    import torch
+    peak, src = hbm_peak_gbs()
+    nrow, ncol = ak.front_sizes()
+    nbytes = float(2 * (nrow * ncol).sum() * 4 + (2 * ncol * 8).sum()
+                   + 2 * (nrow * nrhs * 4 * 2).sum())
+    times = []
+    for _ in range(5):
+        x_d.copy_(b_d)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fk.solve_dev(x_d.data_ptr(), nrhs, n)
+        times.append(time.perf_counter() - t0)
+    t = float(np.median(times))
+    return {"bytes": nbytes, "ms": t * 1e3, "achieved": nbytes / t / 1e9, "peak": peak,
+            "unit": "GB/s", "frac": nbytes / t / 1e9 / peak, "peak_source": src,
+            "hbm_bound_ms": nbytes / peak / 1e6,
+            "note": f"one {nrhs}-RHS forward+backward solve, FP32 factors (host clock "
+                    "around a call that returns with its stream idle)"}
 
 
 def tf32_peak_tflops():
@@ -445,8 +487,8 @@ def run_gpu(args):
     L.spral_ssids_gpu_phase_times(fk.num, ph_ms.ctypes.data_as(ctypes.c_void_p),
                                   ph_cnt.ctypes.data_as(ctypes.c_void_p))
     L.spral_ssids_gpu_set_profiling(fk.num, 0)
-    bandwidth = hbm_rooflines(ak, L, fk, ph_ms, b_d, x_d, n, nrhs)
     fp64_peak = L.spral_ssids_gpu_fp64_peak_tflops(local)
+    bandwidth = hbm_rooflines(ak, L, fk, ph_ms, b_d, x_d, n, nrhs, fp64_peak)
     achieved = ps[1] / (ps[0] * 1e-3) / 1e12 if ps[0] > 0 else 0.0
     traffic = None
     tfile = os.path.join(HERE, "profiles", "contrib_gemm_fp64_lap3d48.md")
@@ -499,7 +541,8 @@ def run_gpu(args):
                  "p99_ms": float(np.percentile(mper, 99)),
                  "gpu_launches": int(mlaunch),
                  "speedup_vs_fp64_gpu": (1000.0 / mms) / (1000.0 / ms),
-                 "roofline": tensor_roofline(L, fm, aval_d)}
+                 "roofline": tensor_roofline(L, fm, aval_d),
+                 "solve": solve_roofline_f32(ak, fm, b_d, x_d, n, nrhs)}
         fm.free()
 
     cpu = None

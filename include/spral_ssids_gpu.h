@@ -342,6 +342,22 @@ int spral_ssids_gpu_tune_format(const char* key, const int* in, int nin, char* b
 int spral_ssids_gpu_tune_cache_lookup(const char* path, const char* key, int* out, int nout);
 int spral_ssids_gpu_tune_cache_store(const char* path, const char* key, const int* in, int nin);
 
+/* Level schedule of the numeric factorisation (host only, no GPU needed),
+ * as spral_ssids_gpu_create_symbolic_subtree builds it.  parent[i] is node
+ * i's parent (0-based, > i; -1 for a root), ncol[i] its fully-summed
+ * columns, small[i] != 0 marks the nodes of small leaf subtrees (NULL: none).
+ * align: 0 root-aligned when it takes at least 10% fewer APP block steps
+ * (sum over levels of the widest front's ceil(ncol/32)) than leaf-aligned,
+ * else leaf-aligned; 1 leaf-aligned (height above the leaves),
+ * 2 root-aligned (depth below the root, as the reference's
+ * assign_nodes_to_levels, src/ssids/gpu/factor.f90:824, with the small
+ * subtrees kept leaf-aligned).  Writes level[i] and *nlev; *steps (if not
+ * NULL) the schedule's APP block steps.  Returns 1 when root-aligned, 0 when
+ * leaf-aligned, -1 on a bad argument. */
+int spral_ssids_gpu_level_schedule(int nnodes, const int* parent, const int* ncol,
+                                   const char* small, int align, int* level, int* nlev,
+                                   int64_t* steps);
+
 /* The contribution update of one front, C -= L21 (L21 D)^T on the lower
  * triangle of the cm x cm block C, on the SIMT kernel of the numeric
  * factorisation, applied reps times on the caller's device buffers and

@@ -117,6 +117,7 @@ def _declare(L):
     f("spral_ssids_gpu_tune_format", I, ctypes.c_char_p, P, I, ctypes.c_char_p, I)
     f("spral_ssids_gpu_tune_cache_lookup", I, ctypes.c_char_p, ctypes.c_char_p, P, I)
     f("spral_ssids_gpu_tune_cache_store", I, ctypes.c_char_p, ctypes.c_char_p, P, I)
+    f("spral_ssids_gpu_level_schedule", I, I, P, P, P, I, P, P, P)
     f("spral_ssids_gpu_mbar_timeout_probe", I, I)
     f("spral_ssids_gpu_wave_timeout_probe", I, I)
     f("spral_ssids_gpu_inject_alloc_failure", None, I)

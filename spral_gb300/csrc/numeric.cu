@@ -31,6 +31,7 @@
 #include "spral_ssids_gpu.h"
 #include "ssids_gpu.cuh"
 #include "tune.h"
+#include "schedule.h"
 
 namespace ssids300 {
 
@@ -319,6 +320,7 @@ static T* upload(const std::vector<T>& v) {
 // ---------------------------------------------------------------------------
 struct Symbolic {
   int device = 0, n = 0, nnodes = 0, nlev = 0;
+  bool root_aligned = false;  // level schedule (see build_symbolic)
   std::vector<int> sptr, ncol, nrow, parent;  // per node (0-based; parent -1 = root)
   std::vector<int64_t> rptr, nptr;
   std::vector<int> rlist;
@@ -421,12 +423,44 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
   S->children.assign(nn, {});
   for (int i = nn - 1; i >= 0; --i)
     if (S->parent[i] >= 0) S->children[S->parent[i]].push_back(i);
-  // levels (leaves = 0)
-  std::vector<int> lev(nn, 0);
+  // small leaf subtrees: flops below each node, then from every leaf up
+  // while the subtree stays below the threshold (a single node is not a
+  // subtree).  Each marked set is a whole subtree: nodes are in postorder,
+  // and the first leaf of an unmarked range walks up to the highest node
+  // below the threshold, whose subtree starts at that leaf.
+  std::vector<char> insl(nn, 0);
+  {
+    const int64_t thr = opts ? opts->small_subtree_threshold : int64_t(4000000);
+    std::vector<int64_t> fl(nn + 1, 0);
+    for (int i = 0; i < nn; ++i) {
+      for (int k = 0; k < S->ncol[i]; ++k) fl[i] += (int64_t)(S->nrow[i] - k) * (S->nrow[i] - k);
+      fl[S->parent[i] >= 0 ? S->parent[i] : nn] += fl[i];
+    }
+    for (int i = 0; i < nn;) {
+      if (!S->children[i].empty()) { ++i; continue; }
+      int last = i;
+      for (int cur = i; cur >= 0 && cur < nn; cur = S->parent[cur]) {
+        if (fl[cur] >= thr) break;
+        last = cur;
+      }
+      if (last == i) { ++i; continue; }
+      for (int j = i; j <= last; ++j) insl[j] = 1;
+      i = last + 1;
+    }
+  }
+  // levels (schedule.cpp): root-aligned where that takes at least 10%
+  // fewer APP block steps, else leaf-aligned; SPRAL_GB300_LEVEL_ALIGN =
+  // leaf | root forces one
+  std::vector<int> lev;
   int nlev = 0;
-  for (int i = 0; i < nn; ++i) {
-    for (int c : S->children[i]) lev[i] = std::max(lev[i], lev[c] + 1);
-    nlev = std::max(nlev, lev[i] + 1);
+  {
+    const char* al = getenv("SPRAL_GB300_LEVEL_ALIGN");
+    const LevelAlign align = !al ? LevelAlign::Choose
+                             : std::string(al) == "root" ? LevelAlign::Root
+                             : std::string(al) == "leaf" ? LevelAlign::Leaf
+                                                         : LevelAlign::Choose;
+    S->root_aligned =
+        level_schedule(nn, S->parent.data(), S->ncol.data(), insl.data(), align, lev, nlev);
   }
   {
     // split crowded levels: kernels index a level's fronts in blockIdx.y
@@ -556,31 +590,8 @@ static Symbolic* build_symbolic(int device, int n, int sa, int en, const int* sp
     S->d_acol = upload(acol);
     S->d_asrc = upload(asrc);
   }
-  // small leaf subtrees: flops below each node, then from every leaf up
-  // while the subtree stays below the threshold (a single node is not a
-  // subtree)
-  {
-    const int64_t thr = opts ? opts->small_subtree_threshold : int64_t(4000000);
-    std::vector<int64_t> fl(nn + 1, 0);
-    for (int i = 0; i < nn; ++i) {
-      for (int k = 0; k < S->ncol[i]; ++k) fl[i] += (int64_t)(S->nrow[i] - k) * (S->nrow[i] - k);
-      fl[S->parent[i] >= 0 ? S->parent[i] : nn] += fl[i];
-    }
-    std::vector<char> insl(nn, 0);
-    for (int i = 0; i < nn;) {
-      if (!S->children[i].empty()) { ++i; continue; }
-      int last = i;
-      for (int cur = i; cur >= 0 && cur < nn; cur = S->parent[cur]) {
-        if (fl[cur] >= thr) break;
-        last = cur;
-      }
-      if (last == i) { ++i; continue; }
-      for (int j = i; j <= last; ++j) insl[j] = 1;
-      i = last + 1;
-    }
-    S->tpp_only.assign(nn, 0);
-    for (int i = 0; i < nn; ++i) S->tpp_only[S->front_of[i]] = insl[i];
-  }
+  S->tpp_only.assign(nn, 0);
+  for (int i = 0; i < nn; ++i) S->tpp_only[S->front_of[i]] = insl[i];
   std::vector<int> fronts(nn);
   S->lvl_napp.assign(nlev, 0);
   for (int l = 0; l < nlev; ++l) {

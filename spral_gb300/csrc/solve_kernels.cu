@@ -809,10 +809,16 @@ __device__ bool fwd_block(const SolveNode<T>& sn, int code, int nrhs, double* x,
       yb[c * NR + q] = (c < jb && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + c0 + c]) : T(0);
     }
     __syncthreads();
+    // a warp's 32 rows and 16 columns are warp-uniform: a warp wholly past
+    // the block's rows or columns holds zeros of L and skips the products
+    // (the padded tiles of narrow fronts; with FP64 factors the passes are
+    // bound by the FMA rate)
+    if (cq * 16 < jb && (r & ~31) < rows) {
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
+      for (int k = 0; k < 16; ++k)
 #pragma unroll
-      for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(cq * 16 + k) * NR + q];
+        for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(cq * 16 + k) * NR + q];
+    }
     __syncthreads();
   }
   if (!ok) {
@@ -844,10 +850,12 @@ __device__ bool fwd_block(const SolveNode<T>& sn, int code, int nrhs, double* x,
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < NR; ++q) acc[q] = T(0);
+    if (cq * 16 < rows && (r & ~31) < rows) {
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
+      for (int k = 0; k < 16; ++k)
 #pragma unroll
-      for (int q = 0; q < NR; ++q) acc[q] += bv[k] * yb[(cq * 16 + k) * NR + q];
+        for (int q = 0; q < NR; ++q) acc[q] += bv[k] * yb[(cq * 16 + k) * NR + q];
+    }
 #pragma unroll
     for (int q = 0; q < NR; ++q) red[(cq * NR + q) * SB + r] = acc[q];
     __syncthreads();
@@ -993,6 +1001,9 @@ __device__ void bwd_l21_item(const SolveNode<T>& sn, int t, int nrhs, T* xs, T* 
   const T* Lp = sn.L + (int64_t)(c0 + col) * sn.ld + R0 + rq * 64;
   // two batches of 32 loads in flight: the item is bound by their latency
   for (int kb = 0; kb < 64; kb += 32) {
+    // warp-uniform: a warp's columns past the block, or a batch of rows
+    // past the chunk, hold zeros of L
+    if ((col & ~31) >= jb || rq * 64 + kb >= nr) continue;
     T lv[32];
 #pragma unroll
     for (int k = 0; k < 32; ++k)
@@ -1079,10 +1090,13 @@ __device__ bool bwd_block(const SolveNode<T>& sn, int b, int nrhs, double* x, in
             (rr < nr && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + R0 + rr]) : T(0);
       }
       __syncthreads();
+      // warp-uniform skip of columns past the block or rows past the tile
+      if ((c & ~31) < jb && rq * 16 < nr) {
 #pragma unroll
-      for (int k = 0; k < 16; ++k)
+        for (int k = 0; k < 16; ++k)
 #pragma unroll
-        for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(rq * 16 + k) * NR + q];
+          for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(rq * 16 + k) * NR + q];
+      }
       __syncthreads();
     }
   }
@@ -1103,10 +1117,12 @@ __device__ bool bwd_block(const SolveNode<T>& sn, int b, int nrhs, double* x, in
       yb[rr * NR + q] = (rr < nr && q < nrhs) ? __ldcg(&sn.xloc[(int64_t)q * m + R0 + rr]) : T(0);
     }
     __syncthreads();
+    if ((c & ~31) < jb && rq * 16 < nr) {
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
+      for (int k = 0; k < 16; ++k)
 #pragma unroll
-      for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(rq * 16 + k) * NR + q];
+        for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(rq * 16 + k) * NR + q];
+    }
     __syncthreads();
   }
   if (!ok) {
@@ -1137,10 +1153,12 @@ __device__ bool bwd_block(const SolveNode<T>& sn, int b, int nrhs, double* x, in
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < NR; ++q) acc[q] = T(0);
+    if ((c & ~31) < jb && rq * 16 < jb) {
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
+      for (int k = 0; k < 16; ++k)
 #pragma unroll
-      for (int q = 0; q < NR; ++q) acc[q] += bv[k] * yb[(rq * 16 + k) * NR + q];
+        for (int q = 0; q < NR; ++q) acc[q] += bv[k] * yb[(rq * 16 + k) * NR + q];
+    }
 #pragma unroll
     for (int q = 0; q < NR; ++q) red[(rq * NR + q) * SB + c] = acc[q];
     __syncthreads();
