@@ -1349,7 +1349,8 @@ namespace tpps {
 enum Kind : int { kStop = 0, kZeroNel, kZeroSwap, kTwo, kOne, kSingular };
 struct Decision {
   int kind, t, p;
-  double d0, d1, d3;
+  double d0, d1, d3;  // FP64 factors: D^{-1} of the pivot
+  float f0, f1, f3;   // FP32 factors: the L columns' multipliers
 };
 
 __device__ __forceinline__ bool wall(bool b) { return __all_sync(0xffffffffu, b); }
@@ -1365,9 +1366,11 @@ __device__ __forceinline__ unsigned long long mag_key(float v) {
 __device__ __forceinline__ unsigned long long mag_key(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
 }
+// the value of a key, in the factor precision (FP32 factors: no conversion
+// to FP64, whose instructions issue slowly)
 template <typename T>
-__device__ __forceinline__ double key_value(unsigned long long k) {
-  if constexpr (sizeof(T) == 4) return (double)__uint_as_float((unsigned)k);
+__device__ __forceinline__ T key_value(unsigned long long k) {
+  if constexpr (sizeof(T) == 4) return __uint_as_float((unsigned)k);
   else return __longlong_as_double((long long)k);
 }
 // the key below which an entry's magnitude is < s (s >= 0): the key of the
@@ -1389,12 +1392,37 @@ __device__ __forceinline__ unsigned long long warp_key_max(unsigned long long k)
   else return warp_max_u64(k);
 }
 
-// all |entries| of row/column idx (row part from `from`) below small
-// (check_col_small, ldlt_tpp.cxx:21-28)
+// The thresholds of a TPP search, formed once per front: the key below
+// which an entry counts as zero, and small and u in the factor precision
+// (FP32: small rounded up, so that (v < small_t) == ((double)v < small) for
+// every FP32 v; the conversions are FP64 instructions, kept off the
+// per-pivot path)
 template <typename T>
-__device__ bool col_small(const T* S, int ld, int idx, int from, int m, double small) {
+struct Thr {
+  unsigned long long sk;
+  T small, u;
+};
+template <typename T>
+__device__ __forceinline__ Thr<T> make_thr(double u, double small) {
+  Thr<T> t;
+  t.sk = below_key<T>(small);
+  if constexpr (sizeof(T) == 4) {
+    float f = (float)small;
+    if ((double)f < small) f = nextafterf(f, INFINITY);
+    t.small = f;
+    t.u = (float)u;
+  } else {
+    t.small = small;
+    t.u = u;
+  }
+  return t;
+}
+
+// all |entries| of row/column idx (row part from `from`) below small
+// (check_col_small, ldlt_tpp.cxx:21-28); sk = the threshold's key
+template <typename T>
+__device__ bool col_small(const T* S, int ld, int idx, int from, int m, unsigned long long sk) {
   const int lane = threadIdx.x & 31;
-  const unsigned long long sk = below_key<T>(small);
   bool ok = true;
   for (int c = from + lane; c < idx; c += 32) ok = ok && (mag_key(S[(size_t)c * ld + idx]) < sk);
   for (int r = idx + lane; r < m; r += 32) ok = ok && (mag_key(S[(size_t)idx * ld + r]) < sk);
@@ -1403,7 +1431,7 @@ __device__ bool col_small(const T* S, int ld, int idx, int from, int m, double s
 // largest |entry| of row/column col excluding position excl and the
 // diagonal (find_rc_abs_max_exclude, ldlt_tpp.cxx:80-92)
 template <typename T>
-__device__ double rc_max(const T* S, int ld, int col, int nel, int m, int excl) {
+__device__ T rc_max(const T* S, int ld, int col, int nel, int m, int excl) {
   const int lane = threadIdx.x & 31;
   unsigned long long k = 0;
   for (int c = nel + lane; c < col; c += 32)
@@ -1451,16 +1479,17 @@ __device__ void sym_swap(T* S, int ld, int m, int i, int j, int* perm, int* opos
 }
 // The 2x2 test of (t, p) (test_2x2, ldlt_tpp.cxx:95-126), then the 1x1
 // test of p (ldlt_tpp.cxx:216-236): true with d set when p is taken.  FP64
-// factors: FP64 arithmetic as the reference.  FP32 factors: FP32 arithmetic,
-// as the FP32 APP block takes its 2x2 test, so the serial search issues no
-// FP64 instruction (on GB300 a division alone is a long chain of slow FP64
-// instructions); D^{-1} of the chosen pivots is formed in FP64 afterwards
-// (tpp_finish_d), and d0..d3 here only scale the L columns.
+// factors: FP64 arithmetic as the reference.  FP32 factors: FP32 arithmetic
+// on the FP32 entries and maxima, as the FP32 APP block takes its 2x2 test,
+// so the serial search issues no FP64 instruction, conversions included (on
+// GB300 a division alone is a long chain of slow FP64 instructions); D^{-1}
+// of the chosen pivots is formed in FP64 afterwards (tpp_finish_d), and
+// f0..f3 here only scale the L columns.
 template <typename T>
-__device__ __forceinline__ bool test_pivots(double a11, double a21, double a22, double maxt,
-                                            double maxp, double u, double small, int t, int p,
-                                            Decision& d) {
+__device__ __forceinline__ bool test_pivots(T a11, T a21, T a22, T maxt, T maxp,
+                                            const Thr<T> th, int t, int p, Decision& d) {
   if constexpr (sizeof(T) == 8) {
+    const double u = th.u, small = th.small;
     const double maxpiv = fmax(fabs(a11), fmax(fabs(a21), fabs(a22)));
     if (!(maxpiv < small)) {
       const double detscale = 1 / maxpiv;
@@ -1489,12 +1518,10 @@ __device__ __forceinline__ bool test_pivots(double a11, double a21, double a22, 
     return false;
   } else {
     // the entries and maxima are FP32 values; thresholds in FP32
-    float fsmall = (float)small;
-    if ((double)fsmall < small) fsmall = nextafterf(fsmall, INFINITY);
-    const float fu = (float)u;
-    const float b11 = (float)a11, b21 = (float)a21, b22 = (float)a22;
-    const float mt = (float)maxt;
-    float mp = (float)maxp;
+    const float fsmall = th.small, fu = th.u;
+    const float b11 = a11, b21 = a21, b22 = a22;
+    const float mt = maxt;
+    float mp = maxp;
     const float maxpiv = fmaxf(fabsf(b11), fmaxf(fabsf(b21), fabsf(b22)));
     if (!(maxpiv < fsmall)) {
       const float detscale = 1.0f / maxpiv;
@@ -1510,7 +1537,7 @@ __device__ __forceinline__ bool test_pivots(double a11, double a21, double a22, 
           const float x2 = fabsf(d1) * mt + fabsf(d3) * mp;
           ok = (fu * fmaxf(x1, x2) < 1.0f);
         }
-        if (ok) { d.kind = kTwo; d.t = t; d.p = p; d.d0 = d0; d.d1 = d1; d.d3 = d3; return true; }
+        if (ok) { d.kind = kTwo; d.t = t; d.p = p; d.f0 = d0; d.f1 = d1; d.f3 = d3; return true; }
       }
     }
     mp = fmaxf(mp, fabsf(b21));
@@ -1520,23 +1547,23 @@ __device__ __forceinline__ bool test_pivots(double a11, double a21, double a22, 
 }
 // the pivot search of one step of ldlt_tpp_factor, in warp 0
 template <typename T>
-__device__ Decision decide(const T* S, int ld, int nel, int m, int n, bool action, double u,
-                           double small) {
+__device__ Decision decide(const T* S, int ld, int nel, int m, int n, bool action,
+                           const Thr<T> th) {
   Decision d{kStop, 0, 0, 0.0, 0.0, 0.0};
-  if (col_small(S, ld, nel, nel, m, small)) { d.kind = action ? kZeroNel : kSingular; return d; }
+  if (col_small(S, ld, nel, nel, m, th.sk)) { d.kind = action ? kZeroNel : kSingular; return d; }
   for (int p = nel + 1; p < n; ++p) {
-    if (col_small(S, ld, p, nel, m, small)) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return d; }
+    if (col_small(S, ld, p, nel, m, th.sk)) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return d; }
     const int t = row_argmax(S, ld, p, nel);
-    const double maxt = rc_max(S, ld, t, nel, m, p);
-    const double maxp = rc_max(S, ld, p, nel, m, t);
-    const double a11 = (double)S[(size_t)t * ld + t], a21 = (double)S[(size_t)t * ld + p];
-    const double a22 = (double)S[(size_t)p * ld + p];
-    if (test_pivots<T>(a11, a21, a22, maxt, maxp, u, small, t, p, d)) return d;
+    const T maxt = rc_max(S, ld, t, nel, m, p);
+    const T maxp = rc_max(S, ld, p, nel, m, t);
+    const T a11 = S[(size_t)t * ld + t], a21 = S[(size_t)t * ld + p];
+    const T a22 = S[(size_t)p * ld + p];
+    if (test_pivots<T>(a11, a21, a22, maxt, maxp, th, t, p, d)) return d;
   }
   // last resort: nel itself as a 1x1 pivot
-  const double maxp = rc_max(S, ld, nel, nel, m, -1);
-  if (sizeof(T) == 8 ? fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp
-                     : fabsf((float)S[(size_t)nel * ld + nel]) >= (float)u * (float)maxp) {
+  const T maxp = rc_max(S, ld, nel, nel, m, -1);
+  if (sizeof(T) == 8 ? fabs((double)S[(size_t)nel * ld + nel]) >= (double)th.u * (double)maxp
+                     : fabsf((float)S[(size_t)nel * ld + nel]) >= (float)th.u * (float)maxp) {
     d.kind = kOne;
     d.p = nel;
   }
@@ -1579,10 +1606,9 @@ __device__ __forceinline__ LineInfo line_shfl(const LineInfo& a, int o) {
   return b;
 }
 template <typename T>
-__device__ LineInfo line_info(const T* S, int ld, int idx, int nel, int m, double small,
-                              LineInfo* sh) {
+__device__ LineInfo line_info(const T* S, int ld, int idx, int nel, int m,
+                              unsigned long long sk, LineInfo* sh) {
   LineInfo a{1, 0, 0x7fffffff, 0, 0x7fffffff, 0, 0x7fffffff};
-  const unsigned long long sk = below_key<T>(small);
   for (int c = nel + (int)threadIdx.x; c < idx; c += blockDim.x) {
     const unsigned long long v = mag_key(S[(size_t)c * ld + idx]);
     a.all_small = a.all_small && (v < sk);
@@ -1609,10 +1635,9 @@ __device__ LineInfo line_info(const T* S, int ld, int idx, int nel, int m, doubl
 // the line information of lines [l0, l1) (one warp per line) into
 // out[idx - nel], then a barrier
 template <typename T>
-__device__ void line_info_batch(const T* S, int ld, int l0, int l1, int nel, int m, double small,
-                                LineInfo* out) {
+__device__ void line_info_batch(const T* S, int ld, int l0, int l1, int nel, int m,
+                                unsigned long long sk, LineInfo* out) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const unsigned long long sk = below_key<T>(small);
   for (int idx = l0 + warp; idx < l1; idx += nw) {
     LineInfo a{1, 0, 0x7fffffff, 0, 0x7fffffff, 0, 0x7fffffff};
     for (int c = nel + lane; c < idx; c += 32) {
@@ -1641,15 +1666,15 @@ __device__ void line_info_batch(const T* S, int ld, int l0, int l1, int nel, int
 // (t, p) or a 1x1 pivot).
 template <typename T>
 __device__ bool try_candidate(const T* S, int ld, int p, const LineInfo& lp, const LineInfo& lt,
-                              bool action, double u, double small, Decision& d) {
+                              bool action, const Thr<T> th, Decision& d) {
   if (lp.all_small) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return true; }
   const int t = lp.ri;
-  const double maxp = key_value<T>((lp.i1 == t) ? lp.v2 : lp.v1);
+  const T maxp = key_value<T>((lp.i1 == t) ? lp.v2 : lp.v1);
   // largest |entry| of line t off its diagonal, excluding position p
-  const double maxt = key_value<T>((lt.i1 == p) ? lt.v2 : lt.v1);
-  const double a11 = (double)S[(size_t)t * ld + t], a21 = (double)S[(size_t)t * ld + p];
-  const double a22 = (double)S[(size_t)p * ld + p];
-  return test_pivots<T>(a11, a21, a22, maxt, maxp, u, small, t, p, d);
+  const T maxt = key_value<T>((lt.i1 == p) ? lt.v2 : lt.v1);
+  const T a11 = S[(size_t)t * ld + t], a21 = S[(size_t)t * ld + p];
+  const T a22 = S[(size_t)p * ld + p];
+  return test_pivots<T>(a11, a21, a22, maxt, maxp, th, t, p, d);
 }
 
 // the pivot search of one step of ldlt_tpp_factor with all threads (each
@@ -1661,47 +1686,46 @@ __device__ bool try_candidate(const T* S, int ld, int p, const LineInfo& lp, con
 // systems) reads each line once instead of twice per candidate.  The
 // records equal line_info's, so the decision is the same either way.
 template <typename T>
-__device__ Decision decide_cta(const T* S, int ld, int nel, int m, int n, bool action, double u,
-                               double small, LineInfo* sh, LineInfo* batch) {
+__device__ Decision decide_cta(const T* S, int ld, int nel, int m, int n, bool action,
+                               const Thr<T> th, LineInfo* sh, LineInfo* batch) {
   Decision d{kStop, 0, 0, 0.0, 0.0, 0.0};
-  if (line_info(S, ld, nel, nel, m, small, sh).all_small) {
+  if (line_info(S, ld, nel, nel, m, th.sk, sh).all_small) {
     d.kind = action ? kZeroNel : kSingular;
     return d;
   }
   int p = nel + 1;
   if (p < n) {
-    const LineInfo lp = line_info(S, ld, p, nel, m, small, sh);
-    const LineInfo lt = line_info(S, ld, lp.ri, nel, m, small, sh);
-    if (try_candidate(S, ld, p, lp, lt, action, u, small, d)) return d;
+    const LineInfo lp = line_info(S, ld, p, nel, m, th.sk, sh);
+    const LineInfo lt = line_info(S, ld, lp.ri, nel, m, th.sk, sh);
+    if (try_candidate(S, ld, p, lp, lt, action, th, d)) return d;
     ++p;
   }
   if (batch != nullptr && p < n) {
-    line_info_batch(S, ld, nel, n, nel, m, small, batch);
+    line_info_batch(S, ld, nel, n, nel, m, th.sk, batch);
     for (; p < n; ++p) {
       const LineInfo lp = batch[p - nel];
-      if (try_candidate(S, ld, p, lp, batch[(lp.all_small ? p : lp.ri) - nel], action, u, small,
-                        d))
+      if (try_candidate(S, ld, p, lp, batch[(lp.all_small ? p : lp.ri) - nel], action, th, d))
         return d;
     }
     const LineInfo ln = batch[0];
-    const double maxp = key_value<T>(ln.v1);
-    if (sizeof(T) == 8 ? fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp
-                       : fabsf((float)S[(size_t)nel * ld + nel]) >= (float)u * (float)maxp) {
+    const T maxp = key_value<T>(ln.v1);
+    if (sizeof(T) == 8 ? fabs((double)S[(size_t)nel * ld + nel]) >= (double)th.u * (double)maxp
+                       : fabsf((float)S[(size_t)nel * ld + nel]) >= (float)th.u * (float)maxp) {
       d.kind = kOne;
       d.p = nel;
     }
     return d;
   }
   for (; p < n; ++p) {
-    const LineInfo lp = line_info(S, ld, p, nel, m, small, sh);
+    const LineInfo lp = line_info(S, ld, p, nel, m, th.sk, sh);
     if (lp.all_small) { d.kind = action ? kZeroSwap : kSingular; d.p = p; return d; }
-    const LineInfo lt = line_info(S, ld, lp.ri, nel, m, small, sh);
-    if (try_candidate(S, ld, p, lp, lt, action, u, small, d)) return d;
+    const LineInfo lt = line_info(S, ld, lp.ri, nel, m, th.sk, sh);
+    if (try_candidate(S, ld, p, lp, lt, action, th, d)) return d;
   }
-  const LineInfo ln = line_info(S, ld, nel, nel, m, small, sh);
-  const double maxp = key_value<T>(ln.v1);
-  if (sizeof(T) == 8 ? fabs((double)S[(size_t)nel * ld + nel]) >= u * maxp
-                     : fabsf((float)S[(size_t)nel * ld + nel]) >= (float)u * (float)maxp) {
+  const LineInfo ln = line_info(S, ld, nel, nel, m, th.sk, sh);
+  const T maxp = key_value<T>(ln.v1);
+  if (sizeof(T) == 8 ? fabs((double)S[(size_t)nel * ld + nel]) >= (double)th.u * (double)maxp
+                     : fabsf((float)S[(size_t)nel * ld + nel]) >= (float)th.u * (float)maxp) {
     d.kind = kOne;
     d.p = nel;
   }
@@ -1718,6 +1742,15 @@ constexpr int kTppWideRows = 1024;
 template <typename T>
 __device__ __forceinline__ tpps::LineInfo* tpp_batch(const FrontDesc<T>& fd) {
   return reinterpret_cast<tpps::LineInfo*>(fd.W + 2 * (size_t)fd.ld);
+}
+
+// a b + c d in FP32 with the rounding error of c d kept (an error-free
+// product by FMA, then one fused add and one add): close to the sum formed
+// exactly and rounded once, also where the two products cancel
+__device__ __forceinline__ float dot2_f32(float a, float b, float c, float d) {
+  const float p = __fmul_rn(c, d);
+  const float e = __fmaf_rn(c, d, -p);
+  return __fadd_rn(__fmaf_rn(a, b, p), e);
 }
 
 // FP32 factors: D^{-1} of the pivots [nel0, nel1) in FP64 from the pivot
@@ -1756,21 +1789,26 @@ __device__ void tpp_finish_d(double* D, int nel0, int nel1) {
 // and D^{-1}.  Swaps cover whole lines (the rows of the eliminated columns
 // to the left included, as swap_cols with aleft, ldlt_tpp.cxx:44-72).
 // Returns the number of columns eliminated in total, or -1 for a singular
-// front with action == false.  Called by all threads of the CTA.
+// front with action == false.  Called by all threads of the CTA.  With
+// finish == false, FP32 factors leave the recorded pivot entries (the D
+// blocks themselves) in D for the caller, which forms D^{-1} with
+// tpp_finish_d afterwards.
 template <typename T>
 __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* perm, int* opos,
-                        double* D, bool action, double u, double small, tpps::LineInfo* batch) {
+                        double* D, bool action, double u, double small, tpps::LineInfo* batch,
+                        bool finish = true) {
   using namespace tpps;
   __shared__ Decision s_dec;
   __shared__ LineInfo s_line[kTppThreads / 32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int nel0 = nel;
+  const Thr<T> th = make_thr<T>(u, small);
   while (nel < n) {
     Decision dw;
     const bool wide = m - nel > kTppWideRows;
-    if (wide) dw = decide_cta(S, ld, nel, m, n, action, u, small, s_line, batch);
+    if (wide) dw = decide_cta(S, ld, nel, m, n, action, th, s_line, batch);
     if (warp == 0) {
-      Decision d = wide ? dw : decide(S, ld, nel, m, n, action, u, small);
+      Decision d = wide ? dw : decide(S, ld, nel, m, n, action, th);
       if (d.kind == kZeroSwap) sym_swap(S, ld, m, d.p, nel, perm, opos);
       if (d.kind == kZeroNel || d.kind == kZeroSwap) {
         for (int r = nel + lane; r < m; r += 32) S[(size_t)nel * ld + r] = T(0);
@@ -1799,14 +1837,12 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
       } else if (d.kind == kOne) {
         sym_swap(S, ld, m, d.p, nel, perm, opos);
         const T app = S[(size_t)nel * ld + nel];
-        double d11;
-        if constexpr (sizeof(T) == 4) d11 = (double)(1.0f / app);  // the L column's multiplier
-        else d11 = 1.0 / app;
-        d.d0 = d11;
+        if constexpr (sizeof(T) == 4) d.f0 = 1.0f / app;  // the L column's multiplier
+        else d.d0 = 1.0 / app;
         for (int r = nel + 1 + lane; r < m; r += 32) W0[r] = S[(size_t)nel * ld + r];
         if (lane == 0) {
           S[(size_t)nel * ld + nel] = T(1);
-          D[2 * nel] = sizeof(T) == 4 ? (double)app : d11;  // FP32: the pivot, see tpp_finish_d
+          D[2 * nel] = sizeof(T) == 4 ? (double)app : d.d0;  // FP32: the pivot, see tpp_finish_d
           D[2 * nel + 1] = 0.0;
         }
       }
@@ -1832,7 +1868,9 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
     // FP32 D^{-1} entries, as the APP path's L columns; D^{-1} itself stays
     // FP64), so the update issues no FP64 instruction for FP32 factors.
     const int c0 = nel + ps;
-    const T e0 = (T)d.d0, e1 = (T)d.d1, e3 = (T)d.d3;
+    T e0, e1, e3;
+    if constexpr (sizeof(T) == 4) { e0 = d.f0; e1 = d.f1; e3 = d.f3; }
+    else { e0 = d.d0; e1 = d.d1; e3 = d.d3; }
     if (ps == 1) {
       for (int r = c0 + threadIdx.x; r < m; r += blockDim.x) S[(size_t)nel * ld + r] = W0[r] * e0;
       for (int c = c0 + warp; c < n; c += nw) {
@@ -1844,25 +1882,38 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
         }
       }
     } else {
+      // FP32 factors: each L entry of a 2x2 pivot is a sum of two products
+      // that can cancel, formed with the second product's rounding error
+      // kept (dot2_f32); FP64 factors as written
       for (int r = c0 + threadIdx.x; r < m; r += blockDim.x) {
         const T a1 = W0[r], a2 = W1[r];
-        S[(size_t)nel * ld + r] = e0 * a1 + e1 * a2;
-        S[(size_t)(nel + 1) * ld + r] = e1 * a1 + e3 * a2;
+        if constexpr (sizeof(T) == 4) {
+          S[(size_t)nel * ld + r] = dot2_f32(e0, a1, e1, a2);
+          S[(size_t)(nel + 1) * ld + r] = dot2_f32(e1, a1, e3, a2);
+        } else {
+          S[(size_t)nel * ld + r] = e0 * a1 + e1 * a2;
+          S[(size_t)(nel + 1) * ld + r] = e1 * a1 + e3 * a2;
+        }
       }
       for (int c = c0 + warp; c < n; c += nw) {
         const T w0 = W0[c], w1 = W1[c];
         T* col = S + (size_t)c * ld;
         for (int r = c + lane; r < m; r += 32) {
           const T a1 = W0[r], a2 = W1[r];
-          const T l1 = e0 * a1 + e1 * a2, l2 = e1 * a1 + e3 * a2;
-          col[r] -= l1 * w0 + l2 * w1;
+          if constexpr (sizeof(T) == 4) {
+            const float l1 = dot2_f32(e0, a1, e1, a2), l2 = dot2_f32(e1, a1, e3, a2);
+            col[r] -= l1 * w0 + l2 * w1;
+          } else {
+            const T l1 = e0 * a1 + e1 * a2, l2 = e1 * a1 + e3 * a2;
+            col[r] -= l1 * w0 + l2 * w1;
+          }
         }
       }
     }
     __syncthreads();
     nel += ps;
   }
-  tpp_finish_d<T>(D, nel0, nel);
+  if (finish) tpp_finish_d<T>(D, nel0, nel);
   return nel;
 }
 
@@ -1917,20 +1968,64 @@ __device__ __forceinline__ void d_column(const double* D, int c, int nel, double
   }
 }
 
+// FP32 factors before tpp_finish_d: D holds the pivot blocks themselves
+// (1x1: d; 2x2: a11, a21, the second-half marker, a22), exact FP32 values,
+// so column c of D is read off directly, without an FP64 division
+__device__ __forceinline__ void d_column_raw(const double* D, int c, int nel, float& alpha,
+                                             float& beta, int& partner) {
+  const double d11 = D[2 * c];
+  if (isinf(d11)) {  // second column of a 2x2: (a21, a22)
+    alpha = (float)D[2 * c + 1]; beta = (float)D[2 * (c - 1) + 1]; partner = c - 1;
+  } else if (c + 1 < nel && isinf(D[2 * c + 2])) {  // first column of a 2x2: (a11, a21)
+    alpha = (float)d11; beta = (float)D[2 * c + 1]; partner = c + 1;
+  } else {
+    alpha = (float)d11; beta = 0.f; partner = c;
+  }
+}
+
 // the fused contribution of one front whose factor is at S (leading
-// dimension ldS); all threads of the CTA
+// dimension ldS); all threads of the CTA.  Column c of D, (alpha, beta,
+// partner), is formed once per column into shared memory: FP64 factors
+// from D^{-1} (d_column, FP64 divisions), FP32 factors from the recorded
+// pivot blocks (d_column_raw, before tpp_finish_d) with LD in FP32
+// arithmetic (compensated for 2x2 columns), so the FP32 contribution issues
+// no FP64 instruction per entry.
 template <typename T>
 __device__ void tpp_front_contrib(const FrontDesc<T>& fd, const T* S, int ldS, int nel) {
   const int n = fd.n, cm = fd.m - fd.n;
   if (cm <= 0 || nel <= 0) return;
-  for (int e = threadIdx.x; e < cm * nel; e += blockDim.x) {
-    const int rr = e % cm, c = e / cm;
-    double alpha, beta;
-    int partner;
-    d_column(fd.D, c, nel, alpha, beta, partner);
-    const T lv = S[(size_t)c * ldS + n + rr];
-    const T lp = (beta != 0.0) ? S[(size_t)partner * ldS + n + rr] : T(0);
-    fd.LD[(int64_t)c * cm + rr] = (T)(alpha * (double)lv + beta * (double)lp);
+  __shared__ T s_alpha[kTppThreads], s_beta[kTppThreads];
+  __shared__ int s_partner[kTppThreads];
+  for (int cb = 0; cb < nel; cb += blockDim.x) {
+    const int nc = min((int)blockDim.x, nel - cb);
+    if ((int)threadIdx.x < nc) {
+      const int c = cb + threadIdx.x;
+      int partner;
+      if constexpr (sizeof(T) == 4) {
+        float alpha, beta;
+        d_column_raw(fd.D, c, nel, alpha, beta, partner);
+        s_alpha[threadIdx.x] = alpha; s_beta[threadIdx.x] = beta;
+      } else {
+        double alpha, beta;
+        d_column(fd.D, c, nel, alpha, beta, partner);
+        s_alpha[threadIdx.x] = alpha; s_beta[threadIdx.x] = beta;
+      }
+      s_partner[threadIdx.x] = partner;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < cm * nc; e += blockDim.x) {
+      const int rr = e % cm, cc = e / cm, c = cb + cc;
+      const T alpha = s_alpha[cc], beta = s_beta[cc];
+      const T lv = S[(size_t)c * ldS + n + rr];
+      const T lp = (beta != T(0)) ? S[(size_t)s_partner[cc] * ldS + n + rr] : T(0);
+      if constexpr (sizeof(T) == 4) {
+        // a 2x2 column's two products can cancel (dot2_f32)
+        fd.LD[(int64_t)c * cm + rr] = dot2_f32(alpha, lv, beta, lp);
+      } else {
+        fd.LD[(int64_t)c * cm + rr] = alpha * lv + beta * lp;
+      }
+    }
+    __syncthreads();  // the coefficients are rewritten by the next chunk
   }
   __syncthreads();  // LD (global) is read back by other threads of this CTA
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -1951,6 +2046,9 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_level(FrontDesc<T>* fds, Fr
                                                            bool action, double u, double small,
                                                            int smem_bytes) {
   extern __shared__ __align__(16) unsigned char tpp_smem[];
+  // FP32 factors: the contribution reads the pivot blocks recorded in D,
+  // which become D^{-1} after it
+  constexpr bool raw_d = sizeof(T) == 4;
   for (int i = blockIdx.x; i < nf; i += gridDim.x) {
     const int f = fronts[i];
     FrontState* st = &sts[f];
@@ -1967,7 +2065,7 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_level(FrontDesc<T>* fds, Fr
       nel = 0;
     } else if (need > (size_t)smem_bytes) {
       nel = tpp_fast(fd.L, fd.ld, m, n, 0, fd.W, fd.W + fd.ld, fd.perm, fd.opos, fd.D, action, u,
-                     small, tpp_batch(fd));
+                     small, tpp_batch(fd), !raw_d);
     } else {
       T* S = reinterpret_cast<T*>(tpp_smem);
       T* W0 = S + (size_t)ldS * n;
@@ -1979,7 +2077,8 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_level(FrontDesc<T>* fds, Fr
           S[(size_t)c * ldS + r] = fd.L[(int64_t)c * fd.ld + r];
       for (int k = threadIdx.x; k < n; k += blockDim.x) { sperm[k] = fd.perm[k]; sopos[k] = fd.opos[k]; }
       __syncthreads();
-      nel = tpp_fast(S, ldS, m, n, 0, W0, W1, sperm, sopos, fd.D, action, u, small, nullptr);
+      nel = tpp_fast(S, ldS, m, n, 0, W0, W1, sperm, sopos, fd.D, action, u, small, nullptr,
+                     !raw_d);
       __syncthreads();
       if (nel >= 0) {
         for (int c = 0; c < n; ++c)
@@ -1996,6 +2095,7 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_level(FrontDesc<T>* fds, Fr
     }
     __syncthreads();  // D and the factor are complete
     if (nel > 0) tpp_front_contrib(fd, F, ldF, nel);
+    if (raw_d && nel > 0) tpp_finish_d<T>(fd.D, 0, nel);
   }
 }
 
@@ -2205,19 +2305,26 @@ void launch_tpp(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, boo
 // Largest dynamic shared memory of k_tpp_small: the fronts of small leaf
 // subtrees hold m * n < ~26k entries (their flops are below 4e6), about
 // 205 KB in FP64.
-constexpr int kTppSmallSmem = 222 * 1024;
+// dynamic shared memory ceiling of k_tpp_level: the 227 KB per CTA less its
+// static shared memory (the search's records and the contribution's
+// per-column coefficients, under 6 KB)
+constexpr int kTppSmallSmem = 220 * 1024;
 
 template <typename T>
 void launch_tpp_level(FrontDesc<T>* fd, FrontState* st, const int* fronts, int nf, bool action,
                       double u, double small, int max_bytes, int threads, cudaStream_t s) {
   if (nf <= 0) return;
-  static bool attr_set = false;  // per template instance, once per process
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_tpp_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kTppSmallSmem);
-    attr_set = true;
+  static int smem_cap = -1;  // per template instance, once per process
+  if (smem_cap < 0) {
+    // without the opt-in the launch keeps to the default 48 KB: fronts that
+    // do not fit are factored in global memory
+    smem_cap = cudaFuncSetAttribute(k_tpp_level<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kTppSmallSmem) == cudaSuccess
+                   ? kTppSmallSmem
+                   : 48 * 1024 - 6 * 1024;
+    cudaGetLastError();
   }
-  const int smem = std::min(std::max(max_bytes, 0), kTppSmallSmem);
+  const int smem = std::min(std::max(max_bytes, 0), smem_cap);
   threads = threads <= 32 ? 32 : threads <= 64 ? 64 : kTppThreads;
   int dev = 0, nsm = 0, occ = 0;
   cudaGetDevice(&dev);

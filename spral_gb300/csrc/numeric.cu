@@ -1759,6 +1759,9 @@ struct Numeric : NumericBase {
       pmark(tm(), kPhHost, s);
       CK(cudaMemcpyAsync(hst.data() + f0, d_st + f0, nf * sizeof(FrontState),
                          cudaMemcpyDeviceToHost, s));
+      // a launch that did not start (a configuration error) fails the
+      // factorisation as a CUDA error, not as the fronts it left untouched
+      CK(cudaGetLastError());
       CK(cudaStreamSynchronize(s));
       if (profile) ptimer.flush();
       bool singular = false, bad = false, notpd = false;
@@ -1805,6 +1808,7 @@ struct Numeric : NumericBase {
     Stats hs;
     CK(cudaMemcpyAsync(&hs, d_stats, sizeof(Stats), cudaMemcpyDeviceToHost, s));
     CK(cudaEventRecord(ev[1], s));
+    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
