@@ -1989,11 +1989,19 @@ __device__ __forceinline__ void d_column_raw(const double* D, int c, int nel, fl
 // from D^{-1} (d_column, FP64 divisions), FP32 factors from the recorded
 // pivot blocks (d_column_raw, before tpp_finish_d) with LD in FP32
 // arithmetic (compensated for 2x2 columns), so the FP32 contribution issues
-// no FP64 instruction per entry.
+// no FP64 instruction per entry.  LD goes to ldsm (shared memory, cm x nel)
+// when given, else to the front's LD workspace.  C -= L21 LD^T on the lower
+// triangle: FP32 factors in 32 x 16 tiles, one per warp at a time, lane
+// (lr, lc) = (lane % 8, lane / 8) holding rows lr + 8i and columns lc + 4j,
+// i, j < 4, so each k takes 8 loads for 16 FMAs; FP64 factors a warp per
+// column and a lane per row (their FMAs, not the loads, bound it, and the
+// tile's registers would cost a CTA per SM).  Either way every entry sums
+// its products in increasing k, one FMA each.
 template <typename T>
-__device__ void tpp_front_contrib(const FrontDesc<T>& fd, const T* S, int ldS, int nel) {
+__device__ void tpp_front_contrib(const FrontDesc<T>& fd, const T* S, int ldS, int nel, T* ldsm) {
   const int n = fd.n, cm = fd.m - fd.n;
   if (cm <= 0 || nel <= 0) return;
+  T* LD = ldsm ? ldsm : fd.LD;  // LD(r, c) at LD[c * cm + r]
   __shared__ T s_alpha[kTppThreads], s_beta[kTppThreads];
   __shared__ int s_partner[kTppThreads];
   for (int cb = 0; cb < nel; cb += blockDim.x) {
@@ -2020,23 +2028,58 @@ __device__ void tpp_front_contrib(const FrontDesc<T>& fd, const T* S, int ldS, i
       const T lp = (beta != T(0)) ? S[(size_t)s_partner[cc] * ldS + n + rr] : T(0);
       if constexpr (sizeof(T) == 4) {
         // a 2x2 column's two products can cancel (dot2_f32)
-        fd.LD[(int64_t)c * cm + rr] = dot2_f32(alpha, lv, beta, lp);
+        LD[(int64_t)c * cm + rr] = dot2_f32(alpha, lv, beta, lp);
       } else {
-        fd.LD[(int64_t)c * cm + rr] = alpha * lv + beta * lp;
+        LD[(int64_t)c * cm + rr] = alpha * lv + beta * lp;
       }
     }
     __syncthreads();  // the coefficients are rewritten by the next chunk
   }
-  __syncthreads();  // LD (global) is read back by other threads of this CTA
+  __syncthreads();  // LD is read back by other threads of this CTA
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int c = warp; c < cm; c += nw) {
-    const T* ldc = fd.LD + c;
-    for (int r = c + lane; r < cm; r += 32) {
-      const T* lr = S + n + r;
-      T acc = T(0);
-      for (int k = 0; k < nel; ++k) acc += lr[(size_t)k * ldS] * ldc[(int64_t)k * cm];
-      fd.C[(int64_t)c * fd.ldc + r] -= acc;
+  if constexpr (sizeof(T) == 8) {
+    for (int c = warp; c < cm; c += nw) {
+      const T* ldc = LD + c;
+      for (int r = c + lane; r < cm; r += 32) {
+        const T* lrow = S + n + r;
+        T acc = T(0);
+        for (int k = 0; k < nel; ++k) acc += lrow[(size_t)k * ldS] * ldc[(int64_t)k * cm];
+        fd.C[(int64_t)c * fd.ldc + r] -= acc;
+      }
     }
+    return;
+  }
+  const int lr = lane & 7, lc = lane >> 3;
+  const int nrt = (cm + 31) / 32, nct = (cm + 15) / 16;
+  for (int t = warp; t < nrt * nct; t += nw) {
+    const int rt = t % nrt, ct = t / nrt;
+    const int r0 = 32 * rt + lr, c0 = 16 * ct + lc;
+    if (32 * rt + 31 < 16 * ct) continue;  // wholly above the diagonal
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+    const T* Ap = S + n + r0;
+    const T* Bp = LD + c0;
+    for (int k = 0; k < nel; ++k) {
+      T a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = (r0 + 8 * i < cm) ? Ap[(size_t)k * ldS + 8 * i] : T(0);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = (c0 + 4 * j < cm) ? Bp[(int64_t)k * cm + 4 * j] : T(0);
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int r = r0 + 8 * i, c = c0 + 4 * j;
+        if (r < cm && c <= r) fd.C[(int64_t)c * fd.ldc + r] -= acc[i][j];
+      }
   }
 }
 
@@ -2061,12 +2104,17 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_level(FrontDesc<T>* fds, Fr
     int nel;
     const T* F = fd.L;  // where the factor is when the contribution is formed
     int ldF = fd.ld;
+    T* ldsm = nullptr;  // LD in shared memory, or the front's workspace
     if (n == 0) {
       nel = 0;
     } else if (need > (size_t)smem_bytes) {
       nel = tpp_fast(fd.L, fd.ld, m, n, 0, fd.W, fd.W + fd.ld, fd.perm, fd.opos, fd.D, action, u,
                      small, tpp_batch(fd), !raw_d);
     } else {
+      // FP32 factors: LD in the shared memory after the front when it fits
+      const size_t ld_off = (need + 15) & ~(size_t)15;
+      if (sizeof(T) == 4 && ld_off + (size_t)(m - n) * n * sizeof(T) <= (size_t)smem_bytes)
+        ldsm = reinterpret_cast<T*>(tpp_smem + ld_off);
       T* S = reinterpret_cast<T*>(tpp_smem);
       T* W0 = S + (size_t)ldS * n;
       T* W1 = W0 + ldS;
@@ -2094,7 +2142,7 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_level(FrontDesc<T>* fds, Fr
       else { st->nelim = nel; st->p = nel; st->step = 0; }
     }
     __syncthreads();  // D and the factor are complete
-    if (nel > 0) tpp_front_contrib(fd, F, ldF, nel);
+    if (nel > 0) tpp_front_contrib(fd, F, ldF, nel, ldsm);
     if (raw_d && nel > 0) tpp_finish_d<T>(fd.D, 0, nel);
   }
 }

@@ -1072,8 +1072,13 @@ struct Numeric : NumericBase {
 
   // shared-memory staging of a small leaf front (k_tpp_small): the front,
   // two workspace columns, perm and opos, bytes
+  // shared memory of a front in k_tpp_level: the front with two workspace
+  // columns, perm and opos, then (FP32 factors, 16-byte aligned) its LD
+  // block for the fused contribution
   int tpp_bytes(int f) const {
-    return ((m_[f] + 1) & ~1) * (n_[f] + 2) * (int)sizeof(T) + 8 * n_[f];
+    const int front = ((m_[f] + 1) & ~1) * (n_[f] + 2) * (int)sizeof(T) + 8 * n_[f];
+    if (sizeof(T) == 8) return front;
+    return ((front + 15) & ~15) + (m_[f] - n_[f]) * n_[f] * (int)sizeof(T);
   }
   // the level-set kernel over level l's small-subtree fronts, one launch
   // per non-empty size class, shared memory sized for the class's largest
