@@ -1873,14 +1873,6 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
     else { e0 = d.d0; e1 = d.d1; e3 = d.d3; }
     if (ps == 1) {
       for (int r = c0 + threadIdx.x; r < m; r += blockDim.x) S[(size_t)nel * ld + r] = W0[r] * e0;
-      for (int c = c0 + warp; c < n; c += nw) {
-        const T wc = W0[c];
-        T* col = S + (size_t)c * ld;
-        for (int r = c + lane; r < m; r += 32) {
-          const T l = W0[r] * e0;
-          col[r] -= l * wc;
-        }
-      }
     } else {
       // FP32 factors: each L entry of a 2x2 pivot is a sum of two products
       // that can cancel, formed with the second product's rounding error
@@ -1895,19 +1887,25 @@ __device__ int tpp_fast(T* S, int ld, int m, int n, int nel, T* W0, T* W1, int* 
           S[(size_t)(nel + 1) * ld + r] = e1 * a1 + e3 * a2;
         }
       }
+    }
+    // the trailing update reads the scaled columns back (other threads wrote
+    // them): one FMA per entry and pivot column instead of forming the
+    // multipliers again for every column
+    __syncthreads();
+    if (ps == 1) {
+      const T* l = S + (size_t)nel * ld;
+      for (int c = c0 + warp; c < n; c += nw) {
+        const T wc = W0[c];
+        T* col = S + (size_t)c * ld;
+        for (int r = c + lane; r < m; r += 32) col[r] -= l[r] * wc;
+      }
+    } else {
+      const T* l1 = S + (size_t)nel * ld;
+      const T* l2 = S + (size_t)(nel + 1) * ld;
       for (int c = c0 + warp; c < n; c += nw) {
         const T w0 = W0[c], w1 = W1[c];
         T* col = S + (size_t)c * ld;
-        for (int r = c + lane; r < m; r += 32) {
-          const T a1 = W0[r], a2 = W1[r];
-          if constexpr (sizeof(T) == 4) {
-            const float l1 = dot2_f32(e0, a1, e1, a2), l2 = dot2_f32(e1, a1, e3, a2);
-            col[r] -= l1 * w0 + l2 * w1;
-          } else {
-            const T l1 = e0 * a1 + e1 * a2, l2 = e1 * a1 + e3 * a2;
-            col[r] -= l1 * w0 + l2 * w1;
-          }
-        }
+        for (int r = c + lane; r < m; r += 32) col[r] -= l1[r] * w0 + l2[r] * w1;
       }
     }
     __syncthreads();
