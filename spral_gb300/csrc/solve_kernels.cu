@@ -185,6 +185,12 @@ template <typename T, int NR>
 constexpr size_t solve_smem_bytes() {
   return sizeof(T) * ((size_t)SB * LDB + (size_t)SB * NR + (size_t)4 * NR * 64);
 }
+// the wavefront passes' kernels: the same, then a small front's local
+// vector (kWaveSmall items: at most SB + kWaveSmallRows rows)
+template <typename T, int NR>
+constexpr size_t wave_smem_bytes() {
+  return solve_smem_bytes<T, NR>() + sizeof(T) * (size_t)(SB + kWaveSmallRows) * NR;
+}
 
 // Solve of diagonal block [j0, j0+jb) inside a block step, after the CTA
 // started staging it with prefetch_diag_block.  Every CTA of the step solves
@@ -921,6 +927,245 @@ __device__ bool fwd_block(const SolveNode<T>& sn, int code, int nrhs, double* x,
   return true;
 }
 
+// Forward small-front item (kWaveSmall: at most one pivot block and
+// kWaveSmallRows rows below it), the whole front in one CTA with its local
+// vector in shared memory (xs[row * NR + q]).  What the children do not
+// write is loaded before waiting for them: the right-hand side's entries of
+// the front's own columns, the row maps and the first two contribution
+// sources of every row (pair lists and child nodes), and the block inverse
+// rows (or the diagonal block).  After the wait one round of loads brings
+// the children's contribution rows; the pivot block and the contribution
+// row blocks then read their inputs from shared memory.  The arithmetic and
+// its order are those of fwd_gather_rows and fwd_block (code 0, then the
+// contribution row blocks), so the results are the same bits.  False if a
+// wait gave up.
+template <typename T, int NR>
+__device__ bool fwd_small(const SolveNode<T>& sn, const SolveNode<T>* sns, const int* children,
+                          const int2* pairs, double* x, int ldx, int nrhs, bool scale_sqrt,
+                          int* status, T* Lb, T* yb, T* red, T* xs, int* s_fail,
+                          const WaveLevel& wl, int it) {
+  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
+  constexpr int RP = (SB + kWaveSmallRows + kSolveThreads - 1) / kSolveThreads;
+  const int tid = threadIdx.x, r = tid % SB, cq = tid / SB;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int m = sn.m, nelim = sn.nelim;
+  T bv[16];
+  if (nelim > 0) {
+    if (sn.binv) {
+      const T* bp = sn.binv + r * SB + cq * 16;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) bv[k] = bp[k];
+    } else {
+      prefetch_diag_block(sn, 0, nelim, Lb);
+    }
+  }
+  // rows tid + j * kSolveThreads: the right-hand side part into xs, the
+  // first two contribution sources; delayed entries and further sources
+  // are looked up after the wait
+  const T* src0[RP];
+  const T* src1[RP];
+  int m0[RP], m1[RP], kn[RP], k1[RP], dl[RP];
+#pragma unroll
+  for (int j = 0; j < RP; ++j) {
+    const int i = tid + j * kSolveThreads;
+    src0[j] = src1[j] = nullptr;
+    m0[j] = m1[j] = 0;
+    kn[j] = k1[j] = 0;
+    dl[j] = -1;
+    if (i >= m) continue;
+    const int pos = (i < sn.n) ? sn.opos[i] : i;
+    int P = -1;
+    if (pos < sn.ncol) {
+#pragma unroll
+      for (int q = 0; q < NR; ++q)
+        xs[i * NR + q] = (q < nrhs) ? (T)x[(int64_t)q * ldx + sn.sptr0 + pos] : T(0);
+      P = pos;
+    } else {
+#pragma unroll
+      for (int q = 0; q < NR; ++q) xs[i * NR + q] = T(0);
+      if (pos < sn.ncol + sn.ndelay_in) dl[j] = pos - sn.ncol;
+      else P = pos - sn.ndelay_in;
+    }
+    if (P >= 0) {
+      kn[j] = sn.gp[P];
+      k1[j] = sn.gp[P + 1];
+      if (kn[j] < k1[j]) {
+        const int2 pr = pairs[kn[j]++];
+        src0[j] = sns[pr.x].xloc + sns[pr.x].n + pr.y;
+        m0[j] = sns[pr.x].m;
+      }
+      if (kn[j] < k1[j]) {
+        const int2 pr = pairs[kn[j]++];
+        src1[j] = sns[pr.x].xloc + sns[pr.x].n + pr.y;
+        m1[j] = sns[pr.x].m;
+      }
+    }
+  }
+  // the children's contribution rows (and delayed entries) are final once
+  // every item of theirs has finished
+  bool ok = true;
+  for (int ci = sn.child_beg; ci < sn.child_end && ok; ++ci) {
+    const SolveNode<T>& cn = sns[children[ci]];
+    ok = wave_wait_count(wave_finished(cn), cn.nitf, status, s_fail);
+  }
+  if (!ok) {
+    if (nelim > 0 && !sn.binv) cp_async_wait_all();
+    return false;
+  }
+  wave_stamp(wl, it, 1);
+#pragma unroll
+  for (int j = 0; j < RP; ++j) {
+    const int i = tid + j * kSolveThreads;
+    if (i >= m) continue;
+    T v[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) v[q] = xs[i * NR + q];
+    if (dl[j] >= 0) {
+      const int k = dl[j];
+      for (int ci = sn.child_beg; ci < sn.child_end; ++ci) {
+        const SolveNode<T>& cn = sns[children[ci]];
+        const int nd = cn.n - cn.nelim;
+        if (k >= cn.doff && k < cn.doff + nd) {
+          const T* src = cn.xloc + cn.nelim + (k - cn.doff);
+#pragma unroll
+          for (int q = 0; q < NR; ++q)
+            if (q < nrhs) v[q] = __ldcg(src + (int64_t)q * cn.m);
+          break;
+        }
+      }
+    }
+    if (src0[j]) {
+#pragma unroll
+      for (int q = 0; q < NR; ++q)
+        if (q < nrhs) v[q] += __ldcg(src0[j] + (int64_t)q * m0[j]);
+    }
+    if (src1[j]) {
+#pragma unroll
+      for (int q = 0; q < NR; ++q)
+        if (q < nrhs) v[q] += __ldcg(src1[j] + (int64_t)q * m1[j]);
+    }
+    for (int k = kn[j]; k < k1[j]; ++k) {
+      const int2 pr = pairs[k];
+      const SolveNode<T>& cn = sns[pr.x];
+      const T* src = cn.xloc + cn.n + pr.y;
+#pragma unroll
+      for (int q = 0; q < NR; ++q)
+        if (q < nrhs) v[q] += __ldcg(src + (int64_t)q * cn.m);
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q) xs[i * NR + q] = v[q];
+  }
+  __syncthreads();
+  if (nelim > 0) {
+    const int rows = nelim;
+    if (sn.binv) {
+      // y = L_bb^{-1} b: the products of the block inverse's row r over
+      // column quarter cq, the quarters added in order
+      for (int e = tid; e < SB * NR; e += kSolveThreads) {
+        const int row = e / NR, q = e % NR;
+        yb[row * NR + q] = (q < nrhs && row < rows) ? xs[row * NR + q] : T(0);
+      }
+      __syncthreads();
+      T acc[NR];
+#pragma unroll
+      for (int q = 0; q < NR; ++q) acc[q] = T(0);
+      if (cq * 16 < rows && (r & ~31) < rows) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k)
+#pragma unroll
+          for (int q = 0; q < NR; ++q) acc[q] += bv[k] * yb[(cq * 16 + k) * NR + q];
+      }
+#pragma unroll
+      for (int q = 0; q < NR; ++q) red[(cq * NR + q) * SB + r] = acc[q];
+      __syncthreads();
+      for (int e = tid; e < SB * NR; e += kSolveThreads) {
+        const int row = e % SB, q = e / SB;
+        if (row < rows && q < nrhs) {
+          const T y = red[q * SB + row] + red[(NR + q) * SB + row] + red[(2 * NR + q) * SB + row] +
+                      red[(3 * NR + q) * SB + row];
+          xs[row * NR + q] = y;
+          sn.xloc[(int64_t)q * m + row] = y;
+          double v = (double)y;
+          if (scale_sqrt) v *= sqrt(sn.D[2 * row]);
+          x[(int64_t)q * ldx + sn.perm[row]] = v;
+        }
+      }
+    } else {
+      T xr[R][2];
+#pragma unroll
+      for (int rr = 0; rr < R; ++rr) {
+        const int q = warp + rr * kSolveWarps;
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          const int row = lane + 32 * g;
+          xr[rr][g] = (q < nrhs && q < NR && row < rows) ? xs[row * NR + q] : T(0);
+        }
+      }
+      cp_async_wait_all();
+      __syncthreads();
+      if (warp < nrhs) solve_in_regs<T, R, true>(rows, Lb, xr);
+#pragma unroll
+      for (int rr = 0; rr < R; ++rr) {
+        const int q = warp + rr * kSolveWarps;
+#pragma unroll
+        for (int g = 0; g < 2; ++g) {
+          const int row = lane + 32 * g;
+          if (q < nrhs && q < NR && row < rows) {
+            xs[row * NR + q] = xr[rr][g];
+            sn.xloc[(int64_t)q * m + row] = xr[rr][g];
+            double v = (double)xr[rr][g];
+            if (scale_sqrt) v *= sqrt(sn.D[2 * row]);
+            x[(int64_t)q * ldx + sn.perm[row]] = v;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (tid == 0) st_release(&sn.flag[0], 1);
+  }
+  if (nelim >= m) return true;
+  // the contribution rows: x_C -= L21 y, 64-row blocks (thread (r, cq): row
+  // r, columns [16 cq, 16 cq + 16) of the pivot block), y staged once
+  const int jb = nelim;
+  for (int e = tid; e < SB * NR; e += kSolveThreads) {
+    const int c = e % SB, q = e / SB;
+    yb[c * NR + q] = (c < jb && q < nrhs) ? xs[c * NR + q] : T(0);
+  }
+  __syncthreads();
+  for (int r0 = nelim; r0 < m; r0 += SB) {
+    const int rows = min(SB, m - r0);
+    T lv[16];
+    {
+      const T* Lp = sn.L + (int64_t)(cq * 16) * sn.ld + r0 + r;
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+        lv[k] = (r < rows && cq * 16 + k < jb) ? Lp[(int64_t)k * sn.ld] : T(0);
+    }
+    T acc[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
+    if (cq * 16 < jb && (r & ~31) < rows) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+#pragma unroll
+        for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(cq * 16 + k) * NR + q];
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q) red[(cq * NR + q) * SB + r] = acc[q];
+    __syncthreads();
+    for (int e = tid; e < SB * NR; e += kSolveThreads) {
+      const int row = e % SB, q = e / SB;
+      if (row < rows && q < nrhs)
+        sn.xloc[(int64_t)q * m + r0 + row] =
+            xs[(r0 + row) * NR + q] - (red[q * SB + row] + red[(NR + q) * SB + row] +
+                                       red[(2 * NR + q) * SB + row] +
+                                       red[(3 * NR + q) * SB + row]);
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
 // Forward pass over the whole tree (item list and waits: see WaveLevel).
 template <typename T, int NR, int CPS>
 __global__ void __launch_bounds__(kSolveThreads, CPS)
@@ -930,6 +1175,7 @@ __global__ void __launch_bounds__(kSolveThreads, CPS)
   T* Lb = reinterpret_cast<T*>(solve_smem);
   T* yb = Lb + SB * LDB;
   T* red = yb + SB * NR;
+  T* xs = red + 4 * NR * 64;  // a small front's local vector
   __shared__ int s_item, s_fail;
   for (;;) {
     const int it = wave_next(wl, &s_item);
@@ -939,7 +1185,11 @@ __global__ void __launch_bounds__(kSolveThreads, CPS)
     const SolveNode<T>& sn = sns[w.x];
     const int code = w.y;
     bool ok = true;
-    if (code >= kWaveGather) {
+    if (code == kWaveSmall) {
+      ok = fwd_small<T, NR>(sn, sns, children, pairs, x, ldx, nrhs, scale_sqrt, status, Lb, yb,
+                            red, xs, &s_fail, wl, it);
+      if (ok) wave_signal(wave_finished(sn), nullptr);
+    } else if (code >= kWaveGather) {
       // the children's contribution rows (and delayed entries) are final
       // once every item of theirs has finished
       for (int ci = sn.child_beg; ci < sn.child_end && ok; ++ci) {
@@ -948,17 +1198,7 @@ __global__ void __launch_bounds__(kSolveThreads, CPS)
       }
       if (!ok) continue;
       wave_stamp(wl, it, 1);
-      if (code == kWaveSmall) {
-        fwd_gather_rows<T, NR>(sn, sns, children, pairs, x, ldx, nrhs, 0, sn.m);
-        __syncthreads();
-        if (sn.nelim > 0)
-          ok = fwd_block<T, NR>(sn, 0, nrhs, x, ldx, scale_sqrt, status, Lb, yb, red, &s_fail, wl,
-                               it);
-        for (int k = 0; ok && sn.nelim + k * SB < sn.m; ++k)
-          ok = fwd_block<T, NR>(sn, kWaveContrib + k, nrhs, x, ldx, scale_sqrt, status, Lb, yb,
-                                red, &s_fail, wl, it);
-        if (ok) wave_signal(wave_finished(sn), nullptr);
-      } else {
+      {
         const int g0 = (code - kWaveGather) * kWaveGatherRows;
         fwd_gather_rows<T, NR>(sn, sns, children, pairs, x, ldx, nrhs, g0,
                         min(sn.m, g0 + kWaveGatherRows));
@@ -1211,6 +1451,217 @@ __device__ bool bwd_block(const SolveNode<T>& sn, int b, int nrhs, double* x, in
   return true;
 }
 
+// Backward small-front item, the whole front in one CTA with its local
+// vector in shared memory (xs[row * NR + q]): the pivot rows' entries of x
+// (this front's own, written by no other item of the pass) with their D^{-1}
+// applied, and the block inverse (or the diagonal block), are loaded before
+// waiting for the parent; after it one round of loads brings the rows below
+// the pivots, solved at the ancestors.  Then x_b -= L21^T x_C over the
+// contribution rows and the unit triangle, with the arithmetic and order of
+// bwd_gather_rows and bwd_block (code 0, no partial items), so the results
+// are the same bits.  False if a wait gave up.
+template <typename T, int NR>
+__device__ bool bwd_small(const SolveNode<T>& sn, const SolveNode<T>* sns, int nrhs, double* x,
+                          int ldx, int diag_mode, int* status, T* Lb, T* yb, T* red, T* xs,
+                          int* s_fail, const WaveLevel& wl, int it) {
+  constexpr int R = (NR + kSolveWarps - 1) / kSolveWarps;
+  constexpr int RP = (SB + kWaveSmallRows + kSolveThreads - 1) / kSolveThreads;
+  const int tid = threadIdx.x, c = tid % SB, rq = tid / SB;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int m = sn.m, nelim = sn.nelim, jb = min(SB, nelim);
+  T bv[16];
+  if (nelim > 0) {
+    if (sn.binv) {
+      const T* bp = sn.binv + (rq * 16) * SB + c;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) bv[k] = bp[k * SB];
+    } else {
+      prefetch_diag_block(sn, 0, jb, Lb);
+    }
+  }
+  int later[RP];  // x position of a row below the pivots, read after the wait
+#pragma unroll
+  for (int j = 0; j < RP; ++j) {
+    const int i = tid + j * kSolveThreads;
+    later[j] = -1;
+    if (i >= m) continue;
+    const int src = (i < sn.n) ? sn.perm[i] : sn.rows[sn.ncol + i - sn.n];
+    if (i >= nelim) {
+      later[j] = src;
+      continue;
+    }
+    int src2 = -1;
+    double ca = 1.0, cb = 0.0;
+    if (diag_mode == 2) {
+      ca = sqrt(sn.D[2 * i]);
+    } else if (diag_mode == 1) {
+      const double di = sn.D[2 * i];
+      if (isinf(di)) {
+        src2 = sn.perm[i - 1];
+        ca = sn.D[2 * i + 1];
+        cb = sn.D[2 * (i - 1) + 1];
+      } else if (i + 1 < nelim && isinf(sn.D[2 * i + 2])) {
+        src2 = sn.perm[i + 1];
+        ca = di;
+        cb = sn.D[2 * i + 1];
+      } else {
+        ca = di;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      T t = T(0);
+      if (q < nrhs) {
+        const double v = __ldcg(&x[(int64_t)q * ldx + src]);
+        const double w = src2 >= 0 ? __ldcg(&x[(int64_t)q * ldx + src2]) : 0.0;
+        double rv;
+        if (src2 < 0) rv = (diag_mode == 0) ? v : ca * v;
+        else if (isinf(sn.D[2 * i])) rv = cb * w + ca * v;
+        else rv = ca * v + cb * w;
+        t = (T)rv;
+        sn.xloc[(int64_t)q * m + i] = t;
+      }
+      xs[i * NR + q] = t;
+    }
+  }
+  // the rows below the pivots are solved at the ancestors, which are final
+  // once the parent has finished (it waited for its own parent)
+  bool ok = true;
+  if (sn.parent >= 0) {
+    const SolveNode<T>& pn = sns[sn.parent];
+    ok = wave_wait_count(wave_finished(pn), pn.nitb, status, s_fail);
+  }
+  if (!ok) {
+    if (nelim > 0 && !sn.binv) cp_async_wait_all();
+    return false;
+  }
+  wave_stamp(wl, it, 1);
+#pragma unroll
+  for (int j = 0; j < RP; ++j) {
+    const int i = tid + j * kSolveThreads;
+    if (later[j] < 0) continue;
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      T t = T(0);
+      if (q < nrhs) {
+        t = (T)__ldcg(&x[(int64_t)q * ldx + later[j]]);
+        sn.xloc[(int64_t)q * m + i] = t;
+      }
+      xs[i * NR + q] = t;
+    }
+  }
+  __syncthreads();
+  if (nelim == 0) return true;
+  T own[R][2];
+#pragma unroll
+  for (int rr = 0; rr < R; ++rr) {
+    const int q = warp + rr * kSolveWarps;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {
+      const int col = lane + 32 * g;
+      own[rr][g] = (q < nrhs && q < NR && col < jb) ? xs[col * NR + q] : T(0);
+    }
+  }
+  T acc[NR];
+#pragma unroll
+  for (int q = 0; q < NR; ++q) acc[q] = T(0);
+  for (int R0 = nelim; R0 < m; R0 += SB) {
+    const int nr = min(SB, m - R0);
+    T lv[16];
+    {
+      const T* Lp = sn.L + (int64_t)c * sn.ld + R0 + rq * 16;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) lv[k] = (c < jb && rq * 16 + k < nr) ? Lp[k] : T(0);
+    }
+    for (int e = tid; e < SB * NR; e += kSolveThreads) {
+      const int rr = e % SB, q = e / SB;
+      yb[rr * NR + q] = (rr < nr && q < nrhs) ? xs[(R0 + rr) * NR + q] : T(0);
+    }
+    __syncthreads();
+    if ((c & ~31) < jb && rq * 16 < nr) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+#pragma unroll
+        for (int q = 0; q < NR; ++q) acc[q] += lv[k] * yb[(rq * 16 + k) * NR + q];
+    }
+    __syncthreads();
+  }
+  wave_stamp(wl, it, 1);
+#pragma unroll
+  for (int q = 0; q < NR; ++q) red[(rq * NR + q) * SB + c] = acc[q];
+  __syncthreads();
+  if (sn.binv) {
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+      const int q = warp + rr * kSolveWarps;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int col = lane + 32 * g;
+        if (q < NR)
+          yb[col * NR + q] = (q < nrhs && col < jb)
+                                 ? own[rr][g] - (red[q * SB + col] + red[(NR + q) * SB + col] +
+                                                 red[(2 * NR + q) * SB + col] +
+                                                 red[(3 * NR + q) * SB + col])
+                                 : T(0);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
+    if ((c & ~31) < jb && rq * 16 < jb) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k)
+#pragma unroll
+        for (int q = 0; q < NR; ++q) acc[q] += bv[k] * yb[(rq * 16 + k) * NR + q];
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q) red[(rq * NR + q) * SB + c] = acc[q];
+    __syncthreads();
+    for (int e = tid; e < SB * NR; e += kSolveThreads) {
+      const int col = e % SB, q = e / SB;
+      if (col < jb && q < nrhs) {
+        const T y = red[q * SB + col] + red[(NR + q) * SB + col] + red[(2 * NR + q) * SB + col] +
+                    red[(3 * NR + q) * SB + col];
+        sn.xloc[(int64_t)q * m + col] = y;
+        x[(int64_t)q * ldx + sn.perm[col]] = (double)y;
+      }
+    }
+  } else {
+    T xr[R][2];
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+      const int q = warp + rr * kSolveWarps;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int col = lane + 32 * g;
+        T v = T(0);
+        if (q < nrhs && q < NR && col < jb)
+          v = own[rr][g] - (red[q * SB + col] + red[(NR + q) * SB + col] +
+                            red[(2 * NR + q) * SB + col] + red[(3 * NR + q) * SB + col]);
+        xr[rr][g] = v;
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (warp < nrhs) solve_in_regs<T, R, false>(jb, Lb, xr);
+#pragma unroll
+    for (int rr = 0; rr < R; ++rr) {
+      const int q = warp + rr * kSolveWarps;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {
+        const int col = lane + 32 * g;
+        if (q < nrhs && q < NR && col < jb) {
+          sn.xloc[(int64_t)q * m + col] = xr[rr][g];
+          x[(int64_t)q * ldx + sn.perm[col]] = (double)xr[rr][g];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0) st_release(&sn.flag[0], 1);
+  return true;
+}
+
 // Backward pass over the whole tree (item list and waits: see WaveLevel).
 template <typename T, int NR, int CPS>
 __global__ void __launch_bounds__(kSolveThreads, CPS)
@@ -1220,6 +1671,7 @@ __global__ void __launch_bounds__(kSolveThreads, CPS)
   T* Lb = reinterpret_cast<T*>(solve_smem);
   T* yb = Lb + SB * LDB;
   T* red = yb + SB * NR;
+  T* xs = red + 4 * NR * 64;  // a small front's local vector
   __shared__ int s_item, s_fail;
   for (;;) {
     const int it = wave_next(wl, &s_item);
@@ -1229,7 +1681,11 @@ __global__ void __launch_bounds__(kSolveThreads, CPS)
     const SolveNode<T>& sn = sns[w.x];
     const int code = w.y;
     bool ok = true;
-    if (code >= kWaveL21) {
+    if (code == kWaveSmall) {
+      ok = bwd_small<T, NR>(sn, sns, nrhs, x, ldx, diag_mode, status, Lb, yb, red, xs, &s_fail,
+                            wl, it);
+      if (ok) wave_signal(wave_finished(sn), nullptr);
+    } else if (code >= kWaveL21) {
       ok = wave_wait_count(wave_gathered(sn), sn.ngat, status, &s_fail);
       if (ok) wave_stamp(wl, it, 1);
       const int t = code - kWaveL21;
@@ -1244,17 +1700,9 @@ __global__ void __launch_bounds__(kSolveThreads, CPS)
       }
       if (!ok) continue;
       wave_stamp(wl, it, 1);
-      const int g0 = code == kWaveSmall ? 0 : (code - kWaveGather) * kWaveGatherRows;
-      const int g1 = code == kWaveSmall ? sn.m : min(sn.m, g0 + kWaveGatherRows);
-      bwd_gather_rows<T, NR>(sn, x, ldx, nrhs, diag_mode, g0, g1);
-      if (code == kWaveSmall) {
-        __syncthreads();
-        if (sn.nelim > 0)
-          ok = bwd_block<T, NR>(sn, 0, nrhs, x, ldx, status, Lb, yb, red, &s_fail, wl, it);
-        if (ok) wave_signal(wave_finished(sn), nullptr);
-      } else {
-        wave_signal(wave_gathered(sn), wave_finished(sn));
-      }
+      const int g0 = (code - kWaveGather) * kWaveGatherRows;
+      bwd_gather_rows<T, NR>(sn, x, ldx, nrhs, diag_mode, g0, min(sn.m, g0 + kWaveGatherRows));
+      wave_signal(wave_gathered(sn), wave_finished(sn));
     } else {
       ok = wave_wait_count(wave_gathered(sn), sn.ngat, status, &s_fail);
       if (ok) ok = bwd_block<T, NR>(sn, code, nrhs, x, ldx, status, Lb, yb, red, &s_fail, wl, it);
@@ -1460,10 +1908,10 @@ void launch_fwd_tree(const SolveNode<T>* sn, const int* children, const int2* pa
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
     if (wl.ctas_per_sm >= 3)
-      k_fwd_tree<T, NR, 3><<<wave_grid(wl.nitems, 3), kSolveThreads, solve_smem_bytes<T, NR>(),
+      k_fwd_tree<T, NR, 3><<<wave_grid(wl.nitems, 3), kSolveThreads, wave_smem_bytes<T, NR>(),
                              s>>>(sn, children, pairs, wl, nrhs, x, ldx, scale_sqrt, status);
     else
-      k_fwd_tree<T, NR, 2><<<wave_grid(wl.nitems, 2), kSolveThreads, solve_smem_bytes<T, NR>(),
+      k_fwd_tree<T, NR, 2><<<wave_grid(wl.nitems, 2), kSolveThreads, wave_smem_bytes<T, NR>(),
                              s>>>(sn, children, pairs, wl, nrhs, x, ldx, scale_sqrt, status);
   });
   note_launches(1);
@@ -1476,10 +1924,10 @@ void launch_bwd_tree(const SolveNode<T>* sn, const WaveLevel& wl, double* x, int
   with_nr(nrhs, [&](auto nrc) {
     constexpr int NR = decltype(nrc)::value;
     if (wl.ctas_per_sm >= 3)
-      k_bwd_tree<T, NR, 3><<<wave_grid(wl.nitems, 3), kSolveThreads, solve_smem_bytes<T, NR>(),
+      k_bwd_tree<T, NR, 3><<<wave_grid(wl.nitems, 3), kSolveThreads, wave_smem_bytes<T, NR>(),
                              s>>>(sn, wl, nrhs, x, ldx, diag_mode, status);
     else
-      k_bwd_tree<T, NR, 2><<<wave_grid(wl.nitems, 2), kSolveThreads, solve_smem_bytes<T, NR>(),
+      k_bwd_tree<T, NR, 2><<<wave_grid(wl.nitems, 2), kSolveThreads, wave_smem_bytes<T, NR>(),
                              s>>>(sn, wl, nrhs, x, ldx, diag_mode, status);
   });
   note_launches(1);
@@ -1503,10 +1951,10 @@ void solve_init() {
         set(k_bwd_step<T, NR, kStepFused>, solve_smem_bytes<T, NR>());
         set(k_bwd_step<T, NR, kStepSolve>, solve_smem_bytes<T, NR>());
         set(k_bwd_step<T, NR, kStepUpdate>, solve_smem_bytes<T, NR>());
-        set(k_fwd_tree<T, NR, 2>, solve_smem_bytes<T, NR>());
-        set(k_bwd_tree<T, NR, 2>, solve_smem_bytes<T, NR>());
-        set(k_fwd_tree<T, NR, 3>, solve_smem_bytes<T, NR>());
-        set(k_bwd_tree<T, NR, 3>, solve_smem_bytes<T, NR>());
+        set(k_fwd_tree<T, NR, 2>, wave_smem_bytes<T, NR>());
+        set(k_bwd_tree<T, NR, 2>, wave_smem_bytes<T, NR>());
+        set(k_fwd_tree<T, NR, 3>, wave_smem_bytes<T, NR>());
+        set(k_bwd_tree<T, NR, 3>, wave_smem_bytes<T, NR>());
       });
     }
   });
