@@ -212,10 +212,12 @@ __global__ void k_bwd_finish(const double* work, int nrhs, int ngroups, double* 
   }
 }
 
-__global__ void k_axpy(int64_t total, int n, int ld, double* x, const double* d) {
+__global__ void k_axpy(int64_t total, int n, int ld, double* x, const double* d,
+                       const int* row_group, const unsigned char* active) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     int64_t q = e / n, i = e % n;
+    if (active && !active[row_group[i]]) continue;
     x[q * ld + i] += d[q * ld + i];
   }
 }
@@ -252,10 +254,13 @@ void launch_resid_bwd_err(const int64_t* aptr, const int* acol, const int64_t* a
   { k_bwd_finish<<<1, 256, 0, s>>>(acc, nrhs, ng, work); note_launches(1); }
 }
 
-void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s) {
+// x += d; with a mask (active != nullptr) only on the rows whose group is
+// active (the others' d was not solved for)
+void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s,
+                 const int* row_group, const unsigned char* active) {
   int64_t total = (int64_t)n * nrhs;
   int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 4096));
-  { k_axpy<<<blocks, 256, 0, s>>>(total, n, ld, x, d); note_launches(1); }
+  { k_axpy<<<blocks, 256, 0, s>>>(total, n, ld, x, d, row_group, active); note_launches(1); }
 }
 
 }  // namespace ssids300

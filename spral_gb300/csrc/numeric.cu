@@ -359,6 +359,7 @@ struct Symbolic {
   // optional row groups of the refinement's backward error (pivot order)
   int ngroups = 0;
   int* d_row_group = nullptr;
+  int* d_front_group = nullptr;  // the group of each front (its first column's)
   std::vector<int64_t> gp_off;
   // FP64 matrix in pivot order (full CSR, both triangles) for refinement
   int64_t* d_aptr = nullptr;
@@ -369,7 +370,8 @@ struct Symbolic {
   ~Symbolic() {
     cudaFree(d_nptr); cudaFree(d_nlist); cudaFree(d_sptr); cudaFree(d_rlist); cudaFree(d_rptr);
     cudaFree(d_rdir); cudaFree(d_rdir_ptr); cudaFree(d_fronts); cudaFree(d_cols); cudaFree(d_tpp);
-    cudaFree(d_pairs); cudaFree(d_gp); cudaFree(d_row_group); cudaFree(d_aptr); cudaFree(d_acol); cudaFree(d_asrc);
+    cudaFree(d_pairs); cudaFree(d_gp); cudaFree(d_row_group); cudaFree(d_front_group);
+    cudaFree(d_aptr); cudaFree(d_acol); cudaFree(d_asrc);
   }
 };
 
@@ -681,7 +683,8 @@ void launch_resid_bwd_err(const int64_t* aptr, const int* acol, const int64_t* a
                           const double* aval, int n, const double* x, const double* b, double* r,
                           int nrhs, int ld, double* work, const int* row_group, int ngroups,
                           cudaStream_t s);
-void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s);
+void launch_axpy(int n, int nrhs, int ld, double* x, const double* d, cudaStream_t s,
+                 const int* row_group = nullptr, const unsigned char* active = nullptr);
 
 // ---------------------------------------------------------------------------
 // Autotuner, run once per device (or read from the tune cache named by
@@ -904,6 +907,9 @@ struct Numeric : NumericBase {
   bool use_wave = true;
   DevBuf<int2> wave_items;
   DevBuf<int> wave_flags, wave_ints;
+  // per row group, whether the refinement still solves for it (all ones
+  // outside the refinement of a forest of row groups)
+  DevBuf<unsigned char> group_active;
   DevBuf<T> wave_l21p;  // backward L21^T partial sums of the wavefront pass
   // inverses of the pivot blocks' unit lower diagonal blocks (FP32 factors'
   // wavefront passes; SPRAL_GB300_SOLVE_BINV=0 keeps the substitution),
@@ -929,6 +935,8 @@ struct Numeric : NumericBase {
     // many small-front items: more CTAs in flight; otherwise the widest
     // fronts' chains set the time and keep their registers
     w.ctas_per_sm = 2 * wave_nsmall > wave_nfwd ? 3 : 2;
+    w.front_group = S->d_front_group;
+    w.active = S->d_front_group ? group_active.p : nullptr;
     if (!wave_trace.empty()) {
       wave_trace_buf.ensure(4 * (size_t)(wave_nfwd + wave_nbwd) + 4);
       w.trace = wave_trace_buf.p + (fwd ? 0 : 4 * (size_t)wave_nfwd);
@@ -1957,6 +1965,10 @@ struct Numeric : NumericBase {
     if (!ch.empty())
       CK(cudaMemcpyAsync(d_children, ch.data(), ch.size() * sizeof(int), cudaMemcpyHostToDevice,
                          stream));
+    if (S->d_front_group) {
+      group_active.ensure((size_t)S->ngroups);
+      CK(cudaMemsetAsync(group_active.p, 1, (size_t)S->ngroups, stream));
+    }
     CK(cudaStreamSynchronize(stream));
     // signature of everything a captured solve sequence depends on
     uint64_t h = 1469598103934665603ull;
@@ -1968,6 +1980,7 @@ struct Numeric : NumericBase {
     mix((uint64_t)(uintptr_t)wave_ints.p); mix((uint64_t)(uintptr_t)wave_l21p.p);
     mix((uint64_t)(uintptr_t)wave_binv.p); mix((uint64_t)binv);
     mix((uint64_t)wave_nfwd); mix((uint64_t)wave_nbwd);
+    mix((uint64_t)(uintptr_t)S->d_front_group); mix((uint64_t)(uintptr_t)group_active.p);
     if (h != solve_sig) drop_graphs();
     solve_sig = h;
     solve_ready = true;
@@ -2208,14 +2221,28 @@ struct Numeric : NumericBase {
       // fallback): stalled only once no group above the target halved its
       // own error, so the other groups finish their refinement.
       bool stalled = it > 0 && !(worst < 0.5 * last_bwd_err);
-      if (S->d_row_group && S->gopts.no_fp64_fallback && worst > S->gopts.refine_tol) {
+      bool masked = false;
+      // row groups judged one by one: FP32 factors whose caller handles
+      // the misses (no FP64 fallback here), and FP64 factors
+      const bool by_group = S->gopts.no_fp64_fallback || std::is_same<T, double>::value;
+      if (S->d_row_group && by_group && worst > S->gopts.refine_tol) {
         last_refine_q = q;
         std::vector<double> ge(S->ngroups);
         group_bwd_errors(ge.data(), S->ngroups);
-        if (it > 0 && group_prev.size() == ge.size()) {
+        if (S->gopts.no_fp64_fallback && it > 0 && group_prev.size() == ge.size()) {
           stalled = true;
           for (size_t g = 0; g < ge.size() && stalled; ++g)
             if (ge[g] > S->gopts.refine_tol && ge[g] < 0.5 * group_prev[g]) stalled = false;
+        }
+        // the next step solves only for the groups above the target: the
+        // wavefront passes skip the others' trees and the update leaves
+        // their rows as they are (their errors stay those just measured)
+        if (use_wave && S->d_front_group && group_active.p) {
+          active_h.resize(ge.size());
+          for (size_t g = 0; g < ge.size(); ++g) active_h[g] = ge[g] > S->gopts.refine_tol;
+          CK(cudaMemcpyAsync(group_active.p, active_h.data(), active_h.size(),
+                             cudaMemcpyHostToDevice, s));
+          masked = true;
         }
         group_prev.swap(ge);
       }
@@ -2223,11 +2250,16 @@ struct Numeric : NumericBase {
       if (!(worst > S->gopts.refine_tol) || it >= maxit || stalled) break;
       solve_dev(0, q, rbuf.p, ld, nullptr);
       pmark(tm(), kPhAxpy, s);
-      launch_axpy(n, q, ld, x, rbuf.p, s);
+      launch_axpy(n, q, ld, x, rbuf.p, s, masked ? S->d_row_group : nullptr,
+                  masked ? group_active.p : nullptr);
       pmark(tm(), kPhHost, s);
     }
+    // later solves are for every group
+    if (S->d_front_group && group_active.p)
+      CK(cudaMemsetAsync(group_active.p, 1, (size_t)S->ngroups, s));
     return it;
   }
+  std::vector<unsigned char> active_h;  // host copy of the refinement's group mask
 
   cudaStream_t get_stream() const override { return stream; }
 
@@ -2808,18 +2840,38 @@ int spral_ssids_gpu_set_row_groups(void* symbolic, int ngroups, const int* row_g
     CK(cudaSetDevice(S->device));
     if (ngroups <= 0 || !row_group) {
       cudaFree(S->d_row_group);
+      cudaFree(S->d_front_group);
       S->d_row_group = nullptr;
+      S->d_front_group = nullptr;
       S->ngroups = 0;
       return 0;
     }
     for (int i = 0; i < S->n; ++i)
       if (row_group[i] < 0 || row_group[i] >= ngroups) return -2;
+    // a front's group: its columns' when they and its parent's share one
+    // (the groups are the trees of a forest, e.g. the matrices of a batch);
+    // otherwise no front groups, and the refinement never skips a group
+    std::vector<int> fg(std::max(S->nnodes, 1), 0);
+    bool trees = true;
+    for (int i = 0; i < S->nnodes && trees; ++i) {
+      const int g = S->sptr[i] < S->n ? row_group[S->sptr[i]] : 0;
+      for (int c = S->sptr[i]; c < S->sptr[i + 1] && trees; ++c) trees = row_group[c] == g;
+      const int p = S->parent[i];
+      if (trees && p >= 0 && S->sptr[p] < S->n) trees = row_group[S->sptr[p]] == g;
+      fg[S->front_of[i]] = g;
+    }
     int* d = nullptr;
+    int* dfg = nullptr;
     CK(cudaMalloc(&d, std::max(S->n, 1) * sizeof(int)));
-    const cudaError_t e = cudaMemcpy(d, row_group, S->n * sizeof(int), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) { cudaFree(d); CK(e); }
+    cudaError_t e = trees ? cudaMalloc(&dfg, fg.size() * sizeof(int)) : cudaSuccess;
+    if (e == cudaSuccess) e = cudaMemcpy(d, row_group, S->n * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && dfg)
+      e = cudaMemcpy(dfg, fg.data(), fg.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { cudaFree(d); cudaFree(dfg); CK(e); }
     cudaFree(S->d_row_group);
+    cudaFree(S->d_front_group);
     S->d_row_group = d;
+    S->d_front_group = dfg;
     S->ngroups = ngroups;
     return 0;
   } catch (CudaFail const& e) {

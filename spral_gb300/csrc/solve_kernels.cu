@@ -1182,6 +1182,13 @@ __global__ void __launch_bounds__(kSolveThreads, CPS)
     if (it >= wl.nitems) break;
     wave_stamp(wl, it, 0);
     const int2 w = wl.items[it];
+    if (wl.active && !wl.active[wl.front_group[w.x]]) {
+      // a row group the refinement no longer solves for: a whole tree that
+      // no other item waits for
+      wave_stamp(wl, it, 1);
+      wave_stamp(wl, it, 2);
+      continue;
+    }
     const SolveNode<T>& sn = sns[w.x];
     const int code = w.y;
     bool ok = true;
@@ -1678,6 +1685,13 @@ __global__ void __launch_bounds__(kSolveThreads, CPS)
     if (it >= wl.nitems) break;
     wave_stamp(wl, it, 0);
     const int2 w = wl.items[it];
+    if (wl.active && !wl.active[wl.front_group[w.x]]) {
+      // a row group the refinement no longer solves for: a whole tree that
+      // no other item waits for
+      wave_stamp(wl, it, 1);
+      wave_stamp(wl, it, 2);
+      continue;
+    }
     const SolveNode<T>& sn = sns[w.x];
     const int code = w.y;
     bool ok = true;

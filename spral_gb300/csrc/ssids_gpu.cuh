@@ -333,6 +333,12 @@ struct WaveLevel {
   // took it, when its last wait was over, when it finished, and the SM
   unsigned long long* trace;
   int ctas_per_sm;  // persistent CTAs per SM: 3 when small fronts dominate, else 2
+  // optional mask (nullptr: every front): the items of front f run only when
+  // active[front_group[f]] != 0; a group is one matrix of a batch stacked as
+  // a forest, so the skipped fronts are whole trees that no other item waits
+  // for
+  const int* front_group;
+  const unsigned char* active;
 };
 
 constexpr int kSolveBlk = 64;   // diagonal block of the blocked triangular solves
