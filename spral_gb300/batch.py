@@ -142,7 +142,8 @@ class BatchFkeep:
 
     def _fp64_sub(self, failed):
         """The FP64 sub-batch of the matrices `failed`, factored with their
-        current values, and the map from its pivot positions to the batch's."""
+        current values, and the map from its pivot positions to the batch's:
+        [BatchAkeep, BatchFkeep, index map, (its device copy, once used)]."""
         key = tuple(int(i) for i in failed)
         ent = self._subs.get(key)
         if ent is None:
@@ -200,7 +201,7 @@ class BatchFkeep:
         X = self.fk.solve_refined(B)
         self.failed = self._failed_after_refinement()
         if self.failed.size:
-            sub_ak, sub, _ = self._fp64_sub(self.failed)
+            sub_ak, sub = self._fp64_sub(self.failed)[:2]
             xs = sub.solve_refined([B[self.bak.var_off[i]:self.bak.var_off[i + 1]]
                                     for i in self.failed])
             for j, i in enumerate(self.failed):
@@ -221,8 +222,12 @@ class BatchFkeep:
                                             ctypes.byref(it), ctypes.byref(bw))
         self.failed = self._failed_after_refinement()
         if self.failed.size:
-            sub_ak, sub, idx = self._fp64_sub(self.failed)
-            ix = torch.as_tensor(idx, device=x_dev.device)
+            ent = self._fp64_sub(self.failed)
+            sub_ak, sub, idx = ent[:3]
+            # the index map on the device, kept with the sub-batch
+            if len(ent) < 4 or ent[3].device != x_dev.device:
+                ent[3:] = [torch.as_tensor(idx, device=x_dev.device)]
+            ix = ent[3]
             bm, xm = b_dev.view(nrhs, n), x_dev.view(nrhs, n)
             bs = bm[:, ix].contiguous()
             xs = torch.empty_like(bs)
