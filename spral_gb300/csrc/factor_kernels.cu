@@ -2153,6 +2153,22 @@ __global__ void __launch_bounds__(kTppThreads) k_tpp_level(FrontDesc<T>* fds, Fr
 // Grid: (row blocks of 128, column chunks of kLdCols, fronts).  Each thread
 // issues the loads of all of its chunk's columns before the first store, so
 // one memory round trip covers kLdCols columns.
+// alpha lv + beta lp for FP32 factors in FP32 instructions, alpha and beta
+// given as float pairs (hi + lo): the two hi products with their exact
+// errors (FMA), their sum with its exact error (two-sum), then the error
+// and lo terms added once, so the result is within an ulp of the FP64
+// expression rounded to FP32, a 2x2 column's cancelling products included
+__device__ __forceinline__ float ld_entry_f32(float ahi, float alo, float bhi, float blo,
+                                              float lv, float lp) {
+  const float p1 = __fmul_rn(ahi, lv), e1 = __fmaf_rn(ahi, lv, -p1);
+  const float p2 = __fmul_rn(bhi, lp), e2 = __fmaf_rn(bhi, lp, -p2);
+  const float sm = __fadd_rn(p1, p2);
+  const float bb = __fsub_rn(sm, p1);
+  const float es = __fadd_rn(__fsub_rn(p1, __fsub_rn(sm, bb)), __fsub_rn(p2, bb));
+  const float corr = __fmaf_rn(alo, lv, __fmaf_rn(blo, lp, __fadd_rn(__fadd_rn(e1, e2), es)));
+  return __fadd_rn(sm, corr);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) k_calc_ld(FrontDesc<T>* fds, const FrontState* sts,
                                                  const int* fronts) {
@@ -2181,19 +2197,36 @@ __global__ void __launch_bounds__(128) k_calc_ld(FrontDesc<T>* fds, const FrontS
       partner[threadIdx.x] = c;
     }
   }
+  // FP32 factors: alpha and beta as pairs of floats, hi + lo, formed once
+  // per column, so the entries need no FP64 instruction
+  __shared__ float ahi[kLdCols], alo[kLdCols], bhi[kLdCols], blo[kLdCols];
+  if (sizeof(T) == 4 && (int)threadIdx.x < nc) {
+    const int k = threadIdx.x;
+    ahi[k] = (float)alpha[k];
+    alo[k] = (float)(alpha[k] - (double)ahi[k]);
+    bhi[k] = (float)beta[k];
+    blo[k] = (float)(beta[k] - (double)bhi[k]);
+  }
   __syncthreads();
   for (int rr = blockIdx.x * blockDim.x + threadIdx.x; rr < cm; rr += gridDim.x * blockDim.x) {
     const T* Lr = fd.L + fd.n + rr;
     T lv[kLdCols], lp[kLdCols];
 #pragma unroll
     for (int k = 0; k < kLdCols; ++k) {
+      bool two;
+      if constexpr (sizeof(T) == 4) two = bhi[k] != 0.f || blo[k] != 0.f;
+      else two = beta[k] != 0.0;
       lv[k] = (k < nc) ? Lr[(int64_t)(c0 + k) * fd.ld] : T(0);
-      lp[k] = (k < nc && beta[k] != 0.0) ? Lr[(int64_t)partner[k] * fd.ld] : T(0);
+      lp[k] = (k < nc && two) ? Lr[(int64_t)partner[k] * fd.ld] : T(0);
     }
 #pragma unroll
-    for (int k = 0; k < kLdCols; ++k)
-      if (k < nc)
+    for (int k = 0; k < kLdCols; ++k) {
+      if (k >= nc) continue;
+      if constexpr (sizeof(T) == 4)
+        fd.LD[(int64_t)(c0 + k) * cm + rr] = ld_entry_f32(ahi[k], alo[k], bhi[k], blo[k], lv[k], lp[k]);
+      else
         fd.LD[(int64_t)(c0 + k) * cm + rr] = (T)(alpha[k] * (double)lv[k] + beta[k] * (double)lp[k]);
+    }
   }
 }
 
