@@ -205,7 +205,11 @@ int spral_ssids_gpu_fp64_fallbacks(const void* numeric, struct spral_ssids_threa
  * batch of independent matrices stacked into one subtree.  The scaled
  * backward error that stops the refinement is then the largest over the
  * groups, each with its own norms (||A_g||, ||x_g||, ||b_g||), so every
- * group meets the target.  ngroups <= 0 or row_group == NULL removes the
+ * group meets the target.  When the groups are whole trees of the assembly
+ * forest (every front's columns and its parent's in one group, as for
+ * stacked independent matrices), each refinement step of an FP64 handle,
+ * or of an FP32 handle with no_fp64_fallback, solves only for the groups
+ * still above the target.  ngroups <= 0 or row_group == NULL removes the
  * groups.  Returns 0, -1 (NULL handle), -2 (a group out of range) or -51. */
 int spral_ssids_gpu_set_row_groups(void* symbolic, int ngroups, const int* row_group);
 
